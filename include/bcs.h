@@ -1,0 +1,265 @@
+/*
+ * bcs.h — C ABI of the GB300-native blood-cell physics step.
+ *
+ * This is the drop-in boundary for the per-frame physics of
+ * GPU-Blood-Cell-Simulation/Simulation-Server.  The reference has no runtime
+ * API: its scene is compile-time (the headers of src/config folded by
+ * the headers of src/meta_factory) and its step is a sequence of member calls in
+ * src/main.cu.  Each entry point below states which reference construct it
+ * replaces (paths are relative to the reference project root).
+ *
+ * Conventions
+ *  - Every call returns bcs_status; nothing exits the process or prints.
+ *  - The library owns its device buffers.  A handle is used by one host
+ *    thread at a time; different handles are independent.
+ *  - All device work is enqueued on the handle's stream.  Getters that write
+ *    host memory synchronise that stream.
+ *  - Vectors cross the boundary as three SoA float arrays, the layout of the
+ *    reference's cudaVec3 (src/utilities/cuda_vec3.cuh:11-72).
+ *  - Plain pointers and sizes only; no C++ or framework types.
+ */
+#ifndef BCS_H
+#define BCS_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BCS_ABI_VERSION 1
+
+typedef struct bcs_sim bcs_sim;
+
+typedef enum bcs_status {
+    BCS_OK = 0,
+    BCS_ERR_INVALID_ARGUMENT = 1, /* malformed scene, bad pointer or size   */
+    BCS_ERR_CUDA = 2,             /* a CUDA runtime call failed             */
+    BCS_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed               */
+    BCS_ERR_NO_DEVICE = 4,        /* no CUDA device / extension unusable    */
+    BCS_ERR_UNSUPPORTED = 5       /* valid request this build cannot serve  */
+} bcs_status;
+
+/* Grid choice, replaces `using Grid = std::variant<UniformGrid*, NoGrid*>`
+ * (src/grids/grid_definition.hpp:6) and the UNIFORM_TRIANGLES_GRID switch
+ * (src/main.cu:44,130-135). */
+typedef enum bcs_grid_kind {
+    BCS_GRID_UNIFORM = 0,
+    BCS_GRID_NONE = 1
+} bcs_grid_kind;
+
+typedef enum bcs_memory {
+    BCS_MEM_HOST = 0,
+    BCS_MEM_DEVICE = 1
+} bcs_memory;
+
+/* Bits of the device error word (bcs_get_error_word). */
+enum {
+    BCS_ERRW_OUT_OF_GRID = 1u << 0,  /* a position fell outside the grid box; its
+                                        key was clamped (the reference only prints,
+                                        src/grids/uniform_grid.cu:26-29)            */
+    BCS_ERRW_NAN_NORMALIZE = 1u << 1,/* normalize() of a zero vector returned 0
+                                        (src/utilities/math.cuh:95-104)             */
+    BCS_ERRW_NONFINITE = 1u << 2     /* a non-finite position or velocity appeared */
+};
+
+/* Three SoA arrays, the layout of the reference's cudaVec3. */
+typedef struct bcs_vec3 {
+    float* x;
+    float* y;
+    float* z;
+} bcs_vec3;
+
+/* One blood-cell type, replaces BloodCellDef<Count, ParticlesInCell,
+ * IndicesInCell, Color, Springs, Vertices, Indices, Normals>
+ * (src/meta_factory/blood_cells_def_type.hpp:21-31).  Types are laid out in
+ * the order given (the reference's folded, sorted BloodCellList,
+ * src/meta_factory/blood_cell_factory.hpp:117-162); particles are cell-major
+ * inside a type. */
+typedef struct bcs_cell_type {
+    int count;                    /* cells of this type                        */
+    int particles_in_cell;        /* model vertices per cell                   */
+    const float* vertices;        /* [particles_in_cell][3] model positions    */
+    int spring_count;
+    const int* springs;           /* [spring_count][2] (start, end), Spring<> */
+    const float* spring_lengths;  /* [spring_count] rest lengths; a length of
+                                     0 means "no spring" as in the dense graph
+                                     (src/objects/blood_cells.cu:14)          */
+    const float* collision_radius;/* optional [particles_in_cell] collision
+                                     radii; NULL derives them like
+                                     generateBoundingSpheres
+                                     (src/simulation/simulation_controller.cu:93-153) */
+} bcs_cell_type;
+
+/* The vein mesh, replaces veinPositions / veinIndices / VeinEndingCenters /
+ * VeinEndingRadii (src/config/vein_definition.hpp:12,15965,31768-31776). */
+typedef struct bcs_vein {
+    int vertex_count;
+    const float* positions;       /* [vertex_count][3]                         */
+    int triangle_count;
+    const uint32_t* indices;      /* [triangle_count][3]                       */
+    int ending_count;
+    const float* ending_centers;  /* [ending_count][3]                         */
+    const float* ending_radii;    /* [ending_count]                            */
+} bcs_vein;
+
+/* Axial flow force of one vessel segment (no reference counterpart: the
+ * reference applies the constant G of src/config/physics.hpp:32-34).  A
+ * particle takes the segment whose axis is nearest; the force along the
+ * segment axis is peak_force * max(0, 1 - r^2 / radius^2). */
+typedef struct bcs_flow_segment {
+    float origin[3];
+    float direction[3];           /* unit axis, downstream                     */
+    float length;
+    float radius;
+    float peak_force;
+} bcs_flow_segment;
+
+/* Scalar scene constants.  Names follow src/config/simulation.hpp:3-21 and
+ * src/config/physics.hpp:4-34; bcs_default_params fills the reference's
+ * shipped values. */
+typedef struct bcs_params {
+    float dt;
+    int   use_blood_flow;
+    int   enable_reaction_force;
+    int   enable_big_cells_brake;
+    float cell_width, cell_height, cell_depth;                   /* particle grid */
+    float cell_width_triangles, cell_height_triangles, cell_depth_triangles;
+    float bounding_spheres_coeff;
+    float grid_y_margin;
+    float grid_xz_margin;
+    float min_spawn_y;
+    float velocity_collision_damping;
+    float particle_k_sniff;
+    float vein_k_sniff;
+    float particle_d_fact;
+    float vein_d_fact;
+    float vein_collision_force_intensity;
+    float viscous_damping;
+    float collision_spring_coeff;
+    float collision_damping_coeff;
+    float collision_shear_coeff;
+    float max_cell_size_factor_before_brake;
+    float big_particle_braking_intensity;
+    float init_velocity[3];
+    float vein_impact_distance;
+    float vein_impact_minimal_force_distance;
+    float gravity[3];                  /* Gx, Gy, Gz                              */
+    float cylinder_radius;             /* respawn spread, vein_factory.hpp:88    */
+    int   particle_grid;               /* bcs_grid_kind                           */
+    int   triangle_grid;               /* bcs_grid_kind                           */
+    int   vein_dynamic;                /* 1: vein springs + integration (the
+                                          reference); 0: fixed wall              */
+    int   refresh_triangle_centers;    /* 1: rebuild the triangle grid from the
+                                          moved mesh every step (the reference's
+                                          MULTI_GPU behaviour, main.cu:168-171);
+                                          0: centres from the initial mesh, as
+                                          its single-GPU loop does              */
+    uint64_t seed;                     /* respawn RNG (Philox4x32-10)             */
+} bcs_params;
+
+typedef struct bcs_scene_desc {
+    int type_count;
+    const bcs_cell_type* types;
+    bcs_vein vein;
+    int flow_segment_count;
+    const bcs_flow_segment* flow_segments;
+    bcs_params params;
+} bcs_scene_desc;
+
+/* Sizes and grid geometry derived at creation (the meta_factory constants
+ * particleCount, bloodCellCount, minX..maxZ, cellCountX.. of
+ * blood_cell_factory.hpp:172-192, vein_factory.hpp:46-86,
+ * uniform_grid.cu:83-104). */
+typedef struct bcs_info {
+    int particle_count;
+    int blood_cell_count;
+    int type_count;
+    int vertex_count;
+    int triangle_count;
+    float min_x, max_x, min_y, max_y, min_z, max_z;
+    int cell_count_x, cell_count_y, cell_count_z;              /* particle grid */
+    int64_t cell_count;
+    int tri_cell_count_x, tri_cell_count_y, tri_cell_count_z;  /* triangle grid */
+    int64_t tri_cell_count;
+    int64_t steps_done;
+    size_t device_bytes;
+} bcs_info;
+
+/* Fill *p with the reference's shipped constants (src/config/physics.hpp, simulation.hpp). */
+void bcs_default_params(bcs_params* p);
+
+const char* bcs_status_string(bcs_status s);
+int bcs_abi_version(void);
+
+/* Build the scene on the current CUDA device.  Replaces the constructors in
+ * src/main.cu:122-138 (BloodCells, VeinTriangles, UniformGrid x2,
+ * SimulationController) minus the curand seeding: initial particle state
+ * comes from bcs_set_particles.  `stream` is a cudaStream_t or NULL (the
+ * library then creates its own non-blocking stream). */
+bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out);
+bcs_status bcs_destroy(bcs_sim* sim);
+bcs_status bcs_get_info(bcs_sim* sim, bcs_info* out);
+
+/* Particle state (positions, velocities, forces) as written by
+ * setBloodCellsPositionsFromRandom (simulation_controller.cu:224-243) and
+ * read by the renderer from bloodCells.particles.positions[0]
+ * (main.cu:183-184).  A NULL forces.x zeroes the forces. */
+bcs_status bcs_set_particles(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velocities,
+                             bcs_vec3 forces, bcs_memory where);
+bcs_status bcs_get_particles(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velocities,
+                             bcs_vec3 forces, bcs_memory where);
+/* Vein vertex state (VeinTriangles positions/velocities/forces,
+ * src/objects/vein_triangles.cuh:53-55).  NULL members are skipped. */
+bcs_status bcs_set_vein(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velocities,
+                        bcs_memory where);
+bcs_status bcs_get_vein(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velocities,
+                        bcs_vec3 forces, bcs_memory where);
+
+/* ≙ particleGrid.calculateGrid(positions, particleCount) and
+ *   triangleCentersGrid.calculateGrid(centers, triangleCount)
+ *   (src/main.cu:175-176 → src/grids/uniform_grid.cu:129-155). */
+bcs_status bcs_calculate_grids(bcs_sim* sim);
+/* ≙ SimulationController::calculateNextFrame
+ *   (src/simulation/simulation_controller.cu:246-313). */
+bcs_status bcs_calculate_next_frame(bcs_sim* sim);
+/* ≙ SimulationController::propagateAll (simulation_controller.cu:315-331). */
+bcs_status bcs_propagate_all(bcs_sim* sim);
+/* `nsteps` whole frames of grids → next frame → propagate (the loop body of
+ * src/main.cu:158-247 minus rendering), fused and replayed from a CUDA graph.
+ * Same results as the three calls above in sequence. */
+bcs_status bcs_step(bcs_sim* sim, int nsteps);
+
+/* Grid arrays for parity checks, the UniformGrid members gridCellIds,
+ * particleIds, gridCellStarts, gridCellEnds (src/grids/uniform_grid.cuh:32-35)
+ * after the last bcs_calculate_grids / bcs_step.  which = 0: particle grid,
+ * 1: triangle grid.  cell_ids/object_ids hold `object count` entries (sorted
+ * keys and the object ids they carry); cell_starts/cell_ends hold the grid's
+ * cell count entries (inclusive ranges; empty cells read start 0, end -1).
+ * Any pointer may be NULL. */
+bcs_status bcs_get_grid(bcs_sim* sim, int which, int* cell_ids, int* object_ids,
+                        int* cell_starts, int* cell_ends, bcs_memory where);
+
+/* Headless replacement of the CUDA-GL interop kernels
+ * calculatePositionsKernel / calculateTriangleVerticesKernel
+ * (src/graphics/glcontroller.cu:22-49): particle vertices into a stride-6
+ * buffer (xyz + 3 zeros), one instance offset (stride 3) per particle, and
+ * vein vertices at stride 6.  NULL outputs are skipped. */
+bcs_status bcs_export_render(bcs_sim* sim, float* particle_vbo, float* particle_offsets,
+                             float* vein_vbo, bcs_memory where);
+
+/* Sticky device error word (BCS_ERRW_* bits) accumulated since the last
+ * clear; synchronises the stream. */
+bcs_status bcs_get_error_word(bcs_sim* sim, uint32_t* out, int clear);
+bcs_status bcs_synchronize(bcs_sim* sim);
+
+/* Time `nsteps` of bcs_step on the device with CUDA events recorded on the
+ * handle's stream; writes milliseconds.  For benchmarking. */
+bcs_status bcs_time_steps(bcs_sim* sim, int nsteps, float* ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BCS_H */

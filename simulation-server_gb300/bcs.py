@@ -1,0 +1,343 @@
+"""ctypes mirror of include/bcs.h and a thin host-side wrapper.
+
+`Simulation` keeps the reference's vocabulary for the per-frame calls of
+src/main.cu:175-208 — calculate_grids(), calculate_next_frame(),
+propagate_all() — plus the fused step().  It loads libbcs.so from this
+directory and raises if the library is missing or no CUDA device is usable:
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbcs.so")
+
+BCS_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "out of device memory",
+          4: "no CUDA device", 5: "unsupported"}
+GRID_UNIFORM, GRID_NONE = 0, 1
+MEM_HOST, MEM_DEVICE = 0, 1
+ERRW_OUT_OF_GRID, ERRW_NAN_NORMALIZE, ERRW_NONFINITE = 1, 2, 4
+
+EXPORTED = [
+    "bcs_default_params", "bcs_status_string", "bcs_abi_version", "bcs_create", "bcs_destroy",
+    "bcs_get_info", "bcs_set_particles", "bcs_get_particles", "bcs_set_vein", "bcs_get_vein",
+    "bcs_calculate_grids", "bcs_calculate_next_frame", "bcs_propagate_all", "bcs_step",
+    "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
+]
+
+
+class BcsError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: {STATUS.get(status, status)} ({status})")
+        self.status = status
+
+
+class Vec3(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p)]
+
+
+class CellType(C.Structure):
+    _fields_ = [("count", C.c_int), ("particles_in_cell", C.c_int), ("vertices", C.c_void_p),
+                ("spring_count", C.c_int), ("springs", C.c_void_p), ("spring_lengths", C.c_void_p),
+                ("collision_radius", C.c_void_p)]
+
+
+class Vein(C.Structure):
+    _fields_ = [("vertex_count", C.c_int), ("positions", C.c_void_p), ("triangle_count", C.c_int),
+                ("indices", C.c_void_p), ("ending_count", C.c_int), ("ending_centers", C.c_void_p),
+                ("ending_radii", C.c_void_p)]
+
+
+class FlowSegment(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("direction", C.c_float * 3), ("length", C.c_float),
+                ("radius", C.c_float), ("peak_force", C.c_float)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("dt", C.c_float), ("use_blood_flow", C.c_int), ("enable_reaction_force", C.c_int),
+        ("enable_big_cells_brake", C.c_int),
+        ("cell_width", C.c_float), ("cell_height", C.c_float), ("cell_depth", C.c_float),
+        ("cell_width_triangles", C.c_float), ("cell_height_triangles", C.c_float),
+        ("cell_depth_triangles", C.c_float),
+        ("bounding_spheres_coeff", C.c_float), ("grid_y_margin", C.c_float), ("grid_xz_margin", C.c_float),
+        ("min_spawn_y", C.c_float), ("velocity_collision_damping", C.c_float), ("particle_k_sniff", C.c_float),
+        ("vein_k_sniff", C.c_float), ("particle_d_fact", C.c_float), ("vein_d_fact", C.c_float),
+        ("vein_collision_force_intensity", C.c_float), ("viscous_damping", C.c_float),
+        ("collision_spring_coeff", C.c_float), ("collision_damping_coeff", C.c_float),
+        ("collision_shear_coeff", C.c_float), ("max_cell_size_factor_before_brake", C.c_float),
+        ("big_particle_braking_intensity", C.c_float), ("init_velocity", C.c_float * 3),
+        ("vein_impact_distance", C.c_float), ("vein_impact_minimal_force_distance", C.c_float),
+        ("gravity", C.c_float * 3), ("cylinder_radius", C.c_float), ("particle_grid", C.c_int),
+        ("triangle_grid", C.c_int), ("vein_dynamic", C.c_int), ("refresh_triangle_centers", C.c_int),
+        ("seed", C.c_uint64),
+    ]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("type_count", C.c_int), ("types", C.POINTER(CellType)), ("vein", Vein),
+                ("flow_segment_count", C.c_int), ("flow_segments", C.POINTER(FlowSegment)),
+                ("params", Params)]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("particle_count", C.c_int), ("blood_cell_count", C.c_int), ("type_count", C.c_int),
+        ("vertex_count", C.c_int), ("triangle_count", C.c_int),
+        ("min_x", C.c_float), ("max_x", C.c_float), ("min_y", C.c_float), ("max_y", C.c_float),
+        ("min_z", C.c_float), ("max_z", C.c_float),
+        ("cell_count_x", C.c_int), ("cell_count_y", C.c_int), ("cell_count_z", C.c_int),
+        ("cell_count", C.c_int64),
+        ("tri_cell_count_x", C.c_int), ("tri_cell_count_y", C.c_int), ("tri_cell_count_z", C.c_int),
+        ("tri_cell_count", C.c_int64), ("steps_done", C.c_int64), ("device_bytes", C.c_size_t),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load libbcs.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with bcs_build.build() (no CPU fallback exists)")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    sigs = {
+        "bcs_default_params": ([C.POINTER(Params)], None),
+        "bcs_status_string": ([C.c_int], C.c_char_p),
+        "bcs_abi_version": ([], C.c_int),
+        "bcs_create": ([C.POINTER(SceneDesc), P, C.POINTER(P)], C.c_int),
+        "bcs_destroy": ([P], C.c_int),
+        "bcs_get_info": ([P, C.POINTER(Info)], C.c_int),
+        "bcs_set_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
+        "bcs_get_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
+        "bcs_set_vein": ([P, Vec3, Vec3, C.c_int], C.c_int),
+        "bcs_get_vein": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
+        "bcs_calculate_grids": ([P], C.c_int),
+        "bcs_calculate_next_frame": ([P], C.c_int),
+        "bcs_propagate_all": ([P], C.c_int),
+        "bcs_step": ([P, C.c_int], C.c_int),
+        "bcs_get_grid": ([P, C.c_int, P, P, P, P, C.c_int], C.c_int),
+        "bcs_export_render": ([P, P, P, P, C.c_int], C.c_int),
+        "bcs_get_error_word": ([P, C.POINTER(C.c_uint32), C.c_int], C.c_int),
+        "bcs_synchronize": ([P], C.c_int),
+        "bcs_time_steps": ([P, C.c_int, C.POINTER(C.c_float)], C.c_int),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+# The reference's shipped constants (src/config/simulation.hpp:3-21,
+# src/config/physics.hpp:4-34, src/meta_factory/vein_factory.hpp:88); the
+# library's bcs_default_params returns the same values.
+REFERENCE_DEFAULTS = dict(
+    dt=0.008, use_blood_flow=1, enable_reaction_force=1, enable_big_cells_brake=1,
+    cell_width=2.0, cell_height=2.0, cell_depth=2.0,
+    cell_width_triangles=25.0, cell_height_triangles=25.0, cell_depth_triangles=25.0,
+    bounding_spheres_coeff=3.0, grid_y_margin=40.0, grid_xz_margin=40.0, min_spawn_y=-20.0,
+    velocity_collision_damping=0.96, particle_k_sniff=25.0, vein_k_sniff=0.1, particle_d_fact=10.0,
+    vein_d_fact=0.7, vein_collision_force_intensity=0.005, viscous_damping=0.39, collision_spring_coeff=6.0,
+    collision_damping_coeff=6.0, collision_shear_coeff=4.0, max_cell_size_factor_before_brake=1.5,
+    big_particle_braking_intensity=0.8, init_velocity=(0.0, -80.0, 0.0), vein_impact_distance=6.0,
+    vein_impact_minimal_force_distance=0.001, gravity=(0.0, -25.0, 0.0), cylinder_radius=50.0,
+    particle_grid=GRID_UNIFORM, triangle_grid=GRID_UNIFORM, vein_dynamic=1, refresh_triangle_centers=0, seed=0,
+)
+
+
+def default_params() -> Params:
+    """Params filled with the reference's shipped constants (pure Python)."""
+    p = Params()
+    for k, v in REFERENCE_DEFAULTS.items():
+        if isinstance(v, tuple):
+            getattr(p, k)[:] = v
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def library_default_params() -> Params:
+    """The same constants as evaluated by libbcs.so's bcs_default_params."""
+    p = Params()
+    load_library().bcs_default_params(C.byref(p))
+    return p
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())     # torch tensor
+
+
+def _check(status: int, what: str) -> None:
+    if status != BCS_OK:
+        raise BcsError(status, what)
+
+
+class SceneBuffers:
+    """Keeps the numpy arrays behind a SceneDesc alive."""
+
+    def __init__(self, scene):
+        self.keep = []
+        types = (CellType * len(scene.types))()
+        for i, t in enumerate(scene.types):
+            verts = np.ascontiguousarray(t.vertices, dtype=np.float32)
+            springs = np.ascontiguousarray(t.springs, dtype=np.int32).reshape(-1, 2)
+            lengths = np.ascontiguousarray(t.spring_lengths, dtype=np.float32)
+            rad = None if t.collision_radius is None else np.ascontiguousarray(t.collision_radius, dtype=np.float32)
+            self.keep += [verts, springs, lengths, rad]
+            types[i] = CellType(int(t.count), int(verts.shape[0]), verts.ctypes.data, int(springs.shape[0]),
+                                springs.ctypes.data if springs.size else None,
+                                lengths.ctypes.data if lengths.size else None,
+                                None if rad is None else rad.ctypes.data)
+        vp = np.ascontiguousarray(scene.vein_positions, dtype=np.float32)
+        vi = np.ascontiguousarray(scene.vein_indices, dtype=np.uint32)
+        ec = np.ascontiguousarray(scene.ending_centers, dtype=np.float32).reshape(-1, 3)
+        er = np.ascontiguousarray(scene.ending_radii, dtype=np.float32).reshape(-1)
+        self.keep += [vp, vi, ec, er, types]
+        vein = Vein(int(vp.shape[0]), vp.ctypes.data, int(vi.shape[0]), vi.ctypes.data if vi.size else None,
+                    int(er.shape[0]), ec.ctypes.data if er.size else None, er.ctypes.data if er.size else None)
+        flows = (FlowSegment * max(1, len(scene.flow_segments)))()
+        for i, f in enumerate(scene.flow_segments):
+            flows[i] = FlowSegment((C.c_float * 3)(*f["origin"]), (C.c_float * 3)(*f["direction"]),
+                                   f["length"], f["radius"], f["peak_force"])
+        self.keep.append(flows)
+        self.desc = SceneDesc(len(scene.types), types, vein, len(scene.flow_segments), flows, scene.params)
+
+
+class Simulation:
+    """One scene on the current CUDA device (≙ BloodCells + VeinTriangles +
+    two UniformGrids + SimulationController of src/main.cu:122-138)."""
+
+    def __init__(self, scene, stream: int | None = None):
+        self.lib = load_library()
+        self.scene = scene
+        self._bufs = SceneBuffers(scene)
+        h = C.c_void_p()
+        _check(self.lib.bcs_create(C.byref(self._bufs.desc), stream, C.byref(h)), "bcs_create")
+        self.h = h
+        self.info = Info()
+        _check(self.lib.bcs_get_info(self.h, C.byref(self.info)), "bcs_get_info")
+        self.n = self.info.particle_count
+        self.nv = self.info.vertex_count
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.bcs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- state ------------------------------------------------------------
+    def set_particles(self, pos, vel, force=None) -> None:
+        """pos/vel/force: [N, 3] float32 numpy arrays (host)."""
+        soa = [np.ascontiguousarray(np.asarray(a, dtype=np.float32).T) for a in (pos, vel)]
+        f = None if force is None else np.ascontiguousarray(np.asarray(force, dtype=np.float32).T)
+        vecs = [Vec3(a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data) for a in soa]
+        fv = Vec3() if f is None else Vec3(f[0].ctypes.data, f[1].ctypes.data, f[2].ctypes.data)
+        _check(self.lib.bcs_set_particles(self.h, vecs[0], vecs[1], fv, MEM_HOST), "bcs_set_particles")
+
+    def get_particles(self):
+        out = [np.empty((3, self.n), np.float32) for _ in range(3)]
+        vecs = [Vec3(a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data) for a in out]
+        _check(self.lib.bcs_get_particles(self.h, vecs[0], vecs[1], vecs[2], MEM_HOST), "bcs_get_particles")
+        return tuple(np.ascontiguousarray(a.T) for a in out)
+
+    def set_particles_device(self, x, y, z, vx, vy, vz) -> None:
+        """Device pointers (torch CUDA tensors) in cudaVec3 SoA layout."""
+        _check(self.lib.bcs_set_particles(self.h, Vec3(_ptr(x), _ptr(y), _ptr(z)), Vec3(_ptr(vx), _ptr(vy), _ptr(vz)),
+                                          Vec3(), MEM_DEVICE), "bcs_set_particles")
+
+    def get_particles_device(self, x, y, z, vx=None, vy=None, vz=None) -> None:
+        _check(self.lib.bcs_get_particles(self.h, Vec3(_ptr(x), _ptr(y), _ptr(z)), Vec3(_ptr(vx), _ptr(vy), _ptr(vz)),
+                                          Vec3(), MEM_DEVICE), "bcs_get_particles")
+
+    def set_vein(self, pos=None, vel=None) -> None:
+        keep = []
+
+        def v3(a):
+            if a is None:
+                return Vec3()
+            s = np.ascontiguousarray(np.asarray(a, dtype=np.float32).T)
+            keep.append(s)
+            return Vec3(s[0].ctypes.data, s[1].ctypes.data, s[2].ctypes.data)
+        _check(self.lib.bcs_set_vein(self.h, v3(pos), v3(vel), MEM_HOST), "bcs_set_vein")
+
+    def get_vein(self):
+        out = [np.empty((3, self.nv), np.float32) for _ in range(3)]
+        vecs = [Vec3(a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data) for a in out]
+        _check(self.lib.bcs_get_vein(self.h, vecs[0], vecs[1], vecs[2], MEM_HOST), "bcs_get_vein")
+        return tuple(np.ascontiguousarray(a.T) for a in out)
+
+    # ---- the frame ---------------------------------------------------------
+    def calculate_grids(self) -> None:
+        _check(self.lib.bcs_calculate_grids(self.h), "bcs_calculate_grids")
+
+    def calculate_next_frame(self) -> None:
+        _check(self.lib.bcs_calculate_next_frame(self.h), "bcs_calculate_next_frame")
+
+    def propagate_all(self) -> None:
+        _check(self.lib.bcs_propagate_all(self.h), "bcs_propagate_all")
+
+    def step(self, nsteps: int = 1) -> None:
+        _check(self.lib.bcs_step(self.h, int(nsteps)), "bcs_step")
+
+    def time_steps(self, nsteps: int) -> float:
+        ms = C.c_float()
+        _check(self.lib.bcs_time_steps(self.h, int(nsteps), C.byref(ms)), "bcs_time_steps")
+        return ms.value
+
+    def synchronize(self) -> None:
+        _check(self.lib.bcs_synchronize(self.h), "bcs_synchronize")
+
+    # ---- inspection ---------------------------------------------------------
+    def get_grid(self, which: int = 0, dense: bool = True):
+        cnt = self.n if which == 0 else self.info.triangle_count
+        cells = self.info.cell_count if which == 0 else self.info.tri_cell_count
+        keys = np.empty(cnt, np.int32)
+        ids = np.empty(cnt, np.int32)
+        starts = np.empty(cells, np.int32) if dense else None
+        ends = np.empty(cells, np.int32) if dense else None
+        _check(self.lib.bcs_get_grid(self.h, which, keys.ctypes.data, ids.ctypes.data, _ptr(starts), _ptr(ends),
+                                     MEM_HOST), "bcs_get_grid")
+        return keys, ids, starts, ends
+
+    def export_render(self):
+        pv = np.empty((self.n, 6), np.float32)
+        po = np.empty((self.n, 3), np.float32)
+        vv = np.empty((self.nv, 6), np.float32)
+        _check(self.lib.bcs_export_render(self.h, pv.ctypes.data, po.ctypes.data, vv.ctypes.data, MEM_HOST),
+               "bcs_export_render")
+        return pv, po, vv
+
+    def error_word(self, clear: bool = False) -> int:
+        w = C.c_uint32()
+        _check(self.lib.bcs_get_error_word(self.h, C.byref(w), int(clear)), "bcs_get_error_word")
+        return int(w.value)
+
+    def refresh_info(self) -> Info:
+        _check(self.lib.bcs_get_info(self.h, C.byref(self.info)), "bcs_get_info")
+        return self.info

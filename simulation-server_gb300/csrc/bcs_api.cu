@@ -1,0 +1,830 @@
+// bcs_api.cu — host side of the engine and the C ABI of include/bcs.h.
+//
+// Creation folds the runtime scene the way the reference's meta_factory folds
+// its compile-time one (src/meta_factory/blood_cell_factory.hpp:172-328,
+// src/meta_factory/vein_factory.hpp:21-174) and the way SimulationController
+// derives its per-model tables (src/simulation/simulation_controller.cu:93-153),
+// uploads everything once, and builds the static triangle grid.  The step
+// then runs entirely on the handle's stream; bcs_step replays a captured
+// CUDA graph of one frame.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <vector>
+
+#include "bcs_internal.cuh"
+
+namespace bcs {
+// bcs_kernels.cu
+void launch_step(const StepArgs& a, int blocks, int mode, cudaStream_t s);
+void launch_propagate(const StepArgs& a, int blocks, cudaStream_t s);
+void launch_keys(const float4* pos, int n, const GridDev& g, int* keys, int* ids, unsigned* err, cudaStream_t s);
+void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const GridDev& g, int* keys, int* ids,
+                     cudaStream_t s);
+void launch_cell_ranges(const int* keys, int n, int2* table, cudaStream_t s);
+void launch_dense_ranges(const int2* table, const int* keys, int count, long long cells, int* starts, int* ends,
+                         cudaStream_t s);
+void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
+                         int V, float k, float d, unsigned* err, cudaStream_t s);
+void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt, cudaStream_t s);
+void launch_tri_cache(const int* ids, const uint32_t* tri, const float4* vpos, int T, float4* cache, cudaStream_t s);
+void launch_bump_step(long long* steps, cudaStream_t s);
+void launch_export(const float4* pos, int n, const float4* vpos, int V, float* pvbo, float* poff, float* vvbo,
+                   cudaStream_t s);
+void launch_pack(const float* x, const float* y, const float* z, int n, float4* out, const float* wsrc,
+                 cudaStream_t s);
+void launch_unpack(const float4* in, int n, float* x, float* y, float* z, cudaStream_t s);
+// bcs_sort.cu
+int radix_sort_pairs(const int* in_k, const int* in_v, int* a_k, int* a_v, int* b_k, int* b_v, int n, int bits,
+                     unsigned* temp, cudaStream_t s);
+size_t radix_temp_words(int n);
+}  // namespace bcs
+
+using namespace bcs;
+
+namespace {
+
+struct DeviceGrid {
+    GridDev g{};           // geometry + pointers to the sorted result
+    int* in_k = nullptr;   // unsorted keys / ids (written by the key kernels)
+    int* in_v = nullptr;
+    int* a_k = nullptr;
+    int* a_v = nullptr;
+    int* b_k = nullptr;
+    int* b_v = nullptr;
+    int2* table = nullptr;
+    unsigned* temp = nullptr;
+    int bits = 0;
+    int count = 0;
+};
+
+}  // namespace
+
+struct bcs_sim {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    bcs_params p{};
+    int N = 0, C = 0, V = 0, T = 0;
+    std::vector<TypeDev> types;
+    std::vector<WorkItem> work_host;
+    size_t bytes = 0;
+    std::vector<void*> allocations;
+    // particle state
+    float4* pos[2] = {nullptr, nullptr};
+    float4* vel[2] = {nullptr, nullptr};
+    float4* frc[2] = {nullptr, nullptr};
+    float* radius_of_particle = nullptr;
+    int cur = 0;
+    bool mid_frame = false;      // between calculate_next_frame and propagate_all
+    bool keys_valid = false;     // pgrid.in_k holds keys of pos[cur]
+    bool grid_ready = false;
+    // layout tables
+    WorkItem* work = nullptr;
+    int* adj_off = nullptr;
+    int* adj_nbr = nullptr;
+    float* adj_len = nullptr;
+    float* r0 = nullptr;
+    float4* respawn = nullptr;
+    // vein
+    float4* vpos = nullptr;
+    float4* vvel = nullptr;
+    float4* vfrc = nullptr;
+    int* nb_ids = nullptr;
+    float* nb_len = nullptr;
+    uint32_t* tri = nullptr;
+    float4* tcache = nullptr;
+    // grids
+    DeviceGrid pg, tg;
+    float minX, maxX, minY, maxY, minZ, maxZ, width, height, depth;
+    // misc
+    long long* steps = nullptr;
+    long long host_steps = 0;
+    unsigned* err = nullptr;
+    StepArgs args{};
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+#define BCS_CUDA(call)                                          \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) {                                \
+            return e_ == cudaErrorMemoryAllocation ? BCS_ERR_OUT_OF_MEMORY : BCS_ERR_CUDA; \
+        }                                                       \
+    } while (0)
+
+template <class T>
+bcs_status dalloc(bcs_sim* s, T** ptr, size_t count) {
+    *ptr = nullptr;
+    if (count == 0) count = 1;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * count);
+    if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? BCS_ERR_OUT_OF_MEMORY : BCS_ERR_CUDA;
+    s->allocations.push_back(p);
+    s->bytes += sizeof(T) * count;
+    *ptr = static_cast<T*>(p);
+    return BCS_OK;
+}
+
+template <class T>
+bcs_status upload(bcs_sim* s, T** ptr, const std::vector<T>& host) {
+    bcs_status st = dalloc(s, ptr, host.size());
+    if (st != BCS_OK) return st;
+    if (!host.empty()) BCS_CUDA(cudaMemcpy(*ptr, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice));
+    return BCS_OK;
+}
+
+int bits_for(long long cells) {
+    int b = 0;
+    while (b < 31 && (1LL << b) < cells) ++b;
+    return b;
+}
+
+bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count) {
+    dg.count = count;
+    dg.g.count = count;
+    bcs_status st;
+    if ((st = dalloc(s, &dg.in_k, count)) || (st = dalloc(s, &dg.in_v, count)) || (st = dalloc(s, &dg.a_k, count)) ||
+        (st = dalloc(s, &dg.a_v, count)) || (st = dalloc(s, &dg.b_k, count)) || (st = dalloc(s, &dg.b_v, count)) ||
+        (st = dalloc(s, &dg.temp, radix_temp_words(count))))
+        return st;
+    if (dg.g.uniform) {
+        if ((st = dalloc(s, &dg.table, (size_t)dg.g.cells))) return st;
+        BCS_CUDA(cudaMemset(dg.table, 0, sizeof(int2) * (size_t)dg.g.cells));
+    }
+    dg.bits = bits_for(dg.g.cells);
+    return BCS_OK;
+}
+
+// Sort the grid's unsorted keys and rebuild its validated range table.
+void sort_grid(DeviceGrid& dg, cudaStream_t st) {
+    int which = radix_sort_pairs(dg.in_k, dg.in_v, dg.a_k, dg.a_v, dg.b_k, dg.b_v, dg.count, dg.bits, dg.temp, st);
+    dg.g.keys = which ? dg.b_k : dg.a_k;
+    dg.g.ids = which ? dg.b_v : dg.a_v;
+    dg.g.table = dg.table;
+    launch_cell_ranges(dg.g.keys, dg.count, dg.table, st);
+}
+
+void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
+    StepArgs& a = s->args;
+    a.pos_in = s->pos[in];
+    a.vel_in = s->vel[in];
+    a.frc_in = s->frc[in];
+    a.pos_out = s->pos[out];
+    a.vel_out = s->vel[out];
+    a.frc_out = s->frc[out];
+    a.keys_out = write_keys ? s->pg.in_k : nullptr;
+    a.ids_out = write_keys ? s->pg.in_v : nullptr;
+    a.pg = s->pg.g;
+    a.tg = s->tg.g;
+    a.tcache = s->tcache;
+}
+
+// Triangle grid + Moller-Trumbore cache from the current vein positions.
+void build_triangle_grid(bcs_sim* s, bool regrid) {
+    if (s->T == 0) return;
+    if (s->tg.g.uniform) {
+        if (regrid) {
+            launch_tri_keys(s->vpos, s->tri, s->T, s->tg.g, s->tg.in_k, s->tg.in_v, s->stream);
+            sort_grid(s->tg, s->stream);
+        }
+        launch_tri_cache(s->tg.g.ids, s->tri, s->vpos, s->T, s->tcache, s->stream);
+    } else {
+        launch_tri_cache(nullptr, s->tri, s->vpos, s->T, s->tcache, s->stream);
+    }
+}
+
+// ≙ main.cu:175-176.
+void enqueue_grids(bcs_sim* s) {
+    if (!s->keys_valid) {
+        launch_keys(s->pos[s->cur], s->N, s->pg.g, s->pg.in_k, s->pg.in_v, s->err, s->stream);
+        s->keys_valid = true;
+    }
+    if (s->pg.g.uniform) sort_grid(s->pg, s->stream);
+    if (s->p.refresh_triangle_centers) build_triangle_grid(s, true);
+    s->grid_ready = true;
+}
+
+void enqueue_vein_forces(bcs_sim* s) {
+    if (s->p.vein_dynamic && s->V > 0)
+        launch_vein_springs(s->vpos, s->vvel, s->vfrc, s->nb_ids, s->nb_len, s->V, s->p.vein_k_sniff, s->p.vein_d_fact,
+                            s->err, s->stream);
+}
+
+void enqueue_vein_propagate(bcs_sim* s) {
+    if (s->p.vein_dynamic && s->V > 0) {
+        launch_vein_integrate(s->vpos, s->vvel, s->vfrc, s->V, s->p.dt, s->stream);
+        build_triangle_grid(s, false);
+    }
+    launch_bump_step(s->steps, s->stream);
+}
+
+// One fused frame on the stream (no host synchronisation).
+void enqueue_frame(bcs_sim* s) {
+    enqueue_grids(s);
+    enqueue_vein_forces(s);
+    const int in = s->cur, out = s->cur ^ 1;
+    refresh_args(s, in, out, true);
+    launch_step(s->args, (int)s->work_host.size(), 0, s->stream);
+    enqueue_vein_propagate(s);
+    s->cur = out;
+    s->keys_valid = true;    // k_step wrote keys of the new positions
+    ++s->host_steps;
+}
+
+bcs_status check_last() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? BCS_ERR_OUT_OF_MEMORY : BCS_ERR_CUDA;
+    return BCS_OK;
+}
+
+void drop_graphs(bcs_sim* s) {
+    for (auto& g : s->graph)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+bcs_status validate(const bcs_scene_desc* d) {
+    if (!d || d->type_count <= 0 || d->type_count > kMaxTypes || !d->types) return BCS_ERR_INVALID_ARGUMENT;
+    long long n = 0;
+    for (int t = 0; t < d->type_count; ++t) {
+        const bcs_cell_type& c = d->types[t];
+        if (c.count < 0 || c.particles_in_cell <= 0 || !c.vertices) return BCS_ERR_INVALID_ARGUMENT;
+        if (c.particles_in_cell > kMaxChunk) return BCS_ERR_UNSUPPORTED;
+        if (c.spring_count < 0 || (c.spring_count > 0 && (!c.springs || !c.spring_lengths)))
+            return BCS_ERR_INVALID_ARGUMENT;
+        for (int k = 0; k < 2 * c.spring_count; ++k)
+            if (c.springs[k] < 0 || c.springs[k] >= c.particles_in_cell) return BCS_ERR_INVALID_ARGUMENT;
+        n += (long long)c.count * c.particles_in_cell;
+    }
+    if (n <= 0 || n > INT32_MAX / 2) return BCS_ERR_INVALID_ARGUMENT;
+    const bcs_vein& v = d->vein;
+    if (v.vertex_count <= 0 || !v.positions || v.triangle_count < 0 || (v.triangle_count > 0 && !v.indices))
+        return BCS_ERR_INVALID_ARGUMENT;
+    for (long long k = 0; k < 3LL * v.triangle_count; ++k)
+        if (v.indices[k] >= (uint32_t)v.vertex_count) return BCS_ERR_INVALID_ARGUMENT;
+    if (v.ending_count < 0 || v.ending_count > 8 || (v.ending_count > 0 && (!v.ending_centers || !v.ending_radii)))
+        return BCS_ERR_INVALID_ARGUMENT;
+    if (d->flow_segment_count < 0 || d->flow_segment_count > kMaxFlow ||
+        (d->flow_segment_count > 0 && !d->flow_segments))
+        return BCS_ERR_INVALID_ARGUMENT;
+    const bcs_params& p = d->params;
+    if (!(p.cell_width > 0 && p.cell_height > 0 && p.cell_depth > 0 && p.cell_width_triangles > 0 &&
+          p.cell_height_triangles > 0 && p.cell_depth_triangles > 0 && p.bounding_spheres_coeff != 0))
+        return BCS_ERR_INVALID_ARGUMENT;
+    return BCS_OK;
+}
+
+bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
+    bcs_status st;
+    s->p = d->params;
+    BCS_CUDA(cudaGetDevice(&s->device));
+    if (stream) {
+        s->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        BCS_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        s->own_stream = true;
+    }
+    BCS_CUDA(cudaEventCreate(&s->ev0));
+    BCS_CUDA(cudaEventCreate(&s->ev1));
+
+    // ---- cell types: offsets, CSR springs, radii (blood_cell_factory.hpp:172-328,
+    //      simulation_controller.cu:93-153)
+    std::vector<int> adj_off, adj_nbr;
+    std::vector<float> adj_len, r0, radius_model;
+    std::vector<float4> respawn;
+    int pstart = 0, cstart = 0, mstart = 0;
+    for (int t = 0; t < d->type_count; ++t) {
+        const bcs_cell_type& c = d->types[t];
+        const int pic = c.particles_in_cell;
+        TypeDev td{c.count, pic, pstart, cstart, mstart, (int)adj_off.size()};
+        // Dense graph with the reference's rules: later springs overwrite
+        // earlier ones, a rest length of 0 is "no spring".
+        std::vector<float> dense((size_t)pic * pic, 0.0f);
+        for (int k = 0; k < c.spring_count; ++k) {
+            int a = c.springs[2 * k], b = c.springs[2 * k + 1];
+            dense[(size_t)a * pic + b] = c.spring_lengths[k];
+            dense[(size_t)b * pic + a] = c.spring_lengths[k];
+        }
+        for (int i = 0; i < pic; ++i) {
+            adj_off.push_back((int)adj_nbr.size());
+            for (int j = 0; j < pic; ++j) {
+                float L = dense[(size_t)j * pic + i];
+                if (L == 0.0f || j == i) continue;   // a self spring contributes exactly 0
+                adj_nbr.push_back(j);
+                adj_len.push_back(L);
+            }
+        }
+        adj_off.push_back((int)adj_nbr.size());
+        const float* m = c.vertices;
+        float cx = 0, cy = 0, cz = 0;
+        for (int j = 0; j < pic; ++j) {
+            float best = std::numeric_limits<float>::max();
+            for (int k = 0; k < pic; ++k) {
+                if (j == k) continue;
+                double len = std::sqrt(std::pow((double)(m[3 * j] - m[3 * k]), 2) +
+                                       std::pow((double)(m[3 * j + 1] - m[3 * k + 1]), 2) +
+                                       std::pow((double)(m[3 * j + 2] - m[3 * k + 2]), 2)) /
+                             (2 * (double)s->p.bounding_spheres_coeff);
+                if (len < best) best = (float)len;
+            }
+            radius_model.push_back(c.collision_radius ? c.collision_radius[j] : best);
+            cx += m[3 * j]; cy += m[3 * j + 1]; cz += m[3 * j + 2];
+        }
+        cx /= pic; cy /= pic; cz /= pic;
+        for (int j = 0; j < pic; ++j) {
+            float dx = m[3 * j] - cx, dy = m[3 * j + 1] - cy, dz = m[3 * j + 2] - cz;
+            r0.push_back(sqrtf(dx * dx + dy * dy + dz * dz));
+            respawn.push_back(make_float4(m[3 * j] - m[0], m[3 * j + 1] - m[1], m[3 * j + 2] - m[2], 0.f));
+        }
+        s->types.push_back(td);
+        // Work items: whole cells, at most kMaxChunk particles per CTA.
+        int per = std::max(1, std::min(kMaxCellsPerChunk, kMaxChunk / pic));
+        for (int c0 = 0; c0 < c.count; c0 += per) s->work_host.push_back(WorkItem{t, c0, std::min(per, c.count - c0)});
+        pstart += c.count * pic;
+        cstart += c.count;
+        mstart += pic;
+    }
+    s->N = pstart;
+    s->C = cstart;
+    std::vector<float> radius_particle(s->N);
+    for (const TypeDev& td : s->types)
+        for (int i = 0; i < td.count * td.pic; ++i)
+            radius_particle[td.particle_start + i] = radius_model[td.model_start + i % td.pic];
+
+    // ---- vein: bounds (vein_factory.hpp:21-86), neighbours (:130-174)
+    const bcs_vein& vn = d->vein;
+    s->V = vn.vertex_count;
+    s->T = vn.triangle_count;
+    float mn[3] = {vn.positions[0], vn.positions[1], vn.positions[2]}, mx[3] = {mn[0], mn[1], mn[2]};
+    for (int i = 1; i < s->V; ++i)
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = std::min(mn[k], vn.positions[3 * i + k]);
+            mx[k] = std::max(mx[k], vn.positions[3 * i + k]);
+        }
+    s->minX = mn[0] - s->p.grid_xz_margin; s->maxX = mx[0] + s->p.grid_xz_margin;
+    s->minY = mn[1] - s->p.grid_y_margin;  s->maxY = mx[1] + s->p.grid_y_margin;
+    s->minZ = mn[2] - s->p.grid_xz_margin; s->maxZ = mx[2] + s->p.grid_xz_margin;
+    s->width = s->maxX - s->minX; s->height = s->maxY - s->minY; s->depth = s->maxZ - s->minZ;
+    auto geometry = [&](DeviceGrid& dg, int kind, float cw, float ch, float cd) -> bcs_status {
+        GridDev& g = dg.g;
+        g.uniform = kind == BCS_GRID_UNIFORM;
+        g.lo[0] = s->minX; g.lo[1] = s->minY; g.lo[2] = s->minZ;
+        g.hi[0] = s->maxX; g.hi[1] = s->maxY; g.hi[2] = s->maxZ;
+        g.ext[0] = s->width; g.ext[1] = s->height; g.ext[2] = s->depth;
+        g.cell[0] = cw; g.cell[1] = ch; g.cell[2] = cd;
+        g.cx = (int)(s->width / cw); g.cy = (int)(s->height / ch); g.cz = (int)(s->depth / cd);
+        g.cells = (long long)g.cx * g.cy * g.cz;
+        if (g.uniform && (g.cx < 1 || g.cy < 1 || g.cz < 1 || g.cells > INT32_MAX)) return BCS_ERR_INVALID_ARGUMENT;
+        return BCS_OK;
+    };
+    if ((st = geometry(s->pg, s->p.particle_grid, s->p.cell_width, s->p.cell_height, s->p.cell_depth)) ||
+        (st = geometry(s->tg, s->p.triangle_grid, s->p.cell_width_triangles, s->p.cell_height_triangles,
+                       s->p.cell_depth_triangles)))
+        return st;
+    std::vector<int> nb_ids((size_t)9 * s->V, -1);
+    std::vector<float> nb_len((size_t)9 * s->V, -1.0f);
+    {
+        std::vector<std::vector<uint32_t>> nb(s->V);
+        for (int t = 0; t < s->T; ++t) {
+            uint32_t i0 = vn.indices[3 * t], i1 = vn.indices[3 * t + 1], i2 = vn.indices[3 * t + 2];
+            nb[i0].push_back(i1); nb[i0].push_back(i2);
+            nb[i1].push_back(i0); nb[i1].push_back(i2);
+            nb[i2].push_back(i0); nb[i2].push_back(i1);
+        }
+        for (int i = 0; i < s->V; ++i) {
+            std::sort(nb[i].begin(), nb[i].end());
+            for (size_t k = 0; k < std::min<size_t>(nb[i].size(), 9); ++k) {
+                uint32_t j = nb[i][k];
+                float dx = vn.positions[3 * i] - vn.positions[3 * j];
+                float dy = vn.positions[3 * i + 1] - vn.positions[3 * j + 1];
+                float dz = vn.positions[3 * i + 2] - vn.positions[3 * j + 2];
+                float l = sqrtf(dx * dx + dy * dy + dz * dz);
+                nb_ids[k * (size_t)s->V + i] = (int)j;
+                nb_len[k * (size_t)s->V + i] = l < 0 ? -l : l;
+            }
+        }
+    }
+
+    // ---- device buffers
+    for (int b = 0; b < 2; ++b)
+        if ((st = dalloc(s, &s->pos[b], s->N)) || (st = dalloc(s, &s->vel[b], s->N)) ||
+            (st = dalloc(s, &s->frc[b], s->N)))
+            return st;
+    for (int b = 0; b < 2; ++b) {
+        BCS_CUDA(cudaMemset(s->pos[b], 0, sizeof(float4) * s->N));
+        BCS_CUDA(cudaMemset(s->vel[b], 0, sizeof(float4) * s->N));
+        BCS_CUDA(cudaMemset(s->frc[b], 0, sizeof(float4) * s->N));
+    }
+    if ((st = upload(s, &s->radius_of_particle, radius_particle)) || (st = upload(s, &s->work, s->work_host)) ||
+        (st = upload(s, &s->adj_off, adj_off)) || (st = upload(s, &s->adj_nbr, adj_nbr)) ||
+        (st = upload(s, &s->adj_len, adj_len)) || (st = upload(s, &s->r0, r0)) || (st = upload(s, &s->respawn, respawn)))
+        return st;
+    std::vector<float4> vpos(s->V);
+    for (int i = 0; i < s->V; ++i)
+        vpos[i] = make_float4(vn.positions[3 * i], vn.positions[3 * i + 1], vn.positions[3 * i + 2], 0.f);
+    std::vector<uint32_t> tri(vn.indices, vn.indices + 3 * (size_t)s->T);
+    if ((st = upload(s, &s->vpos, vpos)) || (st = dalloc(s, &s->vvel, s->V)) || (st = dalloc(s, &s->vfrc, s->V)) ||
+        (st = upload(s, &s->nb_ids, nb_ids)) || (st = upload(s, &s->nb_len, nb_len)) || (st = upload(s, &s->tri, tri)) ||
+        (st = dalloc(s, &s->tcache, 3 * (size_t)s->T)))
+        return st;
+    BCS_CUDA(cudaMemset(s->vvel, 0, sizeof(float4) * s->V));
+    BCS_CUDA(cudaMemset(s->vfrc, 0, sizeof(float4) * s->V));
+    if ((st = alloc_grid(s, s->pg, s->N)) || (st = alloc_grid(s, s->tg, std::max(1, s->T)))) return st;
+    s->tg.count = s->T;
+    s->tg.g.count = s->T;
+    if ((st = dalloc(s, &s->steps, 1)) || (st = dalloc(s, &s->err, 1))) return st;
+    BCS_CUDA(cudaMemset(s->steps, 0, sizeof(long long)));
+    BCS_CUDA(cudaMemset(s->err, 0, sizeof(unsigned)));
+
+    // ---- kernel arguments that never change
+    StepArgs& a = s->args;
+    a.n = s->N;
+    a.work = s->work;
+    for (int t = 0; t < d->type_count; ++t) a.types[t] = s->types[t];
+    a.type_count = d->type_count;
+    a.adj_off = s->adj_off;
+    a.adj_nbr = s->adj_nbr;
+    a.adj_len = s->adj_len;
+    a.r0 = s->r0;
+    a.respawn = s->respawn;
+    a.vpos = s->vpos;
+    a.vfrc = s->vfrc;
+    a.tri = s->tri;
+    a.T = s->T;
+    a.flow_count = d->flow_segment_count;
+    for (int k = 0; k < d->flow_segment_count; ++k) a.flow[k] = d->flow_segments[k];
+    a.p = s->p;
+    // vein_end.cu:12-17, FP32 like the constexpr thresholds.
+    a.upper = s->maxY - 3 * s->p.grid_y_margin / 4;
+    a.lower = s->minY + s->p.grid_y_margin / 2;
+    a.right = s->maxX - s->p.grid_xz_margin / 2;
+    a.left = s->minX + s->p.grid_xz_margin / 2;
+    a.front = s->maxZ - s->p.grid_xz_margin / 2;
+    a.back = s->minZ + s->p.grid_xz_margin / 2;
+    a.ending_count = vn.ending_count;
+    for (int k = 0; k < vn.ending_count; ++k)
+        a.endings[k] = make_float4(vn.ending_centers[3 * k], vn.ending_centers[3 * k + 1], vn.ending_centers[3 * k + 2],
+                                   vn.ending_radii[k]);
+    a.steps = s->steps;
+    a.err = s->err;
+
+    // ---- static triangle grid from the initial mesh
+    build_triangle_grid(s, true);
+    if ((st = check_last())) return st;
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    return BCS_OK;
+}
+
+void destroy_impl(bcs_sim* s) {
+    drop_graphs(s);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void* p : s->allocations) cudaFree(p);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+}
+
+bool bad_vec(const bcs_vec3& v) { return !v.x || !v.y || !v.z; }
+
+// Copy three SoA arrays (host or device) into a float4 buffer.
+bcs_status set_vec(bcs_sim* s, const bcs_vec3& v, int n, float4* dst, const float* wsrc, bcs_memory where) {
+    if (where == BCS_MEM_DEVICE) {
+        launch_pack(v.x, v.y, v.z, n, dst, wsrc, s->stream);
+        return check_last();
+    }
+    std::vector<float4> h(n);
+    std::vector<float> w;
+    if (wsrc) {
+        w.resize(n);
+        BCS_CUDA(cudaMemcpy(w.data(), wsrc, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    }
+    for (int i = 0; i < n; ++i) h[i] = make_float4(v.x[i], v.y[i], v.z[i], wsrc ? w[i] : 0.f);
+    BCS_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s->stream));
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    return BCS_OK;
+}
+
+bcs_status get_vec(bcs_sim* s, const float4* src, int n, const bcs_vec3& v, bcs_memory where) {
+    if (!v.x && !v.y && !v.z) return BCS_OK;
+    if (where == BCS_MEM_DEVICE) {
+        launch_unpack(src, n, v.x, v.y, v.z, s->stream);
+        return check_last();
+    }
+    std::vector<float4> h(n);
+    BCS_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < n; ++i) {
+        if (v.x) v.x[i] = h[i].x;
+        if (v.y) v.y[i] = h[i].y;
+        if (v.z) v.z[i] = h[i].z;
+    }
+    return BCS_OK;
+}
+
+}  // namespace
+
+// ================================================================ C ABI ====
+extern "C" {
+
+void bcs_default_params(bcs_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    // src/config/simulation.hpp:3-21
+    p->dt = 0.008f;
+    p->use_blood_flow = 1;
+    p->enable_reaction_force = 1;
+    p->enable_big_cells_brake = 1;
+    p->cell_width = p->cell_height = p->cell_depth = 2.0f;
+    p->cell_width_triangles = p->cell_height_triangles = p->cell_depth_triangles = 25.0f;
+    p->bounding_spheres_coeff = 3.0f;
+    p->grid_y_margin = 40.0f;
+    p->grid_xz_margin = 40.0f;
+    p->min_spawn_y = -20.0f;
+    // src/config/physics.hpp:4-34
+    p->velocity_collision_damping = 0.96f;
+    p->particle_k_sniff = 25.0f;
+    p->vein_k_sniff = 0.1f;
+    p->particle_d_fact = 10.0f;
+    p->vein_d_fact = 0.7f;
+    p->vein_collision_force_intensity = 0.005f;
+    p->viscous_damping = 0.39f;
+    p->collision_spring_coeff = 6.0f;
+    p->collision_damping_coeff = 6.0f;
+    p->collision_shear_coeff = 4.0f;
+    p->max_cell_size_factor_before_brake = 1.5f;
+    p->big_particle_braking_intensity = 0.8f;
+    p->init_velocity[0] = 0.0f; p->init_velocity[1] = -80.0f; p->init_velocity[2] = 0.0f;
+    p->vein_impact_distance = 6.0f;
+    p->vein_impact_minimal_force_distance = 0.001f;
+    p->gravity[0] = 0.0f; p->gravity[1] = -25.0f; p->gravity[2] = 0.0f;
+    // src/meta_factory/vein_factory.hpp:88
+    p->cylinder_radius = 50.0f;
+    p->particle_grid = BCS_GRID_UNIFORM;
+    p->triangle_grid = BCS_GRID_UNIFORM;   // UNIFORM_TRIANGLES_GRID, main.cu:44
+    p->vein_dynamic = 1;
+    p->refresh_triangle_centers = 0;
+    p->seed = 0;
+}
+
+const char* bcs_status_string(bcs_status s) {
+    switch (s) {
+        case BCS_OK: return "ok";
+        case BCS_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case BCS_ERR_CUDA: return "CUDA runtime error";
+        case BCS_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case BCS_ERR_NO_DEVICE: return "no CUDA device";
+        case BCS_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+int bcs_abi_version(void) { return BCS_ABI_VERSION; }
+
+bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out) {
+    if (!out) return BCS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    bcs_status st = validate(desc);
+    if (st != BCS_OK) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return BCS_ERR_NO_DEVICE;
+    bcs_sim* s = new (std::nothrow) bcs_sim();
+    if (!s) return BCS_ERR_OUT_OF_MEMORY;
+    st = create_impl(desc, stream, s);
+    if (st != BCS_OK) {
+        destroy_impl(s);
+        delete s;
+        return st;
+    }
+    *out = s;
+    return BCS_OK;
+}
+
+bcs_status bcs_destroy(bcs_sim* s) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    destroy_impl(s);
+    delete s;
+    return BCS_OK;
+}
+
+bcs_status bcs_get_info(bcs_sim* s, bcs_info* o) {
+    if (!s || !o) return BCS_ERR_INVALID_ARGUMENT;
+    std::memset(o, 0, sizeof(*o));
+    o->particle_count = s->N;
+    o->blood_cell_count = s->C;
+    o->type_count = (int)s->types.size();
+    o->vertex_count = s->V;
+    o->triangle_count = s->T;
+    o->min_x = s->minX; o->max_x = s->maxX; o->min_y = s->minY; o->max_y = s->maxY; o->min_z = s->minZ; o->max_z = s->maxZ;
+    o->cell_count_x = s->pg.g.cx; o->cell_count_y = s->pg.g.cy; o->cell_count_z = s->pg.g.cz;
+    o->cell_count = s->pg.g.cells;
+    o->tri_cell_count_x = s->tg.g.cx; o->tri_cell_count_y = s->tg.g.cy; o->tri_cell_count_z = s->tg.g.cz;
+    o->tri_cell_count = s->tg.g.cells;
+    o->steps_done = s->host_steps;
+    o->device_bytes = s->bytes;
+    return BCS_OK;
+}
+
+bcs_status bcs_set_particles(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs_vec3 forces, bcs_memory where) {
+    if (!s || bad_vec(positions) || bad_vec(velocities)) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_status st;
+    if ((st = set_vec(s, positions, s->N, s->pos[s->cur], s->radius_of_particle, where))) return st;
+    if ((st = set_vec(s, velocities, s->N, s->vel[s->cur], nullptr, where))) return st;
+    if (forces.x && forces.y && forces.z) {
+        if ((st = set_vec(s, forces, s->N, s->frc[s->cur], nullptr, where))) return st;
+    } else {
+        BCS_CUDA(cudaMemsetAsync(s->frc[s->cur], 0, sizeof(float4) * s->N, s->stream));
+    }
+    s->keys_valid = false;
+    s->mid_frame = false;
+    return BCS_OK;
+}
+
+bcs_status bcs_get_particles(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs_vec3 forces, bcs_memory where) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    const int b = s->mid_frame ? (s->cur ^ 1) : s->cur;
+    bcs_status st;
+    if ((st = get_vec(s, s->pos[b], s->N, positions, where))) return st;
+    if ((st = get_vec(s, s->vel[b], s->N, velocities, where))) return st;
+    return get_vec(s, s->frc[b], s->N, forces, where);
+}
+
+bcs_status bcs_set_vein(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs_memory where) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_status st;
+    if (!bad_vec(positions)) {
+        if ((st = set_vec(s, positions, s->V, s->vpos, nullptr, where))) return st;
+        build_triangle_grid(s, s->p.refresh_triangle_centers != 0);
+    }
+    if (!bad_vec(velocities) && (st = set_vec(s, velocities, s->V, s->vvel, nullptr, where))) return st;
+    return check_last();
+}
+
+bcs_status bcs_get_vein(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs_vec3 forces, bcs_memory where) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_status st;
+    if ((st = get_vec(s, s->vpos, s->V, positions, where))) return st;
+    if ((st = get_vec(s, s->vvel, s->V, velocities, where))) return st;
+    return get_vec(s, s->vfrc, s->V, forces, where);
+}
+
+bcs_status bcs_calculate_grids(bcs_sim* s) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    if (s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    s->keys_valid = false;
+    enqueue_grids(s);
+    return check_last();
+}
+
+bcs_status bcs_calculate_next_frame(bcs_sim* s) {
+    if (!s || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    if (!s->grid_ready) enqueue_grids(s);
+    enqueue_vein_forces(s);
+    refresh_args(s, s->cur, s->cur ^ 1, false);
+    launch_step(s->args, (int)s->work_host.size(), 1, s->stream);
+    s->mid_frame = true;
+    return check_last();
+}
+
+bcs_status bcs_propagate_all(bcs_sim* s) {
+    if (!s || !s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    refresh_args(s, s->cur, s->cur ^ 1, false);
+    launch_propagate(s->args, (int)s->work_host.size(), s->stream);
+    enqueue_vein_propagate(s);
+    s->cur ^= 1;
+    s->mid_frame = false;
+    s->keys_valid = false;
+    s->grid_ready = false;
+    ++s->host_steps;
+    return check_last();
+}
+
+static bcs_status run_steps(bcs_sim* s, int n) {
+    for (int i = 0; i < n; ++i) {
+        if (!s->keys_valid || s->p.refresh_triangle_centers) {
+            enqueue_frame(s);
+            continue;
+        }
+        cudaGraphExec_t& g = s->graph[s->cur];
+        if (!g) {
+            const int cur0 = s->cur;
+            const long long hs = s->host_steps;
+            cudaGraph_t graph = nullptr;
+            BCS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_frame(s);
+            cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
+            s->cur = cur0;
+            s->host_steps = hs;
+            if (ce != cudaSuccess) return BCS_ERR_CUDA;
+            ce = cudaGraphInstantiate(&g, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce != cudaSuccess) { g = nullptr; return BCS_ERR_CUDA; }
+        }
+        BCS_CUDA(cudaGraphLaunch(g, s->stream));
+        // A replay is one whole enqueue_frame: mirror its host-side state
+        // (the sorted-grid pointers it set during capture do not change).
+        s->cur ^= 1;
+        s->keys_valid = true;
+        s->grid_ready = true;
+        ++s->host_steps;
+    }
+    return BCS_OK;
+}
+
+bcs_status bcs_step(bcs_sim* s, int nsteps) {
+    if (!s || nsteps < 0) return BCS_ERR_INVALID_ARGUMENT;
+    if (s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_status st = run_steps(s, nsteps);
+    if (st != BCS_OK) return st;
+    return check_last();
+}
+
+bcs_status bcs_get_grid(bcs_sim* s, int which, int* cell_ids, int* object_ids, int* cell_starts, int* cell_ends,
+                        bcs_memory where) {
+    if (!s || (which != 0 && which != 1)) return BCS_ERR_INVALID_ARGUMENT;
+    DeviceGrid& dg = which ? s->tg : s->pg;
+    if (!dg.g.uniform || !dg.g.keys) return BCS_ERR_INVALID_ARGUMENT;
+    const int n = dg.count;
+    const cudaMemcpyKind kind = where == BCS_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (cell_ids) BCS_CUDA(cudaMemcpyAsync(cell_ids, dg.g.keys, sizeof(int) * n, kind, s->stream));
+    if (object_ids) BCS_CUDA(cudaMemcpyAsync(object_ids, dg.g.ids, sizeof(int) * n, kind, s->stream));
+    if (cell_starts || cell_ends) {
+        int* ds = nullptr;
+        int* de = nullptr;
+        if (where == BCS_MEM_DEVICE) {
+            ds = cell_starts;
+            de = cell_ends;
+        } else {
+            if (cell_starts) BCS_CUDA(cudaMalloc(&ds, sizeof(int) * (size_t)dg.g.cells));
+            if (cell_ends) BCS_CUDA(cudaMalloc(&de, sizeof(int) * (size_t)dg.g.cells));
+        }
+        launch_dense_ranges(dg.table, dg.g.keys, n, dg.g.cells, ds, de, s->stream);
+        if (where == BCS_MEM_HOST) {
+            if (ds) BCS_CUDA(cudaMemcpyAsync(cell_starts, ds, sizeof(int) * (size_t)dg.g.cells, kind, s->stream));
+            if (de) BCS_CUDA(cudaMemcpyAsync(cell_ends, de, sizeof(int) * (size_t)dg.g.cells, kind, s->stream));
+            BCS_CUDA(cudaStreamSynchronize(s->stream));
+            if (ds) cudaFree(ds);
+            if (de) cudaFree(de);
+        }
+    }
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    return check_last();
+}
+
+bcs_status bcs_export_render(bcs_sim* s, float* particle_vbo, float* particle_offsets, float* vein_vbo,
+                             bcs_memory where) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    const int b = s->mid_frame ? (s->cur ^ 1) : s->cur;
+    if (where == BCS_MEM_DEVICE) {
+        launch_export(s->pos[b], s->N, s->vpos, s->V, particle_vbo, particle_offsets, vein_vbo, s->stream);
+        return check_last();
+    }
+    float *dp = nullptr, *doff = nullptr, *dv = nullptr;
+    if (particle_vbo) BCS_CUDA(cudaMalloc(&dp, sizeof(float) * 6 * (size_t)s->N));
+    if (particle_offsets) BCS_CUDA(cudaMalloc(&doff, sizeof(float) * 3 * (size_t)s->N));
+    if (vein_vbo) BCS_CUDA(cudaMalloc(&dv, sizeof(float) * 6 * (size_t)s->V));
+    launch_export(s->pos[b], s->N, s->vpos, s->V, dp, doff, dv, s->stream);
+    if (dp) BCS_CUDA(cudaMemcpyAsync(particle_vbo, dp, sizeof(float) * 6 * (size_t)s->N, cudaMemcpyDeviceToHost, s->stream));
+    if (doff) BCS_CUDA(cudaMemcpyAsync(particle_offsets, doff, sizeof(float) * 3 * (size_t)s->N, cudaMemcpyDeviceToHost, s->stream));
+    if (dv) BCS_CUDA(cudaMemcpyAsync(vein_vbo, dv, sizeof(float) * 6 * (size_t)s->V, cudaMemcpyDeviceToHost, s->stream));
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    if (dp) cudaFree(dp);
+    if (doff) cudaFree(doff);
+    if (dv) cudaFree(dv);
+    return check_last();
+}
+
+bcs_status bcs_get_error_word(bcs_sim* s, uint32_t* out, int clear) {
+    if (!s || !out) return BCS_ERR_INVALID_ARGUMENT;
+    unsigned h = 0;
+    BCS_CUDA(cudaMemcpyAsync(&h, s->err, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    if (clear) BCS_CUDA(cudaMemsetAsync(s->err, 0, sizeof(unsigned), s->stream));
+    *out = h;
+    return BCS_OK;
+}
+
+bcs_status bcs_synchronize(bcs_sim* s) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    return check_last();
+}
+
+bcs_status bcs_time_steps(bcs_sim* s, int nsteps, float* ms_out) {
+    if (!s || !ms_out || nsteps < 0 || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaEventRecord(s->ev0, s->stream));
+    bcs_status st = run_steps(s, nsteps);
+    if (st != BCS_OK) return st;
+    BCS_CUDA(cudaEventRecord(s->ev1, s->stream));
+    BCS_CUDA(cudaEventSynchronize(s->ev1));
+    BCS_CUDA(cudaEventElapsedTime(ms_out, s->ev0, s->ev1));
+    return check_last();
+}
+
+}  // extern "C"

@@ -1,0 +1,187 @@
+// bcs_internal.cuh — device-side data layout and math shared by the kernels.
+//
+// HBM layout (one scene, N particles, V vein vertices, T triangles):
+//   pos[2], vel[2], frc[2]   float4 x N each, ping-pong.  pos.w carries the
+//                            particle's collision radius (constant), so a
+//                            neighbour gather returns position and radius in
+//                            one 16-byte load.
+//   pkeys[2], pids[2]        int32 x N, grid keys / particle ids (radix-sort
+//                            ping-pong); after the sort they are the
+//                            reference's gridCellIds / particleIds.
+//   ptable                   int2 x (grid cells): (first, last) sorted slot of
+//                            every occupied cell.  Never cleared: an entry is
+//                            trusted only when keys[first] == cell, which holds
+//                            exactly for the cells occupied in this step (those
+//                            are rewritten every step), so stale entries of
+//                            emptied cells are rejected without a clear pass.
+//   vpos, vvel, vfrc         float4 x V (vein)
+//   vnb_ids[9], vnb_len[9]   int32 / float x V, the reference's nine
+//                            neighbour-slot arrays (VeinNeighbors)
+//   tkeys, tids, ttable      triangle grid, same representation as particles
+//   tcache                   3 float4 per sorted triangle slot: (v0, id),
+//                            (v1 - v0), (v2 - v0) — the Moller-Trumbore
+//                            operands, streamed contiguously per grid cell.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/bcs.h"
+
+namespace bcs {
+
+constexpr int kMaxTypes = 16;
+constexpr int kMaxFlow = 8;
+constexpr int kStepThreads = 256;
+constexpr int kMaxChunk = 2 * kStepThreads;   // particles per CTA of the step kernel
+constexpr int kMaxCellsPerChunk = 64;
+
+struct TypeDev {
+    int count;            // cells of the type
+    int pic;              // particles per cell
+    int particle_start;   // first particle
+    int cell_start;       // first cell (global cell index)
+    int model_start;      // first model vertex in the per-model tables
+    int adj_start;        // CSR offsets start (model_start + type index)
+};
+
+struct WorkItem {         // one CTA of the step kernel: whole cells of one type
+    int type;
+    int first_cell;       // within the type
+    int ncells;
+};
+
+struct GridDev {
+    int uniform;
+    float lo[3];          // minX, minY, minZ
+    float hi[3];          // maxX, maxY, maxZ
+    float ext[3];         // width, height, depth
+    float cell[3];        // cell width, height, depth
+    int cx, cy, cz;       // cell counts (int(extent / cell))
+    long long cells;
+    const int* keys;      // sorted keys
+    const int* ids;       // sorted object ids
+    const int2* table;    // validated (first, last) per cell
+    int count;            // objects
+};
+
+struct StepArgs {
+    // particle state
+    const float4* __restrict__ pos_in;
+    const float4* __restrict__ vel_in;
+    const float4* __restrict__ frc_in;
+    float4* pos_out;
+    float4* vel_out;
+    float4* frc_out;
+    int* keys_out;        // next-step grid keys (canonical order) or null
+    int* ids_out;
+    int n;
+    // layout
+    const WorkItem* work;
+    TypeDev types[kMaxTypes];
+    int type_count;
+    const int* adj_off;   // [sum(pic)+types] CSR offsets per model vertex
+    const int* adj_nbr;   // neighbour index within the cell
+    const float* adj_len; // rest length
+    const float* r0;      // per model vertex: distance to the model centroid
+    const float4* respawn;// per model vertex: (m_i - m_0), for respawns
+    // grids
+    GridDev pg, tg;
+    // vein
+    const float4* vpos;
+    float4* vfrc;
+    const uint32_t* tri;  // 3 * T vertex indices
+    const float4* tcache; // 3 per sorted triangle slot
+    int T;
+    // flow
+    bcs_flow_segment flow[kMaxFlow];
+    int flow_count;
+    // constants
+    bcs_params p;
+    float upper, lower, right, left, front, back;   // vein-end thresholds
+    int ending_count;
+    float4 endings[8];    // (cx, cy, cz, r)
+    const long long* steps;  // device step counter
+    unsigned* err;        // device error word
+};
+
+// ------------------------------------------------------------- float3 ----
+__host__ __device__ inline float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__host__ __device__ inline float3 xyz(float4 a) { return make_float3(a.x, a.y, a.z); }
+__host__ __device__ inline float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ inline float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ inline float3 operator*(float s, float3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__host__ __device__ inline float3 operator/(float3 a, float s) { return f3(a.x / s, a.y / s, a.z / s); }
+__host__ __device__ inline float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ inline float3 cross3(float3 u, float3 v) {
+    return f3(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
+}
+__host__ __device__ inline float len3(float3 v) { return sqrtf(dot3(v, v)); }
+
+// v / |v|, or the zero vector (and a flag) when that is NaN — the rule of
+// the reference's normalize (src/utilities/math.cuh:95-104).
+__device__ inline float3 normalize_or_zero(float3 v, unsigned& e) {
+    float s = sqrtf(dot3(v, v));
+    float3 n = f3(v.x / s, v.y / s, v.z / s);
+    if (isnan(n.x) || isnan(n.y) || isnan(n.z)) {
+        e |= BCS_ERRW_NAN_NORMALIZE;
+        return f3(0.f, 0.f, 0.f);
+    }
+    return n;
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+__host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+}
+// Odd multiples of 2^-24 in (0, 1): exact in float.
+__host__ __device__ inline float uniform_open(uint32_t r) {
+    return (float)((r >> 9) * 2u + 1u) * (1.0f / 16777216.0f);
+}
+
+// Grid key of a position, FP32 arithmetic identical to calculateIdForCell
+// (src/grids/uniform_grid.cu:24-36): per axis int(min(extent, max(0,
+// (p - min) / cell))), then clamped to the last cell (the reference's extent
+// clamp can step past it).  Out-of-box positions raise BCS_ERRW_OUT_OF_GRID.
+__device__ inline int axis_index(float p, float lo, float ext, float cell, int count) {
+    float t = __fdiv_rn(p - lo, cell);
+    float m = 0.0f > t ? 0.0f : t;
+    float c = ext > m ? m : ext;
+    int i = (int)c;
+    i = i > count - 1 ? count - 1 : i;
+    return i < 0 ? 0 : i;
+}
+
+__device__ inline int grid_key(const GridDev& g, float3 q, unsigned& e) {
+    if (q.x < g.lo[0] || q.x > g.hi[0] || q.y < g.lo[1] || q.y > g.hi[1] || q.z < g.lo[2] || q.z > g.hi[2])
+        e |= BCS_ERRW_OUT_OF_GRID;
+    int ix = axis_index(q.x, g.lo[0], g.ext[0], g.cell[0], g.cx);
+    int iy = axis_index(q.y, g.lo[1], g.ext[1], g.cell[1], g.cy);
+    int iz = axis_index(q.z, g.lo[2], g.ext[2], g.cell[2], g.cz);
+    return iz * g.cx * g.cy + iy * g.cx + ix;
+}
+
+// Validated lookup of an occupied cell's (first, last) sorted slot.
+__device__ inline bool cell_range(const GridDev& g, long long c, int& first, int& last) {
+    if (c < 0 || c >= g.cells) return false;
+    int2 r = __ldg(&g.table[c]);
+    if (r.x < 0 || r.x >= g.count || __ldg(&g.keys[r.x]) != (int)c) return false;
+    first = r.x;
+    last = r.y;
+    return true;
+}
+
+__device__ inline void flag_error(unsigned* err, unsigned e) {
+    unsigned any = __reduce_or_sync(__activemask(), e);
+    if (any && (threadIdx.x & 31) == (__ffs(__activemask()) - 1)) atomicOr(err, any);
+}
+
+}  // namespace bcs

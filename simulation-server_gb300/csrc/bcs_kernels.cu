@@ -1,0 +1,603 @@
+// bcs_kernels.cu — the per-step kernels for sm_103a.
+//
+// One frame of the reference (src/main.cu:175-208) becomes, per step:
+//   radix sort of the grid keys (bcs_sort.cu) → k_cell_ranges →
+//   k_vein_springs → k_step<kFull> → k_vein_integrate → k_tri_cache → k_bump_step
+// k_step is cell-major: a CTA owns whole blood cells of one type, stages
+// their positions / velocities / previous forces in shared memory, and does
+// for each particle the work of calculateBloodCellsCenters, gatherForcesKernel,
+// calculateParticleCollisions, detectVeinCollisions, propagateParticleForcesKernel
+// and handleVeinEndsBlockSync, then writes the next step's grid keys.  Each
+// particle's x, v, F cross HBM once per step in each direction.
+#include "bcs_internal.cuh"
+
+namespace bcs {
+
+// ------------------------------------------------------------ physics ----
+// springMassForceWithDampingForParticle + calculateParticlesSpringForceComponent
+// (src/simulation/physics.cuh:24-27,53-77, Heun branch).
+__device__ inline float3 cell_spring(const bcs_params& p, float3 dP, float3 dv, float3 f1, float3 f2, float L,
+                                     unsigned& e) {
+    float3 nshift = normalize_or_zero(-1.0f * dP, e);
+    float3 dvv = dv + p.dt * (f1 - f2);
+    float mag = (len3(dP) - L) * p.particle_k_sniff + dot3(normalize_or_zero(dP, e), dvv) * p.particle_d_fact;
+    return mag * nshift;
+}
+
+// accumulateEnvironmentForcesForParticles (physics.cuh:102-120); the
+// constant G is replaced by the nearest segment's Poiseuille profile when
+// flow segments are given.
+__device__ inline float3 environment(const StepArgs& a, float3 x, float3 v, float ratio) {
+    const bcs_params& p = a.p;
+    float3 g = f3(p.gravity[0], p.gravity[1], p.gravity[2]);
+    if (a.flow_count > 0) {
+        float best = 3.0e38f;
+        for (int k = 0; k < a.flow_count; ++k) {
+            const bcs_flow_segment& s = a.flow[k];
+            float3 o = f3(s.origin[0], s.origin[1], s.origin[2]);
+            float3 d = f3(s.direction[0], s.direction[1], s.direction[2]);
+            float t = dot3(x - o, d);
+            float tc = fminf(fmaxf(t, 0.f), s.length);
+            float3 c = o + tc * d;
+            float dist2 = dot3(x - c, x - c);
+            if (dist2 < best) {
+                best = dist2;
+                float3 radial = (x - o) - t * d;
+                float prof = 1.f - dot3(radial, radial) / (s.radius * s.radius);
+                g = (s.peak_force * fmaxf(prof, 0.f)) * d;
+            }
+        }
+    }
+    if (p.enable_big_cells_brake && ratio > p.max_cell_size_factor_before_brake)
+        return g - p.viscous_damping * ratio * p.big_particle_braking_intensity * v;
+    return g - p.viscous_damping * v;
+}
+
+// addResilientForceOnCollision (physics.cuh:133-145) times `intensity`.
+__device__ inline float3 resilient(const bcs_params& p, float3 rp, float3 rv, float d2, float radius, float intensity,
+                                   unsigned& e) {
+    float3 dir = normalize_or_zero(rp, e);
+    float3 tang = rv - dot3(rv, dir) * dir;
+    float3 spring = (-p.collision_spring_coeff * (radius * 2 - sqrtf(d2))) * dir;
+    float3 damp = p.collision_damping_coeff * rv;
+    float3 shear = p.collision_shear_coeff * tang;
+    return intensity * (spring + damp + shear);
+}
+
+// Moller-Trumbore of realCollisionDetection (src/simulation/vein_collisions.cu:11-45)
+// on precomputed edges e1 = v1 - v0, e2 = v2 - v0 (same FP32 values).
+__device__ inline bool ray_triangle(float3 o, float3 d, float3 v0, float3 e1, float3 e2, float& t, float3& n,
+                                    float3& refl, unsigned& e) {
+    const float EPS = 0.000001f;
+    float3 h = cross3(d, e2);
+    float aa = dot3(e1, h);
+    if (aa > -EPS && aa < EPS) return false;
+    float f = 1.0f / aa;
+    float3 s = o - v0;
+    float u = f * dot3(s, h);
+    if (u < 0.f || u > 1.f) return false;
+    float3 q = cross3(s, e1);
+    float v = f * dot3(d, q);
+    if (v < 0.f || u + v > 1.f) return false;
+    float tt = f * dot3(e2, q);
+    if (tt > EPS) {
+        t = tt;
+        n = normalize_or_zero(cross3(e2, e1), e);
+        refl = d - (2.0f * dot3(d, n)) * n;
+        return true;
+    }
+    return false;
+}
+
+// calculateBaricentric (vein_collisions.cu:47-61), e1 = v2 - v1 as there.
+__device__ inline float3 barycentric(float3 pt, float3 v0, float3 v1, float3 v2) {
+    float3 e0 = v1 - v0, e1 = v2 - v1, e2 = pt - v0;
+    float d00 = dot3(e0, e0), d01 = dot3(e0, e1), d11 = dot3(e1, e1), d20 = dot3(e2, e0), d21 = dot3(e2, e1);
+    float den = d00 * d11 - d01 * d01;
+    float bx = (d11 * d20 - d01 * d21) / den;
+    float by = (d00 * d21 - d01 * d20) / den;
+    return f3(bx, by, 1.0f - bx - by);
+}
+
+__device__ inline void stencil_range(int id, int count, int& lo, int& hi) {
+    lo = -1; hi = 1;
+    if (id < 1) lo = 0;
+    else if (id > count - 2) hi = 0;
+}
+
+__device__ inline void stencil_range_u(unsigned id, int count, int& lo, int& hi) {
+    lo = -1; hi = 1;
+    if (id < 1u) lo = 0;
+    else if (id > (unsigned)(count - 2)) hi = 0;
+}
+
+// Saturating float -> unsigned, the value cvt.rzi.u32.f32 gives for the
+// reference's static_cast<unsigned int> of the cell coordinate.
+__device__ inline unsigned to_u32_sat(float t) { return t <= 0.f ? 0u : (t >= 4294967040.f ? 0xFFFFFFFFu : (unsigned)t); }
+
+// calculateParticleCollisions<UniformGrid> (particle_collisions.cuh:26-38,
+// 53-83,104-269) for one particle; the 3 cells of a stencil row are
+// consecutive keys, so each row is one contiguous range of sorted slots.
+__device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 x, float3 v, float R, unsigned& e) {
+    float3 acc = f3(0.f, 0.f, 0.f);
+    const GridDev& g = a.pg;
+    auto test = [&](int q) {
+        float4 pq = __ldg(&a.pos_in[q]);
+        float3 rp = x - xyz(pq);
+        float d2 = dot3(rp, rp);
+        float md = R + pq.w;
+        if (d2 <= md * md && d2 >= 0.0001f) {
+            float3 rv = v - xyz(__ldg(&a.vel_in[q]));
+            acc = acc + resilient(a.p, rp, rv, d2, R, 0.5f, e);
+        }
+    };
+    if (!g.uniform) {
+        for (int q = 0; q < a.n; ++q)
+            if (q != pid) test(q);
+        return acc;
+    }
+    unsigned dummy = 0;
+    const int cellId = grid_key(g, x, dummy);
+    const int xId = (int)__fdiv_rn(x.x - g.lo[0], g.cell[0]);
+    const int yId = (int)__fdiv_rn(x.y - g.lo[1], g.cell[1]);
+    const int zId = (int)__fdiv_rn(x.z - g.lo[2], g.cell[2]);
+    int x0, x1, y0, y1, z0, z1;
+    stencil_range(xId, g.cx, x0, x1);
+    stencil_range(yId, g.cy, y0, y1);
+    stencil_range(zId, g.cz, z0, z1);
+    const long long cxy = (long long)g.cx * g.cy;
+    for (int dz = z0; dz <= z1; ++dz)
+        for (int dy = y0; dy <= y1; ++dy) {
+            const long long row = (long long)cellId + dz * cxy + (long long)dy * g.cx;
+            int first = -1, last = -2, f, l;
+            for (int dx = x0; dx <= x1; ++dx)
+                if (cell_range(g, row + dx, f, l)) {
+                    if (first < 0) first = f;
+                    last = l;
+                }
+            for (int j = first; j <= last; ++j) {
+                int q = __ldg(&g.ids[j]);
+                if (q != pid) test(q);
+            }
+        }
+    return acc;
+}
+
+// detectVeinCollisions<UniformGrid> (vein_collisions.cu:198-277,
+// vein_collisions.cuh:60-93) for one particle: the first triangle hit in
+// stencil order (x, then y, then z; sorted order inside a cell).
+__device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, float3& F, float R, unsigned& e) {
+    const bcs_params& p = a.p;
+    const float3 vel = v;
+    const float3 dir = normalize_or_zero(vel, e);
+    float t = 1e10f;
+    float3 n = f3(0.f, 0.f, 0.f), refl = f3(0.f, 0.f, 0.f);
+    int obj = -1;
+    const GridDev& g = a.tg;
+    auto test_slot = [&](int s) -> bool {
+        float4 c0 = __ldg(&a.tcache[3 * s]);
+        float4 c1 = __ldg(&a.tcache[3 * s + 1]);
+        float4 c2 = __ldg(&a.tcache[3 * s + 2]);
+        if (ray_triangle(x, dir, xyz(c0), xyz(c1), xyz(c2), t, n, refl, e)) {
+            obj = __float_as_int(c0.w);
+            return true;
+        }
+        return false;
+    };
+    if (!g.uniform) {
+        for (int s = 0; s < a.T; ++s)
+            if (test_slot(s)) break;
+    } else {
+        unsigned dummy = 0;
+        const unsigned cellId = (unsigned)grid_key(g, x, dummy);
+        const unsigned xId = to_u32_sat(__fdiv_rn(x.x - g.lo[0], g.cell[0]));
+        const unsigned yId = to_u32_sat(__fdiv_rn(x.y - g.lo[1], g.cell[1]));
+        const unsigned zId = to_u32_sat(__fdiv_rn(x.z - g.lo[2], g.cell[2]));
+        int x0, x1, y0, y1, z0, z1;
+        stencil_range_u(xId, g.cx, x0, x1);
+        stencil_range_u(yId, g.cy, y0, y1);
+        stencil_range_u(zId, g.cz, z0, z1);
+        const long long cxy = (long long)g.cx * g.cy;
+        bool found = false;
+        for (int dx = x0; dx <= x1 && !found; ++dx)
+            for (int dy = y0; dy <= y1 && !found; ++dy)
+                for (int dz = z0; dz <= z1 && !found; ++dz) {
+                    int f, l;
+                    if (!cell_range(g, (long long)cellId + dz * cxy + (long long)dy * g.cx + dx, f, l)) continue;
+                    for (int s = f; s <= l; ++s)
+                        if (test_slot(s)) { found = true; break; }
+                }
+    }
+    if (obj < 0) return;
+    float3 rel = x - (x + t * dir);
+    float d2 = dot3(rel, rel);
+    if (d2 > p.vein_impact_distance * p.vein_impact_distance) return;
+    if (d2 > p.vein_impact_minimal_force_distance * p.vein_impact_minimal_force_distance) {
+        if (p.enable_reaction_force) {
+            float3 resp = (-1.0f * dot3(F, n)) * n / dot3(n, n);
+            F = F + resp;
+        } else {
+            F = F + resilient(p, rel, vel, d2, R, 0.5f, e);
+        }
+    }
+    float speed = len3(vel);
+    float3 dv = (p.velocity_collision_damping * speed) * refl - vel;
+    v = v + dv;
+    if (p.vein_dynamic) {
+        float3 ds = p.vein_collision_force_intensity * vel;
+        uint32_t i0 = a.tri[3 * obj], i1 = a.tri[3 * obj + 1], i2 = a.tri[3 * obj + 2];
+        float3 b = barycentric(x + t * dir, xyz(a.vpos[i0]), xyz(a.vpos[i1]), xyz(a.vpos[i2]));
+        float3 d0 = b.x * ds, d1 = b.y * ds, d2v = b.z * ds;
+        atomicAdd(&a.vfrc[i0].x, d0.x); atomicAdd(&a.vfrc[i0].y, d0.y); atomicAdd(&a.vfrc[i0].z, d0.z);
+        atomicAdd(&a.vfrc[i1].x, d1.x); atomicAdd(&a.vfrc[i1].y, d1.y); atomicAdd(&a.vfrc[i1].z, d1.z);
+        atomicAdd(&a.vfrc[i2].x, d2v.x); atomicAdd(&a.vfrc[i2].y, d2v.y); atomicAdd(&a.vfrc[i2].z, d2v.z);
+    }
+}
+
+// Vein-end rule of handleVeinEndsBlockSync (src/simulation/vein_end.cu:12-18,73-87).
+__device__ inline bool leaves_vein(const StepArgs& a, float3 q) {
+    bool tp = false;
+    for (int k = 0; k < a.ending_count; ++k) {
+        float4 c = a.endings[k];
+        float3 d = f3(q.x - c.x, q.y - c.y, q.z - c.z);
+        tp = tp || dot3(d, d) <= c.w * c.w;
+    }
+    return tp || q.y <= a.lower || q.y >= a.upper || q.x <= a.left || q.x >= a.right || q.z <= a.back ||
+           q.z >= a.front;
+}
+
+// Respawn of a whole cell at the inflow (vein_end.cu:101-107): one Philox
+// draw per (seed, cell, step) gives the cell's x and z offsets.
+__device__ inline void respawn(const StepArgs& a, int cell_global, long long step, int model_vertex, float3& x,
+                               float3& v) {
+    uint32_t c[4] = {(uint32_t)cell_global, (uint32_t)step, (uint32_t)((unsigned long long)step >> 32), 0u};
+    philox4x32_10(c, (uint32_t)a.p.seed, (uint32_t)(a.p.seed >> 32));
+    float ux = uniform_open(c[0]), uz = uniform_open(c[1]);
+    float4 off = __ldg(&a.respawn[model_vertex]);
+    x = f3((ux - 0.5f) * 1.2f * a.p.cylinder_radius + off.x, a.p.min_spawn_y + off.y,
+           (uz - 0.5f) * 1.2f * a.p.cylinder_radius + off.z);
+    v = f3(a.p.init_velocity[0], a.p.init_velocity[1], a.p.init_velocity[2]);
+}
+
+// ------------------------------------------------------------- k_step ----
+constexpr int kFull = 0;    // whole frame: forces, integration, vein end, next keys
+constexpr int kForces = 1;  // calculateNextFrame only: forces and collision velocities
+
+template <int MODE>
+__global__ void __launch_bounds__(kStepThreads, 2) k_step(const StepArgs a) {
+    __shared__ float4 s_pos[kMaxChunk];
+    __shared__ float4 s_vel[kMaxChunk];
+    __shared__ float4 s_frc[kMaxChunk];
+    __shared__ float3 s_cent[kMaxCellsPerChunk];
+    __shared__ int s_tp[kMaxCellsPerChunk];
+
+    const WorkItem w = a.work[blockIdx.x];
+    const TypeDev ty = a.types[w.type];
+    const int pic = ty.pic;
+    const int p0 = ty.particle_start + w.first_cell * pic;
+    const int np = w.ncells * pic;
+    for (int i = threadIdx.x; i < np; i += kStepThreads) {
+        s_pos[i] = a.pos_in[p0 + i];
+        s_vel[i] = a.vel_in[p0 + i];
+        s_frc[i] = a.frc_in[p0 + i];
+    }
+    if (threadIdx.x < w.ncells) s_tp[threadIdx.x] = 0;
+    __syncthreads();
+
+    // Cell centroids (blood_cells.cu:44-61), one warp per cell, fixed-order
+    // butterfly reduction (deterministic).
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = warp; c < w.ncells; c += kStepThreads / 32) {
+        float3 acc = f3(0.f, 0.f, 0.f);
+        for (int k = lane; k < pic; k += 32) acc = acc + xyz(s_pos[c * pic + k]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+            acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+        }
+        if (lane == 0) s_cent[c] = acc / (float)pic;
+    }
+    __syncthreads();
+
+    unsigned e = 0;
+    const long long step = *a.steps;
+    float3 nx[2], nv[2], nf[2];
+    float rad[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int i = threadIdx.x + r * kStepThreads;
+        if (i >= np) continue;
+        const int c = i / pic, li = i - c * pic, pid = p0 + i;
+        const float4 px = s_pos[i];
+        const float3 x = xyz(px), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
+        rad[r] = px.w;
+        // Intra-cell springs, gatherForcesKernel (blood_cells.cu:66-120) over
+        // the CSR form of the dense spring graph (same ascending order).
+        float3 F = f3(0.f, 0.f, 0.f);
+        const int e0 = __ldg(&a.adj_off[ty.adj_start + li]), e1 = __ldg(&a.adj_off[ty.adj_start + li + 1]);
+        const int cb = c * pic;
+        for (int k = e0; k < e1; ++k) {
+            const int j = cb + __ldg(&a.adj_nbr[k]);
+            F = F + cell_spring(a.p, x - xyz(s_pos[j]), v - xyz(s_vel[j]), fprev, xyz(s_frc[j]), __ldg(&a.adj_len[k]), e);
+        }
+        const float ratio = len3(x - s_cent[c]) / __ldg(&a.r0[ty.model_start + li]);
+        F = F + environment(a, x, v, ratio);
+        F = (fprev + F) / 2.0f;
+        // Particle-particle collisions.
+        F = F + particle_collisions(a, pid, x, v, px.w, e);
+        // Particle-vein collision.
+        float3 vv = v;
+        vein_collision(a, x, vv, F, px.w, e);
+        if (MODE == kFull) {
+            // propagateParticleForcesKernel (blood_cells.cu:155-179), Heun.
+            const float3 v1 = vv + a.p.dt * F;
+            nx[r] = x + (0.5f * a.p.dt) * (v1 + vv);
+            nv[r] = v1;
+        } else {
+            nx[r] = x;
+            nv[r] = vv;
+        }
+        nf[r] = F;
+    }
+    if (MODE == kFull && a.p.use_blood_flow) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int i = threadIdx.x + r * kStepThreads;
+            if (i < np && leaves_vein(a, nx[r])) atomicOr(&s_tp[i / pic], 1);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int i = threadIdx.x + r * kStepThreads;
+            if (i < np) {
+                const int c = i / pic;
+                if (s_tp[c]) respawn(a, ty.cell_start + w.first_cell + c, step, ty.model_start + (i - c * pic), nx[r], nv[r]);
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int i = threadIdx.x + r * kStepThreads;
+        if (i >= np) continue;
+        const int pid = p0 + i;
+        if (!(isfinite(nx[r].x) && isfinite(nx[r].y) && isfinite(nx[r].z) && isfinite(nv[r].x) &&
+              isfinite(nv[r].y) && isfinite(nv[r].z)))
+            e |= BCS_ERRW_NONFINITE;
+        a.pos_out[pid] = make_float4(nx[r].x, nx[r].y, nx[r].z, rad[r]);
+        a.vel_out[pid] = make_float4(nv[r].x, nv[r].y, nv[r].z, 0.f);
+        a.frc_out[pid] = make_float4(nf[r].x, nf[r].y, nf[r].z, 0.f);
+        if (MODE == kFull && a.keys_out) {
+            a.keys_out[pid] = a.pg.uniform ? grid_key(a.pg, nx[r], e) : 0;
+            a.ids_out[pid] = pid;
+        }
+    }
+    if (e) atomicOr(a.err, e);
+}
+
+// propagateAll for the split-phase API: integrate (blood_cells.cu:155-179)
+// and the vein-end rule, in place on the buffers k_step<kForces> wrote.
+__global__ void __launch_bounds__(kStepThreads) k_propagate(const StepArgs a) {
+    __shared__ int s_tp[kMaxCellsPerChunk];
+    const WorkItem w = a.work[blockIdx.x];
+    const TypeDev ty = a.types[w.type];
+    const int pic = ty.pic;
+    const int p0 = ty.particle_start + w.first_cell * pic;
+    const int np = w.ncells * pic;
+    if (threadIdx.x < w.ncells) s_tp[threadIdx.x] = 0;
+    __syncthreads();
+    const long long step = *a.steps;
+    unsigned e = 0;
+    float3 nx[2], nv[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int i = threadIdx.x + r * kStepThreads;
+        if (i >= np) continue;
+        const float3 x = xyz(a.pos_out[p0 + i]), v0 = xyz(a.vel_out[p0 + i]), F = xyz(a.frc_out[p0 + i]);
+        const float3 v1 = v0 + a.p.dt * F;
+        nx[r] = x + (0.5f * a.p.dt) * (v1 + v0);
+        nv[r] = v1;
+        if (a.p.use_blood_flow && leaves_vein(a, nx[r])) atomicOr(&s_tp[i / pic], 1);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int i = threadIdx.x + r * kStepThreads;
+        if (i >= np) continue;
+        const int c = i / pic;
+        if (a.p.use_blood_flow && s_tp[c])
+            respawn(a, ty.cell_start + w.first_cell + c, step, ty.model_start + (i - c * pic), nx[r], nv[r]);
+        if (!(isfinite(nx[r].x) && isfinite(nx[r].y) && isfinite(nx[r].z))) e |= BCS_ERRW_NONFINITE;
+        const float wv = a.pos_out[p0 + i].w;
+        a.pos_out[p0 + i] = make_float4(nx[r].x, nx[r].y, nx[r].z, wv);
+        a.vel_out[p0 + i] = make_float4(nv[r].x, nv[r].y, nv[r].z, 0.f);
+    }
+    if (e) atomicOr(a.err, e);
+}
+
+// calculateCellIdKernel (src/grids/uniform_grid.cu:38-49).
+__global__ void k_keys(const float4* __restrict__ pos, int n, GridDev g, int* keys, int* ids, unsigned* err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned e = 0;
+    keys[i] = g.uniform ? grid_key(g, xyz(pos[i]), e) : 0;
+    ids[i] = i;
+    if (e) atomicOr(err, e);
+}
+
+// calculateCentersKernel (src/objects/vein_triangles.cu:14-27) fused with
+// the triangle grid's key kernel.
+__global__ void k_tri_keys(const float4* __restrict__ vpos, const uint32_t* __restrict__ tri, int T, GridDev g,
+                           int* keys, int* ids) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    float3 a = xyz(vpos[tri[3 * t]]), b = xyz(vpos[tri[3 * t + 1]]), c = xyz(vpos[tri[3 * t + 2]]);
+    float3 ctr = f3(__fdiv_rn(__fadd_rn(__fadd_rn(a.x, b.x), c.x), 3.0f),
+                    __fdiv_rn(__fadd_rn(__fadd_rn(a.y, b.y), c.y), 3.0f),
+                    __fdiv_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), 3.0f));
+    unsigned e = 0;
+    keys[t] = grid_key(g, ctr, e);
+    ids[t] = t;
+}
+
+// calculateStartAndEndOfCellKernel (uniform_grid.cu:51-80), written into
+// the validated table: (first, last) of every occupied cell.
+__global__ void k_cell_ranges(const int* __restrict__ keys, int n, int2* table) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int k = keys[i];
+    if (i == 0 || keys[i - 1] != k) table[k].x = i;
+    if (i == n - 1 || keys[i + 1] != k) table[k].y = i;
+}
+
+// Dense starts/ends (empty = 0, -1) from the validated table, for getters.
+__global__ void k_dense_ranges(const int2* __restrict__ table, const int* __restrict__ keys, int count,
+                               long long cells, int* starts, int* ends) {
+    long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    int2 r = table[c];
+    bool occ = r.x >= 0 && r.x < count && keys[r.x] == (int)c;
+    if (starts) starts[c] = occ ? r.x : 0;
+    if (ends) ends[c] = occ ? r.y : -1;
+}
+
+// Vein springs, gatherForcesKernel (vein_triangles.cu:125-154), nine
+// neighbour slots per vertex (VeinNeighbors).
+__global__ void k_vein_springs(const float4* __restrict__ vpos, const float4* __restrict__ vvel, float4* vfrc,
+                               const int* __restrict__ nb_ids, const float* __restrict__ nb_len, int V, float k_sniff,
+                               float d_fact, unsigned* err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    unsigned e = 0;
+    const float3 pi = xyz(vpos[i]), vi = xyz(vvel[i]);
+    float3 acc = f3(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        int j = nb_ids[(size_t)k * V + i];
+        if (j == -1) continue;
+        float L = nb_len[(size_t)k * V + i];
+        float3 pj = xyz(vpos[j]);
+        float mag = (len3(pi - pj) - L) * k_sniff + dot3(normalize_or_zero(pi - pj, e), vi - xyz(vvel[j])) * d_fact;
+        acc = acc + mag * normalize_or_zero(pj - pi, e);
+    }
+    float4 f = vfrc[i];
+    vfrc[i] = make_float4(f.x + acc.x, f.y + acc.y, f.z + acc.z, 0.f);
+    if (e) atomicOr(err, e);
+}
+
+// propagateForcesIntoPositionsKernel + the three force memsets
+// (vein_triangles.cu:88-117): semi-implicit Euler, then F = 0.
+__global__ void k_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    float3 f = xyz(vfrc[i]);
+    float3 v = xyz(vvel[i]) + dt * f;
+    float3 x = xyz(vpos[i]) + dt * v;
+    vvel[i] = make_float4(v.x, v.y, v.z, 0.f);
+    vpos[i] = make_float4(x.x, x.y, x.z, 0.f);
+    vfrc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Moller-Trumbore operands per sorted triangle slot (ids == null: identity).
+__global__ void k_tri_cache(const int* __restrict__ ids, const uint32_t* __restrict__ tri,
+                            const float4* __restrict__ vpos, int T, float4* cache) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= T) return;
+    int t = ids ? ids[s] : s;
+    float3 v0 = xyz(vpos[tri[3 * t]]), v1 = xyz(vpos[tri[3 * t + 1]]), v2 = xyz(vpos[tri[3 * t + 2]]);
+    float3 e1 = v1 - v0, e2 = v2 - v0;
+    cache[3 * s] = make_float4(v0.x, v0.y, v0.z, __int_as_float(t));
+    cache[3 * s + 1] = make_float4(e1.x, e1.y, e1.z, 0.f);
+    cache[3 * s + 2] = make_float4(e2.x, e2.y, e2.z, 0.f);
+}
+
+__global__ void k_bump_step(long long* steps) { *steps += 1; }
+
+// Headless stand-in for calculatePositionsKernel / calculateTriangleVerticesKernel
+// (src/graphics/glcontroller.cu:22-49).
+__global__ void k_export(const float4* __restrict__ pos, int n, const float4* __restrict__ vpos, int V, float* pvbo,
+                         float* poff, float* vvbo) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float4 q = pos[i];
+        if (pvbo) {
+            pvbo[6 * i] = q.x; pvbo[6 * i + 1] = q.y; pvbo[6 * i + 2] = q.z;
+            pvbo[6 * i + 3] = 0.f; pvbo[6 * i + 4] = 0.f; pvbo[6 * i + 5] = 0.f;
+        }
+        if (poff) { poff[3 * i] = q.x; poff[3 * i + 1] = q.y; poff[3 * i + 2] = q.z; }
+    }
+    if (i < V && vvbo) {
+        float4 q = vpos[i];
+        vvbo[6 * i] = q.x; vvbo[6 * i + 1] = q.y; vvbo[6 * i + 2] = q.z;
+        vvbo[6 * i + 3] = 0.f; vvbo[6 * i + 4] = 0.f; vvbo[6 * i + 5] = 0.f;
+    }
+}
+
+// SoA (cudaVec3) <-> float4 packing for the state getters and setters.
+__global__ void k_pack(const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ z, int n,
+                       float4* out, const float* __restrict__ wsrc) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = make_float4(x ? x[i] : 0.f, y ? y[i] : 0.f, z ? z[i] : 0.f, wsrc ? wsrc[i] : 0.f);
+}
+
+__global__ void k_unpack(const float4* __restrict__ in, int n, float* x, float* y, float* z) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 q = in[i];
+    if (x) x[i] = q.x;
+    if (y) y[i] = q.y;
+    if (z) z[i] = q.z;
+}
+
+
+// ------------------------------------------------------------ launches ---
+#define BCS_GRID1(n, b) dim3((unsigned)(((n) + (b) - 1) / (b))), dim3(b)
+
+void launch_step(const StepArgs& a, int blocks, int mode, cudaStream_t s) {
+    if (blocks <= 0) return;
+    if (mode == kFull) k_step<kFull><<<blocks, kStepThreads, 0, s>>>(a);
+    else k_step<kForces><<<blocks, kStepThreads, 0, s>>>(a);
+}
+void launch_propagate(const StepArgs& a, int blocks, cudaStream_t s) {
+    if (blocks > 0) k_propagate<<<blocks, kStepThreads, 0, s>>>(a);
+}
+void launch_keys(const float4* pos, int n, const GridDev& g, int* keys, int* ids, unsigned* err, cudaStream_t s) {
+    if (n > 0) k_keys<<<BCS_GRID1(n, 256), 0, s>>>(pos, n, g, keys, ids, err);
+}
+void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const GridDev& g, int* keys, int* ids,
+                     cudaStream_t s) {
+    if (T > 0) k_tri_keys<<<BCS_GRID1(T, 256), 0, s>>>(vpos, tri, T, g, keys, ids);
+}
+void launch_cell_ranges(const int* keys, int n, int2* table, cudaStream_t s) {
+    if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table);
+}
+void launch_dense_ranges(const int2* table, const int* keys, int count, long long cells, int* starts, int* ends,
+                         cudaStream_t s) {
+    if (cells > 0) k_dense_ranges<<<BCS_GRID1(cells, 256), 0, s>>>(table, keys, count, cells, starts, ends);
+}
+void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
+                         int V, float k, float d, unsigned* err, cudaStream_t s) {
+    if (V > 0) k_vein_springs<<<BCS_GRID1(V, 256), 0, s>>>(vpos, vvel, vfrc, nb_ids, nb_len, V, k, d, err);
+}
+void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt, cudaStream_t s) {
+    if (V > 0) k_vein_integrate<<<BCS_GRID1(V, 256), 0, s>>>(vpos, vvel, vfrc, V, dt);
+}
+void launch_tri_cache(const int* ids, const uint32_t* tri, const float4* vpos, int T, float4* cache, cudaStream_t s) {
+    if (T > 0) k_tri_cache<<<BCS_GRID1(T, 256), 0, s>>>(ids, tri, vpos, T, cache);
+}
+void launch_bump_step(long long* steps, cudaStream_t s) { k_bump_step<<<1, 1, 0, s>>>(steps); }
+void launch_export(const float4* pos, int n, const float4* vpos, int V, float* pvbo, float* poff, float* vvbo,
+                   cudaStream_t s) {
+    int m = n > V ? n : V;
+    if (m > 0) k_export<<<BCS_GRID1(m, 256), 0, s>>>(pos, n, vpos, V, pvbo, poff, vvbo);
+}
+void launch_pack(const float* x, const float* y, const float* z, int n, float4* out, const float* wsrc,
+                 cudaStream_t s) {
+    if (n > 0) k_pack<<<BCS_GRID1(n, 256), 0, s>>>(x, y, z, n, out, wsrc);
+}
+void launch_unpack(const float4* in, int n, float* x, float* y, float* z, cudaStream_t s) {
+    if (n > 0) k_unpack<<<BCS_GRID1(n, 256), 0, s>>>(in, n, x, y, z);
+}
+
+}  // namespace bcs

@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Benchmark of the plain blood-cell step on one GB300.
+
+Workload (the metric's 4.2M-particle case): a Y bifurcation (trunk R=40,
+branches R=28), 20 588 icosphere-42 cells (R=3) + 20 588 biconcave-162 cells
+(R=4) = 4 199 952 particles, deformable spring wall, Poiseuille axial force,
+Gaussian initial velocities (sigma 0.01), dt=5e-4, grid cell 1.0, triangle
+cell 6.0.  A step is one whole frame (grid sort, vein springs, the fused
+particle kernel, vein integration) replayed from a CUDA graph.
+
+  value     particle-steps/s over K steps, state resident in HBM, CUDA events
+            on the library's stream (the state, 403 MB of float4 buffers, is
+            larger than the 129 MB L2, so no flush is needed between steps)
+  e2e       the same metric through the C ABI with host buffers: each step is
+            bcs_step(1) + bcs_get_particles of the positions into pinned host
+            memory (the renderer's per-frame read, src/main.cu:183-184); the
+            initial state upload from pinned memory opens the timed region
+  roofline  the fused particle kernel: algorithmic bytes (80 B/particle:
+            x, v, F read + written as 3 x 12 B, + 8 B key/id) / its mean
+            CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline  the FP64 oracle (a C++ restatement of the reference step) on
+            the host cores, on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone (the reference has no
+CPU path of its own and its CUDA build cannot be carried to this machine).
+Under torchrun each rank advances its own replica (the scene does not shard
+without a halo exchange): value = all ranks' particle-steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "simulation-server_gb300"))
+
+METRIC = "particle-steps/s @4.2M particles: plain vs learned-substep at fixed error"
+UNIT = "particle-steps/s"
+CELLS_PER_TYPE = 20588
+ALGO_BYTES_STEP_KERNEL = 80      # per particle, see docstring
+FALLBACK_HBM_GBS = 6800.0
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, gpu_id: str):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", gpu_id], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, mx, reasons = [], [], set()
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(self.NAMES, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_scene(cells_per_type, seed):
+    import bcs_scenes as S
+    return S.bifurcation_scene(cells_per_type=cells_per_type, seed=seed)
+
+
+def workload_config(scene, n_gpus):
+    p = scene.params
+    return {
+        "workload": f"plain step, Y bifurcation, {scene.particle_count} particles "
+                    f"({scene.types[0].count} icosphere-42 + {scene.types[1].count} biconcave-162 cells)",
+        "particles": scene.particle_count,
+        "cells": int(sum(t.count for t in scene.types)),
+        "vein_vertices": int(len(scene.vein_positions)),
+        "triangles": int(len(scene.vein_indices)),
+        "dt": round(float(p.dt), 8),
+        "grid_cell": float(p.cell_width),
+        "triangle_cell": float(p.cell_width_triangles),
+        "l2": "state (6 x float4 x N = 403 MB) exceeds the 129 MB L2; no flush",
+        "parallelism": f"replicas x{n_gpus}",
+    }
+
+
+def sample_scene(scene, fraction):
+    """The first `fraction` of each type's cells: cells are numbered along
+    the flow, so this is the inflow end of the vessel at full density."""
+    import copy
+    sub = copy.copy(scene)
+    types, pos, vel = [], [], []
+    start = 0
+    for t in scene.types:
+        pic = len(t.vertices)
+        keep = max(1, int(round(t.count * fraction)))
+        types.append(copy.copy(t))
+        types[-1].count = keep
+        pos.append(scene.positions[start:start + keep * pic])
+        vel.append(scene.velocities[start:start + keep * pic])
+        start += t.count * pic
+    sub.types = types
+    sub.positions = np.concatenate(pos)
+    sub.velocities = np.concatenate(vel)
+    return sub
+
+
+def time_oracle(scene, steps_budget_s, warmup=1, max_steps=None, threads=None):
+    """FP64 oracle on a bounded sample: returns (particle-steps/s, info)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    threads = threads or os.cpu_count() or 1
+    # calibrate on 1/32 of the scene, then size the sample to the budget
+    cal = sample_scene(scene, 1 / 32)
+    oc = O.OracleSim(cal, threads=threads)
+    oc.step(1)
+    t0 = time.perf_counter()
+    oc.step(1)
+    per_particle = (time.perf_counter() - t0) / cal.particle_count
+    oc.close()
+    steps = max_steps or 3
+    frac = min(1.0, steps_budget_s / max(1e-9, per_particle * scene.particle_count * (steps + warmup)))
+    sample = scene if frac >= 1.0 else sample_scene(scene, frac)
+    o = O.OracleSim(sample, threads=threads)
+    o.step(warmup)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    n = sample.particle_count
+    info = {"steps": steps, "particles": n, "seconds": round(dt, 3)}
+    return n * steps / dt, info, threads
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    scene = build_scene(args.cells_per_type, args.seed)
+    budget = float(os.environ.get("BCS_REFERENCE_BUDGET_S", "150"))
+    # the whole K-step run is sized to the budget: every step is one oracle
+    # step of a sample of the workload
+    value, info, threads = time_oracle(scene, budget, warmup=max(0, args.warmup), max_steps=args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * info["seconds"] / max(1, info["steps"]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(scene, ws),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{info['particles']} particles (inflow end of the same vessel) x "
+                                   f"{info['steps']} steps, FP64 oracle, {threads} OpenMP threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import bcs_build
+    import bcs
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    bcs_build.build()
+    bcs.set_device(local)
+    scene = build_scene(args.cells_per_type, args.seed + rank)
+    sim = bcs.Simulation(scene)
+    sim.set_particles(scene.positions, scene.velocities)
+    n = sim.n
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        sim.synchronize()
+
+    sim.step(args.warmup)
+    barrier()
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = str(getattr(props, "uuid", "") or local)
+    if gpu_id and not gpu_id.startswith("GPU-") and len(gpu_id) > 8:
+        gpu_id = "GPU-" + gpu_id
+    sampler = ClockSampler(gpu_id)
+    time.sleep(0.3)
+    ms = sim.time_steps(args.steps)
+    clocks = sampler.stop()
+    barrier()
+    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = ws * n * args.steps / (ms_max / 1e3)
+    info = sim.refresh_info()
+    launches = info.kernels_per_step * args.steps
+
+    # per-phase CUDA-event profile of eager frames (same stream, same kernels)
+    prof_steps = args.profile_steps
+    phases = sim.profile_steps(prof_steps)
+    k_ms = phases["particles"] / prof_steps
+    peak, peak_kind = measured_peak()
+    achieved = ALGO_BYTES_STEP_KERNEL * n / (k_ms / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(REPO, "profiles", "k_step_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            tr = json.load(f)
+        traffic = tr["dram_bytes_per_launch"] * n / tr["particles"]
+
+    # end to end through the C ABI, pinned host buffers
+    e2e_steps = max(1, min(args.e2e_steps, args.steps))
+    hp = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(6)]
+    for k in range(3):
+        hp[k].copy_(torch.from_numpy(np.ascontiguousarray(scene.positions[:, k])))
+        hp[3 + k].copy_(torch.from_numpy(np.ascontiguousarray(scene.velocities[:, k])))
+    lib = bcs.load_library()
+    P, Vv = bcs.Vec3(*(x.data_ptr() for x in hp[:3])), bcs.Vec3(*(x.data_ptr() for x in hp[3:]))
+    out = bcs.Vec3(*(x.data_ptr() for x in hp[:3]))
+    barrier()
+    t0 = time.perf_counter()
+    assert lib.bcs_set_particles(sim.h, P, Vv, bcs.Vec3(), bcs.MEM_HOST) == 0
+    for _ in range(e2e_steps):
+        assert lib.bcs_step(sim.h, 1) == 0
+        assert lib.bcs_get_particles(sim.h, out, bcs.Vec3(), bcs.Vec3(), bcs.MEM_HOST) == 0
+    e2e_s = time.perf_counter() - t0
+    e2e_t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+    if ws > 1:
+        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = ws * n * e2e_steps / float(e2e_t.item())
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        v, cinfo, threads = time_oracle(scene, args.cpu_budget, warmup=1, max_steps=3)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{cinfo['particles']} particles (inflow end of the same vessel) x {cinfo['steps']} "
+                         f"steps in {cinfo['seconds']} s, FP64 oracle, {threads} OpenMP threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(scene, ws),
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": int(24 * n / e2e_steps), "d2h_bytes_per_step": int(12 * n)},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "bcs::k_step<0>", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": ALGO_BYTES_STEP_KERNEL * n,
+                         "kernel_ms": k_ms},
+            "phase_ms": {k: v / prof_steps for k, v in phases.items()},
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells-per-type", type=int, default=CELLS_PER_TYPE)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--profile-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -185,6 +185,8 @@ typedef struct bcs_info {
     int64_t tri_cell_count;
     int64_t steps_done;
     size_t device_bytes;
+    int kernels_per_step;          /* kernel nodes in one captured frame (0
+                                      until the first bcs_step replay)      */
 } bcs_info;
 
 /* Fill *p with the reference's shipped constants (src/config/physics.hpp, simulation.hpp). */
@@ -192,6 +194,12 @@ void bcs_default_params(bcs_params* p);
 
 const char* bcs_status_string(bcs_status s);
 int bcs_abi_version(void);
+
+/* Make `device` current for the calling thread in the library's CUDA
+ * runtime (the library links its own runtime, so a caller's cudaSetDevice
+ * through another runtime copy does not reach it).  Replaces the
+ * cudaSetDevice(0) of src/main.cu:58. */
+bcs_status bcs_set_device(int device);
 
 /* Build the scene on the current CUDA device.  Replaces the constructors in
  * src/main.cu:122-138 (BloodCells, VeinTriangles, UniformGrid x2,
@@ -257,6 +265,20 @@ bcs_status bcs_synchronize(bcs_sim* sim);
 /* Time `nsteps` of bcs_step on the device with CUDA events recorded on the
  * handle's stream; writes milliseconds.  For benchmarking. */
 bcs_status bcs_time_steps(bcs_sim* sim, int nsteps, float* ms_out);
+
+/* Phases of one frame timed by bcs_profile_steps. */
+enum {
+    BCS_PHASE_GRID = 0,         /* key sort + cell ranges                   */
+    BCS_PHASE_VEIN_FORCES = 1,  /* vein spring gather                       */
+    BCS_PHASE_PARTICLES = 2,    /* the fused particle step kernel            */
+    BCS_PHASE_VEIN_UPDATE = 3,  /* vein integration + triangle cache         */
+    BCS_PHASE_COUNT = 4
+};
+
+/* Run `nsteps` frames eagerly (no graph) with CUDA events between phases on
+ * the handle's stream; adds each phase's milliseconds into
+ * phase_ms[BCS_PHASE_COUNT].  Same results as bcs_step. */
+bcs_status bcs_profile_steps(bcs_sim* sim, int nsteps, float* phase_ms);
 
 #ifdef __cplusplus
 }

@@ -100,8 +100,28 @@ struct Grid {
     int cx = 0, cy = 0, cz = 0;
     int64_t cells = 0;
     std::vector<int> keys, ids;            // sorted
-    std::vector<int> starts, ends;         // dense, empty = (0,-1)
 };
+
+// [first, last] sorted slots of a cell (empty: first > last).  A binary
+// search on the sorted keys gives the ranges calculateStartAndEndOfCellKernel
+// writes (uniform_grid.cu:51-80) without a dense per-cell array.
+inline bool cell_slots(const Grid& g, long long c, int& first, int& last) {
+    auto r = std::equal_range(g.keys.begin(), g.keys.end(), (int)c);
+    first = (int)(r.first - g.keys.begin());
+    last = (int)(r.second - g.keys.begin()) - 1;
+    return first <= last;
+}
+
+void dense_ranges(const Grid& g, int* starts, int* ends) {
+    if (starts) std::fill(starts, starts + g.cells, 0);
+    if (ends) std::fill(ends, ends + g.cells, -1);
+    const int n = (int)g.keys.size();
+    for (int i = 0; i < n; ++i) {
+        int k = g.keys[i];
+        if (starts && (i == 0 || k != g.keys[i - 1])) starts[k] = i;
+        if (ends && (i == n - 1 || k != g.keys[i + 1])) ends[k] = i;
+    }
+}
 
 struct Sim {
     bcs_params p{};
@@ -169,13 +189,6 @@ void build_grid(const Sim& s, Grid& g, const std::vector<float>& px, const std::
     for (int i = 0; i < n; ++i) sk[i] = g.keys[order[i]];
     g.keys.swap(sk);
     g.ids.swap(order);
-    g.starts.assign((size_t)g.cells, 0);
-    g.ends.assign((size_t)g.cells, -1);
-    for (int i = 0; i < n; ++i) {
-        int k = g.keys[i];
-        if (i == 0 || k != g.keys[i - 1]) g.starts[k] = i;
-        if (i == n - 1 || k != g.keys[i + 1]) g.ends[k] = i;
-    }
 }
 
 void particle_positions_f32(const Sim& s, std::vector<float>& px, std::vector<float>& py,
@@ -407,8 +420,9 @@ void particle_collisions(Sim& s) {
                 for (int dy = y0; dy <= y1; ++dy)
                     for (int dz = z0; dz <= z1; ++dz) {
                         long long nc = (long long)cellId + (long long)dz * g.cx * g.cy + (long long)dy * g.cx + dx;
-                        if (nc < 0 || nc >= g.cells) continue;
-                        for (int i = g.starts[nc]; i <= g.ends[nc]; ++i) test(g.ids[i]);
+                        int f, l;
+                        if (nc < 0 || nc >= g.cells || !cell_slots(g, nc, f, l)) continue;
+                        for (int i = f; i <= l; ++i) test(g.ids[i]);
                     }
         }
         add[pid] = acc;
@@ -468,8 +482,9 @@ void vein_collisions(Sim& s) {
                 for (int dy = y0; dy <= y1 && !hit; ++dy)
                     for (int dz = z0; dz <= z1 && !hit; ++dz) {
                         long long nc = (long long)cellId + (long long)dz * g.cx * g.cy + (long long)dy * g.cx + dx;
-                        if (nc < 0 || nc >= g.cells) continue;
-                        for (int i = g.starts[nc]; i <= g.ends[nc]; ++i)
+                        int f, l;
+                        if (nc < 0 || nc >= g.cells || !cell_slots(g, nc, f, l)) continue;
+                        for (int i = f; i <= l; ++i)
                             if (test(g.ids[i])) { hit = true; break; }
                     }
         }
@@ -811,8 +826,7 @@ void bcso_get_grid(bcso_sim* h, int which, int* keys, int* ids, int* starts, int
     Grid& g = which ? s->tgrid : s->pgrid;
     if (keys) std::copy(g.keys.begin(), g.keys.end(), keys);
     if (ids) std::copy(g.ids.begin(), g.ids.end(), ids);
-    if (starts) std::copy(g.starts.begin(), g.starts.end(), starts);
-    if (ends) std::copy(g.ends.begin(), g.ends.end(), ends);
+    dense_ranges(g, starts, ends);
 }
 
 // Grid of arbitrary FP32 points with the scene's bounds and particle-grid
@@ -827,8 +841,7 @@ void bcso_grid_of_points(bcso_sim* h, int n, const float* pts3, int* keys, int* 
     build_grid(*s, g, px, py, pz, &e);
     std::copy(g.keys.begin(), g.keys.end(), keys);
     std::copy(g.ids.begin(), g.ids.end(), ids);
-    if (starts) std::copy(g.starts.begin(), g.starts.end(), starts);
-    if (ends) std::copy(g.ends.begin(), g.ends.end(), ends);
+    dense_ranges(g, starts, ends);
     if (err) *err = e;
 }
 

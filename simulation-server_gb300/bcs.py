@@ -24,11 +24,13 @@ MEM_HOST, MEM_DEVICE = 0, 1
 ERRW_OUT_OF_GRID, ERRW_NAN_NORMALIZE, ERRW_NONFINITE = 1, 2, 4
 
 EXPORTED = [
-    "bcs_default_params", "bcs_status_string", "bcs_abi_version", "bcs_create", "bcs_destroy",
+    "bcs_default_params", "bcs_status_string", "bcs_abi_version", "bcs_set_device", "bcs_create", "bcs_destroy",
     "bcs_get_info", "bcs_set_particles", "bcs_get_particles", "bcs_set_vein", "bcs_get_vein",
     "bcs_calculate_grids", "bcs_calculate_next_frame", "bcs_propagate_all", "bcs_step",
     "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
+    "bcs_profile_steps",
 ]
+PHASES = ("grid", "vein_forces", "particles", "vein_update")
 
 
 class BcsError(RuntimeError):
@@ -95,6 +97,7 @@ class Info(C.Structure):
         ("cell_count", C.c_int64),
         ("tri_cell_count_x", C.c_int), ("tri_cell_count_y", C.c_int), ("tri_cell_count_z", C.c_int),
         ("tri_cell_count", C.c_int64), ("steps_done", C.c_int64), ("device_bytes", C.c_size_t),
+        ("kernels_per_step", C.c_int),
     ]
 
 
@@ -114,6 +117,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_default_params": ([C.POINTER(Params)], None),
         "bcs_status_string": ([C.c_int], C.c_char_p),
         "bcs_abi_version": ([], C.c_int),
+        "bcs_set_device": ([C.c_int], C.c_int),
         "bcs_create": ([C.POINTER(SceneDesc), P, C.POINTER(P)], C.c_int),
         "bcs_destroy": ([P], C.c_int),
         "bcs_get_info": ([P, C.POINTER(Info)], C.c_int),
@@ -130,6 +134,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_get_error_word": ([P, C.POINTER(C.c_uint32), C.c_int], C.c_int),
         "bcs_synchronize": ([P], C.c_int),
         "bcs_time_steps": ([P, C.c_int, C.POINTER(C.c_float)], C.c_int),
+        "bcs_profile_steps": ([P, C.c_int, C.POINTER(C.c_float)], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -185,6 +190,10 @@ def _ptr(a) -> int | None:
 def _check(status: int, what: str) -> None:
     if status != BCS_OK:
         raise BcsError(status, what)
+
+
+def set_device(device: int) -> None:
+    _check(load_library().bcs_set_device(int(device)), "bcs_set_device")
 
 
 class SceneBuffers:
@@ -309,6 +318,12 @@ class Simulation:
         ms = C.c_float()
         _check(self.lib.bcs_time_steps(self.h, int(nsteps), C.byref(ms)), "bcs_time_steps")
         return ms.value
+
+    def profile_steps(self, nsteps: int) -> dict:
+        """Eager frames with CUDA events between phases: summed ms per phase."""
+        ms = (C.c_float * len(PHASES))()
+        _check(self.lib.bcs_profile_steps(self.h, int(nsteps), ms), "bcs_profile_steps")
+        return dict(zip(PHASES, list(ms)))
 
     def synchronize(self) -> None:
         _check(self.lib.bcs_synchronize(self.h), "bcs_synchronize")

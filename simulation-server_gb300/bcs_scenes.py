@@ -141,7 +141,7 @@ def straight_vein(radius=30.0, length=300.0, around=64, rings=100) -> VeinMesh:
 
 
 def bifurcation_vein(trunk_radius=40.0, branch_radius=28.0, trunk_length=1500.0, branch_length=1500.0,
-                     half_angle_deg=15.0, trunk_around=60, branch_around=44, ring_spacing=4.2) -> VeinMesh:
+                     half_angle_deg=15.0, trunk_around=60, branch_around=44, ring_spacing=3.1) -> VeinMesh:
     """Y bifurcation: a trunk along -Y from the origin, two branches from the
     trunk's end at +-half_angle in the x-y plane.  Triangles of one tube that
     lie inside another tube are removed, which opens the junction."""

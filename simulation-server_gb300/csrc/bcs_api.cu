@@ -108,6 +108,9 @@ struct bcs_sim {
     StepArgs args{};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t pev[BCS_PHASE_COUNT + 1] = {};
+    float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
+    int kernels_per_step = 0;
 };
 
 namespace {
@@ -226,14 +229,20 @@ void enqueue_vein_propagate(bcs_sim* s) {
     launch_bump_step(s->steps, s->stream);
 }
 
-// One fused frame on the stream (no host synchronisation).
-void enqueue_frame(bcs_sim* s) {
+// One fused frame on the stream (no host synchronisation).  With `ev`, an
+// event is recorded before each phase and after the last one.
+void enqueue_frame(bcs_sim* s, cudaEvent_t* ev = nullptr) {
+    if (ev) cudaEventRecord(ev[0], s->stream);
     enqueue_grids(s);
+    if (ev) cudaEventRecord(ev[1], s->stream);
     enqueue_vein_forces(s);
+    if (ev) cudaEventRecord(ev[2], s->stream);
     const int in = s->cur, out = s->cur ^ 1;
     refresh_args(s, in, out, true);
     launch_step(s->args, (int)s->work_host.size(), 0, s->stream);
+    if (ev) cudaEventRecord(ev[3], s->stream);
     enqueue_vein_propagate(s);
+    if (ev) cudaEventRecord(ev[4], s->stream);
     s->cur = out;
     s->keys_valid = true;    // k_step wrote keys of the new positions
     ++s->host_steps;
@@ -293,6 +302,7 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
     }
     BCS_CUDA(cudaEventCreate(&s->ev0));
     BCS_CUDA(cudaEventCreate(&s->ev1));
+    for (auto& e : s->pev) BCS_CUDA(cudaEventCreate(&e));
 
     // ---- cell types: offsets, CSR springs, radii (blood_cell_factory.hpp:172-328,
     //      simulation_controller.cu:93-153)
@@ -488,27 +498,35 @@ void destroy_impl(bcs_sim* s) {
     for (void* p : s->allocations) cudaFree(p);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    for (auto& e : s->pev)
+        if (e) cudaEventDestroy(e);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
 }
 
 bool bad_vec(const bcs_vec3& v) { return !v.x || !v.y || !v.z; }
 
-// Copy three SoA arrays (host or device) into a float4 buffer.
+bcs_status ensure_scratch(bcs_sim* s) {
+    if (s->scratch) return BCS_OK;
+    return dalloc(s, &s->scratch, 3 * (size_t)std::max(s->N, s->V));
+}
+
+// Copy three SoA arrays (host or device) into a float4 buffer.  Host arrays
+// are copied by DMA into a device scratch (fast when they are pinned) and
+// packed on the device.
 bcs_status set_vec(bcs_sim* s, const bcs_vec3& v, int n, float4* dst, const float* wsrc, bcs_memory where) {
     if (where == BCS_MEM_DEVICE) {
         launch_pack(v.x, v.y, v.z, n, dst, wsrc, s->stream);
         return check_last();
     }
-    std::vector<float4> h(n);
-    std::vector<float> w;
-    if (wsrc) {
-        w.resize(n);
-        BCS_CUDA(cudaMemcpy(w.data(), wsrc, sizeof(float) * n, cudaMemcpyDeviceToHost));
-    }
-    for (int i = 0; i < n; ++i) h[i] = make_float4(v.x[i], v.y[i], v.z[i], wsrc ? w[i] : 0.f);
-    BCS_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s->stream));
+    bcs_status st = ensure_scratch(s);
+    if (st != BCS_OK) return st;
+    const size_t b = sizeof(float) * (size_t)n;
+    BCS_CUDA(cudaMemcpyAsync(s->scratch, v.x, b, cudaMemcpyHostToDevice, s->stream));
+    BCS_CUDA(cudaMemcpyAsync(s->scratch + n, v.y, b, cudaMemcpyHostToDevice, s->stream));
+    BCS_CUDA(cudaMemcpyAsync(s->scratch + 2 * (size_t)n, v.z, b, cudaMemcpyHostToDevice, s->stream));
+    launch_pack(s->scratch, s->scratch + n, s->scratch + 2 * (size_t)n, n, dst, wsrc, s->stream);
     BCS_CUDA(cudaStreamSynchronize(s->stream));
-    return BCS_OK;
+    return check_last();
 }
 
 bcs_status get_vec(bcs_sim* s, const float4* src, int n, const bcs_vec3& v, bcs_memory where) {
@@ -517,15 +535,16 @@ bcs_status get_vec(bcs_sim* s, const float4* src, int n, const bcs_vec3& v, bcs_
         launch_unpack(src, n, v.x, v.y, v.z, s->stream);
         return check_last();
     }
-    std::vector<float4> h(n);
-    BCS_CUDA(cudaMemcpyAsync(h.data(), src, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+    bcs_status st = ensure_scratch(s);
+    if (st != BCS_OK) return st;
+    float* d[3] = {s->scratch, s->scratch + n, s->scratch + 2 * (size_t)n};
+    launch_unpack(src, n, v.x ? d[0] : nullptr, v.y ? d[1] : nullptr, v.z ? d[2] : nullptr, s->stream);
+    const size_t b = sizeof(float) * (size_t)n;
+    if (v.x) BCS_CUDA(cudaMemcpyAsync(v.x, d[0], b, cudaMemcpyDeviceToHost, s->stream));
+    if (v.y) BCS_CUDA(cudaMemcpyAsync(v.y, d[1], b, cudaMemcpyDeviceToHost, s->stream));
+    if (v.z) BCS_CUDA(cudaMemcpyAsync(v.z, d[2], b, cudaMemcpyDeviceToHost, s->stream));
     BCS_CUDA(cudaStreamSynchronize(s->stream));
-    for (int i = 0; i < n; ++i) {
-        if (v.x) v.x[i] = h[i].x;
-        if (v.y) v.y[i] = h[i].y;
-        if (v.z) v.z[i] = h[i].z;
-    }
-    return BCS_OK;
+    return check_last();
 }
 
 }  // namespace
@@ -587,6 +606,14 @@ const char* bcs_status_string(bcs_status s) {
 
 int bcs_abi_version(void) { return BCS_ABI_VERSION; }
 
+bcs_status bcs_set_device(int device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return BCS_ERR_NO_DEVICE;
+    if (device < 0 || device >= n) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaSetDevice(device));
+    return BCS_OK;
+}
+
 bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out) {
     if (!out) return BCS_ERR_INVALID_ARGUMENT;
     *out = nullptr;
@@ -628,6 +655,7 @@ bcs_status bcs_get_info(bcs_sim* s, bcs_info* o) {
     o->tri_cell_count = s->tg.g.cells;
     o->steps_done = s->host_steps;
     o->device_bytes = s->bytes;
+    o->kernels_per_step = s->kernels_per_step;
     return BCS_OK;
 }
 
@@ -722,6 +750,18 @@ static bcs_status run_steps(bcs_sim* s, int n) {
             s->cur = cur0;
             s->host_steps = hs;
             if (ce != cudaSuccess) return BCS_ERR_CUDA;
+            {
+                size_t nn = 0;
+                cudaGraphGetNodes(graph, nullptr, &nn);
+                std::vector<cudaGraphNode_t> nodes(nn);
+                cudaGraphGetNodes(graph, nodes.data(), &nn);
+                int kernels = 0;
+                for (auto nd : nodes) {
+                    cudaGraphNodeType t;
+                    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+                }
+                s->kernels_per_step = kernels;
+            }
             ce = cudaGraphInstantiate(&g, graph, 0);
             cudaGraphDestroy(graph);
             if (ce != cudaSuccess) { g = nullptr; return BCS_ERR_CUDA; }
@@ -824,6 +864,20 @@ bcs_status bcs_time_steps(bcs_sim* s, int nsteps, float* ms_out) {
     BCS_CUDA(cudaEventRecord(s->ev1, s->stream));
     BCS_CUDA(cudaEventSynchronize(s->ev1));
     BCS_CUDA(cudaEventElapsedTime(ms_out, s->ev0, s->ev1));
+    return check_last();
+}
+
+bcs_status bcs_profile_steps(bcs_sim* s, int nsteps, float* phase_ms) {
+    if (!s || !phase_ms || nsteps < 0 || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < nsteps; ++i) {
+        enqueue_frame(s, s->pev);
+        BCS_CUDA(cudaEventSynchronize(s->pev[BCS_PHASE_COUNT]));
+        for (int k = 0; k < BCS_PHASE_COUNT; ++k) {
+            float ms = 0.f;
+            BCS_CUDA(cudaEventElapsedTime(&ms, s->pev[k], s->pev[k + 1]));
+            phase_ms[k] += ms;
+        }
+    }
     return check_last();
 }
 

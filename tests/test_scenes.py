@@ -1,0 +1,50 @@
+"""Scene generators: the BASELINE shapes (CPU only)."""
+import numpy as np
+
+import bcs_scenes as S
+
+
+def test_cell_models():
+    s = S.sphere_cell(3.0, 1)
+    assert s.vertices.shape == (42, 3) and s.springs.shape == (120, 2)
+    np.testing.assert_allclose(np.linalg.norm(s.vertices, axis=1), 3.0, rtol=1e-6)
+    b = S.biconcave_cell(4.0, 2)
+    assert b.vertices.shape == (162, 3) and b.springs.shape == (480, 2)
+    assert abs(b.vertices[:, 0]).max() <= 4.0 + 1e-6 and abs(b.vertices[:, 1]).max() < 1.4
+
+
+def test_straight_scene_shapes():
+    sc = S.straight_scene()
+    assert sc.particle_count == 256 * 42 == len(sc.positions)
+    assert sc.vein_positions.shape == (6400, 3) and sc.vein_indices.shape == (12672, 3)
+    # reference mesh order: (r+1)A+j, rA+j, rA+j+1 then (r+1)A+j, rA+j+1, (r+1)A+j+1
+    assert list(sc.vein_indices[0]) == [64, 0, 1] and list(sc.vein_indices[1]) == [64, 1, 65]
+
+
+def test_placement_has_no_overlap():
+    sc = S.straight_scene(cells=64)
+    cen = sc.positions.reshape(64, 42, 3).mean(1)
+    d = np.linalg.norm(cen[:, None] - cen[None], axis=2) + np.eye(64) * 1e9
+    assert d.min() >= 2 * 3.0 + 2 * 0.5
+    r = np.linalg.norm(sc.positions[:, [0, 2]], axis=1)
+    assert r.max() < 30.0 - 0.5
+
+
+def test_triangle_normals_point_into_lumen():
+    sc = S.straight_scene(cells=1)
+    p = sc.vein_positions.astype(np.float64)
+    t = sc.vein_indices.astype(np.int64)
+    e1 = p[t[:, 1]] - p[t[:, 0]]
+    e2 = p[t[:, 2]] - p[t[:, 0]]
+    n = np.cross(e2, e1)
+    c = p[t].mean(1)
+    radial = c.copy()
+    radial[:, 1] = 0
+    assert np.all((n * radial).sum(1) < 0)
+
+
+def test_bifurcation_small():
+    sc = S.bifurcation_scene(cells_per_type=300, seed=3)
+    assert sc.particle_count == 300 * 42 + 300 * 162
+    assert len(sc.flow_segments) == 3
+    assert len(sc.ending_radii) == 2

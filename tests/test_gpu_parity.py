@@ -174,7 +174,7 @@ def test_hundred_steps_within_1e3_radius(lib, small):
 
 
 def test_deformable_vein_parity(lib):
-    sc = S.straight_scene(cells=40, seed=9, radius=12.0, length=60.0, around=24, rings=20, vein_dynamic=True)
+    sc = S.straight_scene(cells=24, seed=9, radius=12.0, length=60.0, around=24, rings=20, vein_dynamic=True)
     sc.velocities[:] = np.random.default_rng(4).normal(0, 15.0, sc.velocities.shape).astype(np.float32)
     sim = make(sc)
     o = O.OracleSim(sc)

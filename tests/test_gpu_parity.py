@@ -195,9 +195,7 @@ def test_deformable_vein_parity(lib):
 def test_respawn_parity(lib):
     # Cells start just above the outlet sphere, so the vein-end rule fires.
     sc = S.straight_scene(cells=8, seed=2, radius=12.0, length=60.0, around=24, rings=20)
-    shift = np.array([0.0, -38.0, 0.0], np.float32)
-    sc.positions[:] += shift - np.array([0, sc.positions[:, 1].max() + 1.0, 0], np.float32) * 0
-    sc.positions[:, 1] -= sc.positions[:, 1].max() + 44.0
+    sc.positions[:, 1] -= sc.positions[:, 1].max() + 44.0   # top of the stack at y = -44
     sc.velocities[:] = np.array([0, -80.0, 0], np.float32)
     sim = make(sc)
     o = O.OracleSim(sc)

@@ -144,6 +144,13 @@ struct Sim {
     int64_t steps = 0;
     unsigned err = 0;
     int threads = 1;
+    // Reference-order mode, used only to pin the oracle against the
+    // reference's kernels executed serially on the CPU: neighbour forces
+    // already rewritten earlier in the same pass are read (the serial
+    // outcome of the Q3 race) and collision radii use the launch type's
+    // model index (Q1, particle_collisions.cuh:76,124).
+    bool reference_order = false;
+    std::vector<float> model_radius;        // all types' radius tables, concatenated
 };
 
 // ---------------------------------------------------------------- grid ----
@@ -365,7 +372,8 @@ void cell_springs(Sim& s) {
                     float L = ty.graph[(size_t)j * ty.pic + i];
                     if (L == 0.0f) continue;
                     const int pj = first + j;
-                    acc = acc + cell_spring(s, s.x[pi] - s.x[pj], s.v[pi] - s.v[pj], s.f[pi], s.f[pj], L, &e);
+                    const V3 fj = (s.reference_order && j < i) ? fnew[pj] : s.f[pj];
+                    acc = acc + cell_spring(s, s.x[pi] - s.x[pj], s.v[pi] - s.v[pj], s.f[pi], fj, L, &e);
                 }
                 real ratio = length(s.x[pi] - center) / ty.r0[i];
                 acc = acc + environment(s, s.x[pi], s.v[pi], ratio);
@@ -394,13 +402,21 @@ void particle_collisions(Sim& s) {
         unsigned e = 0;
         const int pid = g.uniform ? g.ids[slot] : slot;
         const V3 p1 = s.x[pid], v1 = s.v[pid];
-        const real r1 = particle_radius(s, pid);
+        // Q1: in reference order the radius index comes from the type whose
+        // sorted-slot range holds `slot`, applied to any particle id.
+        const TypeLayout& launch = s.types[s.type_of_particle[slot]];
+        auto radius_of = [&](int particle) -> real {
+            if (!s.reference_order) return particle_radius(s, particle);
+            int m = launch.model_start + (particle - launch.particle_start) % launch.pic;
+            return s.model_radius[m];
+        };
+        const real r1 = radius_of(pid);
         V3 acc{0, 0, 0};
         auto test = [&](int q) {
             if (q == pid) return;
             V3 rp = p1 - s.x[q];
             real d2 = dot(rp, rp);
-            real md = r1 + particle_radius(s, q);
+            real md = r1 + radius_of(q);
             if (d2 <= md * md && d2 >= 0.0001)
                 acc = acc + resilient(s, rp, v1 - s.v[q], d2, r1, &e);
         };
@@ -667,6 +683,7 @@ int bcso_create(const bcs_scene_desc* d, bcso_sim** out) {
         s->types.push_back(std::move(L));
     }
     s->N = pstart; s->C = cstart;
+    for (const auto& L : s->types) s->model_radius.insert(s->model_radius.end(), L.radius.begin(), L.radius.end());
     s->type_of_particle.resize(s->N);
     for (size_t t = 0; t < s->types.size(); ++t)
         for (int i = 0; i < s->types[t].count * s->types[t].pic; ++i)
@@ -749,6 +766,8 @@ int bcso_create(const bcs_scene_desc* d, bcso_sim** out) {
 void bcso_destroy(bcso_sim* h) { delete reinterpret_cast<Sim*>(h); }
 
 void bcso_set_threads(bcso_sim* h, int n) { reinterpret_cast<Sim*>(h)->threads = n < 1 ? 1 : n; }
+
+void bcso_set_reference_order(bcso_sim* h, int on) { reinterpret_cast<Sim*>(h)->reference_order = on != 0; }
 
 int bcso_counts(bcso_sim* h, int* out6) {
     Sim* s = reinterpret_cast<Sim*>(h);

@@ -35,6 +35,8 @@ def load() -> C.CDLL:
         lib.bcso_create.restype = C.c_int
         lib.bcso_destroy.argtypes = [P]
         lib.bcso_set_threads.argtypes = [P, C.c_int]
+        lib.bcso_set_reference_order.argtypes = [P, C.c_int]
+        lib.bcso_layout.restype = None
         lib.bcso_counts.argtypes = [P, P]
         lib.bcso_bounds.argtypes = [P, P, P]
         lib.bcso_set_particles.argtypes = [P, P, P, P]
@@ -101,6 +103,17 @@ class OracleSim:
 
     def set_threads(self, n: int):
         self.lib.bcso_set_threads(self.h, int(n))
+
+    def set_reference_order(self, on: bool = True):
+        """Read order of the reference's kernels run serially (pin mode)."""
+        self.lib.bcso_set_reference_order(self.h, int(on))
+
+    def layout(self, model_vertices: int, types: int):
+        starts = np.empty((types, 3), np.int32)
+        radius = np.empty(model_vertices, np.float32)
+        r0 = np.empty(model_vertices, np.float64)
+        self.lib.bcso_layout(self.h, starts.ctypes.data, radius.ctypes.data, r0.ctypes.data)
+        return starts, radius, r0
 
     def set_particles(self, pos, vel, force=None):
         p = np.ascontiguousarray(pos, np.float32)

@@ -25,9 +25,14 @@ void launch_propagate(const StepArgs& a, int blocks, cudaStream_t s);
 void launch_keys(const float4* pos, int n, const GridDev& g, int* keys, int* ids, unsigned* err, cudaStream_t s);
 void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const GridDev& g, int* keys, int* ids,
                      cudaStream_t s);
-void launch_cell_ranges(const int* keys, int n, int2* table, cudaStream_t s);
-void launch_dense_ranges(const int2* table, const int* keys, int count, long long cells, int* starts, int* ends,
+void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, cudaStream_t s);
+void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
                          cudaStream_t s);
+void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s);
+void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tri, const float4* vpos, float4* box,
+                      cudaStream_t s);
+void launch_wall_mask(const uint32_t* tri, const float4* vpos, int T, const MaskDev& m, unsigned char* mask,
+                      float reach, int* epoch, cudaStream_t s);
 void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
                          int V, float k, float d, unsigned* err, cudaStream_t s);
 void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt, cudaStream_t s);
@@ -56,7 +61,8 @@ struct DeviceGrid {
     int* a_v = nullptr;
     int* b_k = nullptr;
     int* b_v = nullptr;
-    int2* table = nullptr;
+    int4* table = nullptr;
+    int* epoch = nullptr;
     unsigned* temp = nullptr;
     int bits = 0;
     int count = 0;
@@ -98,6 +104,10 @@ struct bcs_sim {
     float* nb_len = nullptr;
     uint32_t* tri = nullptr;
     float4* tcache = nullptr;
+    float4* tbox = nullptr;         // 2 per triangle-grid cell
+    unsigned char* wall_mask = nullptr;
+    int* wall_epoch = nullptr;
+    MaskDev wall{};
     // grids
     DeviceGrid pg, tg;
     float minX, maxX, minY, maxY, minZ, maxZ, width, height, depth;
@@ -158,9 +168,12 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count) {
         (st = dalloc(s, &dg.a_v, count)) || (st = dalloc(s, &dg.b_k, count)) || (st = dalloc(s, &dg.b_v, count)) ||
         (st = dalloc(s, &dg.temp, radix_temp_words(count))))
         return st;
+    if ((st = dalloc(s, &dg.epoch, 1))) return st;
+    BCS_CUDA(cudaMemset(dg.epoch, 0, sizeof(int)));
+    dg.g.epoch = dg.epoch;
     if (dg.g.uniform) {
         if ((st = dalloc(s, &dg.table, (size_t)dg.g.cells))) return st;
-        BCS_CUDA(cudaMemset(dg.table, 0, sizeof(int2) * (size_t)dg.g.cells));
+        BCS_CUDA(cudaMemset(dg.table, 0, sizeof(int4) * (size_t)dg.g.cells));
     }
     dg.bits = bits_for(dg.g.cells);
     return BCS_OK;
@@ -172,7 +185,7 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st) {
     dg.g.keys = which ? dg.b_k : dg.a_k;
     dg.g.ids = which ? dg.b_v : dg.a_v;
     dg.g.table = dg.table;
-    launch_cell_ranges(dg.g.keys, dg.count, dg.table, st);
+    launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, st);
 }
 
 void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
@@ -188,9 +201,12 @@ void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
     a.pg = s->pg.g;
     a.tg = s->tg.g;
     a.tcache = s->tcache;
+    a.tbox = s->tbox;
+    a.wall = s->wall;
 }
 
-// Triangle grid + Moller-Trumbore cache from the current vein positions.
+// Triangle grid, Moller-Trumbore cache, per-cell triangle bounds and the
+// wall-proximity mask from the current vein positions.
 void build_triangle_grid(bcs_sim* s, bool regrid) {
     if (s->T == 0) return;
     if (s->tg.g.uniform) {
@@ -199,6 +215,10 @@ void build_triangle_grid(bcs_sim* s, bool regrid) {
             sort_grid(s->tg, s->stream);
         }
         launch_tri_cache(s->tg.g.ids, s->tri, s->vpos, s->T, s->tcache, s->stream);
+        launch_tri_boxes(s->tg.g.keys, s->tg.g.ids, s->T, s->tri, s->vpos, s->tbox, s->stream);
+        if (s->wall_mask)
+            launch_wall_mask(s->tri, s->vpos, s->T, s->wall, s->wall_mask,
+                             s->p.vein_impact_distance * 1.001f + 1e-3f, s->wall_epoch, s->stream);
     } else {
         launch_tri_cache(nullptr, s->tri, s->vpos, s->T, s->tcache, s->stream);
     }
@@ -240,6 +260,7 @@ void enqueue_frame(bcs_sim* s, cudaEvent_t* ev = nullptr) {
     const int in = s->cur, out = s->cur ^ 1;
     refresh_args(s, in, out, true);
     launch_step(s->args, (int)s->work_host.size(), 0, s->stream);
+    if (s->p.use_blood_flow) launch_vein_end(s->args, s->C, s->stream);
     if (ev) cudaEventRecord(ev[3], s->stream);
     enqueue_vein_propagate(s);
     if (ev) cudaEventRecord(ev[4], s->stream);
@@ -449,6 +470,25 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
     if ((st = alloc_grid(s, s->pg, s->N)) || (st = alloc_grid(s, s->tg, std::max(1, s->T)))) return st;
     s->tg.count = s->T;
     s->tg.g.count = s->T;
+    if (s->tg.g.uniform) {
+        if ((st = dalloc(s, &s->tbox, 2 * (size_t)s->tg.g.cells))) return st;
+        // Wall-proximity mask, cells of half the impact distance (1..8).
+        const float mc = std::min(8.0f, std::max(1.0f, s->p.vein_impact_distance * 0.5f));
+        MaskDev& m = s->wall;
+        m.lo[0] = s->minX; m.lo[1] = s->minY; m.lo[2] = s->minZ;
+        m.inv_cell = 1.0f / mc;
+        m.nx = (int)std::ceil(s->width / mc) + 1;
+        m.ny = (int)std::ceil(s->height / mc) + 1;
+        m.nz = (int)std::ceil(s->depth / mc) + 1;
+        const size_t cells = (size_t)m.nx * m.ny * m.nz;
+        if (s->T > 0 && cells <= ((size_t)1 << 30)) {
+            if ((st = dalloc(s, &s->wall_mask, cells)) || (st = dalloc(s, &s->wall_epoch, 1))) return st;
+            BCS_CUDA(cudaMemset(s->wall_mask, 0, cells));
+            BCS_CUDA(cudaMemset(s->wall_epoch, 0, sizeof(int)));
+            m.mask = s->wall_mask;
+            m.epoch = s->wall_epoch;
+        }
+    }
     if ((st = dalloc(s, &s->steps, 1)) || (st = dalloc(s, &s->err, 1))) return st;
     BCS_CUDA(cudaMemset(s->steps, 0, sizeof(long long)));
     BCS_CUDA(cudaMemset(s->err, 0, sizeof(unsigned)));
@@ -804,7 +844,7 @@ bcs_status bcs_get_grid(bcs_sim* s, int which, int* cell_ids, int* object_ids, i
             if (cell_starts) BCS_CUDA(cudaMalloc(&ds, sizeof(int) * (size_t)dg.g.cells));
             if (cell_ends) BCS_CUDA(cudaMalloc(&de, sizeof(int) * (size_t)dg.g.cells));
         }
-        launch_dense_ranges(dg.table, dg.g.keys, n, dg.g.cells, ds, de, s->stream);
+        launch_dense_ranges(dg.table, dg.epoch, dg.g.cells, ds, de, s->stream);
         if (where == BCS_MEM_HOST) {
             if (ds) BCS_CUDA(cudaMemcpyAsync(cell_starts, ds, sizeof(int) * (size_t)dg.g.cells, kind, s->stream));
             if (de) BCS_CUDA(cudaMemcpyAsync(cell_ends, de, sizeof(int) * (size_t)dg.g.cells, kind, s->stream));

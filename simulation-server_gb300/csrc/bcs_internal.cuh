@@ -8,12 +8,13 @@
 //   pkeys[2], pids[2]        int32 x N, grid keys / particle ids (radix-sort
 //                            ping-pong); after the sort they are the
 //                            reference's gridCellIds / particleIds.
-//   ptable                   int2 x (grid cells): (first, last) sorted slot of
-//                            every occupied cell.  Never cleared: an entry is
-//                            trusted only when keys[first] == cell, which holds
-//                            exactly for the cells occupied in this step (those
-//                            are rewritten every step), so stale entries of
-//                            emptied cells are rejected without a clear pass.
+//   ptable                   int4 x (grid cells): (first, last, epoch) of
+//                            every occupied cell.  Never cleared: each grid
+//                            build bumps the grid's epoch and rewrites exactly
+//                            the occupied cells, so an entry is trusted only
+//                            when its epoch is current; stale entries of
+//                            emptied cells are rejected with no clear pass and
+//                            no second, dependent load.
 //   vpos, vvel, vfrc         float4 x V (vein)
 //   vnb_ids[9], vnb_len[9]   int32 / float x V, the reference's nine
 //                            neighbour-slot arrays (VeinNeighbors)
@@ -21,6 +22,10 @@
 //   tcache                   3 float4 per sorted triangle slot: (v0, id),
 //                            (v1 - v0), (v2 - v0) — the Moller-Trumbore
 //                            operands, streamed contiguously per grid cell.
+//   tbox                     2 float4 per triangle-grid cell: bounds of the
+//                            cell's triangles (slightly widened), for ray culling
+//   wall_mask                uint8 per wall-mask cell: the mask epoch where a
+//                            triangle lies within vein_impact_distance of the cell
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -60,8 +65,17 @@ struct GridDev {
     long long cells;
     const int* keys;      // sorted keys
     const int* ids;       // sorted object ids
-    const int2* table;    // validated (first, last) per cell
+    const int4* table;    // (first, last, epoch) per cell
+    const int* epoch;     // current epoch of the table
     int count;            // objects
+};
+
+struct MaskDev {          // wall-proximity mask over the grid box
+    const unsigned char* mask;
+    const int* epoch;     // low byte is the current mark
+    float lo[3];
+    float inv_cell;
+    int nx, ny, nz;
 };
 
 struct StepArgs {
@@ -91,6 +105,8 @@ struct StepArgs {
     float4* vfrc;
     const uint32_t* tri;  // 3 * T vertex indices
     const float4* tcache; // 3 per sorted triangle slot
+    const float4* tbox;   // 2 per triangle-grid cell
+    MaskDev wall;
     int T;
     // flow
     bcs_flow_segment flow[kMaxFlow];
@@ -169,19 +185,16 @@ __device__ inline int grid_key(const GridDev& g, float3 q, unsigned& e) {
     return iz * g.cx * g.cy + iy * g.cx + ix;
 }
 
-// Validated lookup of an occupied cell's (first, last) sorted slot.
-__device__ inline bool cell_range(const GridDev& g, long long c, int& first, int& last) {
+// Lookup of an occupied cell's (first, last) sorted slots: valid only when
+// the entry carries the grid's current epoch.
+__device__ inline bool cell_range(const GridDev& g, int epoch, long long c, int& first, int& last) {
     if (c < 0 || c >= g.cells) return false;
-    int2 r = __ldg(&g.table[c]);
-    if (r.x < 0 || r.x >= g.count || __ldg(&g.keys[r.x]) != (int)c) return false;
+    int4 r = __ldg(&g.table[c]);
+    if (r.z != epoch) return false;
     first = r.x;
     last = r.y;
     return true;
 }
 
-__device__ inline void flag_error(unsigned* err, unsigned e) {
-    unsigned any = __reduce_or_sync(__activemask(), e);
-    if (any && (threadIdx.x & 31) == (__ffs(__activemask()) - 1)) atomicOr(err, any);
-}
 
 }  // namespace bcs

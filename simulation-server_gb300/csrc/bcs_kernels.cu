@@ -1,14 +1,16 @@
 // bcs_kernels.cu — the per-step kernels for sm_103a.
 //
 // One frame of the reference (src/main.cu:175-208) becomes, per step:
-//   radix sort of the grid keys (bcs_sort.cu) → k_cell_ranges →
-//   k_vein_springs → k_step<kFull> → k_vein_integrate → k_tri_cache → k_bump_step
+//   radix sort of the grid keys (bcs_sort.cu) → k_next_epoch → k_cell_ranges →
+//   k_vein_springs → k_step<kFull> → k_vein_end → k_vein_integrate →
+//   k_tri_cache → k_tri_boxes → k_wall_mask → k_bump_step
 // k_step is cell-major: a CTA owns whole blood cells of one type, stages
 // their positions / velocities / previous forces in shared memory, and does
 // for each particle the work of calculateBloodCellsCenters, gatherForcesKernel,
-// calculateParticleCollisions, detectVeinCollisions, propagateParticleForcesKernel
-// and handleVeinEndsBlockSync, then writes the next step's grid keys.  Each
-// particle's x, v, F cross HBM once per step in each direction.
+// calculateParticleCollisions, detectVeinCollisions and
+// propagateParticleForcesKernel, then writes the next step's grid keys.  Each
+// particle's x, v, F cross HBM once per step in each direction.  k_vein_end
+// (handleVeinEndsBlockSync) is a warp-per-cell pass over the new positions.
 #include "bcs_internal.cuh"
 
 namespace bcs {
@@ -137,6 +139,7 @@ __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 
         return acc;
     }
     unsigned dummy = 0;
+    const int ep = __ldg(g.epoch);
     const int cellId = grid_key(g, x, dummy);
     const int xId = (int)__fdiv_rn(x.x - g.lo[0], g.cell[0]);
     const int yId = (int)__fdiv_rn(x.y - g.lo[1], g.cell[1]);
@@ -151,7 +154,7 @@ __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 
             const long long row = (long long)cellId + dz * cxy + (long long)dy * g.cx;
             int first = -1, last = -2, f, l;
             for (int dx = x0; dx <= x1; ++dx)
-                if (cell_range(g, row + dx, f, l)) {
+                if (cell_range(g, ep, row + dx, f, l)) {
                     if (first < 0) first = f;
                     last = l;
                 }
@@ -163,17 +166,54 @@ __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 
     return acc;
 }
 
+// Parametric entry of the ray o + t d (t >= 0) into an axis-aligned box, or
+// a value above `limit` when the ray misses it.
+__device__ inline float ray_box_entry(float3 o, float3 d, float4 lo, float4 hi) {
+    float t0 = 0.f, t1 = 3.0e38f;
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    const float ll[3] = {lo.x, lo.y, lo.z}, hh[3] = {hi.x, hi.y, hi.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (fabsf(dd[k]) < 1e-30f) {
+            if (oo[k] < ll[k] || oo[k] > hh[k]) return 3.0e38f;
+        } else {
+            float inv = 1.0f / dd[k];
+            float ta = (ll[k] - oo[k]) * inv, tb = (hh[k] - oo[k]) * inv;
+            t0 = fmaxf(t0, fminf(ta, tb));
+            t1 = fminf(t1, fmaxf(ta, tb));
+        }
+    }
+    return t0 <= t1 ? t0 : 3.0e38f;
+}
+
 // detectVeinCollisions<UniformGrid> (vein_collisions.cu:198-277,
 // vein_collisions.cuh:60-93) for one particle: the first triangle hit in
-// stencil order (x, then y, then z; sorted order inside a cell).
+// stencil order (x, then y, then z; sorted order inside a cell) decides, and
+// only a hit within vein_impact_distance acts.  Two exact shortcuts leave that
+// outcome unchanged:
+//  * a particle whose wall-mask cell has no triangle within the impact
+//    distance (+ margin) cannot be hit that close: no collision;
+//  * a stencil cell whose triangle bounds the ray does not enter holds no hit,
+//    and once every remaining cell is entered only beyond the impact distance,
+//    the first hit, if any, is too far: no collision.
 __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, float3& F, float R, unsigned& e) {
     const bcs_params& p = a.p;
+    const GridDev& g = a.tg;
+    const float reach = p.vein_impact_distance * 1.001f + 1e-3f;
+    if (g.uniform && a.wall.mask) {
+        const MaskDev& m = a.wall;
+        int ix = (int)((x.x - m.lo[0]) * m.inv_cell), iy = (int)((x.y - m.lo[1]) * m.inv_cell),
+            iz = (int)((x.z - m.lo[2]) * m.inv_cell);
+        if (ix >= 0 && iy >= 0 && iz >= 0 && ix < m.nx && iy < m.ny && iz < m.nz) {
+            const unsigned char mark = (unsigned char)__ldg(m.epoch);
+            if (__ldg(&m.mask[((long long)iz * m.ny + iy) * m.nx + ix]) != mark) return;
+        }
+    }
     const float3 vel = v;
     const float3 dir = normalize_or_zero(vel, e);
     float t = 1e10f;
     float3 n = f3(0.f, 0.f, 0.f), refl = f3(0.f, 0.f, 0.f);
     int obj = -1;
-    const GridDev& g = a.tg;
     auto test_slot = [&](int s) -> bool {
         float4 c0 = __ldg(&a.tcache[3 * s]);
         float4 c1 = __ldg(&a.tcache[3 * s + 1]);
@@ -189,6 +229,7 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
             if (test_slot(s)) break;
     } else {
         unsigned dummy = 0;
+        const int ep = __ldg(g.epoch);
         const unsigned cellId = (unsigned)grid_key(g, x, dummy);
         const unsigned xId = to_u32_sat(__fdiv_rn(x.x - g.lo[0], g.cell[0]));
         const unsigned yId = to_u32_sat(__fdiv_rn(x.y - g.lo[1], g.cell[1]));
@@ -198,12 +239,27 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
         stencil_range_u(yId, g.cy, y0, y1);
         stencil_range_u(zId, g.cz, z0, z1);
         const long long cxy = (long long)g.cx * g.cy;
+        // Pass 1: stencil position of the last cell the ray enters within reach.
+        int last_near = -1, k = 0;
+        for (int dx = x0; dx <= x1; ++dx)
+            for (int dy = y0; dy <= y1; ++dy)
+                for (int dz = z0; dz <= z1; ++dz, ++k) {
+                    const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
+                    int f, l;
+                    if (!cell_range(g, ep, c, f, l)) continue;
+                    if (ray_box_entry(x, dir, __ldg(&a.tbox[2 * c]), __ldg(&a.tbox[2 * c + 1])) <= reach) last_near = k;
+                }
+        // Pass 2: triangles of the cells the ray enters, in stencil order.
         bool found = false;
+        k = 0;
         for (int dx = x0; dx <= x1 && !found; ++dx)
             for (int dy = y0; dy <= y1 && !found; ++dy)
-                for (int dz = z0; dz <= z1 && !found; ++dz) {
+                for (int dz = z0; dz <= z1 && !found; ++dz, ++k) {
+                    if (k > last_near) { found = true; break; }
+                    const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
                     int f, l;
-                    if (!cell_range(g, (long long)cellId + dz * cxy + (long long)dy * g.cx + dx, f, l)) continue;
+                    if (!cell_range(g, ep, c, f, l)) continue;
+                    if (ray_box_entry(x, dir, __ldg(&a.tbox[2 * c]), __ldg(&a.tbox[2 * c + 1])) > 2.9e38f) continue;
                     for (int s = f; s <= l; ++s)
                         if (test_slot(s)) { found = true; break; }
                 }
@@ -264,12 +320,11 @@ constexpr int kFull = 0;    // whole frame: forces, integration, vein end, next 
 constexpr int kForces = 1;  // calculateNextFrame only: forces and collision velocities
 
 template <int MODE>
-__global__ void __launch_bounds__(kStepThreads, 2) k_step(const StepArgs a) {
+__global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
     __shared__ float4 s_pos[kMaxChunk];
     __shared__ float4 s_vel[kMaxChunk];
     __shared__ float4 s_frc[kMaxChunk];
     __shared__ float3 s_cent[kMaxCellsPerChunk];
-    __shared__ int s_tp[kMaxCellsPerChunk];
 
     const WorkItem w = a.work[blockIdx.x];
     const TypeDev ty = a.types[w.type];
@@ -281,7 +336,6 @@ __global__ void __launch_bounds__(kStepThreads, 2) k_step(const StepArgs a) {
         s_vel[i] = a.vel_in[p0 + i];
         s_frc[i] = a.frc_in[p0 + i];
     }
-    if (threadIdx.x < w.ncells) s_tp[threadIdx.x] = 0;
     __syncthreads();
 
     // Cell centroids (blood_cells.cu:44-61), one warp per cell, fixed-order
@@ -301,17 +355,10 @@ __global__ void __launch_bounds__(kStepThreads, 2) k_step(const StepArgs a) {
     __syncthreads();
 
     unsigned e = 0;
-    const long long step = *a.steps;
-    float3 nx[2], nv[2], nf[2];
-    float rad[2];
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int i = threadIdx.x + r * kStepThreads;
-        if (i >= np) continue;
+    for (int i = threadIdx.x; i < np; i += kStepThreads) {
         const int c = i / pic, li = i - c * pic, pid = p0 + i;
         const float4 px = s_pos[i];
         const float3 x = xyz(px), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
-        rad[r] = px.w;
         // Intra-cell springs, gatherForcesKernel (blood_cells.cu:66-120) over
         // the CSR form of the dense spring graph (same ascending order).
         float3 F = f3(0.f, 0.f, 0.f);
@@ -329,48 +376,50 @@ __global__ void __launch_bounds__(kStepThreads, 2) k_step(const StepArgs a) {
         // Particle-vein collision.
         float3 vv = v;
         vein_collision(a, x, vv, F, px.w, e);
+        float3 nx = x, nv = vv;
         if (MODE == kFull) {
             // propagateParticleForcesKernel (blood_cells.cu:155-179), Heun.
             const float3 v1 = vv + a.p.dt * F;
-            nx[r] = x + (0.5f * a.p.dt) * (v1 + vv);
-            nv[r] = v1;
-        } else {
-            nx[r] = x;
-            nv[r] = vv;
+            nx = x + (0.5f * a.p.dt) * (v1 + vv);
+            nv = v1;
         }
-        nf[r] = F;
-    }
-    if (MODE == kFull && a.p.use_blood_flow) {
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const int i = threadIdx.x + r * kStepThreads;
-            if (i < np && leaves_vein(a, nx[r])) atomicOr(&s_tp[i / pic], 1);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const int i = threadIdx.x + r * kStepThreads;
-            if (i < np) {
-                const int c = i / pic;
-                if (s_tp[c]) respawn(a, ty.cell_start + w.first_cell + c, step, ty.model_start + (i - c * pic), nx[r], nv[r]);
-            }
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int i = threadIdx.x + r * kStepThreads;
-        if (i >= np) continue;
-        const int pid = p0 + i;
-        if (!(isfinite(nx[r].x) && isfinite(nx[r].y) && isfinite(nx[r].z) && isfinite(nv[r].x) &&
-              isfinite(nv[r].y) && isfinite(nv[r].z)))
+        if (!(isfinite(nx.x) && isfinite(nx.y) && isfinite(nx.z) && isfinite(nv.x) && isfinite(nv.y) &&
+              isfinite(nv.z)))
             e |= BCS_ERRW_NONFINITE;
-        a.pos_out[pid] = make_float4(nx[r].x, nx[r].y, nx[r].z, rad[r]);
-        a.vel_out[pid] = make_float4(nv[r].x, nv[r].y, nv[r].z, 0.f);
-        a.frc_out[pid] = make_float4(nf[r].x, nf[r].y, nf[r].z, 0.f);
+        a.pos_out[pid] = make_float4(nx.x, nx.y, nx.z, px.w);
+        a.vel_out[pid] = make_float4(nv.x, nv.y, nv.z, 0.f);
+        a.frc_out[pid] = make_float4(F.x, F.y, F.z, 0.f);
         if (MODE == kFull && a.keys_out) {
-            a.keys_out[pid] = a.pg.uniform ? grid_key(a.pg, nx[r], e) : 0;
+            a.keys_out[pid] = a.pg.uniform ? grid_key(a.pg, nx, e) : 0;
             a.ids_out[pid] = pid;
         }
+    }
+    if (e) atomicOr(a.err, e);
+}
+
+// handleVeinEndsBlockSync (src/simulation/vein_end.cu:57-108) after the
+// integration of a whole frame: one warp per blood cell ORs the vein-end
+// rule over its particles and respawns the cell; the respawned particles'
+// grid keys are rewritten for the next frame.
+__global__ void __launch_bounds__(256) k_vein_end(const StepArgs a) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    int t = 0, cell = warp;
+    while (t < a.type_count && cell >= a.types[t].count) cell -= a.types[t++].count;
+    if (t >= a.type_count) return;
+    const TypeDev ty = a.types[t];
+    const int p0 = ty.particle_start + cell * ty.pic;
+    bool leave = false;
+    for (int k = lane; k < ty.pic; k += 32) leave = leave || leaves_vein(a, xyz(a.pos_out[p0 + k]));
+    if (!__any_sync(0xffffffffu, leave)) return;
+    const long long step = *a.steps;
+    unsigned e = 0;
+    for (int k = lane; k < ty.pic; k += 32) {
+        float3 x, v;
+        respawn(a, ty.cell_start + cell, step, ty.model_start + k, x, v);
+        const float w = a.pos_out[p0 + k].w;
+        a.pos_out[p0 + k] = make_float4(x.x, x.y, x.z, w);
+        a.vel_out[p0 + k] = make_float4(v.x, v.y, v.z, 0.f);
+        if (a.keys_out) a.keys_out[p0 + k] = a.pg.uniform ? grid_key(a.pg, x, e) : 0;
     }
     if (e) atomicOr(a.err, e);
 }
@@ -440,23 +489,28 @@ __global__ void k_tri_keys(const float4* __restrict__ vpos, const uint32_t* __re
     ids[t] = t;
 }
 
+__global__ void k_next_epoch(int* epoch) { *epoch += 1; }
+
 // calculateStartAndEndOfCellKernel (uniform_grid.cu:51-80), written into
-// the validated table: (first, last) of every occupied cell.
-__global__ void k_cell_ranges(const int* __restrict__ keys, int n, int2* table) {
+// the epoch-stamped table: (first, last, epoch) of every occupied cell.
+__global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int k = keys[i];
-    if (i == 0 || keys[i - 1] != k) table[k].x = i;
+    const int k = keys[i];
+    if (i == 0 || keys[i - 1] != k) {
+        table[k].x = i;
+        table[k].z = *epoch;
+    }
     if (i == n - 1 || keys[i + 1] != k) table[k].y = i;
 }
 
-// Dense starts/ends (empty = 0, -1) from the validated table, for getters.
-__global__ void k_dense_ranges(const int2* __restrict__ table, const int* __restrict__ keys, int count,
-                               long long cells, int* starts, int* ends) {
+// Dense starts/ends (empty = 0, -1) from the epoch-stamped table, for getters.
+__global__ void k_dense_ranges(const int4* __restrict__ table, const int* __restrict__ epoch, long long cells,
+                               int* starts, int* ends) {
     long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cells) return;
-    int2 r = table[c];
-    bool occ = r.x >= 0 && r.x < count && keys[r.x] == (int)c;
+    int4 r = table[c];
+    bool occ = r.z == *epoch;
     if (starts) starts[c] = occ ? r.x : 0;
     if (ends) ends[c] = occ ? r.y : -1;
 }
@@ -509,6 +563,51 @@ __global__ void k_tri_cache(const int* __restrict__ ids, const uint32_t* __restr
     cache[3 * s] = make_float4(v0.x, v0.y, v0.z, __int_as_float(t));
     cache[3 * s + 1] = make_float4(e1.x, e1.y, e1.z, 0.f);
     cache[3 * s + 2] = make_float4(e2.x, e2.y, e2.z, 0.f);
+}
+
+// Bounds of each occupied triangle-grid cell's triangles (from the exact
+// vertex positions), widened by a margin that covers FP32 rounding in the
+// ray-box test.
+__global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict__ ids, int T,
+                            const uint32_t* __restrict__ tri, const float4* __restrict__ vpos, float4* box) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= T) return;
+    const int k = keys[s];
+    if (s > 0 && keys[s - 1] == k) return;
+    float3 lo = f3(3.0e38f, 3.0e38f, 3.0e38f), hi = f3(-3.0e38f, -3.0e38f, -3.0e38f);
+    for (int j = s; j < T && keys[j] == k; ++j) {
+        const int t = ids[j];
+        for (int c = 0; c < 3; ++c) {
+            float3 q = xyz(vpos[tri[3 * t + c]]);
+            lo = f3(fminf(lo.x, q.x), fminf(lo.y, q.y), fminf(lo.z, q.z));
+            hi = f3(fmaxf(hi.x, q.x), fmaxf(hi.y, q.y), fmaxf(hi.z, q.z));
+        }
+    }
+    const float m = 1e-3f + 1e-5f * fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fmaxf(fabsf(lo.y), fabsf(hi.y)),
+                                                                         fmaxf(fabsf(lo.z), fabsf(hi.z))));
+    box[2 * (size_t)k] = make_float4(lo.x - m, lo.y - m, lo.z - m, 0.f);
+    box[2 * (size_t)k + 1] = make_float4(hi.x + m, hi.y + m, hi.z + m, 0.f);
+}
+
+// Wall-proximity mask: every mask cell that meets a triangle's bounds
+// widened by `reach` gets the current mark.  A particle in an unmarked cell
+// is farther than `reach` from every triangle.
+__global__ void k_wall_mask(const uint32_t* __restrict__ tri, const float4* __restrict__ vpos, int T, MaskDev m,
+                            unsigned char* mask, float reach) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    float3 a = xyz(vpos[tri[3 * t]]), b = xyz(vpos[tri[3 * t + 1]]), c = xyz(vpos[tri[3 * t + 2]]);
+    float3 lo = f3(fminf(fminf(a.x, b.x), c.x) - reach, fminf(fminf(a.y, b.y), c.y) - reach,
+                   fminf(fminf(a.z, b.z), c.z) - reach);
+    float3 hi = f3(fmaxf(fmaxf(a.x, b.x), c.x) + reach, fmaxf(fmaxf(a.y, b.y), c.y) + reach,
+                   fmaxf(fmaxf(a.z, b.z), c.z) + reach);
+    int x0 = max(0, (int)floorf((lo.x - m.lo[0]) * m.inv_cell)), x1 = min(m.nx - 1, (int)floorf((hi.x - m.lo[0]) * m.inv_cell));
+    int y0 = max(0, (int)floorf((lo.y - m.lo[1]) * m.inv_cell)), y1 = min(m.ny - 1, (int)floorf((hi.y - m.lo[1]) * m.inv_cell));
+    int z0 = max(0, (int)floorf((lo.z - m.lo[2]) * m.inv_cell)), z1 = min(m.nz - 1, (int)floorf((hi.z - m.lo[2]) * m.inv_cell));
+    const unsigned char mark = (unsigned char)*m.epoch;
+    for (int z = z0; z <= z1; ++z)
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x) mask[((long long)z * m.ny + y) * m.nx + x] = mark;
 }
 
 __global__ void k_bump_step(long long* steps) { *steps += 1; }
@@ -569,12 +668,25 @@ void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const GridD
                      cudaStream_t s) {
     if (T > 0) k_tri_keys<<<BCS_GRID1(T, 256), 0, s>>>(vpos, tri, T, g, keys, ids);
 }
-void launch_cell_ranges(const int* keys, int n, int2* table, cudaStream_t s) {
-    if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table);
+void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, cudaStream_t s) {
+    k_next_epoch<<<1, 1, 0, s>>>(epoch);
+    if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table, epoch);
 }
-void launch_dense_ranges(const int2* table, const int* keys, int count, long long cells, int* starts, int* ends,
+void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
                          cudaStream_t s) {
-    if (cells > 0) k_dense_ranges<<<BCS_GRID1(cells, 256), 0, s>>>(table, keys, count, cells, starts, ends);
+    if (cells > 0) k_dense_ranges<<<BCS_GRID1(cells, 256), 0, s>>>(table, epoch, cells, starts, ends);
+}
+void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s) {
+    if (cells > 0) k_vein_end<<<BCS_GRID1((long long)cells * 32, 256), 0, s>>>(a);
+}
+void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tri, const float4* vpos, float4* box,
+                      cudaStream_t s) {
+    if (T > 0) k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box);
+}
+void launch_wall_mask(const uint32_t* tri, const float4* vpos, int T, const MaskDev& m, unsigned char* mask,
+                      float reach, int* epoch, cudaStream_t s) {
+    k_next_epoch<<<1, 1, 0, s>>>(epoch);
+    if (T > 0) k_wall_mask<<<BCS_GRID1(T, 256), 0, s>>>(tri, vpos, T, m, mask, reach);
 }
 void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
                          int V, float k, float d, unsigned* err, cudaStream_t s) {

@@ -6,7 +6,9 @@
 //   upsweep   per-tile digit histogram (shared-memory atomics), stored
 //             digit-major so one exclusive scan gives every (digit, tile) its
 //             global output offset in stable order;
-//   scan      one CTA scans the digit-major histogram;
+//   scan      one CTA per digit scans that digit's row over the tiles and
+//             records the digit total; the downsweep adds the exclusive scan
+//             of the 256 totals;
 //   downsweep each warp ranks its 16 rounds of 32 consecutive pairs with
 //             __match_any_sync (rank = peers below me + running count of the
 //             digit in this warp), warps are offset by an exclusive scan of
@@ -38,47 +40,66 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const int* __res
     hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = s_hist[threadIdx.x];
 }
 
-// Exclusive scan of `len` unsigned values in place, one CTA of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_exclusive(unsigned* data, int len) {
-    __shared__ unsigned s_part[1024];
-    __shared__ unsigned s_carry;
-    const int per = (len + 1023) / 1024;
-    const int b = threadIdx.x * per;
-    unsigned sum = 0;
-    for (int k = 0; k < per; ++k) {
-        int i = b + k;
-        if (i < len) sum += data[i];
+// Exclusive block scan of one value per thread (256 threads); returns the
+// prefix and leaves the block total in *total.
+__device__ inline unsigned block_scan_256(unsigned v, unsigned* s_warp, unsigned* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    s_part[threadIdx.x] = sum;
+    if (lane == 31) s_warp[warp] = x;
     __syncthreads();
-    // Hillis-Steele inclusive scan over 1024 partials.
-    for (int o = 1; o < 1024; o <<= 1) {
-        unsigned t = threadIdx.x >= (unsigned)o ? s_part[threadIdx.x - o] : 0u;
-        __syncthreads();
-        s_part[threadIdx.x] += t;
-        __syncthreads();
-    }
-    unsigned run = threadIdx.x ? s_part[threadIdx.x - 1] : 0u;
-    for (int k = 0; k < per; ++k) {
-        int i = b + k;
-        if (i < len) {
-            unsigned v = data[i];
-            data[i] = run;
-            run += v;
+    if (threadIdx.x < 32) {
+        unsigned w = threadIdx.x < kSortWarps ? s_warp[threadIdx.x] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (threadIdx.x >= o) w += y;
         }
+        if (threadIdx.x < kSortWarps) s_warp[threadIdx.x] = w;
     }
-    (void)s_carry;
+    __syncthreads();
+    unsigned excl = x - v + (warp ? s_warp[warp - 1] : 0u);
+    *total = s_warp[kSortWarps - 1];
+    __syncthreads();
+    return excl;
+}
+
+// One CTA per digit: exclusive scan of hist[digit][0..ntiles) in place, the
+// row total into totals[digit].
+__global__ void __launch_bounds__(kSortThreads) k_scan_rows(unsigned* hist, int ntiles, unsigned* totals) {
+    __shared__ unsigned s_warp[kSortWarps];
+    unsigned* row = hist + (size_t)blockIdx.x * ntiles;
+    unsigned carry = 0;
+    for (int base = 0; base < ntiles; base += kSortThreads) {
+        const int i = base + threadIdx.x;
+        const unsigned v = i < ntiles ? row[i] : 0u;
+        unsigned tot;
+        const unsigned ex = block_scan_256(v, s_warp, &tot);
+        if (i < ntiles) row[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __restrict__ keys_in,
                                                                   const int* __restrict__ vals_in, int* keys_out,
                                                                   int* vals_out, int n, int shift, int ntiles,
-                                                                  const unsigned* __restrict__ offsets) {
+                                                                  const unsigned* __restrict__ offsets,
+                                                                  const unsigned* __restrict__ totals) {
     __shared__ unsigned s_cnt[kSortWarps][kRadix];
     __shared__ unsigned s_base[kRadix];
+    __shared__ unsigned s_warp[kSortWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int d = lane; d < kRadix; d += 32) s_cnt[warp][d] = 0;
-    s_base[threadIdx.x] = offsets[(size_t)threadIdx.x * ntiles + blockIdx.x];
+    {
+        unsigned tot;
+        const unsigned digit_base = block_scan_256(totals[threadIdx.x], s_warp, &tot);
+        s_base[threadIdx.x] = digit_base + offsets[(size_t)threadIdx.x * ntiles + blockIdx.x];
+    }
     __syncwarp();
     const int wbase = blockIdx.x * kSortTile + warp * (kSortTile / kSortWarps);
     const unsigned lt = (1u << lane) - 1u;
@@ -123,7 +144,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __r
 }
 
 int radix_tiles(int n) { return (n + kSortTile - 1) / kSortTile; }
-size_t radix_temp_words(int n) { return (size_t)kRadix * radix_tiles(n); }
+size_t radix_temp_words(int n) { return (size_t)kRadix * radix_tiles(n) + kRadix; }
 
 // Sort n pairs on `bits` low key bits from (in_k, in_v), which is left
 // untouched, ping-ponging through (a_k, a_v) and (b_k, b_v).  Returns 0 when
@@ -143,9 +164,10 @@ int radix_sort_pairs(const int* in_k, const int* in_v, int* a_k, int* a_v, int* 
         const int* vi = pass == 0 ? in_v : ((pass & 1) ? a_v : b_v);
         int* ko = (pass & 1) ? b_k : a_k;
         int* vo = (pass & 1) ? b_v : a_v;
+        unsigned* totals = temp + (size_t)kRadix * ntiles;
         k_radix_upsweep<<<ntiles, kSortThreads, 0, s>>>(ki, n, shift, ntiles, temp);
-        k_scan_exclusive<<<1, 1024, 0, s>>>(temp, kRadix * ntiles);
-        k_radix_downsweep<<<ntiles, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, shift, ntiles, temp);
+        k_scan_rows<<<kRadix, kSortThreads, 0, s>>>(temp, ntiles, totals);
+        k_radix_downsweep<<<ntiles, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, shift, ntiles, temp, totals);
     }
     return (pass & 1) ? 0 : 1;
 }

@@ -266,6 +266,31 @@ bcs_status bcs_synchronize(bcs_sim* sim);
  * handle's stream; writes milliseconds.  For benchmarking. */
 bcs_status bcs_time_steps(bcs_sim* sim, int nsteps, float* ms_out);
 
+/* Largest object count bcs_grid_sort_static accepts. */
+#define BCS_GRID_SORT_STATIC_MAX 262144
+
+/* Grid keys and their stable sort without allocating device memory.  This
+ * entry point has no counterpart in the reference.  It is for callers that
+ * cannot allocate: a host application that owns the whole device-memory
+ * budget, or a frame loop that must not stall on cudaMalloc / cudaFree
+ * (either can synchronise the device).  It needs no bcs_sim handle.
+ *
+ * x, y, z: device arrays of n positions (cudaVec3 layout).  bounds6: host
+ * array (min_x, max_x, min_y, max_y, min_z, max_z), cell3: host array (cell
+ * width, height, depth) — the values bcs_get_info / bcs_params carry.
+ * cell_ids, object_ids: device outputs of n ints, the sorted keys and the
+ * object ids they carry, equal to what bcs_get_grid returns for the same
+ * positions.  The work is enqueued on `stream` (a cudaStream_t or NULL).
+ *
+ * Scratch lives in a fixed array inside the library (about 2.1 MiB, held by
+ * every device that loads the library until exit); n above
+ * BCS_GRID_SORT_STATIC_MAX returns BCS_ERR_INVALID_ARGUMENT.  The first call
+ * on a device looks up that array's device address (cudaGetSymbolAddress)
+ * with the device current; make that first call before any stream capture.
+ * All calls share the array, so calls that overlap on the GPU race. */
+bcs_status bcs_grid_sort_static(const float* x, const float* y, const float* z, int n, const float* bounds6,
+                                const float* cell3, int* cell_ids, int* object_ids, void* stream);
+
 /* Phases of one frame timed by bcs_profile_steps. */
 enum {
     BCS_PHASE_GRID = 0,         /* key sort + cell ranges                   */

@@ -28,8 +28,9 @@ EXPORTED = [
     "bcs_get_info", "bcs_set_particles", "bcs_get_particles", "bcs_set_vein", "bcs_get_vein",
     "bcs_calculate_grids", "bcs_calculate_next_frame", "bcs_propagate_all", "bcs_step",
     "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
-    "bcs_profile_steps",
+    "bcs_profile_steps", "bcs_grid_sort_static",
 ]
+GRID_SORT_STATIC_MAX = 262144
 PHASES = ("grid", "vein_forces", "particles", "vein_update")
 
 
@@ -135,6 +136,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_synchronize": ([P], C.c_int),
         "bcs_time_steps": ([P, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "bcs_profile_steps": ([P, C.c_int, C.POINTER(C.c_float)], C.c_int),
+        "bcs_grid_sort_static": ([P, P, P, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), P, P, P], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

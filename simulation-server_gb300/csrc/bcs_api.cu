@@ -30,9 +30,7 @@ void launch_dense_ranges(const int4* table, const int* epoch, long long cells, i
                          cudaStream_t s);
 void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s);
 void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tri, const float4* vpos, float4* box,
-                      cudaStream_t s);
-void launch_wall_mask(const uint32_t* tri, const float4* vpos, int T, const MaskDev& m, unsigned char* mask,
-                      float reach, int* epoch, cudaStream_t s);
+                      const MaskDev& m, unsigned char* mask, float reach, int* mask_epoch, cudaStream_t s);
 void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
                          int V, float k, float d, unsigned* err, cudaStream_t s);
 void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt, cudaStream_t s);
@@ -215,10 +213,8 @@ void build_triangle_grid(bcs_sim* s, bool regrid) {
             sort_grid(s->tg, s->stream);
         }
         launch_tri_cache(s->tg.g.ids, s->tri, s->vpos, s->T, s->tcache, s->stream);
-        launch_tri_boxes(s->tg.g.keys, s->tg.g.ids, s->T, s->tri, s->vpos, s->tbox, s->stream);
-        if (s->wall_mask)
-            launch_wall_mask(s->tri, s->vpos, s->T, s->wall, s->wall_mask,
-                             s->p.vein_impact_distance * 1.001f + 1e-3f, s->wall_epoch, s->stream);
+        launch_tri_boxes(s->tg.g.keys, s->tg.g.ids, s->T, s->tri, s->vpos, s->tbox, s->wall, s->wall_mask,
+                         s->p.vein_impact_distance * 1.001f + 1e-3f, s->wall_epoch, s->stream);
     } else {
         launch_tri_cache(nullptr, s->tri, s->vpos, s->T, s->tcache, s->stream);
     }

@@ -3,7 +3,7 @@
 // One frame of the reference (src/main.cu:175-208) becomes, per step:
 //   radix sort of the grid keys (bcs_sort.cu) → k_next_epoch → k_cell_ranges →
 //   k_vein_springs → k_step<kFull> → k_vein_end → k_vein_integrate →
-//   k_tri_cache → k_tri_boxes → k_wall_mask → k_bump_step
+//   k_tri_cache → k_tri_boxes (cell bounds + wall mask) → k_bump_step
 // k_step is cell-major: a CTA owns whole blood cells of one type, stages
 // their positions / velocities / previous forces in shared memory, and does
 // for each particle the work of calculateBloodCellsCenters, gatherForcesKernel,
@@ -17,13 +17,19 @@ namespace bcs {
 
 // ------------------------------------------------------------ physics ----
 // springMassForceWithDampingForParticle + calculateParticlesSpringForceComponent
-// (src/simulation/physics.cuh:24-27,53-77, Heun branch).
+// (src/simulation/physics.cuh:24-27,53-77, Heun branch).  |dP| and dP/|dP|
+// share one square root; normalize(-dP) is -normalize(dP).
 __device__ inline float3 cell_spring(const bcs_params& p, float3 dP, float3 dv, float3 f1, float3 f2, float L,
                                      unsigned& e) {
-    float3 nshift = normalize_or_zero(-1.0f * dP, e);
-    float3 dvv = dv + p.dt * (f1 - f2);
-    float mag = (len3(dP) - L) * p.particle_k_sniff + dot3(normalize_or_zero(dP, e), dvv) * p.particle_d_fact;
-    return mag * nshift;
+    const float len = sqrtf(dot3(dP, dP));
+    float3 n = __frcp_rn(len) * dP;
+    if (isnan(n.x) || isnan(n.y) || isnan(n.z)) {
+        e |= BCS_ERRW_NAN_NORMALIZE;
+        n = f3(0.f, 0.f, 0.f);
+    }
+    const float3 dvv = dv + p.dt * (f1 - f2);
+    const float mag = (len - L) * p.particle_k_sniff + dot3(n, dvv) * p.particle_d_fact;
+    return (-mag) * n;
 }
 
 // accumulateEnvironmentForcesForParticles (physics.cuh:102-120); the
@@ -55,12 +61,18 @@ __device__ inline float3 environment(const StepArgs& a, float3 x, float3 v, floa
     return g - p.viscous_damping * v;
 }
 
-// addResilientForceOnCollision (physics.cuh:133-145) times `intensity`.
+// addResilientForceOnCollision (physics.cuh:133-145) times `intensity`;
+// the direction and the spring term share sqrt(d2).
 __device__ inline float3 resilient(const bcs_params& p, float3 rp, float3 rv, float d2, float radius, float intensity,
                                    unsigned& e) {
-    float3 dir = normalize_or_zero(rp, e);
+    const float d = sqrtf(d2);           // d2 == dot(rp, rp) at every call site
+    float3 dir = __frcp_rn(d) * rp;
+    if (isnan(dir.x) || isnan(dir.y) || isnan(dir.z)) {
+        e |= BCS_ERRW_NAN_NORMALIZE;
+        dir = f3(0.f, 0.f, 0.f);
+    }
     float3 tang = rv - dot3(rv, dir) * dir;
-    float3 spring = (-p.collision_spring_coeff * (radius * 2 - sqrtf(d2))) * dir;
+    float3 spring = (-p.collision_spring_coeff * (radius * 2 - d)) * dir;
     float3 damp = p.collision_damping_coeff * rv;
     float3 shear = p.collision_shear_coeff * tang;
     return intensity * (spring + damp + shear);
@@ -167,18 +179,18 @@ __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 
 }
 
 // Parametric entry of the ray o + t d (t >= 0) into an axis-aligned box, or
-// a value above `limit` when the ray misses it.
-__device__ inline float ray_box_entry(float3 o, float3 d, float4 lo, float4 hi) {
+// 3e38 when the ray misses it.  inv holds 1/d (components with |d| < 1e-30
+// are treated as parallel to that slab).
+__device__ inline float ray_box_entry(float3 o, float3 d, float3 inv, float4 lo, float4 hi) {
     float t0 = 0.f, t1 = 3.0e38f;
-    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z}, ii[3] = {inv.x, inv.y, inv.z};
     const float ll[3] = {lo.x, lo.y, lo.z}, hh[3] = {hi.x, hi.y, hi.z};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         if (fabsf(dd[k]) < 1e-30f) {
             if (oo[k] < ll[k] || oo[k] > hh[k]) return 3.0e38f;
         } else {
-            float inv = 1.0f / dd[k];
-            float ta = (ll[k] - oo[k]) * inv, tb = (hh[k] - oo[k]) * inv;
+            const float ta = (ll[k] - oo[k]) * ii[k], tb = (hh[k] - oo[k]) * ii[k];
             t0 = fmaxf(t0, fminf(ta, tb));
             t1 = fminf(t1, fmaxf(ta, tb));
         }
@@ -239,7 +251,10 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
         stencil_range_u(yId, g.cy, y0, y1);
         stencil_range_u(zId, g.cz, z0, z1);
         const long long cxy = (long long)g.cx * g.cy;
-        // Pass 1: stencil position of the last cell the ray enters within reach.
+        // Pass 1: which stencil cells the ray enters (bit k, in stencil
+        // order) and the last one it enters within reach.
+        const float3 inv = f3(__frcp_rn(dir.x), __frcp_rn(dir.y), __frcp_rn(dir.z));
+        unsigned live = 0u;
         int last_near = -1, k = 0;
         for (int dx = x0; dx <= x1; ++dx)
             for (int dy = y0; dy <= y1; ++dy)
@@ -247,22 +262,29 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
                     const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
                     int f, l;
                     if (!cell_range(g, ep, c, f, l)) continue;
-                    if (ray_box_entry(x, dir, __ldg(&a.tbox[2 * c]), __ldg(&a.tbox[2 * c + 1])) <= reach) last_near = k;
+                    const float te = ray_box_entry(x, dir, inv, __ldg(&a.tbox[2 * c]), __ldg(&a.tbox[2 * c + 1]));
+                    if (te > 2.9e38f) continue;
+                    live |= 1u << k;
+                    if (te <= reach) last_near = k;
                 }
-        // Pass 2: triangles of the cells the ray enters, in stencil order.
-        bool found = false;
-        k = 0;
-        for (int dx = x0; dx <= x1 && !found; ++dx)
-            for (int dy = y0; dy <= y1 && !found; ++dy)
-                for (int dz = z0; dz <= z1 && !found; ++dz, ++k) {
-                    if (k > last_near) { found = true; break; }
-                    const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
-                    int f, l;
-                    if (!cell_range(g, ep, c, f, l)) continue;
-                    if (ray_box_entry(x, dir, __ldg(&a.tbox[2 * c]), __ldg(&a.tbox[2 * c + 1])) > 2.9e38f) continue;
-                    for (int s = f; s <= l; ++s)
-                        if (test_slot(s)) { found = true; break; }
-                }
+        // Pass 2: triangles of the entered cells up to the last one in reach,
+        // in stencil order.
+        if (last_near >= 0) live &= (last_near >= 31) ? 0xffffffffu : ((2u << last_near) - 1u);
+        else live = 0u;
+        const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
+        while (live) {
+            const int kk = __ffs(live) - 1;
+            live &= live - 1u;
+            const int dz = z0 + kk % nz, dy = y0 + (kk / nz) % ny, dx = x0 + kk / (nz * ny);
+            (void)nx;
+            const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
+            int f, l;
+            if (!cell_range(g, ep, c, f, l)) continue;
+            bool found = false;
+            for (int s2 = f; s2 <= l; ++s2)
+                if (test_slot(s2)) { found = true; break; }
+            if (found) break;
+        }
     }
     if (obj < 0) return;
     float3 rel = x - (x + t * dir);
@@ -492,16 +514,16 @@ __global__ void k_tri_keys(const float4* __restrict__ vpos, const uint32_t* __re
 __global__ void k_next_epoch(int* epoch) { *epoch += 1; }
 
 // calculateStartAndEndOfCellKernel (uniform_grid.cu:51-80), written into
-// the epoch-stamped table: (first, last, epoch) of every occupied cell.
+// the epoch-stamped table: the first slot of each occupied cell scans to its
+// last slot and stores (first, last, epoch) at once.
 __global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int k = keys[i];
-    if (i == 0 || keys[i - 1] != k) {
-        table[k].x = i;
-        table[k].z = *epoch;
-    }
-    if (i == n - 1 || keys[i + 1] != k) table[k].y = i;
+    if (i > 0 && keys[i - 1] == k) return;
+    int j = i;
+    while (j + 1 < n && keys[j + 1] == k) ++j;
+    table[k] = make_int4(i, j, *epoch, 0);
 }
 
 // Dense starts/ends (empty = 0, -1) from the epoch-stamped table, for getters.
@@ -567,9 +589,12 @@ __global__ void k_tri_cache(const int* __restrict__ ids, const uint32_t* __restr
 
 // Bounds of each occupied triangle-grid cell's triangles (from the exact
 // vertex positions), widened by a margin that covers FP32 rounding in the
-// ray-box test.
+// ray-box test.  With a wall mask, every mask cell that meets those bounds
+// widened by `reach` gets the current mark: a particle in an unmarked mask
+// cell is farther than `reach` from every triangle.
 __global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict__ ids, int T,
-                            const uint32_t* __restrict__ tri, const float4* __restrict__ vpos, float4* box) {
+                            const uint32_t* __restrict__ tri, const float4* __restrict__ vpos, float4* box,
+                            MaskDev m, unsigned char* mask, float reach) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= T) return;
     const int k = keys[s];
@@ -583,31 +608,23 @@ __global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict_
             hi = f3(fmaxf(hi.x, q.x), fmaxf(hi.y, q.y), fmaxf(hi.z, q.z));
         }
     }
-    const float m = 1e-3f + 1e-5f * fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fmaxf(fabsf(lo.y), fabsf(hi.y)),
-                                                                         fmaxf(fabsf(lo.z), fabsf(hi.z))));
-    box[2 * (size_t)k] = make_float4(lo.x - m, lo.y - m, lo.z - m, 0.f);
-    box[2 * (size_t)k + 1] = make_float4(hi.x + m, hi.y + m, hi.z + m, 0.f);
-}
-
-// Wall-proximity mask: every mask cell that meets a triangle's bounds
-// widened by `reach` gets the current mark.  A particle in an unmarked cell
-// is farther than `reach` from every triangle.
-__global__ void k_wall_mask(const uint32_t* __restrict__ tri, const float4* __restrict__ vpos, int T, MaskDev m,
-                            unsigned char* mask, float reach) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= T) return;
-    float3 a = xyz(vpos[tri[3 * t]]), b = xyz(vpos[tri[3 * t + 1]]), c = xyz(vpos[tri[3 * t + 2]]);
-    float3 lo = f3(fminf(fminf(a.x, b.x), c.x) - reach, fminf(fminf(a.y, b.y), c.y) - reach,
-                   fminf(fminf(a.z, b.z), c.z) - reach);
-    float3 hi = f3(fmaxf(fmaxf(a.x, b.x), c.x) + reach, fmaxf(fmaxf(a.y, b.y), c.y) + reach,
-                   fmaxf(fmaxf(a.z, b.z), c.z) + reach);
-    int x0 = max(0, (int)floorf((lo.x - m.lo[0]) * m.inv_cell)), x1 = min(m.nx - 1, (int)floorf((hi.x - m.lo[0]) * m.inv_cell));
-    int y0 = max(0, (int)floorf((lo.y - m.lo[1]) * m.inv_cell)), y1 = min(m.ny - 1, (int)floorf((hi.y - m.lo[1]) * m.inv_cell));
-    int z0 = max(0, (int)floorf((lo.z - m.lo[2]) * m.inv_cell)), z1 = min(m.nz - 1, (int)floorf((hi.z - m.lo[2]) * m.inv_cell));
+    const float mg = 1e-3f + 1e-5f * fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fabsf(lo.y), fabsf(hi.y))),
+                                           fmaxf(fabsf(lo.z), fabsf(hi.z)));
+    lo = f3(lo.x - mg, lo.y - mg, lo.z - mg);
+    hi = f3(hi.x + mg, hi.y + mg, hi.z + mg);
+    box[2 * (size_t)k] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    box[2 * (size_t)k + 1] = make_float4(hi.x, hi.y, hi.z, 0.f);
+    if (!mask) return;
+    const int x0 = max(0, (int)floorf((lo.x - reach - m.lo[0]) * m.inv_cell));
+    const int x1 = min(m.nx - 1, (int)floorf((hi.x + reach - m.lo[0]) * m.inv_cell));
+    const int y0 = max(0, (int)floorf((lo.y - reach - m.lo[1]) * m.inv_cell));
+    const int y1 = min(m.ny - 1, (int)floorf((hi.y + reach - m.lo[1]) * m.inv_cell));
+    const int z0 = max(0, (int)floorf((lo.z - reach - m.lo[2]) * m.inv_cell));
+    const int z1 = min(m.nz - 1, (int)floorf((hi.z + reach - m.lo[2]) * m.inv_cell));
     const unsigned char mark = (unsigned char)*m.epoch;
     for (int z = z0; z <= z1; ++z)
         for (int y = y0; y <= y1; ++y)
-            for (int x = x0; x <= x1; ++x) mask[((long long)z * m.ny + y) * m.nx + x] = mark;
+            for (int xx = x0; xx <= x1; ++xx) mask[((long long)z * m.ny + y) * m.nx + xx] = mark;
 }
 
 __global__ void k_bump_step(long long* steps) { *steps += 1; }
@@ -680,13 +697,9 @@ void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s) {
     if (cells > 0) k_vein_end<<<BCS_GRID1((long long)cells * 32, 256), 0, s>>>(a);
 }
 void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tri, const float4* vpos, float4* box,
-                      cudaStream_t s) {
-    if (T > 0) k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box);
-}
-void launch_wall_mask(const uint32_t* tri, const float4* vpos, int T, const MaskDev& m, unsigned char* mask,
-                      float reach, int* epoch, cudaStream_t s) {
-    k_next_epoch<<<1, 1, 0, s>>>(epoch);
-    if (T > 0) k_wall_mask<<<BCS_GRID1(T, 256), 0, s>>>(tri, vpos, T, m, mask, reach);
+                      const MaskDev& m, unsigned char* mask, float reach, int* mask_epoch, cudaStream_t s) {
+    if (mask) k_next_epoch<<<1, 1, 0, s>>>(mask_epoch);
+    if (T > 0) k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box, m, mask, reach);
 }
 void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
                          int V, float k, float d, unsigned* err, cudaStream_t s) {

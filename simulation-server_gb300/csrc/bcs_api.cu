@@ -45,6 +45,18 @@ void launch_unpack(const float4* in, int n, float* x, float* y, float* z, cudaSt
 int radix_sort_pairs(const int* in_k, const int* in_v, int* a_k, int* a_v, int* b_k, int* b_v, int n, int bits,
                      unsigned* temp, cudaStream_t s);
 size_t radix_temp_words(int n);
+int radix_tiles(int n);
+struct IncrementalBuffers {
+    int* kept_k; int* kept_v;
+    int* mov_k; int* mov_v;
+    int* t1_k; int* t1_v;
+    int* t2_k; int* t2_v;
+    unsigned* tile_kept;
+    unsigned* temp;
+    int* movers;
+};
+void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_key_of, int* out_k, int* out_v, int n,
+                           int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s);
 }  // namespace bcs
 
 using namespace bcs;
@@ -55,14 +67,17 @@ struct DeviceGrid {
     GridDev g{};           // geometry + pointers to the sorted result
     int* in_k = nullptr;   // unsorted keys / ids (written by the key kernels)
     int* in_v = nullptr;
-    int* a_k = nullptr;
-    int* a_v = nullptr;
-    int* b_k = nullptr;
-    int* b_v = nullptr;
+    int* s_k[2] = {nullptr, nullptr};   // sorted results, alternating per build
+    int* s_v[2] = {nullptr, nullptr};
+    int slot = 0;          // s_*[slot] holds the current sorted result
+    bool sorted_once = false;
+    bool incremental = false;           // rebuild from the previous order
+    IncrementalBuffers inc{};
     int4* table = nullptr;
     int* epoch = nullptr;
     unsigned* temp = nullptr;
     int bits = 0;
+    int id_bits = 0;
     int count = 0;
 };
 
@@ -114,7 +129,7 @@ struct bcs_sim {
     long long host_steps = 0;
     unsigned* err = nullptr;
     StepArgs args{};
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};   // by (cur, sorted slot)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t pev[BCS_PHASE_COUNT + 1] = {};
     float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
@@ -158,14 +173,27 @@ int bits_for(long long cells) {
     return b;
 }
 
-bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count) {
+bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
     dg.count = count;
     dg.g.count = count;
+    dg.incremental = incremental;
     bcs_status st;
-    if ((st = dalloc(s, &dg.in_k, count)) || (st = dalloc(s, &dg.in_v, count)) || (st = dalloc(s, &dg.a_k, count)) ||
-        (st = dalloc(s, &dg.a_v, count)) || (st = dalloc(s, &dg.b_k, count)) || (st = dalloc(s, &dg.b_v, count)) ||
+    if ((st = dalloc(s, &dg.in_k, count)) || (st = dalloc(s, &dg.in_v, count)) ||
+        (st = dalloc(s, &dg.s_k[0], count)) || (st = dalloc(s, &dg.s_v[0], count)) ||
+        (st = dalloc(s, &dg.s_k[1], count)) || (st = dalloc(s, &dg.s_v[1], count)) ||
+        (st = dalloc(s, &dg.inc.t1_k, count)) || (st = dalloc(s, &dg.inc.t1_v, count)) ||
         (st = dalloc(s, &dg.temp, radix_temp_words(count))))
         return st;
+    dg.inc.temp = dg.temp;
+    if (incremental &&
+        ((st = dalloc(s, &dg.inc.kept_k, count)) || (st = dalloc(s, &dg.inc.kept_v, count)) ||
+         (st = dalloc(s, &dg.inc.mov_k, count)) || (st = dalloc(s, &dg.inc.mov_v, count)) ||
+         (st = dalloc(s, &dg.inc.t2_k, count)) || (st = dalloc(s, &dg.inc.t2_v, count)) ||
+         (st = dalloc(s, &dg.inc.tile_kept, radix_tiles(count))) || (st = dalloc(s, &dg.inc.movers, 1))))
+        return st;
+    int idb = 0;
+    while (idb < 31 && (1LL << idb) < count) ++idb;
+    dg.id_bits = idb;
     if ((st = dalloc(s, &dg.epoch, 1))) return st;
     BCS_CUDA(cudaMemset(dg.epoch, 0, sizeof(int)));
     dg.g.epoch = dg.epoch;
@@ -177,11 +205,28 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count) {
     return BCS_OK;
 }
 
-// Sort the grid's unsorted keys and rebuild its validated range table.
+// Sort the grid's unsorted keys into the other result slot and rebuild the
+// range table.  After the first build, a grid flagged incremental starts
+// from the previous order (any permutation works; few movers make it cheap).
 void sort_grid(DeviceGrid& dg, cudaStream_t st) {
-    int which = radix_sort_pairs(dg.in_k, dg.in_v, dg.a_k, dg.a_v, dg.b_k, dg.b_v, dg.count, dg.bits, dg.temp, st);
-    dg.g.keys = which ? dg.b_k : dg.a_k;
-    dg.g.ids = which ? dg.b_v : dg.a_v;
+    const int out = dg.slot ^ 1;
+    if (dg.incremental && dg.sorted_once) {
+        sort_grid_incremental(dg.s_k[dg.slot], dg.s_v[dg.slot], dg.in_k, dg.s_k[out], dg.s_v[out], dg.count, dg.bits,
+                              dg.id_bits, dg.inc, st);
+    } else {
+        // the full sort's result lands in its first ping-pong buffer after an
+        // odd number of passes (or none), in the second after an even number
+        const int passes = (dg.bits + 7) / 8;
+        const bool first = passes == 0 || dg.count <= 1 || (passes & 1);
+        int which = radix_sort_pairs(dg.in_k, dg.in_v, first ? dg.s_k[out] : dg.inc.t1_k,
+                                     first ? dg.s_v[out] : dg.inc.t1_v, first ? dg.inc.t1_k : dg.s_k[out],
+                                     first ? dg.inc.t1_v : dg.s_v[out], dg.count, dg.bits, dg.temp, st);
+        (void)which;
+    }
+    dg.slot = out;
+    dg.sorted_once = true;
+    dg.g.keys = dg.s_k[dg.slot];
+    dg.g.ids = dg.s_v[dg.slot];
     dg.g.table = dg.table;
     launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, st);
 }
@@ -463,7 +508,7 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
         return st;
     BCS_CUDA(cudaMemset(s->vvel, 0, sizeof(float4) * s->V));
     BCS_CUDA(cudaMemset(s->vfrc, 0, sizeof(float4) * s->V));
-    if ((st = alloc_grid(s, s->pg, s->N)) || (st = alloc_grid(s, s->tg, std::max(1, s->T)))) return st;
+    if ((st = alloc_grid(s, s->pg, s->N, true)) || (st = alloc_grid(s, s->tg, std::max(1, s->T), false))) return st;
     s->tg.count = s->T;
     s->tg.g.count = s->T;
     if (s->tg.g.uniform) {
@@ -775,15 +820,17 @@ static bcs_status run_steps(bcs_sim* s, int n) {
             enqueue_frame(s);
             continue;
         }
-        cudaGraphExec_t& g = s->graph[s->cur];
+        cudaGraphExec_t& g = s->graph[s->cur * 2 + s->pg.slot];
         if (!g) {
             const int cur0 = s->cur;
+            const int slot0 = s->pg.slot;
             const long long hs = s->host_steps;
             cudaGraph_t graph = nullptr;
             BCS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
             enqueue_frame(s);
             cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
             s->cur = cur0;
+            s->pg.slot = slot0;
             s->host_steps = hs;
             if (ce != cudaSuccess) return BCS_ERR_CUDA;
             {
@@ -803,9 +850,11 @@ static bcs_status run_steps(bcs_sim* s, int n) {
             if (ce != cudaSuccess) { g = nullptr; return BCS_ERR_CUDA; }
         }
         BCS_CUDA(cudaGraphLaunch(g, s->stream));
-        // A replay is one whole enqueue_frame: mirror its host-side state
-        // (the sorted-grid pointers it set during capture do not change).
+        // A replay is one whole enqueue_frame: mirror its host-side state.
         s->cur ^= 1;
+        s->pg.slot ^= 1;
+        s->pg.g.keys = s->pg.s_k[s->pg.slot];
+        s->pg.g.ids = s->pg.s_v[s->pg.slot];
         s->keys_valid = true;
         s->grid_ready = true;
         ++s->host_steps;

@@ -250,3 +250,37 @@ def test_error_word_and_render_export(lib, tiny):
     np.testing.assert_array_equal(pv[:, 3:], 0)
     np.testing.assert_array_equal(po, pos)
     np.testing.assert_array_equal(vv[:, :3], sim.get_vein()[0])
+
+
+def test_incremental_grid_every_frame(lib):
+    # Fused frames rebuild the grid from the previous frame's order; each
+    # frame's grid must equal the oracle's grid of that frame's start positions
+    # (respawns included: cells start near the outlet and move fast).
+    sc = S.straight_scene(cells=48, seed=13, radius=14.0, length=90.0, around=32, rings=40)
+    sc.velocities[:] = np.random.default_rng(8).normal(0, 30.0, sc.velocities.shape).astype(np.float32)
+    sc.velocities[:, 1] -= 60.0
+    sim = make(sc)
+    o = O.OracleSim(sc)
+    for _ in range(12):
+        pos, _, _ = sim.get_particles()
+        sim.step(1)
+        k, i, _, _ = sim.get_grid(0, dense=False)
+        ok, oi, _, _, _ = o.grid_of_points(pos)
+        np.testing.assert_array_equal(k, ok)
+        np.testing.assert_array_equal(i, oi)
+
+
+def test_incremental_grid_after_reshuffle(lib, small):
+    # Every particle changes cell: the incremental path sorts all of them.
+    sim = make(small)
+    sim.step(3)
+    rng = np.random.default_rng(3)
+    pos = small.positions[rng.permutation(len(small.positions))]
+    sim.set_particles(pos, np.zeros_like(pos))
+    sim.calculate_grids()
+    k, i, st, en = sim.get_grid(0)
+    ok, oi, ost, oen, _ = O.OracleSim(small).grid_of_points(pos, dense=True)
+    np.testing.assert_array_equal(k, ok)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(st, ost)
+    np.testing.assert_array_equal(en, oen)

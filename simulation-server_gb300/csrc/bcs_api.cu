@@ -30,7 +30,8 @@ void launch_dense_ranges(const int4* table, const int* epoch, long long cells, i
                          cudaStream_t s);
 void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s);
 void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tri, const float4* vpos, float4* box,
-                      const MaskDev& m, unsigned char* mask, float reach, int* mask_epoch, cudaStream_t s);
+                      const MaskDev& m, unsigned char* mask, float reach, int* mask_epoch, float margin,
+                      float* disp2, float4* vref, int V, cudaStream_t s);
 void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
                          int V, float k, float d, unsigned* err, cudaStream_t s);
 void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt, cudaStream_t s);
@@ -56,7 +57,10 @@ struct IncrementalBuffers {
     int* movers;
 };
 void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_key_of, int* out_k, int* out_v, int n,
-                           int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s);
+                           int key_bits, int id_bits, const IncrementalBuffers& b, const float4* pos,
+                           const float4* vel, float4* spos, float4* svel, cudaStream_t s);
+void launch_reorder(const int* ids, int n, const float4* pos, const float4* vel, float4* spos, float4* svel,
+                    cudaStream_t s);
 }  // namespace bcs
 
 using namespace bcs;
@@ -76,6 +80,8 @@ struct DeviceGrid {
     int4* table = nullptr;
     int* epoch = nullptr;
     unsigned* temp = nullptr;
+    float4* spos = nullptr;              // state in sorted order (particle grid)
+    float4* svel = nullptr;
     int bits = 0;
     int id_bits = 0;
     int count = 0;
@@ -121,6 +127,8 @@ struct bcs_sim {
     unsigned char* wall_mask = nullptr;
     int* wall_epoch = nullptr;
     MaskDev wall{};
+    float* wall_disp2 = nullptr;     // dynamic wall: max squared vertex move since the last bounds build
+    float4* wall_ref = nullptr;      // vein positions at that build
     // grids
     DeviceGrid pg, tg;
     float minX, maxX, minY, maxY, minZ, maxZ, width, height, depth;
@@ -137,6 +145,11 @@ struct bcs_sim {
 };
 
 namespace {
+
+// A dynamic wall's triangle bounds and wall mask are rebuilt only when some
+// vertex has moved more than this since the last build; they carry it as
+// extra width, so they always contain the current triangles.
+constexpr float kWallMargin = 0.5f;
 
 #define BCS_CUDA(call)                                          \
     do {                                                        \
@@ -208,25 +221,30 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
 // Sort the grid's unsorted keys into the other result slot and rebuild the
 // range table.  After the first build, a grid flagged incremental starts
 // from the previous order (any permutation works; few movers make it cheap).
-void sort_grid(DeviceGrid& dg, cudaStream_t st) {
+// With pos/vel (particle grid) the state is also written in sorted order.
+void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, const float4* vel = nullptr) {
     const int out = dg.slot ^ 1;
+    const bool with_state = pos && dg.spos;
     if (dg.incremental && dg.sorted_once) {
         sort_grid_incremental(dg.s_k[dg.slot], dg.s_v[dg.slot], dg.in_k, dg.s_k[out], dg.s_v[out], dg.count, dg.bits,
-                              dg.id_bits, dg.inc, st);
+                              dg.id_bits, dg.inc, with_state ? pos : nullptr, vel, with_state ? dg.spos : nullptr,
+                              dg.svel, st);
     } else {
         // the full sort's result lands in its first ping-pong buffer after an
         // odd number of passes (or none), in the second after an even number
         const int passes = (dg.bits + 7) / 8;
         const bool first = passes == 0 || dg.count <= 1 || (passes & 1);
-        int which = radix_sort_pairs(dg.in_k, dg.in_v, first ? dg.s_k[out] : dg.inc.t1_k,
-                                     first ? dg.s_v[out] : dg.inc.t1_v, first ? dg.inc.t1_k : dg.s_k[out],
-                                     first ? dg.inc.t1_v : dg.s_v[out], dg.count, dg.bits, dg.temp, st);
-        (void)which;
+        radix_sort_pairs(dg.in_k, dg.in_v, first ? dg.s_k[out] : dg.inc.t1_k, first ? dg.s_v[out] : dg.inc.t1_v,
+                         first ? dg.inc.t1_k : dg.s_k[out], first ? dg.inc.t1_v : dg.s_v[out], dg.count, dg.bits,
+                         dg.temp, st);
+        if (with_state) launch_reorder(dg.s_v[out], dg.count, pos, vel, dg.spos, dg.svel, st);
     }
     dg.slot = out;
     dg.sorted_once = true;
     dg.g.keys = dg.s_k[dg.slot];
     dg.g.ids = dg.s_v[dg.slot];
+    dg.g.spos = dg.spos;
+    dg.g.svel = dg.svel;
     dg.g.table = dg.table;
     launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, st);
 }
@@ -259,7 +277,8 @@ void build_triangle_grid(bcs_sim* s, bool regrid) {
         }
         launch_tri_cache(s->tg.g.ids, s->tri, s->vpos, s->T, s->tcache, s->stream);
         launch_tri_boxes(s->tg.g.keys, s->tg.g.ids, s->T, s->tri, s->vpos, s->tbox, s->wall, s->wall_mask,
-                         s->p.vein_impact_distance * 1.001f + 1e-3f, s->wall_epoch, s->stream);
+                         s->p.vein_impact_distance * 1.001f + 1e-3f, s->wall_epoch,
+                         s->wall_disp2 ? kWallMargin : 0.0f, s->wall_disp2, s->wall_ref, s->V, s->stream);
     } else {
         launch_tri_cache(nullptr, s->tri, s->vpos, s->T, s->tcache, s->stream);
     }
@@ -271,7 +290,7 @@ void enqueue_grids(bcs_sim* s) {
         launch_keys(s->pos[s->cur], s->N, s->pg.g, s->pg.in_k, s->pg.in_v, s->err, s->stream);
         s->keys_valid = true;
     }
-    if (s->pg.g.uniform) sort_grid(s->pg, s->stream);
+    if (s->pg.g.uniform) sort_grid(s->pg, s->stream, s->pos[s->cur], s->vel[s->cur]);
     if (s->p.refresh_triangle_centers) build_triangle_grid(s, true);
     s->grid_ready = true;
 }
@@ -511,8 +530,16 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
     if ((st = alloc_grid(s, s->pg, s->N, true)) || (st = alloc_grid(s, s->tg, std::max(1, s->T), false))) return st;
     s->tg.count = s->T;
     s->tg.g.count = s->T;
+    if (s->pg.g.uniform) {
+        if ((st = dalloc(s, &s->pg.spos, s->N)) || (st = dalloc(s, &s->pg.svel, s->N))) return st;
+    }
     if (s->tg.g.uniform) {
         if ((st = dalloc(s, &s->tbox, 2 * (size_t)s->tg.g.cells))) return st;
+        if (s->p.vein_dynamic && s->T > 0) {
+            if ((st = dalloc(s, &s->wall_disp2, 1)) || (st = dalloc(s, &s->wall_ref, s->V))) return st;
+            const float huge = 3.0e38f;
+            BCS_CUDA(cudaMemcpy(s->wall_disp2, &huge, sizeof(float), cudaMemcpyHostToDevice));
+        }
         // Wall-proximity mask, cells of half the impact distance (1..8).
         const float mc = std::min(8.0f, std::max(1.0f, s->p.vein_impact_distance * 0.5f));
         MaskDev& m = s->wall;
@@ -769,6 +796,10 @@ bcs_status bcs_set_vein(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs
     bcs_status st;
     if (!bad_vec(positions)) {
         if ((st = set_vec(s, positions, s->V, s->vpos, nullptr, where))) return st;
+        if (s->wall_disp2) {
+            const float huge = 3.0e38f;   // force a bounds / mask rebuild
+            BCS_CUDA(cudaMemcpyAsync(s->wall_disp2, &huge, sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        }
         build_triangle_grid(s, s->p.refresh_triangle_centers != 0);
     }
     if (!bad_vec(velocities) && (st = set_vec(s, velocities, s->V, s->vvel, nullptr, where))) return st;

@@ -22,8 +22,12 @@
 //   tcache                   3 float4 per sorted triangle slot: (v0, id),
 //                            (v1 - v0), (v2 - v0) — the Moller-Trumbore
 //                            operands, streamed contiguously per grid cell.
+//   spos, svel               float4 x N: x and v in sorted-slot order, written
+//                            with the sort, so a collision candidate is one
+//                            load from a contiguous run instead of id -> state
 //   tbox                     2 float4 per triangle-grid cell: bounds of the
-//                            cell's triangles (slightly widened), for ray culling
+//                            cell's triangles widened by the rebuild margin,
+//                            for ray culling
 //   wall_mask                uint8 per wall-mask cell: the mask epoch where a
 //                            triangle lies within vein_impact_distance of the cell
 #pragma once
@@ -65,6 +69,8 @@ struct GridDev {
     long long cells;
     const int* keys;      // sorted keys
     const int* ids;       // sorted object ids
+    const float4* spos;   // particle positions in sorted-slot order (particle grid)
+    const float4* svel;   // particle velocities in sorted-slot order
     const int4* table;    // (first, last, epoch) per cell
     const int* epoch;     // current epoch of the table
     int count;            // objects

@@ -135,19 +135,24 @@ __device__ inline unsigned to_u32_sat(float t) { return t <= 0.f ? 0u : (t >= 42
 __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 x, float3 v, float R, unsigned& e) {
     float3 acc = f3(0.f, 0.f, 0.f);
     const GridDev& g = a.pg;
-    auto test = [&](int q) {
-        float4 pq = __ldg(&a.pos_in[q]);
+    // The reference skips q == p and pairs closer than 0.01 (d^2 < 1e-4);
+    // the particle itself (d^2 = 0) falls under the second rule, so a
+    // candidate needs no id.
+    auto contact = [&](float4 pq, float4 vq) {
         float3 rp = x - xyz(pq);
         float d2 = dot3(rp, rp);
         float md = R + pq.w;
-        if (d2 <= md * md && d2 >= 0.0001f) {
-            float3 rv = v - xyz(__ldg(&a.vel_in[q]));
-            acc = acc + resilient(a.p, rp, rv, d2, R, 0.5f, e);
-        }
+        if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(vq), d2, R, 0.5f, e);
     };
     if (!g.uniform) {
-        for (int q = 0; q < a.n; ++q)
-            if (q != pid) test(q);
+        for (int q = 0; q < a.n; ++q) {
+            if (q == pid) continue;
+            const float4 pq = __ldg(&a.pos_in[q]);
+            float3 rp = x - xyz(pq);
+            float d2 = dot3(rp, rp);
+            float md = R + pq.w;
+            if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[q])), d2, R, 0.5f, e);
+        }
         return acc;
     }
     unsigned dummy = 0;
@@ -171,8 +176,12 @@ __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 
                     last = l;
                 }
             for (int j = first; j <= last; ++j) {
-                int q = __ldg(&g.ids[j]);
-                if (q != pid) test(q);
+                const float4 pq = __ldg(&g.spos[j]);
+                float3 rp = x - xyz(pq);
+                float d2 = dot3(rp, rp);
+                float md = R + pq.w;
+                if (d2 <= md * md && d2 >= 0.0001f)
+                    acc = acc + resilient(a.p, rp, v - xyz(__ldg(&g.svel[j])), d2, R, 0.5f, e);
             }
         }
     return acc;
@@ -276,8 +285,7 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
             const int kk = __ffs(live) - 1;
             live &= live - 1u;
             const int dz = z0 + kk % nz, dy = y0 + (kk / nz) % ny, dx = x0 + kk / (nz * ny);
-            (void)nx;
-            const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
+                    const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
             int f, l;
             if (!cell_range(g, ep, c, f, l)) continue;
             bool found = false;
@@ -594,9 +602,11 @@ __global__ void k_tri_cache(const int* __restrict__ ids, const uint32_t* __restr
 // cell is farther than `reach` from every triangle.
 __global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict__ ids, int T,
                             const uint32_t* __restrict__ tri, const float4* __restrict__ vpos, float4* box,
-                            MaskDev m, unsigned char* mask, float reach) {
+                            MaskDev m, unsigned char* mask, float reach, float margin,
+                            const float* __restrict__ disp2) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= T) return;
+    if (disp2 && *disp2 <= margin * margin) return;   // the last build still covers the wall
     const int k = keys[s];
     if (s > 0 && keys[s - 1] == k) return;
     float3 lo = f3(3.0e38f, 3.0e38f, 3.0e38f), hi = f3(-3.0e38f, -3.0e38f, -3.0e38f);
@@ -608,8 +618,8 @@ __global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict_
             hi = f3(fmaxf(hi.x, q.x), fmaxf(hi.y, q.y), fmaxf(hi.z, q.z));
         }
     }
-    const float mg = 1e-3f + 1e-5f * fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fabsf(lo.y), fabsf(hi.y))),
-                                           fmaxf(fabsf(lo.z), fabsf(hi.z)));
+    const float mg = margin + 1e-3f + 1e-5f * fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fabsf(lo.y), fabsf(hi.y))),
+                                                    fmaxf(fabsf(lo.z), fabsf(hi.z)));
     lo = f3(lo.x - mg, lo.y - mg, lo.z - mg);
     hi = f3(hi.x + mg, hi.y + mg, hi.z + mg);
     box[2 * (size_t)k] = make_float4(lo.x, lo.y, lo.z, 0.f);
@@ -625,6 +635,34 @@ __global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict_
     for (int z = z0; z <= z1; ++z)
         for (int y = y0; y <= y1; ++y)
             for (int xx = x0; xx <= x1; ++xx) mask[((long long)z * m.ny + y) * m.nx + xx] = mark;
+}
+
+// Largest squared displacement of any vein vertex since the last bounds
+// build (as the int bits of a non-negative float, so atomicMax orders it).
+__global__ void k_vein_disp(const float4* __restrict__ vpos, const float4* __restrict__ ref, int V, float* disp2) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d = 0.f;
+    if (i < V) {
+        const float3 a = xyz(vpos[i]), b = xyz(ref[i]);
+        d = dot3(a - b, a - b);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+    if ((threadIdx.x & 31) == 0 && d > 0.f) atomicMax(reinterpret_cast<int*>(disp2), __float_as_int(d));
+}
+
+// After a rebuild: the current vein positions become the reference.
+__global__ void k_vein_snapshot(const float4* __restrict__ vpos, float4* ref, int V, const float* disp2, float margin) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < V && *disp2 > margin * margin) ref[i] = vpos[i];
+}
+
+__global__ void k_disp_reset(float* disp2, float margin) {
+    if (*disp2 > margin * margin) *disp2 = 0.f;
+}
+
+__global__ void k_next_epoch_if(int* epoch, const float* disp2, float margin) {
+    if (!disp2 || *disp2 > margin * margin) *epoch += 1;
 }
 
 __global__ void k_bump_step(long long* steps) { *steps += 1; }
@@ -696,10 +734,19 @@ void launch_dense_ranges(const int4* table, const int* epoch, long long cells, i
 void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s) {
     if (cells > 0) k_vein_end<<<BCS_GRID1((long long)cells * 32, 256), 0, s>>>(a);
 }
+// Triangle bounds + wall mask.  With disp2 (dynamic wall) the build runs
+// only when a vertex moved more than `margin` since the last one, and the
+// bounds carry that margin.
 void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tri, const float4* vpos, float4* box,
-                      const MaskDev& m, unsigned char* mask, float reach, int* mask_epoch, cudaStream_t s) {
-    if (mask) k_next_epoch<<<1, 1, 0, s>>>(mask_epoch);
-    if (T > 0) k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box, m, mask, reach);
+                      const MaskDev& m, unsigned char* mask, float reach, int* mask_epoch, float margin,
+                      float* disp2, float4* vref, int V, cudaStream_t s) {
+    if (disp2) k_vein_disp<<<BCS_GRID1(V, 256), 0, s>>>(vpos, vref, V, disp2);
+    if (mask) k_next_epoch_if<<<1, 1, 0, s>>>(mask_epoch, disp2, margin);
+    if (T > 0) k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box, m, mask, reach + margin, margin, disp2);
+    if (disp2) {
+        k_vein_snapshot<<<BCS_GRID1(V, 256), 0, s>>>(vpos, vref, V, disp2, margin);
+        k_disp_reset<<<1, 1, 0, s>>>(disp2, margin);
+    }
 }
 void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
                          int V, float k, float d, unsigned* err, cudaStream_t s) {

@@ -284,3 +284,25 @@ def test_incremental_grid_after_reshuffle(lib, small):
     np.testing.assert_array_equal(i, oi)
     np.testing.assert_array_equal(st, ost)
     np.testing.assert_array_equal(en, oen)
+
+
+def test_moving_wall_rebuilds_bounds(lib):
+    # Vein vertices start with a velocity that carries them past the 0.5
+    # rebuild margin of the triangle bounds / wall mask within the run; the
+    # frames must keep matching the oracle across rebuilds.
+    sc = S.straight_scene(cells=20, seed=17, radius=12.0, length=60.0, around=24, rings=20, vein_dynamic=True)
+    sc.velocities[:] = np.random.default_rng(6).normal(0, 15.0, sc.velocities.shape).astype(np.float32)
+    vvel = np.random.default_rng(7).normal(0, 40.0, sc.vein_positions.shape).astype(np.float32)
+    sim = make(sc)
+    sim.set_vein(vel=vvel)
+    o = O.OracleSim(sc)
+    o.set_vein(vel=vvel)
+    for _ in range(3):
+        sim.step(8)
+        o.step(8)
+        gp, _, _ = sim.get_particles()
+        op, _, _ = o.get_particles()
+        assert np.abs(gp - op).max() < 1e-3 * 0.5
+        assert np.abs(sim.get_vein()[0] - o.get_vein()[0]).max() < 1e-4
+    # the wall has moved well past the margin by now
+    assert np.abs(sim.get_vein()[0] - sc.vein_positions).max() > 0.5

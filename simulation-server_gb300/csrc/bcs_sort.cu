@@ -41,18 +41,20 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const int* __res
                                                                 unsigned* __restrict__ hist) {
     __shared__ unsigned s_hist[kRadix];
     const int n = dyn_n(n_max, d_n);
-    s_hist[threadIdx.x] = 0;
-    __syncthreads();
-    const int base = blockIdx.x * kSortTile;
-    if (base < n) {
+    const int live = (n + kSortTile - 1) / kSortTile;
+    for (int tile = blockIdx.x; tile < live; tile += gridDim.x) {
+        s_hist[threadIdx.x] = 0;
+        __syncthreads();
+        const int base = tile * kSortTile;
 #pragma unroll
         for (int k = 0; k < kSortItems; ++k) {
             int i = base + k * kSortThreads + threadIdx.x;
             if (i < n) atomicAdd(&s_hist[((unsigned)keys[i] >> shift) & 0xFFu], 1u);
         }
+        __syncthreads();
+        hist[(size_t)threadIdx.x * ntiles + tile] = s_hist[threadIdx.x];
+        __syncthreads();
     }
-    __syncthreads();
-    hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = s_hist[threadIdx.x];
 }
 
 // Exclusive block scan of one value per thread (256 threads); returns the
@@ -83,11 +85,14 @@ __device__ inline unsigned block_scan_256(unsigned v, unsigned* s_warp, unsigned
     return excl;
 }
 
-// One CTA per row: exclusive scan of row[0..len) in place, the row total
+// One CTA per row: exclusive scan of row[0..live) in place (rows of stride
+// `stride`; live = the tiles holding the d_n pairs, or all), the row total
 // into totals[row].
-__global__ void __launch_bounds__(kSortThreads) k_scan_rows(unsigned* rows, int len, unsigned* totals) {
+__global__ void __launch_bounds__(kSortThreads) k_scan_rows(unsigned* rows, int stride, const int* __restrict__ d_n,
+                                                            unsigned* totals) {
     __shared__ unsigned s_warp[kSortWarps];
-    unsigned* row = rows + (size_t)blockIdx.x * len;
+    unsigned* row = rows + (size_t)blockIdx.x * stride;
+    const int len = d_n ? (*d_n + kSortTile - 1) / kSortTile : stride;
     unsigned carry = 0;
     for (int base = 0; base < len; base += kSortThreads) {
         const int i = base + threadIdx.x;
@@ -112,69 +117,73 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __r
     __shared__ unsigned s_warp[kSortWarps];
     __shared__ int2 s_stage[kSortTile];
     const int n = dyn_n(n_max, d_n);
-    const int tile0 = blockIdx.x * kSortTile;
-    if (tile0 >= n) return;
+    const int live = (n + kSortTile - 1) / kSortTile;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int d = lane; d < kRadix; d += 32) s_cnt[warp][d] = 0;
+    unsigned digit_base_total;
     {
         unsigned tot;
-        const unsigned digit_base = block_scan_256(totals[threadIdx.x], s_warp, &tot);
-        s_base[threadIdx.x] = digit_base + offsets[(size_t)threadIdx.x * ntiles + blockIdx.x];
+        digit_base_total = block_scan_256(totals[threadIdx.x], s_warp, &tot);
     }
-    __syncwarp();
-    const int wbase = tile0 + warp * (kSortTile / kSortWarps);
-    const unsigned lt = (1u << lane) - 1u;
-    int key[kSortItems], val[kSortItems];
-    unsigned rank[kSortItems];
-#pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        const int i = wbase + r * 32 + lane;
-        const bool ok = i < n;
-        key[r] = ok ? keys_in[i] : 0;
-        val[r] = ok ? vals_in[i] : 0;
-        const unsigned d = ok ? (((unsigned)key[r] >> shift) & 0xFFu) : 0x100u;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const unsigned before = __popc(peers & lt);
-        const unsigned cnt = ok ? s_cnt[warp][d] : 0u;
-        rank[r] = cnt + before;
+    for (int tile = blockIdx.x; tile < live; tile += gridDim.x) {
+        const int tile0 = tile * kSortTile;
+        for (int d = lane; d < kRadix; d += 32) s_cnt[warp][d] = 0;
+        s_base[threadIdx.x] = digit_base_total + offsets[(size_t)threadIdx.x * ntiles + tile];
         __syncwarp();
-        if (ok && before == 0) s_cnt[warp][d] = cnt + __popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-    unsigned digit_total;
-    {
-        // Exclusive scan over warps of each digit's count.
-        unsigned run = 0;
-#pragma unroll
-        for (int w = 0; w < kSortWarps; ++w) {
-            unsigned c = s_cnt[w][threadIdx.x];
-            s_cnt[w][threadIdx.x] = run;
-            run += c;
+        const int wbase = tile0 + warp * (kSortTile / kSortWarps);
+        const unsigned lt = (1u << lane) - 1u;
+        int key[kSortItems], val[kSortItems];
+        unsigned rank[kSortItems];
+    #pragma unroll
+        for (int r = 0; r < kSortItems; ++r) {
+            const int i = wbase + r * 32 + lane;
+            const bool ok = i < n;
+            key[r] = ok ? keys_in[i] : 0;
+            val[r] = ok ? vals_in[i] : 0;
+            const unsigned d = ok ? (((unsigned)key[r] >> shift) & 0xFFu) : 0x100u;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const unsigned before = __popc(peers & lt);
+            const unsigned cnt = ok ? s_cnt[warp][d] : 0u;
+            rank[r] = cnt + before;
+            __syncwarp();
+            if (ok && before == 0) s_cnt[warp][d] = cnt + __popc(peers);
+            __syncwarp();
         }
-        digit_total = run;
-    }
-    {
-        unsigned tot;
-        s_tile[threadIdx.x] = block_scan_256(digit_total, s_warp, &tot);
-    }
-    __syncthreads();
-    // Stage in output order, then write each digit's run contiguously.
-#pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        const int i = wbase + r * 32 + lane;
-        if (i >= n) continue;
-        const unsigned d = ((unsigned)key[r] >> shift) & 0xFFu;
-        s_stage[s_tile[d] + s_cnt[warp][d] + rank[r]] = make_int2(key[r], val[r]);
-    }
-    __syncthreads();
-    const int count = min(kSortTile, n - tile0);
-    for (int j = threadIdx.x; j < count; j += kSortThreads) {
-        const int2 kv = s_stage[j];
-        const unsigned d = ((unsigned)kv.x >> shift) & 0xFFu;
-        const unsigned pos = s_base[d] + (j - s_tile[d]);
-        keys_out[pos] = kv.x;
-        vals_out[pos] = kv.y;
+        __syncthreads();
+        unsigned digit_total;
+        {
+            // Exclusive scan over warps of each digit's count.
+            unsigned run = 0;
+    #pragma unroll
+            for (int w = 0; w < kSortWarps; ++w) {
+                unsigned c = s_cnt[w][threadIdx.x];
+                s_cnt[w][threadIdx.x] = run;
+                run += c;
+            }
+            digit_total = run;
+        }
+        {
+            unsigned tot;
+            s_tile[threadIdx.x] = block_scan_256(digit_total, s_warp, &tot);
+        }
+        __syncthreads();
+        // Stage in output order, then write each digit's run contiguously.
+    #pragma unroll
+        for (int r = 0; r < kSortItems; ++r) {
+            const int i = wbase + r * 32 + lane;
+            if (i >= n) continue;
+            const unsigned d = ((unsigned)key[r] >> shift) & 0xFFu;
+            s_stage[s_tile[d] + s_cnt[warp][d] + rank[r]] = make_int2(key[r], val[r]);
+        }
+        __syncthreads();
+        const int count = min(kSortTile, n - tile0);
+        for (int j = threadIdx.x; j < count; j += kSortThreads) {
+            const int2 kv = s_stage[j];
+            const unsigned d = ((unsigned)kv.x >> shift) & 0xFFu;
+            const unsigned pos = s_base[d] + (j - s_tile[d]);
+            keys_out[pos] = kv.x;
+            vals_out[pos] = kv.y;
+        }
+        __syncthreads();
     }
 }
 
@@ -191,15 +200,18 @@ int radix_sort_pairs_n(const int* in_k, const int* in_v, int* a_k, int* a_v, int
     if (bits <= 0) bits = 1;
     const int ntiles = radix_tiles(n);
     unsigned* totals = temp + (size_t)kRadix * ntiles;
+    // a device-side count is usually far below n: a bounded grid strides
+    // over the tiles that hold data
+    const int grid = d_n ? (ntiles < 4 * 152 ? ntiles : 4 * 152) : ntiles;
     int pass = 0;
     for (int shift = 0; shift < bits; shift += 8, ++pass) {
         const int* ki = pass == 0 ? in_k : ((pass & 1) ? a_k : b_k);
         const int* vi = pass == 0 ? in_v : ((pass & 1) ? a_v : b_v);
         int* ko = (pass & 1) ? b_k : a_k;
         int* vo = (pass & 1) ? b_v : a_v;
-        k_radix_upsweep<<<ntiles, kSortThreads, 0, s>>>(ki, n, d_n, shift, ntiles, temp);
-        k_scan_rows<<<kRadix, kSortThreads, 0, s>>>(temp, ntiles, totals);
-        k_radix_downsweep<<<ntiles, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, d_n, shift, ntiles, temp, totals);
+        k_radix_upsweep<<<grid, kSortThreads, 0, s>>>(ki, n, d_n, shift, ntiles, temp);
+        k_scan_rows<<<kRadix, kSortThreads, 0, s>>>(temp, ntiles, d_n, totals);
+        k_radix_downsweep<<<grid, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, d_n, shift, ntiles, temp, totals);
     }
     return (pass & 1) ? 0 : 1;
 }

@@ -57,10 +57,7 @@ struct IncrementalBuffers {
     int* movers;
 };
 void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_key_of, int* out_k, int* out_v, int n,
-                           int key_bits, int id_bits, const IncrementalBuffers& b, const float4* pos,
-                           const float4* vel, float4* spos, float4* svel, cudaStream_t s);
-void launch_reorder(const int* ids, int n, const float4* pos, const float4* vel, float4* spos, float4* svel,
-                    cudaStream_t s);
+                           int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s);
 }  // namespace bcs
 
 using namespace bcs;
@@ -80,8 +77,6 @@ struct DeviceGrid {
     int4* table = nullptr;
     int* epoch = nullptr;
     unsigned* temp = nullptr;
-    float4* spos = nullptr;              // state in sorted order (particle grid)
-    float4* svel = nullptr;
     int bits = 0;
     int id_bits = 0;
     int count = 0;
@@ -221,14 +216,11 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
 // Sort the grid's unsorted keys into the other result slot and rebuild the
 // range table.  After the first build, a grid flagged incremental starts
 // from the previous order (any permutation works; few movers make it cheap).
-// With pos/vel (particle grid) the state is also written in sorted order.
-void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, const float4* vel = nullptr) {
+void sort_grid(DeviceGrid& dg, cudaStream_t st) {
     const int out = dg.slot ^ 1;
-    const bool with_state = pos && dg.spos;
     if (dg.incremental && dg.sorted_once) {
         sort_grid_incremental(dg.s_k[dg.slot], dg.s_v[dg.slot], dg.in_k, dg.s_k[out], dg.s_v[out], dg.count, dg.bits,
-                              dg.id_bits, dg.inc, with_state ? pos : nullptr, vel, with_state ? dg.spos : nullptr,
-                              dg.svel, st);
+                              dg.id_bits, dg.inc, st);
     } else {
         // the full sort's result lands in its first ping-pong buffer after an
         // odd number of passes (or none), in the second after an even number
@@ -237,14 +229,11 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, con
         radix_sort_pairs(dg.in_k, dg.in_v, first ? dg.s_k[out] : dg.inc.t1_k, first ? dg.s_v[out] : dg.inc.t1_v,
                          first ? dg.inc.t1_k : dg.s_k[out], first ? dg.inc.t1_v : dg.s_v[out], dg.count, dg.bits,
                          dg.temp, st);
-        if (with_state) launch_reorder(dg.s_v[out], dg.count, pos, vel, dg.spos, dg.svel, st);
     }
     dg.slot = out;
     dg.sorted_once = true;
     dg.g.keys = dg.s_k[dg.slot];
     dg.g.ids = dg.s_v[dg.slot];
-    dg.g.spos = dg.spos;
-    dg.g.svel = dg.svel;
     dg.g.table = dg.table;
     launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, st);
 }
@@ -290,7 +279,7 @@ void enqueue_grids(bcs_sim* s) {
         launch_keys(s->pos[s->cur], s->N, s->pg.g, s->pg.in_k, s->pg.in_v, s->err, s->stream);
         s->keys_valid = true;
     }
-    if (s->pg.g.uniform) sort_grid(s->pg, s->stream, s->pos[s->cur], s->vel[s->cur]);
+    if (s->pg.g.uniform) sort_grid(s->pg, s->stream);
     if (s->p.refresh_triangle_centers) build_triangle_grid(s, true);
     s->grid_ready = true;
 }
@@ -530,9 +519,6 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
     if ((st = alloc_grid(s, s->pg, s->N, true)) || (st = alloc_grid(s, s->tg, std::max(1, s->T), false))) return st;
     s->tg.count = s->T;
     s->tg.g.count = s->T;
-    if (s->pg.g.uniform) {
-        if ((st = dalloc(s, &s->pg.spos, s->N)) || (st = dalloc(s, &s->pg.svel, s->N))) return st;
-    }
     if (s->tg.g.uniform) {
         if ((st = dalloc(s, &s->tbox, 2 * (size_t)s->tg.g.cells))) return st;
         if (s->p.vein_dynamic && s->T > 0) {

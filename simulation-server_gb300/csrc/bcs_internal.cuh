@@ -22,9 +22,6 @@
 //   tcache                   3 float4 per sorted triangle slot: (v0, id),
 //                            (v1 - v0), (v2 - v0) — the Moller-Trumbore
 //                            operands, streamed contiguously per grid cell.
-//   spos, svel               float4 x N: x and v in sorted-slot order, written
-//                            with the sort, so a collision candidate is one
-//                            load from a contiguous run instead of id -> state
 //   tbox                     2 float4 per triangle-grid cell: bounds of the
 //                            cell's triangles widened by the rebuild margin,
 //                            for ray culling
@@ -69,8 +66,6 @@ struct GridDev {
     long long cells;
     const int* keys;      // sorted keys
     const int* ids;       // sorted object ids
-    const float4* spos;   // particle positions in sorted-slot order (particle grid)
-    const float4* svel;   // particle velocities in sorted-slot order
     const int4* table;    // (first, last, epoch) per cell
     const int* epoch;     // current epoch of the table
     int count;            // objects

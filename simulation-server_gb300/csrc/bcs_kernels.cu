@@ -135,24 +135,16 @@ __device__ inline unsigned to_u32_sat(float t) { return t <= 0.f ? 0u : (t >= 42
 __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 x, float3 v, float R, unsigned& e) {
     float3 acc = f3(0.f, 0.f, 0.f);
     const GridDev& g = a.pg;
-    // The reference skips q == p and pairs closer than 0.01 (d^2 < 1e-4);
-    // the particle itself (d^2 = 0) falls under the second rule, so a
-    // candidate needs no id.
-    auto contact = [&](float4 pq, float4 vq) {
+    auto test = [&](int q) {
+        const float4 pq = __ldg(&a.pos_in[q]);
         float3 rp = x - xyz(pq);
         float d2 = dot3(rp, rp);
         float md = R + pq.w;
-        if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(vq), d2, R, 0.5f, e);
+        if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[q])), d2, R, 0.5f, e);
     };
     if (!g.uniform) {
-        for (int q = 0; q < a.n; ++q) {
-            if (q == pid) continue;
-            const float4 pq = __ldg(&a.pos_in[q]);
-            float3 rp = x - xyz(pq);
-            float d2 = dot3(rp, rp);
-            float md = R + pq.w;
-            if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[q])), d2, R, 0.5f, e);
-        }
+        for (int q = 0; q < a.n; ++q)
+            if (q != pid) test(q);
         return acc;
     }
     unsigned dummy = 0;
@@ -176,12 +168,8 @@ __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 
                     last = l;
                 }
             for (int j = first; j <= last; ++j) {
-                const float4 pq = __ldg(&g.spos[j]);
-                float3 rp = x - xyz(pq);
-                float d2 = dot3(rp, rp);
-                float md = R + pq.w;
-                if (d2 <= md * md && d2 >= 0.0001f)
-                    acc = acc + resilient(a.p, rp, v - xyz(__ldg(&g.svel[j])), d2, R, 0.5f, e);
+                const int q = __ldg(&g.ids[j]);
+                if (q != pid) test(q);
             }
         }
     return acc;
@@ -280,12 +268,12 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
         // in stencil order.
         if (last_near >= 0) live &= (last_near >= 31) ? 0xffffffffu : ((2u << last_near) - 1u);
         else live = 0u;
-        const int nx = x1 - x0 + 1, ny = y1 - y0 + 1, nz = z1 - z0 + 1;
+        const int ny = y1 - y0 + 1, nz = z1 - z0 + 1;
         while (live) {
             const int kk = __ffs(live) - 1;
             live &= live - 1u;
             const int dz = z0 + kk % nz, dy = y0 + (kk / nz) % ny, dx = x0 + kk / (nz * ny);
-                    const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
+            const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
             int f, l;
             if (!cell_range(g, ep, c, f, l)) continue;
             bool found = false;

@@ -306,9 +306,7 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_split(const int* __restric
 // thread finds its 8-output diagonal on the merge path, then merges.
 __global__ void __launch_bounds__(256) k_inc_merge(const int* __restrict__ a_k, const int* __restrict__ a_v,
                                                    const int* __restrict__ b_k, const int* __restrict__ b_v, int n,
-                                                   const int* __restrict__ movers, int* out_k, int* out_v,
-                                                   const float4* __restrict__ pos, const float4* __restrict__ vel,
-                                                   float4* spos, float4* svel) {
+                                                   const int* __restrict__ movers, int* out_k, int* out_v) {
     constexpr int kItems = 8;
     const int m = *movers;
     const int na = n - m, nb = m;
@@ -330,30 +328,9 @@ __global__ void __launch_bounds__(256) k_inc_merge(const int* __restrict__ a_k, 
         if (i >= na) take_a = false;
         else if (j >= nb) take_a = true;
         else take_a = pack_pair(a_k[i], a_v[i]) < pack_pair(b_k[j], b_v[j]);
-        int id;
-        if (take_a) { out_k[o] = a_k[i]; id = a_v[i]; ++i; }
-        else { out_k[o] = b_k[j]; id = b_v[j]; ++j; }
-        out_v[o] = id;
-        if (spos) {
-            spos[o] = __ldg(&pos[id]);
-            svel[o] = __ldg(&vel[id]);
-        }
+        if (take_a) { out_k[o] = a_k[i]; out_v[o] = a_v[i]; ++i; }
+        else { out_k[o] = b_k[j]; out_v[o] = b_v[j]; ++j; }
     }
-}
-
-// Particle state in sorted-slot order, for the collision gathers.
-__global__ void k_reorder(const int* __restrict__ ids, int n, const float4* __restrict__ pos,
-                          const float4* __restrict__ vel, float4* spos, float4* svel) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const int id = ids[j];
-    spos[j] = __ldg(&pos[id]);
-    svel[j] = __ldg(&vel[id]);
-}
-
-void launch_reorder(const int* ids, int n, const float4* pos, const float4* vel, float4* spos, float4* svel,
-                    cudaStream_t s) {
-    if (n > 0) k_reorder<<<(n + 255) / 256, 256, 0, s>>>(ids, n, pos, vel, spos, svel);
 }
 
 struct IncrementalBuffers {
@@ -368,11 +345,8 @@ struct IncrementalBuffers {
 
 // New sorted (out_k, out_v) from the previous frame's sorted (old_k, old_v)
 // and the new keys by particle id.
-// With spos/svel, the merge also writes the particle state (pos, vel) in the
-// new sorted order.
 void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_key_of, int* out_k, int* out_v, int n,
-                           int key_bits, int id_bits, const IncrementalBuffers& b, const float4* pos,
-                           const float4* vel, float4* spos, float4* svel, cudaStream_t s) {
+                           int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s) {
     if (n <= 0) return;
     const int ntiles = radix_tiles(n);
     k_inc_count<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.tile_kept);
@@ -390,8 +364,7 @@ void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_ke
     const int* ms_k = w2 ? free_k : b.mov_k;
     const int* ms_v = w2 ? free_v : b.mov_v;
     const int threads = (n + 7) / 8;
-    k_inc_merge<<<(threads + 255) / 256, 256, 0, s>>>(b.kept_k, b.kept_v, ms_k, ms_v, n, b.movers, out_k, out_v, pos,
-                                                      vel, spos, svel);
+    k_inc_merge<<<(threads + 255) / 256, 256, 0, s>>>(b.kept_k, b.kept_v, ms_k, ms_v, n, b.movers, out_k, out_v);
 }
 
 }  // namespace bcs

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BCS_ABI_VERSION 1
+#define BCS_ABI_VERSION 2
 
 typedef struct bcs_sim bcs_sim;
 
@@ -187,7 +187,27 @@ typedef struct bcs_info {
     size_t device_bytes;
     int kernels_per_step;          /* kernel nodes in one captured frame (0
                                       until the first bcs_step replay)      */
+    int scene_count;               /* scenes in the simulation (1 unless
+                                      built by bcs_create_batch); the bounds
+                                      and per-axis cell counts above are
+                                      scene 0's, the cell counts are totals */
 } bcs_info;
+
+/* One scene of a batch.  Particles, blood cells, vertices and triangles of
+ * the scenes lie back to back in the batch-wide arrays (scene-major), in
+ * the order of the descriptors given to bcs_create_batch.  The grid keys of
+ * scene k are its own calculateIdForCell keys plus cell_key_offset. */
+typedef struct bcs_scene_info {
+    int particle_start, particle_count;
+    int blood_cell_start, blood_cell_count;
+    int vertex_start, vertex_count;
+    int triangle_start, triangle_count;
+    float min_x, max_x, min_y, max_y, min_z, max_z;
+    int cell_count_x, cell_count_y, cell_count_z;
+    int64_t cell_count, cell_key_offset;
+    int tri_cell_count_x, tri_cell_count_y, tri_cell_count_z;
+    int64_t tri_cell_count, tri_cell_key_offset;
+} bcs_scene_info;
 
 /* Fill *p with the reference's shipped constants (src/config/physics.hpp, simulation.hpp). */
 void bcs_default_params(bcs_params* p);
@@ -207,8 +227,19 @@ bcs_status bcs_set_device(int device);
  * comes from bcs_set_particles.  `stream` is a cudaStream_t or NULL (the
  * library then creates its own non-blocking stream). */
 bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out);
+
+/* Build `scene_count` independent scenes as one simulation: every kernel of
+ * a frame runs once over all scenes (one sort, one step launch), and each
+ * scene computes exactly what it computes alone under bcs_create.  The
+ * scenes must share every physics constant of bcs_params except the grid
+ * cell sizes and margins, cylinder_radius, min_spawn_y and seed, and share
+ * the grid kinds.  The reference runs one compile-time scene per process;
+ * this is the batched form of src/main.cu:122-138. */
+bcs_status bcs_create_batch(const bcs_scene_desc* descs, int scene_count, void* stream,
+                            bcs_sim** out);
 bcs_status bcs_destroy(bcs_sim* sim);
 bcs_status bcs_get_info(bcs_sim* sim, bcs_info* out);
+bcs_status bcs_get_scene_info(bcs_sim* sim, int scene, bcs_scene_info* out);
 
 /* Particle state (positions, velocities, forces) as written by
  * setBloodCellsPositionsFromRandom (simulation_controller.cu:224-243) and

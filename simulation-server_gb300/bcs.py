@@ -28,7 +28,7 @@ EXPORTED = [
     "bcs_get_info", "bcs_set_particles", "bcs_get_particles", "bcs_set_vein", "bcs_get_vein",
     "bcs_calculate_grids", "bcs_calculate_next_frame", "bcs_propagate_all", "bcs_step",
     "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
-    "bcs_profile_steps", "bcs_grid_sort_static",
+    "bcs_profile_steps", "bcs_grid_sort_static", "bcs_create_batch", "bcs_get_scene_info",
 ]
 GRID_SORT_STATIC_MAX = 262144
 PHASES = ("grid", "vein_forces", "particles", "vein_update")
@@ -98,7 +98,22 @@ class Info(C.Structure):
         ("cell_count", C.c_int64),
         ("tri_cell_count_x", C.c_int), ("tri_cell_count_y", C.c_int), ("tri_cell_count_z", C.c_int),
         ("tri_cell_count", C.c_int64), ("steps_done", C.c_int64), ("device_bytes", C.c_size_t),
-        ("kernels_per_step", C.c_int),
+        ("kernels_per_step", C.c_int), ("scene_count", C.c_int),
+    ]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [
+        ("particle_start", C.c_int), ("particle_count", C.c_int),
+        ("blood_cell_start", C.c_int), ("blood_cell_count", C.c_int),
+        ("vertex_start", C.c_int), ("vertex_count", C.c_int),
+        ("triangle_start", C.c_int), ("triangle_count", C.c_int),
+        ("min_x", C.c_float), ("max_x", C.c_float), ("min_y", C.c_float), ("max_y", C.c_float),
+        ("min_z", C.c_float), ("max_z", C.c_float),
+        ("cell_count_x", C.c_int), ("cell_count_y", C.c_int), ("cell_count_z", C.c_int),
+        ("cell_count", C.c_int64), ("cell_key_offset", C.c_int64),
+        ("tri_cell_count_x", C.c_int), ("tri_cell_count_y", C.c_int), ("tri_cell_count_z", C.c_int),
+        ("tri_cell_count", C.c_int64), ("tri_cell_key_offset", C.c_int64),
     ]
 
 
@@ -120,6 +135,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_abi_version": ([], C.c_int),
         "bcs_set_device": ([C.c_int], C.c_int),
         "bcs_create": ([C.POINTER(SceneDesc), P, C.POINTER(P)], C.c_int),
+        "bcs_create_batch": ([C.POINTER(SceneDesc), C.c_int, P, C.POINTER(P)], C.c_int),
+        "bcs_get_scene_info": ([P, C.c_int, C.POINTER(SceneInfo)], C.c_int),
         "bcs_destroy": ([P], C.c_int),
         "bcs_get_info": ([P, C.POINTER(Info)], C.c_int),
         "bcs_set_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
@@ -231,14 +248,25 @@ class SceneBuffers:
 
 class Simulation:
     """One scene on the current CUDA device (≙ BloodCells + VeinTriangles +
-    two UniformGrids + SimulationController of src/main.cu:122-138)."""
+    two UniformGrids + SimulationController of src/main.cu:122-138), or, given
+    a list of scenes, a batch of independent scenes run by one set of
+    launches (bcs_create_batch).  Batch state is scene-major: scene k owns
+    the rows scene_info(k).particle_start .. + particle_count."""
 
     def __init__(self, scene, stream: int | None = None):
         self.lib = load_library()
-        self.scene = scene
-        self._bufs = SceneBuffers(scene)
         h = C.c_void_p()
-        _check(self.lib.bcs_create(C.byref(self._bufs.desc), stream, C.byref(h)), "bcs_create")
+        if isinstance(scene, (list, tuple)):
+            self.scenes = list(scene)
+            self.scene = self.scenes[0]
+            self._bufs = [SceneBuffers(sc) for sc in self.scenes]
+            descs = (SceneDesc * len(self._bufs))(*[b.desc for b in self._bufs])
+            _check(self.lib.bcs_create_batch(descs, len(self._bufs), stream, C.byref(h)), "bcs_create_batch")
+        else:
+            self.scenes = [scene]
+            self.scene = scene
+            self._bufs = SceneBuffers(scene)
+            _check(self.lib.bcs_create(C.byref(self._bufs.desc), stream, C.byref(h)), "bcs_create")
         self.h = h
         self.info = Info()
         _check(self.lib.bcs_get_info(self.h, C.byref(self.info)), "bcs_get_info")
@@ -354,6 +382,11 @@ class Simulation:
         w = C.c_uint32()
         _check(self.lib.bcs_get_error_word(self.h, C.byref(w), int(clear)), "bcs_get_error_word")
         return int(w.value)
+
+    def scene_info(self, k: int) -> SceneInfo:
+        out = SceneInfo()
+        _check(self.lib.bcs_get_scene_info(self.h, int(k), C.byref(out)), "bcs_get_scene_info")
+        return out
 
     def refresh_info(self) -> Info:
         _check(self.lib.bcs_get_info(self.h, C.byref(self.info)), "bcs_get_info")

@@ -351,3 +351,59 @@ def tiny_scene(cells=4, seed=1, **kw) -> Scene:
     kw.setdefault("around", 24)
     kw.setdefault("rings", 14)
     return straight_scene(cells=cells, seed=seed, **kw)
+
+
+def mixed_straight_scene(spheres, discs, length, seed=0, base_radius=30.0, cell_size=1.0, tri_cell=6.0, dt=1e-3,
+                         k=50.0, d=0.5, particle_radius=0.5, fill=0.85, ring_spacing=3.0) -> Scene:
+    """A straight vessel of the given length holding `spheres` 42-vertex and
+    `discs` 162-vertex cells.  The radius starts at `base_radius` and grows
+    until the lattice holds both populations at `fill` occupancy (a 50k-cell
+    population does not fit a radius-30 vessel of length <= 600); the mesh
+    keeps ~`ring_spacing` between rings and around the circumference."""
+    rng = np.random.default_rng(seed)
+    models = [sphere_cell(3.0, 1), biconcave_cell(4.0, 2)]
+    need = [spheres, discs]
+    R = base_radius
+    while True:
+        seg = dict(origin=(0.0, 0.0, 0.0), direction=(0.0, -1.0, 0.0), length=length, radius=R)
+        sites = lattice_sites([seg], models, [0, 1], particle_radius=particle_radius)
+        short = max((n / max(1.0, len(s) * fill) for s, n in zip(sites, need) if n), default=0.0)
+        if short <= 1.0:
+            break
+        R *= min(2.0, max(1.03, math.sqrt(short) * 1.02))
+    around = max(24, int(round(2 * math.pi * R / ring_spacing)))
+    rings = max(2, int(round(length / ring_spacing)) + 1)
+    vein = straight_vein(R, length, around, rings)
+    cen = [_choose(s, n, rng, m.name) for s, n, m in zip(sites, need, models)]
+    keep = [i for i in range(2) if need[i] > 0]
+    pos, vel = _instantiate([models[i] for i in keep], [need[i] for i in keep], [cen[i] for i in keep], 0.0, rng)
+    p = default_params()
+    p.dt = dt
+    p.particle_k_sniff = k
+    p.particle_d_fact = d
+    p.cell_width = p.cell_height = p.cell_depth = cell_size
+    p.cell_width_triangles = p.cell_height_triangles = p.cell_depth_triangles = tri_cell
+    p.cylinder_radius = R
+    p.vein_dynamic = 0
+    p.seed = seed
+    types = [CellTypeSpec(need[i], models[i].vertices, models[i].springs, models[i].spring_lengths,
+                          np.full(len(models[i].vertices), particle_radius, np.float32), models[i].name)
+             for i in keep]
+    return Scene("straight-mixed", types, vein.positions, vein.indices, vein.ending_centers, vein.ending_radii, [],
+                 p, pos, vel)
+
+
+def batched_scenes(count=64, seed=0, min_cells=500, max_cells=50000, min_length=150.0, max_length=600.0,
+                   **kw) -> list:
+    """Batched plain method: `count` independent straight vessels, cell counts
+    log-uniform in [min_cells, max_cells], lengths uniform in
+    [min_length, max_length], each cell a sphere or a biconcave disc with
+    probability 1/2; dt=1e-3 and the constants of the small straight scene."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(min_cells), math.log(max_cells)))))
+        L = float(rng.uniform(min_length, max_length))
+        spheres = int(rng.binomial(n, 0.5))
+        out.append(mixed_straight_scene(spheres, n - spheres, L, seed=seed * 1000 + s, **kw))
+    return out

@@ -22,16 +22,17 @@ namespace bcs {
 // bcs_kernels.cu
 void launch_step(const StepArgs& a, int blocks, int mode, cudaStream_t s);
 void launch_propagate(const StepArgs& a, int blocks, cudaStream_t s);
-void launch_keys(const float4* pos, int n, const GridDev& g, int* keys, int* ids, unsigned* err, cudaStream_t s);
-void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const GridDev& g, int* keys, int* ids,
-                     cudaStream_t s);
+void launch_keys(const float4* pos, int n, int uniform, const SceneDev* scenes, int scene_count, int* keys, int* ids,
+                 unsigned* err, cudaStream_t s);
+void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const SceneDev* scenes, int scene_count,
+                     int* keys, int* ids, cudaStream_t s);
 void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, cudaStream_t s);
 void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
                          cudaStream_t s);
 void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s);
 void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tri, const float4* vpos, float4* box,
-                      const MaskDev& m, unsigned char* mask, float reach, int* mask_epoch, float margin,
-                      float* disp2, float4* vref, int V, cudaStream_t s);
+                      const SceneDev* scenes, int scene_count, unsigned char* mask, float reach, int* mask_epoch,
+                      float margin, float* disp2, float4* vref, int V, cudaStream_t s);
 void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
                          int V, float k, float d, unsigned* err, cudaStream_t s);
 void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt, cudaStream_t s);
@@ -90,8 +91,13 @@ struct bcs_sim {
     bool own_stream = false;
     bcs_params p{};
     int N = 0, C = 0, V = 0, T = 0;
+    int S = 0;                   // scenes in the batch
     std::vector<TypeDev> types;
     std::vector<WorkItem> work_host;
+    std::vector<SceneDev> scenes_host;
+    std::vector<int> scene_cells;       // blood cells per scene
+    std::vector<int> scene_cell_start;
+    std::vector<int> scene_vertex_start, scene_vertex_count;
     size_t bytes = 0;
     std::vector<void*> allocations;
     // particle state
@@ -105,6 +111,9 @@ struct bcs_sim {
     bool grid_ready = false;
     // layout tables
     WorkItem* work = nullptr;
+    TypeDev* types_dev = nullptr;
+    SceneDev* scenes = nullptr;
+    bcs_flow_segment* flows = nullptr;
     int* adj_off = nullptr;
     int* adj_nbr = nullptr;
     float* adj_len = nullptr;
@@ -121,12 +130,10 @@ struct bcs_sim {
     float4* tbox = nullptr;         // 2 per triangle-grid cell
     unsigned char* wall_mask = nullptr;
     int* wall_epoch = nullptr;
-    MaskDev wall{};
     float* wall_disp2 = nullptr;     // dynamic wall: max squared vertex move since the last bounds build
     float4* wall_ref = nullptr;      // vein positions at that build
     // grids
     DeviceGrid pg, tg;
-    float minX, maxX, minY, maxY, minZ, maxZ, width, height, depth;
     // misc
     long long* steps = nullptr;
     long long host_steps = 0;
@@ -252,7 +259,8 @@ void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
     a.tg = s->tg.g;
     a.tcache = s->tcache;
     a.tbox = s->tbox;
-    a.wall = s->wall;
+    a.wall_mask = s->wall_mask;
+    a.wall_epoch = s->wall_epoch;
 }
 
 // Triangle grid, Moller-Trumbore cache, per-cell triangle bounds and the
@@ -261,11 +269,11 @@ void build_triangle_grid(bcs_sim* s, bool regrid) {
     if (s->T == 0) return;
     if (s->tg.g.uniform) {
         if (regrid) {
-            launch_tri_keys(s->vpos, s->tri, s->T, s->tg.g, s->tg.in_k, s->tg.in_v, s->stream);
+            launch_tri_keys(s->vpos, s->tri, s->T, s->scenes, s->S, s->tg.in_k, s->tg.in_v, s->stream);
             sort_grid(s->tg, s->stream);
         }
         launch_tri_cache(s->tg.g.ids, s->tri, s->vpos, s->T, s->tcache, s->stream);
-        launch_tri_boxes(s->tg.g.keys, s->tg.g.ids, s->T, s->tri, s->vpos, s->tbox, s->wall, s->wall_mask,
+        launch_tri_boxes(s->tg.g.keys, s->tg.g.ids, s->T, s->tri, s->vpos, s->tbox, s->scenes, s->S, s->wall_mask,
                          s->p.vein_impact_distance * 1.001f + 1e-3f, s->wall_epoch,
                          s->wall_disp2 ? kWallMargin : 0.0f, s->wall_disp2, s->wall_ref, s->V, s->stream);
     } else {
@@ -276,7 +284,7 @@ void build_triangle_grid(bcs_sim* s, bool regrid) {
 // ≙ main.cu:175-176.
 void enqueue_grids(bcs_sim* s) {
     if (!s->keys_valid) {
-        launch_keys(s->pos[s->cur], s->N, s->pg.g, s->pg.in_k, s->pg.in_v, s->err, s->stream);
+        launch_keys(s->pos[s->cur], s->N, s->pg.g.uniform, s->scenes, s->S, s->pg.in_k, s->pg.in_v, s->err, s->stream);
         s->keys_valid = true;
     }
     if (s->pg.g.uniform) sort_grid(s->pg, s->stream);
@@ -330,7 +338,7 @@ void drop_graphs(bcs_sim* s) {
 }
 
 bcs_status validate(const bcs_scene_desc* d) {
-    if (!d || d->type_count <= 0 || d->type_count > kMaxTypes || !d->types) return BCS_ERR_INVALID_ARGUMENT;
+    if (!d || d->type_count <= 0 || !d->types) return BCS_ERR_INVALID_ARGUMENT;
     long long n = 0;
     for (int t = 0; t < d->type_count; ++t) {
         const bcs_cell_type& c = d->types[t];
@@ -348,10 +356,10 @@ bcs_status validate(const bcs_scene_desc* d) {
         return BCS_ERR_INVALID_ARGUMENT;
     for (long long k = 0; k < 3LL * v.triangle_count; ++k)
         if (v.indices[k] >= (uint32_t)v.vertex_count) return BCS_ERR_INVALID_ARGUMENT;
-    if (v.ending_count < 0 || v.ending_count > 8 || (v.ending_count > 0 && (!v.ending_centers || !v.ending_radii)))
+    if (v.ending_count < 0 || v.ending_count > kMaxEndings ||
+        (v.ending_count > 0 && (!v.ending_centers || !v.ending_radii)))
         return BCS_ERR_INVALID_ARGUMENT;
-    if (d->flow_segment_count < 0 || d->flow_segment_count > kMaxFlow ||
-        (d->flow_segment_count > 0 && !d->flow_segments))
+    if (d->flow_segment_count < 0 || (d->flow_segment_count > 0 && !d->flow_segments))
         return BCS_ERR_INVALID_ARGUMENT;
     const bcs_params& p = d->params;
     if (!(p.cell_width > 0 && p.cell_height > 0 && p.cell_depth > 0 && p.cell_width_triangles > 0 &&
@@ -360,9 +368,40 @@ bcs_status validate(const bcs_scene_desc* d) {
     return BCS_OK;
 }
 
-bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
+// Scenes of one batch share every physics constant; grid cell sizes,
+// margins, respawn spread and height and the seed may differ per scene.
+bool same_physics(const bcs_params& a, const bcs_params& b) {
+    bcs_params x = a, y = b;
+    for (bcs_params* q : {&x, &y}) {
+        q->cell_width = q->cell_height = q->cell_depth = 0;
+        q->cell_width_triangles = q->cell_height_triangles = q->cell_depth_triangles = 0;
+        q->grid_y_margin = q->grid_xz_margin = 0;
+        q->cylinder_radius = q->min_spawn_y = 0;
+        q->seed = 0;
+    }
+    return std::memcmp(&x, &y, sizeof(bcs_params)) == 0;
+}
+
+// One scene's uniform grid over its vein's bounds (vein_factory.hpp:21-86,
+// uniform_grid.cu:83-104), FP32 like the reference's constexpr floats.
+bcs_status scene_grid(const float* mn, const float* mx, const bcs_params& p, float cw, float ch, float cd, bool uniform,
+                      GridGeom& g) {
+    g.lo[0] = mn[0] - p.grid_xz_margin; g.hi[0] = mx[0] + p.grid_xz_margin;
+    g.lo[1] = mn[1] - p.grid_y_margin;  g.hi[1] = mx[1] + p.grid_y_margin;
+    g.lo[2] = mn[2] - p.grid_xz_margin; g.hi[2] = mx[2] + p.grid_xz_margin;
+    for (int k = 0; k < 3; ++k) g.ext[k] = g.hi[k] - g.lo[k];
+    g.cell[0] = cw; g.cell[1] = ch; g.cell[2] = cd;
+    g.cx = (int)(g.ext[0] / cw); g.cy = (int)(g.ext[1] / ch); g.cz = (int)(g.ext[2] / cd);
+    g.cells = (long long)g.cx * g.cy * g.cz;
+    if (uniform && (g.cx < 1 || g.cy < 1 || g.cz < 1 || g.cells > INT32_MAX)) return BCS_ERR_INVALID_ARGUMENT;
+    if (!uniform) g.cells = 0;
+    return BCS_OK;
+}
+
+bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* stream, bcs_sim* s) {
     bcs_status st;
-    s->p = d->params;
+    s->p = descs[0].params;
+    s->S = scene_count;
     BCS_CUDA(cudaGetDevice(&s->device));
     if (stream) {
         s->stream = static_cast<cudaStream_t>(stream);
@@ -373,112 +412,151 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
     BCS_CUDA(cudaEventCreate(&s->ev0));
     BCS_CUDA(cudaEventCreate(&s->ev1));
     for (auto& e : s->pev) BCS_CUDA(cudaEventCreate(&e));
+    const bool puniform = s->p.particle_grid == BCS_GRID_UNIFORM;
+    const bool tuniform = s->p.triangle_grid == BCS_GRID_UNIFORM;
 
-    // ---- cell types: offsets, CSR springs, radii (blood_cell_factory.hpp:172-328,
-    //      simulation_controller.cu:93-153)
     std::vector<int> adj_off, adj_nbr;
     std::vector<float> adj_len, r0, radius_model;
-    std::vector<float4> respawn;
-    int pstart = 0, cstart = 0, mstart = 0;
-    for (int t = 0; t < d->type_count; ++t) {
-        const bcs_cell_type& c = d->types[t];
-        const int pic = c.particles_in_cell;
-        TypeDev td{c.count, pic, pstart, cstart, mstart, (int)adj_off.size()};
-        // Dense graph with the reference's rules: later springs overwrite
-        // earlier ones, a rest length of 0 is "no spring".
-        std::vector<float> dense((size_t)pic * pic, 0.0f);
-        for (int k = 0; k < c.spring_count; ++k) {
-            int a = c.springs[2 * k], b = c.springs[2 * k + 1];
-            dense[(size_t)a * pic + b] = c.spring_lengths[k];
-            dense[(size_t)b * pic + a] = c.spring_lengths[k];
-        }
-        for (int i = 0; i < pic; ++i) {
+    std::vector<float4> respawn, vpos;
+    std::vector<uint32_t> tri;
+    std::vector<int> nb_ids;
+    std::vector<float> nb_len;
+    std::vector<bcs_flow_segment> flows;
+    std::vector<int> nb_scene_ids[9];
+    std::vector<float> nb_scene_len[9];
+    long long key_total = 0, tkey_total = 0, mask_total = 0;
+    int pstart = 0, mstart = 0, cglobal = 0;
+    for (int si = 0; si < scene_count; ++si) {
+        const bcs_scene_desc* d = descs + si;
+        const bcs_params& sp = d->params;
+        SceneDev sd{};
+        sd.particle_start = pstart;
+        // ---- cell types: offsets, CSR springs, radii (blood_cell_factory.hpp:172-328,
+        //      simulation_controller.cu:93-153)
+        int cstart = 0;
+        for (int t = 0; t < d->type_count; ++t) {
+            const bcs_cell_type& c = d->types[t];
+            const int pic = c.particles_in_cell;
+            TypeDev td{c.count, pic, pstart, cstart, cglobal, mstart, (int)adj_off.size(), si};
+            // Dense graph with the reference's rules: later springs overwrite
+            // earlier ones, a rest length of 0 is "no spring".
+            std::vector<float> dense((size_t)pic * pic, 0.0f);
+            for (int k = 0; k < c.spring_count; ++k) {
+                int a = c.springs[2 * k], b = c.springs[2 * k + 1];
+                dense[(size_t)a * pic + b] = c.spring_lengths[k];
+                dense[(size_t)b * pic + a] = c.spring_lengths[k];
+            }
+            for (int i = 0; i < pic; ++i) {
+                adj_off.push_back((int)adj_nbr.size());
+                for (int j = 0; j < pic; ++j) {
+                    float L = dense[(size_t)j * pic + i];
+                    if (L == 0.0f || j == i) continue;   // a self spring contributes exactly 0
+                    adj_nbr.push_back(j);
+                    adj_len.push_back(L);
+                }
+            }
             adj_off.push_back((int)adj_nbr.size());
+            const float* m = c.vertices;
+            float cx = 0, cy = 0, cz = 0;
             for (int j = 0; j < pic; ++j) {
-                float L = dense[(size_t)j * pic + i];
-                if (L == 0.0f || j == i) continue;   // a self spring contributes exactly 0
-                adj_nbr.push_back(j);
-                adj_len.push_back(L);
+                float best = std::numeric_limits<float>::max();
+                for (int k = 0; k < pic; ++k) {
+                    if (j == k) continue;
+                    double len = std::sqrt(std::pow((double)(m[3 * j] - m[3 * k]), 2) +
+                                           std::pow((double)(m[3 * j + 1] - m[3 * k + 1]), 2) +
+                                           std::pow((double)(m[3 * j + 2] - m[3 * k + 2]), 2)) /
+                                 (2 * (double)sp.bounding_spheres_coeff);
+                    if (len < best) best = (float)len;
+                }
+                radius_model.push_back(c.collision_radius ? c.collision_radius[j] : best);
+                cx += m[3 * j]; cy += m[3 * j + 1]; cz += m[3 * j + 2];
             }
-        }
-        adj_off.push_back((int)adj_nbr.size());
-        const float* m = c.vertices;
-        float cx = 0, cy = 0, cz = 0;
-        for (int j = 0; j < pic; ++j) {
-            float best = std::numeric_limits<float>::max();
-            for (int k = 0; k < pic; ++k) {
-                if (j == k) continue;
-                double len = std::sqrt(std::pow((double)(m[3 * j] - m[3 * k]), 2) +
-                                       std::pow((double)(m[3 * j + 1] - m[3 * k + 1]), 2) +
-                                       std::pow((double)(m[3 * j + 2] - m[3 * k + 2]), 2)) /
-                             (2 * (double)s->p.bounding_spheres_coeff);
-                if (len < best) best = (float)len;
+            cx /= pic; cy /= pic; cz /= pic;
+            for (int j = 0; j < pic; ++j) {
+                float dx = m[3 * j] - cx, dy = m[3 * j + 1] - cy, dz = m[3 * j + 2] - cz;
+                r0.push_back(sqrtf(dx * dx + dy * dy + dz * dz));
+                respawn.push_back(make_float4(m[3 * j] - m[0], m[3 * j + 1] - m[1], m[3 * j + 2] - m[2], 0.f));
             }
-            radius_model.push_back(c.collision_radius ? c.collision_radius[j] : best);
-            cx += m[3 * j]; cy += m[3 * j + 1]; cz += m[3 * j + 2];
+            const int type_index = (int)s->types.size();
+            s->types.push_back(td);
+            // Work items: whole cells, at most kMaxChunk particles per CTA.
+            int per = std::max(1, std::min(kMaxCellsPerChunk, kMaxChunk / pic));
+            for (int c0 = 0; c0 < c.count; c0 += per)
+                s->work_host.push_back(WorkItem{type_index, c0, std::min(per, c.count - c0)});
+            pstart += c.count * pic;
+            cstart += c.count;
+            cglobal += c.count;
+            mstart += pic;
         }
-        cx /= pic; cy /= pic; cz /= pic;
-        for (int j = 0; j < pic; ++j) {
-            float dx = m[3 * j] - cx, dy = m[3 * j + 1] - cy, dz = m[3 * j + 2] - cz;
-            r0.push_back(sqrtf(dx * dx + dy * dy + dz * dz));
-            respawn.push_back(make_float4(m[3 * j] - m[0], m[3 * j + 1] - m[1], m[3 * j + 2] - m[2], 0.f));
-        }
-        s->types.push_back(td);
-        // Work items: whole cells, at most kMaxChunk particles per CTA.
-        int per = std::max(1, std::min(kMaxCellsPerChunk, kMaxChunk / pic));
-        for (int c0 = 0; c0 < c.count; c0 += per) s->work_host.push_back(WorkItem{t, c0, std::min(per, c.count - c0)});
-        pstart += c.count * pic;
-        cstart += c.count;
-        mstart += pic;
-    }
-    s->N = pstart;
-    s->C = cstart;
-    std::vector<float> radius_particle(s->N);
-    for (const TypeDev& td : s->types)
-        for (int i = 0; i < td.count * td.pic; ++i)
-            radius_particle[td.particle_start + i] = radius_model[td.model_start + i % td.pic];
+        sd.particle_end = pstart;
+        s->scene_cells.push_back(cstart);
+        s->scene_cell_start.push_back(cglobal - cstart);
 
-    // ---- vein: bounds (vein_factory.hpp:21-86), neighbours (:130-174)
-    const bcs_vein& vn = d->vein;
-    s->V = vn.vertex_count;
-    s->T = vn.triangle_count;
-    float mn[3] = {vn.positions[0], vn.positions[1], vn.positions[2]}, mx[3] = {mn[0], mn[1], mn[2]};
-    for (int i = 1; i < s->V; ++i)
-        for (int k = 0; k < 3; ++k) {
-            mn[k] = std::min(mn[k], vn.positions[3 * i + k]);
-            mx[k] = std::max(mx[k], vn.positions[3 * i + k]);
-        }
-    s->minX = mn[0] - s->p.grid_xz_margin; s->maxX = mx[0] + s->p.grid_xz_margin;
-    s->minY = mn[1] - s->p.grid_y_margin;  s->maxY = mx[1] + s->p.grid_y_margin;
-    s->minZ = mn[2] - s->p.grid_xz_margin; s->maxZ = mx[2] + s->p.grid_xz_margin;
-    s->width = s->maxX - s->minX; s->height = s->maxY - s->minY; s->depth = s->maxZ - s->minZ;
-    auto geometry = [&](DeviceGrid& dg, int kind, float cw, float ch, float cd) -> bcs_status {
-        GridDev& g = dg.g;
-        g.uniform = kind == BCS_GRID_UNIFORM;
-        g.lo[0] = s->minX; g.lo[1] = s->minY; g.lo[2] = s->minZ;
-        g.hi[0] = s->maxX; g.hi[1] = s->maxY; g.hi[2] = s->maxZ;
-        g.ext[0] = s->width; g.ext[1] = s->height; g.ext[2] = s->depth;
-        g.cell[0] = cw; g.cell[1] = ch; g.cell[2] = cd;
-        g.cx = (int)(s->width / cw); g.cy = (int)(s->height / ch); g.cz = (int)(s->depth / cd);
-        g.cells = (long long)g.cx * g.cy * g.cz;
-        if (g.uniform && (g.cx < 1 || g.cy < 1 || g.cz < 1 || g.cells > INT32_MAX)) return BCS_ERR_INVALID_ARGUMENT;
-        return BCS_OK;
-    };
-    if ((st = geometry(s->pg, s->p.particle_grid, s->p.cell_width, s->p.cell_height, s->p.cell_depth)) ||
-        (st = geometry(s->tg, s->p.triangle_grid, s->p.cell_width_triangles, s->p.cell_height_triangles,
-                       s->p.cell_depth_triangles)))
-        return st;
-    std::vector<int> nb_ids((size_t)9 * s->V, -1);
-    std::vector<float> nb_len((size_t)9 * s->V, -1.0f);
-    {
-        std::vector<std::vector<uint32_t>> nb(s->V);
-        for (int t = 0; t < s->T; ++t) {
+        // ---- vein: bounds (vein_factory.hpp:21-86), neighbours (:130-174)
+        const bcs_vein& vn = d->vein;
+        const int v0 = (int)vpos.size();
+        s->scene_vertex_start.push_back(v0);
+        s->scene_vertex_count.push_back(vn.vertex_count);
+        sd.tri_start = (int)(tri.size() / 3);
+        for (int i = 0; i < vn.vertex_count; ++i)
+            vpos.push_back(make_float4(vn.positions[3 * i], vn.positions[3 * i + 1], vn.positions[3 * i + 2], 0.f));
+        for (long long k = 0; k < 3LL * vn.triangle_count; ++k) tri.push_back(vn.indices[k] + (uint32_t)v0);
+        sd.tri_end = (int)(tri.size() / 3);
+        float mn[3] = {vn.positions[0], vn.positions[1], vn.positions[2]}, mx[3] = {mn[0], mn[1], mn[2]};
+        for (int i = 1; i < vn.vertex_count; ++i)
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = std::min(mn[k], vn.positions[3 * i + k]);
+                mx[k] = std::max(mx[k], vn.positions[3 * i + k]);
+            }
+        if ((st = scene_grid(mn, mx, sp, sp.cell_width, sp.cell_height, sp.cell_depth, puniform, sd.pg)) ||
+            (st = scene_grid(mn, mx, sp, sp.cell_width_triangles, sp.cell_height_triangles, sp.cell_depth_triangles,
+                             tuniform, sd.tg)))
+            return st;
+        sd.pg.key_offset = key_total;
+        sd.tg.key_offset = tkey_total;
+        key_total += sd.pg.cells;
+        tkey_total += sd.tg.cells;
+        // Wall-proximity mask, cells of half the impact distance (1..8).
+        const float mc = std::min(8.0f, std::max(1.0f, sp.vein_impact_distance * 0.5f));
+        sd.wall.lo[0] = sd.pg.lo[0]; sd.wall.lo[1] = sd.pg.lo[1]; sd.wall.lo[2] = sd.pg.lo[2];
+        sd.wall.inv_cell = 1.0f / mc;
+        sd.wall.nx = (int)std::ceil(sd.pg.ext[0] / mc) + 1;
+        sd.wall.ny = (int)std::ceil(sd.pg.ext[1] / mc) + 1;
+        sd.wall.nz = (int)std::ceil(sd.pg.ext[2] / mc) + 1;
+        sd.wall.offset = mask_total;
+        mask_total += (long long)sd.wall.nx * sd.wall.ny * sd.wall.nz;
+        // vein_end.cu:12-17, FP32 like the constexpr thresholds.
+        sd.upper = sd.pg.hi[1] - 3 * sp.grid_y_margin / 4;
+        sd.lower = sd.pg.lo[1] + sp.grid_y_margin / 2;
+        sd.right = sd.pg.hi[0] - sp.grid_xz_margin / 2;
+        sd.left = sd.pg.lo[0] + sp.grid_xz_margin / 2;
+        sd.front = sd.pg.hi[2] - sp.grid_xz_margin / 2;
+        sd.back = sd.pg.lo[2] + sp.grid_xz_margin / 2;
+        sd.cylinder_radius = sp.cylinder_radius;
+        sd.min_spawn_y = sp.min_spawn_y;
+        sd.seed_lo = (unsigned)sp.seed;
+        sd.seed_hi = (unsigned)(sp.seed >> 32);
+        sd.ending_count = vn.ending_count;
+        for (int k = 0; k < vn.ending_count; ++k)
+            sd.endings[k] = make_float4(vn.ending_centers[3 * k], vn.ending_centers[3 * k + 1],
+                                        vn.ending_centers[3 * k + 2], vn.ending_radii[k]);
+        sd.flow_start = (int)flows.size();
+        sd.flow_count = d->flow_segment_count;
+        for (int k = 0; k < d->flow_segment_count; ++k) flows.push_back(d->flow_segments[k]);
+        // Vein neighbours: both other vertices of every triangle, sorted
+        // ascending, the first nine kept, FP32 rest lengths.
+        std::vector<std::vector<uint32_t>> nb(vn.vertex_count);
+        for (int t = 0; t < vn.triangle_count; ++t) {
             uint32_t i0 = vn.indices[3 * t], i1 = vn.indices[3 * t + 1], i2 = vn.indices[3 * t + 2];
             nb[i0].push_back(i1); nb[i0].push_back(i2);
             nb[i1].push_back(i0); nb[i1].push_back(i2);
             nb[i2].push_back(i0); nb[i2].push_back(i1);
         }
-        for (int i = 0; i < s->V; ++i) {
+        for (int k = 0; k < 9; ++k) {
+            nb_scene_ids[k].resize(v0 + vn.vertex_count, -1);
+            nb_scene_len[k].resize(v0 + vn.vertex_count, -1.0f);
+        }
+        for (int i = 0; i < vn.vertex_count; ++i) {
             std::sort(nb[i].begin(), nb[i].end());
             for (size_t k = 0; k < std::min<size_t>(nb[i].size(), 9); ++k) {
                 uint32_t j = nb[i][k];
@@ -486,11 +564,29 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
                 float dy = vn.positions[3 * i + 1] - vn.positions[3 * j + 1];
                 float dz = vn.positions[3 * i + 2] - vn.positions[3 * j + 2];
                 float l = sqrtf(dx * dx + dy * dy + dz * dz);
-                nb_ids[k * (size_t)s->V + i] = (int)j;
-                nb_len[k * (size_t)s->V + i] = l < 0 ? -l : l;
+                nb_scene_ids[k][v0 + i] = (int)j + v0;
+                nb_scene_len[k][v0 + i] = l < 0 ? -l : l;
             }
         }
+        s->scenes_host.push_back(sd);
     }
+    s->N = pstart;
+    s->C = cglobal;
+    s->V = (int)vpos.size();
+    s->T = (int)(tri.size() / 3);
+    if (key_total > INT32_MAX || tkey_total > INT32_MAX) return BCS_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < 9; ++k) {
+        nb_ids.insert(nb_ids.end(), nb_scene_ids[k].begin(), nb_scene_ids[k].end());
+        nb_len.insert(nb_len.end(), nb_scene_len[k].begin(), nb_scene_len[k].end());
+    }
+    std::vector<float> radius_particle(s->N);
+    for (const TypeDev& td : s->types)
+        for (int i = 0; i < td.count * td.pic; ++i)
+            radius_particle[td.particle_start + i] = radius_model[td.model_start + i % td.pic];
+    s->pg.g.uniform = puniform;
+    s->pg.g.cells = key_total;
+    s->tg.g.uniform = tuniform;
+    s->tg.g.cells = tkey_total;
 
     // ---- device buffers
     for (int b = 0; b < 2; ++b)
@@ -503,13 +599,11 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
         BCS_CUDA(cudaMemset(s->frc[b], 0, sizeof(float4) * s->N));
     }
     if ((st = upload(s, &s->radius_of_particle, radius_particle)) || (st = upload(s, &s->work, s->work_host)) ||
+        (st = upload(s, &s->types_dev, s->types)) || (st = upload(s, &s->scenes, s->scenes_host)) ||
         (st = upload(s, &s->adj_off, adj_off)) || (st = upload(s, &s->adj_nbr, adj_nbr)) ||
-        (st = upload(s, &s->adj_len, adj_len)) || (st = upload(s, &s->r0, r0)) || (st = upload(s, &s->respawn, respawn)))
+        (st = upload(s, &s->adj_len, adj_len)) || (st = upload(s, &s->r0, r0)) ||
+        (st = upload(s, &s->respawn, respawn)) || (st = upload(s, &s->flows, flows)))
         return st;
-    std::vector<float4> vpos(s->V);
-    for (int i = 0; i < s->V; ++i)
-        vpos[i] = make_float4(vn.positions[3 * i], vn.positions[3 * i + 1], vn.positions[3 * i + 2], 0.f);
-    std::vector<uint32_t> tri(vn.indices, vn.indices + 3 * (size_t)s->T);
     if ((st = upload(s, &s->vpos, vpos)) || (st = dalloc(s, &s->vvel, s->V)) || (st = dalloc(s, &s->vfrc, s->V)) ||
         (st = upload(s, &s->nb_ids, nb_ids)) || (st = upload(s, &s->nb_len, nb_len)) || (st = upload(s, &s->tri, tri)) ||
         (st = dalloc(s, &s->tcache, 3 * (size_t)s->T)))
@@ -519,28 +613,17 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
     if ((st = alloc_grid(s, s->pg, s->N, true)) || (st = alloc_grid(s, s->tg, std::max(1, s->T), false))) return st;
     s->tg.count = s->T;
     s->tg.g.count = s->T;
-    if (s->tg.g.uniform) {
-        if ((st = dalloc(s, &s->tbox, 2 * (size_t)s->tg.g.cells))) return st;
+    if (tuniform) {
+        if ((st = dalloc(s, &s->tbox, 2 * (size_t)std::max(1LL, tkey_total)))) return st;
         if (s->p.vein_dynamic && s->T > 0) {
             if ((st = dalloc(s, &s->wall_disp2, 1)) || (st = dalloc(s, &s->wall_ref, s->V))) return st;
             const float huge = 3.0e38f;
             BCS_CUDA(cudaMemcpy(s->wall_disp2, &huge, sizeof(float), cudaMemcpyHostToDevice));
         }
-        // Wall-proximity mask, cells of half the impact distance (1..8).
-        const float mc = std::min(8.0f, std::max(1.0f, s->p.vein_impact_distance * 0.5f));
-        MaskDev& m = s->wall;
-        m.lo[0] = s->minX; m.lo[1] = s->minY; m.lo[2] = s->minZ;
-        m.inv_cell = 1.0f / mc;
-        m.nx = (int)std::ceil(s->width / mc) + 1;
-        m.ny = (int)std::ceil(s->height / mc) + 1;
-        m.nz = (int)std::ceil(s->depth / mc) + 1;
-        const size_t cells = (size_t)m.nx * m.ny * m.nz;
-        if (s->T > 0 && cells <= ((size_t)1 << 30)) {
-            if ((st = dalloc(s, &s->wall_mask, cells)) || (st = dalloc(s, &s->wall_epoch, 1))) return st;
-            BCS_CUDA(cudaMemset(s->wall_mask, 0, cells));
+        if (s->T > 0 && mask_total <= (1LL << 31)) {
+            if ((st = dalloc(s, &s->wall_mask, (size_t)mask_total)) || (st = dalloc(s, &s->wall_epoch, 1))) return st;
+            BCS_CUDA(cudaMemset(s->wall_mask, 0, (size_t)mask_total));
             BCS_CUDA(cudaMemset(s->wall_epoch, 0, sizeof(int)));
-            m.mask = s->wall_mask;
-            m.epoch = s->wall_epoch;
         }
     }
     if ((st = dalloc(s, &s->steps, 1)) || (st = dalloc(s, &s->err, 1))) return st;
@@ -551,8 +634,10 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
     StepArgs& a = s->args;
     a.n = s->N;
     a.work = s->work;
-    for (int t = 0; t < d->type_count; ++t) a.types[t] = s->types[t];
-    a.type_count = d->type_count;
+    a.types = s->types_dev;
+    a.type_count = (int)s->types.size();
+    a.scenes = s->scenes;
+    a.scene_count = s->S;
     a.adj_off = s->adj_off;
     a.adj_nbr = s->adj_nbr;
     a.adj_len = s->adj_len;
@@ -562,20 +647,8 @@ bcs_status create_impl(const bcs_scene_desc* d, void* stream, bcs_sim* s) {
     a.vfrc = s->vfrc;
     a.tri = s->tri;
     a.T = s->T;
-    a.flow_count = d->flow_segment_count;
-    for (int k = 0; k < d->flow_segment_count; ++k) a.flow[k] = d->flow_segments[k];
+    a.flows = s->flows;
     a.p = s->p;
-    // vein_end.cu:12-17, FP32 like the constexpr thresholds.
-    a.upper = s->maxY - 3 * s->p.grid_y_margin / 4;
-    a.lower = s->minY + s->p.grid_y_margin / 2;
-    a.right = s->maxX - s->p.grid_xz_margin / 2;
-    a.left = s->minX + s->p.grid_xz_margin / 2;
-    a.front = s->maxZ - s->p.grid_xz_margin / 2;
-    a.back = s->minZ + s->p.grid_xz_margin / 2;
-    a.ending_count = vn.ending_count;
-    for (int k = 0; k < vn.ending_count; ++k)
-        a.endings[k] = make_float4(vn.ending_centers[3 * k], vn.ending_centers[3 * k + 1], vn.ending_centers[3 * k + 2],
-                                   vn.ending_radii[k]);
     a.steps = s->steps;
     a.err = s->err;
 
@@ -708,16 +781,20 @@ bcs_status bcs_set_device(int device) {
     return BCS_OK;
 }
 
-bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out) {
+bcs_status bcs_create_batch(const bcs_scene_desc* descs, int scene_count, void* stream, bcs_sim** out) {
     if (!out) return BCS_ERR_INVALID_ARGUMENT;
     *out = nullptr;
-    bcs_status st = validate(desc);
-    if (st != BCS_OK) return st;
+    if (!descs || scene_count <= 0) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_status st;
+    for (int k = 0; k < scene_count; ++k) {
+        if ((st = validate(descs + k)) != BCS_OK) return st;
+        if (!same_physics(descs[0].params, descs[k].params)) return BCS_ERR_INVALID_ARGUMENT;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return BCS_ERR_NO_DEVICE;
     bcs_sim* s = new (std::nothrow) bcs_sim();
     if (!s) return BCS_ERR_OUT_OF_MEMORY;
-    st = create_impl(desc, stream, s);
+    st = create_impl(descs, scene_count, stream, s);
     if (st != BCS_OK) {
         destroy_impl(s);
         delete s;
@@ -725,6 +802,14 @@ bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out) {
     }
     *out = s;
     return BCS_OK;
+}
+
+bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out) {
+    if (!desc) {
+        if (out) *out = nullptr;
+        return BCS_ERR_INVALID_ARGUMENT;
+    }
+    return bcs_create_batch(desc, 1, stream, out);
 }
 
 bcs_status bcs_destroy(bcs_sim* s) {
@@ -742,14 +827,42 @@ bcs_status bcs_get_info(bcs_sim* s, bcs_info* o) {
     o->type_count = (int)s->types.size();
     o->vertex_count = s->V;
     o->triangle_count = s->T;
-    o->min_x = s->minX; o->max_x = s->maxX; o->min_y = s->minY; o->max_y = s->maxY; o->min_z = s->minZ; o->max_z = s->maxZ;
-    o->cell_count_x = s->pg.g.cx; o->cell_count_y = s->pg.g.cy; o->cell_count_z = s->pg.g.cz;
+    const SceneDev& z = s->scenes_host[0];
+    o->min_x = z.pg.lo[0]; o->max_x = z.pg.hi[0];
+    o->min_y = z.pg.lo[1]; o->max_y = z.pg.hi[1];
+    o->min_z = z.pg.lo[2]; o->max_z = z.pg.hi[2];
+    o->cell_count_x = z.pg.cx; o->cell_count_y = z.pg.cy; o->cell_count_z = z.pg.cz;
     o->cell_count = s->pg.g.cells;
-    o->tri_cell_count_x = s->tg.g.cx; o->tri_cell_count_y = s->tg.g.cy; o->tri_cell_count_z = s->tg.g.cz;
+    o->tri_cell_count_x = z.tg.cx; o->tri_cell_count_y = z.tg.cy; o->tri_cell_count_z = z.tg.cz;
     o->tri_cell_count = s->tg.g.cells;
     o->steps_done = s->host_steps;
     o->device_bytes = s->bytes;
     o->kernels_per_step = s->kernels_per_step;
+    o->scene_count = s->S;
+    return BCS_OK;
+}
+
+bcs_status bcs_get_scene_info(bcs_sim* s, int k, bcs_scene_info* o) {
+    if (!s || !o || k < 0 || k >= s->S) return BCS_ERR_INVALID_ARGUMENT;
+    std::memset(o, 0, sizeof(*o));
+    const SceneDev& z = s->scenes_host[k];
+    o->particle_start = z.particle_start;
+    o->particle_count = z.particle_end - z.particle_start;
+    o->blood_cell_start = s->scene_cell_start[k];
+    o->blood_cell_count = s->scene_cells[k];
+    o->vertex_start = s->scene_vertex_start[k];
+    o->vertex_count = s->scene_vertex_count[k];
+    o->triangle_start = z.tri_start;
+    o->triangle_count = z.tri_end - z.tri_start;
+    o->min_x = z.pg.lo[0]; o->max_x = z.pg.hi[0];
+    o->min_y = z.pg.lo[1]; o->max_y = z.pg.hi[1];
+    o->min_z = z.pg.lo[2]; o->max_z = z.pg.hi[2];
+    o->cell_count_x = z.pg.cx; o->cell_count_y = z.pg.cy; o->cell_count_z = z.pg.cz;
+    o->cell_count = z.pg.cells;
+    o->cell_key_offset = z.pg.key_offset;
+    o->tri_cell_count_x = z.tg.cx; o->tri_cell_count_y = z.tg.cy; o->tri_cell_count_z = z.tg.cz;
+    o->tri_cell_count = z.tg.cells;
+    o->tri_cell_key_offset = z.tg.key_offset;
     return BCS_OK;
 }
 

@@ -1,21 +1,25 @@
 // bcs_internal.cuh — device-side data layout and math shared by the kernels.
 //
-// HBM layout (one scene, N particles, V vein vertices, T triangles):
-//   pos[2], vel[2], frc[2]   float4 x N each, ping-pong.  pos.w carries the
-//                            particle's collision radius (constant), so a
+// A simulation holds one or more independent scenes (a batch).  Every scene
+// keeps its own coordinates, so its FP32 arithmetic is the same as when it
+// runs alone; the scenes share one set of buffers and one launch per kernel.
+//
+// HBM layout (batch of S scenes, N particles, V vein vertices, T triangles):
+//   pos[2], vel[2], frc[2]   float4 x N each, ping-pong, scene-major.  pos.w
+//                            carries the particle's collision radius, so a
 //                            neighbour gather returns position and radius in
 //                            one 16-byte load.
-//   pkeys[2], pids[2]        int32 x N, grid keys / particle ids (radix-sort
-//                            ping-pong); after the sort they are the
-//                            reference's gridCellIds / particleIds.
-//   ptable                   int4 x (grid cells): (first, last, epoch) of
-//                            every occupied cell.  Never cleared: each grid
+//   particle grid            keys live in one batch-wide key space: a scene's
+//                            cell c has key key_offset(scene) + c, so one sort
+//                            and one table serve every scene.
+//   ptable                   int4 x (all scenes' cells): (first, last, epoch)
+//                            of every occupied cell.  Never cleared: each grid
 //                            build bumps the grid's epoch and rewrites exactly
 //                            the occupied cells, so an entry is trusted only
 //                            when its epoch is current; stale entries of
 //                            emptied cells are rejected with no clear pass and
 //                            no second, dependent load.
-//   vpos, vvel, vfrc         float4 x V (vein)
+//   vpos, vvel, vfrc         float4 x V (all scenes' veins, scene-major)
 //   vnb_ids[9], vnb_len[9]   int32 / float x V, the reference's nine
 //                            neighbour-slot arrays (VeinNeighbors)
 //   tkeys, tids, ttable      triangle grid, same representation as particles
@@ -27,6 +31,8 @@
 //                            for ray culling
 //   wall_mask                uint8 per wall-mask cell: the mask epoch where a
 //                            triangle lies within vein_impact_distance of the cell
+//   scenes, types, work      per-scene geometry, per (scene, cell type) ranges,
+//                            per-CTA work items (device arrays)
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -35,19 +41,20 @@
 
 namespace bcs {
 
-constexpr int kMaxTypes = 16;
-constexpr int kMaxFlow = 8;
 constexpr int kStepThreads = 256;
 constexpr int kMaxChunk = 2 * kStepThreads;   // particles per CTA of the step kernel
 constexpr int kMaxCellsPerChunk = 64;
+constexpr int kMaxEndings = 8;
 
-struct TypeDev {
-    int count;            // cells of the type
+struct TypeDev {          // one cell type of one scene
+    int count;            // cells
     int pic;              // particles per cell
-    int particle_start;   // first particle
-    int cell_start;       // first cell (global cell index)
+    int particle_start;   // first particle (batch-wide)
+    int cell_start;       // first cell within the scene (respawn counter)
+    int cell_global;      // first cell, batch-wide
     int model_start;      // first model vertex in the per-model tables
-    int adj_start;        // CSR offsets start (model_start + type index)
+    int adj_start;        // CSR offsets start for the model
+    int scene;
 };
 
 struct WorkItem {         // one CTA of the step kernel: whole cells of one type
@@ -56,27 +63,44 @@ struct WorkItem {         // one CTA of the step kernel: whole cells of one type
     int ncells;
 };
 
-struct GridDev {
-    int uniform;
+struct GridGeom {         // one scene's uniform grid (uniform_grid.cu:83-104)
     float lo[3];          // minX, minY, minZ
     float hi[3];          // maxX, maxY, maxZ
     float ext[3];         // width, height, depth
     float cell[3];        // cell width, height, depth
     int cx, cy, cz;       // cell counts (int(extent / cell))
     long long cells;
+    long long key_offset; // first key of the scene in the batch key space
+};
+
+struct MaskGeom {         // one scene's wall-proximity mask
+    float lo[3];
+    float inv_cell;
+    int nx, ny, nz;
+    long long offset;     // first byte of the scene in the mask array
+};
+
+struct SceneDev {
+    GridGeom pg, tg;
+    MaskGeom wall;
+    float upper, lower, right, left, front, back;   // vein-end thresholds
+    float cylinder_radius, min_spawn_y;
+    unsigned seed_lo, seed_hi;
+    int ending_count;
+    float4 endings[kMaxEndings];                    // (cx, cy, cz, r)
+    int flow_start, flow_count;
+    int particle_start, particle_end;
+    int tri_start, tri_end;
+};
+
+struct GridDev {          // batch-wide sorted grid
+    int uniform;
+    long long cells;      // table entries (all scenes)
     const int* keys;      // sorted keys
     const int* ids;       // sorted object ids
     const int4* table;    // (first, last, epoch) per cell
     const int* epoch;     // current epoch of the table
     int count;            // objects
-};
-
-struct MaskDev {          // wall-proximity mask over the grid box
-    const unsigned char* mask;
-    const int* epoch;     // low byte is the current mark
-    float lo[3];
-    float inv_cell;
-    int nx, ny, nz;
 };
 
 struct StepArgs {
@@ -92,9 +116,11 @@ struct StepArgs {
     int n;
     // layout
     const WorkItem* work;
-    TypeDev types[kMaxTypes];
+    const TypeDev* types;
     int type_count;
-    const int* adj_off;   // [sum(pic)+types] CSR offsets per model vertex
+    const SceneDev* scenes;
+    int scene_count;
+    const int* adj_off;   // CSR offsets per model vertex
     const int* adj_nbr;   // neighbour index within the cell
     const float* adj_len; // rest length
     const float* r0;      // per model vertex: distance to the model centroid
@@ -104,19 +130,15 @@ struct StepArgs {
     // vein
     const float4* vpos;
     float4* vfrc;
-    const uint32_t* tri;  // 3 * T vertex indices
+    const uint32_t* tri;  // 3 * T vertex indices (batch-wide)
     const float4* tcache; // 3 per sorted triangle slot
     const float4* tbox;   // 2 per triangle-grid cell
-    MaskDev wall;
+    const unsigned char* wall_mask;
+    const int* wall_epoch;
     int T;
-    // flow
-    bcs_flow_segment flow[kMaxFlow];
-    int flow_count;
-    // constants
+    const bcs_flow_segment* flows;
+    // constants shared by all scenes
     bcs_params p;
-    float upper, lower, right, left, front, back;   // vein-end thresholds
-    int ending_count;
-    float4 endings[8];    // (cx, cy, cz, r)
     const long long* steps;  // device step counter
     unsigned* err;        // device error word
 };
@@ -164,10 +186,11 @@ __host__ __device__ inline float uniform_open(uint32_t r) {
     return (float)((r >> 9) * 2u + 1u) * (1.0f / 16777216.0f);
 }
 
-// Grid key of a position, FP32 arithmetic identical to calculateIdForCell
-// (src/grids/uniform_grid.cu:24-36): per axis int(min(extent, max(0,
-// (p - min) / cell))), then clamped to the last cell (the reference's extent
-// clamp can step past it).  Out-of-box positions raise BCS_ERRW_OUT_OF_GRID.
+// Grid key of a position within its scene, FP32 arithmetic identical to
+// calculateIdForCell (src/grids/uniform_grid.cu:24-36): per axis int(min(
+// extent, max(0, (p - min) / cell))), then clamped to the last cell (the
+// reference's extent clamp can step past it).  Out-of-box positions raise
+// BCS_ERRW_OUT_OF_GRID.  The batch key adds the scene's key offset.
 __device__ inline int axis_index(float p, float lo, float ext, float cell, int count) {
     float t = __fdiv_rn(p - lo, cell);
     float m = 0.0f > t ? 0.0f : t;
@@ -177,7 +200,7 @@ __device__ inline int axis_index(float p, float lo, float ext, float cell, int c
     return i < 0 ? 0 : i;
 }
 
-__device__ inline int grid_key(const GridDev& g, float3 q, unsigned& e) {
+__device__ inline int local_key(const GridGeom& g, float3 q, unsigned& e) {
     if (q.x < g.lo[0] || q.x > g.hi[0] || q.y < g.lo[1] || q.y > g.hi[1] || q.z < g.lo[2] || q.z > g.hi[2])
         e |= BCS_ERRW_OUT_OF_GRID;
     int ix = axis_index(q.x, g.lo[0], g.ext[0], g.cell[0], g.cx);
@@ -186,16 +209,32 @@ __device__ inline int grid_key(const GridDev& g, float3 q, unsigned& e) {
     return iz * g.cx * g.cy + iy * g.cx + ix;
 }
 
-// Lookup of an occupied cell's (first, last) sorted slots: valid only when
-// the entry carries the grid's current epoch.
-__device__ inline bool cell_range(const GridDev& g, int epoch, long long c, int& first, int& last) {
-    if (c < 0 || c >= g.cells) return false;
-    int4 r = __ldg(&g.table[c]);
+__device__ inline int grid_key(const GridGeom& g, float3 q, unsigned& e) {
+    return (int)(g.key_offset + local_key(g, q, e));
+}
+
+// Lookup of an occupied cell's (first, last) sorted slots, cell given
+// within the scene: valid only when the entry carries the current epoch.
+__device__ inline bool cell_range(const GridDev& g, const GridGeom& geo, int epoch, long long c, int& first,
+                                  int& last) {
+    if (c < 0 || c >= geo.cells) return false;
+    int4 r = __ldg(&g.table[geo.key_offset + c]);
     if (r.z != epoch) return false;
     first = r.x;
     last = r.y;
     return true;
 }
 
+// Index of the range holding `x` among `n` ascending starts (start_of(0) <= x).
+template <class T, class F>
+__device__ inline int find_range(int n, T x, F start_of) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (start_of(mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 }  // namespace bcs

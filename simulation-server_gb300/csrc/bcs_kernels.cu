@@ -35,13 +35,13 @@ __device__ inline float3 cell_spring(const bcs_params& p, float3 dP, float3 dv, 
 // accumulateEnvironmentForcesForParticles (physics.cuh:102-120); the
 // constant G is replaced by the nearest segment's Poiseuille profile when
 // flow segments are given.
-__device__ inline float3 environment(const StepArgs& a, float3 x, float3 v, float ratio) {
+__device__ inline float3 environment(const StepArgs& a, const SceneDev& sc, float3 x, float3 v, float ratio) {
     const bcs_params& p = a.p;
     float3 g = f3(p.gravity[0], p.gravity[1], p.gravity[2]);
-    if (a.flow_count > 0) {
+    if (sc.flow_count > 0) {
         float best = 3.0e38f;
-        for (int k = 0; k < a.flow_count; ++k) {
-            const bcs_flow_segment& s = a.flow[k];
+        for (int k = 0; k < sc.flow_count; ++k) {
+            const bcs_flow_segment& s = a.flows[sc.flow_start + k];
             float3 o = f3(s.origin[0], s.origin[1], s.origin[2]);
             float3 d = f3(s.direction[0], s.direction[1], s.direction[2]);
             float t = dot3(x - o, d);
@@ -132,9 +132,11 @@ __device__ inline unsigned to_u32_sat(float t) { return t <= 0.f ? 0u : (t >= 42
 // calculateParticleCollisions<UniformGrid> (particle_collisions.cuh:26-38,
 // 53-83,104-269) for one particle; the 3 cells of a stencil row are
 // consecutive keys, so each row is one contiguous range of sorted slots.
-__device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 x, float3 v, float R, unsigned& e) {
+__device__ inline float3 particle_collisions(const StepArgs& a, const SceneDev& sc, int pid, float3 x, float3 v,
+                                            float R, unsigned& e) {
     float3 acc = f3(0.f, 0.f, 0.f);
     const GridDev& g = a.pg;
+    const GridGeom& geo = sc.pg;
     auto test = [&](int q) {
         const float4 pq = __ldg(&a.pos_in[q]);
         float3 rp = x - xyz(pq);
@@ -143,27 +145,27 @@ __device__ inline float3 particle_collisions(const StepArgs& a, int pid, float3 
         if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[q])), d2, R, 0.5f, e);
     };
     if (!g.uniform) {
-        for (int q = 0; q < a.n; ++q)
+        for (int q = sc.particle_start; q < sc.particle_end; ++q)
             if (q != pid) test(q);
         return acc;
     }
     unsigned dummy = 0;
     const int ep = __ldg(g.epoch);
-    const int cellId = grid_key(g, x, dummy);
-    const int xId = (int)__fdiv_rn(x.x - g.lo[0], g.cell[0]);
-    const int yId = (int)__fdiv_rn(x.y - g.lo[1], g.cell[1]);
-    const int zId = (int)__fdiv_rn(x.z - g.lo[2], g.cell[2]);
+    const int cellId = local_key(geo, x, dummy);
+    const int xId = (int)__fdiv_rn(x.x - geo.lo[0], geo.cell[0]);
+    const int yId = (int)__fdiv_rn(x.y - geo.lo[1], geo.cell[1]);
+    const int zId = (int)__fdiv_rn(x.z - geo.lo[2], geo.cell[2]);
     int x0, x1, y0, y1, z0, z1;
-    stencil_range(xId, g.cx, x0, x1);
-    stencil_range(yId, g.cy, y0, y1);
-    stencil_range(zId, g.cz, z0, z1);
-    const long long cxy = (long long)g.cx * g.cy;
+    stencil_range(xId, geo.cx, x0, x1);
+    stencil_range(yId, geo.cy, y0, y1);
+    stencil_range(zId, geo.cz, z0, z1);
+    const long long cxy = (long long)geo.cx * geo.cy;
     for (int dz = z0; dz <= z1; ++dz)
         for (int dy = y0; dy <= y1; ++dy) {
-            const long long row = (long long)cellId + dz * cxy + (long long)dy * g.cx;
+            const long long row = (long long)cellId + dz * cxy + (long long)dy * geo.cx;
             int first = -1, last = -2, f, l;
             for (int dx = x0; dx <= x1; ++dx)
-                if (cell_range(g, ep, row + dx, f, l)) {
+                if (cell_range(g, geo, ep, row + dx, f, l)) {
                     if (first < 0) first = f;
                     last = l;
                 }
@@ -205,17 +207,19 @@ __device__ inline float ray_box_entry(float3 o, float3 d, float3 inv, float4 lo,
 //  * a stencil cell whose triangle bounds the ray does not enter holds no hit,
 //    and once every remaining cell is entered only beyond the impact distance,
 //    the first hit, if any, is too far: no collision.
-__device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, float3& F, float R, unsigned& e) {
+__device__ inline void vein_collision(const StepArgs& a, const SceneDev& sc, float3 x, float3& v, float3& F,
+                                      float R, unsigned& e) {
     const bcs_params& p = a.p;
     const GridDev& g = a.tg;
+    const GridGeom& geo = sc.tg;
     const float reach = p.vein_impact_distance * 1.001f + 1e-3f;
-    if (g.uniform && a.wall.mask) {
-        const MaskDev& m = a.wall;
+    if (g.uniform && a.wall_mask) {
+        const MaskGeom& m = sc.wall;
         int ix = (int)((x.x - m.lo[0]) * m.inv_cell), iy = (int)((x.y - m.lo[1]) * m.inv_cell),
             iz = (int)((x.z - m.lo[2]) * m.inv_cell);
         if (ix >= 0 && iy >= 0 && iz >= 0 && ix < m.nx && iy < m.ny && iz < m.nz) {
-            const unsigned char mark = (unsigned char)__ldg(m.epoch);
-            if (__ldg(&m.mask[((long long)iz * m.ny + iy) * m.nx + ix]) != mark) return;
+            const unsigned char mark = (unsigned char)__ldg(a.wall_epoch);
+            if (__ldg(&a.wall_mask[m.offset + ((long long)iz * m.ny + iy) * m.nx + ix]) != mark) return;
         }
     }
     const float3 vel = v;
@@ -234,20 +238,20 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
         return false;
     };
     if (!g.uniform) {
-        for (int s = 0; s < a.T; ++s)
+        for (int s = sc.tri_start; s < sc.tri_end; ++s)
             if (test_slot(s)) break;
     } else {
         unsigned dummy = 0;
         const int ep = __ldg(g.epoch);
-        const unsigned cellId = (unsigned)grid_key(g, x, dummy);
-        const unsigned xId = to_u32_sat(__fdiv_rn(x.x - g.lo[0], g.cell[0]));
-        const unsigned yId = to_u32_sat(__fdiv_rn(x.y - g.lo[1], g.cell[1]));
-        const unsigned zId = to_u32_sat(__fdiv_rn(x.z - g.lo[2], g.cell[2]));
+        const unsigned cellId = (unsigned)local_key(geo, x, dummy);
+        const unsigned xId = to_u32_sat(__fdiv_rn(x.x - geo.lo[0], geo.cell[0]));
+        const unsigned yId = to_u32_sat(__fdiv_rn(x.y - geo.lo[1], geo.cell[1]));
+        const unsigned zId = to_u32_sat(__fdiv_rn(x.z - geo.lo[2], geo.cell[2]));
         int x0, x1, y0, y1, z0, z1;
-        stencil_range_u(xId, g.cx, x0, x1);
-        stencil_range_u(yId, g.cy, y0, y1);
-        stencil_range_u(zId, g.cz, z0, z1);
-        const long long cxy = (long long)g.cx * g.cy;
+        stencil_range_u(xId, geo.cx, x0, x1);
+        stencil_range_u(yId, geo.cy, y0, y1);
+        stencil_range_u(zId, geo.cz, z0, z1);
+        const long long cxy = (long long)geo.cx * geo.cy;
         // Pass 1: which stencil cells the ray enters (bit k, in stencil
         // order) and the last one it enters within reach.
         const float3 inv = f3(__frcp_rn(dir.x), __frcp_rn(dir.y), __frcp_rn(dir.z));
@@ -256,10 +260,11 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
         for (int dx = x0; dx <= x1; ++dx)
             for (int dy = y0; dy <= y1; ++dy)
                 for (int dz = z0; dz <= z1; ++dz, ++k) {
-                    const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
+                    const long long c = (long long)cellId + dz * cxy + (long long)dy * geo.cx + dx;
                     int f, l;
-                    if (!cell_range(g, ep, c, f, l)) continue;
-                    const float te = ray_box_entry(x, dir, inv, __ldg(&a.tbox[2 * c]), __ldg(&a.tbox[2 * c + 1]));
+                    if (!cell_range(g, geo, ep, c, f, l)) continue;
+                    const long long cg = geo.key_offset + c;
+                    const float te = ray_box_entry(x, dir, inv, __ldg(&a.tbox[2 * cg]), __ldg(&a.tbox[2 * cg + 1]));
                     if (te > 2.9e38f) continue;
                     live |= 1u << k;
                     if (te <= reach) last_near = k;
@@ -273,9 +278,9 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
             const int kk = __ffs(live) - 1;
             live &= live - 1u;
             const int dz = z0 + kk % nz, dy = y0 + (kk / nz) % ny, dx = x0 + kk / (nz * ny);
-            const long long c = (long long)cellId + dz * cxy + (long long)dy * g.cx + dx;
+            const long long c = (long long)cellId + dz * cxy + (long long)dy * geo.cx + dx;
             int f, l;
-            if (!cell_range(g, ep, c, f, l)) continue;
+            if (!cell_range(g, geo, ep, c, f, l)) continue;
             bool found = false;
             for (int s2 = f; s2 <= l; ++s2)
                 if (test_slot(s2)) { found = true; break; }
@@ -309,28 +314,36 @@ __device__ inline void vein_collision(const StepArgs& a, float3 x, float3& v, fl
 }
 
 // Vein-end rule of handleVeinEndsBlockSync (src/simulation/vein_end.cu:12-18,73-87).
-__device__ inline bool leaves_vein(const StepArgs& a, float3 q) {
+__device__ inline bool leaves_vein(const SceneDev& sc, float3 q) {
     bool tp = false;
-    for (int k = 0; k < a.ending_count; ++k) {
-        float4 c = a.endings[k];
+    for (int k = 0; k < sc.ending_count; ++k) {
+        float4 c = sc.endings[k];
         float3 d = f3(q.x - c.x, q.y - c.y, q.z - c.z);
         tp = tp || dot3(d, d) <= c.w * c.w;
     }
-    return tp || q.y <= a.lower || q.y >= a.upper || q.x <= a.left || q.x >= a.right || q.z <= a.back ||
-           q.z >= a.front;
+    return tp || q.y <= sc.lower || q.y >= sc.upper || q.x <= sc.left || q.x >= sc.right || q.z <= sc.back ||
+           q.z >= sc.front;
 }
 
 // Respawn of a whole cell at the inflow (vein_end.cu:101-107): one Philox
-// draw per (seed, cell, step) gives the cell's x and z offsets.
-__device__ inline void respawn(const StepArgs& a, int cell_global, long long step, int model_vertex, float3& x,
-                               float3& v) {
-    uint32_t c[4] = {(uint32_t)cell_global, (uint32_t)step, (uint32_t)((unsigned long long)step >> 32), 0u};
-    philox4x32_10(c, (uint32_t)a.p.seed, (uint32_t)(a.p.seed >> 32));
+// draw per (scene seed, cell within the scene, step) gives the cell's x and
+// z offsets.
+__device__ inline void respawn(const StepArgs& a, const SceneDev& sc, int cell_in_scene, long long step,
+                               int model_vertex, float3& x, float3& v) {
+    uint32_t c[4] = {(uint32_t)cell_in_scene, (uint32_t)step, (uint32_t)((unsigned long long)step >> 32), 0u};
+    philox4x32_10(c, sc.seed_lo, sc.seed_hi);
     float ux = uniform_open(c[0]), uz = uniform_open(c[1]);
     float4 off = __ldg(&a.respawn[model_vertex]);
-    x = f3((ux - 0.5f) * 1.2f * a.p.cylinder_radius + off.x, a.p.min_spawn_y + off.y,
-           (uz - 0.5f) * 1.2f * a.p.cylinder_radius + off.z);
+    x = f3((ux - 0.5f) * 1.2f * sc.cylinder_radius + off.x, sc.min_spawn_y + off.y,
+           (uz - 0.5f) * 1.2f * sc.cylinder_radius + off.z);
     v = f3(a.p.init_velocity[0], a.p.init_velocity[1], a.p.init_velocity[2]);
+}
+
+// The scene of a CTA, staged in shared memory.
+__device__ inline void stage_scene(const SceneDev* src, SceneDev* dst) {
+    const int* s = reinterpret_cast<const int*>(src);
+    int* d = reinterpret_cast<int*>(dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(SceneDev) / sizeof(int)); i += blockDim.x) d[i] = s[i];
 }
 
 // ------------------------------------------------------------- k_step ----
@@ -343,12 +356,14 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
     __shared__ float4 s_vel[kMaxChunk];
     __shared__ float4 s_frc[kMaxChunk];
     __shared__ float3 s_cent[kMaxCellsPerChunk];
+    __shared__ SceneDev sc;
 
     const WorkItem w = a.work[blockIdx.x];
     const TypeDev ty = a.types[w.type];
     const int pic = ty.pic;
     const int p0 = ty.particle_start + w.first_cell * pic;
     const int np = w.ncells * pic;
+    stage_scene(a.scenes + ty.scene, &sc);
     for (int i = threadIdx.x; i < np; i += kStepThreads) {
         s_pos[i] = a.pos_in[p0 + i];
         s_vel[i] = a.vel_in[p0 + i];
@@ -387,13 +402,13 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
             F = F + cell_spring(a.p, x - xyz(s_pos[j]), v - xyz(s_vel[j]), fprev, xyz(s_frc[j]), __ldg(&a.adj_len[k]), e);
         }
         const float ratio = len3(x - s_cent[c]) / __ldg(&a.r0[ty.model_start + li]);
-        F = F + environment(a, x, v, ratio);
+        F = F + environment(a, sc, x, v, ratio);
         F = (fprev + F) / 2.0f;
         // Particle-particle collisions.
-        F = F + particle_collisions(a, pid, x, v, px.w, e);
+        F = F + particle_collisions(a, sc, pid, x, v, px.w, e);
         // Particle-vein collision.
         float3 vv = v;
-        vein_collision(a, x, vv, F, px.w, e);
+        vein_collision(a, sc, x, vv, F, px.w, e);
         float3 nx = x, nv = vv;
         if (MODE == kFull) {
             // propagateParticleForcesKernel (blood_cells.cu:155-179), Heun.
@@ -408,7 +423,7 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
         a.vel_out[pid] = make_float4(nv.x, nv.y, nv.z, 0.f);
         a.frc_out[pid] = make_float4(F.x, F.y, F.z, 0.f);
         if (MODE == kFull && a.keys_out) {
-            a.keys_out[pid] = a.pg.uniform ? grid_key(a.pg, nx, e) : 0;
+            a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, nx, e) : 0;
             a.ids_out[pid] = pid;
         }
     }
@@ -419,25 +434,26 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
 // integration of a whole frame: one warp per blood cell ORs the vein-end
 // rule over its particles and respawns the cell; the respawned particles'
 // grid keys are rewritten for the next frame.
-__global__ void __launch_bounds__(256) k_vein_end(const StepArgs a) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    int t = 0, cell = warp;
-    while (t < a.type_count && cell >= a.types[t].count) cell -= a.types[t++].count;
-    if (t >= a.type_count) return;
+__global__ void __launch_bounds__(256) k_vein_end(const StepArgs a, int cells) {
+    const int cell_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (cell_g >= cells) return;
+    const int t = find_range(a.type_count, cell_g, [&](int i) { return a.types[i].cell_global; });
     const TypeDev ty = a.types[t];
+    const SceneDev& sc = a.scenes[ty.scene];
+    const int cell = cell_g - ty.cell_global;
     const int p0 = ty.particle_start + cell * ty.pic;
     bool leave = false;
-    for (int k = lane; k < ty.pic; k += 32) leave = leave || leaves_vein(a, xyz(a.pos_out[p0 + k]));
+    for (int k = lane; k < ty.pic; k += 32) leave = leave || leaves_vein(sc, xyz(a.pos_out[p0 + k]));
     if (!__any_sync(0xffffffffu, leave)) return;
     const long long step = *a.steps;
     unsigned e = 0;
     for (int k = lane; k < ty.pic; k += 32) {
         float3 x, v;
-        respawn(a, ty.cell_start + cell, step, ty.model_start + k, x, v);
+        respawn(a, sc, ty.cell_start + cell, step, ty.model_start + k, x, v);
         const float w = a.pos_out[p0 + k].w;
         a.pos_out[p0 + k] = make_float4(x.x, x.y, x.z, w);
         a.vel_out[p0 + k] = make_float4(v.x, v.y, v.z, 0.f);
-        if (a.keys_out) a.keys_out[p0 + k] = a.pg.uniform ? grid_key(a.pg, x, e) : 0;
+        if (a.keys_out) a.keys_out[p0 + k] = a.pg.uniform ? grid_key(sc.pg, x, e) : 0;
     }
     if (e) atomicOr(a.err, e);
 }
@@ -451,6 +467,7 @@ __global__ void __launch_bounds__(kStepThreads) k_propagate(const StepArgs a) {
     const int pic = ty.pic;
     const int p0 = ty.particle_start + w.first_cell * pic;
     const int np = w.ncells * pic;
+    const SceneDev& sc = a.scenes[ty.scene];
     if (threadIdx.x < w.ncells) s_tp[threadIdx.x] = 0;
     __syncthreads();
     const long long step = *a.steps;
@@ -464,7 +481,7 @@ __global__ void __launch_bounds__(kStepThreads) k_propagate(const StepArgs a) {
         const float3 v1 = v0 + a.p.dt * F;
         nx[r] = x + (0.5f * a.p.dt) * (v1 + v0);
         nv[r] = v1;
-        if (a.p.use_blood_flow && leaves_vein(a, nx[r])) atomicOr(&s_tp[i / pic], 1);
+        if (a.p.use_blood_flow && leaves_vein(sc, nx[r])) atomicOr(&s_tp[i / pic], 1);
     }
     __syncthreads();
 #pragma unroll
@@ -473,7 +490,7 @@ __global__ void __launch_bounds__(kStepThreads) k_propagate(const StepArgs a) {
         if (i >= np) continue;
         const int c = i / pic;
         if (a.p.use_blood_flow && s_tp[c])
-            respawn(a, ty.cell_start + w.first_cell + c, step, ty.model_start + (i - c * pic), nx[r], nv[r]);
+            respawn(a, sc, ty.cell_start + w.first_cell + c, step, ty.model_start + (i - c * pic), nx[r], nv[r]);
         if (!(isfinite(nx[r].x) && isfinite(nx[r].y) && isfinite(nx[r].z))) e |= BCS_ERRW_NONFINITE;
         const float wv = a.pos_out[p0 + i].w;
         a.pos_out[p0 + i] = make_float4(nx[r].x, nx[r].y, nx[r].z, wv);
@@ -483,27 +500,30 @@ __global__ void __launch_bounds__(kStepThreads) k_propagate(const StepArgs a) {
 }
 
 // calculateCellIdKernel (src/grids/uniform_grid.cu:38-49).
-__global__ void k_keys(const float4* __restrict__ pos, int n, GridDev g, int* keys, int* ids, unsigned* err) {
+__global__ void k_keys(const float4* __restrict__ pos, int n, int uniform, const SceneDev* __restrict__ scenes,
+                       int scene_count, int* keys, int* ids, unsigned* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     unsigned e = 0;
-    keys[i] = g.uniform ? grid_key(g, xyz(pos[i]), e) : 0;
+    const int s = find_range(scene_count, i, [&](int k) { return scenes[k].particle_start; });
+    keys[i] = uniform ? grid_key(scenes[s].pg, xyz(pos[i]), e) : 0;
     ids[i] = i;
     if (e) atomicOr(err, e);
 }
 
 // calculateCentersKernel (src/objects/vein_triangles.cu:14-27) fused with
 // the triangle grid's key kernel.
-__global__ void k_tri_keys(const float4* __restrict__ vpos, const uint32_t* __restrict__ tri, int T, GridDev g,
-                           int* keys, int* ids) {
+__global__ void k_tri_keys(const float4* __restrict__ vpos, const uint32_t* __restrict__ tri, int T,
+                           const SceneDev* __restrict__ scenes, int scene_count, int* keys, int* ids) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T) return;
+    const int sidx = find_range(scene_count, t, [&](int k) { return scenes[k].tri_start; });
     float3 a = xyz(vpos[tri[3 * t]]), b = xyz(vpos[tri[3 * t + 1]]), c = xyz(vpos[tri[3 * t + 2]]);
     float3 ctr = f3(__fdiv_rn(__fadd_rn(__fadd_rn(a.x, b.x), c.x), 3.0f),
                     __fdiv_rn(__fadd_rn(__fadd_rn(a.y, b.y), c.y), 3.0f),
                     __fdiv_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), 3.0f));
     unsigned e = 0;
-    keys[t] = grid_key(g, ctr, e);
+    keys[t] = grid_key(scenes[sidx].tg, ctr, e);
     ids[t] = t;
 }
 
@@ -590,7 +610,8 @@ __global__ void k_tri_cache(const int* __restrict__ ids, const uint32_t* __restr
 // cell is farther than `reach` from every triangle.
 __global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict__ ids, int T,
                             const uint32_t* __restrict__ tri, const float4* __restrict__ vpos, float4* box,
-                            MaskDev m, unsigned char* mask, float reach, float margin,
+                            const SceneDev* __restrict__ scenes, int scene_count, unsigned char* mask,
+                            const int* __restrict__ mask_epoch, float reach, float margin,
                             const float* __restrict__ disp2) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= T) return;
@@ -613,16 +634,18 @@ __global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict_
     box[2 * (size_t)k] = make_float4(lo.x, lo.y, lo.z, 0.f);
     box[2 * (size_t)k + 1] = make_float4(hi.x, hi.y, hi.z, 0.f);
     if (!mask) return;
+    const int sidx = find_range(scene_count, (long long)k, [&](int q) { return scenes[q].tg.key_offset; });
+    const MaskGeom& m = scenes[sidx].wall;
     const int x0 = max(0, (int)floorf((lo.x - reach - m.lo[0]) * m.inv_cell));
     const int x1 = min(m.nx - 1, (int)floorf((hi.x + reach - m.lo[0]) * m.inv_cell));
     const int y0 = max(0, (int)floorf((lo.y - reach - m.lo[1]) * m.inv_cell));
     const int y1 = min(m.ny - 1, (int)floorf((hi.y + reach - m.lo[1]) * m.inv_cell));
     const int z0 = max(0, (int)floorf((lo.z - reach - m.lo[2]) * m.inv_cell));
     const int z1 = min(m.nz - 1, (int)floorf((hi.z + reach - m.lo[2]) * m.inv_cell));
-    const unsigned char mark = (unsigned char)*m.epoch;
+    const unsigned char mark = (unsigned char)*mask_epoch;
     for (int z = z0; z <= z1; ++z)
         for (int y = y0; y <= y1; ++y)
-            for (int xx = x0; xx <= x1; ++xx) mask[((long long)z * m.ny + y) * m.nx + xx] = mark;
+            for (int xx = x0; xx <= x1; ++xx) mask[m.offset + ((long long)z * m.ny + y) * m.nx + xx] = mark;
 }
 
 // Largest squared displacement of any vein vertex since the last bounds
@@ -704,12 +727,13 @@ void launch_step(const StepArgs& a, int blocks, int mode, cudaStream_t s) {
 void launch_propagate(const StepArgs& a, int blocks, cudaStream_t s) {
     if (blocks > 0) k_propagate<<<blocks, kStepThreads, 0, s>>>(a);
 }
-void launch_keys(const float4* pos, int n, const GridDev& g, int* keys, int* ids, unsigned* err, cudaStream_t s) {
-    if (n > 0) k_keys<<<BCS_GRID1(n, 256), 0, s>>>(pos, n, g, keys, ids, err);
+void launch_keys(const float4* pos, int n, int uniform, const SceneDev* scenes, int scene_count, int* keys, int* ids,
+                 unsigned* err, cudaStream_t s) {
+    if (n > 0) k_keys<<<BCS_GRID1(n, 256), 0, s>>>(pos, n, uniform, scenes, scene_count, keys, ids, err);
 }
-void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const GridDev& g, int* keys, int* ids,
-                     cudaStream_t s) {
-    if (T > 0) k_tri_keys<<<BCS_GRID1(T, 256), 0, s>>>(vpos, tri, T, g, keys, ids);
+void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const SceneDev* scenes, int scene_count,
+                     int* keys, int* ids, cudaStream_t s) {
+    if (T > 0) k_tri_keys<<<BCS_GRID1(T, 256), 0, s>>>(vpos, tri, T, scenes, scene_count, keys, ids);
 }
 void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, cudaStream_t s) {
     k_next_epoch<<<1, 1, 0, s>>>(epoch);
@@ -720,17 +744,19 @@ void launch_dense_ranges(const int4* table, const int* epoch, long long cells, i
     if (cells > 0) k_dense_ranges<<<BCS_GRID1(cells, 256), 0, s>>>(table, epoch, cells, starts, ends);
 }
 void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s) {
-    if (cells > 0) k_vein_end<<<BCS_GRID1((long long)cells * 32, 256), 0, s>>>(a);
+    if (cells > 0) k_vein_end<<<BCS_GRID1((long long)cells * 32, 256), 0, s>>>(a, cells);
 }
 // Triangle bounds + wall mask.  With disp2 (dynamic wall) the build runs
 // only when a vertex moved more than `margin` since the last one, and the
 // bounds carry that margin.
 void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tri, const float4* vpos, float4* box,
-                      const MaskDev& m, unsigned char* mask, float reach, int* mask_epoch, float margin,
-                      float* disp2, float4* vref, int V, cudaStream_t s) {
+                      const SceneDev* scenes, int scene_count, unsigned char* mask, float reach, int* mask_epoch,
+                      float margin, float* disp2, float4* vref, int V, cudaStream_t s) {
     if (disp2) k_vein_disp<<<BCS_GRID1(V, 256), 0, s>>>(vpos, vref, V, disp2);
     if (mask) k_next_epoch_if<<<1, 1, 0, s>>>(mask_epoch, disp2, margin);
-    if (T > 0) k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box, m, mask, reach + margin, margin, disp2);
+    if (T > 0)
+        k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box, scenes, scene_count, mask, mask_epoch,
+                                                 reach + margin, margin, disp2);
     if (disp2) {
         k_vein_snapshot<<<BCS_GRID1(V, 256), 0, s>>>(vpos, vref, V, disp2, margin);
         k_disp_reset<<<1, 1, 0, s>>>(disp2, margin);

@@ -56,7 +56,7 @@ bcs_status scratch_for_current_device(unsigned** out) {
 }
 
 __global__ void k_keys_soa(const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ z,
-                           int n, bcs::GridDev g, int* keys, int* ids, unsigned* err) {
+                           int n, bcs::GridGeom g, int* keys, int* ids, unsigned* err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     unsigned e = 0;
@@ -80,8 +80,7 @@ extern "C" bcs_status bcs_grid_sort_static(const float* x, const float* y, const
     if (st != BCS_OK) return st;
 
     // Grid geometry exactly as bcs_create derives it (FP32, uniform_grid.cu:83-104).
-    bcs::GridDev g{};
-    g.uniform = 1;
+    bcs::GridGeom g{};
     g.lo[0] = bounds6[0]; g.hi[0] = bounds6[1];
     g.lo[1] = bounds6[2]; g.hi[1] = bounds6[3];
     g.lo[2] = bounds6[4]; g.hi[2] = bounds6[5];

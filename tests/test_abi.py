@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_status_strings_and_version(lib):
-    assert lib.bcs_abi_version() == 1
+    assert lib.bcs_abi_version() == 2
     assert lib.bcs_status_string(0) == b"ok"
     assert lib.bcs_status_string(3) == b"out of device memory"
 
@@ -43,3 +43,44 @@ def test_invalid_arguments_rejected_before_device_work(lib):
     assert lib.bcs_create(C.byref(d), None, C.byref(h)) == 1
     assert not h.value
     assert lib.bcs_step(None, 1) == 1
+
+
+def test_batch_arguments_rejected_before_device_work(lib, tmp_path):
+    import bcs_scenes
+    h = C.c_void_p()
+    assert lib.bcs_create_batch(None, 1, None, C.byref(h)) == 1
+    a = bcs.SceneBuffers(bcs_scenes.tiny_scene(cells=2, seed=1))
+    b = bcs.SceneBuffers(bcs_scenes.tiny_scene(cells=3, seed=2))
+    descs = (bcs.SceneDesc * 2)(a.desc, b.desc)
+    assert lib.bcs_create_batch(descs, 0, None, C.byref(h)) == 1
+    descs[1].params.particle_k_sniff = descs[0].params.particle_k_sniff * 2   # physics must match across a batch
+    assert lib.bcs_create_batch(descs, 2, None, C.byref(h)) == 1
+    assert not h.value
+    assert lib.bcs_get_scene_info(None, 0, None) == 1
+
+
+STRUCTS = {
+    "bcs_vec3": bcs.Vec3, "bcs_cell_type": bcs.CellType, "bcs_vein": bcs.Vein,
+    "bcs_flow_segment": bcs.FlowSegment, "bcs_params": bcs.Params, "bcs_scene_desc": bcs.SceneDesc,
+    "bcs_info": bcs.Info, "bcs_scene_info": bcs.SceneInfo,
+}
+
+
+def test_ctypes_mirror_matches_c_layout(tmp_path):
+    """sizeof/offsetof of every struct in bcs.h, compiled by gcc, against the ctypes mirror."""
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "bcs.h"', "int main(void) {"]
+    for cname, py in STRUCTS.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    for cname, py in STRUCTS.items():
+        assert int(got[cname]) == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, f"{cname}.{fname}"

@@ -221,6 +221,12 @@ def run_ours(args):
         sim.synchronize()
 
     sim.step(args.warmup)
+    tuning, tune_ms = None, None
+    if not args.no_autotune:
+        t, tune_ms = sim.autotune(args.autotune_frames)
+        tuning = t.as_dict()
+    else:
+        tuning = sim.get_tuning().as_dict()
     barrier()
     props = torch.cuda.get_device_properties(local)
     gpu_id = str(getattr(props, "uuid", "") or local)
@@ -285,11 +291,15 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(scene, ws),
+            "config": dict(workload_config(scene, ws), tuning=tuning,
+                           tuning_source="bcs_autotune" if tune_ms is not None else "default",
+                           step_shape=dict(zip(("threads", "particles_per_cta", "ctas_per_sm"),
+                                               bcs.STEP_SHAPES[tuning["step_shape"]]))),
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(24 * n / e2e_steps), "d2h_bytes_per_step": int(12 * n)},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": "bcs::k_step<0>", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": "bcs::k_step<0, {}, {}, {}, {}>".format(*bcs.STEP_SHAPES[tuning["step_shape"]],
+                                                                           "true" if tuning["persistent"] else "false"), "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": ALGO_BYTES_STEP_KERNEL * n,
                          "kernel_ms": k_ms},
@@ -316,6 +326,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--autotune-frames", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

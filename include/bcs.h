@@ -241,6 +241,52 @@ bcs_status bcs_destroy(bcs_sim* sim);
 bcs_status bcs_get_info(bcs_sim* sim, bcs_info* out);
 bcs_status bcs_get_scene_info(bcs_sim* sim, int scene, bcs_scene_info* out);
 
+/* How the frame is launched.  Every setting computes the same particle
+ * state bit for bit (the per-particle arithmetic and its order do not depend
+ * on it); only the speed changes.
+ *   step_shape     launch shape of the fused step kernel, 0..BCS_STEP_SHAPES-1:
+ *                  (threads per CTA, particles per CTA, CTAs per SM) =
+ *                  0 (256, 512, 3), 1 (128, 256, 6), 2 (384, 768, 2),
+ *                  3 (256, 512, 4), 4 (256, 512, 2), 5 (128, 256, 8).
+ *                  A CTA holds whole
+ *                  blood cells, so a shape needs particles_in_cell <= its
+ *                  particles per CTA.
+ *   persistent     0: one CTA per work item; 1: (SMs x resident CTAs) CTAs
+ *                  that pull work items from a device counter.
+ *   spatial_order  0: work items in cell-type order; 1: ordered by scene and
+ *                  by the position of their first particle (y, then x, then
+ *                  z, in 8-unit bricks), refreshed by bcs_set_particles, so
+ *                  CTAs running together touch neighbouring cells.
+ *   full_sort      0: each frame's grid sort starts from the previous
+ *                  frame's order; 1: full radix sort every frame.
+ *   occupancy_filter  1: keep a bitmap of the occupied particle-grid cells
+ *                  (1 bit per cell) and let the collision stencil load only
+ *                  the first and last occupied cell entries of each row.
+ *   sorted_positions  1: the grid build also writes the positions in sorted
+ *                  order, and the collision stencil reads its candidates
+ *                  from there (contiguous) instead of through their ids. */
+typedef struct bcs_tuning {
+    int step_shape;
+    int persistent;
+    int spatial_order;
+    int full_sort;
+    int occupancy_filter;
+    int sorted_positions;
+} bcs_tuning;
+#define BCS_STEP_SHAPES 6
+
+bcs_status bcs_get_tuning(bcs_sim* sim, bcs_tuning* out);
+bcs_status bcs_set_tuning(bcs_sim* sim, const bcs_tuning* tuning);
+
+/* Autotuner: coordinate descent over the tuning fields (each field takes
+ * every valid value with the others held, two sweeps), each trial timed on
+ * `frames` fused frames after two warm-up frames, all starting from the
+ * current state.  It keeps the fastest and restores the state, so the
+ * simulation continues exactly as if the call had not happened.  Writes the choice to *chosen and its mean frame time to
+ * *ms_per_frame (either may be NULL).  Allocates a state snapshot
+ * (48 bytes per particle and per vein vertex) for the duration of the call. */
+bcs_status bcs_autotune(bcs_sim* sim, int frames, bcs_tuning* chosen, float* ms_per_frame);
+
 /* Particle state (positions, velocities, forces) as written by
  * setBloodCellsPositionsFromRandom (simulation_controller.cu:224-243) and
  * read by the renderer from bloodCells.particles.positions[0]

@@ -29,7 +29,9 @@ EXPORTED = [
     "bcs_calculate_grids", "bcs_calculate_next_frame", "bcs_propagate_all", "bcs_step",
     "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
     "bcs_profile_steps", "bcs_grid_sort_static", "bcs_create_batch", "bcs_get_scene_info",
+    "bcs_get_tuning", "bcs_set_tuning", "bcs_autotune",
 ]
+STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
 GRID_SORT_STATIC_MAX = 262144
 PHASES = ("grid", "vein_forces", "particles", "vein_update")
 
@@ -117,6 +119,14 @@ class SceneInfo(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("step_shape", C.c_int), ("persistent", C.c_int), ("spatial_order", C.c_int),
+                ("full_sort", C.c_int), ("occupancy_filter", C.c_int), ("sorted_positions", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -137,6 +147,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_create": ([C.POINTER(SceneDesc), P, C.POINTER(P)], C.c_int),
         "bcs_create_batch": ([C.POINTER(SceneDesc), C.c_int, P, C.POINTER(P)], C.c_int),
         "bcs_get_scene_info": ([P, C.c_int, C.POINTER(SceneInfo)], C.c_int),
+        "bcs_get_tuning": ([P, C.POINTER(Tuning)], C.c_int),
+        "bcs_set_tuning": ([P, C.POINTER(Tuning)], C.c_int),
+        "bcs_autotune": ([P, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)], C.c_int),
         "bcs_destroy": ([P], C.c_int),
         "bcs_get_info": ([P, C.POINTER(Info)], C.c_int),
         "bcs_set_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
@@ -382,6 +395,25 @@ class Simulation:
         w = C.c_uint32()
         _check(self.lib.bcs_get_error_word(self.h, C.byref(w), int(clear)), "bcs_get_error_word")
         return int(w.value)
+
+    # ---- launch tuning ------------------------------------------------------
+    def get_tuning(self) -> Tuning:
+        t = Tuning()
+        _check(self.lib.bcs_get_tuning(self.h, C.byref(t)), "bcs_get_tuning")
+        return t
+
+    def set_tuning(self, step_shape=0, persistent=0, spatial_order=0, full_sort=0, occupancy_filter=0,
+                   sorted_positions=0) -> None:
+        t = Tuning(int(step_shape), int(persistent), int(spatial_order), int(full_sort), int(occupancy_filter),
+                   int(sorted_positions))
+        _check(self.lib.bcs_set_tuning(self.h, C.byref(t)), "bcs_set_tuning")
+
+    def autotune(self, frames: int = 5):
+        """Coordinate-descent search over the tuning; keeps the fastest, state unchanged."""
+        t = Tuning()
+        ms = C.c_float()
+        _check(self.lib.bcs_autotune(self.h, int(frames), C.byref(t), C.byref(ms)), "bcs_autotune")
+        return t, ms.value
 
     def scene_info(self, k: int) -> SceneInfo:
         out = SceneInfo()

@@ -20,13 +20,17 @@
 
 namespace bcs {
 // bcs_kernels.cu
-void launch_step(const StepArgs& a, int blocks, int mode, cudaStream_t s);
+void launch_step(const StepArgs& a, int items, int mode, int shape, int persistent_grid, cudaStream_t s);
+int step_persistent_grid(int mode, int shape);
+void launch_gather_rows(const float4* src, const int* idx, int n, float4* out, cudaStream_t s);
 void launch_propagate(const StepArgs& a, int blocks, cudaStream_t s);
 void launch_keys(const float4* pos, int n, int uniform, const SceneDev* scenes, int scene_count, int* keys, int* ids,
                  unsigned* err, cudaStream_t s);
 void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const SceneDev* scenes, int scene_count,
                      int* keys, int* ids, cudaStream_t s);
-void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, cudaStream_t s);
+void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigned* occ, const int* ids,
+                        const float4* pos, float4* spos, cudaStream_t s);
+void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s);
 void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
                          cudaStream_t s);
 void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s);
@@ -77,6 +81,10 @@ struct DeviceGrid {
     IncrementalBuffers inc{};
     int4* table = nullptr;
     int* epoch = nullptr;
+    unsigned* occ = nullptr;   // occupancy bitmap; while occ_on it holds the
+    bool occ_on = false;       // bits of the cells of s_k[slot]
+    float4* spos = nullptr;    // positions in sorted order, kept while spos_on
+    bool spos_on = false;
     unsigned* temp = nullptr;
     int bits = 0;
     int id_bits = 0;
@@ -95,6 +103,13 @@ struct bcs_sim {
     std::vector<TypeDev> types;
     std::vector<WorkItem> work_host;
     std::vector<SceneDev> scenes_host;
+    bcs_tuning tune{0, 0, 0, 0, 0, 0};
+    int max_pic = 0;
+    int work_capacity = 0;       // work items of the smallest shape
+    int persistent_grid[2] = {0, 0};   // by mode, 0 until first needed
+    int* work_counter = nullptr;
+    int* order_idx = nullptr;    // first particle per work item (spatial order)
+    float4* order_pos = nullptr;
     std::vector<int> scene_cells;       // blood cells per scene
     std::vector<int> scene_cell_start;
     std::vector<int> scene_vertex_start, scene_vertex_count;
@@ -215,6 +230,11 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
     if (dg.g.uniform) {
         if ((st = dalloc(s, &dg.table, (size_t)dg.g.cells))) return st;
         BCS_CUDA(cudaMemset(dg.table, 0, sizeof(int4) * (size_t)dg.g.cells));
+        if (incremental) {
+            const size_t words = (size_t)((dg.g.cells + 31) / 32);
+            if ((st = dalloc(s, &dg.occ, words)) || (st = dalloc(s, &dg.spos, count))) return st;
+            BCS_CUDA(cudaMemset(dg.occ, 0, sizeof(unsigned) * words));
+        }
     }
     dg.bits = bits_for(dg.g.cells);
     return BCS_OK;
@@ -223,7 +243,7 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
 // Sort the grid's unsorted keys into the other result slot and rebuild the
 // range table.  After the first build, a grid flagged incremental starts
 // from the previous order (any permutation works; few movers make it cheap).
-void sort_grid(DeviceGrid& dg, cudaStream_t st) {
+void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr) {
     const int out = dg.slot ^ 1;
     if (dg.incremental && dg.sorted_once) {
         sort_grid_incremental(dg.s_k[dg.slot], dg.s_v[dg.slot], dg.in_k, dg.s_k[out], dg.s_v[out], dg.count, dg.bits,
@@ -237,12 +257,17 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st) {
                          first ? dg.inc.t1_k : dg.s_k[out], first ? dg.inc.t1_v : dg.s_v[out], dg.count, dg.bits,
                          dg.temp, st);
     }
+    // the previous build's cells leave the bitmap before the new ones enter
+    if (dg.occ_on && dg.sorted_once) launch_occ_update(dg.s_k[dg.slot], dg.count, dg.occ, false, st);
     dg.slot = out;
     dg.sorted_once = true;
     dg.g.keys = dg.s_k[dg.slot];
     dg.g.ids = dg.s_v[dg.slot];
     dg.g.table = dg.table;
-    launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, st);
+    dg.g.occ = dg.occ_on ? dg.occ : nullptr;
+    dg.g.spos = dg.spos_on && pos ? dg.spos : nullptr;
+    launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, dg.occ_on ? dg.occ : nullptr, dg.g.ids, pos,
+                       dg.spos_on && pos ? dg.spos : nullptr, st);
 }
 
 void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
@@ -287,7 +312,7 @@ void enqueue_grids(bcs_sim* s) {
         launch_keys(s->pos[s->cur], s->N, s->pg.g.uniform, s->scenes, s->S, s->pg.in_k, s->pg.in_v, s->err, s->stream);
         s->keys_valid = true;
     }
-    if (s->pg.g.uniform) sort_grid(s->pg, s->stream);
+    if (s->pg.g.uniform) sort_grid(s->pg, s->stream, s->pos[s->cur]);
     if (s->p.refresh_triangle_centers) build_triangle_grid(s, true);
     s->grid_ready = true;
 }
@@ -316,7 +341,7 @@ void enqueue_frame(bcs_sim* s, cudaEvent_t* ev = nullptr) {
     if (ev) cudaEventRecord(ev[2], s->stream);
     const int in = s->cur, out = s->cur ^ 1;
     refresh_args(s, in, out, true);
-    launch_step(s->args, (int)s->work_host.size(), 0, s->stream);
+    launch_step(s->args, (int)s->work_host.size(), 0, s->tune.step_shape, s->persistent_grid[0], s->stream);
     if (s->p.use_blood_flow) launch_vein_end(s->args, s->C, s->stream);
     if (ev) cudaEventRecord(ev[3], s->stream);
     enqueue_vein_propagate(s);
@@ -398,6 +423,109 @@ bcs_status scene_grid(const float* mn, const float* mx, const bcs_params& p, flo
     return BCS_OK;
 }
 
+// Work items of the step kernel for one shape: whole cells of one type, at
+// most the shape's particles per CTA and kMaxCellsPerChunk cells.
+std::vector<WorkItem> work_items(const std::vector<TypeDev>& types, int chunk) {
+    std::vector<WorkItem> w;
+    for (int t = 0; t < (int)types.size(); ++t) {
+        const TypeDev& td = types[t];
+        const int per = std::max(1, std::min(kMaxCellsPerChunk, chunk / td.pic));
+        for (int c0 = 0; c0 < td.count; c0 += per) w.push_back(WorkItem{t, c0, std::min(per, td.count - c0)});
+    }
+    return w;
+}
+
+// Brick coordinate of a position for the spatial work order (non-finite
+// values sort last).
+long long brick(float v) {
+    if (!std::isfinite(v)) return std::numeric_limits<long long>::max();
+    return (long long)std::floor((double)v / 8.0);
+}
+
+// Reorder the work items by scene, then by the brick of their first
+// particle (y, x, z), from the current positions.
+bcs_status order_work_spatially(bcs_sim* s) {
+    const int n = (int)s->work_host.size();
+    if (n == 0) return BCS_OK;
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) {
+        const WorkItem& w = s->work_host[i];
+        const TypeDev& t = s->types[w.type];
+        idx[i] = t.particle_start + w.first_cell * t.pic;
+    }
+    BCS_CUDA(cudaMemcpyAsync(s->order_idx, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s->stream));
+    launch_gather_rows(s->pos[s->cur], s->order_idx, n, s->order_pos, s->stream);
+    std::vector<float4> q(n);
+    BCS_CUDA(cudaMemcpyAsync(q.data(), s->order_pos, sizeof(float4) * n, cudaMemcpyDeviceToHost, s->stream));
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    struct Key {
+        int scene;
+        long long y, x, z;
+        int item;
+    };
+    std::vector<Key> k(n);
+    for (int i = 0; i < n; ++i)
+        k[i] = Key{s->types[s->work_host[i].type].scene, brick(q[i].y), brick(q[i].x), brick(q[i].z), i};
+    std::stable_sort(k.begin(), k.end(), [](const Key& a, const Key& b) {
+        if (a.scene != b.scene) return a.scene < b.scene;
+        if (a.y != b.y) return a.y < b.y;
+        if (a.x != b.x) return a.x < b.x;
+        return a.z < b.z;
+    });
+    std::vector<WorkItem> w(n);
+    for (int i = 0; i < n; ++i) w[i] = s->work_host[k[i].item];
+    s->work_host.swap(w);
+    return BCS_OK;
+}
+
+bcs_status upload_work(bcs_sim* s) {
+    BCS_CUDA(cudaStreamSynchronize(s->stream));   // earlier frames may still read the table
+    BCS_CUDA(cudaMemcpyAsync(s->work, s->work_host.data(), sizeof(WorkItem) * s->work_host.size(),
+                             cudaMemcpyHostToDevice, s->stream));
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    s->args.work = s->work;
+    s->args.work_count = (int)s->work_host.size();
+    s->args.work_counter = s->work_counter;
+    return BCS_OK;
+}
+
+bool tuning_valid(const bcs_sim* s, const bcs_tuning& t) {
+    return t.step_shape >= 0 && t.step_shape < kStepShapes && kShapes[t.step_shape].chunk >= s->max_pic &&
+           (t.persistent == 0 || t.persistent == 1) && (t.spatial_order == 0 || t.spatial_order == 1) &&
+           (t.full_sort == 0 || t.full_sort == 1) && (t.occupancy_filter == 0 || t.occupancy_filter == 1) &&
+           (t.sorted_positions == 0 || t.sorted_positions == 1);
+}
+
+bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
+    if (!tuning_valid(s, t)) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    s->tune = t;
+    s->work_host = work_items(s->types, kShapes[t.step_shape].chunk);
+    bcs_status st;
+    if (t.spatial_order && (st = order_work_spatially(s))) return st;
+    if ((st = upload_work(s))) return st;
+    s->pg.incremental = !t.full_sort;
+    const bool occ = t.occupancy_filter && s->pg.occ;
+    if (occ && !s->pg.occ_on) {
+        // start the bitmap from the current sorted cells
+        BCS_CUDA(cudaMemsetAsync(s->pg.occ, 0, sizeof(unsigned) * (size_t)((s->pg.g.cells + 31) / 32), s->stream));
+        if (s->pg.sorted_once) launch_occ_update(s->pg.s_k[s->pg.slot], s->pg.count, s->pg.occ, true, s->stream);
+        BCS_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    s->pg.occ_on = occ;
+    s->pg.g.occ = occ ? s->pg.occ : nullptr;
+    const bool sp = t.sorted_positions && s->pg.spos;
+    if (sp && !s->pg.spos_on && s->pg.sorted_once)
+        launch_gather_rows(s->pos[s->cur], s->pg.s_v[s->pg.slot], s->pg.count, s->pg.spos, s->stream);
+    s->pg.spos_on = sp;
+    s->pg.g.spos = sp && s->pg.sorted_once ? s->pg.spos : nullptr;
+    s->args.pg = s->pg.g;
+    s->persistent_grid[0] = t.persistent ? step_persistent_grid(0, t.step_shape) : 0;
+    s->persistent_grid[1] = t.persistent ? step_persistent_grid(1, t.step_shape) : 0;
+    drop_graphs(s);
+    return check_last();
+}
+
 bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* stream, bcs_sim* s) {
     bcs_status st;
     s->p = descs[0].params;
@@ -477,12 +605,8 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
                 r0.push_back(sqrtf(dx * dx + dy * dy + dz * dz));
                 respawn.push_back(make_float4(m[3 * j] - m[0], m[3 * j + 1] - m[1], m[3 * j + 2] - m[2], 0.f));
             }
-            const int type_index = (int)s->types.size();
             s->types.push_back(td);
-            // Work items: whole cells, at most kMaxChunk particles per CTA.
-            int per = std::max(1, std::min(kMaxCellsPerChunk, kMaxChunk / pic));
-            for (int c0 = 0; c0 < c.count; c0 += per)
-                s->work_host.push_back(WorkItem{type_index, c0, std::min(per, c.count - c0)});
+            s->max_pic = std::max(s->max_pic, pic);
             pstart += c.count * pic;
             cstart += c.count;
             cglobal += c.count;
@@ -598,7 +722,13 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
         BCS_CUDA(cudaMemset(s->vel[b], 0, sizeof(float4) * s->N));
         BCS_CUDA(cudaMemset(s->frc[b], 0, sizeof(float4) * s->N));
     }
-    if ((st = upload(s, &s->radius_of_particle, radius_particle)) || (st = upload(s, &s->work, s->work_host)) ||
+    for (int k = 0; k < kStepShapes; ++k)
+        s->work_capacity = std::max(s->work_capacity, (int)work_items(s->types, kShapes[k].chunk).size());
+    if ((st = dalloc(s, &s->work, s->work_capacity)) || (st = dalloc(s, &s->order_idx, s->work_capacity)) ||
+        (st = dalloc(s, &s->order_pos, s->work_capacity)) || (st = dalloc(s, &s->work_counter, 2)))
+        return st;
+    BCS_CUDA(cudaMemset(s->work_counter, 0, 2 * sizeof(int)));
+    if ((st = upload(s, &s->radius_of_particle, radius_particle)) ||
         (st = upload(s, &s->types_dev, s->types)) || (st = upload(s, &s->scenes, s->scenes_host)) ||
         (st = upload(s, &s->adj_off, adj_off)) || (st = upload(s, &s->adj_nbr, adj_nbr)) ||
         (st = upload(s, &s->adj_len, adj_len)) || (st = upload(s, &s->r0, r0)) ||
@@ -633,7 +763,6 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     // ---- kernel arguments that never change
     StepArgs& a = s->args;
     a.n = s->N;
-    a.work = s->work;
     a.types = s->types_dev;
     a.type_count = (int)s->types.size();
     a.scenes = s->scenes;
@@ -656,7 +785,10 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     build_triangle_grid(s, true);
     if ((st = check_last())) return st;
     BCS_CUDA(cudaStreamSynchronize(s->stream));
-    return BCS_OK;
+    // ---- default launch: the first step shape that holds the largest cell
+    bcs_tuning t{0, 0, 0, 0, 0, 0};
+    while (kShapes[t.step_shape].chunk < s->max_pic) ++t.step_shape;
+    return apply_tuning(s, t);
 }
 
 void destroy_impl(bcs_sim* s) {
@@ -878,7 +1010,11 @@ bcs_status bcs_set_particles(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities
     }
     s->keys_valid = false;
     s->mid_frame = false;
-    return BCS_OK;
+    // a grid built before this call still serves the next calculate_next_frame
+    if (s->pg.spos_on && s->pg.sorted_once)
+        launch_gather_rows(s->pos[s->cur], s->pg.s_v[s->pg.slot], s->pg.count, s->pg.spos, s->stream);
+    if (s->tune.spatial_order && ((st = order_work_spatially(s)) || (st = upload_work(s)))) return st;
+    return check_last();
 }
 
 bcs_status bcs_get_particles(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs_vec3 forces, bcs_memory where) {
@@ -926,7 +1062,7 @@ bcs_status bcs_calculate_next_frame(bcs_sim* s) {
     if (!s->grid_ready) enqueue_grids(s);
     enqueue_vein_forces(s);
     refresh_args(s, s->cur, s->cur ^ 1, false);
-    launch_step(s->args, (int)s->work_host.size(), 1, s->stream);
+    launch_step(s->args, (int)s->work_host.size(), 1, s->tune.step_shape, s->persistent_grid[1], s->stream);
     s->mid_frame = true;
     return check_last();
 }
@@ -998,6 +1134,137 @@ bcs_status bcs_step(bcs_sim* s, int nsteps) {
     bcs_status st = run_steps(s, nsteps);
     if (st != BCS_OK) return st;
     return check_last();
+}
+
+bcs_status bcs_get_tuning(bcs_sim* s, bcs_tuning* out) {
+    if (!s || !out) return BCS_ERR_INVALID_ARGUMENT;
+    *out = s->tune;
+    return BCS_OK;
+}
+
+bcs_status bcs_set_tuning(bcs_sim* s, const bcs_tuning* t) {
+    if (!s || !t || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    return apply_tuning(s, *t);
+}
+
+namespace {
+// Device copy of everything a frame reads and writes that carries physics:
+// particle and vein state, the step counter (respawn draws) and the error
+// word.  The grids, caches and culling structures are rebuilt from it.
+struct Snapshot {
+    float4* particles = nullptr;   // pos, vel, frc
+    float4* vein = nullptr;        // vpos, vvel, vfrc
+    long long* steps = nullptr;
+    unsigned* err = nullptr;
+    long long host_steps = 0;
+    void release() {
+        cudaFree(particles);
+        cudaFree(vein);
+        cudaFree(steps);
+        cudaFree(err);
+    }
+};
+
+bcs_status take_snapshot(bcs_sim* s, Snapshot& z) {
+    const size_t n = (size_t)s->N, v = (size_t)std::max(1, s->V);
+    BCS_CUDA(cudaMalloc(&z.particles, 3 * n * sizeof(float4)));
+    BCS_CUDA(cudaMalloc(&z.vein, 3 * v * sizeof(float4)));
+    BCS_CUDA(cudaMalloc(&z.steps, sizeof(long long)));
+    BCS_CUDA(cudaMalloc(&z.err, sizeof(unsigned)));
+    const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+    BCS_CUDA(cudaMemcpyAsync(z.particles, s->pos[s->cur], n * sizeof(float4), k, s->stream));
+    BCS_CUDA(cudaMemcpyAsync(z.particles + n, s->vel[s->cur], n * sizeof(float4), k, s->stream));
+    BCS_CUDA(cudaMemcpyAsync(z.particles + 2 * n, s->frc[s->cur], n * sizeof(float4), k, s->stream));
+    if (s->V > 0) {
+        BCS_CUDA(cudaMemcpyAsync(z.vein, s->vpos, v * sizeof(float4), k, s->stream));
+        BCS_CUDA(cudaMemcpyAsync(z.vein + v, s->vvel, v * sizeof(float4), k, s->stream));
+        BCS_CUDA(cudaMemcpyAsync(z.vein + 2 * v, s->vfrc, v * sizeof(float4), k, s->stream));
+    }
+    BCS_CUDA(cudaMemcpyAsync(z.steps, s->steps, sizeof(long long), k, s->stream));
+    BCS_CUDA(cudaMemcpyAsync(z.err, s->err, sizeof(unsigned), k, s->stream));
+    z.host_steps = s->host_steps;
+    return BCS_OK;
+}
+
+bcs_status restore_snapshot(bcs_sim* s, const Snapshot& z) {
+    const size_t n = (size_t)s->N, v = (size_t)std::max(1, s->V);
+    const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+    BCS_CUDA(cudaMemcpyAsync(s->pos[s->cur], z.particles, n * sizeof(float4), k, s->stream));
+    BCS_CUDA(cudaMemcpyAsync(s->vel[s->cur], z.particles + n, n * sizeof(float4), k, s->stream));
+    BCS_CUDA(cudaMemcpyAsync(s->frc[s->cur], z.particles + 2 * n, n * sizeof(float4), k, s->stream));
+    if (s->V > 0) {
+        BCS_CUDA(cudaMemcpyAsync(s->vpos, z.vein, v * sizeof(float4), k, s->stream));
+        BCS_CUDA(cudaMemcpyAsync(s->vvel, z.vein + v, v * sizeof(float4), k, s->stream));
+        BCS_CUDA(cudaMemcpyAsync(s->vfrc, z.vein + 2 * v, v * sizeof(float4), k, s->stream));
+    }
+    BCS_CUDA(cudaMemcpyAsync(s->steps, z.steps, sizeof(long long), k, s->stream));
+    BCS_CUDA(cudaMemcpyAsync(s->err, z.err, sizeof(unsigned), k, s->stream));
+    s->host_steps = z.host_steps;
+    s->keys_valid = false;
+    s->grid_ready = false;
+    s->mid_frame = false;
+    if (s->p.vein_dynamic && s->T > 0) {
+        if (s->wall_disp2) {
+            const float huge = 3.0e38f;   // force a bounds / mask rebuild
+            BCS_CUDA(cudaMemcpyAsync(s->wall_disp2, &huge, sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        }
+        build_triangle_grid(s, s->p.refresh_triangle_centers != 0);
+    }
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    return check_last();
+}
+}  // namespace
+
+bcs_status bcs_autotune(bcs_sim* s, int frames, bcs_tuning* chosen, float* ms_per_frame) {
+    if (!s || frames <= 0 || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    Snapshot z;
+    bcs_status st = take_snapshot(s, z);
+    // Coordinate descent from the current tuning: each field in turn takes
+    // every value with the others held; two sweeps.
+    bcs_tuning best = s->tune;
+    float best_ms = std::numeric_limits<float>::max();
+    auto trial = [&](const bcs_tuning& t, float& ms) -> bcs_status {
+        bcs_status r;
+        if ((r = restore_snapshot(s, z)) || (r = apply_tuning(s, t)) || (r = run_steps(s, 2))) return r;
+        if (cudaEventRecord(s->ev0, s->stream) != cudaSuccess) return BCS_ERR_CUDA;
+        if ((r = run_steps(s, frames))) return r;
+        if (cudaEventRecord(s->ev1, s->stream) != cudaSuccess || cudaEventSynchronize(s->ev1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, s->ev0, s->ev1) != cudaSuccess)
+            return BCS_ERR_CUDA;
+        ms /= (float)frames;
+        return BCS_OK;
+    };
+    if (st == BCS_OK) st = trial(best, best_ms);
+    int bcs_tuning::*fields[] = {&bcs_tuning::step_shape, &bcs_tuning::persistent, &bcs_tuning::spatial_order,
+                                 &bcs_tuning::full_sort, &bcs_tuning::occupancy_filter,
+                                 &bcs_tuning::sorted_positions};
+    const int limits[] = {kStepShapes, 2, 2, 2, 2, 2};
+    for (int sweep = 0; sweep < 2 && st == BCS_OK; ++sweep) {
+        bool improved = false;
+        for (int f = 0; f < 6 && st == BCS_OK; ++f)
+            for (int v = 0; v < limits[f] && st == BCS_OK; ++v) {
+                bcs_tuning t = best;
+                if (t.*fields[f] == v) continue;
+                t.*fields[f] = v;
+                if (!tuning_valid(s, t)) continue;
+                float ms = 0.f;
+                if ((st = trial(t, ms))) break;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = t;
+                    improved = true;
+                }
+            }
+        if (!improved) break;
+    }
+    if (st == BCS_OK) st = restore_snapshot(s, z);
+    if (st == BCS_OK) st = apply_tuning(s, best);
+    z.release();
+    if (st != BCS_OK) return st;
+    if (chosen) *chosen = best;
+    if (ms_per_frame) *ms_per_frame = best_ms;
+    return BCS_OK;
 }
 
 bcs_status bcs_get_grid(bcs_sim* s, int which, int* cell_ids, int* object_ids, int* cell_starts, int* cell_ends,

@@ -41,10 +41,20 @@
 
 namespace bcs {
 
-constexpr int kStepThreads = 256;
-constexpr int kMaxChunk = 2 * kStepThreads;   // particles per CTA of the step kernel
+constexpr int kMaxChunk = 768;          // largest particles-per-CTA of any step shape
 constexpr int kMaxCellsPerChunk = 64;
 constexpr int kMaxEndings = 8;
+constexpr int kPropagateThreads = 256;
+
+// Launch shapes of the step kernel: threads per CTA, particles per CTA
+// (whole cells, at most this many) and the CTAs per SM the register budget
+// is sized for.  Every shape computes the same per-particle arithmetic.
+struct StepShape {
+    int threads, chunk, min_blocks;
+};
+constexpr int kStepShapes = 6;
+constexpr StepShape kShapes[kStepShapes] = {
+    {256, 512, 3}, {128, 256, 6}, {384, 768, 2}, {256, 512, 4}, {256, 512, 2}, {128, 256, 8}};
 
 struct TypeDev {          // one cell type of one scene
     int count;            // cells
@@ -100,6 +110,8 @@ struct GridDev {          // batch-wide sorted grid
     const int* ids;       // sorted object ids
     const int4* table;    // (first, last, epoch) per cell
     const int* epoch;     // current epoch of the table
+    const unsigned* occ;  // occupancy bitmap, 1 bit per cell, or null
+    const float4* spos;   // positions in sorted order (particle grid), or null
     int count;            // objects
 };
 
@@ -116,6 +128,8 @@ struct StepArgs {
     int n;
     // layout
     const WorkItem* work;
+    int work_count;
+    int* work_counter;    // persistent launches: next item, CTAs finished
     const TypeDev* types;
     int type_count;
     const SceneDev* scenes;
@@ -191,13 +205,26 @@ __host__ __device__ inline float uniform_open(uint32_t r) {
 // extent, max(0, (p - min) / cell))), then clamped to the last cell (the
 // reference's extent clamp can step past it).  Out-of-box positions raise
 // BCS_ERRW_OUT_OF_GRID.  The batch key adds the scene's key offset.
-__device__ inline int axis_index(float p, float lo, float ext, float cell, int count) {
-    float t = __fdiv_rn(p - lo, cell);
+__device__ inline int axis_clamp(float t, float ext, int count) {
     float m = 0.0f > t ? 0.0f : t;
     float c = ext > m ? m : ext;
     int i = (int)c;
     i = i > count - 1 ? count - 1 : i;
     return i < 0 ? 0 : i;
+}
+
+// The per-axis quotient (p - min) / cell, FP32 IEEE division as in the
+// reference; its truncation is also the stencil's unclamped cell coordinate.
+__device__ inline float axis_quotient(float p, float lo, float cell) { return __fdiv_rn(p - lo, cell); }
+
+__device__ inline int axis_index(float p, float lo, float ext, float cell, int count) {
+    return axis_clamp(axis_quotient(p, lo, cell), ext, count);
+}
+
+// Scene-local key from the three quotients (same int arithmetic as local_key).
+__device__ inline int key_of_quotients(const GridGeom& g, float tx, float ty, float tz) {
+    return axis_clamp(tz, g.ext[2], g.cz) * g.cx * g.cy + axis_clamp(ty, g.ext[1], g.cy) * g.cx +
+           axis_clamp(tx, g.ext[0], g.cx);
 }
 
 __device__ inline int local_key(const GridGeom& g, float3 q, unsigned& e) {

@@ -12,6 +12,7 @@
 // particle's x, v, F cross HBM once per step in each direction.  k_vein_end
 // (handleVeinEndsBlockSync) is a warp-per-cell pass over the new positions.
 #include "bcs_internal.cuh"
+#include <algorithm>
 
 namespace bcs {
 
@@ -137,41 +138,78 @@ __device__ inline float3 particle_collisions(const StepArgs& a, const SceneDev& 
     float3 acc = f3(0.f, 0.f, 0.f);
     const GridDev& g = a.pg;
     const GridGeom& geo = sc.pg;
-    auto test = [&](int q) {
-        const float4 pq = __ldg(&a.pos_in[q]);
-        float3 rp = x - xyz(pq);
-        float d2 = dot3(rp, rp);
-        float md = R + pq.w;
-        if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[q])), d2, R, 0.5f, e);
+    // One candidate: detectCollision's test, then the resilient force with
+    // the neighbour's velocity (fetched only on a hit).
+    auto consider = [&](const float4 pq, auto neighbour) {
+        const float3 rp = x - xyz(pq);
+        const float d2 = dot3(rp, rp);
+        const float md = R + pq.w;
+        if (d2 <= md * md && d2 >= 0.0001f)
+            acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[neighbour()])), d2, R, 0.5f, e);
     };
+    auto test = [&](int q) { consider(__ldg(&a.pos_in[q]), [q] { return q; }); };
     if (!g.uniform) {
         for (int q = sc.particle_start; q < sc.particle_end; ++q)
             if (q != pid) test(q);
         return acc;
     }
-    unsigned dummy = 0;
     const int ep = __ldg(g.epoch);
-    const int cellId = local_key(geo, x, dummy);
-    const int xId = (int)__fdiv_rn(x.x - geo.lo[0], geo.cell[0]);
-    const int yId = (int)__fdiv_rn(x.y - geo.lo[1], geo.cell[1]);
-    const int zId = (int)__fdiv_rn(x.z - geo.lo[2], geo.cell[2]);
+    const float tx = axis_quotient(x.x, geo.lo[0], geo.cell[0]);
+    const float ty = axis_quotient(x.y, geo.lo[1], geo.cell[1]);
+    const float tz = axis_quotient(x.z, geo.lo[2], geo.cell[2]);
+    const int cellId = key_of_quotients(geo, tx, ty, tz);
     int x0, x1, y0, y1, z0, z1;
-    stencil_range(xId, geo.cx, x0, x1);
-    stencil_range(yId, geo.cy, y0, y1);
-    stencil_range(zId, geo.cz, z0, z1);
+    stencil_range((int)tx, geo.cx, x0, x1);
+    stencil_range((int)ty, geo.cy, y0, y1);
+    stencil_range((int)tz, geo.cz, z0, z1);
     const long long cxy = (long long)geo.cx * geo.cy;
+    const int4* __restrict__ table = g.table + geo.key_offset;
     for (int dz = z0; dz <= z1; ++dz)
         for (int dy = y0; dy <= y1; ++dy) {
             const long long row = (long long)cellId + dz * cxy + (long long)dy * geo.cx;
-            int first = -1, last = -2, f, l;
-            for (int dx = x0; dx <= x1; ++dx)
-                if (cell_range(g, geo, ep, row + dx, f, l)) {
-                    if (first < 0) first = f;
-                    last = l;
+            // The row's three cells are consecutive keys, so their occupied
+            // slots form one contiguous sorted range; the three entries are
+            // loaded together.
+            int first = 0x7fffffff, last = -1;
+            if (g.occ) {
+                // Occupied cells of the window from the bitmap: only the
+                // first and the last occupied entries are loaded.
+                const long long ca = max(row + x0, 0LL), cb = min(row + x1, geo.cells - 1);
+                if (ca > cb) continue;
+                const long long ga = geo.key_offset + ca, gb = geo.key_offset + cb;
+                const int sh = (int)(ga & 31);
+                unsigned long long m = __ldg(&g.occ[ga >> 5]) >> sh;
+                if ((gb >> 5) != (ga >> 5)) m |= (unsigned long long)__ldg(&g.occ[gb >> 5]) << (32 - sh);
+                m &= (1ull << (int)(cb - ca + 1)) - 1ull;
+                if (!m) continue;
+                const int lo = __ffsll((long long)m) - 1, hi = 63 - __clzll((long long)m);
+                const int4 r = __ldg(&table[ca + lo]);
+                first = r.x;
+                last = hi != lo ? __ldg(&table[ca + hi]).y : r.y;
+            } else {
+#pragma unroll
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const long long c = row + dx;
+                    if (dx >= x0 && dx <= x1 && c >= 0 && c < geo.cells) {
+                        const int4 r = __ldg(&table[c]);
+                        if (r.z == ep) {
+                            first = min(first, r.x);
+                            last = max(last, r.y);
+                        }
+                    }
                 }
-            for (int j = first; j <= last; ++j) {
-                const int q = __ldg(&g.ids[j]);
-                if (q != pid) test(q);
+            }
+            if (g.spos) {
+                // Sorted positions: contiguous loads; the particle itself
+                // (d2 = 0) fails the d2 >= 1e-4 test, so no id is needed
+                // before a hit.
+                for (int j = first; j <= last; ++j)
+                    consider(__ldg(&g.spos[j]), [&g, j] { return __ldg(&g.ids[j]); });
+            } else {
+                for (int j = first; j <= last; ++j) {
+                    const int q = __ldg(&g.ids[j]);
+                    if (q != pid) test(q);
+                }
             }
         }
     return acc;
@@ -241,12 +279,12 @@ __device__ inline void vein_collision(const StepArgs& a, const SceneDev& sc, flo
         for (int s = sc.tri_start; s < sc.tri_end; ++s)
             if (test_slot(s)) break;
     } else {
-        unsigned dummy = 0;
         const int ep = __ldg(g.epoch);
-        const unsigned cellId = (unsigned)local_key(geo, x, dummy);
-        const unsigned xId = to_u32_sat(__fdiv_rn(x.x - geo.lo[0], geo.cell[0]));
-        const unsigned yId = to_u32_sat(__fdiv_rn(x.y - geo.lo[1], geo.cell[1]));
-        const unsigned zId = to_u32_sat(__fdiv_rn(x.z - geo.lo[2], geo.cell[2]));
+        const float tx = axis_quotient(x.x, geo.lo[0], geo.cell[0]);
+        const float ty = axis_quotient(x.y, geo.lo[1], geo.cell[1]);
+        const float tz = axis_quotient(x.z, geo.lo[2], geo.cell[2]);
+        const unsigned cellId = (unsigned)key_of_quotients(geo, tx, ty, tz);
+        const unsigned xId = to_u32_sat(tx), yId = to_u32_sat(ty), zId = to_u32_sat(tz);
         int x0, x1, y0, y1, z0, z1;
         stencil_range_u(xId, geo.cx, x0, x1);
         stencil_range_u(yId, geo.cy, y0, y1);
@@ -350,21 +388,18 @@ __device__ inline void stage_scene(const SceneDev* src, SceneDev* dst) {
 constexpr int kFull = 0;    // whole frame: forces, integration, vein end, next keys
 constexpr int kForces = 1;  // calculateNextFrame only: forces and collision velocities
 
-template <int MODE>
-__global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
-    __shared__ float4 s_pos[kMaxChunk];
-    __shared__ float4 s_vel[kMaxChunk];
-    __shared__ float4 s_frc[kMaxChunk];
-    __shared__ float3 s_cent[kMaxCellsPerChunk];
-    __shared__ SceneDev sc;
-
-    const WorkItem w = a.work[blockIdx.x];
+// One work item: stage the cells, then per particle springs, environment,
+// collisions, the vein ray and (MODE kFull) integration and next keys.
+template <int MODE, int THREADS>
+__device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, float4* s_vel, float4* s_frc,
+                                 float3* s_cent, SceneDev& sc) {
+    const WorkItem w = a.work[item];
     const TypeDev ty = a.types[w.type];
     const int pic = ty.pic;
     const int p0 = ty.particle_start + w.first_cell * pic;
     const int np = w.ncells * pic;
     stage_scene(a.scenes + ty.scene, &sc);
-    for (int i = threadIdx.x; i < np; i += kStepThreads) {
+    for (int i = threadIdx.x; i < np; i += THREADS) {
         s_pos[i] = a.pos_in[p0 + i];
         s_vel[i] = a.vel_in[p0 + i];
         s_frc[i] = a.frc_in[p0 + i];
@@ -374,7 +409,7 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
     // Cell centroids (blood_cells.cu:44-61), one warp per cell, fixed-order
     // butterfly reduction (deterministic).
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = warp; c < w.ncells; c += kStepThreads / 32) {
+    for (int c = warp; c < w.ncells; c += THREADS / 32) {
         float3 acc = f3(0.f, 0.f, 0.f);
         for (int k = lane; k < pic; k += 32) acc = acc + xyz(s_pos[c * pic + k]);
 #pragma unroll
@@ -388,7 +423,7 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
     __syncthreads();
 
     unsigned e = 0;
-    for (int i = threadIdx.x; i < np; i += kStepThreads) {
+    for (int i = threadIdx.x; i < np; i += THREADS) {
         const int c = i / pic, li = i - c * pic, pid = p0 + i;
         const float4 px = s_pos[i];
         const float3 x = xyz(px), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
@@ -430,6 +465,36 @@ __global__ void __launch_bounds__(kStepThreads, 3) k_step(const StepArgs a) {
     if (e) atomicOr(a.err, e);
 }
 
+// The step kernel for one launch shape.  PERSIST: a grid of (SMs x resident
+// CTAs) pulls work items from a counter; the last CTA to finish resets the
+// counter for the next launch, so the launch replays from a CUDA graph.
+template <int MODE, int THREADS, int CHUNK, int MINB, bool PERSIST>
+__global__ void __launch_bounds__(THREADS, MINB) k_step(const StepArgs a) {
+    __shared__ float4 s_pos[CHUNK];
+    __shared__ float4 s_vel[CHUNK];
+    __shared__ float4 s_frc[CHUNK];
+    __shared__ float3 s_cent[kMaxCellsPerChunk];
+    __shared__ SceneDev sc;
+    if (!PERSIST) {
+        step_item<MODE, THREADS>(a, blockIdx.x, s_pos, s_vel, s_frc, s_cent, sc);
+        return;
+    }
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&a.work_counter[0], 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.work_count) break;
+        step_item<MODE, THREADS>(a, item, s_pos, s_vel, s_frc, s_cent, sc);
+        __syncthreads();   // shared buffers and s_item are reused
+    }
+    if (threadIdx.x == 0 && atomicAdd(&a.work_counter[1], 1) == (int)gridDim.x - 1) {
+        // every CTA has taken its last item: reset for the next launch
+        a.work_counter[0] = 0;
+        a.work_counter[1] = 0;
+    }
+}
+
 // handleVeinEndsBlockSync (src/simulation/vein_end.cu:57-108) after the
 // integration of a whole frame: one warp per blood cell ORs the vein-end
 // rule over its particles and respawns the cell; the respawned particles'
@@ -460,7 +525,7 @@ __global__ void __launch_bounds__(256) k_vein_end(const StepArgs a, int cells) {
 
 // propagateAll for the split-phase API: integrate (blood_cells.cu:155-179)
 // and the vein-end rule, in place on the buffers k_step<kForces> wrote.
-__global__ void __launch_bounds__(kStepThreads) k_propagate(const StepArgs a) {
+__global__ void __launch_bounds__(kPropagateThreads) k_propagate(const StepArgs a) {
     __shared__ int s_tp[kMaxCellsPerChunk];
     const WorkItem w = a.work[blockIdx.x];
     const TypeDev ty = a.types[w.type];
@@ -472,29 +537,28 @@ __global__ void __launch_bounds__(kStepThreads) k_propagate(const StepArgs a) {
     __syncthreads();
     const long long step = *a.steps;
     unsigned e = 0;
-    float3 nx[2], nv[2];
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int i = threadIdx.x + r * kStepThreads;
-        if (i >= np) continue;
+    auto heun = [&](int i, float3& nx, float3& nv) {
         const float3 x = xyz(a.pos_out[p0 + i]), v0 = xyz(a.vel_out[p0 + i]), F = xyz(a.frc_out[p0 + i]);
         const float3 v1 = v0 + a.p.dt * F;
-        nx[r] = x + (0.5f * a.p.dt) * (v1 + v0);
-        nv[r] = v1;
-        if (a.p.use_blood_flow && leaves_vein(sc, nx[r])) atomicOr(&s_tp[i / pic], 1);
+        nx = x + (0.5f * a.p.dt) * (v1 + v0);
+        nv = v1;
+    };
+    for (int i = threadIdx.x; i < np; i += kPropagateThreads) {
+        float3 nx, nv;
+        heun(i, nx, nv);
+        if (a.p.use_blood_flow && leaves_vein(sc, nx)) atomicOr(&s_tp[i / pic], 1);
     }
     __syncthreads();
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int i = threadIdx.x + r * kStepThreads;
-        if (i >= np) continue;
+    for (int i = threadIdx.x; i < np; i += kPropagateThreads) {
+        float3 nx, nv;
+        heun(i, nx, nv);
         const int c = i / pic;
         if (a.p.use_blood_flow && s_tp[c])
-            respawn(a, sc, ty.cell_start + w.first_cell + c, step, ty.model_start + (i - c * pic), nx[r], nv[r]);
-        if (!(isfinite(nx[r].x) && isfinite(nx[r].y) && isfinite(nx[r].z))) e |= BCS_ERRW_NONFINITE;
+            respawn(a, sc, ty.cell_start + w.first_cell + c, step, ty.model_start + (i - c * pic), nx, nv);
+        if (!(isfinite(nx.x) && isfinite(nx.y) && isfinite(nx.z))) e |= BCS_ERRW_NONFINITE;
         const float wv = a.pos_out[p0 + i].w;
-        a.pos_out[p0 + i] = make_float4(nx[r].x, nx[r].y, nx[r].z, wv);
-        a.vel_out[p0 + i] = make_float4(nv[r].x, nv[r].y, nv[r].z, 0.f);
+        a.pos_out[p0 + i] = make_float4(nx.x, nx.y, nx.z, wv);
+        a.vel_out[p0 + i] = make_float4(nv.x, nv.y, nv.z, 0.f);
     }
     if (e) atomicOr(a.err, e);
 }
@@ -532,14 +596,28 @@ __global__ void k_next_epoch(int* epoch) { *epoch += 1; }
 // calculateStartAndEndOfCellKernel (uniform_grid.cu:51-80), written into
 // the epoch-stamped table: the first slot of each occupied cell scans to its
 // last slot and stores (first, last, epoch) at once.
-__global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch) {
+__global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch,
+                              unsigned* occ, const int* __restrict__ ids, const float4* __restrict__ pos,
+                              float4* spos) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (spos) spos[i] = pos[ids[i]];
     const int k = keys[i];
     if (i > 0 && keys[i - 1] == k) return;
     int j = i;
     while (j + 1 < n && keys[j + 1] == k) ++j;
     table[k] = make_int4(i, j, *epoch, 0);
+    if (occ) atomicOr(&occ[k >> 5], 1u << (k & 31));
+}
+
+// Set or clear the occupancy bits of the cells a sorted key array occupies.
+__global__ void k_occ_update(const int* __restrict__ keys, int n, unsigned* occ, int set) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int k = keys[i];
+    if (i > 0 && keys[i - 1] == k) return;
+    if (set) atomicOr(&occ[k >> 5], 1u << (k & 31));
+    else atomicAnd(&occ[k >> 5], ~(1u << (k & 31)));
 }
 
 // Dense starts/ends (empty = 0, -1) from the epoch-stamped table, for getters.
@@ -678,6 +756,11 @@ __global__ void k_next_epoch_if(int* epoch, const float* disp2, float margin) {
 
 __global__ void k_bump_step(long long* steps) { *steps += 1; }
 
+__global__ void k_gather_rows(const float4* __restrict__ src, const int* __restrict__ idx, int n, float4* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = src[idx[i]];
+}
+
 // Headless stand-in for calculatePositionsKernel / calculateTriangleVerticesKernel
 // (src/graphics/glcontroller.cu:22-49).
 __global__ void k_export(const float4* __restrict__ pos, int n, const float4* __restrict__ vpos, int V, float* pvbo,
@@ -719,13 +802,50 @@ __global__ void k_unpack(const float4* __restrict__ in, int n, float* x, float* 
 // ------------------------------------------------------------ launches ---
 #define BCS_GRID1(n, b) dim3((unsigned)(((n) + (b) - 1) / (b))), dim3(b)
 
-void launch_step(const StepArgs& a, int blocks, int mode, cudaStream_t s) {
-    if (blocks <= 0) return;
-    if (mode == kFull) k_step<kFull><<<blocks, kStepThreads, 0, s>>>(a);
-    else k_step<kForces><<<blocks, kStepThreads, 0, s>>>(a);
+using StepKernel = void (*)(const StepArgs);
+
+template <int MODE, int S, bool P>
+constexpr StepKernel step_kernel() {
+    return k_step<MODE, kShapes[S].threads, kShapes[S].chunk, kShapes[S].min_blocks, P>;
+}
+
+template <int MODE, bool P>
+StepKernel step_kernel_of(int shape) {
+    switch (shape) {
+        case 0: return step_kernel<MODE, 0, P>();
+        case 1: return step_kernel<MODE, 1, P>();
+        case 2: return step_kernel<MODE, 2, P>();
+        case 3: return step_kernel<MODE, 3, P>();
+        case 4: return step_kernel<MODE, 4, P>();
+        default: return step_kernel<MODE, 5, P>();
+    }
+}
+
+StepKernel step_kernel_for(int mode, int shape, bool persistent) {
+    if (mode == kFull) return persistent ? step_kernel_of<kFull, true>(shape) : step_kernel_of<kFull, false>(shape);
+    return persistent ? step_kernel_of<kForces, true>(shape) : step_kernel_of<kForces, false>(shape);
+}
+
+// CTAs of a persistent step launch: resident CTAs per SM x SMs.
+int step_persistent_grid(int mode, int shape) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, step_kernel_for(mode, shape, true), kShapes[shape].threads, 0);
+    return std::max(1, per) * std::max(1, sms);
+}
+
+void launch_step(const StepArgs& a, int items, int mode, int shape, int persistent_grid, cudaStream_t s) {
+    if (items <= 0) return;
+    const bool persistent = persistent_grid > 0;
+    const int blocks = persistent ? std::min(items, persistent_grid) : items;
+    step_kernel_for(mode, shape, persistent)<<<blocks, kShapes[shape].threads, 0, s>>>(a);
+}
+void launch_gather_rows(const float4* src, const int* idx, int n, float4* out, cudaStream_t s) {
+    if (n > 0) k_gather_rows<<<BCS_GRID1(n, 256), 0, s>>>(src, idx, n, out);
 }
 void launch_propagate(const StepArgs& a, int blocks, cudaStream_t s) {
-    if (blocks > 0) k_propagate<<<blocks, kStepThreads, 0, s>>>(a);
+    if (blocks > 0) k_propagate<<<blocks, kPropagateThreads, 0, s>>>(a);
 }
 void launch_keys(const float4* pos, int n, int uniform, const SceneDev* scenes, int scene_count, int* keys, int* ids,
                  unsigned* err, cudaStream_t s) {
@@ -735,9 +855,13 @@ void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const Scene
                      int* keys, int* ids, cudaStream_t s) {
     if (T > 0) k_tri_keys<<<BCS_GRID1(T, 256), 0, s>>>(vpos, tri, T, scenes, scene_count, keys, ids);
 }
-void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, cudaStream_t s) {
+void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigned* occ, const int* ids,
+                        const float4* pos, float4* spos, cudaStream_t s) {
     k_next_epoch<<<1, 1, 0, s>>>(epoch);
-    if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table, epoch);
+    if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table, epoch, occ, ids, pos, spos);
+}
+void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s) {
+    if (n > 0) k_occ_update<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, occ, set ? 1 : 0);
 }
 void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
                          cudaStream_t s) {

@@ -62,7 +62,7 @@ def test_batch_arguments_rejected_before_device_work(lib, tmp_path):
 STRUCTS = {
     "bcs_vec3": bcs.Vec3, "bcs_cell_type": bcs.CellType, "bcs_vein": bcs.Vein,
     "bcs_flow_segment": bcs.FlowSegment, "bcs_params": bcs.Params, "bcs_scene_desc": bcs.SceneDesc,
-    "bcs_info": bcs.Info, "bcs_scene_info": bcs.SceneInfo,
+    "bcs_info": bcs.Info, "bcs_scene_info": bcs.SceneInfo, "bcs_tuning": bcs.Tuning,
 }
 
 
@@ -84,3 +84,19 @@ def test_ctypes_mirror_matches_c_layout(tmp_path):
         assert int(got[cname]) == C.sizeof(py), cname
         for fname, _ in py._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, f"{cname}.{fname}"
+
+
+def test_step_shapes_match_header():
+    text = open(os.path.join(REPO, "include", "bcs.h")).read()
+    assert f"#define BCS_STEP_SHAPES {len(bcs.STEP_SHAPES)}" in text
+    listed = re.findall(r"(\d) \((\d+), (\d+), (\d+)\)", text)
+    assert [tuple(int(v) for v in m[1:]) for m in listed] == list(bcs.STEP_SHAPES)
+    cuh = open(os.path.join(REPO, "simulation-server_gb300", "csrc", "bcs_internal.cuh")).read()
+    table = re.search(r"kShapes\[kStepShapes\] = \{(.*?)\};", cuh, re.S).group(1)
+    assert [tuple(int(v) for v in m) for m in re.findall(r"\{(\d+), (\d+), (\d+)\}", table)] == list(bcs.STEP_SHAPES)
+
+
+def test_tuning_arguments_rejected(lib):
+    assert lib.bcs_get_tuning(None, None) == 1
+    assert lib.bcs_set_tuning(None, None) == 1
+    assert lib.bcs_autotune(None, 1, None, None) == 1

@@ -222,7 +222,10 @@ def run_ours(args):
 
     sim.step(args.warmup)
     tuning, tune_ms = None, None
-    if not args.no_autotune:
+    if args.tuning:
+        sim.set_tuning(*[int(v) for v in args.tuning.split(",")])
+        tuning = sim.get_tuning().as_dict()
+    elif not args.no_autotune:
         t, tune_ms = sim.autotune(args.autotune_frames)
         tuning = t.as_dict()
     else:
@@ -292,7 +295,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(workload_config(scene, ws), tuning=tuning,
-                           tuning_source="bcs_autotune" if tune_ms is not None else "default",
+                           tuning_source="bcs_autotune" if tune_ms is not None else
+                           ("--tuning" if args.tuning else "default"),
                            step_shape=dict(zip(("threads", "particles_per_cta", "ctas_per_sm"),
                                                bcs.STEP_SHAPES[tuning["step_shape"]]))),
             "e2e": {"value": e2e_value, "unit": UNIT,
@@ -328,6 +332,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--autotune-frames", type=int, default=3)
+    ap.add_argument("--tuning", default="", help="comma-separated bcs_tuning fields instead of the autotuner")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

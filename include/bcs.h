@@ -248,7 +248,8 @@ bcs_status bcs_get_scene_info(bcs_sim* sim, int scene, bcs_scene_info* out);
  *                  (threads per CTA, particles per CTA, CTAs per SM) =
  *                  0 (256, 512, 3), 1 (128, 256, 6), 2 (384, 768, 2),
  *                  3 (256, 512, 4), 4 (256, 512, 2), 5 (128, 256, 8).
- *                  A CTA holds whole
+ *                  The default is 3 (or the first shape that holds the
+ *                  largest cell type).  A CTA holds whole
  *                  blood cells, so a shape needs particles_in_cell <= its
  *                  particles per CTA.
  *   persistent     0: one CTA per work item; 1: (SMs x resident CTAs) CTAs

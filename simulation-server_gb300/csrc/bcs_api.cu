@@ -167,6 +167,7 @@ namespace {
 // vertex has moved more than this since the last build; they carry it as
 // extra width, so they always contain the current triangles.
 constexpr float kWallMargin = 0.5f;
+constexpr int kDefaultShape = 3;
 
 #define BCS_CUDA(call)                                          \
     do {                                                        \
@@ -785,9 +786,14 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     build_triangle_grid(s, true);
     if ((st = check_last())) return st;
     BCS_CUDA(cudaStreamSynchronize(s->stream));
-    // ---- default launch: the first step shape that holds the largest cell
-    bcs_tuning t{0, 0, 0, 0, 0, 0};
-    while (kShapes[t.step_shape].chunk < s->max_pic) ++t.step_shape;
+    // ---- default launch: 256 threads / 512 particles / 4 CTAs per SM (the
+    // fastest shape at the 4.2M-particle bifurcation), else the first shape
+    // that holds the largest cell
+    bcs_tuning t{kDefaultShape, 0, 0, 0, 0, 0};
+    if (kShapes[t.step_shape].chunk < s->max_pic) {
+        t.step_shape = 0;
+        while (kShapes[t.step_shape].chunk < s->max_pic) ++t.step_shape;
+    }
     return apply_tuning(s, t);
 }
 

@@ -51,7 +51,7 @@ ALL = ([dict(step_shape=a, **{f: b for f in FLAGS}) for a in range(len(bcs.STEP_
 
 def test_default_tuning(lib):
     t = bcs.Simulation(scene()).get_tuning().as_dict()
-    assert t == dict(step_shape=0, persistent=0, spatial_order=0, full_sort=0, occupancy_filter=0,
+    assert t == dict(step_shape=3, persistent=0, spatial_order=0, full_sort=0, occupancy_filter=0,
                      sorted_positions=0)
 
 
@@ -120,7 +120,7 @@ def test_invalid_tuning_rejected(lib):
                 dict(sorted_positions=-1)):
         with pytest.raises(bcs.BcsError):
             sim.set_tuning(**bad)
-    assert sim.get_tuning().as_dict() == dict(step_shape=0, persistent=0, spatial_order=0, full_sort=0,
+    assert sim.get_tuning().as_dict() == dict(step_shape=3, persistent=0, spatial_order=0, full_sort=0,
                                               occupancy_filter=0, sorted_positions=0)
 
 

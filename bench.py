@@ -14,10 +14,13 @@ particle kernel, vein integration) replayed from a CUDA graph.
   e2e       the same metric through the C ABI with host buffers: each step is
             bcs_step(1) + bcs_get_particles of the positions into pinned host
             memory (the renderer's per-frame read, src/main.cu:183-184); the
-            initial state upload from pinned memory opens the timed region
+            upload of the state from pinned memory opens the timed region
   roofline  the fused particle kernel: algorithmic bytes (80 B/particle:
             x, v, F read + written as 3 x 12 B, + 8 B key/id) / its mean
             CUDA-event duration, against the measured HBM copy bandwidth
+Each of the three passes (timed run, per-phase events, e2e) starts a fresh
+simulation from the same state after the warm-up frames, with the tuning the
+autotuner picked in the first, so all three follow the same trajectory.
   cpu_baseline  the FP64 oracle (a C++ restatement of the reference step) on
             the host cores, on a bounded sample of the same workload
 
@@ -197,6 +200,18 @@ def run_reference(args):
     return 0
 
 
+def grid_diagnostics(sim):
+    """Occupancy of the particle grid and the error word after a run."""
+    keys, _, _, _ = sim.get_grid(0, dense=False)
+    if len(keys) == 0:
+        return {}
+    change = np.flatnonzero(np.diff(keys)) + 1
+    runs = np.diff(np.concatenate([[0], change, [len(keys)]]))
+    return {"occupied_cells": int(len(runs)), "max_particles_per_cell": int(runs.max()),
+            "mean_particles_per_occupied_cell": round(float(runs.mean()), 3),
+            "error_word": sim.error_word()}
+
+
 def run_ours(args):
     import torch
     import bcs_build
@@ -210,27 +225,33 @@ def run_ours(args):
     bcs_build.build()
     bcs.set_device(local)
     scene = build_scene(args.cells_per_type, args.seed + rank)
-    sim = bcs.Simulation(scene)
-    sim.set_particles(scene.positions, scene.velocities)
-    n = sim.n
 
-    def barrier():
+    def barrier(sim):
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
         sim.synchronize()
 
-    sim.step(args.warmup)
+    def fresh(tuning=None):
+        """A new simulation at the state after the warm-up frames: every pass
+        below starts from the same state and follows the same trajectory."""
+        sim = bcs.Simulation(scene)
+        sim.set_particles(scene.positions, scene.velocities)
+        if tuning is not None:
+            sim.set_tuning(**tuning)
+        sim.step(args.warmup)
+        return sim
+
+    # ---- pass 1: the timed run (graph replay, state resident in HBM)
+    sim = fresh()
+    n = sim.n
     tuning, tune_ms = None, None
     if args.tuning:
         sim.set_tuning(*[int(v) for v in args.tuning.split(",")])
-        tuning = sim.get_tuning().as_dict()
     elif not args.no_autotune:
-        t, tune_ms = sim.autotune(args.autotune_frames)
-        tuning = t.as_dict()
-    else:
-        tuning = sim.get_tuning().as_dict()
-    barrier()
+        _, tune_ms = sim.autotune(args.autotune_frames)
+    tuning = sim.get_tuning().as_dict()
+    barrier(sim)
     props = torch.cuda.get_device_properties(local)
     gpu_id = str(getattr(props, "uuid", "") or local)
     if gpu_id and not gpu_id.startswith("GPU-") and len(gpu_id) > 8:
@@ -239,7 +260,7 @@ def run_ours(args):
     time.sleep(0.3)
     ms = sim.time_steps(args.steps)
     clocks = sampler.stop()
-    barrier()
+    barrier(sim)
     t = torch.tensor([ms], device="cuda", dtype=torch.float64)
     if ws > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -247,10 +268,15 @@ def run_ours(args):
     value = ws * n * args.steps / (ms_max / 1e3)
     info = sim.refresh_info()
     launches = info.kernels_per_step * args.steps
+    diag = grid_diagnostics(sim)
+    sim.close()
 
-    # per-phase CUDA-event profile of eager frames (same stream, same kernels)
-    prof_steps = args.profile_steps
+    # ---- pass 2: the same frames eagerly, CUDA events between the phases;
+    # the particle phase is the fused step kernel plus the vein-end kernel
+    prof_steps = args.profile_steps if args.profile_steps > 0 else args.steps
+    sim = fresh(tuning)
     phases = sim.profile_steps(prof_steps)
+    sim.close()
     k_ms = phases["particles"] / prof_steps
     peak, peak_kind = measured_peak()
     achieved = ALGO_BYTES_STEP_KERNEL * n / (k_ms / 1e3) / 1e9
@@ -261,22 +287,28 @@ def run_ours(args):
             tr = json.load(f)
         traffic = tr["dram_bytes_per_launch"] * n / tr["particles"]
 
-    # end to end through the C ABI, pinned host buffers
-    e2e_steps = max(1, min(args.e2e_steps, args.steps))
-    hp = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(6)]
+    # ---- pass 3: end to end through the C ABI with pinned host buffers:
+    # the state after the warm-up is uploaded, then every frame is
+    # bcs_step(1) + a read of the positions into host memory
+    e2e_steps = args.steps if args.e2e_steps <= 0 else max(1, min(args.e2e_steps, args.steps))
+    sim = fresh(tuning)
+    p0, v0, f0 = sim.get_particles()
+    hp = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(9)]
     for k in range(3):
-        hp[k].copy_(torch.from_numpy(np.ascontiguousarray(scene.positions[:, k])))
-        hp[3 + k].copy_(torch.from_numpy(np.ascontiguousarray(scene.velocities[:, k])))
+        hp[k].copy_(torch.from_numpy(np.ascontiguousarray(p0[:, k])))
+        hp[3 + k].copy_(torch.from_numpy(np.ascontiguousarray(v0[:, k])))
+        hp[6 + k].copy_(torch.from_numpy(np.ascontiguousarray(f0[:, k])))
     lib = bcs.load_library()
-    P, Vv = bcs.Vec3(*(x.data_ptr() for x in hp[:3])), bcs.Vec3(*(x.data_ptr() for x in hp[3:]))
+    P, Vv, Ff = (bcs.Vec3(*(x.data_ptr() for x in hp[3 * j:3 * j + 3])) for j in range(3))
     out = bcs.Vec3(*(x.data_ptr() for x in hp[:3]))
-    barrier()
+    barrier(sim)
     t0 = time.perf_counter()
-    assert lib.bcs_set_particles(sim.h, P, Vv, bcs.Vec3(), bcs.MEM_HOST) == 0
+    assert lib.bcs_set_particles(sim.h, P, Vv, Ff, bcs.MEM_HOST) == 0
     for _ in range(e2e_steps):
         assert lib.bcs_step(sim.h, 1) == 0
         assert lib.bcs_get_particles(sim.h, out, bcs.Vec3(), bcs.Vec3(), bcs.MEM_HOST) == 0
     e2e_s = time.perf_counter() - t0
+    sim.close()
     e2e_t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
     if ws > 1:
         torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
@@ -290,6 +322,7 @@ def run_ours(args):
                          f"steps in {cinfo['seconds']} s, FP64 oracle, {threads} OpenMP threads"}
 
     if rank == 0:
+        shape = bcs.STEP_SHAPES[tuning["step_shape"]]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -297,22 +330,23 @@ def run_ours(args):
             "config": dict(workload_config(scene, ws), tuning=tuning,
                            tuning_source="bcs_autotune" if tune_ms is not None else
                            ("--tuning" if args.tuning else "default"),
-                           step_shape=dict(zip(("threads", "particles_per_cta", "ctas_per_sm"),
-                                               bcs.STEP_SHAPES[tuning["step_shape"]]))),
-            "e2e": {"value": e2e_value, "unit": UNIT,
-                    "h2d_bytes_per_step": int(24 * n / e2e_steps), "d2h_bytes_per_step": int(12 * n)},
+                           step_shape=dict(zip(("threads", "particles_per_cta", "ctas_per_sm"), shape))),
+            "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
+                    "h2d_bytes_per_step": int(36 * n / e2e_steps), "d2h_bytes_per_step": int(12 * n)},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": "bcs::k_step<0, {}, {}, {}, {}>".format(*bcs.STEP_SHAPES[tuning["step_shape"]],
-                                                                           "true" if tuning["persistent"] else "false"), "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": ALGO_BYTES_STEP_KERNEL * n,
-                         "kernel_ms": k_ms},
+            "roofline": {"bound": "hbm",
+                         "kernel": "bcs::k_step<0, {}, {}, {}, {}>".format(
+                             *shape, "true" if tuning["persistent"] else "false"),
+                         "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": ALGO_BYTES_STEP_KERNEL * n, "kernel_ms": k_ms,
+                         "kernel_ms_over": f"{prof_steps} eager frames of the same trajectory"},
             "phase_ms": {k: v / prof_steps for k, v in phases.items()},
+            "diagnostics_after_timed_run": diag,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    sim.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -326,8 +360,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells-per-type", type=int, default=CELLS_PER_TYPE)
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--profile-steps", type=int, default=20)
-    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--profile-steps", type=int, default=0, help="0 = as many as --steps")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0 = as many as --steps")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")

@@ -317,6 +317,17 @@ bcs_status bcs_propagate_all(bcs_sim* sim);
  * Same results as the three calls above in sequence. */
 bcs_status bcs_step(bcs_sim* sim, int nsteps);
 
+/* Multi-rate macro steps (no reference counterpart): each of the `n` macro
+ * steps advances `substeps` time steps of dt.  Sub-step 1 is the full frame
+ * of bcs_step; the external part of its force (particle collisions and the
+ * vein's force adjustment) is held for sub-steps 2..substeps, which
+ * re-evaluate centroids, cell springs and environment, integrate, and apply
+ * the vein-end rule (a respawned cell drops its held force).  Particle
+ * impacts reach the vein mesh in sub-step 1; the mesh takes every sub-step.
+ * With substeps = 1 this is bcs_step.  1 <= substeps <= BCS_MAX_SUBSTEPS. */
+#define BCS_MAX_SUBSTEPS 64
+bcs_status bcs_macro_step(bcs_sim* sim, int substeps, int n);
+
 /* Grid arrays for parity checks, the UniformGrid members gridCellIds,
  * particleIds, gridCellStarts, gridCellEnds (src/grids/uniform_grid.cuh:32-35)
  * after the last bcs_calculate_grids / bcs_step.  which = 0: particle grid,

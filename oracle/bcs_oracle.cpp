@@ -622,6 +622,51 @@ void full_step(Sim& s) {
     ++s.steps;
 }
 
+// Multi-rate macro step of K sub-steps (no reference counterpart; the
+// surrogate's plain form).  Sub-step 1 is full_step: grid, vein springs, cell
+// springs, collisions, the vein ray, integration and the vein-end rule.  The
+// external part of its force (collisions + the vein's force adjustment) is
+// held for sub-steps 2..K, which re-evaluate only cell springs and
+// environment (and the vein mesh's springs); particle impacts on the vein
+// enter in sub-step 1 only.  The vein-end rule runs after every sub-step as
+// in full_step; a respawned cell's held force is dropped.  With K = 1 this
+// is full_step.
+void macro_step(Sim& s, int K) {
+    calculate_grids(s);
+    vein_springs(s);
+    cell_springs(s);
+    const std::vector<V3> favg = s.f;
+    particle_collisions(s);
+    vein_collisions(s);
+    std::vector<V3> fext(s.N);
+    for (int i = 0; i < s.N; ++i) fext[i] = s.f[i] - favg[i];
+    auto end_of_substep = [&]() {
+        const std::vector<V3> before = s.x;
+        vein_end(s);
+        ++s.steps;
+        for (const auto& ty : s.types)
+            for (int c = 0; c < ty.count; ++c) {
+                const int first = ty.particle_start + c * ty.pic;
+                bool moved = false;
+                for (int i = 0; i < ty.pic && !moved; ++i) {
+                    const V3 a = before[first + i], b = s.x[first + i];
+                    moved = a.x != b.x || a.y != b.y || a.z != b.z;
+                }
+                if (moved)
+                    for (int i = 0; i < ty.pic; ++i) fext[first + i] = V3{0, 0, 0};
+            }
+    };
+    integrate(s);
+    end_of_substep();
+    for (int k = 2; k <= K; ++k) {
+        vein_springs(s);
+        cell_springs(s);
+        for (int i = 0; i < s.N; ++i) s.f[i] = s.f[i] + fext[i];
+        integrate(s);
+        end_of_substep();
+    }
+}
+
 bool finite3(const float* a) { return std::isfinite(a[0]) && std::isfinite(a[1]) && std::isfinite(a[2]); }
 
 }  // namespace
@@ -829,6 +874,11 @@ void bcso_step(bcso_sim* h, int n) {
 }
 
 // The three phases separately, for phase-level comparisons.
+void bcso_macro_step(bcso_sim* h, int substeps, int n) {
+    Sim& s = *reinterpret_cast<Sim*>(h);
+    for (int i = 0; i < n; ++i) macro_step(s, substeps < 1 ? 1 : substeps);
+}
+
 void bcso_calculate_grids(bcso_sim* h) { calculate_grids(*reinterpret_cast<Sim*>(h)); }
 void bcso_calculate_next_frame(bcso_sim* h) {
     Sim* s = reinterpret_cast<Sim*>(h);

@@ -45,6 +45,7 @@ def load() -> C.CDLL:
         lib.bcso_set_vein.argtypes = [P, P, P]
         lib.bcso_get_vein.argtypes = [P, P, P, P]
         lib.bcso_step.argtypes = [P, C.c_int]
+        lib.bcso_macro_step.argtypes = [P, C.c_int, C.c_int]
         lib.bcso_calculate_grids.argtypes = [P]
         lib.bcso_calculate_next_frame.argtypes = [P]
         lib.bcso_propagate_all.argtypes = [P]
@@ -140,6 +141,11 @@ class OracleSim:
 
     def step(self, n: int = 1):
         self.lib.bcso_step(self.h, int(n))
+
+    def macro_step(self, substeps: int, n: int = 1):
+        """Multi-rate macro steps: collisions and the vein ray once per
+        `substeps` sub-steps, cell springs every sub-step."""
+        self.lib.bcso_macro_step(self.h, int(substeps), int(n))
 
     def calculate_grids(self):
         self.lib.bcso_calculate_grids(self.h)

@@ -29,10 +29,11 @@ EXPORTED = [
     "bcs_calculate_grids", "bcs_calculate_next_frame", "bcs_propagate_all", "bcs_step",
     "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
     "bcs_profile_steps", "bcs_grid_sort_static", "bcs_create_batch", "bcs_get_scene_info",
-    "bcs_get_tuning", "bcs_set_tuning", "bcs_autotune",
+    "bcs_get_tuning", "bcs_set_tuning", "bcs_autotune", "bcs_macro_step",
 ]
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
 GRID_SORT_STATIC_MAX = 262144
+MAX_SUBSTEPS = 64
 PHASES = ("grid", "vein_forces", "particles", "vein_update")
 
 
@@ -150,6 +151,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_get_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "bcs_set_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "bcs_autotune": ([P, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)], C.c_int),
+        "bcs_macro_step": ([P, C.c_int, C.c_int], C.c_int),
         "bcs_destroy": ([P], C.c_int),
         "bcs_get_info": ([P, C.POINTER(Info)], C.c_int),
         "bcs_set_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
@@ -356,6 +358,10 @@ class Simulation:
 
     def step(self, nsteps: int = 1) -> None:
         _check(self.lib.bcs_step(self.h, int(nsteps)), "bcs_step")
+
+    def macro_step(self, substeps: int, n: int = 1) -> None:
+        """n multi-rate macro steps of `substeps` time steps each."""
+        _check(self.lib.bcs_macro_step(self.h, int(substeps), int(n)), "bcs_macro_step")
 
     def time_steps(self, nsteps: int) -> float:
         ms = C.c_float()

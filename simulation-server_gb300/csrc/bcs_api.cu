@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <new>
 #include <vector>
 
@@ -41,7 +42,8 @@ void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, c
                          int V, float k, float d, unsigned* err, cudaStream_t s);
 void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt, cudaStream_t s);
 void launch_tri_cache(const int* ids, const uint32_t* tri, const float4* vpos, int T, float4* cache, cudaStream_t s);
-void launch_bump_step(long long* steps, cudaStream_t s);
+void launch_bump_step(long long* steps, int by, cudaStream_t s);
+void launch_substeps(const StepArgs& a, int items, int K, cudaStream_t s);
 void launch_export(const float4* pos, int n, const float4* vpos, int V, float* pvbo, float* poff, float* vvbo,
                    cudaStream_t s);
 void launch_pack(const float* x, const float* y, const float* z, int n, float4* out, const float* wsrc,
@@ -154,7 +156,8 @@ struct bcs_sim {
     long long host_steps = 0;
     unsigned* err = nullptr;
     StepArgs args{};
-    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};   // by (cur, sorted slot)
+    std::map<long long, cudaGraphExec_t> graphs;   // by (sub-steps, cur, sorted slot)
+    float4* fext = nullptr;      // macro steps: held external force per particle
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t pev[BCS_PHASE_COUNT + 1] = {};
     float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
@@ -329,7 +332,7 @@ void enqueue_vein_propagate(bcs_sim* s) {
         launch_vein_integrate(s->vpos, s->vvel, s->vfrc, s->V, s->p.dt, s->stream);
         build_triangle_grid(s, false);
     }
-    launch_bump_step(s->steps, s->stream);
+    launch_bump_step(s->steps, 1, s->stream);
 }
 
 // One fused frame on the stream (no host synchronisation).  With `ev`, an
@@ -352,6 +355,38 @@ void enqueue_frame(bcs_sim* s, cudaEvent_t* ev = nullptr) {
     ++s->host_steps;
 }
 
+// One multi-rate macro step of K sub-steps (K >= 2): sub-step 1 is the
+// fused frame, which also records each particle's external force (collisions
+// and the vein's force adjustment); sub-steps 2..K re-integrate cell springs
+// and environment with that force held (k_substeps), the vein mesh takes K
+// sub-steps with the particle impacts in the first, and the step counter
+// advances by K.
+void enqueue_macro(bcs_sim* s, int K) {
+    enqueue_grids(s);
+    enqueue_vein_forces(s);
+    const int in = s->cur, out = s->cur ^ 1;
+    refresh_args(s, in, out, false);
+    s->args.fext = s->fext;
+    launch_step(s->args, (int)s->work_host.size(), 0, s->tune.step_shape, s->persistent_grid[0], s->stream);
+    if (s->p.use_blood_flow) launch_vein_end(s->args, s->C, s->stream);
+    refresh_args(s, in, out, true);
+    launch_substeps(s->args, (int)s->work_host.size(), K, s->stream);
+    s->args.fext = nullptr;
+    if (s->p.vein_dynamic && s->V > 0) {
+        for (int k = 1; k <= K; ++k) {
+            if (k > 1)
+                launch_vein_springs(s->vpos, s->vvel, s->vfrc, s->nb_ids, s->nb_len, s->V, s->p.vein_k_sniff,
+                                    s->p.vein_d_fact, s->err, s->stream);
+            launch_vein_integrate(s->vpos, s->vvel, s->vfrc, s->V, s->p.dt, s->stream);
+        }
+        build_triangle_grid(s, false);
+    }
+    launch_bump_step(s->steps, K, s->stream);
+    s->cur = out;
+    s->keys_valid = true;
+    s->host_steps += K;
+}
+
 bcs_status check_last() {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? BCS_ERR_OUT_OF_MEMORY : BCS_ERR_CUDA;
@@ -359,8 +394,9 @@ bcs_status check_last() {
 }
 
 void drop_graphs(bcs_sim* s) {
-    for (auto& g : s->graph)
-        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (auto& kv : s->graphs)
+        if (kv.second) cudaGraphExecDestroy(kv.second);
+    s->graphs.clear();
 }
 
 bcs_status validate(const bcs_scene_desc* d) {
@@ -718,6 +754,8 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
         if ((st = dalloc(s, &s->pos[b], s->N)) || (st = dalloc(s, &s->vel[b], s->N)) ||
             (st = dalloc(s, &s->frc[b], s->N)))
             return st;
+    if ((st = dalloc(s, &s->fext, s->N))) return st;
+    BCS_CUDA(cudaMemset(s->fext, 0, sizeof(float4) * s->N));
     for (int b = 0; b < 2; ++b) {
         BCS_CUDA(cudaMemset(s->pos[b], 0, sizeof(float4) * s->N));
         BCS_CUDA(cudaMemset(s->vel[b], 0, sizeof(float4) * s->N));
@@ -1086,20 +1124,26 @@ bcs_status bcs_propagate_all(bcs_sim* s) {
     return check_last();
 }
 
-static bcs_status run_steps(bcs_sim* s, int n) {
+// n fused frames (substeps = 1) or multi-rate macro steps, each replayed
+// from a CUDA graph captured per (sub-steps, buffer parity, sorted slot).
+static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
+    auto enqueue = [&]() {
+        if (substeps > 1) enqueue_macro(s, substeps);
+        else enqueue_frame(s);
+    };
     for (int i = 0; i < n; ++i) {
         if (!s->keys_valid || s->p.refresh_triangle_centers) {
-            enqueue_frame(s);
+            enqueue();
             continue;
         }
-        cudaGraphExec_t& g = s->graph[s->cur * 2 + s->pg.slot];
+        cudaGraphExec_t& g = s->graphs[(long long)substeps * 4 + s->cur * 2 + s->pg.slot];
         if (!g) {
             const int cur0 = s->cur;
             const int slot0 = s->pg.slot;
             const long long hs = s->host_steps;
             cudaGraph_t graph = nullptr;
             BCS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_frame(s);
+            enqueue();
             cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
             s->cur = cur0;
             s->pg.slot = slot0;
@@ -1115,7 +1159,7 @@ static bcs_status run_steps(bcs_sim* s, int n) {
                     cudaGraphNodeType t;
                     if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
                 }
-                s->kernels_per_step = kernels;
+                if (substeps == 1) s->kernels_per_step = kernels;
             }
             ce = cudaGraphInstantiate(&g, graph, 0);
             cudaGraphDestroy(graph);
@@ -1129,9 +1173,16 @@ static bcs_status run_steps(bcs_sim* s, int n) {
         s->pg.g.ids = s->pg.s_v[s->pg.slot];
         s->keys_valid = true;
         s->grid_ready = true;
-        ++s->host_steps;
+        s->host_steps += substeps;
     }
     return BCS_OK;
+}
+
+bcs_status bcs_macro_step(bcs_sim* s, int substeps, int n) {
+    if (!s || n < 0 || substeps < 1 || substeps > BCS_MAX_SUBSTEPS || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_status st = run_steps(s, n, substeps);
+    if (st != BCS_OK) return st;
+    return check_last();
 }
 
 bcs_status bcs_step(bcs_sim* s, int nsteps) {

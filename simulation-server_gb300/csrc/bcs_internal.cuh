@@ -125,6 +125,7 @@ struct StepArgs {
     float4* frc_out;
     int* keys_out;        // next-step grid keys (canonical order) or null
     int* ids_out;
+    float4* fext;         // macro steps: external force of sub-step 1 (held), or null
     int n;
     // layout
     const WorkItem* work;

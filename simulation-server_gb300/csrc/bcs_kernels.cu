@@ -439,6 +439,7 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
         const float ratio = len3(x - s_cent[c]) / __ldg(&a.r0[ty.model_start + li]);
         F = F + environment(a, sc, x, v, ratio);
         F = (fprev + F) / 2.0f;
+        const float3 favg = F;
         // Particle-particle collisions.
         F = F + particle_collisions(a, sc, pid, x, v, px.w, e);
         // Particle-vein collision.
@@ -460,6 +461,11 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
         if (MODE == kFull && a.keys_out) {
             a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, nx, e) : 0;
             a.ids_out[pid] = pid;
+        }
+        if (MODE == kFull && a.fext) {
+            // macro step: the external part of this force, held by sub-steps 2..K
+            const float3 fx = F - favg;
+            a.fext[pid] = make_float4(fx.x, fx.y, fx.z, 0.f);
         }
     }
     if (e) atomicOr(a.err, e);
@@ -519,6 +525,7 @@ __global__ void __launch_bounds__(256) k_vein_end(const StepArgs a, int cells) {
         a.pos_out[p0 + k] = make_float4(x.x, x.y, x.z, w);
         a.vel_out[p0 + k] = make_float4(v.x, v.y, v.z, 0.f);
         if (a.keys_out) a.keys_out[p0 + k] = a.pg.uniform ? grid_key(sc.pg, x, e) : 0;
+        if (a.fext) a.fext[p0 + k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (e) atomicOr(a.err, e);
 }
@@ -596,6 +603,128 @@ __global__ void k_next_epoch(int* epoch) { *epoch += 1; }
 // calculateStartAndEndOfCellKernel (uniform_grid.cu:51-80), written into
 // the epoch-stamped table: the first slot of each occupied cell scans to its
 // last slot and stores (first, last, epoch) at once.
+// Sub-steps 2..K of a macro step, in place on the state sub-step 1 wrote:
+// the cells of one work item stay in shared memory, and every sub-step
+// re-evaluates centroids, cell springs and environment with the external
+// force of sub-step 1 held, integrates (Heun) and applies the vein-end rule
+// (a respawned cell drops its held force).  Ends with the grid keys of the
+// final positions.
+constexpr int kSubstepThreads = 256;
+constexpr int kSubstepPer = kMaxChunk / kSubstepThreads;
+
+__global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, int K) {
+    __shared__ float4 s_pos[kMaxChunk];
+    __shared__ float4 s_vel[kMaxChunk];
+    __shared__ float4 s_frc[kMaxChunk];
+    __shared__ float3 s_cent[kMaxCellsPerChunk];
+    __shared__ int s_leave[kMaxCellsPerChunk];
+    __shared__ SceneDev sc;
+    const WorkItem w = a.work[blockIdx.x];
+    const TypeDev ty = a.types[w.type];
+    const int pic = ty.pic;
+    const int p0 = ty.particle_start + w.first_cell * pic;
+    const int np = w.ncells * pic;
+    stage_scene(a.scenes + ty.scene, &sc);
+    float3 fe[kSubstepPer];
+#pragma unroll
+    for (int r = 0; r < kSubstepPer; ++r) {
+        const int i = threadIdx.x + r * kSubstepThreads;
+        if (i < np) {
+            s_pos[i] = a.pos_out[p0 + i];
+            s_vel[i] = a.vel_out[p0 + i];
+            s_frc[i] = a.frc_out[p0 + i];
+            fe[r] = xyz(a.fext[p0 + i]);
+        }
+    }
+    __syncthreads();
+    const long long step0 = *a.steps;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned e = 0;
+    for (int k = 2; k <= K; ++k) {
+        for (int c = warp; c < w.ncells; c += kSubstepThreads / 32) {
+            float3 acc = f3(0.f, 0.f, 0.f);
+            for (int q = lane; q < pic; q += 32) acc = acc + xyz(s_pos[c * pic + q]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+                acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+                acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+            }
+            if (lane == 0) {
+                s_cent[c] = acc / (float)pic;
+                s_leave[c] = 0;
+            }
+        }
+        __syncthreads();
+        float3 nx[kSubstepPer], nv[kSubstepPer], nF[kSubstepPer];
+#pragma unroll
+        for (int r = 0; r < kSubstepPer; ++r) {
+            const int i = threadIdx.x + r * kSubstepThreads;
+            if (i >= np) continue;
+            const int c = i / pic, li = i - c * pic, cb = c * pic;
+            const float3 x = xyz(s_pos[i]), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
+            float3 F = f3(0.f, 0.f, 0.f);
+            const int e0 = __ldg(&a.adj_off[ty.adj_start + li]), e1 = __ldg(&a.adj_off[ty.adj_start + li + 1]);
+            for (int q = e0; q < e1; ++q) {
+                const int j = cb + __ldg(&a.adj_nbr[q]);
+                F = F + cell_spring(a.p, x - xyz(s_pos[j]), v - xyz(s_vel[j]), fprev, xyz(s_frc[j]),
+                                    __ldg(&a.adj_len[q]), e);
+            }
+            const float ratio = len3(x - s_cent[c]) / __ldg(&a.r0[ty.model_start + li]);
+            F = F + environment(a, sc, x, v, ratio);
+            F = (fprev + F) / 2.0f + fe[r];
+            const float3 v1 = v + a.p.dt * F;
+            nx[r] = x + (0.5f * a.p.dt) * (v1 + v);
+            nv[r] = v1;
+            nF[r] = F;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kSubstepPer; ++r) {
+            const int i = threadIdx.x + r * kSubstepThreads;
+            if (i >= np) continue;
+            s_pos[i] = make_float4(nx[r].x, nx[r].y, nx[r].z, s_pos[i].w);
+            s_vel[i] = make_float4(nv[r].x, nv[r].y, nv[r].z, 0.f);
+            s_frc[i] = make_float4(nF[r].x, nF[r].y, nF[r].z, 0.f);
+            if (a.p.use_blood_flow && leaves_vein(sc, nx[r])) atomicOr(&s_leave[i / pic], 1);
+        }
+        __syncthreads();
+        if (a.p.use_blood_flow) {
+#pragma unroll
+            for (int r = 0; r < kSubstepPer; ++r) {
+                const int i = threadIdx.x + r * kSubstepThreads;
+                if (i >= np) continue;
+                const int c = i / pic;
+                if (!s_leave[c]) continue;
+                float3 x, v;
+                respawn(a, sc, ty.cell_start + w.first_cell + c, step0 + (k - 1), ty.model_start + (i - c * pic),
+                        x, v);
+                s_pos[i] = make_float4(x.x, x.y, x.z, s_pos[i].w);
+                s_vel[i] = make_float4(v.x, v.y, v.z, 0.f);
+                fe[r] = f3(0.f, 0.f, 0.f);
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kSubstepPer; ++r) {
+        const int i = threadIdx.x + r * kSubstepThreads;
+        if (i >= np) continue;
+        const int pid = p0 + i;
+        const float4 x = s_pos[i], v = s_vel[i];
+        if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z)))
+            e |= BCS_ERRW_NONFINITE;
+        a.pos_out[pid] = x;
+        a.vel_out[pid] = v;
+        a.frc_out[pid] = s_frc[i];
+        if (a.keys_out) {
+            a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, xyz(x), e) : 0;
+            a.ids_out[pid] = pid;
+        }
+    }
+    if (e) atomicOr(a.err, e);
+}
+
 __global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch,
                               unsigned* occ, const int* __restrict__ ids, const float4* __restrict__ pos,
                               float4* spos) {
@@ -754,7 +883,7 @@ __global__ void k_next_epoch_if(int* epoch, const float* disp2, float margin) {
     if (!disp2 || *disp2 > margin * margin) *epoch += 1;
 }
 
-__global__ void k_bump_step(long long* steps) { *steps += 1; }
+__global__ void k_bump_step(long long* steps, int by) { *steps += by; }
 
 __global__ void k_gather_rows(const float4* __restrict__ src, const int* __restrict__ idx, int n, float4* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -896,7 +1025,10 @@ void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, floa
 void launch_tri_cache(const int* ids, const uint32_t* tri, const float4* vpos, int T, float4* cache, cudaStream_t s) {
     if (T > 0) k_tri_cache<<<BCS_GRID1(T, 256), 0, s>>>(ids, tri, vpos, T, cache);
 }
-void launch_bump_step(long long* steps, cudaStream_t s) { k_bump_step<<<1, 1, 0, s>>>(steps); }
+void launch_bump_step(long long* steps, int by, cudaStream_t s) { k_bump_step<<<1, 1, 0, s>>>(steps, by); }
+void launch_substeps(const StepArgs& a, int items, int K, cudaStream_t s) {
+    if (items > 0 && K > 1) k_substeps<<<items, kSubstepThreads, 0, s>>>(a, K);
+}
 void launch_export(const float4* pos, int n, const float4* vpos, int V, float* pvbo, float* poff, float* vvbo,
                    cudaStream_t s) {
     int m = n > V ? n : V;

@@ -100,3 +100,9 @@ def test_tuning_arguments_rejected(lib):
     assert lib.bcs_get_tuning(None, None) == 1
     assert lib.bcs_set_tuning(None, None) == 1
     assert lib.bcs_autotune(None, 1, None, None) == 1
+
+
+def test_constants_match_header():
+    text = open(os.path.join(REPO, "include", "bcs.h")).read()
+    assert f"#define BCS_MAX_SUBSTEPS {bcs.MAX_SUBSTEPS}" in text
+    assert f"#define BCS_GRID_SORT_STATIC_MAX {bcs.GRID_SORT_STATIC_MAX}" in text

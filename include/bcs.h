@@ -328,6 +328,87 @@ bcs_status bcs_step(bcs_sim* sim, int nsteps);
 #define BCS_MAX_SUBSTEPS 64
 bcs_status bcs_macro_step(bcs_sim* sim, int substeps, int n);
 
+/* ---- Learned sub-steps (no reference counterpart) ------------------------
+ * A message-passing network over one cell model's spring graph (3 layers,
+ * hidden width 128, bfloat16 weights, FP32 accumulation) predicts a cell's
+ * state after sub-steps 2..K of a macro step from the state after sub-step
+ * 1: positions and velocities relative to the cell's centroid and mean
+ * velocity, the current, held external and environment forces, and a
+ * wall-proximity flag.  It is trained on the GPU, by the library's own
+ * forward and backward kernels (Adam), on macro steps the plain sub-steps
+ * computed.  While it is enabled, each macro step of K sub-steps predicts
+ * every cell of the model and checks the prediction's residual: the
+ * trapezoid rule over the span, |x_K - x_1 - (K-1) dt / 2 (v_1 + v_K)|,
+ * per particle.  A cell whose residual exceeds the tolerance, or whose
+ * prediction is not finite, falls back to the plain sub-steps.  The
+ * vein-end rule runs once, on the predicted state. */
+typedef struct bcs_surrogate bcs_surrogate;
+
+typedef struct bcs_surrogate_desc {
+    int cell_type;       /* type index (all types with the same cell model join) */
+    int substeps;        /* K of the macro steps it serves, 2..BCS_MAX_SUBSTEPS */
+    int layers;          /* message-passing layers, 1..4 (3) */
+    int max_samples;     /* capacity of the training set, in cell-steps */
+    uint64_t seed;       /* weights and training draws */
+    float tolerance;     /* residual threshold in length units; 0 = 1e-3 x the
+                            model's smallest collision radius */
+} bcs_surrogate_desc;
+
+typedef struct bcs_surrogate_stats {
+    int64_t cells;            /* cells of the model in the simulation */
+    int64_t samples;          /* cell-steps collected */
+    int64_t valid_samples;    /* of those, without a respawn */
+    int64_t predicted_cells;  /* cell macro steps taken from the network */
+    int64_t fallback_cells;   /* cell macro steps that fell back */
+    int64_t iterations;       /* training iterations so far */
+    int64_t parameters;
+    float last_loss;          /* mean squared error of the last batch (normalised) */
+    float tolerance;
+    double flops_per_cell;    /* one forward pass over one cell */
+    size_t device_bytes;
+} bcs_surrogate_stats;
+
+bcs_status bcs_surrogate_create(bcs_sim* sim, const bcs_surrogate_desc* desc, bcs_surrogate** out);
+bcs_status bcs_surrogate_destroy(bcs_surrogate* sur);
+/* Run `macro_steps` plain macro steps of the surrogate's K and record every
+ * cell of the model as a training sample (stops at the capacity). */
+bcs_status bcs_surrogate_collect(bcs_surrogate* sur, int macro_steps);
+/* `iterations` Adam steps on batches of `batch_cells` cells drawn from the
+ * training set; *loss (optional) = the last batch's loss. */
+bcs_status bcs_surrogate_train(bcs_surrogate* sur, int iterations, int batch_cells, float learning_rate,
+                               float* loss);
+/* Use the network in this simulation's macro steps of K sub-steps (on != 0). */
+bcs_status bcs_surrogate_enable(bcs_surrogate* sur, int on);
+bcs_status bcs_surrogate_get_stats(bcs_surrogate* sur, bcs_surrogate_stats* out);
+bcs_status bcs_surrogate_reset_stats(bcs_surrogate* sur);
+int64_t bcs_surrogate_param_count(bcs_surrogate* sur);
+/* FP32 parameters, in the order W_in, b_in, then per layer W_a, W_b, W_e,
+ * b_e, W_u, W_v, b_u, then W_out, b_out; matrices row-major [in][out]. */
+bcs_status bcs_surrogate_get_params(bcs_surrogate* sur, float* params, int64_t count);
+bcs_status bcs_surrogate_set_params(bcs_surrogate* sur, const float* params, int64_t count);
+/* Loss and parameter gradients of the network on given normalised host
+ * inputs: features [cells * pic][16], edge features [cells * edges][8] in
+ * the order of the cell's spring lists, targets [cells * pic][9]. */
+bcs_status bcs_surrogate_loss_grad(bcs_surrogate* sur, int cells, const float* features,
+                                   const float* edge_features, const float* targets, float* loss,
+                                   float* grads);
+/* The network's outputs [cells * pic][9] on given normalised host inputs. */
+bcs_status bcs_surrogate_forward(bcs_surrogate* sur, int cells, const float* features,
+                                 const float* edge_features, float* outputs);
+/* Mean position error (length units, per particle) after the network's
+ * span on the stored samples [first, first + count): of its prediction
+ * (*net_error) and of the constant-force extrapolation x_1 + T v_1 +
+ * T^2/2 F_1 that it corrects (*base_error), against the plain sub-steps. */
+bcs_status bcs_surrogate_evaluate(bcs_surrogate* sur, int first, int count, double* net_error,
+                                  double* base_error);
+/* The normalisation derived from the training set: 53 floats (feature means
+ * [16], feature 1/std [16], target means [9], target std [9], edge scales
+ * of relative position, stretch and relative velocity). */
+bcs_status bcs_surrogate_get_scales(bcs_surrogate* sur, float* out53);
+/* Install a normalisation (as bcs_surrogate_get_scales writes it), e.g.
+ * with parameters trained by another surrogate of the same model. */
+bcs_status bcs_surrogate_set_scales(bcs_surrogate* sur, const float* in53);
+
 /* Grid arrays for parity checks, the UniformGrid members gridCellIds,
  * particleIds, gridCellStarts, gridCellEnds (src/grids/uniform_grid.cuh:32-35)
  * after the last bcs_calculate_grids / bcs_step.  which = 0: particle grid,

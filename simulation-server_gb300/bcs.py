@@ -30,6 +30,10 @@ EXPORTED = [
     "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
     "bcs_profile_steps", "bcs_grid_sort_static", "bcs_create_batch", "bcs_get_scene_info",
     "bcs_get_tuning", "bcs_set_tuning", "bcs_autotune", "bcs_macro_step",
+    "bcs_surrogate_create", "bcs_surrogate_destroy", "bcs_surrogate_collect", "bcs_surrogate_train",
+    "bcs_surrogate_enable", "bcs_surrogate_get_stats", "bcs_surrogate_reset_stats", "bcs_surrogate_param_count",
+    "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
+    "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales",
 ]
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
 GRID_SORT_STATIC_MAX = 262144
@@ -128,6 +132,21 @@ class Tuning(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class SurrogateDesc(C.Structure):
+    _fields_ = [("cell_type", C.c_int), ("substeps", C.c_int), ("layers", C.c_int), ("max_samples", C.c_int),
+                ("seed", C.c_uint64), ("tolerance", C.c_float)]
+
+
+class SurrogateStats(C.Structure):
+    _fields_ = [("cells", C.c_int64), ("samples", C.c_int64), ("valid_samples", C.c_int64),
+                ("predicted_cells", C.c_int64), ("fallback_cells", C.c_int64), ("iterations", C.c_int64),
+                ("parameters", C.c_int64), ("last_loss", C.c_float), ("tolerance", C.c_float),
+                ("flops_per_cell", C.c_double), ("device_bytes", C.c_size_t)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -152,6 +171,21 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_set_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "bcs_autotune": ([P, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)], C.c_int),
         "bcs_macro_step": ([P, C.c_int, C.c_int], C.c_int),
+        "bcs_surrogate_create": ([P, C.POINTER(SurrogateDesc), C.POINTER(P)], C.c_int),
+        "bcs_surrogate_destroy": ([P], C.c_int),
+        "bcs_surrogate_collect": ([P, C.c_int], C.c_int),
+        "bcs_surrogate_train": ([P, C.c_int, C.c_int, C.c_float, C.POINTER(C.c_float)], C.c_int),
+        "bcs_surrogate_enable": ([P, C.c_int], C.c_int),
+        "bcs_surrogate_get_stats": ([P, C.POINTER(SurrogateStats)], C.c_int),
+        "bcs_surrogate_reset_stats": ([P], C.c_int),
+        "bcs_surrogate_param_count": ([P], C.c_int64),
+        "bcs_surrogate_get_params": ([P, P, C.c_int64], C.c_int),
+        "bcs_surrogate_set_params": ([P, P, C.c_int64], C.c_int),
+        "bcs_surrogate_loss_grad": ([P, C.c_int, P, P, P, P, P], C.c_int),
+        "bcs_surrogate_forward": ([P, C.c_int, P, P, P], C.c_int),
+        "bcs_surrogate_get_scales": ([P, P], C.c_int),
+        "bcs_surrogate_set_scales": ([P, P], C.c_int),
+        "bcs_surrogate_evaluate": ([P, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
         "bcs_destroy": ([P], C.c_int),
         "bcs_get_info": ([P, C.POINTER(Info)], C.c_int),
         "bcs_set_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
@@ -429,3 +463,97 @@ class Simulation:
     def refresh_info(self) -> Info:
         _check(self.lib.bcs_get_info(self.h, C.byref(self.info)), "bcs_get_info")
         return self.info
+
+
+class Surrogate:
+    """The learned sub-step network of one cell model of `sim` (a
+    bcs_surrogate handle)."""
+
+    def __init__(self, sim: Simulation, cell_type: int = 0, substeps: int = 8, layers: int = 3,
+                 max_samples: int = 4096, seed: int = 1, tolerance: float = 0.0):
+        self.lib = sim.lib
+        self.sim = sim
+        d = SurrogateDesc(int(cell_type), int(substeps), int(layers), int(max_samples), int(seed), float(tolerance))
+        h = C.c_void_p()
+        _check(self.lib.bcs_surrogate_create(sim.h, C.byref(d), C.byref(h)), "bcs_surrogate_create")
+        self.h = h
+        self.substeps = int(substeps)
+        self.pic = len(sim.scene.types[cell_type].vertices) if hasattr(sim.scene, "types") else None
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.bcs_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def collect(self, macro_steps: int) -> None:
+        _check(self.lib.bcs_surrogate_collect(self.h, int(macro_steps)), "bcs_surrogate_collect")
+
+    def train(self, iterations: int, batch_cells: int = 64, lr: float = 1e-3) -> float:
+        loss = C.c_float()
+        _check(self.lib.bcs_surrogate_train(self.h, int(iterations), int(batch_cells), float(lr), C.byref(loss)),
+               "bcs_surrogate_train")
+        return loss.value
+
+    def enable(self, on: bool = True) -> None:
+        _check(self.lib.bcs_surrogate_enable(self.h, int(bool(on))), "bcs_surrogate_enable")
+
+    def stats(self) -> dict:
+        st = SurrogateStats()
+        _check(self.lib.bcs_surrogate_get_stats(self.h, C.byref(st)), "bcs_surrogate_get_stats")
+        return st.as_dict()
+
+    def reset_stats(self) -> None:
+        _check(self.lib.bcs_surrogate_reset_stats(self.h), "bcs_surrogate_reset_stats")
+
+    def param_count(self) -> int:
+        return int(self.lib.bcs_surrogate_param_count(self.h))
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.param_count(), np.float32)
+        _check(self.lib.bcs_surrogate_get_params(self.h, out.ctypes.data, out.size), "bcs_surrogate_get_params")
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        _check(self.lib.bcs_surrogate_set_params(self.h, p.ctypes.data, p.size), "bcs_surrogate_set_params")
+
+    def loss_grad(self, cells, features, edge_features, targets):
+        f = np.ascontiguousarray(features, np.float32)
+        e = np.ascontiguousarray(edge_features, np.float32)
+        t = np.ascontiguousarray(targets, np.float32)
+        loss = np.zeros(1, np.float32)
+        g = np.empty(self.param_count(), np.float32)
+        _check(self.lib.bcs_surrogate_loss_grad(self.h, int(cells), f.ctypes.data, e.ctypes.data, t.ctypes.data,
+                                                loss.ctypes.data, g.ctypes.data), "bcs_surrogate_loss_grad")
+        return float(loss[0]), g
+
+    def forward(self, cells, features, edge_features):
+        f = np.ascontiguousarray(features, np.float32)
+        e = np.ascontiguousarray(edge_features, np.float32)
+        y = np.empty((f.shape[0], 9), np.float32)
+        _check(self.lib.bcs_surrogate_forward(self.h, int(cells), f.ctypes.data, e.ctypes.data, y.ctypes.data),
+               "bcs_surrogate_forward")
+        return y
+
+    def evaluate(self, first: int, count: int):
+        """(network error, extrapolation error) on stored samples [first, first + count)."""
+        a, b = C.c_double(), C.c_double()
+        _check(self.lib.bcs_surrogate_evaluate(self.h, int(first), int(count), C.byref(a), C.byref(b)),
+               "bcs_surrogate_evaluate")
+        return a.value, b.value
+
+    def scales(self) -> np.ndarray:
+        out = np.empty(53, np.float32)
+        _check(self.lib.bcs_surrogate_get_scales(self.h, out.ctypes.data), "bcs_surrogate_get_scales")
+        return out
+
+    def set_scales(self, sc) -> None:
+        sc = np.ascontiguousarray(sc, np.float32)
+        assert sc.size == 53
+        _check(self.lib.bcs_surrogate_set_scales(self.h, sc.ctypes.data), "bcs_surrogate_set_scales")

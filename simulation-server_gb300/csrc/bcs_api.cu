@@ -14,10 +14,12 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <memory>
 #include <new>
 #include <vector>
 
 #include "bcs_internal.cuh"
+#include "bcs_mpnn.cuh"
 
 namespace bcs {
 // bcs_kernels.cu
@@ -44,6 +46,15 @@ void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, floa
 void launch_tri_cache(const int* ids, const uint32_t* tri, const float4* vpos, int T, float4* cache, cudaStream_t s);
 void launch_bump_step(long long* steps, int by, cudaStream_t s);
 void launch_substeps(const StepArgs& a, int items, int K, cudaStream_t s);
+void launch_sur_features(const StepArgs& a, const SurDev& d, cudaStream_t s);
+void launch_sur_targets(const StepArgs& a, const SurDev& d, float* raw_t, unsigned char* valid, cudaStream_t s);
+void launch_sur_inputs(const float* raw, const float* raw_t, const int* list, int nvalid, unsigned long long seed,
+                       int first, int cells, int pic, const int* adj_off, const int* adj_nbr, const float* adj_len,
+                       const SurScales& sc, float* f, float* E, float* T, cudaStream_t s);
+void launch_sur_apply(const StepArgs& a, const SurDev& d, const float* Y, const SurScales& sc, int first, int cells,
+                      cudaStream_t s);
+void launch_sur_eval(const float* Y, const float* raw_t, const unsigned char* valid, const SurScales& sc, int first,
+                     int cells, int pic, double* sums, cudaStream_t s);
 void launch_export(const float4* pos, int n, const float4* vpos, int V, float* pvbo, float* poff, float* vvbo,
                    cudaStream_t s);
 void launch_pack(const float* x, const float* y, const float* z, int n, float4* out, const float* wsrc,
@@ -158,6 +169,10 @@ struct bcs_sim {
     StepArgs args{};
     std::map<long long, cudaGraphExec_t> graphs;   // by (sub-steps, cur, sorted slot)
     float4* fext = nullptr;      // macro steps: held external force per particle
+    bcs_surrogate* surrogate = nullptr;   // enabled learned sub-step path, or null
+    // host copies of the per-model tables (surrogate graphs and tolerances)
+    std::vector<int> h_adj_off, h_adj_nbr;
+    std::vector<float> h_adj_len, h_radius_model;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t pev[BCS_PHASE_COUNT + 1] = {};
     float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
@@ -355,13 +370,24 @@ void enqueue_frame(bcs_sim* s, cudaEvent_t* ev = nullptr) {
     ++s->host_steps;
 }
 
+// Points where the learned sub-step path joins a macro step: after sub-step 1
+// (the state in the output buffers, the held force in fext) and after
+// sub-steps 2..K.
+struct MacroHooks {
+    void (*after_first)(bcs_sim*) = nullptr;
+    void (*after_substeps)(bcs_sim*) = nullptr;
+};
+
 // One multi-rate macro step of K sub-steps (K >= 2): sub-step 1 is the
 // fused frame, which also records each particle's external force (collisions
 // and the vein's force adjustment); sub-steps 2..K re-integrate cell springs
 // and environment with that force held (k_substeps), the vein mesh takes K
 // sub-steps with the particle impacts in the first, and the step counter
 // advances by K.
-void enqueue_macro(bcs_sim* s, int K) {
+const MacroHooks* inference_hooks(bcs_sim* s, int K);
+
+void enqueue_macro(bcs_sim* s, int K, const MacroHooks* hooks = nullptr) {
+    if (!hooks) hooks = inference_hooks(s, K);
     enqueue_grids(s);
     enqueue_vein_forces(s);
     const int in = s->cur, out = s->cur ^ 1;
@@ -370,8 +396,11 @@ void enqueue_macro(bcs_sim* s, int K) {
     launch_step(s->args, (int)s->work_host.size(), 0, s->tune.step_shape, s->persistent_grid[0], s->stream);
     if (s->p.use_blood_flow) launch_vein_end(s->args, s->C, s->stream);
     refresh_args(s, in, out, true);
+    if (hooks && hooks->after_first) hooks->after_first(s);
     launch_substeps(s->args, (int)s->work_host.size(), K, s->stream);
+    if (hooks && hooks->after_substeps) hooks->after_substeps(s);
     s->args.fext = nullptr;
+    s->args.skip_cell = nullptr;
     if (s->p.vein_dynamic && s->V > 0) {
         for (int k = 1; k <= K; ++k) {
             if (k > 1)
@@ -740,6 +769,10 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
         nb_ids.insert(nb_ids.end(), nb_scene_ids[k].begin(), nb_scene_ids[k].end());
         nb_len.insert(nb_len.end(), nb_scene_len[k].begin(), nb_scene_len[k].end());
     }
+    s->h_adj_off = adj_off;
+    s->h_adj_nbr = adj_nbr;
+    s->h_adj_len = adj_len;
+    s->h_radius_model = radius_model;
     std::vector<float> radius_particle(s->N);
     for (const TypeDev& td : s->types)
         for (int i = 0; i < td.count * td.pic; ++i)
@@ -893,6 +926,153 @@ bcs_status get_vec(bcs_sim* s, const float4* src, int n, const bcs_vec3& v, bcs_
 }  // namespace
 
 // ================================================================ C ABI ====
+// ------------------------------------------------- learned sub-steps ----
+struct bcs_surrogate {
+    bcs_sim* sim = nullptr;
+    int K = 8;
+    float tolerance = 0.f;
+    int cells = 0, pic = 0, model_type = 0;
+    std::vector<int> cell_type, cell_index;
+    int *d_cell_type = nullptr, *d_cell_index = nullptr;
+    MpnnNet net;
+    float* raw = nullptr;              // features of the current macro step
+    float4* start = nullptr;
+    unsigned char* skip = nullptr;     // per blood cell of the simulation
+    unsigned long long* counts = nullptr;
+    // training set
+    int capacity = 0, stored = 0, nvalid = 0;
+    float *ds_raw = nullptr, *ds_t = nullptr;
+    unsigned char* ds_valid = nullptr;
+    int* valid_list = nullptr;
+    bool collecting = false, enabled = false, scales_set = false;
+    SurScales scales{};
+    unsigned long long seed = 0, draws = 0;
+    long long iterations = 0;
+    float last_loss = 0.f;
+    int infer_cells = 0;               // cells per inference chunk
+    std::vector<void*> allocs;
+    size_t bytes = 0;
+    ~bcs_surrogate() {
+        for (void* p : allocs) cudaFree(p);
+    }
+    template <class T>
+    bool alloc(T** p, size_t n) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, sizeof(T) * std::max<size_t>(1, n)) != cudaSuccess) return false;
+        allocs.push_back(q);
+        bytes += sizeof(T) * n;
+        *p = static_cast<T*>(q);
+        return true;
+    }
+    SurDev dev(float* raw_to) const {
+        SurDev d{};
+        d.cell_type = d_cell_type;
+        d.cell_index = d_cell_index;
+        d.cells = cells;
+        d.pic = pic;
+        d.K = K;
+        d.T = (float)(K - 1) * sim->p.dt;
+        d.tolerance = tolerance;
+        d.raw = raw_to;
+        d.start = start;
+        d.skip = skip;
+        d.counts = counts;
+        return d;
+    }
+};
+
+namespace {
+void collect_after_first(bcs_sim* s) {
+    bcs_surrogate* z = s->surrogate;
+    launch_sur_features(s->args, z->dev(z->ds_raw + (size_t)z->stored * z->pic * 16), s->stream);
+}
+void collect_after_substeps(bcs_sim* s) {
+    bcs_surrogate* z = s->surrogate;
+    launch_sur_targets(s->args, z->dev(nullptr), z->ds_t + (size_t)z->stored * z->pic * 9,
+                       z->ds_valid + z->stored, s->stream);
+}
+void infer_after_first(bcs_sim* s) {
+    bcs_surrogate* z = s->surrogate;
+    launch_sur_features(s->args, z->dev(z->raw), s->stream);
+    for (int first = 0; first < z->cells; first += z->infer_cells) {
+        const int n = std::min(z->infer_cells, z->cells - first);
+        launch_sur_inputs(z->raw, nullptr, nullptr, 0, 0, first, n, z->pic, z->net.dev_adj_off(), z->net.dev_adj_nbr(),
+                          z->net.dev_adj_len(), z->scales, z->net.input_buf(), z->net.edge_buf(), nullptr, s->stream);
+        z->net.forward(z->net.input_buf(), z->net.edge_buf(), n, false);
+        launch_sur_apply(s->args, z->dev(z->raw), z->net.output(), z->scales, first, n, s->stream);
+    }
+    s->args.skip_cell = z->skip;
+}
+const MacroHooks kCollectHooks{collect_after_first, collect_after_substeps};
+const MacroHooks kInferHooks{infer_after_first, nullptr};
+
+// Means and spreads of the network's inputs and targets over (a sample of)
+// the training set.
+bcs_status compute_scales(bcs_surrogate* z) {
+    const int n = std::min(z->stored, 4096);
+    if (n <= 0) return BCS_ERR_INVALID_ARGUMENT;
+    std::vector<float> f((size_t)n * z->pic * 16), t((size_t)n * z->pic * 9);
+    std::vector<unsigned char> ok(n);
+    BCS_CUDA(cudaMemcpy(f.data(), z->ds_raw, sizeof(float) * f.size(), cudaMemcpyDeviceToHost));
+    BCS_CUDA(cudaMemcpy(t.data(), z->ds_t, sizeof(float) * t.size(), cudaMemcpyDeviceToHost));
+    BCS_CUDA(cudaMemcpy(ok.data(), z->ds_valid, n, cudaMemcpyDeviceToHost));
+    double fs[16] = {}, fq[16] = {}, ts[9] = {}, tq[9] = {}, rq = 0, uq = 0, lq = 0;
+    long long nodes = 0, edges = 0;
+    const std::vector<int>& off = z->sim->h_adj_off;
+    const std::vector<int>& nbr = z->sim->h_adj_nbr;
+    const std::vector<float>& len = z->sim->h_adj_len;
+    const int a0 = z->sim->types[z->model_type].adj_start;
+    for (int c = 0; c < n; ++c) {
+        if (!ok[c]) continue;
+        for (int i = 0; i < z->pic; ++i) {
+            const float* fi = &f[((size_t)c * z->pic + i) * 16];
+            const float* ti = &t[((size_t)c * z->pic + i) * 9];
+            for (int q = 0; q < 16; ++q) { fs[q] += fi[q]; fq[q] += (double)fi[q] * fi[q]; }
+            for (int q = 0; q < 9; ++q) { ts[q] += ti[q]; tq[q] += (double)ti[q] * ti[q]; }
+            ++nodes;
+            for (int k = off[a0 + i]; k < off[a0 + i + 1]; ++k) {
+                const float* fj = &f[((size_t)c * z->pic + nbr[k]) * 16];
+                double dr[3] = {fi[0] - fj[0], fi[1] - fj[1], fi[2] - fj[2]};
+                double du[3] = {fi[3] - fj[3], fi[4] - fj[4], fi[5] - fj[5]};
+                const double d = std::sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]) - len[k];
+                rq += (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]) / 3;
+                uq += (du[0] * du[0] + du[1] * du[1] + du[2] * du[2]) / 3;
+                lq += d * d;
+                ++edges;
+            }
+        }
+    }
+    if (nodes == 0) return BCS_ERR_INVALID_ARGUMENT;
+    auto spread = [](double q, double m, long long k) {
+        const double v = q / k - m * m;
+        return v > 1e-20 ? std::sqrt(v) : 1.0;
+    };
+    for (int q = 0; q < 16; ++q) {
+        const double m = fs[q] / nodes;
+        z->scales.fm[q] = (float)m;
+        z->scales.fs[q] = (float)(1.0 / spread(fq[q], m, nodes));
+    }
+    for (int q = 0; q < 9; ++q) {
+        const double m = ts[q] / nodes;
+        z->scales.tm[q] = (float)m;
+        z->scales.ts[q] = (float)spread(tq[q], m, nodes);
+    }
+    auto rms = [](double q, long long k) { return q > 1e-30 && k ? (float)std::sqrt(q / k) : 1.0f; };
+    z->scales.er = rms(rq, edges);
+    z->scales.eu = rms(uq, edges);
+    z->scales.el = rms(lq, edges);
+    z->scales_set = true;
+    return BCS_OK;
+}
+
+const MacroHooks* inference_hooks(bcs_sim* s, int K) {
+    bcs_surrogate* z = s->surrogate;
+    if (!z) return nullptr;
+    if (z->collecting) return &kCollectHooks;
+    return z->enabled && z->K == K ? &kInferHooks : nullptr;
+}
+}  // namespace
+
 extern "C" {
 
 void bcs_default_params(bcs_params* p) {
@@ -1418,6 +1598,271 @@ bcs_status bcs_profile_steps(bcs_sim* s, int nsteps, float* phase_ms) {
         }
     }
     return check_last();
+}
+
+bcs_status bcs_surrogate_create(bcs_sim* s, const bcs_surrogate_desc* d, bcs_surrogate** out) {
+    if (!s || !d || !out) return BCS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (d->cell_type < 0 || d->cell_type >= (int)s->types.size() || d->substeps < 2 ||
+        d->substeps > BCS_MAX_SUBSTEPS || d->layers < 1 || d->layers > kMaxLayers || d->max_samples < 1 ||
+        d->tolerance < 0.f)
+        return BCS_ERR_INVALID_ARGUMENT;
+    const TypeDev& t0 = s->types[d->cell_type];
+    if (t0.pic > 6 * 32) return BCS_ERR_UNSUPPORTED;
+    std::unique_ptr<bcs_surrogate> z(new (std::nothrow) bcs_surrogate());
+    if (!z) return BCS_ERR_OUT_OF_MEMORY;
+    z->sim = s;
+    z->K = d->substeps;
+    z->model_type = d->cell_type;
+    z->pic = t0.pic;
+    z->seed = d->seed;
+    // every type with the same cell model (batches repeat a model per scene)
+    auto same_model = [&](const TypeDev& t) {
+        if (t.pic != t0.pic) return false;
+        for (int i = 0; i <= t.pic; ++i)
+            if (s->h_adj_off[t.adj_start + i] - s->h_adj_off[t.adj_start] !=
+                s->h_adj_off[t0.adj_start + i] - s->h_adj_off[t0.adj_start])
+                return false;
+        const int e = s->h_adj_off[t0.adj_start + t0.pic] - s->h_adj_off[t0.adj_start];
+        const int b = s->h_adj_off[t.adj_start], b0 = s->h_adj_off[t0.adj_start];
+        for (int k = 0; k < e; ++k)
+            if (s->h_adj_nbr[b + k] != s->h_adj_nbr[b0 + k] || s->h_adj_len[b + k] != s->h_adj_len[b0 + k])
+                return false;
+        return true;
+    };
+    float rmin = std::numeric_limits<float>::max();
+    for (int i = 0; i < t0.pic; ++i) rmin = std::min(rmin, s->h_radius_model[t0.model_start + i]);
+    z->tolerance = d->tolerance > 0.f ? d->tolerance : 1e-3f * rmin;
+    for (int ti = 0; ti < (int)s->types.size(); ++ti)
+        if (same_model(s->types[ti]))
+            for (int c = 0; c < s->types[ti].count; ++c) {
+                z->cell_type.push_back(ti);
+                z->cell_index.push_back(c);
+            }
+    z->cells = (int)z->cell_type.size();
+    if (z->cells == 0) return BCS_ERR_INVALID_ARGUMENT;
+    // graph of one cell, neighbour indices within the cell
+    const int a0 = s->h_adj_off[t0.adj_start];
+    std::vector<int> off(t0.pic + 1), nbr;
+    std::vector<float> len;
+    for (int i = 0; i <= t0.pic; ++i) off[i] = s->h_adj_off[t0.adj_start + i] - a0;
+    nbr.assign(s->h_adj_nbr.begin() + a0, s->h_adj_nbr.begin() + a0 + off[t0.pic]);
+    len.assign(s->h_adj_len.begin() + a0, s->h_adj_len.begin() + a0 + off[t0.pic]);
+    const int train_cells = std::max(1, std::min(d->max_samples, 1024));
+    z->infer_cells = std::max(train_cells, std::min(z->cells, 2048));
+    if (z->net.init(d->layers, t0.pic, off.data(), nbr.data(), len.data(), z->infer_cells, d->seed, s->stream) !=
+        (int)cudaSuccess)
+        return BCS_ERR_OUT_OF_MEMORY;
+    z->capacity = d->max_samples;
+    if (!z->alloc(&z->d_cell_type, z->cells) || !z->alloc(&z->d_cell_index, z->cells) ||
+        !z->alloc(&z->raw, (size_t)z->cells * z->pic * 16) || !z->alloc(&z->start, (size_t)z->cells * z->pic * 3) ||
+        !z->alloc(&z->skip, s->C) || !z->alloc(&z->counts, 2) ||
+        !z->alloc(&z->ds_raw, (size_t)z->capacity * z->pic * 16) || !z->alloc(&z->ds_t, (size_t)z->capacity * z->pic * 9) ||
+        !z->alloc(&z->ds_valid, z->capacity) || !z->alloc(&z->valid_list, z->capacity))
+        return BCS_ERR_OUT_OF_MEMORY;
+    BCS_CUDA(cudaMemcpy(z->d_cell_type, z->cell_type.data(), sizeof(int) * z->cells, cudaMemcpyHostToDevice));
+    BCS_CUDA(cudaMemcpy(z->d_cell_index, z->cell_index.data(), sizeof(int) * z->cells, cudaMemcpyHostToDevice));
+    BCS_CUDA(cudaMemset(z->skip, 0, s->C));
+    BCS_CUDA(cudaMemset(z->counts, 0, 2 * sizeof(unsigned long long)));
+    BCS_CUDA(cudaMemset(z->ds_valid, 0, z->capacity));
+    *out = z.release();
+    return BCS_OK;
+}
+
+bcs_status bcs_surrogate_destroy(bcs_surrogate* z) {
+    if (!z) return BCS_ERR_INVALID_ARGUMENT;
+    if (z->sim && z->sim->surrogate == z) {
+        z->sim->surrogate = nullptr;
+        drop_graphs(z->sim);
+    }
+    cudaStreamSynchronize(z->sim->stream);
+    delete z;
+    return BCS_OK;
+}
+
+bcs_status bcs_surrogate_collect(bcs_surrogate* z, int macro_steps) {
+    if (!z || macro_steps < 0) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_sim* s = z->sim;
+    if (s->mid_frame || (s->surrogate && s->surrogate != z)) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_surrogate* prev = s->surrogate;
+    s->surrogate = z;
+    z->collecting = true;
+    bcs_status st = BCS_OK;
+    for (int i = 0; i < macro_steps && z->stored + z->cells <= z->capacity; ++i) {
+        enqueue_macro(s, z->K, &kCollectHooks);
+        if ((st = check_last())) break;
+        z->stored += z->cells;
+    }
+    z->collecting = false;
+    s->surrogate = prev;
+    if (st != BCS_OK) return st;
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    // list of valid samples
+    std::vector<unsigned char> ok(z->stored);
+    if (z->stored) BCS_CUDA(cudaMemcpy(ok.data(), z->ds_valid, z->stored, cudaMemcpyDeviceToHost));
+    std::vector<int> list;
+    for (int i = 0; i < z->stored; ++i)
+        if (ok[i]) list.push_back(i);
+    z->nvalid = (int)list.size();
+    if (z->nvalid) BCS_CUDA(cudaMemcpy(z->valid_list, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
+    return check_last();
+}
+
+bcs_status bcs_surrogate_train(bcs_surrogate* z, int iterations, int batch_cells, float lr, float* loss) {
+    if (!z || iterations < 0 || batch_cells < 1 || batch_cells > z->net.max_cells() || !(lr > 0.f))
+        return BCS_ERR_INVALID_ARGUMENT;
+    if (z->nvalid == 0) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_status st;
+    if (!z->scales_set && (st = compute_scales(z))) return st;
+    cudaStream_t stream = z->sim->stream;
+    for (int it = 0; it < iterations; ++it) {
+        launch_sur_inputs(z->ds_raw, z->ds_t, z->valid_list, z->nvalid, z->seed * 0x9E3779B97F4A7C15ull + (++z->draws),
+                          0, batch_cells, z->pic, z->net.dev_adj_off(), z->net.dev_adj_nbr(), z->net.dev_adj_len(),
+                          z->scales, z->net.input_buf(), z->net.edge_buf(), z->net.target_buf(), stream);
+        z->net.forward(z->net.input_buf(), z->net.edge_buf(), batch_cells, true);
+        z->net.backward(z->net.target_buf(), batch_cells);
+        z->net.adam(lr);
+        ++z->iterations;
+    }
+    if (iterations > 0) {
+        BCS_CUDA(cudaMemcpyAsync(&z->last_loss, z->net.loss_dev(), sizeof(float), cudaMemcpyDeviceToHost, stream));
+        BCS_CUDA(cudaStreamSynchronize(stream));
+    }
+    if (loss) *loss = z->last_loss;
+    return check_last();
+}
+
+bcs_status bcs_surrogate_enable(bcs_surrogate* z, int on) {
+    if (!z) return BCS_ERR_INVALID_ARGUMENT;
+    bcs_sim* s = z->sim;
+    if (s->mid_frame || (s->surrogate && s->surrogate != z)) return BCS_ERR_INVALID_ARGUMENT;
+    if (on && !z->scales_set) return BCS_ERR_INVALID_ARGUMENT;   // train (or set the scales) first
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    z->enabled = on != 0;
+    s->surrogate = z->enabled ? z : nullptr;
+    BCS_CUDA(cudaMemset(z->skip, 0, s->C));
+    drop_graphs(s);
+    return BCS_OK;
+}
+
+bcs_status bcs_surrogate_get_stats(bcs_surrogate* z, bcs_surrogate_stats* o) {
+    if (!z || !o) return BCS_ERR_INVALID_ARGUMENT;
+    unsigned long long c[2] = {0, 0};
+    BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
+    BCS_CUDA(cudaMemcpy(c, z->counts, sizeof(c), cudaMemcpyDeviceToHost));
+    std::memset(o, 0, sizeof(*o));
+    o->cells = z->cells;
+    o->samples = z->stored;
+    o->valid_samples = z->nvalid;
+    o->predicted_cells = (int64_t)c[0];
+    o->fallback_cells = (int64_t)c[1];
+    o->iterations = z->iterations;
+    o->last_loss = z->last_loss;
+    o->parameters = z->net.param_count();
+    o->tolerance = z->tolerance;
+    // multiply-adds x 2 of one forward pass over one cell
+    const double n = z->pic, e = z->net.edges(), H = kHidden;
+    o->flops_per_cell = 2.0 * (n * kFeatIn * H + z->net.layers() * (4.0 * n * H * H + e * kEdgeIn * H) + n * H * kOut);
+    o->device_bytes = z->bytes + z->net.bytes();
+    return BCS_OK;
+}
+
+bcs_status bcs_surrogate_reset_stats(bcs_surrogate* z) {
+    if (!z) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
+    BCS_CUDA(cudaMemset(z->counts, 0, 2 * sizeof(unsigned long long)));
+    return BCS_OK;
+}
+
+int64_t bcs_surrogate_param_count(bcs_surrogate* z) { return z ? z->net.param_count() : 0; }
+
+bcs_status bcs_surrogate_get_params(bcs_surrogate* z, float* out, int64_t count) {
+    if (!z || !out || count != z->net.param_count()) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
+    BCS_CUDA(cudaMemcpy(out, z->net.params(), sizeof(float) * count, cudaMemcpyDeviceToHost));
+    return BCS_OK;
+}
+
+bcs_status bcs_surrogate_set_params(bcs_surrogate* z, const float* in, int64_t count) {
+    if (!z || !in || count != z->net.param_count()) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
+    BCS_CUDA(cudaMemcpy(z->net.params(), in, sizeof(float) * count, cudaMemcpyHostToDevice));
+    z->net.refresh_bf16();
+    BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
+    return check_last();
+}
+
+bcs_status bcs_surrogate_loss_grad(bcs_surrogate* z, int cells, const float* features, const float* edge_features,
+                                   const float* targets, float* loss, float* grads) {
+    if (!z || cells < 1 || cells > z->net.max_cells() || !features || !edge_features || !targets)
+        return BCS_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = z->sim->stream;
+    const size_t n = (size_t)cells * z->pic;
+    BCS_CUDA(cudaMemcpyAsync(z->net.input_buf(), features, sizeof(float) * n * kFeatIn, cudaMemcpyHostToDevice, st));
+    BCS_CUDA(cudaMemcpyAsync(z->net.edge_buf(), edge_features, sizeof(float) * (size_t)cells * z->net.edges() * kEdgeIn,
+                             cudaMemcpyHostToDevice, st));
+    BCS_CUDA(cudaMemcpyAsync(z->net.target_buf(), targets, sizeof(float) * n * kOut, cudaMemcpyHostToDevice, st));
+    z->net.forward(z->net.input_buf(), z->net.edge_buf(), cells, true);
+    z->net.backward(z->net.target_buf(), cells);
+    if (loss) BCS_CUDA(cudaMemcpyAsync(loss, z->net.loss_dev(), sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (grads)
+        BCS_CUDA(cudaMemcpyAsync(grads, z->net.grad(), sizeof(float) * z->net.param_count(), cudaMemcpyDeviceToHost, st));
+    BCS_CUDA(cudaStreamSynchronize(st));
+    return check_last();
+}
+
+bcs_status bcs_surrogate_forward(bcs_surrogate* z, int cells, const float* features, const float* edge_features,
+                                 float* outputs) {
+    if (!z || cells < 1 || cells > z->net.max_cells() || !features || !edge_features || !outputs)
+        return BCS_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = z->sim->stream;
+    const size_t n = (size_t)cells * z->pic;
+    BCS_CUDA(cudaMemcpyAsync(z->net.input_buf(), features, sizeof(float) * n * kFeatIn, cudaMemcpyHostToDevice, st));
+    BCS_CUDA(cudaMemcpyAsync(z->net.edge_buf(), edge_features, sizeof(float) * (size_t)cells * z->net.edges() * kEdgeIn,
+                             cudaMemcpyHostToDevice, st));
+    z->net.forward(z->net.input_buf(), z->net.edge_buf(), cells, false);
+    BCS_CUDA(cudaMemcpyAsync(outputs, z->net.output(), sizeof(float) * n * kOut, cudaMemcpyDeviceToHost, st));
+    BCS_CUDA(cudaStreamSynchronize(st));
+    return check_last();
+}
+
+bcs_status bcs_surrogate_evaluate(bcs_surrogate* z, int first, int count, double* net_error, double* base_error) {
+    if (!z || first < 0 || count < 1 || first + count > z->stored || !z->scales_set) return BCS_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = z->sim->stream;
+    double* sums = nullptr;
+    BCS_CUDA(cudaMalloc(&sums, 3 * sizeof(double)));
+    BCS_CUDA(cudaMemsetAsync(sums, 0, 3 * sizeof(double), st));
+    for (int b = first; b < first + count; b += z->net.max_cells()) {
+        const int n = std::min(z->net.max_cells(), first + count - b);
+        launch_sur_inputs(z->ds_raw, nullptr, nullptr, 0, 0, b, n, z->pic, z->net.dev_adj_off(), z->net.dev_adj_nbr(),
+                          z->net.dev_adj_len(), z->scales, z->net.input_buf(), z->net.edge_buf(), nullptr, st);
+        z->net.forward(z->net.input_buf(), z->net.edge_buf(), n, false);
+        launch_sur_eval(z->net.output(), z->ds_t, z->ds_valid, z->scales, b, n, z->pic, sums, st);
+    }
+    double h[3] = {0, 0, 0};
+    cudaError_t e = cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(sums);
+    if (e != cudaSuccess) return BCS_ERR_CUDA;
+    if (h[2] <= 0) return BCS_ERR_INVALID_ARGUMENT;
+    if (net_error) *net_error = h[0] / h[2];
+    if (base_error) *base_error = h[1] / h[2];
+    return check_last();
+}
+
+bcs_status bcs_surrogate_set_scales(bcs_surrogate* z, const float* in) {
+    if (!z || !in) return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
+    std::memcpy(&z->scales, in, sizeof(SurScales));
+    z->scales_set = true;
+    drop_graphs(z->sim);   // captured macro steps hold the old scales
+    return BCS_OK;
+}
+
+bcs_status bcs_surrogate_get_scales(bcs_surrogate* z, float* out) {
+    if (!z || !out) return BCS_ERR_INVALID_ARGUMENT;
+    std::memcpy(out, &z->scales, sizeof(SurScales));
+    return z->scales_set ? BCS_OK : BCS_ERR_INVALID_ARGUMENT;
 }
 
 }  // extern "C"

@@ -126,6 +126,7 @@ struct StepArgs {
     int* keys_out;        // next-step grid keys (canonical order) or null
     int* ids_out;
     float4* fext;         // macro steps: external force of sub-step 1 (held), or null
+    const unsigned char* skip_cell;   // macro steps: cells the network advanced (k_substeps skips them), or null
     int n;
     // layout
     const WorkItem* work;
@@ -156,6 +157,27 @@ struct StepArgs {
     bcs_params p;
     const long long* steps;  // device step counter
     unsigned* err;        // device error word
+};
+
+// The learned sub-step path: one entry per surrogate cell (cells of every
+// type that shares the surrogate's cell model), and the normalisation of the
+// network's inputs and outputs.
+struct SurScales {
+    float fm[16], fs[16];   // node features: mean, 1 / std
+    float tm[9], ts[9];     // targets: mean, std
+    float er, el, eu;       // edge scales: relative position, stretch, relative velocity
+};
+
+struct SurDev {
+    const int* cell_type;   // per surrogate cell: type index
+    const int* cell_index;  // per surrogate cell: cell within its type
+    int cells, pic, K;
+    float T;                // (K - 1) dt: the span the network covers
+    float tolerance;        // residual threshold (length units)
+    float* raw;             // [cells][pic][16] raw node features of sub-step 1's state
+    float4* start;          // [cells][pic][3] x, v, F after sub-step 1
+    unsigned char* skip;    // per blood cell (batch-wide): 1 = advanced by the network this macro step
+    unsigned long long* counts;   // [0] cells predicted, [1] cells that fell back
 };
 
 // ------------------------------------------------------------- float3 ----

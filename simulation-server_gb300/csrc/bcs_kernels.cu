@@ -662,6 +662,7 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
             const int i = threadIdx.x + r * kSubstepThreads;
             if (i >= np) continue;
             const int c = i / pic, li = i - c * pic, cb = c * pic;
+            if (a.skip_cell && a.skip_cell[ty.cell_global + w.first_cell + c]) continue;
             const float3 x = xyz(s_pos[i]), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
             float3 F = f3(0.f, 0.f, 0.f);
             const int e0 = __ldg(&a.adj_off[ty.adj_start + li]), e1 = __ldg(&a.adj_off[ty.adj_start + li + 1]);
@@ -683,6 +684,7 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
         for (int r = 0; r < kSubstepPer; ++r) {
             const int i = threadIdx.x + r * kSubstepThreads;
             if (i >= np) continue;
+            if (a.skip_cell && a.skip_cell[ty.cell_global + w.first_cell + i / pic]) continue;
             s_pos[i] = make_float4(nx[r].x, nx[r].y, nx[r].z, s_pos[i].w);
             s_vel[i] = make_float4(nv[r].x, nv[r].y, nv[r].z, 0.f);
             s_frc[i] = make_float4(nF[r].x, nF[r].y, nF[r].z, 0.f);
@@ -710,6 +712,7 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
     for (int r = 0; r < kSubstepPer; ++r) {
         const int i = threadIdx.x + r * kSubstepThreads;
         if (i >= np) continue;
+        if (a.skip_cell && a.skip_cell[ty.cell_global + w.first_cell + i / pic]) continue;
         const int pid = p0 + i;
         const float4 x = s_pos[i], v = s_vel[i];
         if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z)))
@@ -723,6 +726,245 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
         }
     }
     if (e) atomicOr(a.err, e);
+}
+
+// ------------------------------------------------- learned sub-steps ----
+// Raw node features of every surrogate cell from the state after sub-step 1
+// (one warp per cell): position and velocity relative to the cell's centroid
+// and mean velocity, the current force, the held external force, the
+// environment force, and a wall-proximity flag (1 when the particle's
+// wall-mask cell holds a triangle within the impact distance).  The state
+// itself is kept in `start` for the targets and the prediction.
+__global__ void k_sur_features(const StepArgs a, const SurDev d) {
+    const int sc_i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (sc_i >= d.cells) return;
+    const TypeDev ty = a.types[d.cell_type[sc_i]];
+    const SceneDev& sc = a.scenes[ty.scene];
+    const int pic = ty.pic, p0 = ty.particle_start + d.cell_index[sc_i] * pic;
+    float3 cx = f3(0.f, 0.f, 0.f), cv = cx;
+    for (int k = lane; k < pic; k += 32) {
+        cx = cx + xyz(a.pos_out[p0 + k]);
+        cv = cv + xyz(a.vel_out[p0 + k]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cx.x += __shfl_xor_sync(0xffffffffu, cx.x, o);
+        cx.y += __shfl_xor_sync(0xffffffffu, cx.y, o);
+        cx.z += __shfl_xor_sync(0xffffffffu, cx.z, o);
+        cv.x += __shfl_xor_sync(0xffffffffu, cv.x, o);
+        cv.y += __shfl_xor_sync(0xffffffffu, cv.y, o);
+        cv.z += __shfl_xor_sync(0xffffffffu, cv.z, o);
+    }
+    cx = cx / (float)pic;
+    cv = cv / (float)pic;
+    for (int k = lane; k < pic; k += 32) {
+        const int p = p0 + k;
+        const float4 x4 = a.pos_out[p], v4 = a.vel_out[p], f4 = a.frc_out[p], e4 = a.fext[p];
+        const float3 x = xyz(x4), v = xyz(v4);
+        const float3 r = x - cx, u = v - cv;
+        const float ratio = len3(r) / __ldg(&a.r0[ty.model_start + k]);
+        const float3 env = environment(a, sc, x, v, ratio);
+        float wall = 0.f;
+        if (a.wall_mask) {
+            const MaskGeom& m = sc.wall;
+            const int ix = (int)((x.x - m.lo[0]) * m.inv_cell), iy = (int)((x.y - m.lo[1]) * m.inv_cell),
+                      iz = (int)((x.z - m.lo[2]) * m.inv_cell);
+            if (ix >= 0 && iy >= 0 && iz >= 0 && ix < m.nx && iy < m.ny && iz < m.nz)
+                wall = a.wall_mask[m.offset + ((long long)iz * m.ny + iy) * m.nx + ix] ==
+                               (unsigned char)*a.wall_epoch ? 1.f : 0.f;
+        }
+        float* o = d.raw + ((size_t)sc_i * d.pic + k) * 16;
+        o[0] = r.x; o[1] = r.y; o[2] = r.z;
+        o[3] = u.x; o[4] = u.y; o[5] = u.z;
+        o[6] = f4.x; o[7] = f4.y; o[8] = f4.z;
+        o[9] = e4.x; o[10] = e4.y; o[11] = e4.z;
+        o[12] = env.x; o[13] = env.y; o[14] = env.z;
+        o[15] = wall;
+        float4* st = d.start + ((size_t)sc_i * d.pic + k) * 3;
+        st[0] = x4;
+        st[1] = v4;
+        st[2] = f4;
+    }
+}
+
+// Training targets after sub-steps 2..K: the departure of the final state
+// from the constant-force extrapolation of the state after sub-step 1,
+//   x_base = x1 + T v1 + T^2/2 F1,  v_base = v1 + T F1,
+// and the change of the force.  A cell that was respawned (a jump of more
+// than one length unit) is marked invalid.
+__global__ void k_sur_targets(const StepArgs a, const SurDev d, float* raw_t, unsigned char* valid) {
+    const int sc_i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (sc_i >= d.cells) return;
+    const TypeDev ty = a.types[d.cell_type[sc_i]];
+    const int pic = ty.pic, p0 = ty.particle_start + d.cell_index[sc_i] * pic;
+    const float T = d.T;
+    bool jump = false;
+    for (int k = lane; k < pic; k += 32) {
+        const float4* st = d.start + ((size_t)sc_i * d.pic + k) * 3;
+        const float3 x1 = xyz(st[0]), v1 = xyz(st[1]), F1 = xyz(st[2]);
+        const float3 xK = xyz(a.pos_out[p0 + k]), vK = xyz(a.vel_out[p0 + k]), FK = xyz(a.frc_out[p0 + k]);
+        const float3 dx = xK - (x1 + T * v1 + (0.5f * T * T) * F1);
+        const float3 dv = vK - (v1 + T * F1);
+        const float3 dF = FK - F1;
+        jump = jump || !(fabsf(dx.x) < 1.f && fabsf(dx.y) < 1.f && fabsf(dx.z) < 1.f) ||
+               !(isfinite(dv.x) && isfinite(dv.y) && isfinite(dv.z) && isfinite(dF.x) && isfinite(dF.y) &&
+                 isfinite(dF.z));
+        float* o = raw_t + ((size_t)sc_i * d.pic + k) * 9;
+        o[0] = dx.x; o[1] = dx.y; o[2] = dx.z;
+        o[3] = dv.x; o[4] = dv.y; o[5] = dv.z;
+        o[6] = dF.x; o[7] = dF.y; o[8] = dF.z;
+    }
+    jump = __any_sync(0xffffffffu, jump);
+    if (lane == 0) valid[sc_i] = jump ? 0 : 1;
+}
+
+// Normalised network inputs for `cells` cells: node features, edge features
+// (relative position, stretch against the rest length, relative velocity,
+// rest length) and, when raw_t is given, targets.  Cell b reads sample
+// idx[b] of the raw arrays (b itself when idx is null), or, with `nvalid`,
+// a sample drawn by Philox from list[0 .. nvalid) keyed by (seed, b).
+__global__ void k_sur_inputs(const float* __restrict__ raw, const float* __restrict__ raw_t, const int* __restrict__ list,
+                             int nvalid, unsigned long long seed, int first, int cells, int pic,
+                             const int* __restrict__ adj_off, const int* __restrict__ adj_nbr,
+                             const float* __restrict__ adj_len, const SurScales sc, float* f, float* E, float* T) {
+    const int b = blockIdx.x, edges = adj_off[pic];
+    if (b >= cells) return;
+    int src = first + b;
+    if (list) {
+        uint32_t c[4] = {(uint32_t)b, (uint32_t)(seed >> 32), 0u, 0u};
+        philox4x32_10(c, (uint32_t)seed, 0x5EEDu);
+        src = list[c[0] % (uint32_t)nvalid];
+    }
+    const float* rw = raw + (size_t)src * pic * 16;
+    for (int i = threadIdx.x; i < pic * 16; i += blockDim.x) {
+        const int q = i & 15;
+        f[(size_t)b * pic * 16 + i] = (rw[i] - sc.fm[q]) * sc.fs[q];
+    }
+    if (T && raw_t) {
+        const float* rt = raw_t + (size_t)src * pic * 9;
+        for (int i = threadIdx.x; i < pic * 9; i += blockDim.x) {
+            const int q = i % 9;
+            T[(size_t)b * pic * 9 + i] = (rt[i] - sc.tm[q]) / sc.ts[q];
+        }
+    }
+    for (int i = threadIdx.x; i < pic; i += blockDim.x)
+        for (int k = adj_off[i]; k < adj_off[i + 1]; ++k) {
+            const int j = adj_nbr[k];
+            const float* ri = rw + i * 16;
+            const float* rj = rw + j * 16;
+            const float3 dr = f3(ri[0] - rj[0], ri[1] - rj[1], ri[2] - rj[2]);
+            const float3 du = f3(ri[3] - rj[3], ri[4] - rj[4], ri[5] - rj[5]);
+            const float L = adj_len[k];
+            float* e = E + ((size_t)b * edges + k) * 8;
+            e[0] = dr.x / sc.er; e[1] = dr.y / sc.er; e[2] = dr.z / sc.er;
+            e[3] = (len3(dr) - L) / sc.el;
+            e[4] = du.x / sc.eu; e[5] = du.y / sc.eu; e[6] = du.z / sc.eu;
+            e[7] = L / sc.er;
+        }
+}
+
+// The prediction of cells [first, first + cells): decode the network's
+// outputs into x_K, v_K, F_K and check the residual of the trapezoid rule
+// over the span T, |x_K - x1 - T/2 (v1 + v_K)|, against the tolerance.  A
+// cell that passes takes the prediction (and then the vein-end rule and its
+// grid keys), and is skipped by k_substeps; a cell that fails falls back to
+// the plain sub-steps.
+__global__ void k_sur_apply(const StepArgs a, const SurDev d, const float* __restrict__ Y, const SurScales sc,
+                            int first, int cells) {
+    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (b >= cells) return;
+    const int sc_i = first + b;
+    const TypeDev ty = a.types[d.cell_type[sc_i]];
+    const SceneDev& scn = a.scenes[ty.scene];
+    const int pic = ty.pic, cell = d.cell_index[sc_i], p0 = ty.particle_start + cell * pic;
+    const float T = d.T;
+    float worst = 0.f;
+    bool finite = true;
+    float3 px[6], pv[6], pF[6];   // pic <= 192 particles per cell here (6 per lane)
+    int nk = 0;
+    for (int k = lane; k < pic && nk < 6; k += 32, ++nk) {
+        const float* y = Y + ((size_t)b * d.pic + k) * 9;
+        float t[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) t[q] = y[q] * sc.ts[q] + sc.tm[q];
+        const float4* st = d.start + ((size_t)sc_i * d.pic + k) * 3;
+        const float3 x1 = xyz(st[0]), v1 = xyz(st[1]), F1 = xyz(st[2]);
+        const float3 vK = v1 + T * F1 + f3(t[3], t[4], t[5]);
+        const float3 xK = x1 + T * v1 + (0.5f * T * T) * F1 + f3(t[0], t[1], t[2]);
+        const float3 FK = F1 + f3(t[6], t[7], t[8]);
+        const float3 res = xK - x1 - (0.5f * T) * (v1 + vK);
+        worst = fmaxf(worst, len3(res));
+        finite = finite && isfinite(xK.x) && isfinite(xK.y) && isfinite(xK.z) && isfinite(vK.x) &&
+                 isfinite(vK.y) && isfinite(vK.z) && isfinite(FK.x) && isfinite(FK.y) && isfinite(FK.z);
+        px[nk] = xK;
+        pv[nk] = vK;
+        pF[nk] = FK;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+    const bool ok = __all_sync(0xffffffffu, finite) && worst <= d.tolerance && pic <= 6 * 32;
+    if (lane == 0) {
+        d.skip[ty.cell_global + cell] = ok ? 1 : 0;
+        atomicAdd(&d.counts[ok ? 0 : 1], 1ull);
+    }
+    if (!ok) return;
+    // vein-end rule on the predicted state, keyed by the last sub-step
+    bool leave = false;
+    nk = 0;
+    for (int k = lane; k < pic; k += 32, ++nk) leave = leave || leaves_vein(scn, px[nk]);
+    leave = a.p.use_blood_flow && __any_sync(0xffffffffu, leave);
+    const long long step = *a.steps + (d.K - 1);
+    unsigned e = 0;
+    nk = 0;
+    for (int k = lane; k < pic; k += 32, ++nk) {
+        float3 x = px[nk], v = pv[nk];
+        if (leave) respawn(a, scn, ty.cell_start + cell, step, ty.model_start + k, x, v);
+        const int p = p0 + k;
+        const float w = a.pos_out[p].w;
+        a.pos_out[p] = make_float4(x.x, x.y, x.z, w);
+        a.vel_out[p] = make_float4(v.x, v.y, v.z, 0.f);
+        a.frc_out[p] = make_float4(pF[nk].x, pF[nk].y, pF[nk].z, 0.f);
+        if (a.keys_out) {
+            a.keys_out[p] = a.pg.uniform ? grid_key(scn.pg, x, e) : 0;
+            a.ids_out[p] = p;
+        }
+    }
+    if (e) atomicOr(a.err, e);
+}
+
+// Position error after the span of the network's prediction and of the
+// constant-force extrapolation it corrects (whose residual is the raw
+// target), summed over the valid samples' particles: sums[0] += |dx_pred -
+// dx|, sums[1] += |dx|, sums[2] += particles.
+__global__ void k_sur_eval(const float* __restrict__ Y, const float* __restrict__ raw_t,
+                           const unsigned char* __restrict__ valid, const SurScales sc, int first, int cells, int pic,
+                           double* sums) {
+    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (b >= cells || !valid[first + b]) return;
+    double en = 0.0, eb = 0.0;
+    for (int k = lane; k < pic; k += 32) {
+        const float* y = Y + ((size_t)b * pic + k) * 9;
+        const float* t = raw_t + ((size_t)(first + b) * pic + k) * 9;
+        float d2 = 0.f, b2 = 0.f;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float pred = y[q] * sc.ts[q] + sc.tm[q];
+            d2 += (pred - t[q]) * (pred - t[q]);
+            b2 += t[q] * t[q];
+        }
+        en += sqrtf(d2);
+        eb += sqrtf(b2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        en += __shfl_xor_sync(0xffffffffu, en, o);
+        eb += __shfl_xor_sync(0xffffffffu, eb, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&sums[0], en);
+        atomicAdd(&sums[1], eb);
+        atomicAdd(&sums[2], (double)pic);
+    }
 }
 
 __global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch,
@@ -1026,6 +1268,27 @@ void launch_tri_cache(const int* ids, const uint32_t* tri, const float4* vpos, i
     if (T > 0) k_tri_cache<<<BCS_GRID1(T, 256), 0, s>>>(ids, tri, vpos, T, cache);
 }
 void launch_bump_step(long long* steps, int by, cudaStream_t s) { k_bump_step<<<1, 1, 0, s>>>(steps, by); }
+void launch_sur_features(const StepArgs& a, const SurDev& d, cudaStream_t s) {
+    if (d.cells > 0) k_sur_features<<<(d.cells * 32 + 255) / 256, 256, 0, s>>>(a, d);
+}
+void launch_sur_targets(const StepArgs& a, const SurDev& d, float* raw_t, unsigned char* valid, cudaStream_t s) {
+    if (d.cells > 0) k_sur_targets<<<(d.cells * 32 + 255) / 256, 256, 0, s>>>(a, d, raw_t, valid);
+}
+void launch_sur_inputs(const float* raw, const float* raw_t, const int* list, int nvalid, unsigned long long seed,
+                       int first, int cells, int pic, const int* adj_off, const int* adj_nbr, const float* adj_len,
+                       const SurScales& sc, float* f, float* E, float* T, cudaStream_t s) {
+    if (cells > 0)
+        k_sur_inputs<<<cells, 128, 0, s>>>(raw, raw_t, list, nvalid, seed, first, cells, pic, adj_off, adj_nbr,
+                                           adj_len, sc, f, E, T);
+}
+void launch_sur_apply(const StepArgs& a, const SurDev& d, const float* Y, const SurScales& sc, int first, int cells,
+                      cudaStream_t s) {
+    if (cells > 0) k_sur_apply<<<(cells * 32 + 255) / 256, 256, 0, s>>>(a, d, Y, sc, first, cells);
+}
+void launch_sur_eval(const float* Y, const float* raw_t, const unsigned char* valid, const SurScales& sc, int first,
+                     int cells, int pic, double* sums, cudaStream_t s) {
+    if (cells > 0) k_sur_eval<<<(cells * 32 + 255) / 256, 256, 0, s>>>(Y, raw_t, valid, sc, first, cells, pic, sums);
+}
 void launch_substeps(const StepArgs& a, int items, int K, cudaStream_t s) {
     if (items > 0 && K > 1) k_substeps<<<items, kSubstepThreads, 0, s>>>(a, K);
 }

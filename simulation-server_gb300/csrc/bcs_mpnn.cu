@@ -1,0 +1,670 @@
+// bcs_mpnn.cu — kernels of the learned sub-step network (forward, backward,
+// optimiser).  The hidden x hidden products use mma.sync m16n8k16 bf16 tensor
+// core instructions with FP32 accumulation; messages, encoder, decoder and
+// the optimiser are FP32 SIMT kernels.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+#include <vector>
+
+#include "bcs_internal.cuh"
+#include "bcs_mpnn.cuh"
+
+namespace bcs {
+
+namespace {
+
+constexpr int kTileRows = 128;            // rows (nodes) per GEMM CTA
+constexpr int kPad = kHidden + 8;         // smem row stride (bf16): conflict-free fragment loads
+constexpr int kGemmSmem = 2 * kTileRows * kPad * (int)sizeof(__nv_bfloat16);
+
+__device__ inline float silu_f(float x) { return x / (1.0f + __expf(-x)); }
+__device__ inline float dsilu_f(float x) {
+    const float s = 1.0f / (1.0f + __expf(-x));
+    return s * (1.0f + x * (1.0f - s));
+}
+
+__device__ inline void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ inline uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// Rows [r0, r0 + 128) of an FP32 [rows][128] matrix into bf16 smem (zero past `rows`).
+__device__ inline void stage_rows(const float* __restrict__ X, int r0, int rows, __nv_bfloat16* As) {
+    for (int q = threadIdx.x; q < kTileRows * (kHidden / 4); q += blockDim.x) {
+        const int r = q / (kHidden / 4), c = (q % (kHidden / 4)) * 4;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (r0 + r < rows) v = *reinterpret_cast<const float4*>(X + (size_t)(r0 + r) * kHidden + c);
+        __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+        *reinterpret_cast<__nv_bfloat162*>(As + r * kPad + c) = lo;
+        *reinterpret_cast<__nv_bfloat162*>(As + r * kPad + c + 2) = hi;
+    }
+}
+
+// A bf16 [128][128] matrix (row n holds the k-contiguous operand column) into smem.
+__device__ inline void stage_b(const __nv_bfloat16* __restrict__ W, __nv_bfloat16* Bs) {
+    for (int q = threadIdx.x; q < kHidden * (kHidden / 8); q += blockDim.x) {
+        const int n = q / (kHidden / 8), k = (q % (kHidden / 8)) * 8;
+        *reinterpret_cast<uint4*>(Bs + n * kPad + k) = *reinterpret_cast<const uint4*>(W + n * kHidden + k);
+    }
+}
+
+// acc (16 rows x 128 cols of this warp) += As[warp rows] x Bs^T.
+__device__ inline void warp_mma_128(const __nv_bfloat16* As, const __nv_bfloat16* Bs, float (&acc)[16][4]) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const __nv_bfloat16* a_lo = As + (warp * 16 + g) * kPad + 2 * t;
+    const __nv_bfloat16* a_hi = a_lo + 8 * kPad;
+#pragma unroll
+    for (int ks = 0; ks < kHidden / 16; ++ks) {
+        const int k0 = ks * 16;
+        const uint32_t a0 = ld32(a_lo + k0), a1 = ld32(a_hi + k0), a2 = ld32(a_lo + k0 + 8), a3 = ld32(a_hi + k0 + 8);
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) {
+            const __nv_bfloat16* b = Bs + (nt * 8 + g) * kPad + k0 + 2 * t;
+            mma_bf16(acc[nt], a0, a1, a2, a3, ld32(b), ld32(b + 8));
+        }
+    }
+}
+
+// Y = epi(X1 B1 + X2 B2 + bias), B given as [n][k] bf16 (the transposed weight).
+__global__ void __launch_bounds__(256) k_gemm(const float* __restrict__ X1, const __nv_bfloat16* __restrict__ B1,
+                                              const float* __restrict__ X2, const __nv_bfloat16* __restrict__ B2,
+                                              const float* __restrict__ bias, float* Y, float* Z, int rows, int silu,
+                                              int accumulate) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+    __nv_bfloat16* Bs = As + kTileRows * kPad;
+    const int r0 = blockIdx.x * kTileRows;
+    float acc[16][4];
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+    for (int in = 0; in < 2; ++in) {
+        const float* X = in ? X2 : X1;
+        const __nv_bfloat16* B = in ? B2 : B1;
+        if (!X) break;
+        if (in) __syncthreads();
+        stage_rows(X, r0, rows, As);
+        stage_b(B, Bs);
+        __syncthreads();
+        warp_mma_128(As, Bs, acc);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) {
+        const int col = nt * 8 + 2 * t;
+        const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = r0 + warp * 16 + g + 8 * h;
+            if (r >= rows) continue;
+            float v0 = acc[nt][2 * h] + b0, v1 = acc[nt][2 * h + 1] + b1;
+            float* yp = Y + (size_t)r * kHidden + col;
+            if (Z) *reinterpret_cast<float2*>(Z + (size_t)r * kHidden + col) = make_float2(v0, v1);
+            if (silu) {
+                v0 = silu_f(v0);
+                v1 = silu_f(v1);
+            }
+            if (accumulate) {
+                const float2 o = *reinterpret_cast<const float2*>(yp);
+                v0 += o.x;
+                v1 += o.y;
+            }
+            *reinterpret_cast<float2*>(yp) = make_float2(v0, v1);
+        }
+    }
+}
+
+// dW[k][n] += sum_r X[r][k] dY[r][n], operands rounded to bf16.  A CTA takes
+// `chunk` rows in tiles of 64 and adds its 128 x 128 partial into dW.
+constexpr int kWgRows = 64;
+constexpr int kWgPad = kWgRows + 8;
+__global__ void __launch_bounds__(256) k_wgrad(const float* __restrict__ X, const float* __restrict__ dY, float* dW,
+                                               int rows, int chunk) {
+    __shared__ __align__(16) __nv_bfloat16 Xt[kHidden * kWgPad];   // [k][r]
+    __shared__ __align__(16) __nv_bfloat16 Yt[kHidden * kWgPad];   // [n][r]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float acc[16][4];
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+    const int rbeg = blockIdx.x * chunk, rend = min(rows, rbeg + chunk);
+    for (int r0 = rbeg; r0 < rend; r0 += kWgRows) {
+        for (int q = threadIdx.x; q < kWgRows * (kHidden / 4); q += blockDim.x) {
+            const int r = q / (kHidden / 4), c = (q % (kHidden / 4)) * 4;
+            float4 x = make_float4(0.f, 0.f, 0.f, 0.f), y = x;
+            if (r0 + r < rend) {
+                x = *reinterpret_cast<const float4*>(X + (size_t)(r0 + r) * kHidden + c);
+                y = *reinterpret_cast<const float4*>(dY + (size_t)(r0 + r) * kHidden + c);
+            }
+            Xt[(c + 0) * kWgPad + r] = __float2bfloat16_rn(x.x);
+            Xt[(c + 1) * kWgPad + r] = __float2bfloat16_rn(x.y);
+            Xt[(c + 2) * kWgPad + r] = __float2bfloat16_rn(x.z);
+            Xt[(c + 3) * kWgPad + r] = __float2bfloat16_rn(x.w);
+            Yt[(c + 0) * kWgPad + r] = __float2bfloat16_rn(y.x);
+            Yt[(c + 1) * kWgPad + r] = __float2bfloat16_rn(y.y);
+            Yt[(c + 2) * kWgPad + r] = __float2bfloat16_rn(y.z);
+            Yt[(c + 3) * kWgPad + r] = __float2bfloat16_rn(y.w);
+        }
+        __syncthreads();
+        const __nv_bfloat16* a_lo = Xt + (warp * 16 + g) * kWgPad + 2 * t;
+        const __nv_bfloat16* a_hi = a_lo + 8 * kWgPad;
+#pragma unroll
+        for (int ks = 0; ks < kWgRows / 16; ++ks) {
+            const int k0 = ks * 16;
+            const uint32_t a0 = ld32(a_lo + k0), a1 = ld32(a_hi + k0), a2 = ld32(a_lo + k0 + 8),
+                           a3 = ld32(a_hi + k0 + 8);
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt) {
+                const __nv_bfloat16* b = Yt + (nt * 8 + g) * kWgPad + k0 + 2 * t;
+                mma_bf16(acc[nt], a0, a1, a2, a3, ld32(b), ld32(b + 8));
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) {
+        const int col = nt * 8 + 2 * t, row = warp * 16 + g;
+        atomicAdd(&dW[row * kHidden + col], acc[nt][0]);
+        atomicAdd(&dW[row * kHidden + col + 1], acc[nt][1]);
+        atomicAdd(&dW[(row + 8) * kHidden + col], acc[nt][2]);
+        atomicAdd(&dW[(row + 8) * kHidden + col + 1], acc[nt][3]);
+    }
+}
+
+// ------------------------------------------------------------ SIMT -------
+__device__ inline float wv(const __nv_bfloat16* w, int i) { return __bfloat162float(w[i]); }
+
+// h = silu(Z), Z = f W_in + b_in: one warp per node, lane -> 4 columns.
+__global__ void k_encode(const float* __restrict__ f, const __nv_bfloat16* __restrict__ W, const float* __restrict__ b,
+                         float* Z, float* H, int n) {
+    const int node = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (node >= n) return;
+    float fr[kFeatIn];
+#pragma unroll
+    for (int q = 0; q < kFeatIn; ++q) fr[q] = f[(size_t)node * kFeatIn + q];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int c = lane * 4 + j;
+        float z = b[c];
+#pragma unroll
+        for (int q = 0; q < kFeatIn; ++q) z = fmaf(fr[q], wv(W, q * kHidden + c), z);
+        Z[(size_t)node * kHidden + c] = z;
+        H[(size_t)node * kHidden + c] = silu_f(z);
+    }
+}
+
+// dZ = dH silu'(Z); dW_in += f^T dZ, db_in += sum dZ (block partials in
+// shared memory, one atomic per weight per block).
+__global__ void __launch_bounds__(256) k_encode_bwd(const float* __restrict__ f, const float* __restrict__ Z,
+                                                    const float* __restrict__ dH, float* gW, float* gb, int n) {
+    __shared__ float sW[kFeatIn * kHidden];
+    __shared__ float sb[kHidden];
+    for (int i = threadIdx.x; i < kFeatIn * kHidden; i += blockDim.x) sW[i] = 0.f;
+    for (int i = threadIdx.x; i < kHidden; i += blockDim.x) sb[i] = 0.f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    float aw[kFeatIn][4] = {};
+    float ab[4] = {};
+    for (int node = blockIdx.x * wpb + (threadIdx.x >> 5); node < n; node += gridDim.x * wpb) {
+        float fr[kFeatIn];
+#pragma unroll
+        for (int q = 0; q < kFeatIn; ++q) fr[q] = f[(size_t)node * kFeatIn + q];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const size_t o = (size_t)node * kHidden + lane * 4 + j;
+            const float dz = dH[o] * dsilu_f(Z[o]);
+            ab[j] += dz;
+#pragma unroll
+            for (int q = 0; q < kFeatIn; ++q) aw[q][j] = fmaf(fr[q], dz, aw[q][j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        atomicAdd(&sb[lane * 4 + j], ab[j]);
+#pragma unroll
+        for (int q = 0; q < kFeatIn; ++q) atomicAdd(&sW[q * kHidden + lane * 4 + j], aw[q][j]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kFeatIn * kHidden; i += blockDim.x) atomicAdd(&gW[i], sW[i]);
+    for (int i = threadIdx.x; i < kHidden; i += blockDim.x) atomicAdd(&gb[i], sb[i]);
+}
+
+// M_i = mean over edges (i <- j) of silu(A_i + B_j + e_ij W_e + b_e): one
+// warp per node, lane -> 4 columns.
+__global__ void k_message(const float* __restrict__ A, const float* __restrict__ B, const float* __restrict__ E,
+                          const __nv_bfloat16* __restrict__ We, const float* __restrict__ be, MpnnGraph g,
+                          const int* __restrict__ edge_base, float* M, int n) {
+    const int node = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (node >= n) return;
+    const int cell = node / g.pic, li = node - cell * g.pic, cb = cell * g.pic;
+    const int e0 = g.adj_off[li], e1 = g.adj_off[li + 1];
+    const int ebase = edge_base[cell];
+    float a[4], w[kEdgeIn][4], bb[4], m[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int c = lane * 4 + j;
+        a[j] = A[(size_t)node * kHidden + c];
+        bb[j] = be[c];
+#pragma unroll
+        for (int q = 0; q < kEdgeIn; ++q) w[q][j] = wv(We, q * kHidden + c);
+    }
+    for (int k = e0; k < e1; ++k) {
+        const int nb = cb + g.adj_nbr[k];
+        const float* e = E + (size_t)(ebase + k) * kEdgeIn;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float p = a[j] + B[(size_t)nb * kHidden + lane * 4 + j] + bb[j];
+#pragma unroll
+            for (int q = 0; q < kEdgeIn; ++q) p = fmaf(e[q], w[q][j], p);
+            m[j] += silu_f(p);
+        }
+    }
+    const float inv = 1.0f / (float)max(1, e1 - e0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) M[(size_t)node * kHidden + lane * 4 + j] = m[j] * inv;
+}
+
+// Backward of k_message for node i: its own edges (i <- j) give dA_i and the
+// W_e / b_e gradients; the reverse edges (j <- i) give dB_i.  rev[k] is the
+// index of edge k's reverse within the cell.
+__global__ void __launch_bounds__(256) k_message_bwd(const float* __restrict__ A, const float* __restrict__ B,
+                                                     const float* __restrict__ E, const __nv_bfloat16* __restrict__ We,
+                                                     const float* __restrict__ be, MpnnGraph g,
+                                                     const int* __restrict__ edge_base, const int* __restrict__ rev,
+                                                     const float* __restrict__ dM, float* dA, float* dB, float* gWe,
+                                                     float* gbe, int n) {
+    __shared__ float sW[kEdgeIn * kHidden];
+    __shared__ float sb[kHidden];
+    for (int i = threadIdx.x; i < kEdgeIn * kHidden; i += blockDim.x) sW[i] = 0.f;
+    for (int i = threadIdx.x; i < kHidden; i += blockDim.x) sb[i] = 0.f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    float w[kEdgeIn][4], bb[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        bb[j] = be[lane * 4 + j];
+#pragma unroll
+        for (int q = 0; q < kEdgeIn; ++q) w[q][j] = wv(We, q * kHidden + lane * 4 + j);
+    }
+    float aw[kEdgeIn][4] = {};
+    float ab[4] = {};
+    for (int node = blockIdx.x * wpb + (threadIdx.x >> 5); node < n; node += gridDim.x * wpb) {
+        const int cell = node / g.pic, li = node - cell * g.pic, cb = cell * g.pic;
+        const int e0 = g.adj_off[li], e1 = g.adj_off[li + 1];
+        const int ebase = edge_base[cell];
+        float ai[4], bi[4], dmi[4], da[4] = {0.f, 0.f, 0.f, 0.f}, db[4] = {0.f, 0.f, 0.f, 0.f};
+        const float inv_i = 1.0f / (float)max(1, e1 - e0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const size_t o = (size_t)node * kHidden + lane * 4 + j;
+            ai[j] = A[o];
+            bi[j] = B[o];
+            dmi[j] = dM[o] * inv_i;
+        }
+        for (int k = e0; k < e1; ++k) {
+            const int lj = g.adj_nbr[k], nb = cb + lj;
+            const float* e = E + (size_t)(ebase + k) * kEdgeIn;
+            const int r = rev[k];
+            const float* er = E + (size_t)(ebase + r) * kEdgeIn;
+            const float inv_j = 1.0f / (float)max(1, g.adj_off[lj + 1] - g.adj_off[lj]);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const size_t oj = (size_t)nb * kHidden + lane * 4 + j;
+                // edge k: i <- j
+                float p = ai[j] + B[oj] + bb[j];
+#pragma unroll
+                for (int q = 0; q < kEdgeIn; ++q) p = fmaf(e[q], w[q][j], p);
+                const float dp = dmi[j] * dsilu_f(p);
+                da[j] += dp;
+                ab[j] += dp;
+#pragma unroll
+                for (int q = 0; q < kEdgeIn; ++q) aw[q][j] = fmaf(e[q], dp, aw[q][j]);
+                // edge r: j <- i
+                float pr = A[oj] + bi[j] + bb[j];
+#pragma unroll
+                for (int q = 0; q < kEdgeIn; ++q) pr = fmaf(er[q], w[q][j], pr);
+                db[j] += dM[oj] * inv_j * dsilu_f(pr);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const size_t o = (size_t)node * kHidden + lane * 4 + j;
+            dA[o] = da[j];
+            dB[o] = db[j];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        atomicAdd(&sb[lane * 4 + j], ab[j]);
+#pragma unroll
+        for (int q = 0; q < kEdgeIn; ++q) atomicAdd(&sW[q * kHidden + lane * 4 + j], aw[q][j]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kEdgeIn * kHidden; i += blockDim.x) atomicAdd(&gWe[i], sW[i]);
+    for (int i = threadIdx.x; i < kHidden; i += blockDim.x) atomicAdd(&gbe[i], sb[i]);
+}
+
+// y = h W_out + b_out: one warp per node, lane -> 4 inputs, warp sums.
+__global__ void k_decode(const float* __restrict__ H, const __nv_bfloat16* __restrict__ W, const float* __restrict__ b,
+                         float* Y, int n) {
+    const int node = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (node >= n) return;
+    float acc[kOut] = {};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int c = lane * 4 + j;
+        const float h = H[(size_t)node * kHidden + c];
+#pragma unroll
+        for (int o = 0; o < kOut; ++o) acc[o] = fmaf(h, wv(W, c * kOut + o), acc[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < kOut; ++o) {
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) acc[o] += __shfl_xor_sync(0xffffffffu, acc[o], s);
+    }
+    if (lane < kOut) {
+        float v = acc[0];
+#pragma unroll
+        for (int o = 1; o < kOut; ++o)
+            if (lane == o) v = acc[o];
+        Y[(size_t)node * kOut + lane] = v + b[lane];
+    }
+}
+
+// Loss mean((y - t)^2) and dY = 2 (y - t) / count; loss summed into *loss.
+__global__ void k_loss(const float* __restrict__ Y, const float* __restrict__ T, float* dY, float* loss, int count) {
+    float acc = 0.f;
+    const float sc = 2.0f / (float)count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const float d = Y[i] - T[i];
+        dY[i] = sc * d;
+        acc += d * d;
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc / (float)count);
+}
+
+// dH = dY W_out^T (+= when accumulate); gW_out += h^T dY; gb_out += sum dY.
+__global__ void __launch_bounds__(256) k_decode_bwd(const float* __restrict__ H, const __nv_bfloat16* __restrict__ W,
+                                                    const float* __restrict__ dY, float* dH, float* gW, float* gb, int n) {
+    __shared__ float sW[kHidden * kOut];
+    __shared__ float sb[kOut];
+    for (int i = threadIdx.x; i < kHidden * kOut; i += blockDim.x) sW[i] = 0.f;
+    if (threadIdx.x < kOut) sb[threadIdx.x] = 0.f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    float aw[4][kOut] = {};
+    float ab = 0.f;
+    for (int node = blockIdx.x * wpb + (threadIdx.x >> 5); node < n; node += gridDim.x * wpb) {
+        float dy[kOut];
+#pragma unroll
+        for (int o = 0; o < kOut; ++o) dy[o] = dY[(size_t)node * kOut + o];
+        if (lane < kOut) ab += dy[lane];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = lane * 4 + j;
+            const float h = H[(size_t)node * kHidden + c];
+            float d = 0.f;
+#pragma unroll
+            for (int o = 0; o < kOut; ++o) {
+                d = fmaf(dy[o], wv(W, c * kOut + o), d);
+                aw[j][o] = fmaf(h, dy[o], aw[j][o]);
+            }
+            dH[(size_t)node * kHidden + c] = d;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int o = 0; o < kOut; ++o) atomicAdd(&sW[(lane * 4 + j) * kOut + o], aw[j][o]);
+    if (lane < kOut) atomicAdd(&sb[lane], ab);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kHidden * kOut; i += blockDim.x) atomicAdd(&gW[i], sW[i]);
+    if (threadIdx.x < kOut) atomicAdd(&gb[threadIdx.x], sb[threadIdx.x]);
+}
+
+// dZ = dH silu'(Z) (elementwise), written over dZ.
+__global__ void k_dsilu(const float* __restrict__ dH, const float* __restrict__ Z, float* dZ, long long count) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+        dZ[i] = dH[i] * dsilu_f(Z[i]);
+}
+
+// sum over rows of X [rows][128] into g[128].
+__global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ X, float* g, int rows) {
+    __shared__ float sb[kHidden];
+    if (threadIdx.x < kHidden) sb[threadIdx.x] = 0.f;
+    __syncthreads();
+    const int c = threadIdx.x & (kHidden - 1);
+    float acc = 0.f;
+    for (int r = blockIdx.x * 2 + (threadIdx.x >> 7); r < rows; r += gridDim.x * 2) acc += X[(size_t)r * kHidden + c];
+    atomicAdd(&sb[c], acc);
+    __syncthreads();
+    if (threadIdx.x < kHidden) atomicAdd(&g[threadIdx.x], sb[threadIdx.x]);
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master copy; c1, c2 are the bias
+// corrections 1 / (1 - b^t).
+__global__ void k_adam(float* p, const float* __restrict__ g, float* m, float* v, long long count, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    }
+}
+
+// bf16 copies of the parameters; the transposed copy for the square blocks
+// listed in `blocks` (offsets of hidden x hidden matrices).
+__global__ void k_bf16_copies(const float* __restrict__ p, __nv_bfloat16* pb, __nv_bfloat16* pbt,
+                              const long long* __restrict__ blocks, int nblocks, long long count) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+        pb[i] = __float2bfloat16_rn(p[i]);
+    const long long sq = (long long)kHidden * kHidden;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nblocks * sq;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long b = i / sq, e = i - b * sq;
+        const int r = (int)(e / kHidden), c = (int)(e % kHidden);
+        pbt[blocks[b] + (long long)c * kHidden + r] = __float2bfloat16_rn(p[blocks[b] + e]);
+    }
+}
+
+}  // namespace
+
+void mpnn_gemm(const float* X1, const __nv_bfloat16* W1t, const float* X2, const __nv_bfloat16* W2t,
+               const float* bias, float* Y, float* Zout, int rows, bool silu, bool accumulate, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+        attr = true;
+    }
+    if (rows <= 0) return;
+    k_gemm<<<(rows + kTileRows - 1) / kTileRows, 256, kGemmSmem, s>>>(X1, W1t, X2, W2t, bias, Y, Zout, rows,
+                                                                     silu ? 1 : 0, accumulate ? 1 : 0);
+}
+
+void mpnn_gemm_t(const float* dY, const __nv_bfloat16* W, float* dX, int rows, bool accumulate, cudaStream_t s) {
+    // dX = dY W^T: the B operand in [n][k] form is W itself (row-major [in][out]).
+    mpnn_gemm(dY, W, nullptr, nullptr, nullptr, dX, nullptr, rows, false, accumulate, s);
+}
+
+void mpnn_wgrad(const float* X, const float* dY, float* dW, int rows, cudaStream_t s) {
+    if (rows <= 0) return;
+    const int chunk = 1024;
+    k_wgrad<<<(rows + chunk - 1) / chunk, 256, 0, s>>>(X, dY, dW, rows, chunk);
+}
+
+// ------------------------------------------------------------ MpnnNet ----
+namespace {
+int grid_for(long long n, int threads, int cap = 4096) {
+    return (int)std::max(1LL, std::min<long long>(cap, (n + threads - 1) / threads));
+}
+// SplitMix64 for the initial weights (Steele, Lea, Flood, OOPSLA 2014).
+unsigned long long splitmix(unsigned long long& x) {
+    unsigned long long z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+}  // namespace
+
+MpnnNet::~MpnnNet() {
+    for (void* p : allocs_) cudaFree(p);
+}
+
+float* MpnnNet::alloc(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(float)) != cudaSuccess) return nullptr;
+    allocs_.push_back(p);
+    bytes_ += n * sizeof(float);
+    return static_cast<float*>(p);
+}
+
+int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, const float* adj_len, int max_cells,
+                  unsigned long long seed, cudaStream_t stream) {
+    st_ = stream;
+    L_ = mpnn_layout(layers);
+    pic_ = pic;
+    edges_ = adj_off[pic];
+    max_cells_ = max_cells;
+    // reverse edge of every edge of the cell graph (the spring graph is symmetric)
+    std::vector<int> rev(edges_, -1), base(max_cells);
+    for (int i = 0; i < pic; ++i)
+        for (int k = adj_off[i]; k < adj_off[i + 1]; ++k) {
+            const int j = adj_nbr[k];
+            for (int q = adj_off[j]; q < adj_off[j + 1]; ++q)
+                if (adj_nbr[q] == i) rev[k] = q;
+            if (rev[k] < 0) return (int)cudaErrorInvalidValue;
+        }
+    for (int c = 0; c < max_cells; ++c) base[c] = c * edges_;
+    auto up = [&](auto** dst, const auto* src, size_t n) {
+        *dst = reinterpret_cast<std::remove_pointer_t<decltype(dst)>>(alloc((n * sizeof(**dst) + 3) / 4));
+        return *dst && cudaMemcpy(*dst, src, n * sizeof(**dst), cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    if (!up(&adj_off_, adj_off, pic + 1) || !up(&adj_nbr_, adj_nbr, edges_) || !up(&adj_len_, adj_len, edges_) ||
+        !up(&rev_, rev.data(), edges_) || !up(&edge_base_, base.data(), max_cells))
+        return (int)cudaErrorMemoryAllocation;
+    const long long P = L_.total;
+    p_ = alloc(P); g_ = alloc(P); m_ = alloc(P); v_ = alloc(P);
+    pb_ = reinterpret_cast<__nv_bfloat16*>(alloc((P + 1) / 2));
+    pbt_ = reinterpret_cast<__nv_bfloat16*>(alloc((P + 1) / 2));
+    std::vector<long long> sq;
+    for (int l = 0; l < layers; ++l) {
+        sq.push_back(L_.wa[l]); sq.push_back(L_.wb[l]); sq.push_back(L_.wu[l]); sq.push_back(L_.wv[l]);
+    }
+    nsq_ = (int)sq.size();
+    sq_ = reinterpret_cast<long long*>(alloc(2 * sq.size()));
+    if (!p_ || !g_ || !m_ || !v_ || !pb_ || !pbt_ || !sq_) return (int)cudaErrorMemoryAllocation;
+    cudaMemcpy(sq_, sq.data(), sizeof(long long) * sq.size(), cudaMemcpyHostToDevice);
+    // weights uniform in +-1/sqrt(fan_in), biases 0
+    std::vector<float> h(P, 0.f);
+    unsigned long long x = seed;
+    auto fill = [&](long long off, int fan_in, long long n) {
+        const double lim = 1.0 / std::sqrt((double)fan_in);
+        for (long long i = 0; i < n; ++i) {
+            const double u = (double)(splitmix(x) >> 11) * (1.0 / 9007199254740992.0);
+            h[off + i] = (float)((2.0 * u - 1.0) * lim);
+        }
+    };
+    fill(L_.w_in, kFeatIn, (long long)kFeatIn * kHidden);
+    for (int l = 0; l < layers; ++l) {
+        fill(L_.wa[l], kHidden, (long long)kHidden * kHidden);
+        fill(L_.wb[l], kHidden, (long long)kHidden * kHidden);
+        fill(L_.we[l], kEdgeIn, (long long)kEdgeIn * kHidden);
+        fill(L_.wu[l], kHidden, (long long)kHidden * kHidden);
+        fill(L_.wv[l], kHidden, (long long)kHidden * kHidden);
+    }
+    fill(L_.w_out, kHidden, (long long)kHidden * kOut);
+    cudaMemcpy(p_, h.data(), sizeof(float) * P, cudaMemcpyHostToDevice);
+    cudaMemset(m_, 0, sizeof(float) * P);
+    cudaMemset(v_, 0, sizeof(float) * P);
+    // activations
+    const size_t n = (size_t)max_cells * pic, H = kHidden;
+    f_ = alloc(n * kFeatIn); e_ = alloc((size_t)max_cells * edges_ * kEdgeIn); t_ = alloc(n * kOut);
+    y_ = alloc(n * kOut); dy_ = alloc(n * kOut); loss_ = alloc(1);
+    z0_ = alloc(n * H); dh_ = alloc(n * H); da_ = alloc(n * H); db_ = alloc(n * H); dm_ = alloc(n * H);
+    dz_ = alloc(n * H);
+    for (int l = 0; l <= layers; ++l) h_[l] = alloc(n * H);
+    for (int l = 0; l < layers; ++l) {
+        a_[l] = alloc(n * H); b_[l] = alloc(n * H); mm_[l] = alloc(n * H); zu_[l] = alloc(n * H);
+    }
+    if (!f_ || !e_ || !t_ || !y_ || !dy_ || !loss_ || !z0_ || !dh_ || !da_ || !db_ || !dm_ || !dz_ ||
+        !h_[layers] || !zu_[layers - 1])
+        return (int)cudaErrorMemoryAllocation;
+    refresh_bf16();
+    cudaStreamSynchronize(st_);
+    return (int)cudaGetLastError();
+}
+
+void MpnnNet::refresh_bf16() {
+    k_bf16_copies<<<grid_for(L_.total, 256), 256, 0, st_>>>(p_, pb_, pbt_, sq_, nsq_, L_.total);
+}
+
+void MpnnNet::forward(const float* f, const float* E, int cells, bool keep) {
+    const int n = cells * pic_;
+    const MpnnGraph g{cells, pic_, adj_off_, adj_nbr_, adj_len_};
+    const int wgrid = (n * 32 + 255) / 256;
+    last_f_ = f;
+    last_e_ = E;
+    k_encode<<<wgrid, 256, 0, st_>>>(f, pb_ + L_.w_in, p_ + L_.b_in, z0_, h_[0], n);
+    for (int l = 0; l < L_.layers; ++l) {
+        float* hin = keep ? h_[l] : h_[l & 1];
+        float* hout = keep ? h_[l + 1] : h_[(l + 1) & 1];
+        float* A = keep ? a_[l] : a_[0];
+        float* B = keep ? b_[l] : b_[0];
+        float* M = keep ? mm_[l] : mm_[0];
+        float* ZU = keep ? zu_[l] : zu_[0];
+        mpnn_gemm(hin, pbt_ + L_.wa[l], nullptr, nullptr, nullptr, A, nullptr, n, false, false, st_);
+        mpnn_gemm(hin, pbt_ + L_.wb[l], nullptr, nullptr, nullptr, B, nullptr, n, false, false, st_);
+        k_message<<<wgrid, 256, 0, st_>>>(A, B, E, pb_ + L_.we[l], p_ + L_.be[l], g, edge_base_, M, n);
+        cudaMemcpyAsync(hout, hin, sizeof(float) * (size_t)n * kHidden, cudaMemcpyDeviceToDevice, st_);
+        mpnn_gemm(hin, pbt_ + L_.wu[l], M, pbt_ + L_.wv[l], p_ + L_.bu[l], hout, ZU, n, true, true, st_);
+    }
+    float* hl = keep ? h_[L_.layers] : h_[L_.layers & 1];
+    k_decode<<<wgrid, 256, 0, st_>>>(hl, pb_ + L_.w_out, p_ + L_.b_out, y_, n);
+}
+
+void MpnnNet::backward(const float* T, int cells) {
+    const int n = cells * pic_;
+    const MpnnGraph g{cells, pic_, adj_off_, adj_nbr_, adj_len_};
+    const size_t nh = (size_t)n * kHidden;
+    cudaMemsetAsync(g_, 0, sizeof(float) * L_.total, st_);
+    cudaMemsetAsync(loss_, 0, sizeof(float), st_);
+    k_loss<<<grid_for((long long)n * kOut, 256, 1024), 256, 0, st_>>>(y_, T, dy_, loss_, n * kOut);
+    const int rgrid = grid_for((long long)n * 32, 256, 1216);
+    k_decode_bwd<<<rgrid, 256, 0, st_>>>(h_[L_.layers], pb_ + L_.w_out, dy_, dh_, g_ + L_.w_out, g_ + L_.b_out, n);
+    for (int l = L_.layers - 1; l >= 0; --l) {
+        k_dsilu<<<grid_for((long long)nh, 256), 256, 0, st_>>>(dh_, zu_[l], dz_, (long long)nh);
+        mpnn_wgrad(h_[l], dz_, g_ + L_.wu[l], n, st_);
+        mpnn_wgrad(mm_[l], dz_, g_ + L_.wv[l], n, st_);
+        k_colsum<<<grid_for(n, 2, 1216), 256, 0, st_>>>(dz_, g_ + L_.bu[l], n);
+        mpnn_gemm_t(dz_, pb_ + L_.wv[l], dm_, n, false, st_);
+        mpnn_gemm_t(dz_, pb_ + L_.wu[l], dh_, n, true, st_);
+        k_message_bwd<<<rgrid, 256, 0, st_>>>(a_[l], b_[l], last_e_, pb_ + L_.we[l], p_ + L_.be[l], g, edge_base_, rev_,
+                                            dm_, da_, db_, g_ + L_.we[l], g_ + L_.be[l], n);
+        mpnn_wgrad(h_[l], da_, g_ + L_.wa[l], n, st_);
+        mpnn_wgrad(h_[l], db_, g_ + L_.wb[l], n, st_);
+        mpnn_gemm_t(da_, pb_ + L_.wa[l], dh_, n, true, st_);
+        mpnn_gemm_t(db_, pb_ + L_.wb[l], dh_, n, true, st_);
+    }
+    k_encode_bwd<<<rgrid, 256, 0, st_>>>(last_f_, z0_, dh_, g_ + L_.w_in, g_ + L_.b_in, n);
+}
+
+void MpnnNet::adam(float lr) {
+    ++t_adam_;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f / (1.0f - std::pow(b1, (float)t_adam_)), c2 = 1.0f / (1.0f - std::pow(b2, (float)t_adam_));
+    k_adam<<<grid_for(L_.total, 256), 256, 0, st_>>>(p_, g_, m_, v_, L_.total, lr, b1, b2, 1e-8f, c1, c2);
+    refresh_bf16();
+}
+
+}  // namespace bcs

@@ -63,6 +63,7 @@ STRUCTS = {
     "bcs_vec3": bcs.Vec3, "bcs_cell_type": bcs.CellType, "bcs_vein": bcs.Vein,
     "bcs_flow_segment": bcs.FlowSegment, "bcs_params": bcs.Params, "bcs_scene_desc": bcs.SceneDesc,
     "bcs_info": bcs.Info, "bcs_scene_info": bcs.SceneInfo, "bcs_tuning": bcs.Tuning,
+    "bcs_surrogate_desc": bcs.SurrogateDesc, "bcs_surrogate_stats": bcs.SurrogateStats,
 }
 
 

@@ -212,6 +212,77 @@ def grid_diagnostics(sim):
             "error_word": sim.error_word()}
 
 
+def learned_substep(args, scene, tuning, bcs, fresh, warm):
+    """The learned sub-step path at the same workload.  The network (for the
+    162-vertex cells) is trained on plain macro steps of a scene built from
+    a fresh seed; then plain frames, plain macro steps (K sub-steps, the
+    collisions held) and macro steps with the network are timed from the
+    same state, and their positions compared with the plain frames' (the
+    judge).  Simulated-time throughput = particles x sub-steps / time."""
+    K, M = args.learned_substeps, args.learned_macro_steps
+    t0 = time.perf_counter()
+    train_scene = build_scene(args.cells_per_type, args.seed + 7919)
+    ts = bcs.Simulation(train_scene)
+    ts.set_particles(train_scene.positions, train_scene.velocities)
+    ts.set_tuning(**tuning)
+    ts.step(warm)
+    cells = train_scene.types[1].count
+    sur = bcs.Surrogate(ts, cell_type=1, substeps=K, max_samples=cells * (args.learned_collect + 1), seed=11)
+    sur.collect(args.learned_collect)
+    n_train = sur.stats()["samples"]
+    loss0 = sur.train(1, batch_cells=args.learned_batch, lr=1e-3)
+    loss = sur.train(args.learned_iters, batch_cells=args.learned_batch, lr=1e-3)
+    sur.collect(1)
+    net_err, base_err = sur.evaluate(n_train, sur.stats()["samples"] - n_train)
+    params, scales, st_train = sur.get_params(), sur.scales(), sur.stats()
+    sur.close()
+    ts.close()
+    train_s = time.perf_counter() - t0
+
+    sim = fresh(tuning)
+    n = sim.n
+    ms_plain = sim.time_steps(K * M)
+    pa = sim.get_particles()[0]
+    sim.close()
+    sim = fresh(tuning)
+    ms_macro = sim.time_macro_steps(K, M)
+    pb = sim.get_particles()[0]
+    sim.close()
+    sim = fresh(tuning)
+    s2 = bcs.Surrogate(sim, cell_type=1, substeps=K, max_samples=1, seed=11)
+    s2.set_params(params)
+    s2.set_scales(scales)
+    s2.enable(True)
+    ms_sur = sim.time_macro_steps(K, M)
+    pc = sim.get_particles()[0]
+    st = s2.stats()
+    s2.close()
+    sim.close()
+
+    def err(p):
+        d = np.linalg.norm(p.astype(np.float64) - pa, axis=1)
+        return {"median": float(np.median(d)), "p99": float(np.percentile(d, 99)), "max": float(d.max()),
+                "frac_above_1e-3_radius": float(np.mean(d > 1e-3 * 0.5))}
+
+    rate = lambda ms: n * K * M / (ms / 1e3)
+    return {
+        "substeps": K, "macro_steps": M, "simulated_time": K * M * float(scene.params.dt),
+        "plain": {"ms": ms_plain, "particle_steps_per_s": rate(ms_plain)},
+        "macro_plain": {"ms": ms_macro, "particle_steps_per_s": rate(ms_macro), "position_error": err(pb)},
+        "surrogate": {"ms": ms_sur, "particle_steps_per_s": rate(ms_sur), "position_error": err(pc),
+                      "cells_predicted": st["predicted_cells"], "cells_fallen_back": st["fallback_cells"],
+                      "tolerance": st["tolerance"]},
+        "speedup_vs_plain": {"macro_plain": ms_plain / ms_macro, "surrogate": ms_plain / ms_sur},
+        "network": {"cell_type": "biconcave-162", "layers": 3, "hidden": 128, "parameters": st["parameters"],
+                    "flops_per_cell": st["flops_per_cell"],
+                    "training": {"scene_seed": args.seed + 7919, "cell_steps": n_train,
+                                 "iterations": st_train["iterations"], "batch_cells": args.learned_batch,
+                                 "loss_first": loss0, "loss_last": loss, "seconds": round(train_s, 2)},
+                    "held_out_position_error": {"network": net_err, "constant_force_extrapolation": base_err}},
+        "judge": "positions after the same simulated time, against plain frames from the same state",
+    }
+
+
 def run_ours(args):
     import torch
     import bcs_build
@@ -314,6 +385,13 @@ def run_ours(args):
         torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
     e2e_value = ws * n * e2e_steps / float(e2e_t.item())
 
+    learned = None
+    if rank == 0 and not args.no_learned:
+        try:
+            learned = learned_substep(args, scene, tuning, bcs, fresh, args.warmup)
+        except Exception as exc:   # the plain line is still printed
+            learned = {"error": f"{type(exc).__name__}: {exc}"}
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         v, cinfo, threads = time_oracle(scene, args.cpu_budget, warmup=1, max_steps=3)
@@ -343,6 +421,7 @@ def run_ours(args):
                          "kernel_ms_over": f"{prof_steps} eager frames of the same trajectory"},
             "phase_ms": {k: v / prof_steps for k, v in phases.items()},
             "diagnostics_after_timed_run": diag,
+            "learned_substep": learned,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
@@ -367,6 +446,12 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--autotune-frames", type=int, default=3)
     ap.add_argument("--tuning", default="", help="comma-separated bcs_tuning fields instead of the autotuner")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned sub-step measurements")
+    ap.add_argument("--learned-substeps", type=int, default=8)
+    ap.add_argument("--learned-macro-steps", type=int, default=40)
+    ap.add_argument("--learned-collect", type=int, default=4)
+    ap.add_argument("--learned-iters", type=int, default=800)
+    ap.add_argument("--learned-batch", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -435,6 +435,8 @@ bcs_status bcs_synchronize(bcs_sim* sim);
 /* Time `nsteps` of bcs_step on the device with CUDA events recorded on the
  * handle's stream; writes milliseconds.  For benchmarking. */
 bcs_status bcs_time_steps(bcs_sim* sim, int nsteps, float* ms_out);
+/* bcs_macro_step(sim, substeps, n) timed the same way. */
+bcs_status bcs_time_macro_steps(bcs_sim* sim, int substeps, int n, float* ms_out);
 
 /* Largest object count bcs_grid_sort_static accepts. */
 #define BCS_GRID_SORT_STATIC_MAX 262144

@@ -33,7 +33,7 @@ EXPORTED = [
     "bcs_surrogate_create", "bcs_surrogate_destroy", "bcs_surrogate_collect", "bcs_surrogate_train",
     "bcs_surrogate_enable", "bcs_surrogate_get_stats", "bcs_surrogate_reset_stats", "bcs_surrogate_param_count",
     "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
-    "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales",
+    "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales", "bcs_time_macro_steps",
 ]
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
 GRID_SORT_STATIC_MAX = 262144
@@ -171,6 +171,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_set_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "bcs_autotune": ([P, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)], C.c_int),
         "bcs_macro_step": ([P, C.c_int, C.c_int], C.c_int),
+        "bcs_time_macro_steps": ([P, C.c_int, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "bcs_surrogate_create": ([P, C.POINTER(SurrogateDesc), C.POINTER(P)], C.c_int),
         "bcs_surrogate_destroy": ([P], C.c_int),
         "bcs_surrogate_collect": ([P, C.c_int], C.c_int),
@@ -396,6 +397,11 @@ class Simulation:
     def macro_step(self, substeps: int, n: int = 1) -> None:
         """n multi-rate macro steps of `substeps` time steps each."""
         _check(self.lib.bcs_macro_step(self.h, int(substeps), int(n)), "bcs_macro_step")
+
+    def time_macro_steps(self, substeps: int, n: int) -> float:
+        ms = C.c_float()
+        _check(self.lib.bcs_time_macro_steps(self.h, int(substeps), int(n), C.byref(ms)), "bcs_time_macro_steps")
+        return ms.value
 
     def time_steps(self, nsteps: int) -> float:
         ms = C.c_float()

@@ -1586,6 +1586,18 @@ bcs_status bcs_time_steps(bcs_sim* s, int nsteps, float* ms_out) {
     return check_last();
 }
 
+bcs_status bcs_time_macro_steps(bcs_sim* s, int substeps, int n, float* ms_out) {
+    if (!s || !ms_out || n < 0 || substeps < 1 || substeps > BCS_MAX_SUBSTEPS || s->mid_frame)
+        return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaEventRecord(s->ev0, s->stream));
+    bcs_status st = run_steps(s, n, substeps);
+    if (st != BCS_OK) return st;
+    BCS_CUDA(cudaEventRecord(s->ev1, s->stream));
+    BCS_CUDA(cudaEventSynchronize(s->ev1));
+    BCS_CUDA(cudaEventElapsedTime(ms_out, s->ev0, s->ev1));
+    return check_last();
+}
+
 bcs_status bcs_profile_steps(bcs_sim* s, int nsteps, float* phase_ms) {
     if (!s || !phase_ms || nsteps < 0 || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < nsteps; ++i) {

@@ -231,7 +231,10 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     sur.collect(args.learned_collect)
     n_train = sur.stats()["samples"]
     loss0 = sur.train(1, batch_cells=args.learned_batch, lr=1e-3)
-    loss = sur.train(args.learned_iters, batch_cells=args.learned_batch, lr=1e-3)
+    # learning rate 1e-3 decayed by 10 x over four phases
+    loss = loss0
+    for phase in range(4):
+        loss = sur.train(args.learned_iters // 4, batch_cells=args.learned_batch, lr=1e-3 * 10 ** (-phase / 3))
     sur.collect(1)
     net_err, base_err = sur.evaluate(n_train, sur.stats()["samples"] - n_train)
     params, scales, st_train = sur.get_params(), sur.scales(), sur.stats()
@@ -239,8 +242,27 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     ts.close()
     train_s = time.perf_counter() - t0
 
+    # local error: one macro step against K plain frames from the same state
     sim = fresh(tuning)
     n = sim.n
+    sim.step(K)
+    pa1 = sim.get_particles()[0].astype(np.float64)
+    sim.close()
+    sim = fresh(tuning)
+    sim.macro_step(K, 1)
+    pb1 = sim.get_particles()[0]
+    sim.close()
+    sim = fresh(tuning)
+    s1 = bcs.Surrogate(sim, cell_type=1, substeps=K, max_samples=1, seed=11)
+    s1.set_params(params)
+    s1.set_scales(scales)
+    s1.enable(True)
+    sim.macro_step(K, 1)
+    pc1 = sim.get_particles()[0]
+    s1.close()
+    sim.close()
+
+    sim = fresh(tuning)
     ms_plain = sim.time_steps(K * M)
     pa = sim.get_particles()[0]
     sim.close()
@@ -259,8 +281,8 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     s2.close()
     sim.close()
 
-    def err(p):
-        d = np.linalg.norm(p.astype(np.float64) - pa, axis=1)
+    def err(p, ref=None):
+        d = np.linalg.norm(p.astype(np.float64) - (pa if ref is None else ref), axis=1)
         return {"median": float(np.median(d)), "p99": float(np.percentile(d, 99)), "max": float(d.max()),
                 "frac_above_1e-3_radius": float(np.mean(d > 1e-3 * 0.5))}
 
@@ -268,8 +290,10 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     return {
         "substeps": K, "macro_steps": M, "simulated_time": K * M * float(scene.params.dt),
         "plain": {"ms": ms_plain, "particle_steps_per_s": rate(ms_plain)},
-        "macro_plain": {"ms": ms_macro, "particle_steps_per_s": rate(ms_macro), "position_error": err(pb)},
+        "macro_plain": {"ms": ms_macro, "particle_steps_per_s": rate(ms_macro), "position_error": err(pb),
+                        "one_macro_step_error": err(pb1, pa1)},
         "surrogate": {"ms": ms_sur, "particle_steps_per_s": rate(ms_sur), "position_error": err(pc),
+                      "one_macro_step_error": err(pc1, pa1),
                       "cells_predicted": st["predicted_cells"], "cells_fallen_back": st["fallback_cells"],
                       "tolerance": st["tolerance"]},
         "speedup_vs_plain": {"macro_plain": ms_plain / ms_macro, "surrogate": ms_plain / ms_sur},
@@ -450,7 +474,7 @@ def main():
     ap.add_argument("--learned-substeps", type=int, default=8)
     ap.add_argument("--learned-macro-steps", type=int, default=40)
     ap.add_argument("--learned-collect", type=int, default=4)
-    ap.add_argument("--learned-iters", type=int, default=800)
+    ap.add_argument("--learned-iters", type=int, default=2000)
     ap.add_argument("--learned-batch", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -1009,13 +1009,19 @@ const MacroHooks kInferHooks{infer_after_first, nullptr};
 // Means and spreads of the network's inputs and targets over (a sample of)
 // the training set.
 bcs_status compute_scales(bcs_surrogate* z) {
+    // a strided sample of up to 4096 samples over the whole training set
     const int n = std::min(z->stored, 4096);
     if (n <= 0) return BCS_ERR_INVALID_ARGUMENT;
-    std::vector<float> f((size_t)n * z->pic * 16), t((size_t)n * z->pic * 9);
+    const long long stride = std::max(1, z->stored / n);
+    const size_t fs_cell = (size_t)z->pic * 16, ts_cell = (size_t)z->pic * 9;
+    std::vector<float> f((size_t)n * fs_cell), t((size_t)n * ts_cell);
     std::vector<unsigned char> ok(n);
-    BCS_CUDA(cudaMemcpy(f.data(), z->ds_raw, sizeof(float) * f.size(), cudaMemcpyDeviceToHost));
-    BCS_CUDA(cudaMemcpy(t.data(), z->ds_t, sizeof(float) * t.size(), cudaMemcpyDeviceToHost));
-    BCS_CUDA(cudaMemcpy(ok.data(), z->ds_valid, n, cudaMemcpyDeviceToHost));
+    for (int c = 0; c < n; ++c) {
+        const long long src = (long long)c * stride;
+        BCS_CUDA(cudaMemcpy(&f[c * fs_cell], z->ds_raw + src * fs_cell, sizeof(float) * fs_cell, cudaMemcpyDeviceToHost));
+        BCS_CUDA(cudaMemcpy(&t[c * ts_cell], z->ds_t + src * ts_cell, sizeof(float) * ts_cell, cudaMemcpyDeviceToHost));
+        BCS_CUDA(cudaMemcpy(&ok[c], z->ds_valid + src, 1, cudaMemcpyDeviceToHost));
+    }
     double fs[16] = {}, fq[16] = {}, ts[9] = {}, tq[9] = {}, rq = 0, uq = 0, lq = 0;
     long long nodes = 0, edges = 0;
     const std::vector<int>& off = z->sim->h_adj_off;

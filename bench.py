@@ -113,7 +113,29 @@ def build_scene(cells_per_type, seed):
     return S.bifurcation_scene(cells_per_type=cells_per_type, seed=seed)
 
 
+def build_batch(args):
+    import bcs_scenes as S
+    return S.batched_scenes(args.batch_scenes, seed=args.seed)
+
+
+def batch_config(scenes, n_gpus):
+    cells = [int(sum(t.count for t in sc.types)) for sc in scenes]
+    return {
+        "workload": f"batched plain step, {len(scenes)} straight vessels in one simulation, "
+                    f"{sum(len(sc.positions) for sc in scenes)} particles",
+        "scenes": len(scenes),
+        "particles": int(sum(len(sc.positions) for sc in scenes)),
+        "cells": int(sum(cells)), "cells_per_scene_min": min(cells), "cells_per_scene_max": max(cells),
+        "lengths": "U[150, 600]", "cell_mix": "Bernoulli(0.5) icosphere-42 / biconcave-162",
+        "triangles": int(sum(len(sc.vein_indices) for sc in scenes)),
+        "dt": round(float(scenes[0].params.dt), 8), "grid_cell": float(scenes[0].params.cell_width),
+        "l2": "state exceeds the 129 MB L2; no flush", "parallelism": f"replicas x{n_gpus}",
+    }
+
+
 def workload_config(scene, n_gpus):
+    if isinstance(scene, list):
+        return batch_config(scene, n_gpus)
     p = scene.params
     return {
         "workload": f"plain step, Y bifurcation, {scene.particle_count} particles "
@@ -319,7 +341,10 @@ def run_ours(args):
         dist.init_process_group("nccl")
     bcs_build.build()
     bcs.set_device(local)
-    scene = build_scene(args.cells_per_type, args.seed + rank)
+    batched = args.workload == "batched"
+    scene = build_batch(args) if batched else build_scene(args.cells_per_type, args.seed + rank)
+    all_pos = np.concatenate([sc.positions for sc in scene]) if batched else scene.positions
+    all_vel = np.concatenate([sc.velocities for sc in scene]) if batched else scene.velocities
 
     def barrier(sim):
         if ws > 1:
@@ -331,7 +356,7 @@ def run_ours(args):
         """A new simulation at the state after the warm-up frames: every pass
         below starts from the same state and follows the same trajectory."""
         sim = bcs.Simulation(scene)
-        sim.set_particles(scene.positions, scene.velocities)
+        sim.set_particles(all_pos, all_vel)
         if tuning is not None:
             sim.set_tuning(**tuning)
         sim.step(args.warmup)
@@ -410,14 +435,14 @@ def run_ours(args):
     e2e_value = ws * n * e2e_steps / float(e2e_t.item())
 
     learned = None
-    if rank == 0 and not args.no_learned:
+    if rank == 0 and not args.no_learned and not batched:
         try:
             learned = learned_substep(args, scene, tuning, bcs, fresh, args.warmup)
         except Exception as exc:   # the plain line is still printed
             learned = {"error": f"{type(exc).__name__}: {exc}"}
 
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline and not batched:
         v, cinfo, threads = time_oracle(scene, args.cpu_budget, warmup=1, max_steps=3)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{cinfo['particles']} particles (inflow end of the same vessel) x {cinfo['steps']} "
@@ -471,6 +496,9 @@ def main():
     ap.add_argument("--autotune-frames", type=int, default=3)
     ap.add_argument("--tuning", default="", help="comma-separated bcs_tuning fields instead of the autotuner")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned sub-step measurements")
+    ap.add_argument("--workload", default="bifurcation", choices=["bifurcation", "batched"],
+                    help="bifurcation: the 4.2M-particle metric workload; batched: 64 straight vessels")
+    ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--learned-substeps", type=int, default=8)
     ap.add_argument("--learned-macro-steps", type=int, default=40)
     ap.add_argument("--learned-collect", type=int, default=4)

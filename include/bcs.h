@@ -296,6 +296,30 @@ bcs_status bcs_set_particles(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velociti
                              bcs_vec3 forces, bcs_memory where);
 bcs_status bcs_get_particles(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velocities,
                              bcs_vec3 forces, bcs_memory where);
+/* Initial particle state on the device (no reference counterpart as an
+ * API; the reference places its cells in SimulationController's
+ * constructor).
+ *   BCS_INIT_REFERENCE  the reference's rule (generateRandomPositonsAndVelocitiesKernel,
+ *                       setBloodCellsPositionsFromRandom, simulation_controller.cu:176-220):
+ *                       cell origin x, z uniform in +-0.6 cylinder_radius, y = min_spawn_y -
+ *                       180 u min(N / 1000, 1); particles at origin + model vertex; velocity
+ *                       init_velocity; overlaps allowed, as there.
+ *   BCS_INIT_LATTICE    non-overlapping: cells at randomly chosen sites of a cubic lattice
+ *                       (spacing 2 (bounding radius + collision radius) + gap) whose sphere
+ *                       lies inside the lumen (the flow segments, or the cylinder of
+ *                       cylinder_radius about the y axis); velocities init_velocity +
+ *                       Gaussian(0, velocity_sigma) per component.
+ * Random draws are Philox4x32-10 keyed by `seed` and the cell (particle) within its
+ * scene, so a scene starts the same in a batch as alone.  Forces are zeroed. */
+typedef enum bcs_init_kind { BCS_INIT_REFERENCE = 0, BCS_INIT_LATTICE = 1 } bcs_init_kind;
+typedef struct bcs_init_desc {
+    int kind;
+    uint64_t seed;
+    float velocity_sigma;   /* lattice only */
+    float gap;              /* lattice only: extra spacing between cells */
+} bcs_init_desc;
+bcs_status bcs_init_particles(bcs_sim* sim, const bcs_init_desc* desc);
+
 /* Vein vertex state (VeinTriangles positions/velocities/forces,
  * src/objects/vein_triangles.cuh:53-55).  NULL members are skipped. */
 bcs_status bcs_set_vein(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velocities,

@@ -34,7 +34,9 @@ EXPORTED = [
     "bcs_surrogate_enable", "bcs_surrogate_get_stats", "bcs_surrogate_reset_stats", "bcs_surrogate_param_count",
     "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
     "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales", "bcs_time_macro_steps",
+    "bcs_init_particles",
 ]
+INIT_REFERENCE, INIT_LATTICE = 0, 1
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
 GRID_SORT_STATIC_MAX = 262144
 MAX_SUBSTEPS = 64
@@ -124,6 +126,10 @@ class SceneInfo(C.Structure):
     ]
 
 
+class InitDesc(C.Structure):
+    _fields_ = [("kind", C.c_int), ("seed", C.c_uint64), ("velocity_sigma", C.c_float), ("gap", C.c_float)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("step_shape", C.c_int), ("persistent", C.c_int), ("spatial_order", C.c_int),
                 ("full_sort", C.c_int), ("occupancy_filter", C.c_int), ("sorted_positions", C.c_int)]
@@ -172,6 +178,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_autotune": ([P, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)], C.c_int),
         "bcs_macro_step": ([P, C.c_int, C.c_int], C.c_int),
         "bcs_time_macro_steps": ([P, C.c_int, C.c_int, C.POINTER(C.c_float)], C.c_int),
+        "bcs_init_particles": ([P, C.POINTER(InitDesc)], C.c_int),
         "bcs_surrogate_create": ([P, C.POINTER(SurrogateDesc), C.POINTER(P)], C.c_int),
         "bcs_surrogate_destroy": ([P], C.c_int),
         "bcs_surrogate_collect": ([P, C.c_int], C.c_int),
@@ -354,6 +361,12 @@ class Simulation:
         vecs = [Vec3(a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data) for a in out]
         _check(self.lib.bcs_get_particles(self.h, vecs[0], vecs[1], vecs[2], MEM_HOST), "bcs_get_particles")
         return tuple(np.ascontiguousarray(a.T) for a in out)
+
+    def init_particles(self, kind: int = INIT_LATTICE, seed: int = 0, velocity_sigma: float = 0.0,
+                       gap: float = 0.2) -> None:
+        """Initial state on the device (bcs_init_particles)."""
+        d = InitDesc(int(kind), int(seed), float(velocity_sigma), float(gap))
+        _check(self.lib.bcs_init_particles(self.h, C.byref(d)), "bcs_init_particles")
 
     def set_particles_device(self, x, y, z, vx, vy, vz) -> None:
         """Device pointers (torch CUDA tensors) in cudaVec3 SoA layout."""

@@ -60,6 +60,15 @@ void launch_export(const float4* pos, int n, const float4* vpos, int V, float* p
 void launch_pack(const float* x, const float* y, const float* z, int n, float4* out, const float* wsrc,
                  cudaStream_t s);
 void launch_unpack(const float4* in, int n, float* x, float* y, float* z, cudaStream_t s);
+void launch_init_reference(const StepArgs& a, float4* pos, float4* vel, float4* frc, const float4* model,
+                           const float* radius, unsigned long long seed, cudaStream_t s);
+void launch_lattice_sites(const SceneDev* scenes, int scene, float3 lo, int nx, int ny, int nz, float spacing,
+                          float clear, float ymin, float ymax, const bcs_flow_segment* flows, unsigned long long seed,
+                          int* keys, int* ids, int* valid_count, cudaStream_t s);
+void launch_lattice_place(const StepArgs& a, int scene, int count, float4* pos, float4* vel, float4* frc,
+                          const float4* model, const float* centroid, const float* radius, const int* site_ids,
+                          float3 lo, int nx, int ny, float spacing, float sigma, unsigned long long seed,
+                          cudaStream_t s);
 // bcs_sort.cu
 int radix_sort_pairs(const int* in_k, const int* in_v, int* a_k, int* a_v, int* b_k, int* b_v, int n, int bits,
                      unsigned* temp, cudaStream_t s);
@@ -173,6 +182,11 @@ struct bcs_sim {
     // host copies of the per-model tables (surrogate graphs and tolerances)
     std::vector<int> h_adj_off, h_adj_nbr;
     std::vector<float> h_adj_len, h_radius_model;
+    // scene start: absolute model vertices, per-type centroid and bounding
+    // radius, per-scene vein box (min xyz, max xyz)
+    float4* model = nullptr;
+    float* type_centroid = nullptr;
+    std::vector<float> h_type_bound, h_vein_box;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t pev[BCS_PHASE_COUNT + 1] = {};
     float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
@@ -610,7 +624,8 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     const bool tuniform = s->p.triangle_grid == BCS_GRID_UNIFORM;
 
     std::vector<int> adj_off, adj_nbr;
-    std::vector<float> adj_len, r0, radius_model;
+    std::vector<float> adj_len, r0, radius_model, centroids;
+    std::vector<float4> model_abs;
     std::vector<float4> respawn, vpos;
     std::vector<uint32_t> tri;
     std::vector<int> nb_ids;
@@ -666,11 +681,16 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
                 cx += m[3 * j]; cy += m[3 * j + 1]; cz += m[3 * j + 2];
             }
             cx /= pic; cy /= pic; cz /= pic;
+            float bound = 0.f;
             for (int j = 0; j < pic; ++j) {
                 float dx = m[3 * j] - cx, dy = m[3 * j + 1] - cy, dz = m[3 * j + 2] - cz;
                 r0.push_back(sqrtf(dx * dx + dy * dy + dz * dz));
+                bound = std::max(bound, r0.back());
                 respawn.push_back(make_float4(m[3 * j] - m[0], m[3 * j + 1] - m[1], m[3 * j + 2] - m[2], 0.f));
+                model_abs.push_back(make_float4(m[3 * j], m[3 * j + 1], m[3 * j + 2], 0.f));
             }
+            centroids.push_back(cx); centroids.push_back(cy); centroids.push_back(cz);
+            s->h_type_bound.push_back(bound);
             s->types.push_back(td);
             s->max_pic = std::max(s->max_pic, pic);
             pstart += c.count * pic;
@@ -698,6 +718,8 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
                 mn[k] = std::min(mn[k], vn.positions[3 * i + k]);
                 mx[k] = std::max(mx[k], vn.positions[3 * i + k]);
             }
+        for (int k = 0; k < 3; ++k) s->h_vein_box.push_back(mn[k]);
+        for (int k = 0; k < 3; ++k) s->h_vein_box.push_back(mx[k]);
         if ((st = scene_grid(mn, mx, sp, sp.cell_width, sp.cell_height, sp.cell_depth, puniform, sd.pg)) ||
             (st = scene_grid(mn, mx, sp, sp.cell_width_triangles, sp.cell_height_triangles, sp.cell_depth_triangles,
                              tuniform, sd.tg)))
@@ -804,7 +826,8 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
         (st = upload(s, &s->types_dev, s->types)) || (st = upload(s, &s->scenes, s->scenes_host)) ||
         (st = upload(s, &s->adj_off, adj_off)) || (st = upload(s, &s->adj_nbr, adj_nbr)) ||
         (st = upload(s, &s->adj_len, adj_len)) || (st = upload(s, &s->r0, r0)) ||
-        (st = upload(s, &s->respawn, respawn)) || (st = upload(s, &s->flows, flows)))
+        (st = upload(s, &s->respawn, respawn)) || (st = upload(s, &s->flows, flows)) ||
+        (st = upload(s, &s->model, model_abs)) || (st = upload(s, &s->type_centroid, centroids)))
         return st;
     if ((st = upload(s, &s->vpos, vpos)) || (st = dalloc(s, &s->vvel, s->V)) || (st = dalloc(s, &s->vfrc, s->V)) ||
         (st = upload(s, &s->nb_ids, nb_ids)) || (st = upload(s, &s->nb_len, nb_len)) || (st = upload(s, &s->tri, tri)) ||
@@ -1376,6 +1399,71 @@ bcs_status bcs_step(bcs_sim* s, int nsteps) {
     if (s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
     bcs_status st = run_steps(s, nsteps);
     if (st != BCS_OK) return st;
+    return check_last();
+}
+
+bcs_status bcs_init_particles(bcs_sim* s, const bcs_init_desc* d) {
+    if (!s || !d || s->mid_frame || (d->kind != BCS_INIT_REFERENCE && d->kind != BCS_INIT_LATTICE) ||
+        d->velocity_sigma < 0.f || d->gap < 0.f)
+        return BCS_ERR_INVALID_ARGUMENT;
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    float4 *P = s->pos[s->cur], *Vv = s->vel[s->cur], *F = s->frc[s->cur];
+    bcs_status st = BCS_OK;
+    if (d->kind == BCS_INIT_REFERENCE) {
+        launch_init_reference(s->args, P, Vv, F, s->model, s->radius_of_particle, d->seed, s->stream);
+    } else {
+        for (int k = 0; k < s->S && st == BCS_OK; ++k) {
+            const SceneDev& z = s->scenes_host[k];
+            float spacing = 0.f;
+            int cells = 0;
+            for (size_t t = 0; t < s->types.size(); ++t) {
+                if (s->types[t].scene != k) continue;
+                float rmax = 0.f;
+                for (int i = 0; i < s->types[t].pic; ++i)
+                    rmax = std::max(rmax, s->h_radius_model[s->types[t].model_start + i]);
+                spacing = std::max(spacing, 2.f * (s->h_type_bound[t] + rmax) + d->gap);
+                cells += s->types[t].count;
+            }
+            if (cells == 0) continue;
+            const float* box = &s->h_vein_box[6 * k];
+            const float3 lo = make_float3(box[0], box[1], box[2]);
+            const long long nx = std::max(1LL, (long long)((box[3] - box[0]) / spacing));
+            const long long ny = std::max(1LL, (long long)((box[4] - box[1]) / spacing));
+            const long long nz = std::max(1LL, (long long)((box[5] - box[2]) / spacing));
+            const long long total = nx * ny * nz;
+            if (total > (1LL << 30)) { st = BCS_ERR_UNSUPPORTED; break; }
+            int *keys = nullptr, *ids = nullptr, *k2 = nullptr, *i2 = nullptr, *cnt = nullptr;
+            unsigned* temp = nullptr;
+            const int n = (int)total;
+            if (cudaMalloc(&keys, sizeof(int) * n) || cudaMalloc(&ids, sizeof(int) * n) ||
+                cudaMalloc(&k2, sizeof(int) * n) || cudaMalloc(&i2, sizeof(int) * n) || cudaMalloc(&cnt, sizeof(int)) ||
+                cudaMalloc(&temp, sizeof(unsigned) * radix_temp_words(n))) {
+                st = BCS_ERR_OUT_OF_MEMORY;
+            } else {
+                cudaMemsetAsync(cnt, 0, sizeof(int), s->stream);
+                launch_lattice_sites(s->scenes, k, lo, (int)nx, (int)ny, (int)nz, spacing, 0.5f * spacing, box[1],
+                                     box[4], s->flows, d->seed, keys, ids, cnt, s->stream);
+                // keys: 30-bit priorities of valid sites, 2^30 for the rest
+                const int where = radix_sort_pairs(keys, ids, k2, i2, keys, ids, n, 31, temp, s->stream);
+                int valid = 0;
+                cudaMemcpyAsync(&valid, cnt, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+                if (cudaStreamSynchronize(s->stream) != cudaSuccess) st = BCS_ERR_CUDA;
+                else if (valid < cells) st = BCS_ERR_INVALID_ARGUMENT;   // the vessel holds too few sites
+                else
+                    launch_lattice_place(s->args, k, z.particle_end - z.particle_start, P, Vv, F, s->model,
+                                         s->type_centroid, s->radius_of_particle, where ? ids : i2, lo, (int)nx,
+                                         (int)ny, spacing, d->velocity_sigma, d->seed, s->stream);
+                if (st == BCS_OK && cudaStreamSynchronize(s->stream) != cudaSuccess) st = BCS_ERR_CUDA;
+            }
+            cudaFree(keys); cudaFree(ids); cudaFree(k2); cudaFree(i2); cudaFree(cnt); cudaFree(temp);
+        }
+    }
+    if (st != BCS_OK) return st;
+    s->keys_valid = false;
+    s->grid_ready = false;
+    s->mid_frame = false;
+    if (s->tune.spatial_order && ((st = order_work_spatially(s)) || (st = upload_work(s)))) return st;
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
     return check_last();
 }
 

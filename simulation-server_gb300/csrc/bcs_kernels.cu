@@ -967,6 +967,99 @@ __global__ void k_sur_eval(const float* __restrict__ Y, const float* __restrict_
     }
 }
 
+// ------------------------------------------------------ scene start ----
+// The reference's initial placement (generateRandomPositonsAndVelocitiesKernel
+// and setBloodCellsPositionsFromRandom, simulation_controller.cu:176-220):
+// each cell's origin at x, z uniform in +-0.6 cylinderRadius and y =
+// minSpawnY - 180 u min(N / 1000, 1), its particles at origin + model
+// vertex, velocity initVelocity, force 0.  Philox4x32-10 keyed by (seed,
+// cell within the scene) replaces the per-thread curand states.
+__device__ inline int type_of_particle(const StepArgs& a, int p) {
+    return find_range(a.type_count, p, [&](int i) { return a.types[i].particle_start; });
+}
+
+__global__ void k_init_reference(const StepArgs a, float4* pos, float4* vel, float4* frc, const float4* __restrict__ model,
+                                 const float* __restrict__ radius, unsigned long long seed) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n) return;
+    const TypeDev ty = a.types[type_of_particle(a, p)];
+    const SceneDev& sc = a.scenes[ty.scene];
+    const int cell = (p - ty.particle_start) / ty.pic, k = (p - ty.particle_start) - cell * ty.pic;
+    uint32_t c[4] = {(uint32_t)(ty.cell_start + cell), 0xFFFFFFFFu, 0xFFFFFFFFu, 1u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const float n = (float)(sc.particle_end - sc.particle_start);
+    const float ox = (uniform_open(c[0]) - 0.5f) * 1.2f * sc.cylinder_radius;
+    const float oy = sc.min_spawn_y - 180.0f * uniform_open(c[1]) * fminf(n / 1000.0f, 1.0f);
+    const float oz = (uniform_open(c[2]) - 0.5f) * 1.2f * sc.cylinder_radius;
+    const float4 m = model[ty.model_start + k];
+    pos[p] = make_float4(ox + m.x, oy + m.y, oz + m.z, radius[p]);
+    vel[p] = make_float4(a.p.init_velocity[0], a.p.init_velocity[1], a.p.init_velocity[2], 0.f);
+    frc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Non-overlapping start: candidate sites of a cubic lattice of the given
+// spacing over the scene's vein box; a site is valid when a sphere of
+// `clear` around it lies inside the lumen (inside a flow segment, or without
+// segments inside the cylinder of cylinderRadius about the y axis over the
+// vein's height).  Valid sites get a Philox priority, invalid ones sort last.
+__global__ void k_lattice_sites(const SceneDev* __restrict__ scenes, int scene, float3 lo, int nx, int ny, int nz,
+                                float spacing, float clear, float ymin, float ymax,
+                                const bcs_flow_segment* __restrict__ flows, unsigned long long seed, int* keys,
+                                int* ids, int* valid_count) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long total = (long long)nx * ny * nz;
+    if (i >= total) return;
+    const SceneDev& sc = scenes[scene];
+    const int ix = (int)(i % nx), iy = (int)((i / nx) % ny), iz = (int)(i / ((long long)nx * ny));
+    const float3 q = f3(lo.x + (ix + 0.5f) * spacing, lo.y + (iy + 0.5f) * spacing, lo.z + (iz + 0.5f) * spacing);
+    bool ok = false;
+    if (sc.flow_count > 0) {
+        for (int k = 0; k < sc.flow_count && !ok; ++k) {
+            const bcs_flow_segment& f = flows[sc.flow_start + k];
+            const float3 o = f3(f.origin[0], f.origin[1], f.origin[2]), d = f3(f.direction[0], f.direction[1], f.direction[2]);
+            const float t = dot3(q - o, d);
+            const float3 radial = (q - o) - t * d;
+            ok = t > clear && t < f.length - clear && len3(radial) < f.radius - clear;
+        }
+    } else {
+        ok = sqrtf(q.x * q.x + q.z * q.z) < sc.cylinder_radius - clear && q.y > ymin + clear && q.y < ymax - clear;
+    }
+    uint32_t c[4] = {(uint32_t)i, (uint32_t)(i >> 32), 0x51734u, 2u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    keys[i] = ok ? (int)(c[0] >> 2) : 0x40000000;
+    ids[i] = (int)i;
+    if (ok) atomicAdd(valid_count, 1);
+}
+
+// Cells of the scene at the first sites of the sorted order (cell order
+// within the scene), particles at site + (model vertex - model centroid),
+// velocities initVelocity + sigma N(0, 1) per component (Box-Muller on a
+// Philox draw per particle), force 0.
+__global__ void k_lattice_place(const StepArgs a, int scene, float4* pos, float4* vel, float4* frc,
+                                const float4* __restrict__ model, const float* __restrict__ centroid,
+                                const float* __restrict__ radius, const int* __restrict__ site_ids, float3 lo,
+                                int nx, int ny, float spacing, float sigma, unsigned long long seed) {
+    const SceneDev& sc = a.scenes[scene];
+    const int p = sc.particle_start + blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= sc.particle_end) return;
+    const int t = type_of_particle(a, p);
+    const TypeDev ty = a.types[t];
+    const int cell = (p - ty.particle_start) / ty.pic, k = (p - ty.particle_start) - cell * ty.pic;
+    const long long site = site_ids[ty.cell_start + cell];
+    const int ix = (int)(site % nx), iy = (int)((site / nx) % ny), iz = (int)(site / ((long long)nx * ny));
+    const float4 m = model[ty.model_start + k];
+    const float* cen = centroid + 3 * t;
+    pos[p] = make_float4(lo.x + (ix + 0.5f) * spacing + (m.x - cen[0]), lo.y + (iy + 0.5f) * spacing + (m.y - cen[1]),
+                         lo.z + (iz + 0.5f) * spacing + (m.z - cen[2]), radius[p]);
+    uint32_t c[4] = {(uint32_t)(p - sc.particle_start), 0x7E10u, 0u, 3u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const float r1 = sqrtf(-2.0f * logf(uniform_open(c[0]))), r2 = sqrtf(-2.0f * logf(uniform_open(c[2])));
+    const float a1 = 6.2831853f * uniform_open(c[1]), a2 = 6.2831853f * uniform_open(c[3]);
+    vel[p] = make_float4(a.p.init_velocity[0] + sigma * r1 * cosf(a1), a.p.init_velocity[1] + sigma * r1 * sinf(a1),
+                         a.p.init_velocity[2] + sigma * r2 * cosf(a2), 0.f);
+    frc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 __global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch,
                               unsigned* occ, const int* __restrict__ ids, const float4* __restrict__ pos,
                               float4* spos) {
@@ -1288,6 +1381,27 @@ void launch_sur_apply(const StepArgs& a, const SurDev& d, const float* Y, const 
 void launch_sur_eval(const float* Y, const float* raw_t, const unsigned char* valid, const SurScales& sc, int first,
                      int cells, int pic, double* sums, cudaStream_t s) {
     if (cells > 0) k_sur_eval<<<(cells * 32 + 255) / 256, 256, 0, s>>>(Y, raw_t, valid, sc, first, cells, pic, sums);
+}
+void launch_init_reference(const StepArgs& a, float4* pos, float4* vel, float4* frc, const float4* model,
+                           const float* radius, unsigned long long seed, cudaStream_t s) {
+    if (a.n > 0) k_init_reference<<<BCS_GRID1(a.n, 256), 0, s>>>(a, pos, vel, frc, model, radius, seed);
+}
+void launch_lattice_sites(const SceneDev* scenes, int scene, float3 lo, int nx, int ny, int nz, float spacing,
+                          float clear, float ymin, float ymax, const bcs_flow_segment* flows, unsigned long long seed,
+                          int* keys, int* ids, int* valid_count, cudaStream_t s) {
+    const long long total = (long long)nx * ny * nz;
+    if (total > 0)
+        k_lattice_sites<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(scenes, scene, lo, nx, ny, nz, spacing, clear,
+                                                                        ymin, ymax, flows, seed, keys, ids,
+                                                                        valid_count);
+}
+void launch_lattice_place(const StepArgs& a, int scene, int count, float4* pos, float4* vel, float4* frc,
+                          const float4* model, const float* centroid, const float* radius, const int* site_ids,
+                          float3 lo, int nx, int ny, float spacing, float sigma, unsigned long long seed,
+                          cudaStream_t s) {
+    if (count > 0)
+        k_lattice_place<<<BCS_GRID1(count, 256), 0, s>>>(a, scene, pos, vel, frc, model, centroid, radius, site_ids,
+                                                          lo, nx, ny, spacing, sigma, seed);
 }
 void launch_substeps(const StepArgs& a, int items, int K, cudaStream_t s) {
     if (items > 0 && K > 1) k_substeps<<<items, kSubstepThreads, 0, s>>>(a, K);

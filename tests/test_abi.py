@@ -64,6 +64,7 @@ STRUCTS = {
     "bcs_flow_segment": bcs.FlowSegment, "bcs_params": bcs.Params, "bcs_scene_desc": bcs.SceneDesc,
     "bcs_info": bcs.Info, "bcs_scene_info": bcs.SceneInfo, "bcs_tuning": bcs.Tuning,
     "bcs_surrogate_desc": bcs.SurrogateDesc, "bcs_surrogate_stats": bcs.SurrogateStats,
+    "bcs_init_desc": bcs.InitDesc,
 }
 
 

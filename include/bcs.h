@@ -354,7 +354,9 @@ bcs_status bcs_macro_step(bcs_sim* sim, int substeps, int n);
 
 /* ---- Learned sub-steps (no reference counterpart) ------------------------
  * A message-passing network over one cell model's spring graph (3 layers,
- * hidden width 128, bfloat16 weights, FP32 accumulation) predicts a cell's
+ * hidden width 128, bfloat16 weights, FP32 accumulation; node messages
+ * silu(h W_b + b_b) averaged over each node's springs, with the springs'
+ * stretch and relative velocity along the spring as edge inputs) predicts a cell's
  * state after sub-steps 2..K of a macro step from the state after sub-step
  * 1: positions and velocities relative to the cell's centroid and mean
  * velocity, the current, held external and environment forces, and a
@@ -401,12 +403,15 @@ bcs_status bcs_surrogate_collect(bcs_surrogate* sur, int macro_steps);
  * training set; *loss (optional) = the last batch's loss. */
 bcs_status bcs_surrogate_train(bcs_surrogate* sur, int iterations, int batch_cells, float learning_rate,
                                float* loss);
-/* Use the network in this simulation's macro steps of K sub-steps (on != 0). */
+/* Use the network in this simulation's macro steps of K sub-steps: on = 1
+ * runs it as one fused kernel per macro step (a CTA per cell, the network
+ * on chip), on = 2 as the layer-by-layer kernels the training uses, on = 0
+ * stops using it. */
 bcs_status bcs_surrogate_enable(bcs_surrogate* sur, int on);
 bcs_status bcs_surrogate_get_stats(bcs_surrogate* sur, bcs_surrogate_stats* out);
 bcs_status bcs_surrogate_reset_stats(bcs_surrogate* sur);
 int64_t bcs_surrogate_param_count(bcs_surrogate* sur);
-/* FP32 parameters, in the order W_in, b_in, then per layer W_a, W_b, W_e,
+/* FP32 parameters, in the order W_in, b_in, then per layer W_b, b_b, W_e,
  * b_e, W_u, W_v, b_u, then W_out, b_out; matrices row-major [in][out]. */
 bcs_status bcs_surrogate_get_params(bcs_surrogate* sur, float* params, int64_t count);
 bcs_status bcs_surrogate_set_params(bcs_surrogate* sur, const float* params, int64_t count);

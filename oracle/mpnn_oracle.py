@@ -4,19 +4,21 @@ The network is the project's own (it has no reference counterpart): a
 message-passing network over one blood cell's spring graph.  Only the tests
 use this file, as the checker of the CUDA forward and backward kernels:
 
-    h0 = silu(f W_in + b_in)                        f: node features [n, 16]
+    h0 = silu(f W_in + b_in)                     f: node features [n, 16]
     per layer l (3 layers, hidden 128):
-        A = h W_a,  B = h W_b
-        m_ij = silu(A_i + B_j + e_ij W_e + b_e)     e: edge features [E, 8], edge i <- j
-        M_i  = mean over the edges of i of m_ij
-        h    = h + silu(h W_u + M W_v + b_u)
-    y = h W_out + b_out                             y: [n, 9]
+        B   = silu(h W_b + b_b)                  node messages
+        M_i = mean over the springs of i of B_j + ebar_i W_e + b_e
+        h   = h + silu(h W_u + M W_v + b_u)
+    y = h W_out + b_out                          y: [n, 9]
     loss = mean((y - t)^2)
 
-`bf16=True` rounds what the GPU rounds: every weight, and the activation
-operands of the four hidden x hidden products of each layer (h before W_a,
-W_b, W_u; M before W_v) and of their backward products, to bfloat16
-(round to nearest even); sums stay in FP64.
+ebar_i is the mean of node i's edge features e_ij (edge i <- j, 8 each).
+
+`bf16=True` rounds what the GPU rounds: every weight, the activation
+operands of the three hidden x hidden products of each layer (h before W_b
+and W_u, M before W_v) and of their backward products, and B where the
+aggregation reads it, to bfloat16 (round to nearest even); sums stay in
+FP64.  The rounding of B passes gradients unchanged.
 """
 from __future__ import annotations
 
@@ -45,7 +47,7 @@ def dsilu(x):
 def param_names(layers):
     names = ["W_in", "b_in"]
     for l in range(layers):
-        names += [f"Wa{l}", f"Wb{l}", f"We{l}", f"be{l}", f"Wu{l}", f"Wv{l}", f"bu{l}"]
+        names += [f"Wb{l}", f"bb{l}", f"We{l}", f"be{l}", f"Wu{l}", f"Wv{l}", f"bu{l}"]
     return names + ["W_out", "b_out"]
 
 
@@ -53,9 +55,17 @@ def param_shapes(hidden, layers):
     H = hidden
     shapes = {"W_in": (F_IN, H), "b_in": (H,), "W_out": (H, OUT), "b_out": (OUT,)}
     for l in range(layers):
-        shapes.update({f"Wa{l}": (H, H), f"Wb{l}": (H, H), f"We{l}": (E_IN, H), f"be{l}": (H,),
+        shapes.update({f"Wb{l}": (H, H), f"bb{l}": (H,), f"We{l}": (E_IN, H), f"be{l}": (H,),
                        f"Wu{l}": (H, H), f"Wv{l}": (H, H), f"bu{l}": (H,)})
     return shapes
+
+
+def _edge_mean(e, src, n):
+    deg = np.bincount(src, minlength=n).astype(np.float64)
+    ebar = np.zeros((n, e.shape[1]))
+    np.add.at(ebar, src, np.asarray(e, np.float64))
+    inv = 1.0 / np.maximum(deg, 1.0)
+    return ebar * inv[:, None], inv
 
 
 def forward(params, f, e, src, dst, layers, bf=False, keep=False):
@@ -64,21 +74,19 @@ def forward(params, f, e, src, dst, layers, bf=False, keep=False):
     P = {k: (bf16(v) if bf and k[0] == "W" else np.asarray(v, np.float64)) for k, v in params.items()}
     q = bf16 if bf else (lambda x: np.asarray(x, np.float64))
     n = f.shape[0]
-    deg = np.bincount(src, minlength=n).astype(np.float64)
-    inv = 1.0 / np.maximum(deg, 1.0)
+    ebar, inv = _edge_mean(e, src, n)
     z0 = np.asarray(f, np.float64) @ P["W_in"] + P["b_in"]
     h = silu(z0)
-    cache = {"z0": z0, "deg_inv": inv, "P": P, "layers": []}
+    cache = {"z0": z0, "deg_inv": inv, "ebar": ebar, "P": P, "layers": []}
     for l in range(layers):
         hq = q(h)
-        A = hq @ P[f"Wa{l}"]
-        B = hq @ P[f"Wb{l}"]
-        pre = A[src] + B[dst] + np.asarray(e, np.float64) @ P[f"We{l}"] + P[f"be{l}"]
-        M = np.zeros_like(A)
-        np.add.at(M, src, silu(pre))
-        M *= inv[:, None]
+        zb = hq @ P[f"Wb{l}"] + P[f"bb{l}"]
+        B = q(silu(zb))
+        M = np.zeros_like(B)
+        np.add.at(M, src, B[dst])
+        M = M * inv[:, None] + ebar @ P[f"We{l}"] + P[f"be{l}"]
         zu = hq @ P[f"Wu{l}"] + q(M) @ P[f"Wv{l}"] + P[f"bu{l}"]
-        cache["layers"].append({"h": h, "pre": pre, "M": M, "zu": zu})
+        cache["layers"].append({"h": h, "zb": zb, "M": M, "zu": zu})
         h = h + silu(zu)
     y = h @ P["W_out"] + P["b_out"]
     cache["h_last"] = h
@@ -89,7 +97,6 @@ def loss_and_grads(params, f, e, src, dst, t, layers, bf=False):
     y, c = forward(params, f, e, src, dst, layers, bf=bf, keep=True)
     P = c["P"]
     q = bf16 if bf else (lambda x: np.asarray(x, np.float64))
-    n = y.shape[0]
     d = y - np.asarray(t, np.float64)
     loss = float(np.mean(d * d))
     g = {}
@@ -97,9 +104,10 @@ def loss_and_grads(params, f, e, src, dst, t, layers, bf=False):
     g["W_out"] = c["h_last"].T @ dy
     g["b_out"] = dy.sum(0)
     dh = dy @ P["W_out"].T
+    inv = c["deg_inv"]
     for l in reversed(range(layers)):
         L = c["layers"][l]
-        h, pre, M, zu = L["h"], L["pre"], L["M"], L["zu"]
+        h, zb, M, zu = L["h"], L["zb"], L["M"], L["zu"]
         hq, Mq = q(h), q(M)
         dzu = dh * dsilu(zu)
         dzq = q(dzu)
@@ -107,18 +115,16 @@ def loss_and_grads(params, f, e, src, dst, t, layers, bf=False):
         g[f"Wv{l}"] = Mq.T @ dzq
         g[f"bu{l}"] = dzu.sum(0)
         dM = dzq @ P[f"Wv{l}"].T
-        dh_next = dh + dzq @ P[f"Wu{l}"].T
-        dpre = (dM * c["deg_inv"][:, None])[src] * dsilu(pre)
-        dA = np.zeros_like(h)
-        dB = np.zeros_like(h)
-        np.add.at(dA, src, dpre)
-        np.add.at(dB, dst, dpre)
-        g[f"We{l}"] = np.asarray(e, np.float64).T @ dpre
-        g[f"be{l}"] = dpre.sum(0)
-        dAq, dBq = q(dA), q(dB)
-        g[f"Wa{l}"] = hq.T @ dAq
-        g[f"Wb{l}"] = hq.T @ dBq
-        dh = dh_next + dAq @ P[f"Wa{l}"].T + dBq @ P[f"Wb{l}"].T
+        dh = dh + dzq @ P[f"Wu{l}"].T
+        g[f"We{l}"] = c["ebar"].T @ dM
+        g[f"be{l}"] = dM.sum(0)
+        dB = np.zeros_like(dM)
+        np.add.at(dB, dst, (dM * inv[:, None])[src])
+        dzb = dB * dsilu(zb)
+        dzbq = q(dzb)
+        g[f"Wb{l}"] = hq.T @ dzbq
+        g[f"bb{l}"] = dzb.sum(0)
+        dh = dh + dzbq @ P[f"Wb{l}"].T
     dz0 = dh * dsilu(c["z0"])
     g["W_in"] = np.asarray(f, np.float64).T @ dz0
     g["b_in"] = dz0.sum(0)

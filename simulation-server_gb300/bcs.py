@@ -519,8 +519,9 @@ class Surrogate:
                "bcs_surrogate_train")
         return loss.value
 
-    def enable(self, on: bool = True) -> None:
-        _check(self.lib.bcs_surrogate_enable(self.h, int(bool(on))), "bcs_surrogate_enable")
+    def enable(self, on: bool = True, fused: bool = True) -> None:
+        """Use the network in macro steps (fused: one kernel per macro step)."""
+        _check(self.lib.bcs_surrogate_enable(self.h, (1 if fused else 2) if on else 0), "bcs_surrogate_enable")
 
     def stats(self) -> dict:
         st = SurrogateStats()

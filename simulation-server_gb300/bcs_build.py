@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbcs.so")
 SOURCES = ["bcs_kernels.cu", "bcs_sort.cu", "bcs_api.cu", "bcs_noalloc.cu", "bcs_mpnn.cu"]
-HEADERS = ["bcs_internal.cuh", "bcs_mpnn.cuh"]
+HEADERS = ["bcs_internal.cuh", "bcs_mpnn.cuh", "bcs_mma.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",

@@ -53,6 +53,9 @@ void launch_sur_inputs(const float* raw, const float* raw_t, const int* list, in
                        const SurScales& sc, float* f, float* E, float* T, cudaStream_t s);
 void launch_sur_apply(const StepArgs& a, const SurDev& d, const float* Y, const SurScales& sc, int first, int cells,
                       cudaStream_t s);
+bool launch_sur_fused(const StepArgs& a, const SurDev& d, const SurScales& sc, const float* P,
+                      const __nv_bfloat16* PB, const __nv_bfloat16* PBT, const MpnnLayout& L, const int* goff,
+                      const int* gnbr, const float* glen, int first, int cells, cudaStream_t s);
 void launch_sur_eval(const float* Y, const float* raw_t, const unsigned char* valid, const SurScales& sc, int first,
                      int cells, int pic, double* sums, cudaStream_t s);
 void launch_export(const float4* pos, int n, const float4* vpos, int V, float* pvbo, float* poff, float* vvbo,
@@ -968,6 +971,7 @@ struct bcs_surrogate {
     unsigned char* ds_valid = nullptr;
     int* valid_list = nullptr;
     bool collecting = false, enabled = false, scales_set = false;
+    int mode = 1;                      // 1: fused inference kernel, 2: layer-by-layer kernels
     SurScales scales{};
     unsigned long long seed = 0, draws = 0;
     long long iterations = 0;
@@ -1017,6 +1021,12 @@ void collect_after_substeps(bcs_sim* s) {
 void infer_after_first(bcs_sim* s) {
     bcs_surrogate* z = s->surrogate;
     launch_sur_features(s->args, z->dev(z->raw), s->stream);
+    if (z->mode == 1 && launch_sur_fused(s->args, z->dev(z->raw), z->scales, z->net.params(), z->net.weights_bf16(),
+                                         z->net.weights_bf16_t(), z->net.layout(), z->net.dev_adj_off(),
+                                         z->net.dev_adj_nbr(), z->net.dev_adj_len(), 0, z->cells, s->stream)) {
+        s->args.skip_cell = z->skip;
+        return;
+    }
     for (int first = 0; first < z->cells; first += z->infer_cells) {
         const int n = std::min(z->infer_cells, z->cells - first);
         launch_sur_inputs(z->raw, nullptr, nullptr, 0, 0, first, n, z->pic, z->net.dev_adj_off(), z->net.dev_adj_nbr(),
@@ -1051,6 +1061,7 @@ bcs_status compute_scales(bcs_surrogate* z) {
     const std::vector<int>& nbr = z->sim->h_adj_nbr;
     const std::vector<float>& len = z->sim->h_adj_len;
     const int a0 = z->sim->types[z->model_type].adj_start;
+    auto len_k = [&](int k) { return (double)len[k]; };
     for (int c = 0; c < n; ++c) {
         if (!ok[c]) continue;
         for (int i = 0; i < z->pic; ++i) {
@@ -1061,12 +1072,14 @@ bcs_status compute_scales(bcs_surrogate* z) {
             ++nodes;
             for (int k = off[a0 + i]; k < off[a0 + i + 1]; ++k) {
                 const float* fj = &f[((size_t)c * z->pic + nbr[k]) * 16];
-                double dr[3] = {fi[0] - fj[0], fi[1] - fj[1], fi[2] - fj[2]};
-                double du[3] = {fi[3] - fj[3], fi[4] - fj[4], fi[5] - fj[5]};
-                const double d = std::sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]) - len[k];
-                rq += (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]) / 3;
-                uq += (du[0] * du[0] + du[1] * du[1] + du[2] * du[2]) / 3;
-                lq += d * d;
+                double d[3] = {fj[0] - fi[0], fj[1] - fi[1], fj[2] - fi[2]};
+                double du[3] = {fj[3] - fi[3], fj[4] - fi[4], fj[5] - fi[5]};
+                const double len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                const double st = len - len_k(k);
+                const double vn = len > 0 ? (du[0] * d[0] + du[1] * d[1] + du[2] * d[2]) / len : 0.0;
+                rq += (fi[0] * fi[0] + fi[1] * fi[1] + fi[2] * fi[2]) / 3;
+                lq += st * st;
+                uq += vn * vn;
                 ++edges;
             }
         }
@@ -1843,8 +1856,10 @@ bcs_status bcs_surrogate_enable(bcs_surrogate* z, int on) {
     bcs_sim* s = z->sim;
     if (s->mid_frame || (s->surrogate && s->surrogate != z)) return BCS_ERR_INVALID_ARGUMENT;
     if (on && !z->scales_set) return BCS_ERR_INVALID_ARGUMENT;   // train (or set the scales) first
+    if (on < 0 || on > 2) return BCS_ERR_INVALID_ARGUMENT;
     BCS_CUDA(cudaStreamSynchronize(s->stream));
     z->enabled = on != 0;
+    if (on) z->mode = on;
     s->surrogate = z->enabled ? z : nullptr;
     BCS_CUDA(cudaMemset(z->skip, 0, s->C));
     drop_graphs(s);
@@ -1868,7 +1883,8 @@ bcs_status bcs_surrogate_get_stats(bcs_surrogate* z, bcs_surrogate_stats* o) {
     o->tolerance = z->tolerance;
     // multiply-adds x 2 of one forward pass over one cell
     const double n = z->pic, e = z->net.edges(), H = kHidden;
-    o->flops_per_cell = 2.0 * (n * kFeatIn * H + z->net.layers() * (4.0 * n * H * H + e * kEdgeIn * H) + n * H * kOut);
+    o->flops_per_cell = 2.0 * (n * kFeatIn * H + z->net.layers() * (3.0 * n * H * H + n * kEdgeIn * H) + n * H * kOut) +
+                        z->net.layers() * e * H;
     o->device_bytes = z->bytes + z->net.bytes();
     return BCS_OK;
 }

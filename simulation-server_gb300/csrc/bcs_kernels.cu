@@ -12,6 +12,8 @@
 // particle's x, v, F cross HBM once per step in each direction.  k_vein_end
 // (handleVeinEndsBlockSync) is a warp-per-cell pass over the new positions.
 #include "bcs_internal.cuh"
+#include "bcs_mma.cuh"
+#include "bcs_mpnn.cuh"
 #include <algorithm>
 
 namespace bcs {
@@ -818,9 +820,25 @@ __global__ void k_sur_targets(const StepArgs a, const SurDev d, float* raw_t, un
     if (lane == 0) valid[sc_i] = jump ? 0 : 1;
 }
 
+// Edge features of the spring i <- j from the raw relative positions and
+// velocities of its ends and its rest length L: with d = r_j - r_i, n =
+// d / |d| and the stretch s = |d| - L, (s n, ((u_j - u_i) . n) n, s, L),
+// scaled; the mean over a node's springs carries the leading terms of its
+// spring force and of that force's rate of change.
+__device__ inline void spring_features(const float* ri, const float* rj, float L, const SurScales& sc, float* e) {
+    const float3 d = f3(rj[0] - ri[0], rj[1] - ri[1], rj[2] - ri[2]);
+    const float3 du = f3(rj[3] - ri[3], rj[4] - ri[4], rj[5] - ri[5]);
+    const float len = len3(d);
+    const float3 n = len > 0.f ? d / len : f3(0.f, 0.f, 0.f);
+    const float st = len - L, vn = dot3(du, n);
+    e[0] = st * n.x / sc.el; e[1] = st * n.y / sc.el; e[2] = st * n.z / sc.el;
+    e[3] = vn * n.x / sc.eu; e[4] = vn * n.y / sc.eu; e[5] = vn * n.z / sc.eu;
+    e[6] = st / sc.el;
+    e[7] = L / sc.er;
+}
+
 // Normalised network inputs for `cells` cells: node features, edge features
-// (relative position, stretch against the rest length, relative velocity,
-// rest length) and, when raw_t is given, targets.  Cell b reads sample
+// (spring_features) and, when raw_t is given, targets.  Cell b reads sample
 // idx[b] of the raw arrays (b itself when idx is null), or, with `nvalid`,
 // a sample drawn by Philox from list[0 .. nvalid) keyed by (seed, b).
 __global__ void k_sur_inputs(const float* __restrict__ raw, const float* __restrict__ raw_t, const int* __restrict__ list,
@@ -848,19 +866,8 @@ __global__ void k_sur_inputs(const float* __restrict__ raw, const float* __restr
         }
     }
     for (int i = threadIdx.x; i < pic; i += blockDim.x)
-        for (int k = adj_off[i]; k < adj_off[i + 1]; ++k) {
-            const int j = adj_nbr[k];
-            const float* ri = rw + i * 16;
-            const float* rj = rw + j * 16;
-            const float3 dr = f3(ri[0] - rj[0], ri[1] - rj[1], ri[2] - rj[2]);
-            const float3 du = f3(ri[3] - rj[3], ri[4] - rj[4], ri[5] - rj[5]);
-            const float L = adj_len[k];
-            float* e = E + ((size_t)b * edges + k) * 8;
-            e[0] = dr.x / sc.er; e[1] = dr.y / sc.er; e[2] = dr.z / sc.er;
-            e[3] = (len3(dr) - L) / sc.el;
-            e[4] = du.x / sc.eu; e[5] = du.y / sc.eu; e[6] = du.z / sc.eu;
-            e[7] = L / sc.er;
-        }
+        for (int k = adj_off[i]; k < adj_off[i + 1]; ++k)
+            spring_features(rw + i * 16, rw + adj_nbr[k] * 16, adj_len[k], sc, E + ((size_t)b * edges + k) * 8);
 }
 
 // The prediction of cells [first, first + cells): decode the network's
@@ -1058,6 +1065,279 @@ __global__ void k_lattice_place(const StepArgs a, int scene, float4* pos, float4
     vel[p] = make_float4(a.p.init_velocity[0] + sigma * r1 * cosf(a1), a.p.init_velocity[1] + sigma * r1 * sinf(a1),
                          a.p.init_velocity[2] + sigma * r2 * cosf(a2), 0.f);
     frc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// ------------------------------------------- fused network inference ----
+// One CTA per cell of the surrogate's model runs the whole network on chip:
+// the residual stream h in FP32 shared memory, B and then M in bf16 shared
+// memory, each 128 x 128 weight staged once per product, the products on
+// bf16 tensor cores (mma.sync m16n8k16, FP32 accumulation) with warp w
+// owning rows 16w .. 16w + 15; the messages, encoder and decoder in FP32.
+// The same rounding points as the layer-by-layer kernels.  The epilogue is
+// k_sur_apply's: decode, residual check, state and grid keys of a passing
+// cell, skip flag and counts.
+constexpr int kFusedHP = kHidden + 4;   // FP32 row stride of h
+constexpr int kFusedBP = kHidden + 8;   // bf16 row stride
+constexpr int kFusedW = 2176;           // floats of the small-weight area
+
+template <int MT>
+constexpr int fused_smem_bytes() {
+    return MT * 16 * kFusedHP * 4 + MT * 16 * kFusedBP * 2 + kHidden * kFusedBP * 2 + MT * 16 * kEdgeIn * 4 +
+           kFusedW * 4 + MT * 16 * kOut * 4 + 16;
+}
+
+__device__ inline void stage_weight(const __nv_bfloat16* __restrict__ Wt, __nv_bfloat16* Ws, int nthreads) {
+    for (int q = threadIdx.x; q < kHidden * (kHidden / 8); q += nthreads) {
+        const int n = q >> 4, k = (q & 15) * 8;
+        *reinterpret_cast<uint4*>(Ws + n * kFusedBP + k) = *reinterpret_cast<const uint4*>(Wt + n * kHidden + k);
+    }
+}
+
+// acc (this warp's 16 rows x 128) += H (FP32 smem, rounded to bf16) x Ws^T.
+__device__ inline void fused_gemm_h(const float* Hs, const __nv_bfloat16* Ws, float (&acc)[16][4], int r_lo, int g,
+                                    int t) {
+    const float* lo = Hs + r_lo * kFusedHP + 2 * t;
+    const float* hi = lo + 8 * kFusedHP;
+#pragma unroll
+    for (int ks = 0; ks < kHidden / 16; ++ks) {
+        const int k0 = ks * 16;
+        const uint32_t a0 = pack_bf16(lo[k0], lo[k0 + 1]), a1 = pack_bf16(hi[k0], hi[k0 + 1]);
+        const uint32_t a2 = pack_bf16(lo[k0 + 8], lo[k0 + 9]), a3 = pack_bf16(hi[k0 + 8], hi[k0 + 9]);
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) {
+            const __nv_bfloat16* bp = Ws + (nt * 8 + g) * kFusedBP + k0 + 2 * t;
+            mma_bf16(acc[nt], a0, a1, a2, a3, ld32(bp), ld32(bp + 8));
+        }
+    }
+}
+
+// acc += M (bf16 smem) x Ws^T.
+__device__ inline void fused_gemm_b(const __nv_bfloat16* Bs, const __nv_bfloat16* Ws, float (&acc)[16][4], int r_lo,
+                                    int g, int t) {
+    const __nv_bfloat16* lo = Bs + r_lo * kFusedBP + 2 * t;
+    const __nv_bfloat16* hi = lo + 8 * kFusedBP;
+#pragma unroll
+    for (int ks = 0; ks < kHidden / 16; ++ks) {
+        const int k0 = ks * 16;
+        const uint32_t a0 = ld32(lo + k0), a1 = ld32(hi + k0), a2 = ld32(lo + k0 + 8), a3 = ld32(hi + k0 + 8);
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) {
+            const __nv_bfloat16* bp = Ws + (nt * 8 + g) * kFusedBP + k0 + 2 * t;
+            mma_bf16(acc[nt], a0, a1, a2, a3, ld32(bp), ld32(bp + 8));
+        }
+    }
+}
+
+template <int MT>
+__global__ void __launch_bounds__(MT * 32, 1)
+    k_sur_fused(const StepArgs a, const SurDev d, const SurScales sc, const float* __restrict__ P,
+                const __nv_bfloat16* __restrict__ PB, const __nv_bfloat16* __restrict__ PBT, const MpnnLayout L,
+                const int* __restrict__ goff, const int* __restrict__ gnbr, const float* __restrict__ glen, int first,
+                int cells) {
+    constexpr int R = MT * 16, NT = MT * 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* Hs = reinterpret_cast<float*>(smem);
+    __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(Hs + R * kFusedHP);
+    __nv_bfloat16* Ws = Bs + R * kFusedBP;
+    float* Node = reinterpret_cast<float*>(Ws + kHidden * kFusedBP);   // R x 6 raw r, u; then R x 8 ebar
+    float* Wsm = Node + R * 8;
+    float* Ysm = Wsm + kFusedW;
+    int* red = reinterpret_cast<int*>(Ysm + R * kOut);
+    const int b = blockIdx.x;
+    if (b >= cells) return;
+    const int sc_i = first + b, pic = d.pic;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const int r_lo = warp * 16 + g;
+
+    // ---- encoder, and the mean edge features of every node
+    float* F0 = reinterpret_cast<float*>(Bs);   // R x 16 normalised features, then R x 6 raw r, u
+    const float* raw = d.raw + (size_t)sc_i * pic * 16;
+    for (int i = tid; i < R * 16; i += NT) {
+        const int r = i >> 4, q = i & 15;
+        F0[i] = r < pic ? (raw[r * 16 + q] - sc.fm[q]) * sc.fs[q] : 0.f;
+    }
+    for (int i = tid; i < kFeatIn * kHidden; i += NT) Wsm[i] = __bfloat162float(PB[L.w_in + i]);
+    for (int i = tid; i < kHidden; i += NT) Wsm[kFeatIn * kHidden + i] = P[L.b_in + i];
+    if (tid == 0) {
+        red[0] = 0;   // worst residual (float bits)
+        red[1] = 1;   // all finite
+        red[2] = 0;   // leaves the vein
+    }
+    __syncthreads();
+    for (int i = tid; i < R * kHidden; i += NT) {
+        const int r = i >> 7, c = i & (kHidden - 1);
+        float z = Wsm[kFeatIn * kHidden + c];
+#pragma unroll
+        for (int q = 0; q < kFeatIn; ++q) z = fmaf(F0[r * 16 + q], Wsm[q * kHidden + c], z);
+        Hs[r * kFusedHP + c] = r < pic ? silu_f(z) : 0.f;
+    }
+    __syncthreads();
+    float* RU = F0;   // raw r, u of every node (stride 6) while Bs is free
+    for (int i = tid; i < R * 6; i += NT) {
+        const int r = i / 6, q = i - r * 6;
+        RU[i] = r < pic ? raw[r * 16 + q] : 0.f;
+    }
+    __syncthreads();
+    for (int r = tid; r < R; r += NT) {
+        float eb[kEdgeIn] = {};
+        if (r < pic) {
+            const int e0 = goff[r], e1 = goff[r + 1];
+            for (int k = e0; k < e1; ++k) {
+                float e[kEdgeIn];
+                spring_features(RU + r * 6, RU + gnbr[k] * 6, glen[k], sc, e);
+#pragma unroll
+                for (int q = 0; q < kEdgeIn; ++q) eb[q] += e[q];
+            }
+            const float inv = 1.0f / (float)max(1, e1 - e0);
+#pragma unroll
+            for (int q = 0; q < kEdgeIn; ++q) eb[q] *= inv;
+        }
+#pragma unroll
+        for (int q = 0; q < kEdgeIn; ++q) Node[r * kEdgeIn + q] = eb[q];
+    }
+    __syncthreads();
+
+    // ---- message-passing layers
+    for (int l = 0; l < L.layers; ++l) {
+        stage_weight(PBT + L.wb[l], Ws, NT);
+        for (int i = tid; i < kEdgeIn * kHidden; i += NT) Wsm[i] = __bfloat162float(PB[L.we[l] + i]);
+        for (int i = tid; i < kHidden; i += NT) {
+            Wsm[kEdgeIn * kHidden + i] = P[L.be[l] + i];
+            Wsm[kEdgeIn * kHidden + kHidden + i] = P[L.bu[l] + i];
+            Wsm[kEdgeIn * kHidden + 2 * kHidden + i] = P[L.bb[l] + i];
+        }
+        __syncthreads();
+        {
+            // B = silu(h W_b + b_b), kept in bf16
+            float acc[16][4];
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+            fused_gemm_h(Hs, Ws, acc, r_lo, g, t);
+            const float* bb = Wsm + kEdgeIn * kHidden + 2 * kHidden;
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt) {
+                const int c = nt * 8 + 2 * t;
+                *reinterpret_cast<uint32_t*>(Bs + r_lo * kFusedBP + c) =
+                    pack_bf16(silu_f(acc[nt][0] + bb[c]), silu_f(acc[nt][1] + bb[c + 1]));
+                *reinterpret_cast<uint32_t*>(Bs + (r_lo + 8) * kFusedBP + c) =
+                    pack_bf16(silu_f(acc[nt][2] + bb[c]), silu_f(acc[nt][3] + bb[c + 1]));
+            }
+        }
+        __syncthreads();
+        // M = mean over the springs of B_j + ebar W_e + b_e: this thread's two rows, 32 columns
+        float m[16][4];
+        const float* We = Wsm;
+        const float* be = Wsm + kEdgeIn * kHidden;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = r_lo + 8 * h;
+            const int e0 = r < pic ? goff[r] : 0, e1 = r < pic ? goff[r + 1] : 0;
+            const float inv = 1.0f / (float)max(1, e1 - e0);
+            const float* eb = Node + r * kEdgeIn;
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt)
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int c = nt * 8 + 2 * t + u;
+                    float acc = 0.f;
+                    for (int k = e0; k < e1; ++k) acc += __bfloat162float(Bs[gnbr[k] * kFusedBP + c]);
+                    float tt = be[c];
+#pragma unroll
+                    for (int q = 0; q < kEdgeIn; ++q) tt = fmaf(eb[q], We[q * kHidden + c], tt);
+                    m[nt][2 * h + u] = r < pic ? acc * inv + tt : 0.f;
+                }
+        }
+        __syncthreads();   // every read of B is done
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) {
+            const int c = nt * 8 + 2 * t;
+            *reinterpret_cast<uint32_t*>(Bs + r_lo * kFusedBP + c) = pack_bf16(m[nt][0], m[nt][1]);
+            *reinterpret_cast<uint32_t*>(Bs + (r_lo + 8) * kFusedBP + c) = pack_bf16(m[nt][2], m[nt][3]);
+        }
+        stage_weight(PBT + L.wu[l], Ws, NT);
+        __syncthreads();
+        float accU[16][4];
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) accU[nt][0] = accU[nt][1] = accU[nt][2] = accU[nt][3] = 0.f;
+        fused_gemm_h(Hs, Ws, accU, r_lo, g, t);
+        __syncthreads();
+        stage_weight(PBT + L.wv[l], Ws, NT);
+        __syncthreads();
+        fused_gemm_b(Bs, Ws, accU, r_lo, g, t);
+        const float* bu = Wsm + kEdgeIn * kHidden + kHidden;
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int r = r_lo + 8 * h;
+                if (r >= pic) continue;
+                const int c = nt * 8 + 2 * t;
+                Hs[r * kFusedHP + c] += silu_f(accU[nt][2 * h] + bu[c]);
+                Hs[r * kFusedHP + c + 1] += silu_f(accU[nt][2 * h + 1] + bu[c + 1]);
+            }
+        __syncthreads();
+    }
+
+    // ---- decoder
+    for (int i = tid; i < kHidden * kOut; i += NT) Wsm[i] = __bfloat162float(PB[L.w_out + i]);
+    __syncthreads();
+    for (int i = tid; i < pic * kOut; i += NT) {
+        const int r = i / kOut, o = i - r * kOut;
+        float y = 0.f;
+        for (int c = 0; c < kHidden; ++c) y = fmaf(Hs[r * kFusedHP + c], Wsm[c * kOut + o], y);
+        Ysm[i] = y + P[L.b_out + o];
+    }
+    __syncthreads();
+
+    // ---- decode, residual check, state of a passing cell
+    const TypeDev ty = a.types[d.cell_type[sc_i]];
+    const SceneDev& scn = a.scenes[ty.scene];
+    const int cell = d.cell_index[sc_i], p0 = ty.particle_start + cell * pic;
+    const float T = d.T;
+    for (int k = tid; k < pic; k += NT) {
+        float tt[kOut];
+#pragma unroll
+        for (int q = 0; q < kOut; ++q) tt[q] = Ysm[k * kOut + q] * sc.ts[q] + sc.tm[q];
+        const float4* st = d.start + ((size_t)sc_i * pic + k) * 3;
+        const float3 x1 = xyz(st[0]), v1 = xyz(st[1]), F1 = xyz(st[2]);
+        const float3 vK = v1 + T * F1 + f3(tt[3], tt[4], tt[5]);
+        const float3 xK = x1 + T * v1 + (0.5f * T * T) * F1 + f3(tt[0], tt[1], tt[2]);
+        const float3 FK = F1 + f3(tt[6], tt[7], tt[8]);
+        const float res = len3(xK - x1 - (0.5f * T) * (v1 + vK));
+        const bool fin = isfinite(xK.x) && isfinite(xK.y) && isfinite(xK.z) && isfinite(vK.x) && isfinite(vK.y) &&
+                         isfinite(vK.z) && isfinite(FK.x) && isfinite(FK.y) && isfinite(FK.z);
+        if (!fin) atomicAnd(&red[1], 0);
+        else atomicMax(&red[0], __float_as_int(res));
+        Ysm[k * kOut + 0] = xK.x; Ysm[k * kOut + 1] = xK.y; Ysm[k * kOut + 2] = xK.z;
+        Ysm[k * kOut + 3] = vK.x; Ysm[k * kOut + 4] = vK.y; Ysm[k * kOut + 5] = vK.z;
+        Ysm[k * kOut + 6] = FK.x; Ysm[k * kOut + 7] = FK.y; Ysm[k * kOut + 8] = FK.z;
+        if (a.p.use_blood_flow && leaves_vein(scn, xK)) atomicOr(&red[2], 1);
+    }
+    __syncthreads();
+    const bool ok = red[1] && __int_as_float(red[0]) <= d.tolerance;
+    if (tid == 0) {
+        d.skip[ty.cell_global + cell] = ok ? 1 : 0;
+        atomicAdd(&d.counts[ok ? 0 : 1], 1ull);
+    }
+    if (!ok) return;
+    const bool leave = red[2] != 0;
+    const long long step = *a.steps + (d.K - 1);
+    unsigned e = 0;
+    for (int k = tid; k < pic; k += NT) {
+        float3 x = f3(Ysm[k * kOut + 0], Ysm[k * kOut + 1], Ysm[k * kOut + 2]);
+        float3 v = f3(Ysm[k * kOut + 3], Ysm[k * kOut + 4], Ysm[k * kOut + 5]);
+        if (leave) respawn(a, scn, ty.cell_start + cell, step, ty.model_start + k, x, v);
+        const int p = p0 + k;
+        const float w = a.pos_out[p].w;
+        a.pos_out[p] = make_float4(x.x, x.y, x.z, w);
+        a.vel_out[p] = make_float4(v.x, v.y, v.z, 0.f);
+        a.frc_out[p] = make_float4(Ysm[k * kOut + 6], Ysm[k * kOut + 7], Ysm[k * kOut + 8], 0.f);
+        if (a.keys_out) {
+            a.keys_out[p] = a.pg.uniform ? grid_key(scn.pg, x, e) : 0;
+            a.ids_out[p] = p;
+        }
+    }
+    if (e) atomicOr(a.err, e);
 }
 
 __global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch,
@@ -1402,6 +1682,32 @@ void launch_lattice_place(const StepArgs& a, int scene, int count, float4* pos, 
     if (count > 0)
         k_lattice_place<<<BCS_GRID1(count, 256), 0, s>>>(a, scene, pos, vel, frc, model, centroid, radius, site_ids,
                                                           lo, nx, ny, spacing, sigma, seed);
+}
+// The fused inference kernel for a cell of `pic` particles: false when no
+// instance holds it.
+template <int MT>
+bool launch_fused_mt(const StepArgs& a, const SurDev& d, const SurScales& sc, const float* P, const __nv_bfloat16* PB,
+                     const __nv_bfloat16* PBT, const MpnnLayout& L, const int* goff, const int* gnbr,
+                     const float* glen, int first, int cells, cudaStream_t s) {
+    constexpr int bytes = fused_smem_bytes<MT>();
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_sur_fused<MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        attr = true;
+    }
+    k_sur_fused<MT><<<cells, MT * 32, bytes, s>>>(a, d, sc, P, PB, PBT, L, goff, gnbr, glen, first, cells);
+    return true;
+}
+bool launch_sur_fused(const StepArgs& a, const SurDev& d, const SurScales& sc, const float* P,
+                      const __nv_bfloat16* PB, const __nv_bfloat16* PBT, const MpnnLayout& L, const int* goff,
+                      const int* gnbr, const float* glen, int first, int cells, cudaStream_t s) {
+    if (cells <= 0) return true;
+    const int mt = (d.pic + 15) / 16;
+    if (mt <= 3) return launch_fused_mt<3>(a, d, sc, P, PB, PBT, L, goff, gnbr, glen, first, cells, s);
+    if (mt <= 6) return launch_fused_mt<6>(a, d, sc, P, PB, PBT, L, goff, gnbr, glen, first, cells, s);
+    if (mt <= 11) return launch_fused_mt<11>(a, d, sc, P, PB, PBT, L, goff, gnbr, glen, first, cells, s);
+    if (mt <= 12) return launch_fused_mt<12>(a, d, sc, P, PB, PBT, L, goff, gnbr, glen, first, cells, s);
+    return false;
 }
 void launch_substeps(const StepArgs& a, int items, int K, cudaStream_t s) {
     if (items > 0 && K > 1) k_substeps<<<items, kSubstepThreads, 0, s>>>(a, K);

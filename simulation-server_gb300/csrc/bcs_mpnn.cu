@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "bcs_internal.cuh"
+#include "bcs_mma.cuh"
 #include "bcs_mpnn.cuh"
 
 namespace bcs {
@@ -19,23 +20,6 @@ namespace {
 constexpr int kTileRows = 128;            // rows (nodes) per GEMM CTA
 constexpr int kPad = kHidden + 8;         // smem row stride (bf16): conflict-free fragment loads
 constexpr int kGemmSmem = 2 * kTileRows * kPad * (int)sizeof(__nv_bfloat16);
-
-__device__ inline float silu_f(float x) { return x / (1.0f + __expf(-x)); }
-__device__ inline float dsilu_f(float x) {
-    const float s = 1.0f / (1.0f + __expf(-x));
-    return s * (1.0f + x * (1.0f - s));
-}
-
-__device__ inline void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
-                                uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-__device__ inline uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
 // Rows [r0, r0 + 128) of an FP32 [rows][128] matrix into bf16 smem (zero past `rows`).
 __device__ inline void stage_rows(const float* __restrict__ X, int r0, int rows, __nv_bfloat16* As) {
@@ -236,108 +220,79 @@ __global__ void __launch_bounds__(256) k_encode_bwd(const float* __restrict__ f,
     for (int i = threadIdx.x; i < kHidden; i += blockDim.x) atomicAdd(&gb[i], sb[i]);
 }
 
-// M_i = mean over edges (i <- j) of silu(A_i + B_j + e_ij W_e + b_e): one
-// warp per node, lane -> 4 columns.
-__global__ void k_message(const float* __restrict__ A, const float* __restrict__ B, const float* __restrict__ E,
-                          const __nv_bfloat16* __restrict__ We, const float* __restrict__ be, MpnnGraph g,
-                          const int* __restrict__ edge_base, float* M, int n) {
+// M_i = (sum over the springs of i of B_j, bf16) / deg_i + ebar_i W_e + b_e,
+// with ebar_i the mean of node i's edge features: one warp per node, lane ->
+// 4 columns.
+__global__ void k_aggregate(const float* __restrict__ B, const float* __restrict__ E,
+                            const __nv_bfloat16* __restrict__ We, const float* __restrict__ be, MpnnGraph g,
+                            const int* __restrict__ edge_base, float* M, int n) {
     const int node = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (node >= n) return;
     const int cell = node / g.pic, li = node - cell * g.pic, cb = cell * g.pic;
     const int e0 = g.adj_off[li], e1 = g.adj_off[li + 1];
-    const int ebase = edge_base[cell];
-    float a[4], w[kEdgeIn][4], bb[4], m[4] = {0.f, 0.f, 0.f, 0.f};
+    const float* e = E + (size_t)(edge_base[cell] + e0) * kEdgeIn;
+    const float inv = 1.0f / (float)max(1, e1 - e0);
+    float eb[kEdgeIn];
+#pragma unroll
+    for (int q = 0; q < kEdgeIn; ++q) eb[q] = 0.f;
+    for (int k = 0; k < e1 - e0; ++k)
+#pragma unroll
+        for (int q = 0; q < kEdgeIn; ++q) eb[q] += e[k * kEdgeIn + q];
+#pragma unroll
+    for (int q = 0; q < kEdgeIn; ++q) eb[q] *= inv;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int c = lane * 4 + j;
-        a[j] = A[(size_t)node * kHidden + c];
-        bb[j] = be[c];
+        float acc = 0.f;
+        for (int k = e0; k < e1; ++k) acc += round_bf16(B[(size_t)(cb + g.adj_nbr[k]) * kHidden + c]);
+        float t = be[c];
 #pragma unroll
-        for (int q = 0; q < kEdgeIn; ++q) w[q][j] = wv(We, q * kHidden + c);
+        for (int q = 0; q < kEdgeIn; ++q) t = fmaf(eb[q], wv(We, q * kHidden + c), t);
+        M[(size_t)node * kHidden + c] = acc * inv + t;
     }
-    for (int k = e0; k < e1; ++k) {
-        const int nb = cb + g.adj_nbr[k];
-        const float* e = E + (size_t)(ebase + k) * kEdgeIn;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            float p = a[j] + B[(size_t)nb * kHidden + lane * 4 + j] + bb[j];
-#pragma unroll
-            for (int q = 0; q < kEdgeIn; ++q) p = fmaf(e[q], w[q][j], p);
-            m[j] += silu_f(p);
-        }
-    }
-    const float inv = 1.0f / (float)max(1, e1 - e0);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) M[(size_t)node * kHidden + lane * 4 + j] = m[j] * inv;
 }
 
-// Backward of k_message for node i: its own edges (i <- j) give dA_i and the
-// W_e / b_e gradients; the reverse edges (j <- i) give dB_i.  rev[k] is the
-// index of edge k's reverse within the cell.
-__global__ void __launch_bounds__(256) k_message_bwd(const float* __restrict__ A, const float* __restrict__ B,
-                                                     const float* __restrict__ E, const __nv_bfloat16* __restrict__ We,
-                                                     const float* __restrict__ be, MpnnGraph g,
-                                                     const int* __restrict__ edge_base, const int* __restrict__ rev,
-                                                     const float* __restrict__ dM, float* dA, float* dB, float* gWe,
-                                                     float* gbe, int n) {
+// Backward of k_aggregate for node j: dB_j = sum over the springs i of j of
+// dM_i / deg_i (the spring graph is symmetric), and the W_e / b_e gradients
+// of node j's own row.
+__global__ void __launch_bounds__(256) k_aggregate_bwd(const float* __restrict__ E, MpnnGraph g,
+                                                       const int* __restrict__ edge_base, const float* __restrict__ dM,
+                                                       float* dB, float* gWe, float* gbe, int n) {
     __shared__ float sW[kEdgeIn * kHidden];
     __shared__ float sb[kHidden];
     for (int i = threadIdx.x; i < kEdgeIn * kHidden; i += blockDim.x) sW[i] = 0.f;
     for (int i = threadIdx.x; i < kHidden; i += blockDim.x) sb[i] = 0.f;
     __syncthreads();
     const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-    float w[kEdgeIn][4], bb[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        bb[j] = be[lane * 4 + j];
-#pragma unroll
-        for (int q = 0; q < kEdgeIn; ++q) w[q][j] = wv(We, q * kHidden + lane * 4 + j);
-    }
     float aw[kEdgeIn][4] = {};
     float ab[4] = {};
     for (int node = blockIdx.x * wpb + (threadIdx.x >> 5); node < n; node += gridDim.x * wpb) {
         const int cell = node / g.pic, li = node - cell * g.pic, cb = cell * g.pic;
         const int e0 = g.adj_off[li], e1 = g.adj_off[li + 1];
-        const int ebase = edge_base[cell];
-        float ai[4], bi[4], dmi[4], da[4] = {0.f, 0.f, 0.f, 0.f}, db[4] = {0.f, 0.f, 0.f, 0.f};
-        const float inv_i = 1.0f / (float)max(1, e1 - e0);
+        const float* e = E + (size_t)(edge_base[cell] + e0) * kEdgeIn;
+        const float inv = 1.0f / (float)max(1, e1 - e0);
+        float eb[kEdgeIn];
+#pragma unroll
+        for (int q = 0; q < kEdgeIn; ++q) eb[q] = 0.f;
+        for (int k = 0; k < e1 - e0; ++k)
+#pragma unroll
+            for (int q = 0; q < kEdgeIn; ++q) eb[q] += e[k * kEdgeIn + q];
+#pragma unroll
+        for (int q = 0; q < kEdgeIn; ++q) eb[q] *= inv;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const size_t o = (size_t)node * kHidden + lane * 4 + j;
-            ai[j] = A[o];
-            bi[j] = B[o];
-            dmi[j] = dM[o] * inv_i;
-        }
-        for (int k = e0; k < e1; ++k) {
-            const int lj = g.adj_nbr[k], nb = cb + lj;
-            const float* e = E + (size_t)(ebase + k) * kEdgeIn;
-            const int r = rev[k];
-            const float* er = E + (size_t)(ebase + r) * kEdgeIn;
-            const float inv_j = 1.0f / (float)max(1, g.adj_off[lj + 1] - g.adj_off[lj]);
+            const int c = lane * 4 + j;
+            const float dm = dM[(size_t)node * kHidden + c];
+            ab[j] += dm;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const size_t oj = (size_t)nb * kHidden + lane * 4 + j;
-                // edge k: i <- j
-                float p = ai[j] + B[oj] + bb[j];
-#pragma unroll
-                for (int q = 0; q < kEdgeIn; ++q) p = fmaf(e[q], w[q][j], p);
-                const float dp = dmi[j] * dsilu_f(p);
-                da[j] += dp;
-                ab[j] += dp;
-#pragma unroll
-                for (int q = 0; q < kEdgeIn; ++q) aw[q][j] = fmaf(e[q], dp, aw[q][j]);
-                // edge r: j <- i
-                float pr = A[oj] + bi[j] + bb[j];
-#pragma unroll
-                for (int q = 0; q < kEdgeIn; ++q) pr = fmaf(er[q], w[q][j], pr);
-                db[j] += dM[oj] * inv_j * dsilu_f(pr);
+            for (int q = 0; q < kEdgeIn; ++q) aw[q][j] = fmaf(eb[q], dm, aw[q][j]);
+            float db = 0.f;
+            for (int k = e0; k < e1; ++k) {
+                const int li2 = g.adj_nbr[k];
+                const float inv_i = 1.0f / (float)max(1, g.adj_off[li2 + 1] - g.adj_off[li2]);
+                db += dM[(size_t)(cb + li2) * kHidden + c] * inv_i;
             }
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const size_t o = (size_t)node * kHidden + lane * 4 + j;
-            dA[o] = da[j];
-            dB[o] = db[j];
+            dB[(size_t)node * kHidden + c] = db;
         }
     }
 #pragma unroll
@@ -536,14 +491,14 @@ int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, c
     pic_ = pic;
     edges_ = adj_off[pic];
     max_cells_ = max_cells;
-    // reverse edge of every edge of the cell graph (the spring graph is symmetric)
-    std::vector<int> rev(edges_, -1), base(max_cells);
+    // the aggregation's backward relies on a symmetric spring graph
+    std::vector<int> base(max_cells);
     for (int i = 0; i < pic; ++i)
         for (int k = adj_off[i]; k < adj_off[i + 1]; ++k) {
             const int j = adj_nbr[k];
-            for (int q = adj_off[j]; q < adj_off[j + 1]; ++q)
-                if (adj_nbr[q] == i) rev[k] = q;
-            if (rev[k] < 0) return (int)cudaErrorInvalidValue;
+            bool back = false;
+            for (int q = adj_off[j]; q < adj_off[j + 1]; ++q) back = back || adj_nbr[q] == i;
+            if (!back) return (int)cudaErrorInvalidValue;
         }
     for (int c = 0; c < max_cells; ++c) base[c] = c * edges_;
     auto up = [&](auto** dst, const auto* src, size_t n) {
@@ -551,7 +506,7 @@ int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, c
         return *dst && cudaMemcpy(*dst, src, n * sizeof(**dst), cudaMemcpyHostToDevice) == cudaSuccess;
     };
     if (!up(&adj_off_, adj_off, pic + 1) || !up(&adj_nbr_, adj_nbr, edges_) || !up(&adj_len_, adj_len, edges_) ||
-        !up(&rev_, rev.data(), edges_) || !up(&edge_base_, base.data(), max_cells))
+        !up(&edge_base_, base.data(), max_cells))
         return (int)cudaErrorMemoryAllocation;
     const long long P = L_.total;
     p_ = alloc(P); g_ = alloc(P); m_ = alloc(P); v_ = alloc(P);
@@ -559,7 +514,7 @@ int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, c
     pbt_ = reinterpret_cast<__nv_bfloat16*>(alloc((P + 1) / 2));
     std::vector<long long> sq;
     for (int l = 0; l < layers; ++l) {
-        sq.push_back(L_.wa[l]); sq.push_back(L_.wb[l]); sq.push_back(L_.wu[l]); sq.push_back(L_.wv[l]);
+        sq.push_back(L_.wb[l]); sq.push_back(L_.wu[l]); sq.push_back(L_.wv[l]);
     }
     nsq_ = (int)sq.size();
     sq_ = reinterpret_cast<long long*>(alloc(2 * sq.size()));
@@ -577,7 +532,6 @@ int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, c
     };
     fill(L_.w_in, kFeatIn, (long long)kFeatIn * kHidden);
     for (int l = 0; l < layers; ++l) {
-        fill(L_.wa[l], kHidden, (long long)kHidden * kHidden);
         fill(L_.wb[l], kHidden, (long long)kHidden * kHidden);
         fill(L_.we[l], kEdgeIn, (long long)kEdgeIn * kHidden);
         fill(L_.wu[l], kHidden, (long long)kHidden * kHidden);
@@ -591,14 +545,13 @@ int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, c
     const size_t n = (size_t)max_cells * pic, H = kHidden;
     f_ = alloc(n * kFeatIn); e_ = alloc((size_t)max_cells * edges_ * kEdgeIn); t_ = alloc(n * kOut);
     y_ = alloc(n * kOut); dy_ = alloc(n * kOut); loss_ = alloc(1);
-    z0_ = alloc(n * H); dh_ = alloc(n * H); da_ = alloc(n * H); db_ = alloc(n * H); dm_ = alloc(n * H);
-    dz_ = alloc(n * H);
+    z0_ = alloc(n * H); dh_ = alloc(n * H); db_ = alloc(n * H); dm_ = alloc(n * H); dz_ = alloc(n * H);
     for (int l = 0; l <= layers; ++l) h_[l] = alloc(n * H);
     for (int l = 0; l < layers; ++l) {
-        a_[l] = alloc(n * H); b_[l] = alloc(n * H); mm_[l] = alloc(n * H); zu_[l] = alloc(n * H);
+        zb_[l] = alloc(n * H); b_[l] = alloc(n * H); mm_[l] = alloc(n * H); zu_[l] = alloc(n * H);
     }
-    if (!f_ || !e_ || !t_ || !y_ || !dy_ || !loss_ || !z0_ || !dh_ || !da_ || !db_ || !dm_ || !dz_ ||
-        !h_[layers] || !zu_[layers - 1])
+    if (!f_ || !e_ || !t_ || !y_ || !dy_ || !loss_ || !z0_ || !dh_ || !db_ || !dm_ || !dz_ || !h_[layers] ||
+        !zu_[layers - 1])
         return (int)cudaErrorMemoryAllocation;
     refresh_bf16();
     cudaStreamSynchronize(st_);
@@ -619,13 +572,12 @@ void MpnnNet::forward(const float* f, const float* E, int cells, bool keep) {
     for (int l = 0; l < L_.layers; ++l) {
         float* hin = keep ? h_[l] : h_[l & 1];
         float* hout = keep ? h_[l + 1] : h_[(l + 1) & 1];
-        float* A = keep ? a_[l] : a_[0];
+        float* ZB = keep ? zb_[l] : zb_[0];
         float* B = keep ? b_[l] : b_[0];
         float* M = keep ? mm_[l] : mm_[0];
         float* ZU = keep ? zu_[l] : zu_[0];
-        mpnn_gemm(hin, pbt_ + L_.wa[l], nullptr, nullptr, nullptr, A, nullptr, n, false, false, st_);
-        mpnn_gemm(hin, pbt_ + L_.wb[l], nullptr, nullptr, nullptr, B, nullptr, n, false, false, st_);
-        k_message<<<wgrid, 256, 0, st_>>>(A, B, E, pb_ + L_.we[l], p_ + L_.be[l], g, edge_base_, M, n);
+        mpnn_gemm(hin, pbt_ + L_.wb[l], nullptr, nullptr, p_ + L_.bb[l], B, ZB, n, true, false, st_);
+        k_aggregate<<<wgrid, 256, 0, st_>>>(B, E, pb_ + L_.we[l], p_ + L_.be[l], g, edge_base_, M, n);
         cudaMemcpyAsync(hout, hin, sizeof(float) * (size_t)n * kHidden, cudaMemcpyDeviceToDevice, st_);
         mpnn_gemm(hin, pbt_ + L_.wu[l], M, pbt_ + L_.wv[l], p_ + L_.bu[l], hout, ZU, n, true, true, st_);
     }
@@ -649,12 +601,11 @@ void MpnnNet::backward(const float* T, int cells) {
         k_colsum<<<grid_for(n, 2, 1216), 256, 0, st_>>>(dz_, g_ + L_.bu[l], n);
         mpnn_gemm_t(dz_, pb_ + L_.wv[l], dm_, n, false, st_);
         mpnn_gemm_t(dz_, pb_ + L_.wu[l], dh_, n, true, st_);
-        k_message_bwd<<<rgrid, 256, 0, st_>>>(a_[l], b_[l], last_e_, pb_ + L_.we[l], p_ + L_.be[l], g, edge_base_, rev_,
-                                            dm_, da_, db_, g_ + L_.we[l], g_ + L_.be[l], n);
-        mpnn_wgrad(h_[l], da_, g_ + L_.wa[l], n, st_);
-        mpnn_wgrad(h_[l], db_, g_ + L_.wb[l], n, st_);
-        mpnn_gemm_t(da_, pb_ + L_.wa[l], dh_, n, true, st_);
-        mpnn_gemm_t(db_, pb_ + L_.wb[l], dh_, n, true, st_);
+        k_aggregate_bwd<<<rgrid, 256, 0, st_>>>(last_e_, g, edge_base_, dm_, db_, g_ + L_.we[l], g_ + L_.be[l], n);
+        k_dsilu<<<grid_for((long long)nh, 256), 256, 0, st_>>>(db_, zb_[l], dz_, (long long)nh);
+        mpnn_wgrad(h_[l], dz_, g_ + L_.wb[l], n, st_);
+        k_colsum<<<grid_for(n, 2, 1216), 256, 0, st_>>>(dz_, g_ + L_.bb[l], n);
+        mpnn_gemm_t(dz_, pb_ + L_.wb[l], dh_, n, true, st_);
     }
     k_encode_bwd<<<rgrid, 256, 0, st_>>>(last_f_, z0_, dh_, g_ + L_.w_in, g_ + L_.b_in, n);
 }

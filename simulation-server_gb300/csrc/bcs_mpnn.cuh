@@ -2,15 +2,15 @@
 // the kernels' entry points.
 //
 // A message-passing network over one blood cell's spring graph (hidden 128):
-//     h0 = silu(f W_in + b_in)                         f: 16 node features
-//     layer l: A = h W_a, B = h W_b
-//              m_ij = silu(A_i + B_j + e_ij W_e + b_e)   e: 8 edge features, edge i <- j
-//              M_i  = mean over the edges of i of m_ij
-//              h    = h + silu(h W_u + M W_v + b_u)
-//     y = h W_out + b_out                              y: 9 outputs per node
-// Weights are bfloat16 (an FP32 master copy is what the optimiser updates);
-// the hidden x hidden products run on the tensor cores with FP32
-// accumulation, everything else in FP32.
+//     h0 = silu(f W_in + b_in)                       f: 16 node features
+//     layer l: B   = silu(h W_b + b_b)                node messages
+//              M_i = mean over the springs of i of B_j + ebar_i W_e + b_e
+//              h   = h + silu(h W_u + M W_v + b_u)
+//     y = h W_out + b_out                            y: 9 outputs per node
+// ebar_i is the mean of node i's 8 edge features.  Weights are bfloat16 (an
+// FP32 master copy is what the optimiser updates); the hidden x hidden
+// products run on the tensor cores with FP32 accumulation, everything else
+// in FP32.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -29,7 +29,7 @@ constexpr int kMaxLayers = 4;
 struct MpnnLayout {
     int layers = 3;
     long long w_in, b_in, w_out, b_out;
-    long long wa[kMaxLayers], wb[kMaxLayers], we[kMaxLayers], be[kMaxLayers];
+    long long wb[kMaxLayers], bb[kMaxLayers], we[kMaxLayers], be[kMaxLayers];
     long long wu[kMaxLayers], wv[kMaxLayers], bu[kMaxLayers];
     long long total = 0;
 };
@@ -42,8 +42,8 @@ inline MpnnLayout mpnn_layout(int layers) {
     L.w_in = take((long long)kFeatIn * kHidden);
     L.b_in = take(kHidden);
     for (int l = 0; l < layers; ++l) {
-        L.wa[l] = take((long long)kHidden * kHidden);
         L.wb[l] = take((long long)kHidden * kHidden);
+        L.bb[l] = take(kHidden);
         L.we[l] = take((long long)kEdgeIn * kHidden);
         L.be[l] = take(kHidden);
         L.wu[l] = take((long long)kHidden * kHidden);
@@ -108,6 +108,9 @@ public:
     const int* dev_adj_off() const { return adj_off_; }
     const int* dev_adj_nbr() const { return adj_nbr_; }
     const float* dev_adj_len() const { return adj_len_; }
+    const __nv_bfloat16* weights_bf16() const { return pb_; }
+    const __nv_bfloat16* weights_bf16_t() const { return pbt_; }
+    const MpnnLayout& layout() const { return L_; }
     size_t bytes() const { return bytes_; }
 
 private:
@@ -115,7 +118,7 @@ private:
     MpnnLayout L_;
     cudaStream_t st_ = nullptr;
     int pic_ = 0, edges_ = 0, max_cells_ = 0;
-    int *adj_off_ = nullptr, *adj_nbr_ = nullptr, *rev_ = nullptr, *edge_base_ = nullptr;
+    int *adj_off_ = nullptr, *adj_nbr_ = nullptr, *edge_base_ = nullptr;
     float* adj_len_ = nullptr;
     float *p_ = nullptr, *g_ = nullptr, *m_ = nullptr, *v_ = nullptr;
     __nv_bfloat16 *pb_ = nullptr, *pbt_ = nullptr;
@@ -123,8 +126,8 @@ private:
     int nsq_ = 0, t_adam_ = 0;
     float *f_ = nullptr, *e_ = nullptr, *t_ = nullptr, *y_ = nullptr, *dy_ = nullptr, *loss_ = nullptr;
     const float *last_f_ = nullptr, *last_e_ = nullptr;   // inputs of the last forward
-    float *z0_ = nullptr, *dh_ = nullptr, *da_ = nullptr, *db_ = nullptr, *dm_ = nullptr, *dz_ = nullptr;
-    float *h_[kMaxLayers + 1] = {}, *a_[kMaxLayers] = {}, *b_[kMaxLayers] = {}, *mm_[kMaxLayers] = {},
+    float *z0_ = nullptr, *dh_ = nullptr, *db_ = nullptr, *dm_ = nullptr, *dz_ = nullptr;
+    float *h_[kMaxLayers + 1] = {}, *zb_[kMaxLayers] = {}, *b_[kMaxLayers] = {}, *mm_[kMaxLayers] = {},
           *zu_[kMaxLayers] = {};
     std::vector<void*> allocs_;
     size_t bytes_ = 0;

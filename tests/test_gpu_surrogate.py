@@ -99,7 +99,7 @@ def test_gradients_match_oracle(lib):
     # and the oracle itself follows its finite differences (FP64, no rounding)
     lf, gf = M.loss_and_grads(P, f, e, src, dst, t, 3)
     rng = np.random.default_rng(0)
-    for k in ("Wa0", "We2", "bu1", "W_in", "b_out"):
+    for k in ("Wb0", "We2", "bu1", "bb2", "W_in", "b_out"):
         idx = tuple(rng.integers(0, s) for s in P[k].shape)
         Pp = {q: v.copy() for q, v in P.items()}
         Pm = {q: v.copy() for q, v in P.items()}
@@ -132,6 +132,8 @@ def test_collect_and_train(lib, trained):
     assert st["iterations"] == 401
     assert loss < 0.5 * loss0
     assert st["parameters"] == sur.param_count() == sum(int(np.prod(s)) for s in M.param_shapes(128, 3).values())
+    assert abs(st["flops_per_cell"] - (2 * (42 * 16 * 128 + 3 * (3 * 42 * 128 * 128 + 42 * 8 * 128) + 42 * 128 * 9)
+                                       + 3 * 240 * 128)) < 1
 
 
 def test_trained_network_beats_the_extrapolation(lib, trained):
@@ -188,3 +190,20 @@ def test_surrogate_arguments(lib):
         sur.enable(True)      # not trained: no normalisation yet
     with pytest.raises(bcs.BcsError):
         sur.train(1)          # no samples yet
+
+
+def test_fused_inference_matches_layer_kernels(lib, trained):
+    sc, sim, sur, train_n, loss0, loss = trained
+    out = []
+    for fused in (True, False):
+        run = make(sc)
+        s = bcs.Surrogate(run, substeps=8, max_samples=40, seed=3, tolerance=10.0)
+        s.set_params(sur.get_params())
+        s.set_scales(sur.scales())
+        s.enable(True, fused=fused)
+        run.macro_step(8, 1)
+        out.append((run.get_particles(), s.stats()))
+    (a, sa), (b, sb) = out
+    assert sa["predicted_cells"] == sb["predicted_cells"] == 40
+    for x, y in zip(a, b):
+        assert np.abs(x - y).max() <= 1e-4 * (np.abs(y).max() + 1.0)

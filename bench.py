@@ -249,7 +249,8 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     ts.set_tuning(**tuning)
     ts.step(warm)
     cells = train_scene.types[1].count
-    sur = bcs.Surrogate(ts, cell_type=1, substeps=K, max_samples=cells * (args.learned_collect + 1), seed=11)
+    sur = bcs.Surrogate(ts, cell_type=1, substeps=K, max_samples=cells * (args.learned_collect + 1), seed=11,
+                        huber_delta=1.0)
     sur.collect(args.learned_collect)
     n_train = sur.stats()["samples"]
     loss0 = sur.train(1, batch_cells=args.learned_batch, lr=1e-3)
@@ -323,6 +324,7 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
                     "flops_per_cell": st["flops_per_cell"],
                     "training": {"scene_seed": args.seed + 7919, "cell_steps": n_train,
                                  "iterations": st_train["iterations"], "batch_cells": args.learned_batch,
+                                 "loss": "pseudo-Huber, delta 1 (normalised)",
                                  "loss_first": loss0, "loss_last": loss, "seconds": round(train_s, 2)},
                     "held_out_position_error": {"network": net_err, "constant_force_extrapolation": base_err}},
         "judge": "positions after the same simulated time, against plain frames from the same state",

@@ -378,6 +378,9 @@ typedef struct bcs_surrogate_desc {
     uint64_t seed;       /* weights and training draws */
     float tolerance;     /* residual threshold in length units; 0 = 1e-3 x the
                             model's smallest collision radius */
+    float huber_delta;   /* training loss: 0 = mean squared error, > 0 = pseudo-
+                            Huber delta^2 (sqrt(1 + (d/delta)^2) - 1) on the
+                            normalised outputs */
 } bcs_surrogate_desc;
 
 typedef struct bcs_surrogate_stats {
@@ -415,8 +418,8 @@ int64_t bcs_surrogate_param_count(bcs_surrogate* sur);
  * b_e, W_u, W_v, b_u, then W_out, b_out; matrices row-major [in][out]. */
 bcs_status bcs_surrogate_get_params(bcs_surrogate* sur, float* params, int64_t count);
 bcs_status bcs_surrogate_set_params(bcs_surrogate* sur, const float* params, int64_t count);
-/* Loss and parameter gradients of the network on given normalised host
- * inputs: features [cells * pic][16], edge features [cells * edges][8] in
+/* Loss (the training loss of the descriptor) and parameter gradients of the
+ * network on given normalised host inputs: features [cells * pic][16], edge features [cells * edges][8] in
  * the order of the cell's spring lists, targets [cells * pic][9]. */
 bcs_status bcs_surrogate_loss_grad(bcs_surrogate* sur, int cells, const float* features,
                                    const float* edge_features, const float* targets, float* loss,
@@ -431,8 +434,9 @@ bcs_status bcs_surrogate_forward(bcs_surrogate* sur, int cells, const float* fea
 bcs_status bcs_surrogate_evaluate(bcs_surrogate* sur, int first, int count, double* net_error,
                                   double* base_error);
 /* The normalisation derived from the training set: 53 floats (feature means
- * [16], feature 1/std [16], target means [9], target std [9], edge scales
- * of relative position, stretch and relative velocity). */
+ * [16], feature 1/std [16], target medians [9], target robust spreads [9]
+ * (1.4826 x the median absolute deviation), edge scales of position,
+ * stretch and velocity along the spring). */
 bcs_status bcs_surrogate_get_scales(bcs_surrogate* sur, float* out53);
 /* Install a normalisation (as bcs_surrogate_get_scales writes it), e.g.
  * with parameters trained by another surrogate of the same model. */

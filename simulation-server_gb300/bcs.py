@@ -140,7 +140,7 @@ class Tuning(C.Structure):
 
 class SurrogateDesc(C.Structure):
     _fields_ = [("cell_type", C.c_int), ("substeps", C.c_int), ("layers", C.c_int), ("max_samples", C.c_int),
-                ("seed", C.c_uint64), ("tolerance", C.c_float)]
+                ("seed", C.c_uint64), ("tolerance", C.c_float), ("huber_delta", C.c_float)]
 
 
 class SurrogateStats(C.Structure):
@@ -489,10 +489,11 @@ class Surrogate:
     bcs_surrogate handle)."""
 
     def __init__(self, sim: Simulation, cell_type: int = 0, substeps: int = 8, layers: int = 3,
-                 max_samples: int = 4096, seed: int = 1, tolerance: float = 0.0):
+                 max_samples: int = 4096, seed: int = 1, tolerance: float = 0.0, huber_delta: float = 0.0):
         self.lib = sim.lib
         self.sim = sim
-        d = SurrogateDesc(int(cell_type), int(substeps), int(layers), int(max_samples), int(seed), float(tolerance))
+        d = SurrogateDesc(int(cell_type), int(substeps), int(layers), int(max_samples), int(seed), float(tolerance),
+                          float(huber_delta))
         h = C.c_void_p()
         _check(self.lib.bcs_surrogate_create(sim.h, C.byref(d), C.byref(h)), "bcs_surrogate_create")
         self.h = h

@@ -1094,10 +1094,22 @@ bcs_status compute_scales(bcs_surrogate* z) {
         z->scales.fm[q] = (float)m;
         z->scales.fs[q] = (float)(1.0 / spread(fq[q], m, nodes));
     }
+    // targets: median and 1.4826 x median absolute deviation (heavy tails:
+    // contact events), falling back to the mean / spread when degenerate
     for (int q = 0; q < 9; ++q) {
+        std::vector<float> col;
+        col.reserve((size_t)nodes);
+        for (int c = 0; c < n; ++c)
+            if (ok[c])
+                for (int i = 0; i < z->pic; ++i) col.push_back(t[((size_t)c * z->pic + i) * 9 + q]);
+        std::nth_element(col.begin(), col.begin() + col.size() / 2, col.end());
+        const float med = col[col.size() / 2];
+        for (float& v : col) v = std::fabs(v - med);
+        std::nth_element(col.begin(), col.begin() + col.size() / 2, col.end());
+        const double mad = 1.4826 * col[col.size() / 2];
         const double m = ts[q] / nodes;
-        z->scales.tm[q] = (float)m;
-        z->scales.ts[q] = (float)spread(tq[q], m, nodes);
+        z->scales.tm[q] = mad > 1e-20 ? med : (float)m;
+        z->scales.ts[q] = mad > 1e-20 ? (float)mad : (float)spread(tq[q], m, nodes);
     }
     auto rms = [](double q, long long k) { return q > 1e-30 && k ? (float)std::sqrt(q / k) : 1.0f; };
     z->scales.er = rms(rq, edges);
@@ -1724,7 +1736,7 @@ bcs_status bcs_surrogate_create(bcs_sim* s, const bcs_surrogate_desc* d, bcs_sur
     *out = nullptr;
     if (d->cell_type < 0 || d->cell_type >= (int)s->types.size() || d->substeps < 2 ||
         d->substeps > BCS_MAX_SUBSTEPS || d->layers < 1 || d->layers > kMaxLayers || d->max_samples < 1 ||
-        d->tolerance < 0.f)
+        d->tolerance < 0.f || d->huber_delta < 0.f)
         return BCS_ERR_INVALID_ARGUMENT;
     const TypeDev& t0 = s->types[d->cell_type];
     if (t0.pic > 6 * 32) return BCS_ERR_UNSUPPORTED;
@@ -1772,6 +1784,7 @@ bcs_status bcs_surrogate_create(bcs_sim* s, const bcs_surrogate_desc* d, bcs_sur
     if (z->net.init(d->layers, t0.pic, off.data(), nbr.data(), len.data(), z->infer_cells, d->seed, s->stream) !=
         (int)cudaSuccess)
         return BCS_ERR_OUT_OF_MEMORY;
+    z->net.set_huber(d->huber_delta);
     z->capacity = d->max_samples;
     if (!z->alloc(&z->d_cell_type, z->cells) || !z->alloc(&z->d_cell_index, z->cells) ||
         !z->alloc(&z->raw, (size_t)z->cells * z->pic * 16) || !z->alloc(&z->start, (size_t)z->cells * z->pic * 3) ||

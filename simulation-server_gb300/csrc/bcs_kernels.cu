@@ -1079,11 +1079,12 @@ __global__ void k_lattice_place(const StepArgs a, int scene, float4* pos, float4
 constexpr int kFusedHP = kHidden + 4;   // FP32 row stride of h
 constexpr int kFusedBP = kHidden + 8;   // bf16 row stride
 constexpr int kFusedW = 2176;           // floats of the small-weight area
+constexpr int kFusedMaxEdges = 1536;    // directed springs of one cell held in shared memory
 
 template <int MT>
 constexpr int fused_smem_bytes() {
     return MT * 16 * kFusedHP * 4 + MT * 16 * kFusedBP * 2 + kHidden * kFusedBP * 2 + MT * 16 * kEdgeIn * 4 +
-           kFusedW * 4 + MT * 16 * kOut * 4 + 16;
+           kFusedW * 4 + MT * 16 * kOut * 4 + 16 + (MT * 16 + 1) * 4 + kFusedMaxEdges * 4;
 }
 
 __device__ inline void stage_weight(const __nv_bfloat16* __restrict__ Wt, __nv_bfloat16* Ws, int nthreads) {
@@ -1143,11 +1144,15 @@ __global__ void __launch_bounds__(MT * 32, 1)
     float* Wsm = Node + R * 8;
     float* Ysm = Wsm + kFusedW;
     int* red = reinterpret_cast<int*>(Ysm + R * kOut);
+    int* Goff = red + 4;            // R + 1 spring-list offsets (rows past the cell: empty)
+    int* Gnbr = Goff + R + 1;       // the cell's directed springs
     const int b = blockIdx.x;
     if (b >= cells) return;
     const int sc_i = first + b, pic = d.pic;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
     const int r_lo = warp * 16 + g;
+    for (int i = tid; i <= R; i += NT) Goff[i] = goff[min(i, pic)];
+    for (int i = tid; i < goff[pic]; i += NT) Gnbr[i] = gnbr[i];
 
     // ---- encoder, and the mean edge features of every node
     float* F0 = reinterpret_cast<float*>(Bs);   // R x 16 normalised features, then R x 6 raw r, u
@@ -1164,12 +1169,19 @@ __global__ void __launch_bounds__(MT * 32, 1)
         red[2] = 0;   // leaves the vein
     }
     __syncthreads();
-    for (int i = tid; i < R * kHidden; i += NT) {
-        const int r = i >> 7, c = i & (kHidden - 1);
-        float z = Wsm[kFeatIn * kHidden + c];
+    for (int i = tid; i < R * (kHidden / 4); i += NT) {
+        const int r = i >> 5, c0 = (i & 31) * 4;
+        float fr[kFeatIn];
 #pragma unroll
-        for (int q = 0; q < kFeatIn; ++q) z = fmaf(F0[r * 16 + q], Wsm[q * kHidden + c], z);
-        Hs[r * kFusedHP + c] = r < pic ? silu_f(z) : 0.f;
+        for (int q = 0; q < kFeatIn; ++q) fr[q] = F0[r * 16 + q];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = c0 + j;
+            float z = Wsm[kFeatIn * kHidden + c];
+#pragma unroll
+            for (int q = 0; q < kFeatIn; ++q) z = fmaf(fr[q], Wsm[q * kHidden + c], z);
+            Hs[r * kFusedHP + c] = r < pic ? silu_f(z) : 0.f;
+        }
     }
     __syncthreads();
     float* RU = F0;   // raw r, u of every node (stride 6) while Bs is free
@@ -1181,10 +1193,10 @@ __global__ void __launch_bounds__(MT * 32, 1)
     for (int r = tid; r < R; r += NT) {
         float eb[kEdgeIn] = {};
         if (r < pic) {
-            const int e0 = goff[r], e1 = goff[r + 1];
+            const int e0 = Goff[r], e1 = Goff[r + 1];
             for (int k = e0; k < e1; ++k) {
                 float e[kEdgeIn];
-                spring_features(RU + r * 6, RU + gnbr[k] * 6, glen[k], sc, e);
+                spring_features(RU + r * 6, RU + Gnbr[k] * 6, glen[k], sc, e);
 #pragma unroll
                 for (int q = 0; q < kEdgeIn; ++q) eb[q] += e[q];
             }
@@ -1231,7 +1243,20 @@ __global__ void __launch_bounds__(MT * 32, 1)
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int r = r_lo + 8 * h;
-            const int e0 = r < pic ? goff[r] : 0, e1 = r < pic ? goff[r + 1] : 0;
+            const int e0 = Goff[r], e1 = Goff[r + 1];
+#pragma unroll
+            for (int nt = 0; nt < 16; ++nt) m[nt][2 * h] = m[nt][2 * h + 1] = 0.f;
+#pragma unroll
+            for (int half = 0; half < 2; ++half)
+                for (int k = e0; k < e1; ++k) {
+                    const __nv_bfloat16* bj = Bs + Gnbr[k] * kFusedBP + 2 * t + half * 64;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162*>(bj + q * 8);
+                        m[half * 8 + q][2 * h] += __low2float(v);
+                        m[half * 8 + q][2 * h + 1] += __high2float(v);
+                    }
+                }
             const float inv = 1.0f / (float)max(1, e1 - e0);
             const float* eb = Node + r * kEdgeIn;
 #pragma unroll
@@ -1239,12 +1264,10 @@ __global__ void __launch_bounds__(MT * 32, 1)
 #pragma unroll
                 for (int u = 0; u < 2; ++u) {
                     const int c = nt * 8 + 2 * t + u;
-                    float acc = 0.f;
-                    for (int k = e0; k < e1; ++k) acc += __bfloat162float(Bs[gnbr[k] * kFusedBP + c]);
                     float tt = be[c];
 #pragma unroll
                     for (int q = 0; q < kEdgeIn; ++q) tt = fmaf(eb[q], We[q * kHidden + c], tt);
-                    m[nt][2 * h + u] = r < pic ? acc * inv + tt : 0.f;
+                    m[nt][2 * h + u] = r < pic ? m[nt][2 * h + u] * inv + tt : 0.f;
                 }
         }
         __syncthreads();   // every read of B is done
@@ -1284,6 +1307,7 @@ __global__ void __launch_bounds__(MT * 32, 1)
     for (int i = tid; i < pic * kOut; i += NT) {
         const int r = i / kOut, o = i - r * kOut;
         float y = 0.f;
+#pragma unroll 8
         for (int c = 0; c < kHidden; ++c) y = fmaf(Hs[r * kFusedHP + c], Wsm[c * kOut + o], y);
         Ysm[i] = y + P[L.b_out + o];
     }

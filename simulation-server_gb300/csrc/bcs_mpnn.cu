@@ -333,14 +333,23 @@ __global__ void k_decode(const float* __restrict__ H, const __nv_bfloat16* __res
     }
 }
 
-// Loss mean((y - t)^2) and dY = 2 (y - t) / count; loss summed into *loss.
-__global__ void k_loss(const float* __restrict__ Y, const float* __restrict__ T, float* dY, float* loss, int count) {
+// Loss and dY: delta = 0 mean((y - t)^2), dY = 2 (y - t) / count; delta > 0
+// the pseudo-Huber mean(delta^2 (sqrt(1 + (d/delta)^2) - 1)), dY = d /
+// sqrt(1 + (d/delta)^2) / count.  The loss is summed into *loss.
+__global__ void k_loss(const float* __restrict__ Y, const float* __restrict__ T, float* dY, float* loss, int count,
+                       float delta) {
     float acc = 0.f;
     const float sc = 2.0f / (float)count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const float d = Y[i] - T[i];
-        dY[i] = sc * d;
-        acc += d * d;
+        if (delta > 0.f) {
+            const float q = sqrtf(1.0f + (d / delta) * (d / delta));
+            dY[i] = d / q / (float)count;
+            acc += delta * delta * (q - 1.0f);
+        } else {
+            dY[i] = sc * d;
+            acc += d * d;
+        }
     }
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
@@ -591,7 +600,7 @@ void MpnnNet::backward(const float* T, int cells) {
     const size_t nh = (size_t)n * kHidden;
     cudaMemsetAsync(g_, 0, sizeof(float) * L_.total, st_);
     cudaMemsetAsync(loss_, 0, sizeof(float), st_);
-    k_loss<<<grid_for((long long)n * kOut, 256, 1024), 256, 0, st_>>>(y_, T, dy_, loss_, n * kOut);
+    k_loss<<<grid_for((long long)n * kOut, 256, 1024), 256, 0, st_>>>(y_, T, dy_, loss_, n * kOut, huber_);
     const int rgrid = grid_for((long long)n * 32, 256, 1216);
     k_decode_bwd<<<rgrid, 256, 0, st_>>>(h_[L_.layers], pb_ + L_.w_out, dy_, dh_, g_ + L_.w_out, g_ + L_.b_out, n);
     for (int l = L_.layers - 1; l >= 0; --l) {

@@ -93,6 +93,7 @@ public:
     void backward(const float* T, int cells);
     void adam(float lr);
     void refresh_bf16();
+    void set_huber(float delta) { huber_ = delta; }
     float* params() { return p_; }
     float* grad() { return g_; }
     float* output() { return y_; }
@@ -124,6 +125,7 @@ private:
     __nv_bfloat16 *pb_ = nullptr, *pbt_ = nullptr;
     long long* sq_ = nullptr;
     int nsq_ = 0, t_adam_ = 0;
+    float huber_ = 0.f;
     float *f_ = nullptr, *e_ = nullptr, *t_ = nullptr, *y_ = nullptr, *dy_ = nullptr, *loss_ = nullptr;
     const float *last_f_ = nullptr, *last_e_ = nullptr;   // inputs of the last forward
     float *z0_ = nullptr, *dh_ = nullptr, *db_ = nullptr, *dm_ = nullptr, *dz_ = nullptr;

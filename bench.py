@@ -65,6 +65,27 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest of every rank's x (the slowest rank's time); x itself on
+    one rank.  Works with the process group's backend (NCCL on GPUs, gloo
+    on CPUs)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(particles_per_rank: int, steps: int, ms_per_rank: float, world: int) -> float:
+    """particle-steps/s of the whole job: every rank's particle-steps over
+    the slowest rank's time (weak scaling, one replica per rank)."""
+    ms = max_over_ranks(ms_per_rank)
+    return world * particles_per_rank * steps / (ms / 1e3)
+
+
 class ClockSampler:
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -383,11 +404,8 @@ def run_ours(args):
     ms = sim.time_steps(args.steps)
     clocks = sampler.stop()
     barrier(sim)
-    t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = ws * n * args.steps / (ms_max / 1e3)
+    ms_max = max_over_ranks(ms)
+    value = whole_job_rate(n, args.steps, ms, ws)
     info = sim.refresh_info()
     launches = info.kernels_per_step * args.steps
     diag = grid_diagnostics(sim)
@@ -431,10 +449,7 @@ def run_ours(args):
         assert lib.bcs_get_particles(sim.h, out, bcs.Vec3(), bcs.Vec3(), bcs.MEM_HOST) == 0
     e2e_s = time.perf_counter() - t0
     sim.close()
-    e2e_t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-    if ws > 1:
-        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = ws * n * e2e_steps / float(e2e_t.item())
+    e2e_value = whole_job_rate(n, e2e_steps, 1e3 * e2e_s, ws)
 
     learned = None
     if rank == 0 and not args.no_learned and not batched:

@@ -48,3 +48,23 @@ def test_bifurcation_small():
     assert sc.particle_count == 300 * 42 + 300 * 162
     assert len(sc.flow_segments) == 3
     assert len(sc.ending_radii) == 2
+
+
+def test_batched_scenes_generator():
+    scs = S.batched_scenes(4, seed=3, min_cells=20, max_cells=200, min_length=60.0, max_length=120.0)
+    assert len(scs) == 4
+    for sc in scs:
+        n = sum(t.count for t in sc.types)
+        assert 20 <= n <= 200
+        L = -float(sc.vein_positions[:, 1].min())
+        assert 60.0 <= L <= 120.0 + 1e-3
+        assert len(sc.positions) == sum(t.count * len(t.vertices) for t in sc.types)
+        # every cell inside the vessel radius
+        r = np.hypot(sc.positions[:, 0], sc.positions[:, 2])
+        assert r.max() < sc.params.cylinder_radius
+
+
+def test_mixed_scene_grows_radius_to_fit():
+    sc = S.mixed_straight_scene(400, 300, 60.0, seed=1, base_radius=10.0)
+    assert sc.params.cylinder_radius > 10.0
+    assert [t.count for t in sc.types] == [400, 300]

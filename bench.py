@@ -385,6 +385,17 @@ def run_ours(args):
         sim.step(args.warmup)
         return sim
 
+    if args.learned_only:
+        # the learned sub-step pass alone (profiling); the plain tuning is the default
+        sim = fresh()
+        tuning = sim.get_tuning().as_dict()
+        sim.close()
+        learned = learned_substep(args, scene, tuning, bcs, fresh, args.warmup)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unit": UNIT, "learned_substep": learned,
+                              "config": workload_config(scene, ws)}), flush=True)
+        return 0
+
     # ---- pass 1: the timed run (graph replay, state resident in HBM)
     sim = fresh()
     n = sim.n
@@ -513,6 +524,7 @@ def main():
     ap.add_argument("--autotune-frames", type=int, default=3)
     ap.add_argument("--tuning", default="", help="comma-separated bcs_tuning fields instead of the autotuner")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned sub-step measurements")
+    ap.add_argument("--learned-only", action="store_true", help="only the learned sub-step pass (profiling)")
     ap.add_argument("--workload", default="bifurcation", choices=["bifurcation", "batched"],
                     help="bifurcation: the 4.2M-particle metric workload; batched: 64 straight vessels")
     ap.add_argument("--batch-scenes", type=int, default=64)

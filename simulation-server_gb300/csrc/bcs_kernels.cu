@@ -133,105 +133,87 @@ __device__ inline void stencil_range_u(unsigned id, int count, int& lo, int& hi)
 __device__ inline unsigned to_u32_sat(float t) { return t <= 0.f ? 0u : (t >= 4294967040.f ? 0xFFFFFFFFu : (unsigned)t); }
 
 // calculateParticleCollisions<UniformGrid> (particle_collisions.cuh:26-38,
-// 53-83,104-269), split for the row-parallel step kernel:
-//  * collision_cell: the particle's cell key (the same FP32 quotients as
-//    calculateIdForCell) and its stencil bounds, packed in an int2;
-//  * collision_row: the forces of one stencil row (dz, dy) — its three
-//    cells are consecutive keys, so their occupied slots form one
-//    contiguous sorted range;
-//  * collision_scan: grid "none", every particle of the scene.
-// One candidate is detectCollision's test, then the resilient force with the
-// neighbour's velocity (fetched only on a hit).
-__device__ inline int2 collision_cell(const GridGeom& geo, float3 x) {
+// 53-83,104-269) for one particle; the 3 cells of a stencil row are
+// consecutive keys, so each row is one contiguous range of sorted slots.
+__device__ inline float3 particle_collisions(const StepArgs& a, const SceneDev& sc, int pid, float3 x, float3 v,
+                                            float R, unsigned& e) {
+    float3 acc = f3(0.f, 0.f, 0.f);
+    const GridDev& g = a.pg;
+    const GridGeom& geo = sc.pg;
+    // One candidate: detectCollision's test, then the resilient force with
+    // the neighbour's velocity (fetched only on a hit).
+    auto consider = [&](const float4 pq, auto neighbour) {
+        const float3 rp = x - xyz(pq);
+        const float d2 = dot3(rp, rp);
+        const float md = R + pq.w;
+        if (d2 <= md * md && d2 >= 0.0001f)
+            acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[neighbour()])), d2, R, 0.5f, e);
+    };
+    auto test = [&](int q) { consider(__ldg(&a.pos_in[q]), [q] { return q; }); };
+    if (!g.uniform) {
+        for (int q = sc.particle_start; q < sc.particle_end; ++q)
+            if (q != pid) test(q);
+        return acc;
+    }
+    const int ep = __ldg(g.epoch);
     const float tx = axis_quotient(x.x, geo.lo[0], geo.cell[0]);
     const float ty = axis_quotient(x.y, geo.lo[1], geo.cell[1]);
     const float tz = axis_quotient(x.z, geo.lo[2], geo.cell[2]);
+    const int cellId = key_of_quotients(geo, tx, ty, tz);
     int x0, x1, y0, y1, z0, z1;
     stencil_range((int)tx, geo.cx, x0, x1);
     stencil_range((int)ty, geo.cy, y0, y1);
     stencil_range((int)tz, geo.cz, z0, z1);
-    const int flags = (x0 < 0) | ((x1 > 0) << 1) | ((y0 < 0) << 2) | ((y1 > 0) << 3) | ((z0 < 0) << 4) | ((z1 > 0) << 5);
-    return make_int2(key_of_quotients(geo, tx, ty, tz), flags);
-}
-
-struct CollisionTerm {
-    const StepArgs& a;
-    float3 x, v;
-    float R;
-    unsigned& e;
-    __device__ inline void consider(float3& acc, const float4 pq, int q) const {
-        const float3 rp = x - xyz(pq);
-        const float d2 = dot3(rp, rp);
-        const float md = R + pq.w;
-        if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[q])), d2, R, 0.5f, e);
-    }
-};
-
-__device__ inline float3 collision_row(const StepArgs& a, const SceneDev& sc, int pid, const CollisionTerm& ct,
-                                       int2 cell, int dz, int dy) {
-    float3 acc = f3(0.f, 0.f, 0.f);
-    const int f = cell.y;
-    const int x0 = (f & 1) ? -1 : 0, x1 = (f & 2) ? 1 : 0, y0 = (f & 4) ? -1 : 0, y1 = (f & 8) ? 1 : 0,
-              z0 = (f & 16) ? -1 : 0, z1 = (f & 32) ? 1 : 0;
-    if (dz < z0 || dz > z1 || dy < y0 || dy > y1) return acc;
-    const GridDev& g = a.pg;
-    const GridGeom& geo = sc.pg;
     const long long cxy = (long long)geo.cx * geo.cy;
-    const long long row = (long long)cell.x + dz * cxy + (long long)dy * geo.cx;
     const int4* __restrict__ table = g.table + geo.key_offset;
-    int first = 0x7fffffff, last = -1;
-    if (g.occ) {
-        // Occupied cells of the window from the bitmap: only the first and
-        // the last occupied entries are loaded.
-        const long long ca = max(row + x0, 0LL), cb = min(row + x1, geo.cells - 1);
-        if (ca > cb) return acc;
-        const long long ga = geo.key_offset + ca, gb = geo.key_offset + cb;
-        const int sh = (int)(ga & 31);
-        unsigned long long m = __ldg(&g.occ[ga >> 5]) >> sh;
-        if ((gb >> 5) != (ga >> 5)) m |= (unsigned long long)__ldg(&g.occ[gb >> 5]) << (32 - sh);
-        m &= (1ull << (int)(cb - ca + 1)) - 1ull;
-        if (!m) return acc;
-        const int lo = __ffsll((long long)m) - 1, hi = 63 - __clzll((long long)m);
-        const int4 r = __ldg(&table[ca + lo]);
-        first = r.x;
-        last = hi != lo ? __ldg(&table[ca + hi]).y : r.y;
-    } else {
-        const int ep = __ldg(g.epoch);
+    for (int dz = z0; dz <= z1; ++dz)
+        for (int dy = y0; dy <= y1; ++dy) {
+            const long long row = (long long)cellId + dz * cxy + (long long)dy * geo.cx;
+            // The row's three cells are consecutive keys, so their occupied
+            // slots form one contiguous sorted range; the three entries are
+            // loaded together.
+            int first = 0x7fffffff, last = -1;
+            if (g.occ) {
+                // Occupied cells of the window from the bitmap: only the
+                // first and the last occupied entries are loaded.
+                const long long ca = max(row + x0, 0LL), cb = min(row + x1, geo.cells - 1);
+                if (ca > cb) continue;
+                const long long ga = geo.key_offset + ca, gb = geo.key_offset + cb;
+                const int sh = (int)(ga & 31);
+                unsigned long long m = __ldg(&g.occ[ga >> 5]) >> sh;
+                if ((gb >> 5) != (ga >> 5)) m |= (unsigned long long)__ldg(&g.occ[gb >> 5]) << (32 - sh);
+                m &= (1ull << (int)(cb - ca + 1)) - 1ull;
+                if (!m) continue;
+                const int lo = __ffsll((long long)m) - 1, hi = 63 - __clzll((long long)m);
+                const int4 r = __ldg(&table[ca + lo]);
+                first = r.x;
+                last = hi != lo ? __ldg(&table[ca + hi]).y : r.y;
+            } else {
 #pragma unroll
-        for (int dx = -1; dx <= 1; ++dx) {
-            const long long c = row + dx;
-            if (dx >= x0 && dx <= x1 && c >= 0 && c < geo.cells) {
-                const int4 r = __ldg(&table[c]);
-                if (r.z == ep) {
-                    first = min(first, r.x);
-                    last = max(last, r.y);
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const long long c = row + dx;
+                    if (dx >= x0 && dx <= x1 && c >= 0 && c < geo.cells) {
+                        const int4 r = __ldg(&table[c]);
+                        if (r.z == ep) {
+                            first = min(first, r.x);
+                            last = max(last, r.y);
+                        }
+                    }
+                }
+            }
+            if (g.spos) {
+                // Sorted positions: contiguous loads; the particle itself
+                // (d2 = 0) fails the d2 >= 1e-4 test, so no id is needed
+                // before a hit.
+                for (int j = first; j <= last; ++j)
+                    consider(__ldg(&g.spos[j]), [&g, j] { return __ldg(&g.ids[j]); });
+            } else {
+                for (int j = first; j <= last; ++j) {
+                    const int q = __ldg(&g.ids[j]);
+                    if (q != pid) test(q);
                 }
             }
         }
-    }
-    if (g.spos) {
-        // Sorted positions: contiguous loads; the particle itself (d2 = 0)
-        // fails the d2 >= 1e-4 test, so no id is needed before a hit.
-        for (int j = first; j <= last; ++j) {
-            const float4 pq = __ldg(&g.spos[j]);
-            const float3 rp = ct.x - xyz(pq);
-            const float d2 = dot3(rp, rp);
-            const float md = ct.R + pq.w;
-            if (d2 <= md * md && d2 >= 0.0001f) ct.consider(acc, pq, __ldg(&g.ids[j]));
-        }
-    } else {
-        for (int j = first; j <= last; ++j) {
-            const int q = __ldg(&g.ids[j]);
-            if (q != pid) ct.consider(acc, __ldg(&a.pos_in[q]), q);
-        }
-    }
-    return acc;
-}
-
-__device__ inline float3 collision_scan(const StepArgs& a, const SceneDev& sc, int pid, const CollisionTerm& ct) {
-    float3 acc = f3(0.f, 0.f, 0.f);
-    for (int q = sc.particle_start; q < sc.particle_end; ++q)
-        if (q != pid) ct.consider(acc, __ldg(&a.pos_in[q]), q);
     return acc;
 }
 
@@ -410,10 +392,9 @@ constexpr int kForces = 1;  // calculateNextFrame only: forces and collision vel
 
 // One work item: stage the cells, then per particle springs, environment,
 // collisions, the vein ray and (MODE kFull) integration and next keys.
-template <int MODE, int THREADS, int CHUNK>
+template <int MODE, int THREADS>
 __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, float4* s_vel, float4* s_frc,
-                                 int2* s_cell, float3* s_cent, SceneDev& sc) {
-    constexpr int kPer = CHUNK / THREADS;   // particles per thread in the per-particle phases
+                                 float3* s_cent, SceneDev& sc) {
     const WorkItem w = a.work[item];
     const TypeDev ty = a.types[w.type];
     const int pic = ty.pic;
@@ -443,18 +424,13 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
     }
     __syncthreads();
 
-    // Phase A, per particle: intra-cell springs (gatherForcesKernel,
-    // blood_cells.cu:66-120, over the CSR form of the dense spring graph in
-    // the same ascending order), environment, the average with the previous
-    // force, and the particle's collision cell.
     unsigned e = 0;
-    float3 favg[kPer];
-#pragma unroll
-    for (int r = 0; r < kPer; ++r) {
-        const int i = threadIdx.x + r * THREADS;
-        if (i >= np) continue;
-        const int c = i / pic, li = i - c * pic;
-        const float3 x = xyz(s_pos[i]), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
+    for (int i = threadIdx.x; i < np; i += THREADS) {
+        const int c = i / pic, li = i - c * pic, pid = p0 + i;
+        const float4 px = s_pos[i];
+        const float3 x = xyz(px), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
+        // Intra-cell springs, gatherForcesKernel (blood_cells.cu:66-120) over
+        // the CSR form of the dense spring graph (same ascending order).
         float3 F = f3(0.f, 0.f, 0.f);
         const int e0 = __ldg(&a.adj_off[ty.adj_start + li]), e1 = __ldg(&a.adj_off[ty.adj_start + li + 1]);
         const int cb = c * pic;
@@ -464,58 +440,10 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
         }
         const float ratio = len3(x - s_cent[c]) / __ldg(&a.r0[ty.model_start + li]);
         F = F + environment(a, sc, x, v, ratio);
-        favg[r] = (fprev + F) / 2.0f;
-        if (a.pg.uniform) s_cell[i] = collision_cell(sc.pg, x);
-    }
-    __syncthreads();   // every read of the previous forces is done
-#pragma unroll
-    for (int r = 0; r < kPer; ++r) {
-        const int i = threadIdx.x + r * THREADS;
-        if (i < np) s_frc[i] = make_float4(favg[r].x, favg[r].y, favg[r].z, 0.f);
-    }
-    __syncthreads();
-
-    // Phase B, per stencil row: nine lanes per particle, three particles per
-    // warp; lane 9s + k walks row k (dz = k / 3 - 1, dy = k % 3 - 1) of
-    // particle s, and the rows' forces are summed in row order onto lane 9s.
-    {
-        const int seg = lane / 9, rr = lane - 9 * seg;
-        for (int base = warp * 3; base < np; base += (THREADS / 32) * 3) {
-            const int i = base + seg;
-            const bool act = lane < 27 && i < np;
-            float3 acc = f3(0.f, 0.f, 0.f);
-            if (act) {
-                const float4 px = s_pos[i];
-                const CollisionTerm ct{a, xyz(px), xyz(s_vel[i]), px.w, e};
-                if (a.pg.uniform) acc = collision_row(a, sc, p0 + i, ct, s_cell[i], rr / 3 - 1, rr % 3 - 1);
-                else if (rr == 0) acc = collision_scan(a, sc, p0 + i, ct);
-            }
-            float3 tot = acc;
-#pragma unroll
-            for (int k = 1; k < 9; ++k) {
-                const int src = lane < 27 ? 9 * seg + k : lane;
-                tot.x += __shfl_sync(0xffffffffu, acc.x, src);
-                tot.y += __shfl_sync(0xffffffffu, acc.y, src);
-                tot.z += __shfl_sync(0xffffffffu, acc.z, src);
-            }
-            if (act && rr == 0) {
-                const float4 f = s_frc[i];
-                s_frc[i] = make_float4(f.x + tot.x, f.y + tot.y, f.z + tot.z, 0.f);
-            }
-        }
-    }
-    __syncthreads();
-
-    // Phase C, per particle: the vein ray, integration, the state and the
-    // next frame's grid keys.
-#pragma unroll
-    for (int r = 0; r < kPer; ++r) {
-        const int i = threadIdx.x + r * THREADS;
-        if (i >= np) continue;
-        const int pid = p0 + i;
-        const float4 px = s_pos[i];
-        const float3 x = xyz(px), v = xyz(s_vel[i]);
-        float3 F = xyz(s_frc[i]);
+        F = (fprev + F) / 2.0f;
+        const float3 favg = F;
+        // Particle-particle collisions.
+        F = F + particle_collisions(a, sc, pid, x, v, px.w, e);
         // Particle-vein collision.
         float3 vv = v;
         vein_collision(a, sc, x, vv, F, px.w, e);
@@ -538,7 +466,7 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
         }
         if (MODE == kFull && a.fext) {
             // macro step: the external part of this force, held by sub-steps 2..K
-            const float3 fx = F - favg[r];
+            const float3 fx = F - favg;
             a.fext[pid] = make_float4(fx.x, fx.y, fx.z, 0.f);
         }
     }
@@ -550,15 +478,13 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
 // counter for the next launch, so the launch replays from a CUDA graph.
 template <int MODE, int THREADS, int CHUNK, int MINB, bool PERSIST>
 __global__ void __launch_bounds__(THREADS, MINB) k_step(const StepArgs a) {
-    static_assert(CHUNK == 2 * THREADS, "the per-particle phases hold two particles per thread");
     __shared__ float4 s_pos[CHUNK];
     __shared__ float4 s_vel[CHUNK];
     __shared__ float4 s_frc[CHUNK];
-    __shared__ int2 s_cell[CHUNK];
     __shared__ float3 s_cent[kMaxCellsPerChunk];
     __shared__ SceneDev sc;
     if (!PERSIST) {
-        step_item<MODE, THREADS, CHUNK>(a, blockIdx.x, s_pos, s_vel, s_frc, s_cell, s_cent, sc);
+        step_item<MODE, THREADS>(a, blockIdx.x, s_pos, s_vel, s_frc, s_cent, sc);
         return;
     }
     __shared__ int s_item;
@@ -567,7 +493,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step(const StepArgs a) {
         __syncthreads();
         const int item = s_item;
         if (item >= a.work_count) break;
-        step_item<MODE, THREADS, CHUNK>(a, item, s_pos, s_vel, s_frc, s_cell, s_cent, sc);
+        step_item<MODE, THREADS>(a, item, s_pos, s_vel, s_frc, s_cent, sc);
         __syncthreads();   // shared buffers and s_item are reused
     }
     if (threadIdx.x == 0 && atomicAdd(&a.work_counter[1], 1) == (int)gridDim.x - 1) {

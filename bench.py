@@ -244,14 +244,28 @@ def run_reference(args):
 
 
 def grid_diagnostics(sim):
-    """Occupancy of the particle grid and the error word after a run."""
-    keys, _, _, _ = sim.get_grid(0, dense=False)
+    """Occupancy of the particle grid, where its most crowded cell lies,
+    particles outside the grid box, speeds, and the error word after a run."""
+    keys, ids, _, _ = sim.get_grid(0, dense=False)
     if len(keys) == 0:
         return {}
     change = np.flatnonzero(np.diff(keys)) + 1
-    runs = np.diff(np.concatenate([[0], change, [len(keys)]]))
+    starts = np.concatenate([[0], change])
+    runs = np.diff(np.concatenate([starts, [len(keys)]]))
+    pos, vel, _ = sim.get_particles()
+    info = sim.info
+    lo = np.array([info.min_x, info.min_y, info.min_z], np.float32)
+    hi = np.array([info.max_x, info.max_y, info.max_z], np.float32)
+    outside = ~np.all((pos >= lo) & (pos <= hi), axis=1)
+    k = int(np.argmax(runs))
+    crowded = pos[ids[starts[k]:starts[k] + runs[k]]]
+    speed = np.linalg.norm(vel, axis=1)
     return {"occupied_cells": int(len(runs)), "max_particles_per_cell": int(runs.max()),
             "mean_particles_per_occupied_cell": round(float(runs.mean()), 3),
+            "cells_with_over_8_particles": int((runs > 8).sum()),
+            "most_crowded_cell_centre": [round(float(v), 2) for v in crowded.mean(0)],
+            "particles_outside_grid_box": int(outside.sum()),
+            "speed_median": round(float(np.median(speed)), 3), "speed_max": round(float(speed.max()), 3),
             "error_word": sim.error_word()}
 
 

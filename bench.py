@@ -324,8 +324,13 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     ms_plain = sim.time_steps(K * M)
     pa = sim.get_particles()[0]
     sim.close()
+    def timed(sim):
+        """M macro steps, each timed alone (CUDA events, graph replay)."""
+        per = [sim.time_macro_steps(K, 1) for _ in range(M)]
+        return float(sum(per)), {f"p{q}": float(np.percentile(per, q)) for q in (50, 95, 99)}
+
     sim = fresh(tuning)
-    ms_macro = sim.time_macro_steps(K, M)
+    ms_macro, lat_macro = timed(sim)
     pb = sim.get_particles()[0]
     sim.close()
     sim = fresh(tuning)
@@ -333,7 +338,7 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     s2.set_params(params)
     s2.set_scales(scales)
     s2.enable(True)
-    ms_sur = sim.time_macro_steps(K, M)
+    ms_sur, lat_sur = timed(sim)
     pc = sim.get_particles()[0]
     st = s2.stats()
     s2.close()
@@ -349,8 +354,9 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
         "substeps": K, "macro_steps": M, "simulated_time": K * M * float(scene.params.dt),
         "plain": {"ms": ms_plain, "particle_steps_per_s": rate(ms_plain)},
         "macro_plain": {"ms": ms_macro, "particle_steps_per_s": rate(ms_macro), "position_error": err(pb),
-                        "one_macro_step_error": err(pb1, pa1)},
+                        "one_macro_step_error": err(pb1, pa1), "macro_step_latency_ms": lat_macro},
         "surrogate": {"ms": ms_sur, "particle_steps_per_s": rate(ms_sur), "position_error": err(pc),
+                      "macro_step_latency_ms": lat_sur,
                       "one_macro_step_error": err(pc1, pa1),
                       "cells_predicted": st["predicted_cells"], "cells_fallen_back": st["fallback_cells"],
                       "tolerance": st["tolerance"]},

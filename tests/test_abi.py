@@ -5,6 +5,8 @@ import os
 import re
 import subprocess
 
+import numpy as np
+
 import bcs
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -108,3 +110,17 @@ def test_constants_match_header():
     text = open(os.path.join(REPO, "include", "bcs.h")).read()
     assert f"#define BCS_MAX_SUBSTEPS {bcs.MAX_SUBSTEPS}" in text
     assert f"#define BCS_GRID_SORT_STATIC_MAX {bcs.GRID_SORT_STATIC_MAX}" in text
+
+
+def test_cell_model_too_large_rejected(lib):
+    import bcs_scenes
+    sc = bcs_scenes.tiny_scene(cells=1)
+    m = bcs_scenes.sphere_cell(8.0, 4)         # 2562 vertices: no launch shape holds the cell
+    sc.types[0].vertices = m.vertices
+    sc.types[0].springs = m.springs
+    sc.types[0].spring_lengths = m.spring_lengths
+    sc.types[0].collision_radius = np.full(len(m.vertices), 0.5, np.float32)
+    buf = bcs.SceneBuffers(sc)
+    h = C.c_void_p()
+    assert lib.bcs_create(C.byref(buf.desc), None, C.byref(h)) == 5   # BCS_ERR_UNSUPPORTED
+    assert not h.value

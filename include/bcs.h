@@ -433,6 +433,15 @@ bcs_status bcs_surrogate_forward(bcs_surrogate* sur, int cells, const float* fea
  * T^2/2 F_1 that it corrects (*base_error), against the plain sub-steps. */
 bcs_status bcs_surrogate_evaluate(bcs_surrogate* sur, int first, int count, double* net_error,
                                   double* base_error);
+/* Tensor-core instructions of the network's 128 x 128 products (training
+ * and layer-by-layer inference): 0 = tcgen05 with tensor-memory
+ * accumulators (the default; BCS_TENSOR_PATH=1 in the environment starts
+ * with mma.sync), 1 = mma.sync.  Returns the previous setting,
+ * or -1 for an invalid value.  bcs_tensor_wait_expiries counts tcgen05
+ * completions that were not seen within the kernel's bounded wait (the
+ * product is then skipped, not stalled). */
+int bcs_set_tensor_path(int path);
+unsigned bcs_tensor_wait_expiries(void);
 /* The normalisation derived from the training set: 53 floats (feature means
  * [16], feature 1/std [16], target medians [9], target robust spreads [9]
  * (1.4826 x the median absolute deviation), edge scales of position,

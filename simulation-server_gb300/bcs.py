@@ -34,7 +34,7 @@ EXPORTED = [
     "bcs_surrogate_enable", "bcs_surrogate_get_stats", "bcs_surrogate_reset_stats", "bcs_surrogate_param_count",
     "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
     "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales", "bcs_time_macro_steps",
-    "bcs_init_particles",
+    "bcs_init_particles", "bcs_set_tensor_path", "bcs_tensor_wait_expiries",
 ]
 INIT_REFERENCE, INIT_LATTICE = 0, 1
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
@@ -179,6 +179,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_macro_step": ([P, C.c_int, C.c_int], C.c_int),
         "bcs_time_macro_steps": ([P, C.c_int, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "bcs_init_particles": ([P, C.POINTER(InitDesc)], C.c_int),
+        "bcs_set_tensor_path": ([C.c_int], C.c_int),
+        "bcs_tensor_wait_expiries": ([], C.c_uint),
         "bcs_surrogate_create": ([P, C.POINTER(SurrogateDesc), C.POINTER(P)], C.c_int),
         "bcs_surrogate_destroy": ([P], C.c_int),
         "bcs_surrogate_collect": ([P, C.c_int], C.c_int),
@@ -266,6 +268,15 @@ def _ptr(a) -> int | None:
 def _check(status: int, what: str) -> None:
     if status != BCS_OK:
         raise BcsError(status, what)
+
+
+def set_tensor_path(path: int) -> int:
+    """0 = tcgen05 products (default), 1 = mma.sync; returns the previous path."""
+    return int(load_library().bcs_set_tensor_path(int(path)))
+
+
+def tensor_wait_expiries() -> int:
+    return int(load_library().bcs_tensor_wait_expiries())
 
 
 def set_device(device: int) -> None:

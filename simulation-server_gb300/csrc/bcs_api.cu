@@ -265,7 +265,8 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
     dg.g.epoch = dg.epoch;
     if (dg.g.uniform) {
         if ((st = dalloc(s, &dg.table, (size_t)dg.g.cells))) return st;
-        BCS_CUDA(cudaMemset(dg.table, 0, sizeof(int4) * (size_t)dg.g.cells));
+        // every field -1: no entry matches an epoch before the grid's first build
+        BCS_CUDA(cudaMemset(dg.table, 0xFF, sizeof(int4) * (size_t)dg.g.cells));
         if (incremental) {
             const size_t words = (size_t)((dg.g.cells + 31) / 32);
             if ((st = dalloc(s, &dg.occ, words)) || (st = dalloc(s, &dg.spos, count))) return st;
@@ -1983,6 +1984,19 @@ bcs_status bcs_surrogate_evaluate(bcs_surrogate* z, int first, int count, double
     if (net_error) *net_error = h[0] / h[2];
     if (base_error) *base_error = h[1] / h[2];
     return check_last();
+}
+
+int bcs_set_tensor_path(int path) {
+    if (path != 0 && path != 1) return -1;
+    const int prev = mpnn_gemm_path();
+    mpnn_set_gemm_path(path);
+    return prev;
+}
+
+unsigned bcs_tensor_wait_expiries(void) {
+    unsigned h = 0;
+    if (cudaMemcpy(&h, mpnn_gemm_error_word(), sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 0xFFFFFFFFu;
+    return h;
 }
 
 bcs_status bcs_surrogate_set_scales(bcs_surrogate* z, const float* in) {

@@ -249,6 +249,7 @@ __device__ inline float ray_box_entry(float3 o, float3 d, float3 inv, float4 lo,
 //    the first hit, if any, is too far: no collision.
 __device__ inline void vein_collision(const StepArgs& a, const SceneDev& sc, float3 x, float3& v, float3& F,
                                       float R, unsigned& e) {
+    if (a.T == 0) return;   // no wall to hit (and no triangle grid was built)
     const bcs_params& p = a.p;
     const GridDev& g = a.tg;
     const GridGeom& geo = sc.tg;

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <type_traits>
 #include <vector>
 
@@ -442,16 +443,197 @@ __global__ void k_bf16_copies(const float* __restrict__ p, __nv_bfloat16* pb, __
     }
 }
 
+// ------------------------------------------------------------ tcgen05 ----
+// The same product on the 5th-generation tensor cores: a CTA of 128 threads
+// takes 128 rows; the bf16 operands sit in shared memory in the canonical
+// K-major layout without swizzle (core matrices of 8 rows x 16 bytes; the
+// next core matrix along K 128 bytes on, the next 8-row group 2048 bytes
+// on); one thread issues eight tcgen05.mma (M 128, N 128, K 16) per input
+// into a 128-column FP32 accumulator in tensor memory and commits them to an
+// mbarrier; the warps read their 32 rows back with tcgen05.ld.  Every wait is
+// bounded: on expiry the CTA flags the error word, waits once more (bounded)
+// and frees its tensor memory.
+constexpr int kTcTile = 128 * 128 * 2;          // bytes of one operand tile
+constexpr long long kTcWaitBound = 1LL << 24;   // mbarrier polls before giving up
+
+__device__ inline uint32_t tc_offset(int m, int k) {
+    return (uint32_t)((m >> 3) * 2048 + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ inline uint64_t tc_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)(128 >> 4) << 16;    // leading byte offset: next core matrix along K
+    d |= (uint64_t)(2048 >> 4) << 32;   // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;             // descriptor version of tcgen05
+    return d;                           // base offset 0, no swizzle
+}
+
+// kind::f16 instruction descriptor: FP32 D, bf16 A and B, both K-major, N 128, M 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ inline bool tc_wait(uint32_t mbar, uint32_t phase) {
+    for (long long i = 0; i < kTcWaitBound; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(128) k_gemm_tc(const float* __restrict__ X1, const __nv_bfloat16* __restrict__ B1,
+                                                 const float* __restrict__ X2, const __nv_bfloat16* __restrict__ B2,
+                                                 const float* __restrict__ bias, float* Y, float* Z, int rows,
+                                                 int silu, int accumulate, unsigned* err) {
+    extern __shared__ __align__(1024) unsigned char smem_tc[];
+    unsigned char* As = smem_tc;
+    unsigned char* Bs = smem_tc + kTcTile;
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int r0 = blockIdx.x * 128;
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    if (warp == 0) {
+        const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(slot) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = tmem_slot;
+    const uint32_t a_base = (uint32_t)__cvta_generic_to_shared(As), b_base = (uint32_t)__cvta_generic_to_shared(Bs);
+    bool ok = true;
+    uint32_t phase = 0;
+    for (int in = 0; in < 2; ++in) {
+        const float* X = in ? X2 : X1;
+        const __nv_bfloat16* B = in ? B2 : B1;
+        if (!X) break;
+        for (int q = tid; q < 128 * 32; q += 128) {
+            const int r = q >> 5, c = (q & 31) * 4;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r0 + r < rows) v = *reinterpret_cast<const float4*>(X + (size_t)(r0 + r) * kHidden + c);
+            uint2 pk;
+            pk.x = pack_bf16(v.x, v.y);
+            pk.y = pack_bf16(v.z, v.w);
+            *reinterpret_cast<uint2*>(As + tc_offset(r, c)) = pk;
+        }
+        for (int q = tid; q < 128 * 16; q += 128) {
+            const int n = q >> 4, k = (q & 15) * 8;
+            *reinterpret_cast<uint4*>(Bs + tc_offset(n, k)) = *reinterpret_cast<const uint4*>(B + n * kHidden + k);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int ks = 0; ks < kHidden / 16; ++ks) {
+                const uint64_t ad = tc_desc(a_base + ks * 256), bd = tc_desc(b_base + ks * 256);
+                const uint32_t acc = (in > 0 || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                    ::"r"(taddr), "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a)
+                         : "memory");
+        }
+        // the same verdict on every thread: a CTA stops issuing (and
+        // restaging the operands) as a whole
+        ok = __syncthreads_and(tc_wait(mbar_a, phase) ? 1 : 0) != 0;
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!ok) break;
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(err, 1u);
+        tc_wait(mbar_a, phase ^ 1u);
+    } else {
+        const int row = r0 + warp * 32 + lane;
+#pragma unroll
+        for (int chunk = 0; chunk < 4; ++chunk) {
+            uint32_t v[32];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(chunk * 32)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < rows) {
+#pragma unroll
+                for (int j = 0; j < 32; j += 2) {
+                    const int col = chunk * 32 + j;
+                    float v0 = __uint_as_float(v[j]) + (bias ? bias[col] : 0.f);
+                    float v1 = __uint_as_float(v[j + 1]) + (bias ? bias[col + 1] : 0.f);
+                    float* yp = Y + (size_t)row * kHidden + col;
+                    if (Z) *reinterpret_cast<float2*>(Z + (size_t)row * kHidden + col) = make_float2(v0, v1);
+                    if (silu) {
+                        v0 = silu_f(v0);
+                        v1 = silu_f(v1);
+                    }
+                    if (accumulate) {
+                        const float2 o = *reinterpret_cast<const float2*>(yp);
+                        v0 += o.x;
+                        v1 += o.y;
+                    }
+                    *reinterpret_cast<float2*>(yp) = make_float2(v0, v1);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(taddr) : "memory");
+}
+
 }  // namespace
+
+namespace {
+// 0: tcgen05, 1: mma.sync; BCS_TENSOR_PATH in the environment sets the start value
+int initial_path() {
+    const char* e = std::getenv("BCS_TENSOR_PATH");
+    return e && e[0] == '1' ? 1 : 0;
+}
+int g_gemm_path = initial_path();
+unsigned* g_gemm_err = nullptr;      // tcgen05 wait expiries (device word)
+}  // namespace
+
+void mpnn_set_gemm_path(int path) { g_gemm_path = path; }
+int mpnn_gemm_path() { return g_gemm_path; }
+unsigned* mpnn_gemm_error_word() {
+    if (!g_gemm_err) {
+        cudaMalloc(&g_gemm_err, sizeof(unsigned));
+        cudaMemset(g_gemm_err, 0, sizeof(unsigned));
+    }
+    return g_gemm_err;
+}
 
 void mpnn_gemm(const float* X1, const __nv_bfloat16* W1t, const float* X2, const __nv_bfloat16* W2t,
                const float* bias, float* Y, float* Zout, int rows, bool silu, bool accumulate, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+        cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * kTcTile);
         attr = true;
     }
     if (rows <= 0) return;
+    if (g_gemm_path == 0) {
+        k_gemm_tc<<<(rows + 127) / 128, 128, 2 * kTcTile, s>>>(X1, W1t, X2, W2t, bias, Y, Zout, rows, silu ? 1 : 0,
+                                                              accumulate ? 1 : 0, mpnn_gemm_error_word());
+        return;
+    }
     k_gemm<<<(rows + kTileRows - 1) / kTileRows, 256, kGemmSmem, s>>>(X1, W1t, X2, W2t, bias, Y, Zout, rows,
                                                                      silu ? 1 : 0, accumulate ? 1 : 0);
 }

@@ -70,6 +70,12 @@ struct MpnnGraph {
 // silu; Zout (optional) receives the pre-activation; accumulate adds to Y.
 void mpnn_gemm(const float* X1, const __nv_bfloat16* W1t, const float* X2, const __nv_bfloat16* W2t,
                const float* bias, float* Y, float* Zout, int rows, bool silu, bool accumulate, cudaStream_t s);
+// Which tensor-core instructions the products use: 0 = tcgen05 (TMEM
+// accumulators, the default), 1 = mma.sync.  The error word counts tcgen05
+// waits that expired.
+void mpnn_set_gemm_path(int path);
+int mpnn_gemm_path();
+unsigned* mpnn_gemm_error_word();
 // dX (+)= dY W^T for hidden x hidden W.
 void mpnn_gemm_t(const float* dY, const __nv_bfloat16* W, float* dX, int rows, bool accumulate, cudaStream_t s);
 // dW += X^T dY (FP32 atomics into dW [hidden][hidden]), both operands rounded to bf16.

@@ -207,3 +207,38 @@ def test_fused_inference_matches_layer_kernels(lib, trained):
     assert sa["predicted_cells"] == sb["predicted_cells"] == 40
     for x, y in zip(a, b):
         assert np.abs(x - y).max() <= 1e-4 * (np.abs(y).max() + 1.0)
+
+
+@pytest.mark.parametrize("path", [0, 1])
+def test_gradients_both_tensor_paths(lib, path):
+    prev = bcs.set_tensor_path(path)
+    try:
+        sc = sphere_scene()
+        sim = make(sc)
+        sur = bcs.Surrogate(sim, max_samples=64)
+        f, e, t, src, dst, P = random_case(sur, sc, 2, 11)
+        loss, g = sur.loss_grad(2, f, e, t)
+        lo, go = M.loss_and_grads(P, f, e, src, dst, t, 3, bf=True)
+        assert abs(loss - lo) <= 2e-3 * abs(lo)
+        gg = unflatten(g, 3)
+        for k in M.param_names(3):
+            assert np.linalg.norm(gg[k] - go[k]) <= 1e-2 * np.linalg.norm(go[k]) + 1e-7, k
+        y = sur.forward(2, f, e)
+        assert np.abs(y - M.forward(P, f, e, src, dst, 3, bf=True)).max() <= 2e-3 * (np.abs(y).max() + 1e-6)
+    finally:
+        bcs.set_tensor_path(prev)
+    assert bcs.tensor_wait_expiries() == 0
+
+
+def test_tensor_paths_agree(lib):
+    sc = sphere_scene()
+    sim = make(sc)
+    sur = bcs.Surrogate(sim, max_samples=64)
+    f, e, t, src, dst, P = random_case(sur, sc, 4, 12)
+    prev = bcs.set_tensor_path(1)
+    y1 = sur.forward(4, f, e)
+    bcs.set_tensor_path(0)
+    y0 = sur.forward(4, f, e)
+    bcs.set_tensor_path(prev)
+    assert np.abs(y0 - y1).max() <= 1e-4 * (np.abs(y1).max() + 1e-6)
+    assert bcs.set_tensor_path(5) == -1

@@ -277,28 +277,7 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     same state, and their positions compared with the plain frames' (the
     judge).  Simulated-time throughput = particles x sub-steps / time."""
     K, M = args.learned_substeps, args.learned_macro_steps
-    t0 = time.perf_counter()
-    train_scene = build_scene(args.cells_per_type, args.seed + 7919)
-    ts = bcs.Simulation(train_scene)
-    ts.set_particles(train_scene.positions, train_scene.velocities)
-    ts.set_tuning(**tuning)
-    ts.step(warm)
-    cells = train_scene.types[1].count
-    sur = bcs.Surrogate(ts, cell_type=1, substeps=K, max_samples=cells * (args.learned_collect + 1), seed=11,
-                        huber_delta=1.0)
-    sur.collect(args.learned_collect)
-    n_train = sur.stats()["samples"]
-    loss0 = sur.train(1, batch_cells=args.learned_batch, lr=1e-3)
-    # learning rate 1e-3 decayed by 10 x over four phases
-    loss = loss0
-    for phase in range(4):
-        loss = sur.train(args.learned_iters // 4, batch_cells=args.learned_batch, lr=1e-3 * 10 ** (-phase / 3))
-    sur.collect(1)
-    net_err, base_err = sur.evaluate(n_train, sur.stats()["samples"] - n_train)
-    params, scales, st_train = sur.get_params(), sur.scales(), sur.stats()
-    sur.close()
-    ts.close()
-    train_s = time.perf_counter() - t0
+    params, scales, training = train_network(args, args.cells_per_type, tuning, bcs, warm)
 
     # local error: one macro step against K plain frames from the same state
     sim = fresh(tuning)
@@ -361,15 +340,191 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
                       "cells_predicted": st["predicted_cells"], "cells_fallen_back": st["fallback_cells"],
                       "tolerance": st["tolerance"]},
         "speedup_vs_plain": {"macro_plain": ms_plain / ms_macro, "surrogate": ms_plain / ms_sur},
-        "network": {"cell_type": "biconcave-162", "layers": 3, "hidden": 128, "parameters": st["parameters"],
-                    "flops_per_cell": st["flops_per_cell"],
-                    "training": {"scene_seed": args.seed + 7919, "cell_steps": n_train,
-                                 "iterations": st_train["iterations"], "batch_cells": args.learned_batch,
-                                 "loss": "pseudo-Huber, delta 1 (normalised)",
-                                 "loss_first": loss0, "loss_last": loss, "seconds": round(train_s, 2)},
-                    "held_out_position_error": {"network": net_err, "constant_force_extrapolation": base_err}},
+        "network": dict(training, parameters=st["parameters"], flops_per_cell=st["flops_per_cell"]),
         "judge": "positions after the same simulated time, against plain frames from the same state",
     }
+
+
+def train_network(args, cells_per_type, tuning, bcs, warm):
+    """Trains the network for the 162-vertex cells on plain macro steps of a
+    bifurcation scene of `cells_per_type` cells per type built from a fresh
+    seed; returns (parameters, scales, description)."""
+    K = args.learned_substeps
+    t0 = time.perf_counter()
+    train_scene = build_scene(cells_per_type, args.seed + 7919)
+    ts = bcs.Simulation(train_scene)
+    ts.set_particles(train_scene.positions, train_scene.velocities)
+    ts.set_tuning(**tuning)
+    ts.step(warm)
+    cells = train_scene.types[1].count
+    sur = bcs.Surrogate(ts, cell_type=1, substeps=K, max_samples=cells * (args.learned_collect + 1), seed=11,
+                        huber_delta=1.0)
+    sur.collect(args.learned_collect)
+    n_train = sur.stats()["samples"]
+    loss0 = sur.train(1, batch_cells=args.learned_batch, lr=1e-3)
+    # learning rate 1e-3 decayed by 10 x over four phases
+    loss = loss0
+    for phase in range(4):
+        loss = sur.train(args.learned_iters // 4, batch_cells=args.learned_batch, lr=1e-3 * 10 ** (-phase / 3))
+    sur.collect(1)
+    net_err, base_err = sur.evaluate(n_train, sur.stats()["samples"] - n_train)
+    params, scales, st_train = sur.get_params(), sur.scales(), sur.stats()
+    sur.close()
+    ts.close()
+    desc = {"cell_type": "biconcave-162", "layers": 3, "hidden": 128,
+            "training": {"scene": f"Y bifurcation, {cells_per_type} cells per type", "scene_seed": args.seed + 7919,
+                         "cell_steps": n_train, "iterations": st_train["iterations"],
+                         "batch_cells": args.learned_batch, "loss": "pseudo-Huber, delta 1 (normalised)",
+                         "loss_first": loss0, "loss_last": loss, "seconds": round(time.perf_counter() - t0, 2)},
+            "held_out_position_error": {"network": net_err, "constant_force_extrapolation": base_err}}
+    return params, scales, desc
+
+
+def position_error(p, ref, radius=0.5):
+    d = np.linalg.norm(np.asarray(p, np.float64) - np.asarray(ref, np.float64), axis=1)
+    return {"median": float(np.median(d)), "p99": float(np.percentile(d, 99)), "max": float(d.max()),
+            "frac_above_1e-3_radius": float(np.mean(d > 1e-3 * radius))}
+
+
+def percentiles(per):
+    return {f"p{q}": float(np.percentile(per, q)) for q in (50, 95, 99)}
+
+
+def run_scale(args):
+    """Surrogate plus batching at scale: 1M cells (half 42-, half 162-vertex,
+    102M particles) in a widened Y bifurcation.  Plain frames, plain macro
+    steps and macro steps with the network (trained on the 4.2M-particle
+    workload's scene from a fresh seed) advance the same simulated time from
+    the same state; every frame and macro step is timed alone for the latency
+    percentiles.  Positions are compared with the plain frames on the whole
+    scene, and on a seeded 1k-cell subset (in the same vessel) every path is
+    compared with the FP64 oracle."""
+    import torch
+    import bcs_build
+    import bcs
+    import bcs_scenes as S
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    bcs_build.build()
+    bcs.set_device(local)
+    K, M = args.learned_substeps, args.scale_macro_steps
+    t0 = time.perf_counter()
+    scene = S.scale_scene(args.scale_cells, seed=args.seed + rank)
+    build_s = time.perf_counter() - t0
+
+    def fresh(sc, tuning=None, warm=args.warmup):
+        sim = bcs.Simulation(sc)
+        sim.set_particles(sc.positions, sc.velocities)
+        if tuning is not None:
+            sim.set_tuning(**tuning)
+        sim.step(warm)
+        return sim
+
+    sim = fresh(scene)
+    n = sim.n
+    _, tune_ms = sim.autotune(args.autotune_frames)
+    tuning = sim.get_tuning().as_dict()
+    sim.close()
+    params, scales, training = train_network(args, CELLS_PER_TYPE, tuning, bcs, args.warmup)
+
+    def with_network(sim, max_samples=1):
+        sur = bcs.Surrogate(sim, cell_type=1, substeps=K, max_samples=max_samples, seed=11)
+        sur.set_params(params)
+        sur.set_scales(scales)
+        sur.enable(True)
+        return sur
+
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = str(getattr(props, "uuid", "") or local)
+    if gpu_id and not gpu_id.startswith("GPU-") and len(gpu_id) > 8:
+        gpu_id = "GPU-" + gpu_id
+    sampler = ClockSampler(gpu_id)
+    sim = fresh(scene, tuning)
+    per_frame = [sim.time_steps(1) for _ in range(K * M)]
+    pa = sim.get_particles()[0]
+    sim.close()
+    sim = fresh(scene, tuning)
+    per_macro = [sim.time_macro_steps(K, 1) for _ in range(M)]
+    pb = sim.get_particles()[0]
+    sim.close()
+    sim = fresh(scene, tuning)
+    sur = with_network(sim)
+    per_sur = [sim.time_macro_steps(K, 1) for _ in range(M)]
+    pc = sim.get_particles()[0]
+    st = sur.stats()
+    sur.close()
+    sim.close()
+    clocks = sampler.stop()
+    ms_plain, ms_macro, ms_sur = float(sum(per_frame)), float(sum(per_macro)), float(sum(per_sur))
+    rate = lambda ms: n * K * M / (ms / 1e3)
+
+    # the seeded 1k-cell subset against the FP64 oracle
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    sub = S.subset_scene(scene, args.scale_subset_cells, seed=args.seed + 1)
+    ms_sub = args.scale_subset_macro_steps
+    t1 = time.perf_counter()
+    o = O.OracleSim(sub, threads=os.cpu_count())
+    o.step(args.warmup + K * ms_sub)
+    po = o.get_particles()[0]
+    o.close()
+    oracle_s = time.perf_counter() - t1
+    s1 = fresh(sub, tuning)
+    s1.step(K * ms_sub)
+    g_plain = s1.get_particles()[0]
+    s1.close()
+    s1 = fresh(sub, tuning)
+    s1.macro_step(K, ms_sub)
+    g_macro = s1.get_particles()[0]
+    s1.close()
+    s1 = fresh(sub, tuning)
+    z = with_network(s1)
+    s1.macro_step(K, ms_sub)
+    g_sur = s1.get_particles()[0]
+    zst = z.stats()
+    z.close()
+    s1.close()
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "unit": UNIT, "workload": "scale",
+            "scale_surrogate": {
+                "substeps": K, "macro_steps": M, "plain_equivalent_steps": K * M,
+                "simulated_time": K * M * float(scene.params.dt),
+                "plain": {"ms": ms_plain, "particle_steps_per_s": rate(ms_plain),
+                          "frame_latency_ms": percentiles(per_frame)},
+                "macro_plain": {"ms": ms_macro, "particle_steps_per_s": rate(ms_macro),
+                                "macro_step_latency_ms": percentiles(per_macro),
+                                "position_error_vs_plain_frames": position_error(pb, pa)},
+                "surrogate": {"ms": ms_sur, "particle_steps_per_s": rate(ms_sur),
+                              "macro_step_latency_ms": percentiles(per_sur),
+                              "position_error_vs_plain_frames": position_error(pc, pa),
+                              "cells_predicted": st["predicted_cells"], "cells_fallen_back": st["fallback_cells"],
+                              "tolerance": st["tolerance"]},
+                "speedup_vs_plain": {"macro_plain": ms_plain / ms_macro, "surrogate": ms_plain / ms_sur},
+                "oracle_subset": {
+                    "cells": int(sum(t.count for t in sub.types)), "particles": sub.particle_count,
+                    "seed": args.seed + 1, "frames": args.warmup + K * ms_sub,
+                    "oracle_seconds": round(oracle_s, 2), "oracle_threads": os.cpu_count(),
+                    "plain_vs_oracle": position_error(g_plain, po),
+                    "macro_plain_vs_oracle": position_error(g_macro, po),
+                    "surrogate_vs_oracle": position_error(g_sur, po),
+                    "surrogate_cells_predicted": zst["predicted_cells"],
+                    "surrogate_cells_fallen_back": zst["fallback_cells"]},
+                "network": dict(training, parameters=st["parameters"], flops_per_cell=st["flops_per_cell"]),
+                "tuning": tuning, "autotune_ms": tune_ms,
+            },
+            "clocks": clocks,
+            "config": dict(workload_config(scene, ws), scene_build_seconds=round(build_s, 1),
+                           workload=f"surrogate at scale, widened Y bifurcation, {scene.particle_count} particles "
+                                    f"({scene.types[0].count} icosphere-42 + {scene.types[1].count} "
+                                    f"biconcave-162 cells)",
+                           trunk_radius=float(scene.params.cylinder_radius),
+                           l2="state exceeds the 129 MB L2; no flush"),
+        }
+        print(json.dumps(out), flush=True)
+    return 0
 
 
 def run_ours(args):
@@ -545,8 +700,13 @@ def main():
     ap.add_argument("--tuning", default="", help="comma-separated bcs_tuning fields instead of the autotuner")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned sub-step measurements")
     ap.add_argument("--learned-only", action="store_true", help="only the learned sub-step pass (profiling)")
-    ap.add_argument("--workload", default="bifurcation", choices=["bifurcation", "batched"],
-                    help="bifurcation: the 4.2M-particle metric workload; batched: 64 straight vessels")
+    ap.add_argument("--workload", default="bifurcation", choices=["bifurcation", "batched", "scale"],
+                    help="bifurcation: the 4.2M-particle metric workload; batched: 64 straight vessels; "
+                         "scale: plain vs learned sub-steps at 1M cells (102M particles)")
+    ap.add_argument("--scale-cells", type=int, default=1_000_000)
+    ap.add_argument("--scale-macro-steps", type=int, default=125)
+    ap.add_argument("--scale-subset-cells", type=int, default=1000)
+    ap.add_argument("--scale-subset-macro-steps", type=int, default=4)
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--learned-substeps", type=int, default=8)
     ap.add_argument("--learned-macro-steps", type=int, default=40)
@@ -558,6 +718,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "scale":
+        return run_scale(args)
     return run_ours(args)
 
 

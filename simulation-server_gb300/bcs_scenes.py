@@ -305,7 +305,8 @@ def straight_scene(cells=256, radius=30.0, length=300.0, around=64, rings=100, s
 
 def bifurcation_scene(cells_per_type=20588, seed=0, cell_size=1.0, tri_cell=6.0, dt=5e-4, k=50.0, d=0.5,
                       particle_radius=0.5, vel_sigma=0.01, peak_force=25.0, half_angle_deg=15.0,
-                      trunk_length=None, branch_length=None, fill=0.85) -> Scene:
+                      trunk_length=None, branch_length=None, fill=0.85, trunk_radius=40.0, branch_radius=28.0,
+                      trunk_around=60, branch_around=44) -> Scene:
     """Plain method, large: half 42-vertex spheres (R=3), half 162-vertex
     biconcave discs (R=4, 480 springs) in a Y bifurcation (trunk R=40,
     branches R=28), deformable spring wall, Gaussian velocities (sigma 0.01),
@@ -318,7 +319,7 @@ def bifurcation_scene(cells_per_type=20588, seed=0, cell_size=1.0, tri_cell=6.0,
     L = trunk_length or 200.0
     while True:
         Lb = branch_length or L
-        vein = bifurcation_vein(40.0, 28.0, L, Lb, half_angle_deg)
+        vein = bifurcation_vein(trunk_radius, branch_radius, L, Lb, half_angle_deg, trunk_around, branch_around)
         sites = lattice_sites(vein.segments, models, pattern, particle_radius=particle_radius)
         if all(len(s) * fill >= n for s, n in zip(sites, need)) or trunk_length:
             break
@@ -332,7 +333,7 @@ def bifurcation_scene(cells_per_type=20588, seed=0, cell_size=1.0, tri_cell=6.0,
     p.particle_d_fact = d
     p.cell_width = p.cell_height = p.cell_depth = cell_size
     p.cell_width_triangles = p.cell_height_triangles = p.cell_depth_triangles = tri_cell
-    p.cylinder_radius = 40.0
+    p.cylinder_radius = trunk_radius
     p.vein_dynamic = 1
     p.seed = seed
     flows = [dict(origin=s["origin"], direction=s["direction"], length=s["length"], radius=s["radius"],
@@ -407,3 +408,43 @@ def batched_scenes(count=64, seed=0, min_cells=500, max_cells=50000, min_length=
         spheres = int(rng.binomial(n, 0.5))
         out.append(mixed_straight_scene(spheres, n - spheres, L, seed=seed * 1000 + s, **kw))
     return out
+
+
+def scale_scene(cells=1_000_000, seed=0, cell_size=1.0, widen=6.0, **kw) -> Scene:
+    """Surrogate at scale: `cells` cells, half 42-vertex spheres and half
+    162-vertex biconcave discs (1M cells = 102M particles), in the Y
+    bifurcation of `bifurcation_scene` with radii (40, 28) and the mesh
+    resolution around them widened by `widen`.  At 1M cells and widen 6 the
+    segments settle at ~1270 long and the grid box at cell 1.0 holds 1.56e9
+    cells, inside the 31-bit key space; the large workload's proportions
+    (widen 1, ~25x the length) would need ~5e11."""
+    return bifurcation_scene(cells_per_type=cells // 2, seed=seed, cell_size=cell_size,
+                             trunk_radius=40.0 * widen, branch_radius=28.0 * widen,
+                             trunk_around=int(round(60 * widen)), branch_around=int(round(44 * widen)), **kw)
+
+
+def subset_scene(scene: Scene, cells: int, seed=0, positions=None, velocities=None) -> Scene:
+    """A seeded subset of `cells` cells of `scene` (drawn across types in
+    proportion to their counts) in the same vessel with the same constants;
+    `positions`/`velocities` (the full scene's state, default its initial
+    one) give the subset's particles."""
+    rng = np.random.default_rng(seed)
+    pos = scene.positions if positions is None else positions
+    vel = scene.velocities if velocities is None else velocities
+    total = sum(t.count for t in scene.types)
+    cells = min(cells, total)
+    pick = np.sort(rng.choice(total, size=cells, replace=False))
+    types, P, V = [], [], []
+    cell0, part0 = 0, 0
+    for t in scene.types:
+        pic = len(t.vertices)
+        mine = pick[(pick >= cell0) & (pick < cell0 + t.count)] - cell0
+        rows = (part0 + mine[:, None] * pic + np.arange(pic)[None, :]).ravel()
+        P.append(pos[rows])
+        V.append(vel[rows])
+        types.append(dataclasses.replace(t, count=int(len(mine))))
+        cell0 += t.count
+        part0 += t.count * pic
+    return dataclasses.replace(scene, name=scene.name + f"-subset{cells}", types=types,
+                               positions=np.concatenate(P).astype(np.float32),
+                               velocities=np.concatenate(V).astype(np.float32))

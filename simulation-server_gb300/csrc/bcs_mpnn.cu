@@ -460,10 +460,10 @@ __device__ inline uint32_t tc_offset(int m, int k) {
     return (uint32_t)((m >> 3) * 2048 + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
 }
 
-__device__ inline uint64_t tc_desc(uint32_t saddr) {
+__device__ inline uint64_t tc_desc(uint32_t saddr, uint32_t sbo = 2048) {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
     d |= (uint64_t)(128 >> 4) << 16;    // leading byte offset: next core matrix along K
-    d |= (uint64_t)(2048 >> 4) << 32;   // stride byte offset: next 8-row group
+    d |= (uint64_t)(sbo >> 4) << 32;    // stride byte offset: next 8-row group
     d |= (uint64_t)1 << 46;             // descriptor version of tcgen05
     return d;                           // base offset 0, no swizzle
 }
@@ -516,17 +516,26 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const float* __restrict__ X1, c
         const float* X = in ? X2 : X1;
         const __nv_bfloat16* B = in ? B2 : B1;
         if (!X) break;
-        for (int q = tid; q < 128 * 32; q += 128) {
-            const int r = q >> 5, c = (q & 31) * 4;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r0 + r < rows) v = *reinterpret_cast<const float4*>(X + (size_t)(r0 + r) * kHidden + c);
-            uint2 pk;
-            pk.x = pack_bf16(v.x, v.y);
-            pk.y = pack_bf16(v.z, v.w);
-            *reinterpret_cast<uint2*>(As + tc_offset(r, c)) = pk;
+        // one 16-byte core-matrix row per thread; the 8 lanes of a store
+        // phase fill the 8 rows of one core matrix (128 contiguous bytes)
+#pragma unroll 4
+        for (int q = tid; q < 128 * 16; q += 128) {
+            const int r = (q >> 7) * 8 + (q & 7), k = ((q >> 3) & 15) * 8;
+            float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+            if (r0 + r < rows) {
+                const float4* src = reinterpret_cast<const float4*>(X + (size_t)(r0 + r) * kHidden + k);
+                v0 = src[0];
+                v1 = src[1];
+            }
+            uint4 pk;
+            pk.x = pack_bf16(v0.x, v0.y);
+            pk.y = pack_bf16(v0.z, v0.w);
+            pk.z = pack_bf16(v1.x, v1.y);
+            pk.w = pack_bf16(v1.z, v1.w);
+            *reinterpret_cast<uint4*>(As + tc_offset(r, k)) = pk;
         }
         for (int q = tid; q < 128 * 16; q += 128) {
-            const int n = q >> 4, k = (q & 15) * 8;
+            const int n = (q >> 7) * 8 + (q & 7), k = ((q >> 3) & 15) * 8;
             *reinterpret_cast<uint4*>(Bs + tc_offset(n, k)) = *reinterpret_cast<const uint4*>(B + n * kHidden + k);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -598,6 +607,113 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const float* __restrict__ X1, c
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(taddr) : "memory");
 }
 
+// dW[k][n] += sum_r X[r][k] dY[r][n] on the tensor cores: A = X^T and B =
+// dY^T are staged transposed (K = rows, 64 per stage, canonical K-major
+// layout, stride byte offset 1024), four tcgen05.mma per stage accumulate in
+// a 128-column tensor-memory tile across the CTA's `chunk` rows, and the
+// tile is added into dW with FP32 atomics.
+constexpr int kTcWgRows = 64;
+constexpr int kTcWgTile = 128 * kTcWgRows * 2;
+
+__device__ inline uint32_t tc_offset64(int m, int k) {
+    return (uint32_t)((m >> 3) * 1024 + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
+}
+
+__global__ void __launch_bounds__(128) k_wgrad_tc(const float* __restrict__ X, const float* __restrict__ dY, float* dW,
+                                                  int rows, int chunk, unsigned* err) {
+    __shared__ __align__(1024) unsigned char smem_wg[2 * kTcWgTile];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    unsigned char* As = smem_wg;
+    unsigned char* Bs = smem_wg + kTcWgTile;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    if (warp == 0) {
+        const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(slot) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = tmem_slot;
+    const uint32_t a_base = (uint32_t)__cvta_generic_to_shared(As), b_base = (uint32_t)__cvta_generic_to_shared(Bs);
+    const int rbeg = blockIdx.x * chunk, rend = min(rows, rbeg + chunk);
+    bool ok = true, any = false;
+    uint32_t phase = 0;
+    for (int r0 = rbeg; r0 < rend; r0 += kTcWgRows) {
+        // thread = feature (warp-coalesced column reads); 8 rows packed
+        // into one 16-byte core-matrix row of X^T and of dY^T
+#pragma unroll 2
+        for (int j = 0; j < kTcWgRows / 8; ++j) {
+            float x[8], y[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int r = r0 + j * 8 + i;
+                x[i] = r < rend ? X[(size_t)r * kHidden + tid] : 0.f;
+                y[i] = r < rend ? dY[(size_t)r * kHidden + tid] : 0.f;
+            }
+            const uint4 px = make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]),
+                                        pack_bf16(x[6], x[7]));
+            const uint4 py = make_uint4(pack_bf16(y[0], y[1]), pack_bf16(y[2], y[3]), pack_bf16(y[4], y[5]),
+                                        pack_bf16(y[6], y[7]));
+            *reinterpret_cast<uint4*>(As + tc_offset64(tid, j * 8)) = px;
+            *reinterpret_cast<uint4*>(Bs + tc_offset64(tid, j * 8)) = py;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int ks = 0; ks < kTcWgRows / 16; ++ks) {
+                const uint64_t ad = tc_desc(a_base + ks * 256, 1024), bd = tc_desc(b_base + ks * 256, 1024);
+                const uint32_t acc = (any || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                    ::"r"(taddr), "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a)
+                         : "memory");
+        }
+        any = true;
+        ok = __syncthreads_and(tc_wait(mbar_a, phase) ? 1 : 0) != 0;
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!ok) break;
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(err, 1u);
+        tc_wait(mbar_a, phase ^ 1u);
+    } else if (any) {
+        const int row = warp * 32 + lane;   // feature k of X
+#pragma unroll
+        for (int chunk32 = 0; chunk32 < 4; ++chunk32) {
+            uint32_t v[32];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(chunk32 * 32)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 32; ++j) atomicAdd(&dW[row * kHidden + chunk32 * 32 + j], __uint_as_float(v[j]));
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(taddr) : "memory");
+}
+
 }  // namespace
 
 namespace {
@@ -646,6 +762,12 @@ void mpnn_gemm_t(const float* dY, const __nv_bfloat16* W, float* dX, int rows, b
 void mpnn_wgrad(const float* X, const float* dY, float* dW, int rows, cudaStream_t s) {
     if (rows <= 0) return;
     const int chunk = 1024;
+    if (g_gemm_path == 0) {
+        // about two CTAs per SM, in whole 64-row stages
+        const int tc_chunk = std::max(kTcWgRows, (rows / 304 + kTcWgRows - 1) / kTcWgRows * kTcWgRows);
+        k_wgrad_tc<<<(rows + tc_chunk - 1) / tc_chunk, 128, 0, s>>>(X, dY, dW, rows, tc_chunk, mpnn_gemm_error_word());
+        return;
+    }
     k_wgrad<<<(rows + chunk - 1) / chunk, 256, 0, s>>>(X, dY, dW, rows, chunk);
 }
 

@@ -68,3 +68,43 @@ def test_mixed_scene_grows_radius_to_fit():
     sc = S.mixed_straight_scene(400, 300, 60.0, seed=1, base_radius=10.0)
     assert sc.params.cylinder_radius > 10.0
     assert [t.count for t in sc.types] == [400, 300]
+
+
+def test_scale_scene_small_and_subset():
+    sc = S.scale_scene(600, seed=2, widen=2.0)
+    assert [t.count for t in sc.types] == [300, 300]
+    assert sc.params.cylinder_radius == 80.0
+    assert len(sc.flow_segments) == 3
+    sub = S.subset_scene(sc, 50, seed=4)
+    assert sum(t.count for t in sub.types) == 50
+    assert len(sub.positions) == sub.particle_count
+    # every chosen cell is a whole cell of the full scene, in order
+    full = {}
+    start = 0
+    for t in sc.types:
+        pic = len(t.vertices)
+        for c in range(t.count):
+            full[sc.positions[start + c * pic].tobytes()] = sc.positions[start + c * pic:start + (c + 1) * pic]
+        start += t.count * pic
+    start = 0
+    for t in sub.types:
+        pic = len(t.vertices)
+        for c in range(t.count):
+            rows = sub.positions[start + c * pic:start + (c + 1) * pic]
+            np.testing.assert_array_equal(full[rows[0].tobytes()], rows)
+        start += t.count * pic
+
+
+def test_scale_scene_key_space_at_one_million_cells():
+    """The 1M-cell vessel's grid box at cell 1.0 stays inside 31-bit keys
+    (computed from the vessel's segments, without building the scene)."""
+    import math
+    w = 6.0
+    R, Rb = 40.0 * w, 28.0 * w
+    # the length the generator settles on for 1M cells (checked on the host: 1269)
+    L = 1269.3
+    a = math.radians(15.0)
+    ext_x = 2 * (L * math.sin(a) + Rb * math.cos(a)) + 80
+    ext_y = L + L * math.cos(a) + Rb * math.sin(a) + 80
+    ext_z = 2 * R + 80
+    assert ext_x * ext_y * ext_z < 2 ** 31

@@ -15,7 +15,8 @@ particle kernel, vein integration) replayed from a CUDA graph.
             bcs_step(1) + bcs_get_particles of the positions into pinned host
             memory (the renderer's per-frame read, src/main.cu:183-184); the
             upload of the state from pinned memory opens the timed region
-  roofline  the fused particle kernel: algorithmic bytes (80 B/particle:
+  roofline  the particle phase (the fused step kernel, its crowded-particle
+            kernel, the vein-end kernel): algorithmic bytes (80 B/particle:
             x, v, F read + written as 3 x 12 B, + 8 B key/id) / its mean
             CUDA-event duration, against the measured HBM copy bandwidth
 Each of the three passes (timed run, per-phase events, e2e) starts a fresh
@@ -598,7 +599,8 @@ def run_ours(args):
     sim.close()
 
     # ---- pass 2: the same frames eagerly, CUDA events between the phases;
-    # the particle phase is the fused step kernel plus the vein-end kernel
+    # the particle phase is the fused step kernel, its crowded-particle
+    # kernel and the vein-end kernel
     prof_steps = args.profile_steps if args.profile_steps > 0 else args.steps
     sim = fresh(tuning)
     phases = sim.profile_steps(prof_steps)
@@ -665,7 +667,7 @@ def run_ours(args):
                     "h2d_bytes_per_step": int(36 * n / e2e_steps), "d2h_bytes_per_step": int(12 * n)},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm",
-                         "kernel": "bcs::k_step<0, {}, {}, {}, {}>".format(
+                         "kernel": "bcs::k_step<0, {}, {}, {}, {}> + k_crowded<0> + k_vein_end".format(
                              *shape, "true" if tuning["persistent"] else "false"),
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,

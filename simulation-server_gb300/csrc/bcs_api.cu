@@ -133,6 +133,10 @@ struct bcs_sim {
     int work_capacity = 0;       // work items of the smallest shape
     int persistent_grid[2] = {0, 0};   // by mode, 0 until first needed
     int* work_counter = nullptr;
+    int* crowded = nullptr;      // crowded-particle lists of the step kernel (N each)
+    int* crowded_cells = nullptr;
+    int* crowded_counter = nullptr;
+    float4* cent = nullptr;      // cell centroids of the step (C)
     int* order_idx = nullptr;    // first particle per work item (spatial order)
     float4* order_pos = nullptr;
     std::vector<int> scene_cells;       // blood cells per scene
@@ -823,9 +827,16 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     for (int k = 0; k < kStepShapes; ++k)
         s->work_capacity = std::max(s->work_capacity, (int)work_items(s->types, kShapes[k].chunk).size());
     if ((st = dalloc(s, &s->work, s->work_capacity)) || (st = dalloc(s, &s->order_idx, s->work_capacity)) ||
-        (st = dalloc(s, &s->order_pos, s->work_capacity)) || (st = dalloc(s, &s->work_counter, 2)))
+        (st = dalloc(s, &s->order_pos, s->work_capacity)) || (st = dalloc(s, &s->work_counter, 2)) ||
+        (st = dalloc(s, &s->crowded, s->N)) || (st = dalloc(s, &s->crowded_cells, s->N)) ||
+        (st = dalloc(s, &s->crowded_counter, 4)) || (st = dalloc(s, &s->cent, s->C)))
         return st;
     BCS_CUDA(cudaMemset(s->work_counter, 0, 2 * sizeof(int)));
+    BCS_CUDA(cudaMemset(s->crowded_counter, 0, 4 * sizeof(int)));
+    s->args.crowded = s->crowded;
+    s->args.crowded_cells = s->crowded_cells;
+    s->args.crowded_counter = s->crowded_counter;
+    s->args.cent = s->cent;
     if ((st = upload(s, &s->radius_of_particle, radius_particle)) ||
         (st = upload(s, &s->types_dev, s->types)) || (st = upload(s, &s->scenes, s->scenes_host)) ||
         (st = upload(s, &s->adj_off, adj_off)) || (st = upload(s, &s->adj_nbr, adj_nbr)) ||

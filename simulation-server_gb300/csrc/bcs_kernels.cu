@@ -132,88 +132,217 @@ __device__ inline void stencil_range_u(unsigned id, int count, int& lo, int& hi)
 // reference's static_cast<unsigned int> of the cell coordinate.
 __device__ inline unsigned to_u32_sat(float t) { return t <= 0.f ? 0u : (t >= 4294967040.f ? 0xFFFFFFFFu : (unsigned)t); }
 
-// calculateParticleCollisions<UniformGrid> (particle_collisions.cuh:26-38,
-// 53-83,104-269) for one particle; the 3 cells of a stencil row are
-// consecutive keys, so each row is one contiguous range of sorted slots.
-__device__ inline float3 particle_collisions(const StepArgs& a, const SceneDev& sc, int pid, float3 x, float3 v,
-                                            float R, unsigned& e) {
-    float3 acc = f3(0.f, 0.f, 0.f);
-    const GridDev& g = a.pg;
-    const GridGeom& geo = sc.pg;
-    // One candidate: detectCollision's test, then the resilient force with
-    // the neighbour's velocity (fetched only on a hit).
-    auto consider = [&](const float4 pq, auto neighbour) {
-        const float3 rp = x - xyz(pq);
-        const float d2 = dot3(rp, rp);
-        const float md = R + pq.w;
-        if (d2 <= md * md && d2 >= 0.0001f)
-            acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[neighbour()])), d2, R, 0.5f, e);
-    };
-    auto test = [&](int q) { consider(__ldg(&a.pos_in[q]), [q] { return q; }); };
-    if (!g.uniform) {
-        for (int q = sc.particle_start; q < sc.particle_end; ++q)
-            if (q != pid) test(q);
-        return acc;
-    }
-    const int ep = __ldg(g.epoch);
+// Collision stencil of a particle in the uniform grid (particle_collisions.cuh:
+// 104-124): the centre cell comes from the clamped key, the stencil's edges
+// from the unclamped quotients (Q7).
+struct Stencil {
+    int cell;                  // scene-local key of the centre cell
+    int x0, x1, y0, y1, z0, z1;
+    bool regular;              // the unclamped cell indices are the key's: every
+                               // such particle of the cell has this stencil
+};
+
+__device__ inline Stencil particle_stencil(const GridGeom& geo, float3 x) {
     const float tx = axis_quotient(x.x, geo.lo[0], geo.cell[0]);
     const float ty = axis_quotient(x.y, geo.lo[1], geo.cell[1]);
     const float tz = axis_quotient(x.z, geo.lo[2], geo.cell[2]);
-    const int cellId = key_of_quotients(geo, tx, ty, tz);
-    int x0, x1, y0, y1, z0, z1;
-    stencil_range((int)tx, geo.cx, x0, x1);
-    stencil_range((int)ty, geo.cy, y0, y1);
-    stencil_range((int)tz, geo.cz, z0, z1);
-    const long long cxy = (long long)geo.cx * geo.cy;
+    Stencil st;
+    const int ix = axis_clamp(tx, geo.ext[0], geo.cx), iy = axis_clamp(ty, geo.ext[1], geo.cy),
+              iz = axis_clamp(tz, geo.ext[2], geo.cz);
+    st.cell = iz * geo.cx * geo.cy + iy * geo.cx + ix;   // key_of_quotients
+    st.regular = (int)tx == ix && (int)ty == iy && (int)tz == iz;
+    stencil_range((int)tx, geo.cx, st.x0, st.x1);
+    stencil_range((int)ty, geo.cy, st.y0, st.y1);
+    stencil_range((int)tz, geo.cz, st.z0, st.z1);
+    return st;
+}
+
+// Sorted-slot range [first, last] of stencil row (dz, dy): the row's (up to)
+// three cells are consecutive keys, so their occupied slots are one
+// contiguous range.  Empty: last < first.
+__device__ inline int2 row_range(const GridDev& g, const GridGeom& geo, int ep, const Stencil& st, int dz, int dy) {
     const int4* __restrict__ table = g.table + geo.key_offset;
-    for (int dz = z0; dz <= z1; ++dz)
-        for (int dy = y0; dy <= y1; ++dy) {
-            const long long row = (long long)cellId + dz * cxy + (long long)dy * geo.cx;
-            // The row's three cells are consecutive keys, so their occupied
-            // slots form one contiguous sorted range; the three entries are
-            // loaded together.
-            int first = 0x7fffffff, last = -1;
-            if (g.occ) {
-                // Occupied cells of the window from the bitmap: only the
-                // first and the last occupied entries are loaded.
-                const long long ca = max(row + x0, 0LL), cb = min(row + x1, geo.cells - 1);
-                if (ca > cb) continue;
-                const long long ga = geo.key_offset + ca, gb = geo.key_offset + cb;
-                const int sh = (int)(ga & 31);
-                unsigned long long m = __ldg(&g.occ[ga >> 5]) >> sh;
-                if ((gb >> 5) != (ga >> 5)) m |= (unsigned long long)__ldg(&g.occ[gb >> 5]) << (32 - sh);
-                m &= (1ull << (int)(cb - ca + 1)) - 1ull;
-                if (!m) continue;
-                const int lo = __ffsll((long long)m) - 1, hi = 63 - __clzll((long long)m);
-                const int4 r = __ldg(&table[ca + lo]);
-                first = r.x;
-                last = hi != lo ? __ldg(&table[ca + hi]).y : r.y;
-            } else {
+    const long long row = (long long)st.cell + dz * ((long long)geo.cx * geo.cy) + (long long)dy * geo.cx;
+    int first = 0x7fffffff, last = -1;
+    if (g.occ) {
+        // Occupied cells of the window from the bitmap: only the first and
+        // the last occupied entries are loaded.
+        const long long ca = max(row + st.x0, 0LL), cb = min(row + st.x1, geo.cells - 1);
+        if (ca > cb) return make_int2(first, last);
+        const long long ga = geo.key_offset + ca, gb = geo.key_offset + cb;
+        const int sh = (int)(ga & 31);
+        unsigned long long m = __ldg(&g.occ[ga >> 5]) >> sh;
+        if ((gb >> 5) != (ga >> 5)) m |= (unsigned long long)__ldg(&g.occ[gb >> 5]) << (32 - sh);
+        m &= (1ull << (int)(cb - ca + 1)) - 1ull;
+        if (!m) return make_int2(first, last);
+        const int lo = __ffsll((long long)m) - 1, hi = 63 - __clzll((long long)m);
+        const int4 r = __ldg(&table[ca + lo]);
+        first = r.x;
+        last = hi != lo ? __ldg(&table[ca + hi]).y : r.y;
+    } else {
 #pragma unroll
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const long long c = row + dx;
-                    if (dx >= x0 && dx <= x1 && c >= 0 && c < geo.cells) {
-                        const int4 r = __ldg(&table[c]);
-                        if (r.z == ep) {
-                            first = min(first, r.x);
-                            last = max(last, r.y);
-                        }
-                    }
+        for (int dx = -1; dx <= 1; ++dx) {
+            const long long c = row + dx;
+            if (dx >= st.x0 && dx <= st.x1 && c >= 0 && c < geo.cells) {
+                const int4 r = __ldg(&table[c]);
+                if (r.z == ep) {
+                    first = min(first, r.x);
+                    last = max(last, r.y);
                 }
             }
+        }
+    }
+    return make_int2(first, last);
+}
+
+// A particle whose stencil holds more sorted slots (itself included) than
+// this is crowded: a whole warp takes its collision search
+// (heavy_collisions).  The split depends only on the state, so every launch
+// shape sums each particle's collisions in the same order.
+constexpr int kCrowdedSlots = 48;
+
+// One candidate of particle (x, v, R): detectCollision's test, then the
+// resilient force with the neighbour's velocity (fetched only on a hit).
+template <class Neighbour>
+__device__ inline void collide(const StepArgs& a, float3 x, float3 v, float R, float4 pq, Neighbour neighbour,
+                               float3& acc, unsigned& e) {
+    const float3 rp = x - xyz(pq);
+    const float d2 = dot3(rp, rp);
+    const float md = R + pq.w;
+    if (d2 <= md * md && d2 >= 0.0001f)
+        acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[neighbour()])), d2, R, 0.5f, e);
+}
+
+// calculateParticleCollisions<UniformGrid> (particle_collisions.cuh:26-38,
+// 53-83,104-269) for one particle, rows in stencil order, into `acc`.
+// Returns false, with `acc` incomplete, as soon as the rows seen so far hold
+// more than kCrowdedSlots slots (a crowded particle).
+__device__ inline bool particle_collisions(const StepArgs& a, const SceneDev& sc, int pid, float3 x, float3 v,
+                                           float R, float3& acc, unsigned& e) {
+    acc = f3(0.f, 0.f, 0.f);
+    const GridDev& g = a.pg;
+    const GridGeom& geo = sc.pg;
+    auto test = [&](int q) { collide(a, x, v, R, __ldg(&a.pos_in[q]), [q] { return q; }, acc, e); };
+    if (!g.uniform) {
+        for (int q = sc.particle_start; q < sc.particle_end; ++q)
+            if (q != pid) test(q);
+        return true;
+    }
+    const int ep = __ldg(g.epoch);
+    const Stencil st = particle_stencil(geo, x);
+    int slots = 0;
+    for (int dz = st.z0; dz <= st.z1; ++dz)
+        for (int dy = st.y0; dy <= st.y1; ++dy) {
+            const int2 r = row_range(g, geo, ep, st, dz, dy);
+            slots += max(0, r.y - r.x + 1);
+            if (slots > kCrowdedSlots) return false;
             if (g.spos) {
                 // Sorted positions: contiguous loads; the particle itself
                 // (d2 = 0) fails the d2 >= 1e-4 test, so no id is needed
                 // before a hit.
-                for (int j = first; j <= last; ++j)
-                    consider(__ldg(&g.spos[j]), [&g, j] { return __ldg(&g.ids[j]); });
+                for (int j = r.x; j <= r.y; ++j)
+                    collide(a, x, v, R, __ldg(&g.spos[j]), [&g, j] { return __ldg(&g.ids[j]); }, acc, e);
             } else {
-                for (int j = first; j <= last; ++j) {
+                for (int j = r.x; j <= r.y; ++j) {
                     const int q = __ldg(&g.ids[j]);
                     if (q != pid) test(q);
                 }
             }
         }
+    return true;
+}
+
+// The nine rows of a stencil for a whole warp: lanes 0..8 look up one row
+// each; every lane receives each row's first slot (rf) and its start in the
+// stencil's slot numbering (rs, rows in stencil order); returns the number
+// of slots.  Slot number c lies in the last row with rs[r] <= c (an empty
+// row starts where the next one does).
+__device__ inline int stencil_rows(const GridDev& g, const GridGeom& geo, const Stencil& st, int lane, int (&rs)[9],
+                                   int (&rf)[9]) {
+    const int ep = __ldg(g.epoch);
+    int first = 0, len = 0;
+    if (lane < 9) {
+        const int dz = lane / 3 - 1, dy = lane % 3 - 1;
+        if (dz >= st.z0 && dz <= st.z1 && dy >= st.y0 && dy <= st.y1) {
+            const int2 r = row_range(g, geo, ep, st, dz, dy);
+            if (r.y >= r.x) {
+                first = r.x;
+                len = r.y - r.x + 1;
+            }
+        }
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 8);
+    const int start = incl - len;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        rs[r] = __shfl_sync(0xffffffffu, start, r);
+        rf[r] = __shfl_sync(0xffffffffu, first, r);
+    }
+    return total;
+}
+
+__device__ inline int stencil_slot(int c, const int (&rs)[9], const int (&rf)[9]) {
+    int j = rf[0];
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+        if (c >= rs[r]) j = rf[r] + (c - rs[r]);
+    return j;
+}
+
+// The same sum for one crowded particle, taken by a whole warp: the slots of
+// the nine rows are numbered in stencil order and lane l takes slots l,
+// l + 32, ...; a fixed butterfly combines the lanes' partial sums (every
+// lane returns the total).
+__device__ inline float3 heavy_collisions(const StepArgs& a, const SceneDev& sc, int pid, float3 x, float3 v,
+                                         float R, int lane, unsigned& e) {
+    const GridDev& g = a.pg;
+    const Stencil st = particle_stencil(sc.pg, x);
+    int rs[9], rf[9];
+    const int total = stencil_rows(g, sc.pg, st, lane, rs, rf);
+    float3 acc = f3(0.f, 0.f, 0.f);
+    // Four slots per lane and pass (c, c + 32, c + 64, c + 96), their loads
+    // issued together: ids, then positions (sorted copy, or by id) and
+    // velocities whether or not the pair touches; the lane still adds its
+    // slots in increasing order.
+    constexpr int U = 4;
+    for (int c0 = lane; c0 < total; c0 += 32 * U) {
+        int q[U];
+        float4 pq[U], vq[U];
+        bool live[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int c = c0 + 32 * u;
+            live[u] = c < total;
+            const int j = stencil_slot(c, rs, rf);
+            q[u] = live[u] ? __ldg(&g.ids[j]) : pid;
+            if (g.spos) pq[u] = live[u] ? __ldg(&g.spos[j]) : make_float4(x.x, x.y, x.z, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!g.spos) pq[u] = __ldg(&a.pos_in[q[u]]);
+            vq[u] = __ldg(&a.vel_in[q[u]]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!live[u] || q[u] == pid) continue;
+            const float3 rp = x - xyz(pq[u]);
+            const float d2 = dot3(rp, rp);
+            const float md = R + pq[u].w;
+            if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(vq[u]), d2, R, 0.5f, e);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+    }
     return acc;
 }
 
@@ -391,8 +520,61 @@ __device__ inline void stage_scene(const SceneDev* src, SceneDev* dst) {
 constexpr int kFull = 0;    // whole frame: forces, integration, vein end, next keys
 constexpr int kForces = 1;  // calculateNextFrame only: forces and collision velocities
 
-// One work item: stage the cells, then per particle springs, environment,
-// collisions, the vein ray and (MODE kFull) integration and next keys.
+// Everything of one particle after the staging and its collision sum
+// `coll`: springs, environment and the force average, the vein ray,
+// integration (MODE kFull) and the outputs.
+// cpos / cvel / cfrc hold the particle's blood cell (vertex li of it), in
+// shared memory (k_step) or global memory (k_crowded); cent is its centroid.
+template <int MODE>
+__device__ inline void advance_particle(const StepArgs& a, const SceneDev& sc, const TypeDev& ty, int pid, int li,
+                                        const float4* cpos, const float4* cvel, const float4* cfrc, float3 cent,
+                                        float3 coll, unsigned& e) {
+    const float4 px = cpos[li];
+    const float3 x = xyz(px), v = xyz(cvel[li]), fprev = xyz(cfrc[li]);
+    // Intra-cell springs, gatherForcesKernel (blood_cells.cu:66-120) over
+    // the CSR form of the dense spring graph (same ascending order).
+    float3 F = f3(0.f, 0.f, 0.f);
+    const int e0 = __ldg(&a.adj_off[ty.adj_start + li]), e1 = __ldg(&a.adj_off[ty.adj_start + li + 1]);
+    for (int k = e0; k < e1; ++k) {
+        const int j = __ldg(&a.adj_nbr[k]);
+        F = F + cell_spring(a.p, x - xyz(cpos[j]), v - xyz(cvel[j]), fprev, xyz(cfrc[j]), __ldg(&a.adj_len[k]), e);
+    }
+    const float ratio = len3(x - cent) / __ldg(&a.r0[ty.model_start + li]);
+    F = F + environment(a, sc, x, v, ratio);
+    F = (fprev + F) / 2.0f;
+    const float3 favg = F;
+    // Particle-particle collisions.
+    F = F + coll;
+    // Particle-vein collision.
+    float3 vv = v;
+    vein_collision(a, sc, x, vv, F, px.w, e);
+    float3 nx = x, nv = vv;
+    if (MODE == kFull) {
+        // propagateParticleForcesKernel (blood_cells.cu:155-179), Heun.
+        const float3 v1 = vv + a.p.dt * F;
+        nx = x + (0.5f * a.p.dt) * (v1 + vv);
+        nv = v1;
+    }
+    if (!(isfinite(nx.x) && isfinite(nx.y) && isfinite(nx.z) && isfinite(nv.x) && isfinite(nv.y) && isfinite(nv.z)))
+        e |= BCS_ERRW_NONFINITE;
+    a.pos_out[pid] = make_float4(nx.x, nx.y, nx.z, px.w);
+    a.vel_out[pid] = make_float4(nv.x, nv.y, nv.z, 0.f);
+    a.frc_out[pid] = make_float4(F.x, F.y, F.z, 0.f);
+    if (MODE == kFull && a.keys_out) {
+        a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, nx, e) : 0;
+        a.ids_out[pid] = pid;
+    }
+    if (MODE == kFull && a.fext) {
+        // macro step: the external part of this force, held by sub-steps 2..K
+        const float3 fx = F - favg;
+        a.fext[pid] = make_float4(fx.x, fx.y, fx.z, 0.f);
+    }
+}
+
+// One work item: stage the cells and their centroids, then every particle:
+// its collision sum, then advance_particle.  A crowded particle (more than
+// kCrowdedSlots sorted slots in its stencil) is set aside as soon as its
+// search sees that many, and k_crowded finishes it.
 template <int MODE, int THREADS>
 __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, float4* s_vel, float4* s_frc,
                                  float3* s_cent, SceneDev& sc) {
@@ -421,55 +603,34 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
             acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
             acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
         }
-        if (lane == 0) s_cent[c] = acc / (float)pic;
+        if (lane == 0) {
+            const float3 m = acc / (float)pic;
+            s_cent[c] = m;
+            a.cent[ty.cell_global + w.first_cell + c] = make_float4(m.x, m.y, m.z, 0.f);
+        }
     }
     __syncthreads();
 
     unsigned e = 0;
     for (int i = threadIdx.x; i < np; i += THREADS) {
-        const int c = i / pic, li = i - c * pic, pid = p0 + i;
         const float4 px = s_pos[i];
-        const float3 x = xyz(px), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
-        // Intra-cell springs, gatherForcesKernel (blood_cells.cu:66-120) over
-        // the CSR form of the dense spring graph (same ascending order).
-        float3 F = f3(0.f, 0.f, 0.f);
-        const int e0 = __ldg(&a.adj_off[ty.adj_start + li]), e1 = __ldg(&a.adj_off[ty.adj_start + li + 1]);
-        const int cb = c * pic;
-        for (int k = e0; k < e1; ++k) {
-            const int j = cb + __ldg(&a.adj_nbr[k]);
-            F = F + cell_spring(a.p, x - xyz(s_pos[j]), v - xyz(s_vel[j]), fprev, xyz(s_frc[j]), __ldg(&a.adj_len[k]), e);
+        float3 coll;
+        if (!particle_collisions(a, sc, p0 + i, xyz(px), xyz(s_vel[i]), px.w, coll, e)) {
+            // crowded: every particle of the cell that shares this stencil is
+            // crowded too, and the first to claim the cell (the table entry's
+            // spare word, zero after each build) lists it once for k_crowded
+            const Stencil st = particle_stencil(sc.pg, xyz(px));
+            if (st.regular) {
+                int4* entry = const_cast<int4*>(a.pg.table) + sc.pg.key_offset + st.cell;
+                if (atomicExch(&entry->w, 1) == 0) a.crowded_cells[atomicAdd(&a.crowded_counter[2], 1)] = p0 + i;
+            } else {
+                a.crowded[atomicAdd(&a.crowded_counter[0], 1)] = p0 + i;
+            }
+            continue;
         }
-        const float ratio = len3(x - s_cent[c]) / __ldg(&a.r0[ty.model_start + li]);
-        F = F + environment(a, sc, x, v, ratio);
-        F = (fprev + F) / 2.0f;
-        const float3 favg = F;
-        // Particle-particle collisions.
-        F = F + particle_collisions(a, sc, pid, x, v, px.w, e);
-        // Particle-vein collision.
-        float3 vv = v;
-        vein_collision(a, sc, x, vv, F, px.w, e);
-        float3 nx = x, nv = vv;
-        if (MODE == kFull) {
-            // propagateParticleForcesKernel (blood_cells.cu:155-179), Heun.
-            const float3 v1 = vv + a.p.dt * F;
-            nx = x + (0.5f * a.p.dt) * (v1 + vv);
-            nv = v1;
-        }
-        if (!(isfinite(nx.x) && isfinite(nx.y) && isfinite(nx.z) && isfinite(nv.x) && isfinite(nv.y) &&
-              isfinite(nv.z)))
-            e |= BCS_ERRW_NONFINITE;
-        a.pos_out[pid] = make_float4(nx.x, nx.y, nx.z, px.w);
-        a.vel_out[pid] = make_float4(nv.x, nv.y, nv.z, 0.f);
-        a.frc_out[pid] = make_float4(F.x, F.y, F.z, 0.f);
-        if (MODE == kFull && a.keys_out) {
-            a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, nx, e) : 0;
-            a.ids_out[pid] = pid;
-        }
-        if (MODE == kFull && a.fext) {
-            // macro step: the external part of this force, held by sub-steps 2..K
-            const float3 fx = F - favg;
-            a.fext[pid] = make_float4(fx.x, fx.y, fx.z, 0.f);
-        }
+        const int c = i / pic;
+        advance_particle<MODE>(a, sc, ty, p0 + i, i - c * pic, s_pos + c * pic, s_vel + c * pic, s_frc + c * pic,
+                               s_cent[c], coll, e);
     }
     if (e) atomicOr(a.err, e);
 }
@@ -501,6 +662,145 @@ __global__ void __launch_bounds__(THREADS, MINB) k_step(const StepArgs a) {
         // every CTA has taken its last item: reset for the next launch
         a.work_counter[0] = 0;
         a.work_counter[1] = 0;
+    }
+}
+
+__device__ inline int type_of_particle(const StepArgs& a, int p) {
+    return find_range(a.type_count, p, [&](int i) { return a.types[i].particle_start; });
+}
+
+// The crowded particles k_step set aside.
+//  * Crowded grid cells (a.crowded_cells, one particle of each): a warp
+//    takes a cell, up to 32 of its particles at a time, and stages the slots
+//    of their common stencil in shared memory, 64 at a time and in stencil
+//    order.  With G particles in a pass each has L = 32 / G lanes (rounded
+//    down to a power of two); lane `sub` of a particle sums slots sub,
+//    sub + L, ... in order and a fixed butterfly adds the L partial sums.
+//    Only particles of the cell with the cell's regular stencil are taken;
+//    the others are the light path's or in a.crowded.
+//  * Crowded particles off the regular stencils (a.crowded: outside the grid
+//    box, rare): a warp takes a batch of up to 32, sums the collisions of
+//    each with the whole warp (heavy_collisions), then every lane finishes
+//    its own particle.
+// Each particle is then finished by advance_particle from the step's input
+// state in global memory.  The last CTA to finish empties both lists.
+constexpr int kCrowdedThreads = 256;
+constexpr int kCrowdedStage = 64;    // stencil slots staged per warp and pass
+
+template <int MODE>
+__global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a) {
+    __shared__ float4 s_cpos[kCrowdedThreads / 32][kCrowdedStage];
+    __shared__ float4 s_cvel[kCrowdedThreads / 32][kCrowdedStage];
+    __shared__ int s_cslot[kCrowdedThreads / 32][kCrowdedStage];
+    const int count = a.crowded_counter[0], ncells = a.crowded_counter[2];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gwarp = (blockIdx.x * kCrowdedThreads + threadIdx.x) >> 5;
+    const int nwarps = gridDim.x * (kCrowdedThreads / 32);
+    const GridDev& g = a.pg;
+    unsigned e = 0;
+    for (int k = gwarp; k < ncells; k += nwarps) {
+        const int leader = a.crowded_cells[k];
+        const TypeDev& lt = a.types[type_of_particle(a, leader)];
+        const SceneDev& sc = a.scenes[lt.scene];
+        const Stencil st = particle_stencil(sc.pg, xyz(a.pos_in[leader]));
+        int rs[9], rf[9];
+        const int total = stencil_rows(g, sc.pg, st, lane, rs, rf);
+        const int4 own = __ldg(&g.table[sc.pg.key_offset + st.cell]);
+        for (int s0 = own.x; s0 <= own.y; s0 += 32) {
+            // G particles of the cell in this pass, L lanes each (the
+            // largest power of two with G * L <= 32): lane = particle * L +
+            // sub, and sub takes the staged slots sub, sub + L, ...
+            const int G = min(32, own.y - s0 + 1);
+            const int L = G > 16 ? 1 : G > 8 ? 2 : G > 4 ? 4 : G > 2 ? 8 : G > 1 ? 16 : 32;
+            const int gp = lane / L, sub = lane - gp * L;
+            const int my_slot = s0 + gp;
+            int pid = -1;
+            float3 x = f3(0.f, 0.f, 0.f), v = x;
+            float R = 0.f;
+            if (gp < G) {
+                pid = __ldg(&g.ids[my_slot]);
+                const float4 px = a.pos_in[pid];
+                const Stencil ps = particle_stencil(sc.pg, xyz(px));
+                if (ps.regular) {
+                    x = xyz(px);
+                    R = px.w;
+                    v = xyz(a.vel_in[pid]);
+                } else {
+                    pid = -1;
+                }
+            }
+            float3 acc = f3(0.f, 0.f, 0.f);
+            for (int c0 = 0; c0 < total; c0 += kCrowdedStage) {
+                const int n = min(kCrowdedStage, total - c0);
+                for (int t = lane; t < n; t += 32) {
+                    const int j = stencil_slot(c0 + t, rs, rf);
+                    const int q = __ldg(&g.ids[j]);
+                    s_cpos[wib][t] = g.spos ? __ldg(&g.spos[j]) : __ldg(&a.pos_in[q]);
+                    s_cvel[wib][t] = __ldg(&a.vel_in[q]);
+                    s_cslot[wib][t] = j;
+                }
+                __syncwarp();
+                if (pid >= 0) {
+                    for (int t = sub; t < n; t += L) {
+                        if (s_cslot[wib][t] == my_slot) continue;
+                        const float4 pq = s_cpos[wib][t];
+                        const float3 rp = x - xyz(pq);
+                        const float d2 = dot3(rp, rp);
+                        const float md = R + pq.w;
+                        if (d2 <= md * md && d2 >= 0.0001f)
+                            acc = acc + resilient(a.p, rp, v - xyz(s_cvel[wib][t]), d2, R, 0.5f, e);
+                    }
+                }
+                __syncwarp();
+            }
+            // the particle's L partial sums, fixed butterfly within its lanes
+            for (int o = L >> 1; o > 0; o >>= 1) {
+                acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+                acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+                acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+            }
+            if (pid >= 0 && sub == 0) {
+                const TypeDev& ty = a.types[type_of_particle(a, pid)];
+                const int rel = pid - ty.particle_start, cell = rel / ty.pic, li = rel - cell * ty.pic;
+                const int first = pid - li;
+                advance_particle<MODE>(a, sc, ty, pid, li, a.pos_in + first, a.vel_in + first, a.frc_in + first,
+                                       xyz(a.cent[ty.cell_global + cell]), acc, e);
+            }
+        }
+        // release the claim: the table is clean for a step on the same grid
+        if (lane == 0) const_cast<int4*>(g.table)[sc.pg.key_offset + st.cell].w = 0;
+    }
+    // batches of up to 32 particles, as small as the list allows: a warp's
+    // collision sums run one after another
+    const int per = min(32, (count + nwarps - 1) / nwarps);
+    for (int b0 = gwarp * per; b0 < count; b0 += nwarps * per) {
+        const int nb = min(per, count - b0);
+        const int mine = lane < nb ? a.crowded[b0 + lane] : -1;
+        float3 my_coll = f3(0.f, 0.f, 0.f);
+        for (int k = 0; k < nb; ++k) {
+            const int pid = __shfl_sync(0xffffffffu, mine, k);
+            const TypeDev& ty = a.types[type_of_particle(a, pid)];
+            const float4 px = a.pos_in[pid];
+            const float3 c = heavy_collisions(a, a.scenes[ty.scene], pid, xyz(px), xyz(a.vel_in[pid]), px.w, lane, e);
+            if (lane == k) my_coll = c;
+        }
+        if (lane < nb) {
+            const TypeDev& ty = a.types[type_of_particle(a, mine)];
+            const int rel = mine - ty.particle_start, cell = rel / ty.pic, li = rel - cell * ty.pic;
+            const int first = mine - li;
+            advance_particle<MODE>(a, a.scenes[ty.scene], ty, mine, li, a.pos_in + first, a.vel_in + first,
+                                   a.frc_in + first, xyz(a.cent[ty.cell_global + cell]), my_coll, e);
+        }
+    }
+    if (e) atomicOr(a.err, e);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&a.crowded_counter[1], 1) == (int)gridDim.x - 1) {
+            a.crowded_counter[0] = 0;
+            a.crowded_counter[1] = 0;
+            a.crowded_counter[2] = 0;
+        }
     }
 }
 
@@ -982,10 +1282,6 @@ __global__ void k_sur_eval(const float* __restrict__ Y, const float* __restrict_
 // minSpawnY - 180 u min(N / 1000, 1), its particles at origin + model
 // vertex, velocity initVelocity, force 0.  Philox4x32-10 keyed by (seed,
 // cell within the scene) replaces the per-thread curand states.
-__device__ inline int type_of_particle(const StepArgs& a, int p) {
-    return find_range(a.type_count, p, [&](int i) { return a.types[i].particle_start; });
-}
-
 __global__ void k_init_reference(const StepArgs a, float4* pos, float4* vel, float4* frc, const float4* __restrict__ model,
                                  const float* __restrict__ radius, unsigned long long seed) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1609,6 +1905,16 @@ void launch_step(const StepArgs& a, int items, int mode, int shape, int persiste
     const bool persistent = persistent_grid > 0;
     const int blocks = persistent ? std::min(items, persistent_grid) : items;
     step_kernel_for(mode, shape, persistent)<<<blocks, kShapes[shape].threads, 0, s>>>(a);
+    if (!a.pg.uniform) return;   // no stencil, no crowded particles
+    static int grid = 0;
+    if (!grid) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = 4 * std::max(1, sms);
+    }
+    if (mode == 0) k_crowded<0><<<grid, kCrowdedThreads, 0, s>>>(a);
+    else k_crowded<1><<<grid, kCrowdedThreads, 0, s>>>(a);
 }
 void launch_gather_rows(const float4* src, const int* idx, int n, float4* out, cudaStream_t s) {
     if (n > 0) k_gather_rows<<<BCS_GRID1(n, 256), 0, s>>>(src, idx, n, out);

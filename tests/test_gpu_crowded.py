@@ -1,0 +1,164 @@
+"""Crowded particles.  A particle whose collision stencil holds more than 48
+sorted slots is left by the step kernel to k_crowded: inside the grid box a
+warp takes its whole grid cell (the stencil's slots staged in shared memory,
+the lanes of each particle splitting them), outside it a warp takes the
+particle alone (lanes split the slots); fixed butterflies add the partial
+sums.  Scenes with cells piled onto a few points put many
+particles on both paths: the result must match the FP64 oracle like any
+other step, and stay bit-identical across every launch shape and grid
+option.
+
+Tolerances as the plain parity tests: one step 1e-5 relative (FP32 against
+FP64, elementwise against |oracle| + rms(oracle)); after a few steps 1e-3 of
+the particle radius.
+"""
+import numpy as np
+import pytest
+
+import bcs
+import bcs_scenes as S
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CROWDED = 48
+
+
+def rel_err(g, o):
+    o = np.asarray(o, np.float64)
+    scale = np.abs(o) + np.sqrt(np.mean(o * o)) + 1e-30
+    return float(np.max(np.abs(np.asarray(g, np.float64) - o) / scale))
+
+
+def crowded_scene(seed=4, spread=0.7, vel=2.0, anchors=None, **kw):
+    """60 icosphere cells piled in threes onto three points of a straight
+    vessel, each cell a little off its point."""
+    sc = S.straight_scene(cells=60, seed=seed, radius=14.0, length=90.0, around=32, rings=40, **kw)
+    rng = np.random.default_rng(seed)
+    pic = len(sc.types[0].vertices)
+    if anchors is None:
+        anchors = [[0.0, -20.0, 0.0], [3.0, -45.0, -2.0], [-4.0, -70.0, 3.0]]
+    anchors = np.array(anchors, np.float32)
+    P = sc.positions.reshape(-1, pic, 3)
+    off = anchors[np.arange(len(P)) % 3][:, None, :] + rng.normal(0, spread, (len(P), 1, 3)).astype(np.float32)
+    sc.positions[:] = (P - P.mean(1, keepdims=True) + off).reshape(-1, 3)
+    sc.velocities[:] = rng.normal(0, vel, sc.velocities.shape).astype(np.float32)
+    return sc
+
+
+def stencil_slots(sc, pos):
+    """Host count of the slots in each particle's 27-cell stencil (grid cell
+    1.0 over the vein's box and margins)."""
+    p = sc.params
+    m = np.array([p.grid_xz_margin, p.grid_y_margin, p.grid_xz_margin])
+    lo = sc.vein_positions.min(0) - m
+    q = np.floor((pos - lo) / 1.0).astype(np.int64)
+    dims = q.max(0) + 3
+    key = (q[:, 2] * dims[1] + q[:, 1]) * dims[0] + q[:, 0]
+    uk, cnt = np.unique(key, return_counts=True)
+    n = np.zeros(len(pos), np.int64)
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                k2 = key + (dz * dims[1] + dy) * dims[0] + dx
+                ix = np.minimum(np.searchsorted(uk, k2), len(uk) - 1)
+                n += np.where(uk[ix] == k2, cnt[ix], 0)
+    return n
+
+
+def make(sc, **tuning):
+    sim = bcs.Simulation(sc)
+    sim.set_particles(sc.positions, sc.velocities)
+    if tuning:
+        sim.set_tuning(**tuning)
+    return sim
+
+
+def test_scene_is_crowded():
+    sc = crowded_scene()
+    n = stencil_slots(sc, sc.positions)
+    assert (n > CROWDED).sum() > 1000 and (n <= CROWDED).sum() > 100
+
+
+def test_one_step_matches_oracle(lib):
+    sc = crowded_scene()
+    sim = make(sc)
+    sim.step(1)
+    o = O.OracleSim(sc)
+    o.step(1)
+    for name, a, b in zip(("position", "velocity", "force"), sim.get_particles(), o.get_particles()):
+        e = rel_err(a, b)
+        assert e <= 1e-5, f"{name}: relative error {e:.3e}"
+
+
+def test_few_steps_within_1e3_radius(lib):
+    sc = crowded_scene(vel=0.5)
+    sim = make(sc)
+    sim.step(4)
+    o = O.OracleSim(sc)
+    o.step(4)
+    gp, op = sim.get_particles()[0], o.get_particles()[0]
+    assert np.abs(gp - op).max() < 1e-3 * 0.5
+    assert (stencil_slots(sc, gp) > CROWDED).sum() > 1000
+
+
+FLAGS = ("persistent", "spatial_order", "full_sort", "occupancy_filter", "sorted_positions")
+
+
+@pytest.mark.parametrize("shape", range(len(bcs.STEP_SHAPES)))
+@pytest.mark.parametrize("flags", [0, 1])
+def test_every_shape_same_state(lib, shape, flags):
+    sc = crowded_scene()
+    want = make(sc)
+    want.step(5)
+    want = want.get_particles()
+    sim = make(sc, step_shape=shape, **{f: flags for f in FLAGS})
+    sim.step(5)
+    for a, b in zip(sim.get_particles(), want):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_split_phases_match_fused(lib):
+    sc = crowded_scene()
+    a, b = make(sc), make(sc, occupancy_filter=1, sorted_positions=1)
+    for _ in range(3):
+        a.calculate_grids()
+        a.calculate_next_frame()
+        a.propagate_all()
+    b.step(3)
+    for x, y in zip(a.get_particles(), b.get_particles()):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_macro_steps_match_oracle(lib):
+    sc = crowded_scene(vel=0.5)
+    sim = make(sc)
+    o = O.OracleSim(sc)
+    sim.macro_step(4, 1)
+    o.macro_step(4, 1)
+    g, r = sim.get_particles(), o.get_particles()
+    assert rel_err(g[0], r[0]) <= 4e-5
+    assert rel_err(g[1], r[1]) <= 4e-4
+
+
+def test_crowded_outside_the_grid_box(lib):
+    """A pile beyond the grid box's top face: clamped keys, so those
+    particles' stencils are not their cell's regular one (the per-particle
+    warp path); the other two piles are inside."""
+    sc = crowded_scene(anchors=[[0.0, 47.0, 0.0], [3.0, -45.0, -2.0], [-4.0, -70.0, 3.0]], use_blood_flow=False)
+    top = sc.positions[:, 1].max()
+    assert top > sc.vein_positions[:, 1].max() + sc.params.grid_y_margin
+    sim = make(sc)
+    sim.step(1)
+    o = O.OracleSim(sc)
+    o.step(1)
+    for name, a, b in zip(("position", "velocity", "force"), sim.get_particles(), o.get_particles()):
+        e = rel_err(a, b)
+        assert e <= 1e-5, f"{name}: relative error {e:.3e}"
+    want = sim.get_particles()
+    for shape in range(len(bcs.STEP_SHAPES)):
+        other = make(sc, step_shape=shape, **{f: shape % 2 for f in FLAGS})
+        other.step(1)
+        for a, b in zip(other.get_particles(), want):
+            np.testing.assert_array_equal(a, b)
+

@@ -65,11 +65,13 @@ __device__ inline float3 environment(const StepArgs& a, const SceneDev& sc, floa
 }
 
 // addResilientForceOnCollision (physics.cuh:133-145) times `intensity`;
-// the direction and the spring term share sqrt(d2).
+// the direction and the spring term share one reciprocal square root of d2
+// (every call site has d2 == dot(rp, rp) >= 1e-4 or a vein hit's distance).
 __device__ inline float3 resilient(const bcs_params& p, float3 rp, float3 rv, float d2, float radius, float intensity,
                                    unsigned& e) {
-    const float d = sqrtf(d2);           // d2 == dot(rp, rp) at every call site
-    float3 dir = __frcp_rn(d) * rp;
+    const float rs = rsqrtf(d2);
+    const float d = d2 * rs;
+    float3 dir = rs * rp;
     if (isnan(dir.x) || isnan(dir.y) || isnan(dir.z)) {
         e |= BCS_ERRW_NAN_NORMALIZE;
         dir = f3(0.f, 0.f, 0.f);
@@ -691,7 +693,6 @@ template <int MODE>
 __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a) {
     __shared__ float4 s_cpos[kCrowdedThreads / 32][kCrowdedStage];
     __shared__ float4 s_cvel[kCrowdedThreads / 32][kCrowdedStage];
-    __shared__ int s_cslot[kCrowdedThreads / 32][kCrowdedStage];
     const int count = a.crowded_counter[0], ncells = a.crowded_counter[2];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gwarp = (blockIdx.x * kCrowdedThreads + threadIdx.x) >> 5;
@@ -736,19 +737,19 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
                     const int j = stencil_slot(c0 + t, rs, rf);
                     const int q = __ldg(&g.ids[j]);
                     s_cpos[wib][t] = g.spos ? __ldg(&g.spos[j]) : __ldg(&a.pos_in[q]);
-                    s_cvel[wib][t] = __ldg(&a.vel_in[q]);
-                    s_cslot[wib][t] = j;
+                    const float4 vq = __ldg(&a.vel_in[q]);
+                    s_cvel[wib][t] = make_float4(vq.x, vq.y, vq.z, __int_as_float(j));   // w: the slot
                 }
                 __syncwarp();
                 if (pid >= 0) {
                     for (int t = sub; t < n; t += L) {
-                        if (s_cslot[wib][t] == my_slot) continue;
+                        const float4 vq = s_cvel[wib][t];
+                        if (__float_as_int(vq.w) == my_slot) continue;
                         const float4 pq = s_cpos[wib][t];
                         const float3 rp = x - xyz(pq);
                         const float d2 = dot3(rp, rp);
                         const float md = R + pq.w;
-                        if (d2 <= md * md && d2 >= 0.0001f)
-                            acc = acc + resilient(a.p, rp, v - xyz(s_cvel[wib][t]), d2, R, 0.5f, e);
+                        if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(vq), d2, R, 0.5f, e);
                     }
                 }
                 __syncwarp();

@@ -12,9 +12,12 @@ particle kernel, vein integration) replayed from a CUDA graph.
             on the library's stream (the state, 403 MB of float4 buffers, is
             larger than the 129 MB L2, so no flush is needed between steps)
   e2e       the same metric through the C ABI with host buffers: each step is
-            bcs_step(1) + bcs_get_particles of the positions into pinned host
-            memory (the renderer's per-frame read, src/main.cu:183-184); the
-            upload of the state from pinned memory opens the timed region
+            bcs_step(1) + a read of the positions into pinned host memory
+            (the renderer's per-frame read, src/main.cu:183-184), issued with
+            bcs_get_particles_async into two alternating buffers so that it
+            overlaps the next frame; the upload of the state from pinned
+            memory opens the timed region and the last read's arrival on the
+            host closes it
   roofline  the particle phase (the fused step kernel, its crowded-particle
             kernel, the vein-end kernel): algorithmic bytes (80 B/particle:
             x, v, F read + written as 3 x 12 B, + 8 B key/id) / its mean
@@ -617,24 +620,28 @@ def run_ours(args):
 
     # ---- pass 3: end to end through the C ABI with pinned host buffers:
     # the state after the warm-up is uploaded, then every frame is
-    # bcs_step(1) + a read of the positions into host memory
+    # bcs_step(1) + a read of its positions into host memory, overlapped
+    # with the next frame (bcs_get_particles_async into two alternating
+    # pinned buffers, as a renderer double-buffers); the timed region ends
+    # when the last read has reached the host
     e2e_steps = args.steps if args.e2e_steps <= 0 else max(1, min(args.e2e_steps, args.steps))
     sim = fresh(tuning)
     p0, v0, f0 = sim.get_particles()
-    hp = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(9)]
+    hp = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(12)]
     for k in range(3):
         hp[k].copy_(torch.from_numpy(np.ascontiguousarray(p0[:, k])))
         hp[3 + k].copy_(torch.from_numpy(np.ascontiguousarray(v0[:, k])))
         hp[6 + k].copy_(torch.from_numpy(np.ascontiguousarray(f0[:, k])))
     lib = bcs.load_library()
     P, Vv, Ff = (bcs.Vec3(*(x.data_ptr() for x in hp[3 * j:3 * j + 3])) for j in range(3))
-    out = bcs.Vec3(*(x.data_ptr() for x in hp[:3]))
+    outs = [bcs.Vec3(*(x.data_ptr() for x in hp[:3])), bcs.Vec3(*(x.data_ptr() for x in hp[9:12]))]
     barrier(sim)
     t0 = time.perf_counter()
     assert lib.bcs_set_particles(sim.h, P, Vv, Ff, bcs.MEM_HOST) == 0
-    for _ in range(e2e_steps):
+    for k in range(e2e_steps):
         assert lib.bcs_step(sim.h, 1) == 0
-        assert lib.bcs_get_particles(sim.h, out, bcs.Vec3(), bcs.Vec3(), bcs.MEM_HOST) == 0
+        assert lib.bcs_get_particles_async(sim.h, outs[k & 1], bcs.Vec3(), bcs.Vec3()) == 0
+    assert lib.bcs_wait_particles(sim.h) == 0
     e2e_s = time.perf_counter() - t0
     sim.close()
     e2e_value = whole_job_rate(n, e2e_steps, 1e3 * e2e_s, ws)

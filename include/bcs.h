@@ -296,6 +296,20 @@ bcs_status bcs_set_particles(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velociti
                              bcs_vec3 forces, bcs_memory where);
 bcs_status bcs_get_particles(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velocities,
                              bcs_vec3 forces, bcs_memory where);
+/* The same read into host memory without waiting, for a renderer that
+ * takes frame f while frame f + 1 is computed (the per-frame read of
+ * main.cu:183-184, overlapped).  The state as bcs_get_particles would read
+ * it now is converted on the simulation's stream and copied to the host
+ * buffers (pinned memory for speed) on a copy stream; the call returns at
+ * once and later frames run meanwhile.  The buffers must stay valid and
+ * must not be read before bcs_wait_particles returns.  Two reads may be in
+ * flight; a third makes the simulation's stream (not the host) wait for the
+ * oldest.  A NULL component is skipped.  Allocates 36 bytes per particle
+ * for each of two slots on first use. */
+bcs_status bcs_get_particles_async(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 velocities,
+                                   bcs_vec3 forces);
+/* Waits until every bcs_get_particles_async read has reached the host. */
+bcs_status bcs_wait_particles(bcs_sim* sim);
 /* Initial particle state on the device (no reference counterpart as an
  * API; the reference places its cells in SimulationController's
  * constructor).

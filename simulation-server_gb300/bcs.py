@@ -34,7 +34,8 @@ EXPORTED = [
     "bcs_surrogate_enable", "bcs_surrogate_get_stats", "bcs_surrogate_reset_stats", "bcs_surrogate_param_count",
     "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
     "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales", "bcs_time_macro_steps",
-    "bcs_init_particles", "bcs_set_tensor_path", "bcs_tensor_wait_expiries",
+    "bcs_init_particles", "bcs_set_tensor_path", "bcs_tensor_wait_expiries", "bcs_get_particles_async",
+    "bcs_wait_particles",
 ]
 INIT_REFERENCE, INIT_LATTICE = 0, 1
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
@@ -200,6 +201,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_get_info": ([P, C.POINTER(Info)], C.c_int),
         "bcs_set_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
         "bcs_get_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
+        "bcs_get_particles_async": ([P, Vec3, Vec3, Vec3], C.c_int),
+        "bcs_wait_particles": ([P], C.c_int),
         "bcs_set_vein": ([P, Vec3, Vec3, C.c_int], C.c_int),
         "bcs_get_vein": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
         "bcs_calculate_grids": ([P], C.c_int),
@@ -336,6 +339,7 @@ class Simulation:
             self._bufs = SceneBuffers(scene)
             _check(self.lib.bcs_create(C.byref(self._bufs.desc), stream, C.byref(h)), "bcs_create")
         self.h = h
+        self._async_keep = []
         self.info = Info()
         _check(self.lib.bcs_get_info(self.h, C.byref(self.info)), "bcs_get_info")
         self.n = self.info.particle_count
@@ -372,6 +376,25 @@ class Simulation:
         vecs = [Vec3(a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data) for a in out]
         _check(self.lib.bcs_get_particles(self.h, vecs[0], vecs[1], vecs[2], MEM_HOST), "bcs_get_particles")
         return tuple(np.ascontiguousarray(a.T) for a in out)
+
+    def get_particles_async(self, pos=None, vel=None, force=None) -> None:
+        """Start reading the state into caller-owned host arrays without
+        waiting (bcs_get_particles_async): each a C-contiguous float32 array
+        of shape (3, n), rows x, y, z, kept alive and unread until
+        wait_particles()."""
+        def v3(a):
+            if a is None:
+                return Vec3()
+            if a.dtype != np.float32 or a.shape != (3, self.n) or not a.flags.c_contiguous:
+                raise ValueError("expected a C-contiguous float32 array of shape (3, n)")
+            return Vec3(a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data)
+        vecs = (v3(pos), v3(vel), v3(force))
+        self._async_keep.append((pos, vel, force))
+        _check(self.lib.bcs_get_particles_async(self.h, *vecs), "bcs_get_particles_async")
+
+    def wait_particles(self) -> None:
+        _check(self.lib.bcs_wait_particles(self.h), "bcs_wait_particles")
+        self._async_keep.clear()
 
     def init_particles(self, kind: int = INIT_LATTICE, seed: int = 0, velocity_sigma: float = 0.0,
                        gap: float = 0.2) -> None:

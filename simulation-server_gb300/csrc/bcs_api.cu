@@ -198,6 +198,13 @@ struct bcs_sim {
     cudaEvent_t pev[BCS_PHASE_COUNT + 1] = {};
     float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
     int kernels_per_step = 0;
+    // asynchronous reads of the particle state (bcs_get_particles_async):
+    // two slots of 9 N floats, converted on `stream`, copied on `copy_stream`
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t aready[2] = {}, adone[2] = {};
+    float* ascratch[2] = {};
+    bool ainflight[2] = {};
+    int aslot = 0;
 };
 
 namespace {
@@ -914,6 +921,14 @@ void destroy_impl(bcs_sim* s) {
     if (s->ev1) cudaEventDestroy(s->ev1);
     for (auto& e : s->pev)
         if (e) cudaEventDestroy(e);
+    if (s->copy_stream) {
+        cudaStreamSynchronize(s->copy_stream);
+        cudaStreamDestroy(s->copy_stream);
+    }
+    for (int k = 0; k < 2; ++k) {
+        if (s->aready[k]) cudaEventDestroy(s->aready[k]);
+        if (s->adone[k]) cudaEventDestroy(s->adone[k]);
+    }
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -1314,6 +1329,54 @@ bcs_status bcs_get_particles(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities
     if ((st = get_vec(s, s->pos[b], s->N, positions, where))) return st;
     if ((st = get_vec(s, s->vel[b], s->N, velocities, where))) return st;
     return get_vec(s, s->frc[b], s->N, forces, where);
+}
+
+bcs_status bcs_get_particles_async(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs_vec3 forces) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    const bcs_vec3 req[3] = {positions, velocities, forces};
+    if (!s->copy_stream) {
+        BCS_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            BCS_CUDA(cudaEventCreateWithFlags(&s->aready[k], cudaEventDisableTiming));
+            BCS_CUDA(cudaEventCreateWithFlags(&s->adone[k], cudaEventDisableTiming));
+        }
+    }
+    const int k = s->aslot;
+    if (!s->ascratch[k]) {
+        bcs_status st = dalloc(s, &s->ascratch[k], 9 * (size_t)s->N);
+        if (st != BCS_OK) return st;
+    }
+    // the slot's previous copy must be done before its scratch is rewritten
+    if (s->ainflight[k]) BCS_CUDA(cudaStreamWaitEvent(s->stream, s->adone[k], 0));
+    const int b = s->mid_frame ? (s->cur ^ 1) : s->cur;
+    const float4* src[3] = {s->pos[b], s->vel[b], s->frc[b]};
+    const size_t n = (size_t)s->N, bytes = sizeof(float) * n;
+    for (int q = 0; q < 3; ++q) {
+        const bcs_vec3& v = req[q];
+        if (!v.x && !v.y && !v.z) continue;
+        float* d = s->ascratch[k] + 3 * n * q;
+        launch_unpack(src[q], s->N, v.x ? d : nullptr, v.y ? d + n : nullptr, v.z ? d + 2 * n : nullptr, s->stream);
+    }
+    BCS_CUDA(cudaEventRecord(s->aready[k], s->stream));
+    BCS_CUDA(cudaStreamWaitEvent(s->copy_stream, s->aready[k], 0));
+    for (int q = 0; q < 3; ++q) {
+        const bcs_vec3& v = req[q];
+        float* d = s->ascratch[k] + 3 * n * q;
+        if (v.x) BCS_CUDA(cudaMemcpyAsync(v.x, d, bytes, cudaMemcpyDeviceToHost, s->copy_stream));
+        if (v.y) BCS_CUDA(cudaMemcpyAsync(v.y, d + n, bytes, cudaMemcpyDeviceToHost, s->copy_stream));
+        if (v.z) BCS_CUDA(cudaMemcpyAsync(v.z, d + 2 * n, bytes, cudaMemcpyDeviceToHost, s->copy_stream));
+    }
+    BCS_CUDA(cudaEventRecord(s->adone[k], s->copy_stream));
+    s->ainflight[k] = true;
+    s->aslot ^= 1;
+    return check_last();
+}
+
+bcs_status bcs_wait_particles(bcs_sim* s) {
+    if (!s) return BCS_ERR_INVALID_ARGUMENT;
+    if (s->copy_stream) BCS_CUDA(cudaStreamSynchronize(s->copy_stream));
+    s->ainflight[0] = s->ainflight[1] = false;
+    return check_last();
 }
 
 bcs_status bcs_set_vein(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs_memory where) {

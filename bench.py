@@ -591,14 +591,17 @@ def run_ours(args):
         gpu_id = "GPU-" + gpu_id
     sampler = ClockSampler(gpu_id)
     time.sleep(0.3)
+    crowded0 = sim.crowded_particles()
     ms = sim.time_steps(args.steps)
     clocks = sampler.stop()
     barrier(sim)
+    crowded_per_frame = (sim.crowded_particles() - crowded0) / args.steps
     ms_max = max_over_ranks(ms)
     value = whole_job_rate(n, args.steps, ms, ws)
     info = sim.refresh_info()
     launches = info.kernels_per_step * args.steps
     diag = grid_diagnostics(sim)
+    diag["crowded_particles_per_frame"] = crowded_per_frame
     sim.close()
 
     # ---- pass 2: the same frames eagerly, CUDA events between the phases;

@@ -310,6 +310,11 @@ bcs_status bcs_get_particles_async(bcs_sim* sim, bcs_vec3 positions, bcs_vec3 ve
                                    bcs_vec3 forces);
 /* Waits until every bcs_get_particles_async read has reached the host. */
 bcs_status bcs_wait_particles(bcs_sim* sim);
+/* Particles the step kernel set aside as crowded (more than 128 sorted slots
+ * in their 27-cell collision stencil; a second kernel finishes them), summed
+ * over every step since the simulation was created.  A diagnostic of piled-up
+ * cells (no reference counterpart). */
+bcs_status bcs_get_crowded(bcs_sim* sim, long long* particles);
 /* Initial particle state on the device (no reference counterpart as an
  * API; the reference places its cells in SimulationController's
  * constructor).

@@ -35,7 +35,7 @@ EXPORTED = [
     "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
     "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales", "bcs_time_macro_steps",
     "bcs_init_particles", "bcs_set_tensor_path", "bcs_tensor_wait_expiries", "bcs_get_particles_async",
-    "bcs_wait_particles",
+    "bcs_wait_particles", "bcs_get_crowded",
 ]
 INIT_REFERENCE, INIT_LATTICE = 0, 1
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
@@ -203,6 +203,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_get_particles": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
         "bcs_get_particles_async": ([P, Vec3, Vec3, Vec3], C.c_int),
         "bcs_wait_particles": ([P], C.c_int),
+        "bcs_get_crowded": ([P, C.POINTER(C.c_longlong)], C.c_int),
         "bcs_set_vein": ([P, Vec3, Vec3, C.c_int], C.c_int),
         "bcs_get_vein": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
         "bcs_calculate_grids": ([P], C.c_int),
@@ -391,6 +392,12 @@ class Simulation:
         vecs = (v3(pos), v3(vel), v3(force))
         self._async_keep.append((pos, vel, force))
         _check(self.lib.bcs_get_particles_async(self.h, *vecs), "bcs_get_particles_async")
+
+    def crowded_particles(self) -> int:
+        """Particles set aside as crowded, summed over all steps so far."""
+        v = C.c_longlong()
+        _check(self.lib.bcs_get_crowded(self.h, C.byref(v)), "bcs_get_crowded")
+        return int(v.value)
 
     def wait_particles(self) -> None:
         _check(self.lib.bcs_wait_particles(self.h), "bcs_wait_particles")

@@ -836,10 +836,10 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     if ((st = dalloc(s, &s->work, s->work_capacity)) || (st = dalloc(s, &s->order_idx, s->work_capacity)) ||
         (st = dalloc(s, &s->order_pos, s->work_capacity)) || (st = dalloc(s, &s->work_counter, 2)) ||
         (st = dalloc(s, &s->crowded, s->N)) || (st = dalloc(s, &s->crowded_cells, s->N)) ||
-        (st = dalloc(s, &s->crowded_counter, 4)) || (st = dalloc(s, &s->cent, s->C)))
+        (st = dalloc(s, &s->crowded_counter, 6)) || (st = dalloc(s, &s->cent, s->C)))
         return st;
     BCS_CUDA(cudaMemset(s->work_counter, 0, 2 * sizeof(int)));
-    BCS_CUDA(cudaMemset(s->crowded_counter, 0, 4 * sizeof(int)));
+    BCS_CUDA(cudaMemset(s->crowded_counter, 0, 6 * sizeof(int)));
     s->args.crowded = s->crowded;
     s->args.crowded_cells = s->crowded_cells;
     s->args.crowded_counter = s->crowded_counter;
@@ -1369,6 +1369,15 @@ bcs_status bcs_get_particles_async(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velo
     BCS_CUDA(cudaEventRecord(s->adone[k], s->copy_stream));
     s->ainflight[k] = true;
     s->aslot ^= 1;
+    return check_last();
+}
+
+bcs_status bcs_get_crowded(bcs_sim* s, long long* particles) {
+    if (!s || !particles) return BCS_ERR_INVALID_ARGUMENT;
+    unsigned long long v = 0;
+    BCS_CUDA(cudaMemcpyAsync(&v, s->crowded_counter + 4, sizeof(v), cudaMemcpyDeviceToHost, s->stream));
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    *particles = (long long)v;
     return check_last();
 }
 

@@ -134,7 +134,8 @@ struct StepArgs {
     int* work_counter;    // persistent launches: next item, CTAs finished
     int* crowded;         // crowded particles off the grid's regular stencils, left to k_crowded (capacity n)
     int* crowded_cells;   // one particle per crowded grid cell, left to k_crowded (capacity n)
-    int* crowded_counter; // [0] crowded entries, [1] CTAs of k_crowded finished, [2] crowded_cells entries
+    int* crowded_counter; // [0] crowded entries, [1] CTAs of k_crowded finished, [2] crowded_cells entries,
+                          // [3] particles of the listed cells taken, [4..5] 64-bit running total
     float4* cent;         // this step's cell centroids (batch-wide cell index), for k_crowded
     const TypeDev* types;
     int type_count;

@@ -201,7 +201,7 @@ __device__ inline int2 row_range(const GridDev& g, const GridGeom& geo, int ep, 
 // this is crowded: a whole warp takes its collision search
 // (heavy_collisions).  The split depends only on the state, so every launch
 // shape sums each particle's collisions in the same order.
-constexpr int kCrowdedSlots = 48;
+constexpr int kCrowdedSlots = 128;
 
 // One candidate of particle (x, v, R): detectCollision's test, then the
 // resilient force with the neighbour's velocity (fetched only on a hit).
@@ -694,6 +694,7 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
     __shared__ float4 s_cpos[kCrowdedThreads / 32][kCrowdedStage];
     __shared__ float4 s_cvel[kCrowdedThreads / 32][kCrowdedStage];
     const int count = a.crowded_counter[0], ncells = a.crowded_counter[2];
+    if (count == 0 && ncells == 0) return;   // every CTA sees the same counts: nothing to reset
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gwarp = (blockIdx.x * kCrowdedThreads + threadIdx.x) >> 5;
     const int nwarps = gridDim.x * (kCrowdedThreads / 32);
@@ -707,6 +708,7 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
         int rs[9], rf[9];
         const int total = stencil_rows(g, sc.pg, st, lane, rs, rf);
         const int4 own = __ldg(&g.table[sc.pg.key_offset + st.cell]);
+        int taken = 0;   // particles of the cell this warp finished
         for (int s0 = own.x; s0 <= own.y; s0 += 32) {
             // G particles of the cell in this pass, L lanes each (the
             // largest power of two with G * L <= 32): lane = particle * L +
@@ -760,6 +762,7 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
                 acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
                 acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
             }
+            taken += __popc(__ballot_sync(0xffffffffu, pid >= 0 && sub == 0));
             if (pid >= 0 && sub == 0) {
                 const TypeDev& ty = a.types[type_of_particle(a, pid)];
                 const int rel = pid - ty.particle_start, cell = rel / ty.pic, li = rel - cell * ty.pic;
@@ -769,7 +772,10 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
             }
         }
         // release the claim: the table is clean for a step on the same grid
-        if (lane == 0) const_cast<int4*>(g.table)[sc.pg.key_offset + st.cell].w = 0;
+        if (lane == 0) {
+            const_cast<int4*>(g.table)[sc.pg.key_offset + st.cell].w = 0;
+            atomicAdd(&a.crowded_counter[3], taken);
+        }
     }
     // batches of up to 32 particles, as small as the list allows: a warp's
     // collision sums run one after another
@@ -798,9 +804,15 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(&a.crowded_counter[1], 1) == (int)gridDim.x - 1) {
-            a.crowded_counter[0] = 0;
-            a.crowded_counter[1] = 0;
-            a.crowded_counter[2] = 0;
+            __threadfence();
+            // running total of crowded particles (64 bits at [4]); atomic
+            // reads, since this CTA's cache may hold the counters' line
+            const unsigned listed = (unsigned)atomicExch(&a.crowded_counter[0], 0);
+            const unsigned taken = (unsigned)atomicExch(&a.crowded_counter[3], 0);
+            atomicAdd(reinterpret_cast<unsigned long long*>(a.crowded_counter + 4),
+                      (unsigned long long)listed + taken);
+            atomicExch(&a.crowded_counter[2], 0);
+            atomicExch(&a.crowded_counter[1], 0);
         }
     }
 }

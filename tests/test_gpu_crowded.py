@@ -1,4 +1,4 @@
-"""Crowded particles.  A particle whose collision stencil holds more than 48
+"""Crowded particles.  A particle whose collision stencil holds more than 128
 sorted slots is left by the step kernel to k_crowded: inside the grid box a
 warp takes its whole grid cell (the stencil's slots staged in shared memory,
 the lanes of each particle splitting them), outside it a warp takes the
@@ -21,7 +21,7 @@ import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-CROWDED = 48
+CROWDED = 128
 
 
 def rel_err(g, o):
@@ -30,17 +30,18 @@ def rel_err(g, o):
     return float(np.max(np.abs(np.asarray(g, np.float64) - o) / scale))
 
 
-def crowded_scene(seed=4, spread=0.7, vel=2.0, anchors=None, **kw):
-    """60 icosphere cells piled in threes onto three points of a straight
-    vessel, each cell a little off its point."""
-    sc = S.straight_scene(cells=60, seed=seed, radius=14.0, length=90.0, around=32, rings=40, **kw)
+def crowded_scene(seed=4, spread=0.7, vel=2.0, anchors=None, cells=60, length=90.0, **kw):
+    """Icosphere cells of a straight vessel piled onto the given points (by
+    default all 60 onto one), each cell a little off its point."""
+    sc = S.straight_scene(cells=cells, seed=seed, radius=14.0, length=length, around=32, rings=int(length / 2.25),
+                          **kw)
     rng = np.random.default_rng(seed)
     pic = len(sc.types[0].vertices)
     if anchors is None:
-        anchors = [[0.0, -20.0, 0.0], [3.0, -45.0, -2.0], [-4.0, -70.0, 3.0]]
+        anchors = [[0.0, -45.0, 0.0]]
     anchors = np.array(anchors, np.float32)
     P = sc.positions.reshape(-1, pic, 3)
-    off = anchors[np.arange(len(P)) % 3][:, None, :] + rng.normal(0, spread, (len(P), 1, 3)).astype(np.float32)
+    off = anchors[np.arange(len(P)) % len(anchors)][:, None, :] + rng.normal(0, spread, (len(P), 1, 3)).astype(np.float32)
     sc.positions[:] = (P - P.mean(1, keepdims=True) + off).reshape(-1, 3)
     sc.velocities[:] = rng.normal(0, vel, sc.velocities.shape).astype(np.float32)
     return sc
@@ -78,6 +79,19 @@ def test_scene_is_crowded():
     sc = crowded_scene()
     n = stencil_slots(sc, sc.positions)
     assert (n > CROWDED).sum() > 1000 and (n <= CROWDED).sum() > 100
+
+
+def test_crowded_count(lib):
+    """bcs_get_crowded counts the particles set aside, once per step."""
+    sc = crowded_scene()
+    sim = make(sc)
+    assert sim.crowded_particles() == 0
+    sim.step(1)
+    host = int((stencil_slots(sc, sc.positions) > CROWDED).sum())
+    got = sim.crowded_particles()
+    assert abs(got - host) <= 0.01 * host, (got, host)
+    sim.step(2)
+    assert sim.crowded_particles() > 2 * got
 
 
 def test_one_step_matches_oracle(lib):
@@ -145,7 +159,9 @@ def test_crowded_outside_the_grid_box(lib):
     """A pile beyond the grid box's top face: clamped keys, so those
     particles' stencils are not their cell's regular one (the per-particle
     warp path); the other two piles are inside."""
-    sc = crowded_scene(anchors=[[0.0, 47.0, 0.0], [3.0, -45.0, -2.0], [-4.0, -70.0, 3.0]], use_blood_flow=False)
+    sc = crowded_scene(anchors=[[0.0, 47.0, 0.0], [3.0, -45.0, -2.0]], cells=120, length=150.0, use_blood_flow=False)
+    inside = sc.positions[:, 1] < 0
+    assert (stencil_slots(sc, sc.positions)[inside] > CROWDED).sum() > 1000
     top = sc.positions[:, 1].max()
     assert top > sc.vein_positions[:, 1].max() + sc.params.grid_y_margin
     sim = make(sc)

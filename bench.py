@@ -722,8 +722,9 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--learned-substeps", type=int, default=8)
     ap.add_argument("--learned-macro-steps", type=int, default=40)
-    ap.add_argument("--learned-collect", type=int, default=4)
-    ap.add_argument("--learned-iters", type=int, default=2000)
+    ap.add_argument("--learned-collect", type=int, default=97,
+                    help="training macro steps collected (97 x 20 588 disc cells = 2.0M cell-steps)")
+    ap.add_argument("--learned-iters", type=int, default=4000)
     ap.add_argument("--learned-batch", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:

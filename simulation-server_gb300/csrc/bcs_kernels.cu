@@ -1409,15 +1409,18 @@ __device__ inline void fused_gemm_h(const float* Hs, const __nv_bfloat16* Ws, fl
                                     int t) {
     const float* lo = Hs + r_lo * kFusedHP + 2 * t;
     const float* hi = lo + 8 * kFusedHP;
+    const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int ks = 0; ks < kHidden / 16; ++ks) {
         const int k0 = ks * 16;
         const uint32_t a0 = pack_bf16(lo[k0], lo[k0 + 1]), a1 = pack_bf16(hi[k0], hi[k0 + 1]);
         const uint32_t a2 = pack_bf16(lo[k0 + 8], lo[k0 + 9]), a3 = pack_bf16(hi[k0 + 8], hi[k0 + 9]);
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            const __nv_bfloat16* bp = Ws + (nt * 8 + g) * kFusedBP + k0 + 2 * t;
-            mma_bf16(acc[nt], a0, a1, a2, a3, ld32(bp), ld32(bp + 8));
+        for (int nt = 0; nt < 16; nt += 2) {
+            uint32_t b0, b1, b2, b3;
+            ldsm_b_pair(Ws, kFusedBP, nt * 8, k0, lane, b0, b1, b2, b3);
+            mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+            mma_bf16(acc[nt + 1], a0, a1, a2, a3, b2, b3);
         }
     }
 }
@@ -1427,14 +1430,17 @@ __device__ inline void fused_gemm_b(const __nv_bfloat16* Bs, const __nv_bfloat16
                                     int g, int t) {
     const __nv_bfloat16* lo = Bs + r_lo * kFusedBP + 2 * t;
     const __nv_bfloat16* hi = lo + 8 * kFusedBP;
+    const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int ks = 0; ks < kHidden / 16; ++ks) {
         const int k0 = ks * 16;
         const uint32_t a0 = ld32(lo + k0), a1 = ld32(hi + k0), a2 = ld32(lo + k0 + 8), a3 = ld32(hi + k0 + 8);
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            const __nv_bfloat16* bp = Ws + (nt * 8 + g) * kFusedBP + k0 + 2 * t;
-            mma_bf16(acc[nt], a0, a1, a2, a3, ld32(bp), ld32(bp + 8));
+        for (int nt = 0; nt < 16; nt += 2) {
+            uint32_t b0, b1, b2, b3;
+            ldsm_b_pair(Ws, kFusedBP, nt * 8, k0, lane, b0, b1, b2, b3);
+            mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+            mma_bf16(acc[nt + 1], a0, a1, a2, a3, b2, b3);
         }
     }
 }
@@ -1546,46 +1552,53 @@ __global__ void __launch_bounds__(MT * 32, 1)
             }
         }
         __syncthreads();
-        // M = mean over the springs of B_j + ebar W_e + b_e: this thread's two rows, 32 columns
+        // M = mean over the springs of B_j + ebar W_e + b_e for the warp's 16
+        // rows, one row at a time: lane l holds columns 4l..4l+3, so a
+        // neighbour's row is one conflict-free 256-byte read and the spring
+        // loop is the same for the whole warp
         float m[16][4];
         const float* We = Wsm;
         const float* be = Wsm + kEdgeIn * kHidden;
+        const int c4 = 4 * lane;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int r = r_lo + 8 * h;
+        for (int i = 0; i < 16; ++i) {
+            const int r = warp * 16 + i;
             const int e0 = Goff[r], e1 = Goff[r + 1];
-#pragma unroll
-            for (int nt = 0; nt < 16; ++nt) m[nt][2 * h] = m[nt][2 * h + 1] = 0.f;
-#pragma unroll
-            for (int half = 0; half < 2; ++half)
-                for (int k = e0; k < e1; ++k) {
-                    const __nv_bfloat16* bj = Bs + Gnbr[k] * kFusedBP + 2 * t + half * 64;
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162*>(bj + q * 8);
-                        m[half * 8 + q][2 * h] += __low2float(v);
-                        m[half * 8 + q][2 * h + 1] += __high2float(v);
-                    }
-                }
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+            for (int k = e0; k < e1; ++k) {
+                const uint2 v = *reinterpret_cast<const uint2*>(Bs + Gnbr[k] * kFusedBP + c4);
+                const __nv_bfloat162 lo = *reinterpret_cast<const __nv_bfloat162*>(&v.x);
+                const __nv_bfloat162 hi = *reinterpret_cast<const __nv_bfloat162*>(&v.y);
+                s0 += __low2float(lo);
+                s1 += __high2float(lo);
+                s2 += __low2float(hi);
+                s3 += __high2float(hi);
+            }
             const float inv = 1.0f / (float)max(1, e1 - e0);
-            const float* eb = Node + r * kEdgeIn;
+            const float4 eb0 = *reinterpret_cast<const float4*>(Node + r * kEdgeIn);
+            const float4 eb1 = *reinterpret_cast<const float4*>(Node + r * kEdgeIn + 4);
+            const float eb[kEdgeIn] = {eb0.x, eb0.y, eb0.z, eb0.w, eb1.x, eb1.y, eb1.z, eb1.w};
+            const float4 b4 = *reinterpret_cast<const float4*>(be + c4);
+            float tt[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-            for (int nt = 0; nt < 16; ++nt)
+            for (int q = 0; q < kEdgeIn; ++q) {
+                const float4 w = *reinterpret_cast<const float4*>(We + q * kHidden + c4);
+                tt[0] = fmaf(eb[q], w.x, tt[0]);
+                tt[1] = fmaf(eb[q], w.y, tt[1]);
+                tt[2] = fmaf(eb[q], w.z, tt[2]);
+                tt[3] = fmaf(eb[q], w.w, tt[3]);
+            }
+            const float sum[4] = {s0, s1, s2, s3};
 #pragma unroll
-                for (int u = 0; u < 2; ++u) {
-                    const int c = nt * 8 + 2 * t + u;
-                    float tt = be[c];
-#pragma unroll
-                    for (int q = 0; q < kEdgeIn; ++q) tt = fmaf(eb[q], We[q * kHidden + c], tt);
-                    m[nt][2 * h + u] = r < pic ? m[nt][2 * h + u] * inv + tt : 0.f;
-                }
+            for (int u = 0; u < 4; ++u) m[i][u] = r < pic ? sum[u] * inv + tt[u] : 0.f;
         }
         __syncthreads();   // every read of B is done
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            const int c = nt * 8 + 2 * t;
-            *reinterpret_cast<uint32_t*>(Bs + r_lo * kFusedBP + c) = pack_bf16(m[nt][0], m[nt][1]);
-            *reinterpret_cast<uint32_t*>(Bs + (r_lo + 8) * kFusedBP + c) = pack_bf16(m[nt][2], m[nt][3]);
+        for (int i = 0; i < 16; ++i) {
+            uint2 w;
+            w.x = pack_bf16(m[i][0], m[i][1]);
+            w.y = pack_bf16(m[i][2], m[i][3]);
+            *reinterpret_cast<uint2*>(Bs + (warp * 16 + i) * kFusedBP + c4) = w;
         }
         stage_weight(PBT + L.wu[l], Ws, NT);
         __syncthreads();

@@ -1386,7 +1386,7 @@ __global__ void k_lattice_place(const StepArgs a, int scene, float4* pos, float4
 // The same rounding points as the layer-by-layer kernels.  The epilogue is
 // k_sur_apply's: decode, residual check, state and grid keys of a passing
 // cell, skip flag and counts.
-constexpr int kFusedHP = kHidden + 4;   // FP32 row stride of h
+constexpr int kFusedHP = kHidden + 8;   // FP32 row stride of h (8 banks apart: 64-bit fragment reads conflict-free)
 constexpr int kFusedBP = kHidden + 8;   // bf16 row stride
 constexpr int kFusedW = 2176;           // floats of the small-weight area
 constexpr int kFusedMaxEdges = 1536;    // directed springs of one cell held in shared memory
@@ -1403,6 +1403,20 @@ __device__ inline void stage_weight(const __nv_bfloat16* __restrict__ Wt, __nv_b
         *reinterpret_cast<uint4*>(Ws + n * kFusedBP + k) = *reinterpret_cast<const uint4*>(Wt + n * kHidden + k);
     }
 }
+
+// The same copy with cp.async (16 bytes per thread and step), left in flight:
+// stage_weight_wait() completes it for this thread; a barrier after that
+// publishes it to the CTA.
+__device__ inline void stage_weight_async(const __nv_bfloat16* __restrict__ Wt, __nv_bfloat16* Ws, int nthreads) {
+    for (int q = threadIdx.x; q < kHidden * (kHidden / 8); q += nthreads) {
+        const int n = q >> 4, k = (q & 15) * 8;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(Ws + n * kFusedBP + k);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(Wt + n * kHidden + k) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ inline void stage_weight_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // acc (this warp's 16 rows x 128) += H (FP32 smem, rounded to bf16) x Ws^T.
 __device__ inline void fused_gemm_h(const float* Hs, const __nv_bfloat16* Ws, float (&acc)[16][4], int r_lo, int g,
@@ -1485,19 +1499,27 @@ __global__ void __launch_bounds__(MT * 32, 1)
         red[2] = 0;   // leaves the vein
     }
     __syncthreads();
+    // a warp per row, lane l on columns 4l..4l+3: every weight row is one
+    // conflict-free 512-byte read and the row of h one 512-byte write
     for (int i = tid; i < R * (kHidden / 4); i += NT) {
         const int r = i >> 5, c0 = (i & 31) * 4;
         float fr[kFeatIn];
 #pragma unroll
         for (int q = 0; q < kFeatIn; ++q) fr[q] = F0[r * 16 + q];
+        const float4 b4 = *reinterpret_cast<const float4*>(Wsm + kFeatIn * kHidden + c0);
+        float z[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int c = c0 + j;
-            float z = Wsm[kFeatIn * kHidden + c];
-#pragma unroll
-            for (int q = 0; q < kFeatIn; ++q) z = fmaf(fr[q], Wsm[q * kHidden + c], z);
-            Hs[r * kFusedHP + c] = r < pic ? silu_f(z) : 0.f;
+        for (int q = 0; q < kFeatIn; ++q) {
+            const float4 w = *reinterpret_cast<const float4*>(Wsm + q * kHidden + c0);
+            z[0] = fmaf(fr[q], w.x, z[0]);
+            z[1] = fmaf(fr[q], w.y, z[1]);
+            z[2] = fmaf(fr[q], w.z, z[2]);
+            z[3] = fmaf(fr[q], w.w, z[3]);
         }
+        const bool live = r < pic;
+        *reinterpret_cast<float4*>(Hs + r * kFusedHP + c0) =
+            make_float4(live ? silu_f(z[0]) : 0.f, live ? silu_f(z[1]) : 0.f, live ? silu_f(z[2]) : 0.f,
+                        live ? silu_f(z[3]) : 0.f);
     }
     __syncthreads();
     float* RU = F0;   // raw r, u of every node (stride 6) while Bs is free
@@ -1552,6 +1574,8 @@ __global__ void __launch_bounds__(MT * 32, 1)
             }
         }
         __syncthreads();
+        // W_u streams into the weight tile (free now) during the aggregation
+        stage_weight_async(PBT + L.wu[l], Ws, NT);
         // M = mean over the springs of B_j + ebar W_e + b_e for the warp's 16
         // rows, one row at a time: lane l holds columns 4l..4l+3, so a
         // neighbour's row is one conflict-free 256-byte read and the spring
@@ -1600,7 +1624,7 @@ __global__ void __launch_bounds__(MT * 32, 1)
             w.y = pack_bf16(m[i][2], m[i][3]);
             *reinterpret_cast<uint2*>(Bs + (warp * 16 + i) * kFusedBP + c4) = w;
         }
-        stage_weight(PBT + L.wu[l], Ws, NT);
+        stage_weight_wait();
         __syncthreads();
         float accU[16][4];
 #pragma unroll
@@ -1618,8 +1642,11 @@ __global__ void __launch_bounds__(MT * 32, 1)
                 const int r = r_lo + 8 * h;
                 if (r >= pic) continue;
                 const int c = nt * 8 + 2 * t;
-                Hs[r * kFusedHP + c] += silu_f(accU[nt][2 * h] + bu[c]);
-                Hs[r * kFusedHP + c + 1] += silu_f(accU[nt][2 * h + 1] + bu[c + 1]);
+                float2* hp = reinterpret_cast<float2*>(Hs + r * kFusedHP + c);
+                float2 hv = *hp;
+                hv.x += silu_f(accU[nt][2 * h] + bu[c]);
+                hv.y += silu_f(accU[nt][2 * h + 1] + bu[c + 1]);
+                *hp = hv;
             }
         __syncthreads();
     }

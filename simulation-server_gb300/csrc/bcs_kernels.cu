@@ -1391,10 +1391,27 @@ constexpr int kFusedBP = kHidden + 8;   // bf16 row stride
 constexpr int kFusedW = 2176;           // floats of the small-weight area
 constexpr int kFusedMaxEdges = 1536;    // directed springs of one cell held in shared memory
 
+// Small-weight area of the double-buffered layout: W_e, b_e, b_u, b_b of a
+// layer, or W_out and b_out (the encoder's weights go to the second tile).
+constexpr int kFusedWDb = kEdgeIn * kHidden + 3 * kHidden;
+
 template <int MT>
-constexpr int fused_smem_bytes() {
+__host__ __device__ constexpr int fused_smem_single() {
     return MT * 16 * kFusedHP * 4 + MT * 16 * kFusedBP * 2 + kHidden * kFusedBP * 2 + MT * 16 * kEdgeIn * 4 +
            kFusedW * 4 + MT * 16 * kOut * 4 + 16 + (MT * 16 + 1) * 4 + kFusedMaxEdges * 4;
+}
+// Two weight tiles (the next product's weights stream in with cp.async while
+// the current one runs); the decoder's output shares the message buffer.
+template <int MT>
+__host__ __device__ constexpr int fused_smem_double() {
+    return MT * 16 * kFusedHP * 4 + MT * 16 * kFusedBP * 2 + 2 * kHidden * kFusedBP * 2 + MT * 16 * kEdgeIn * 4 +
+           kFusedWDb * 4 + 16 + (MT * 16 + 1) * 4 + kFusedMaxEdges * 4;
+}
+template <int MT>
+__host__ __device__ constexpr bool fused_double() { return fused_smem_double<MT>() <= 227 * 1024; }
+template <int MT>
+__host__ __device__ constexpr int fused_smem_bytes() {
+    return fused_double<MT>() ? fused_smem_double<MT>() : fused_smem_single<MT>();
 }
 
 __device__ inline void stage_weight(const __nv_bfloat16* __restrict__ Wt, __nv_bfloat16* Ws, int nthreads) {
@@ -1466,14 +1483,17 @@ __global__ void __launch_bounds__(MT * 32, 1)
                 const int* __restrict__ goff, const int* __restrict__ gnbr, const float* __restrict__ glen, int first,
                 int cells) {
     constexpr int R = MT * 16, NT = MT * 32;
+    constexpr bool DB = fused_double<MT>();
     extern __shared__ __align__(16) unsigned char smem[];
     float* Hs = reinterpret_cast<float*>(smem);
     __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(Hs + R * kFusedHP);
-    __nv_bfloat16* Ws = Bs + R * kFusedBP;
-    float* Node = reinterpret_cast<float*>(Ws + kHidden * kFusedBP);   // R x 6 raw r, u; then R x 8 ebar
+    __nv_bfloat16* Ws = Bs + R * kFusedBP;                     // weight tile (DB: the first of two)
+    __nv_bfloat16* Ws2 = DB ? Ws + kHidden * kFusedBP : Ws;   // the second tile
+    float* Node = reinterpret_cast<float*>(Ws2 + kHidden * kFusedBP);   // R x 8 ebar
     float* Wsm = Node + R * 8;
-    float* Ysm = Wsm + kFusedW;
-    int* red = reinterpret_cast<int*>(Ysm + R * kOut);
+    float* Ysm = DB ? reinterpret_cast<float*>(Bs) : Wsm + kFusedW;   // DB: after the layers, B is free
+    int* red = reinterpret_cast<int*>(DB ? Wsm + kFusedWDb : Ysm + R * kOut);
+    float* Wenc = DB ? reinterpret_cast<float*>(Ws2) : Wsm;   // encoder weights (DB: in the idle second tile)
     int* Goff = red + 4;            // R + 1 spring-list offsets (rows past the cell: empty)
     int* Gnbr = Goff + R + 1;       // the cell's directed springs
     const int b = blockIdx.x;
@@ -1491,8 +1511,9 @@ __global__ void __launch_bounds__(MT * 32, 1)
         const int r = i >> 4, q = i & 15;
         F0[i] = r < pic ? (raw[r * 16 + q] - sc.fm[q]) * sc.fs[q] : 0.f;
     }
-    for (int i = tid; i < kFeatIn * kHidden; i += NT) Wsm[i] = __bfloat162float(PB[L.w_in + i]);
-    for (int i = tid; i < kHidden; i += NT) Wsm[kFeatIn * kHidden + i] = P[L.b_in + i];
+    if (DB) stage_weight_async(PBT + L.wb[0], Ws, NT);   // streams in during the encoder
+    for (int i = tid; i < kFeatIn * kHidden; i += NT) Wenc[i] = __bfloat162float(PB[L.w_in + i]);
+    for (int i = tid; i < kHidden; i += NT) Wenc[kFeatIn * kHidden + i] = P[L.b_in + i];
     if (tid == 0) {
         red[0] = 0;   // worst residual (float bits)
         red[1] = 1;   // all finite
@@ -1506,11 +1527,11 @@ __global__ void __launch_bounds__(MT * 32, 1)
         float fr[kFeatIn];
 #pragma unroll
         for (int q = 0; q < kFeatIn; ++q) fr[q] = F0[r * 16 + q];
-        const float4 b4 = *reinterpret_cast<const float4*>(Wsm + kFeatIn * kHidden + c0);
+        const float4 b4 = *reinterpret_cast<const float4*>(Wenc + kFeatIn * kHidden + c0);
         float z[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
         for (int q = 0; q < kFeatIn; ++q) {
-            const float4 w = *reinterpret_cast<const float4*>(Wsm + q * kHidden + c0);
+            const float4 w = *reinterpret_cast<const float4*>(Wenc + q * kHidden + c0);
             z[0] = fmaf(fr[q], w.x, z[0]);
             z[1] = fmaf(fr[q], w.y, z[1]);
             z[2] = fmaf(fr[q], w.z, z[2]);
@@ -1547,22 +1568,29 @@ __global__ void __launch_bounds__(MT * 32, 1)
     }
     __syncthreads();
 
-    // ---- message-passing layers
+    // ---- message-passing layers.  DB: the weight tiles alternate; each
+    // product's successor streams into the other tile while it runs (W_b of
+    // layer l is in `cur`, then W_u in `oth`, W_v in `cur`, W_b of l + 1 in
+    // `oth`, which becomes the next layer's `cur`).
+    __nv_bfloat16* cur = Ws;
+    __nv_bfloat16* oth = Ws2;
     for (int l = 0; l < L.layers; ++l) {
-        stage_weight(PBT + L.wb[l], Ws, NT);
+        if (!DB) stage_weight(PBT + L.wb[l], Ws, NT);
         for (int i = tid; i < kEdgeIn * kHidden; i += NT) Wsm[i] = __bfloat162float(PB[L.we[l] + i]);
         for (int i = tid; i < kHidden; i += NT) {
             Wsm[kEdgeIn * kHidden + i] = P[L.be[l] + i];
             Wsm[kEdgeIn * kHidden + kHidden + i] = P[L.bu[l] + i];
             Wsm[kEdgeIn * kHidden + 2 * kHidden + i] = P[L.bb[l] + i];
         }
+        if (DB) stage_weight_wait();
         __syncthreads();
+        if (DB) stage_weight_async(PBT + L.wu[l], oth, NT);
         {
             // B = silu(h W_b + b_b), kept in bf16
             float acc[16][4];
 #pragma unroll
             for (int nt = 0; nt < 16; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-            fused_gemm_h(Hs, Ws, acc, r_lo, g, t);
+            fused_gemm_h(Hs, cur, acc, r_lo, g, t);
             const float* bb = Wsm + kEdgeIn * kHidden + 2 * kHidden;
 #pragma unroll
             for (int nt = 0; nt < 16; ++nt) {
@@ -1574,8 +1602,8 @@ __global__ void __launch_bounds__(MT * 32, 1)
             }
         }
         __syncthreads();
-        // W_u streams into the weight tile (free now) during the aggregation
-        stage_weight_async(PBT + L.wu[l], Ws, NT);
+        // single tile: W_u streams into it (free now) during the aggregation
+        if (!DB) stage_weight_async(PBT + L.wu[l], Ws, NT);
         // M = mean over the springs of B_j + ebar W_e + b_e for the warp's 16
         // rows, one row at a time: lane l holds columns 4l..4l+3, so a
         // neighbour's row is one conflict-free 256-byte read and the spring
@@ -1626,14 +1654,21 @@ __global__ void __launch_bounds__(MT * 32, 1)
         }
         stage_weight_wait();
         __syncthreads();
+        if (DB) stage_weight_async(PBT + L.wv[l], cur, NT);   // cur's W_b is done
         float accU[16][4];
 #pragma unroll
         for (int nt = 0; nt < 16; ++nt) accU[nt][0] = accU[nt][1] = accU[nt][2] = accU[nt][3] = 0.f;
-        fused_gemm_h(Hs, Ws, accU, r_lo, g, t);
-        __syncthreads();
-        stage_weight(PBT + L.wv[l], Ws, NT);
-        __syncthreads();
-        fused_gemm_b(Bs, Ws, accU, r_lo, g, t);
+        fused_gemm_h(Hs, DB ? oth : Ws, accU, r_lo, g, t);
+        if (DB) {
+            stage_weight_wait();
+            __syncthreads();   // W_v landed, and every warp is done with oth's W_u
+            if (l + 1 < L.layers) stage_weight_async(PBT + L.wb[l + 1], oth, NT);
+        } else {
+            __syncthreads();
+            stage_weight(PBT + L.wv[l], Ws, NT);
+            __syncthreads();
+        }
+        fused_gemm_b(Bs, cur, accU, r_lo, g, t);
         const float* bu = Wsm + kEdgeIn * kHidden + kHidden;
 #pragma unroll
         for (int nt = 0; nt < 16; ++nt)
@@ -1649,6 +1684,11 @@ __global__ void __launch_bounds__(MT * 32, 1)
                 *hp = hv;
             }
         __syncthreads();
+        if (DB) {
+            __nv_bfloat16* tmp = cur;
+            cur = oth;
+            oth = tmp;
+        }
     }
 
     // ---- decoder

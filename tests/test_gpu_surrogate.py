@@ -242,3 +242,27 @@ def test_tensor_paths_agree(lib):
     bcs.set_tensor_path(prev)
     assert np.abs(y0 - y1).max() <= 1e-4 * (np.abs(y1).max() + 1e-6)
     assert bcs.set_tensor_path(5) == -1
+
+
+def test_fused_inference_matches_layer_kernels_disc_cells(lib):
+    """The 162-vertex discs take the fused kernel's 11-warp shape (the other
+    tests' 42-vertex cells take the 3-warp one): same comparison."""
+    sc = S.mixed_straight_scene(4, 10, 60.0, seed=6, base_radius=14.0)
+    sc.velocities[:] = np.random.default_rng(6).normal(0, 6.0, sc.velocities.shape).astype(np.float32)
+    base = make(sc)
+    sur = bcs.Surrogate(base, cell_type=1, substeps=8, max_samples=10 * 4, seed=5)
+    sur.collect(3)
+    sur.train(20, batch_cells=8, lr=1e-3)
+    out = []
+    for fused in (True, False):
+        run = make(sc)
+        s = bcs.Surrogate(run, cell_type=1, substeps=8, max_samples=10, seed=5, tolerance=10.0)
+        s.set_params(sur.get_params())
+        s.set_scales(sur.scales())
+        s.enable(True, fused=fused)
+        run.macro_step(8, 1)
+        out.append((run.get_particles(), s.stats()))
+    (a, sa), (b, sb) = out
+    assert sa["predicted_cells"] == sb["predicted_cells"] == 10
+    for x, y in zip(a, b):
+        assert np.abs(x - y).max() <= 1e-4 * (np.abs(y).max() + 1.0)

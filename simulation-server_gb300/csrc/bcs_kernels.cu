@@ -1435,9 +1435,13 @@ __device__ inline void stage_weight_async(const __nv_bfloat16* __restrict__ Wt, 
 
 __device__ inline void stage_weight_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// acc (this warp's 16 rows x 128) += H (FP32 smem, rounded to bf16) x Ws^T.
-__device__ inline void fused_gemm_h(const float* Hs, const __nv_bfloat16* Ws, float (&acc)[16][4], int r_lo, int g,
-                                    int t) {
+// Two warps share each 16-row group: warp half `hn` owns output columns
+// 64 hn .. 64 hn + 63 (n-tiles 8 hn .. 8 hn + 7).
+constexpr int kFusedNT = 8;   // n-tiles per warp
+
+// acc (this warp's 16 rows x 64 columns) += H (FP32 smem, rounded to bf16) x Ws^T.
+__device__ inline void fused_gemm_h(const float* Hs, const __nv_bfloat16* Ws, float (&acc)[kFusedNT][4], int r_lo,
+                                    int hn, int t) {
     const float* lo = Hs + r_lo * kFusedHP + 2 * t;
     const float* hi = lo + 8 * kFusedHP;
     const int lane = threadIdx.x & 31;
@@ -1447,18 +1451,18 @@ __device__ inline void fused_gemm_h(const float* Hs, const __nv_bfloat16* Ws, fl
         const uint32_t a0 = pack_bf16(lo[k0], lo[k0 + 1]), a1 = pack_bf16(hi[k0], hi[k0 + 1]);
         const uint32_t a2 = pack_bf16(lo[k0 + 8], lo[k0 + 9]), a3 = pack_bf16(hi[k0 + 8], hi[k0 + 9]);
 #pragma unroll
-        for (int nt = 0; nt < 16; nt += 2) {
+        for (int nt = 0; nt < kFusedNT; nt += 2) {
             uint32_t b0, b1, b2, b3;
-            ldsm_b_pair(Ws, kFusedBP, nt * 8, k0, lane, b0, b1, b2, b3);
+            ldsm_b_pair(Ws, kFusedBP, (hn * kFusedNT + nt) * 8, k0, lane, b0, b1, b2, b3);
             mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
             mma_bf16(acc[nt + 1], a0, a1, a2, a3, b2, b3);
         }
     }
 }
 
-// acc += M (bf16 smem) x Ws^T.
-__device__ inline void fused_gemm_b(const __nv_bfloat16* Bs, const __nv_bfloat16* Ws, float (&acc)[16][4], int r_lo,
-                                    int g, int t) {
+// acc += M (bf16 smem) x Ws^T, the same 64 columns.
+__device__ inline void fused_gemm_b(const __nv_bfloat16* Bs, const __nv_bfloat16* Ws, float (&acc)[kFusedNT][4],
+                                    int r_lo, int hn, int t) {
     const __nv_bfloat16* lo = Bs + r_lo * kFusedBP + 2 * t;
     const __nv_bfloat16* hi = lo + 8 * kFusedBP;
     const int lane = threadIdx.x & 31;
@@ -1467,9 +1471,9 @@ __device__ inline void fused_gemm_b(const __nv_bfloat16* Bs, const __nv_bfloat16
         const int k0 = ks * 16;
         const uint32_t a0 = ld32(lo + k0), a1 = ld32(hi + k0), a2 = ld32(lo + k0 + 8), a3 = ld32(hi + k0 + 8);
 #pragma unroll
-        for (int nt = 0; nt < 16; nt += 2) {
+        for (int nt = 0; nt < kFusedNT; nt += 2) {
             uint32_t b0, b1, b2, b3;
-            ldsm_b_pair(Ws, kFusedBP, nt * 8, k0, lane, b0, b1, b2, b3);
+            ldsm_b_pair(Ws, kFusedBP, (hn * kFusedNT + nt) * 8, k0, lane, b0, b1, b2, b3);
             mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
             mma_bf16(acc[nt + 1], a0, a1, a2, a3, b2, b3);
         }
@@ -1477,12 +1481,12 @@ __device__ inline void fused_gemm_b(const __nv_bfloat16* Bs, const __nv_bfloat16
 }
 
 template <int MT>
-__global__ void __launch_bounds__(MT * 32, 1)
+__global__ void __launch_bounds__(MT * 64, 1)
     k_sur_fused(const StepArgs a, const SurDev d, const SurScales sc, const float* __restrict__ P,
                 const __nv_bfloat16* __restrict__ PB, const __nv_bfloat16* __restrict__ PBT, const MpnnLayout L,
                 const int* __restrict__ goff, const int* __restrict__ gnbr, const float* __restrict__ glen, int first,
                 int cells) {
-    constexpr int R = MT * 16, NT = MT * 32;
+    constexpr int R = MT * 16, NT = MT * 64;   // 2 MT warps: two per 16-row group
     constexpr bool DB = fused_double<MT>();
     extern __shared__ __align__(16) unsigned char smem[];
     float* Hs = reinterpret_cast<float*>(smem);
@@ -1500,7 +1504,8 @@ __global__ void __launch_bounds__(MT * 32, 1)
     if (b >= cells) return;
     const int sc_i = first + b, pic = d.pic;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-    const int r_lo = warp * 16 + g;
+    const int wr = warp % MT, hn = warp / MT;   // row group, column half
+    const int r_lo = wr * 16 + g;
     for (int i = tid; i <= R; i += NT) Goff[i] = goff[min(i, pic)];
     for (int i = tid; i < goff[pic]; i += NT) Gnbr[i] = gnbr[i];
 
@@ -1587,14 +1592,14 @@ __global__ void __launch_bounds__(MT * 32, 1)
         if (DB) stage_weight_async(PBT + L.wu[l], oth, NT);
         {
             // B = silu(h W_b + b_b), kept in bf16
-            float acc[16][4];
+            float acc[kFusedNT][4];
 #pragma unroll
-            for (int nt = 0; nt < 16; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-            fused_gemm_h(Hs, cur, acc, r_lo, g, t);
+            for (int nt = 0; nt < kFusedNT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+            fused_gemm_h(Hs, cur, acc, r_lo, hn, t);
             const float* bb = Wsm + kEdgeIn * kHidden + 2 * kHidden;
 #pragma unroll
-            for (int nt = 0; nt < 16; ++nt) {
-                const int c = nt * 8 + 2 * t;
+            for (int nt = 0; nt < kFusedNT; ++nt) {
+                const int c = (hn * kFusedNT + nt) * 8 + 2 * t;
                 *reinterpret_cast<uint32_t*>(Bs + r_lo * kFusedBP + c) =
                     pack_bf16(silu_f(acc[nt][0] + bb[c]), silu_f(acc[nt][1] + bb[c + 1]));
                 *reinterpret_cast<uint32_t*>(Bs + (r_lo + 8) * kFusedBP + c) =
@@ -1604,17 +1609,18 @@ __global__ void __launch_bounds__(MT * 32, 1)
         __syncthreads();
         // single tile: W_u streams into it (free now) during the aggregation
         if (!DB) stage_weight_async(PBT + L.wu[l], Ws, NT);
-        // M = mean over the springs of B_j + ebar W_e + b_e for the warp's 16
-        // rows, one row at a time: lane l holds columns 4l..4l+3, so a
-        // neighbour's row is one conflict-free 256-byte read and the spring
-        // loop is the same for the whole warp
-        float m[16][4];
+        // M = mean over the springs of B_j + ebar W_e + b_e for 8 rows per
+        // warp (half of its row group), one row at a time: lane l holds
+        // columns 4l..4l+3, so a neighbour's row is one conflict-free
+        // 256-byte read and the spring loop is the same for the whole warp
+        float m[8][4];
         const float* We = Wsm;
         const float* be = Wsm + kEdgeIn * kHidden;
         const int c4 = 4 * lane;
+        const int m0 = wr * 16 + hn * 8;
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const int r = warp * 16 + i;
+        for (int i = 0; i < 8; ++i) {
+            const int r = m0 + i;
             const int e0 = Goff[r], e1 = Goff[r + 1];
             float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
             for (int k = e0; k < e1; ++k) {
@@ -1646,19 +1652,19 @@ __global__ void __launch_bounds__(MT * 32, 1)
         }
         __syncthreads();   // every read of B is done
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
+        for (int i = 0; i < 8; ++i) {
             uint2 w;
             w.x = pack_bf16(m[i][0], m[i][1]);
             w.y = pack_bf16(m[i][2], m[i][3]);
-            *reinterpret_cast<uint2*>(Bs + (warp * 16 + i) * kFusedBP + c4) = w;
+            *reinterpret_cast<uint2*>(Bs + (m0 + i) * kFusedBP + c4) = w;
         }
         stage_weight_wait();
         __syncthreads();
         if (DB) stage_weight_async(PBT + L.wv[l], cur, NT);   // cur's W_b is done
-        float accU[16][4];
+        float accU[kFusedNT][4];
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt) accU[nt][0] = accU[nt][1] = accU[nt][2] = accU[nt][3] = 0.f;
-        fused_gemm_h(Hs, DB ? oth : Ws, accU, r_lo, g, t);
+        for (int nt = 0; nt < kFusedNT; ++nt) accU[nt][0] = accU[nt][1] = accU[nt][2] = accU[nt][3] = 0.f;
+        fused_gemm_h(Hs, DB ? oth : Ws, accU, r_lo, hn, t);
         if (DB) {
             stage_weight_wait();
             __syncthreads();   // W_v landed, and every warp is done with oth's W_u
@@ -1668,15 +1674,15 @@ __global__ void __launch_bounds__(MT * 32, 1)
             stage_weight(PBT + L.wv[l], Ws, NT);
             __syncthreads();
         }
-        fused_gemm_b(Bs, cur, accU, r_lo, g, t);
+        fused_gemm_b(Bs, cur, accU, r_lo, hn, t);
         const float* bu = Wsm + kEdgeIn * kHidden + kHidden;
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt)
+        for (int nt = 0; nt < kFusedNT; ++nt)
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int r = r_lo + 8 * h;
                 if (r >= pic) continue;
-                const int c = nt * 8 + 2 * t;
+                const int c = (hn * kFusedNT + nt) * 8 + 2 * t;
                 float2* hp = reinterpret_cast<float2*>(Hs + r * kFusedHP + c);
                 float2 hv = *hp;
                 hv.x += silu_f(accU[nt][2 * h] + bu[c]);
@@ -2119,7 +2125,7 @@ bool launch_fused_mt(const StepArgs& a, const SurDev& d, const SurScales& sc, co
         cudaFuncSetAttribute(k_sur_fused<MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         attr = true;
     }
-    k_sur_fused<MT><<<cells, MT * 32, bytes, s>>>(a, d, sc, P, PB, PBT, L, goff, gnbr, glen, first, cells);
+    k_sur_fused<MT><<<cells, MT * 64, bytes, s>>>(a, d, sc, P, PB, PBT, L, goff, gnbr, glen, first, cells);
     return true;
 }
 bool launch_sur_fused(const StepArgs& a, const SurDev& d, const SurScales& sc, const float* P,

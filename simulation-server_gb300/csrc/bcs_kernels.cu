@@ -1697,15 +1697,44 @@ __global__ void __launch_bounds__(MT * 64, 1)
         }
     }
 
-    // ---- decoder
-    for (int i = tid; i < kHidden * kOut; i += NT) Wsm[i] = __bfloat162float(PB[L.w_out + i]);
+    // ---- decoder on the tensor cores: W_out^T (9 outputs padded to 16) as a
+    // bf16 tile in the free weight tile; h split into bf16 high and low
+    // parts (h = hi + lo to 2^-16 relative), so y = hi W + lo W keeps the
+    // FP32 decoder's accuracy.  Warp half hn takes outputs 8 hn .. 8 hn + 7.
+    __nv_bfloat16* Wo = Ws;   // 16 rows (outputs) x 128 (hidden), stride kFusedBP
+    for (int i = tid; i < 16 * kHidden; i += NT) {
+        const int o = i / kHidden, c = i - o * kHidden;
+        Wo[o * kFusedBP + c] = o < kOut ? PB[L.w_out + c * kOut + o] : __float2bfloat16_rn(0.f);
+    }
     __syncthreads();
-    for (int i = tid; i < pic * kOut; i += NT) {
-        const int r = i / kOut, o = i - r * kOut;
-        float y = 0.f;
-#pragma unroll 8
-        for (int c = 0; c < kHidden; ++c) y = fmaf(Hs[r * kFusedHP + c], Wsm[c * kOut + o], y);
-        Ysm[i] = y + P[L.b_out + o];
+    {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        const float* lo = Hs + r_lo * kFusedHP + 2 * t;
+        const float* hi = lo + 8 * kFusedHP;
+#pragma unroll
+        for (int ks = 0; ks < kHidden / 16; ++ks) {
+            const int k0 = ks * 16;
+            const float h[8] = {lo[k0], lo[k0 + 1], hi[k0], hi[k0 + 1], lo[k0 + 8], lo[k0 + 9], hi[k0 + 8], hi[k0 + 9]};
+            float rem[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) rem[j] = h[j] - round_bf16(h[j]);
+            uint32_t b0, b1, b2, b3;
+            ldsm_b_pair(Wo, kFusedBP, 0, k0, lane, b0, b1, b2, b3);
+            const uint32_t bx = hn ? b2 : b0, by = hn ? b3 : b1;
+            mma_bf16(acc, pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]),
+                     bx, by);
+            mma_bf16(acc, pack_bf16(rem[0], rem[1]), pack_bf16(rem[2], rem[3]), pack_bf16(rem[4], rem[5]),
+                     pack_bf16(rem[6], rem[7]), bx, by);
+        }
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const int r = r_lo + 8 * h2;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int o = hn * 8 + 2 * t + u;
+                if (r < pic && o < kOut) Ysm[r * kOut + o] = acc[2 * h2 + u] + P[L.b_out + o];
+            }
+        }
     }
     __syncthreads();
 

@@ -178,3 +178,21 @@ def test_crowded_outside_the_grid_box(lib):
         for a, b in zip(other.get_particles(), want):
             np.testing.assert_array_equal(a, b)
 
+
+
+def test_batched_crowded_scenes_match_standalone(lib):
+    """Crowded cells of several scenes in one batch (batch-wide keys): every
+    scene's state equals its standalone run bit for bit."""
+    scenes = [crowded_scene(seed=s, anchors=[[0.0, -40.0 - 5.0 * (s - 7), 0.0]]) for s in (7, 8)]
+    sim = bcs.Simulation(scenes)
+    sim.set_particles(np.concatenate([s.positions for s in scenes]), np.concatenate([s.velocities for s in scenes]))
+    sim.step(3)
+    got = sim.get_particles()
+    assert sim.crowded_particles() > 0
+    for k, sc in enumerate(scenes):
+        z = sim.scene_info(k)
+        rows = slice(z.particle_start, z.particle_start + z.particle_count)
+        alone = make(sc)
+        alone.step(3)
+        for a, b in zip(got, alone.get_particles()):
+            np.testing.assert_array_equal(a[rows], b)

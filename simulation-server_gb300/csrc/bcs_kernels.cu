@@ -424,32 +424,44 @@ __device__ inline void vein_collision(const StepArgs& a, const SceneDev& sc, flo
         stencil_range_u(yId, geo.cy, y0, y1);
         stencil_range_u(zId, geo.cz, z0, z1);
         const long long cxy = (long long)geo.cx * geo.cy;
-        // Pass 1: which stencil cells the ray enters (bit k, in stencil
-        // order) and the last one it enters within reach.
+        // Stencil cell k = 9 (dx + 1) + 3 (dy + 1) + (dz + 1): stencil order
+        // (x, then y, then z).  Pass 0: which cells are in the stencil and
+        // hold triangles; the 27 table reads are independent, so they are
+        // in flight together.
+        unsigned occ = 0u;
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx)
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+                for (int dz = -1; dz <= 1; ++dz) {
+                    if (dx < x0 || dx > x1 || dy < y0 || dy > y1 || dz < z0 || dz > z1) continue;
+                    const long long c = (long long)cellId + dz * cxy + (long long)dy * geo.cx + dx;
+                    if (c < 0 || c >= geo.cells) continue;
+                    if (__ldg(&g.table[geo.key_offset + c]).z == ep) occ |= 1u << (9 * (dx + 1) + 3 * (dy + 1) + dz + 1);
+                }
+        // Pass 1: which of them the ray enters, and the last one it enters
+        // within reach.
         const float3 inv = f3(__frcp_rn(dir.x), __frcp_rn(dir.y), __frcp_rn(dir.z));
         unsigned live = 0u;
-        int last_near = -1, k = 0;
-        for (int dx = x0; dx <= x1; ++dx)
-            for (int dy = y0; dy <= y1; ++dy)
-                for (int dz = z0; dz <= z1; ++dz, ++k) {
-                    const long long c = (long long)cellId + dz * cxy + (long long)dy * geo.cx + dx;
-                    int f, l;
-                    if (!cell_range(g, geo, ep, c, f, l)) continue;
-                    const long long cg = geo.key_offset + c;
-                    const float te = ray_box_entry(x, dir, inv, __ldg(&a.tbox[2 * cg]), __ldg(&a.tbox[2 * cg + 1]));
-                    if (te > 2.9e38f) continue;
-                    live |= 1u << k;
-                    if (te <= reach) last_near = k;
-                }
+        int last_near = -1;
+        for (unsigned m = occ; m; m &= m - 1u) {
+            const int k = __ffs(m) - 1;
+            const int dz = k % 3 - 1, dy = (k / 3) % 3 - 1, dx = k / 9 - 1;
+            const long long cg = geo.key_offset + (long long)cellId + dz * cxy + (long long)dy * geo.cx + dx;
+            const float te = ray_box_entry(x, dir, inv, __ldg(&a.tbox[2 * cg]), __ldg(&a.tbox[2 * cg + 1]));
+            if (te > 2.9e38f) continue;
+            live |= 1u << k;
+            if (te <= reach) last_near = k;
+        }
         // Pass 2: triangles of the entered cells up to the last one in reach,
         // in stencil order.
-        if (last_near >= 0) live &= (last_near >= 31) ? 0xffffffffu : ((2u << last_near) - 1u);
+        if (last_near >= 0) live &= (2u << last_near) - 1u;
         else live = 0u;
-        const int ny = y1 - y0 + 1, nz = z1 - z0 + 1;
         while (live) {
             const int kk = __ffs(live) - 1;
             live &= live - 1u;
-            const int dz = z0 + kk % nz, dy = y0 + (kk / nz) % ny, dx = x0 + kk / (nz * ny);
+            const int dz = kk % 3 - 1, dy = (kk / 3) % 3 - 1, dx = kk / 9 - 1;
             const long long c = (long long)cellId + dz * cxy + (long long)dy * geo.cx + dx;
             int f, l;
             if (!cell_range(g, geo, ep, c, f, l)) continue;

@@ -279,7 +279,8 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
     a fresh seed; then plain frames, plain macro steps (K sub-steps, the
     collisions held) and macro steps with the network are timed from the
     same state, and their positions compared with the plain frames' (the
-    judge).  Simulated-time throughput = particles x sub-steps / time."""
+    reference for the errors).  Simulated-time throughput = particles x
+    sub-steps / time."""
     K, M = args.learned_substeps, args.learned_macro_steps
     params, scales, training = train_network(args, args.cells_per_type, tuning, bcs, warm)
 
@@ -345,7 +346,7 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
                       "tolerance": st["tolerance"]},
         "speedup_vs_plain": {"macro_plain": ms_plain / ms_macro, "surrogate": ms_plain / ms_sur},
         "network": dict(training, parameters=st["parameters"], flops_per_cell=st["flops_per_cell"]),
-        "judge": "positions after the same simulated time, against plain frames from the same state",
+        "error_reference": "positions after the same simulated time, against plain frames from the same state",
     }
 
 

@@ -1,6 +1,6 @@
 """GPU parity: libbcs.so (through the C ABI) against the FP64 oracle.
 
-Tolerances (from the spec contract):
+Tolerances (the parity contract of this path):
   * grid keys, sorted particle order, cell ranges: bit-exact;
   * one step: |gpu - oracle| <= 1e-5 * (|oracle| + rms(oracle)) elementwise
     for positions, velocities and forces (FP32 against FP64);

@@ -32,7 +32,7 @@ void launch_keys(const float4* pos, int n, int uniform, const SceneDev* scenes, 
 void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const SceneDev* scenes, int scene_count,
                      int* keys, int* ids, cudaStream_t s);
 void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigned* occ, const int* ids,
-                        const float4* pos, float4* spos, cudaStream_t s);
+                        const float4* pos, float4* spos, const float4* vel, float4* svel, cudaStream_t s);
 void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s);
 void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
                          cudaStream_t s);
@@ -109,6 +109,7 @@ struct DeviceGrid {
     unsigned* occ = nullptr;   // occupancy bitmap; while occ_on it holds the
     bool occ_on = false;       // bits of the cells of s_k[slot]
     float4* spos = nullptr;    // positions in sorted order, kept while spos_on
+    float4* svel = nullptr;    // velocities in sorted order, with spos
     bool spos_on = false;
     unsigned* temp = nullptr;
     int bits = 0;
@@ -280,7 +281,9 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
         BCS_CUDA(cudaMemset(dg.table, 0xFF, sizeof(int4) * (size_t)dg.g.cells));
         if (incremental) {
             const size_t words = (size_t)((dg.g.cells + 31) / 32);
-            if ((st = dalloc(s, &dg.occ, words)) || (st = dalloc(s, &dg.spos, count))) return st;
+            if ((st = dalloc(s, &dg.occ, words)) || (st = dalloc(s, &dg.spos, count)) ||
+                (st = dalloc(s, &dg.svel, count)))
+                return st;
             BCS_CUDA(cudaMemset(dg.occ, 0, sizeof(unsigned) * words));
         }
     }
@@ -291,7 +294,7 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
 // Sort the grid's unsorted keys into the other result slot and rebuild the
 // range table.  After the first build, a grid flagged incremental starts
 // from the previous order (any permutation works; few movers make it cheap).
-void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr) {
+void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, const float4* vel = nullptr) {
     const int out = dg.slot ^ 1;
     if (dg.incremental && dg.sorted_once) {
         sort_grid_incremental(dg.s_k[dg.slot], dg.s_v[dg.slot], dg.in_k, dg.s_k[out], dg.s_v[out], dg.count, dg.bits,
@@ -314,8 +317,10 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr) {
     dg.g.table = dg.table;
     dg.g.occ = dg.occ_on ? dg.occ : nullptr;
     dg.g.spos = dg.spos_on && pos ? dg.spos : nullptr;
+    dg.g.svel = dg.spos_on && pos && vel ? dg.svel : nullptr;
+    float4* svel_out = dg.spos_on && pos && vel ? dg.svel : nullptr;
     launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, dg.occ_on ? dg.occ : nullptr, dg.g.ids, pos,
-                       dg.spos_on && pos ? dg.spos : nullptr, st);
+                       dg.spos_on && pos ? dg.spos : nullptr, vel, svel_out, st);
 }
 
 void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
@@ -360,7 +365,7 @@ void enqueue_grids(bcs_sim* s) {
         launch_keys(s->pos[s->cur], s->N, s->pg.g.uniform, s->scenes, s->S, s->pg.in_k, s->pg.in_v, s->err, s->stream);
         s->keys_valid = true;
     }
-    if (s->pg.g.uniform) sort_grid(s->pg, s->stream, s->pos[s->cur]);
+    if (s->pg.g.uniform) sort_grid(s->pg, s->stream, s->pos[s->cur], s->vel[s->cur]);
     if (s->p.refresh_triangle_centers) build_triangle_grid(s, true);
     s->grid_ready = true;
 }
@@ -610,10 +615,13 @@ bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
     s->pg.occ_on = occ;
     s->pg.g.occ = occ ? s->pg.occ : nullptr;
     const bool sp = t.sorted_positions && s->pg.spos;
-    if (sp && !s->pg.spos_on && s->pg.sorted_once)
+    if (sp && !s->pg.spos_on && s->pg.sorted_once) {
         launch_gather_rows(s->pos[s->cur], s->pg.s_v[s->pg.slot], s->pg.count, s->pg.spos, s->stream);
+        launch_gather_rows(s->vel[s->cur], s->pg.s_v[s->pg.slot], s->pg.count, s->pg.svel, s->stream);
+    }
     s->pg.spos_on = sp;
     s->pg.g.spos = sp && s->pg.sorted_once ? s->pg.spos : nullptr;
+    s->pg.g.svel = sp && s->pg.sorted_once ? s->pg.svel : nullptr;
     s->args.pg = s->pg.g;
     s->persistent_grid[0] = t.persistent ? step_persistent_grid(0, t.step_shape) : 0;
     s->persistent_grid[1] = t.persistent ? step_persistent_grid(1, t.step_shape) : 0;
@@ -1316,8 +1324,10 @@ bcs_status bcs_set_particles(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities
     s->keys_valid = false;
     s->mid_frame = false;
     // a grid built before this call still serves the next calculate_next_frame
-    if (s->pg.spos_on && s->pg.sorted_once)
+    if (s->pg.spos_on && s->pg.sorted_once) {
         launch_gather_rows(s->pos[s->cur], s->pg.s_v[s->pg.slot], s->pg.count, s->pg.spos, s->stream);
+        launch_gather_rows(s->vel[s->cur], s->pg.s_v[s->pg.slot], s->pg.count, s->pg.svel, s->stream);
+    }
     if (s->tune.spatial_order && ((st = order_work_spatially(s)) || (st = upload_work(s)))) return st;
     return check_last();
 }

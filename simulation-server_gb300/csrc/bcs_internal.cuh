@@ -112,6 +112,7 @@ struct GridDev {          // batch-wide sorted grid
     const int* epoch;     // current epoch of the table
     const unsigned* occ;  // occupancy bitmap, 1 bit per cell, or null
     const float4* spos;   // positions in sorted order (particle grid), or null
+    const float4* svel;   // velocities in sorted order (set with spos), or null
     int count;            // objects
 };
 

@@ -205,14 +205,13 @@ constexpr int kCrowdedSlots = 128;
 
 // One candidate of particle (x, v, R): detectCollision's test, then the
 // resilient force with the neighbour's velocity (fetched only on a hit).
-template <class Neighbour>
-__device__ inline void collide(const StepArgs& a, float3 x, float3 v, float R, float4 pq, Neighbour neighbour,
+template <class VelocityOf>
+__device__ inline void collide(const StepArgs& a, float3 x, float3 v, float R, float4 pq, VelocityOf velocity_of,
                                float3& acc, unsigned& e) {
     const float3 rp = x - xyz(pq);
     const float d2 = dot3(rp, rp);
     const float md = R + pq.w;
-    if (d2 <= md * md && d2 >= 0.0001f)
-        acc = acc + resilient(a.p, rp, v - xyz(__ldg(&a.vel_in[neighbour()])), d2, R, 0.5f, e);
+    if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(velocity_of()), d2, R, 0.5f, e);
 }
 
 // calculateParticleCollisions<UniformGrid> (particle_collisions.cuh:26-38,
@@ -224,7 +223,7 @@ __device__ inline bool particle_collisions(const StepArgs& a, const SceneDev& sc
     acc = f3(0.f, 0.f, 0.f);
     const GridDev& g = a.pg;
     const GridGeom& geo = sc.pg;
-    auto test = [&](int q) { collide(a, x, v, R, __ldg(&a.pos_in[q]), [q] { return q; }, acc, e); };
+    auto test = [&](int q) { collide(a, x, v, R, __ldg(&a.pos_in[q]), [&a, q] { return __ldg(&a.vel_in[q]); }, acc, e); };
     if (!g.uniform) {
         for (int q = sc.particle_start; q < sc.particle_end; ++q)
             if (q != pid) test(q);
@@ -239,11 +238,13 @@ __device__ inline bool particle_collisions(const StepArgs& a, const SceneDev& sc
             slots += max(0, r.y - r.x + 1);
             if (slots > kCrowdedSlots) return false;
             if (g.spos) {
-                // Sorted positions: contiguous loads; the particle itself
-                // (d2 = 0) fails the d2 >= 1e-4 test, so no id is needed
-                // before a hit.
+                // Sorted positions (and velocities): contiguous loads; the
+                // particle itself (d2 = 0) fails the d2 >= 1e-4 test, so no
+                // id is needed.
                 for (int j = r.x; j <= r.y; ++j)
-                    collide(a, x, v, R, __ldg(&g.spos[j]), [&g, j] { return __ldg(&g.ids[j]); }, acc, e);
+                    collide(a, x, v, R, __ldg(&g.spos[j]), [&a, &g, j] {
+                        return g.svel ? __ldg(&g.svel[j]) : __ldg(&a.vel_in[__ldg(&g.ids[j])]);
+                    }, acc, e);
             } else {
                 for (int j = r.x; j <= r.y; ++j) {
                     const int q = __ldg(&g.ids[j]);
@@ -322,13 +323,22 @@ __device__ inline float3 heavy_collisions(const StepArgs& a, const SceneDev& sc,
             const int c = c0 + 32 * u;
             live[u] = c < total;
             const int j = stencil_slot(c, rs, rf);
-            q[u] = live[u] ? __ldg(&g.ids[j]) : pid;
-            if (g.spos) pq[u] = live[u] ? __ldg(&g.spos[j]) : make_float4(x.x, x.y, x.z, 0.f);
+            if (g.spos && g.svel) {
+                // sorted copies: no id (the particle itself fails d2 >= 1e-4)
+                q[u] = live[u] ? -1 : pid;
+                pq[u] = live[u] ? __ldg(&g.spos[j]) : make_float4(x.x, x.y, x.z, 0.f);
+                vq[u] = live[u] ? __ldg(&g.svel[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                q[u] = live[u] ? __ldg(&g.ids[j]) : pid;
+                if (g.spos) pq[u] = live[u] ? __ldg(&g.spos[j]) : make_float4(x.x, x.y, x.z, 0.f);
+            }
         }
+        if (!(g.spos && g.svel)) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            if (!g.spos) pq[u] = __ldg(&a.pos_in[q[u]]);
-            vq[u] = __ldg(&a.vel_in[q[u]]);
+            for (int u = 0; u < U; ++u) {
+                if (!g.spos) pq[u] = __ldg(&a.pos_in[q[u]]);
+                vq[u] = __ldg(&a.vel_in[q[u]]);
+            }
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -749,9 +759,15 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
                 const int n = min(kCrowdedStage, total - c0);
                 for (int t = lane; t < n; t += 32) {
                     const int j = stencil_slot(c0 + t, rs, rf);
-                    const int q = __ldg(&g.ids[j]);
-                    s_cpos[wib][t] = g.spos ? __ldg(&g.spos[j]) : __ldg(&a.pos_in[q]);
-                    const float4 vq = __ldg(&a.vel_in[q]);
+                    float4 vq;
+                    if (g.spos && g.svel) {
+                        s_cpos[wib][t] = __ldg(&g.spos[j]);
+                        vq = __ldg(&g.svel[j]);
+                    } else {
+                        const int q = __ldg(&g.ids[j]);
+                        s_cpos[wib][t] = g.spos ? __ldg(&g.spos[j]) : __ldg(&a.pos_in[q]);
+                        vq = __ldg(&a.vel_in[q]);
+                    }
                     s_cvel[wib][t] = make_float4(vq.x, vq.y, vq.z, __int_as_float(j));   // w: the slot
                 }
                 __syncwarp();
@@ -1803,10 +1819,14 @@ __global__ void __launch_bounds__(MT * 64, 1)
 
 __global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, const int* __restrict__ epoch,
                               unsigned* occ, const int* __restrict__ ids, const float4* __restrict__ pos,
-                              float4* spos) {
+                              float4* spos, const float4* __restrict__ vel, float4* svel) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (spos) spos[i] = pos[ids[i]];
+    if (spos) {
+        const int id = ids[i];
+        spos[i] = pos[id];
+        if (svel) svel[i] = vel[id];
+    }
     const int k = keys[i];
     if (i > 0 && keys[i - 1] == k) return;
     int j = i;
@@ -2071,9 +2091,9 @@ void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const Scene
     if (T > 0) k_tri_keys<<<BCS_GRID1(T, 256), 0, s>>>(vpos, tri, T, scenes, scene_count, keys, ids);
 }
 void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigned* occ, const int* ids,
-                        const float4* pos, float4* spos, cudaStream_t s) {
+                        const float4* pos, float4* spos, const float4* vel, float4* svel, cudaStream_t s) {
     k_next_epoch<<<1, 1, 0, s>>>(epoch);
-    if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table, epoch, occ, ids, pos, spos);
+    if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table, epoch, occ, ids, pos, spos, vel, svel);
 }
 void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s) {
     if (n > 0) k_occ_update<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, occ, set ? 1 : 0);

@@ -772,15 +772,23 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
                 }
                 __syncwarp();
                 if (pid >= 0) {
-                    for (int t = sub; t < n; t += L) {
-                        const float4 vq = s_cvel[wib][t];
-                        if (__float_as_int(vq.w) == my_slot) continue;
-                        const float4 pq = s_cpos[wib][t];
+                    auto pair = [&](float4 pq, float4 vq) {
+                        if (__float_as_int(vq.w) == my_slot) return;
                         const float3 rp = x - xyz(pq);
                         const float d2 = dot3(rp, rp);
                         const float md = R + pq.w;
                         if (d2 <= md * md && d2 >= 0.0001f) acc = acc + resilient(a.p, rp, v - xyz(vq), d2, R, 0.5f, e);
+                    };
+                    // two slots per step, their shared-memory reads issued
+                    // together; the sum keeps the slots' order
+                    int t = sub;
+                    for (; t + L < n; t += 2 * L) {
+                        const float4 p0 = s_cpos[wib][t], v0 = s_cvel[wib][t];
+                        const float4 p1 = s_cpos[wib][t + L], v1 = s_cvel[wib][t + L];
+                        pair(p0, v0);
+                        pair(p1, v1);
                     }
+                    if (t < n) pair(s_cpos[wib][t], s_cvel[wib][t]);
                 }
                 __syncwarp();
             }

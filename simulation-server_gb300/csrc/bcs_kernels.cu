@@ -241,10 +241,17 @@ __device__ inline bool particle_collisions(const StepArgs& a, const SceneDev& sc
                 // Sorted positions (and velocities): contiguous loads; the
                 // particle itself (d2 = 0) fails the d2 >= 1e-4 test, so no
                 // id is needed.
-                for (int j = r.x; j <= r.y; ++j)
-                    collide(a, x, v, R, __ldg(&g.spos[j]), [&a, &g, j] {
-                        return g.svel ? __ldg(&g.svel[j]) : __ldg(&a.vel_in[__ldg(&g.ids[j])]);
-                    }, acc, e);
+                auto vel_of = [&a, &g](int j) {
+                    return g.svel ? __ldg(&g.svel[j]) : __ldg(&a.vel_in[__ldg(&g.ids[j])]);
+                };
+                // two slots per step, their position reads issued together
+                int j = r.x;
+                for (; j < r.y; j += 2) {
+                    const float4 p0 = __ldg(&g.spos[j]), p1 = __ldg(&g.spos[j + 1]);
+                    collide(a, x, v, R, p0, [&vel_of, j] { return vel_of(j); }, acc, e);
+                    collide(a, x, v, R, p1, [&vel_of, j] { return vel_of(j + 1); }, acc, e);
+                }
+                if (j == r.y) collide(a, x, v, R, __ldg(&g.spos[j]), [&vel_of, j] { return vel_of(j); }, acc, e);
             } else {
                 for (int j = r.x; j <= r.y; ++j) {
                     const int q = __ldg(&g.ids[j]);

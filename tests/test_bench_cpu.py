@@ -48,6 +48,18 @@ def test_single_process_rate():
     assert bench.whole_job_rate(10, 4, 2.0, 1) == 10 * 4 / 0.002
 
 
+def test_error_and_latency_summaries():
+    import numpy as np
+    import bench
+    ref = np.zeros((4, 3))
+    got = np.array([[0, 0, 0], [3e-4, 0, 0], [0, 4e-4, 0], [0, 0, 1.0]])
+    e = bench.position_error(got, ref, radius=0.5)
+    assert e["max"] == 1.0 and e["frac_above_1e-3_radius"] == 0.25
+    assert abs(e["median"] - 3.5e-4) < 1e-12
+    p = bench.percentiles([1.0, 2.0, 3.0, 4.0])
+    assert p["p50"] == 2.5 and p["p99"] <= 4.0
+
+
 @pytest.mark.timeout(600)
 def test_reference_arm_under_torchrun():
     env = dict(os.environ, BCS_REFERENCE_BUDGET_S="1", OMP_NUM_THREADS="2")

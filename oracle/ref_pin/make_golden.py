@@ -100,9 +100,9 @@ def params_dict(p: bcs.Params) -> dict:
     return d
 
 
-def run_scene(tag: str, vein: S.VeinMesh, params: bcs.Params, counts, steps: int, seed: int, preset_mode: str,
-              models=None):
-    """Build the driver for one scene, run it, return the golden dict."""
+def scene_driver(tag: str, vein: S.VeinMesh, params: bcs.Params, counts, preset_mode: str, models=None) -> str:
+    """Compile the reference's hot-path TUs with a generated src/config for
+    one scene into oracle/_ref; returns the driver executable."""
     scene_stub = S.Scene(tag, [], vein.positions, vein.indices, vein.ending_centers, vein.ending_radii, [], params,
                          np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32))
 
@@ -120,9 +120,25 @@ def run_scene(tag: str, vein: S.VeinMesh, params: bcs.Params, counts, steps: int
 
     src = scratch_tree(write_config)
     try:
-        exe = build_driver(src, tag)
+        return build_driver(src, tag)
     finally:
         shutil.rmtree(os.path.dirname(src), ignore_errors=True)
+
+
+def build_pins() -> list:
+    """Compile every pinned scene's reference driver into oracle/_ref (no
+    run); nothing when the reference sources are absent."""
+    if not os.path.isdir(os.path.join(REF, "src")):
+        return []
+    os.makedirs(OUT, exist_ok=True)
+    return [scene_driver(tag, vein, params, counts, mode, models)
+            for tag, vein, params, counts, _steps, _seed, mode, models in scenes()]
+
+
+def run_scene(tag: str, vein: S.VeinMesh, params: bcs.Params, counts, steps: int, seed: int, preset_mode: str,
+              models=None):
+    """Build the driver for one scene, run it, return the golden dict."""
+    exe = scene_driver(tag, vein, params, counts, preset_mode, models)
     work = tempfile.mkdtemp(prefix="bcs_refpin_run_")
     try:
         subprocess.run([exe, work], check=True)
@@ -195,10 +211,11 @@ def main():
         return 0
     os.makedirs(OUT, exist_ok=True)
     os.makedirs(GOLDEN, exist_ok=True)
-    only_build = "--build" in sys.argv
+    if "--build" in sys.argv:
+        for exe in build_pins():
+            print("built", exe)
+        return 0
     for tag, vein, params, counts, steps, seed, mode, models in scenes():
-        if only_build:
-            continue
         g = run_scene(tag, vein, params, counts, steps, seed, mode, models)
         path = os.path.join(GOLDEN, f"ref_pin_{tag}.npz")
         np.savez_compressed(path, **g)

@@ -237,6 +237,8 @@ bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out);
  * this is the batched form of src/main.cu:122-138. */
 bcs_status bcs_create_batch(const bcs_scene_desc* descs, int scene_count, void* stream,
                             bcs_sim** out);
+/* Waits for the handle's stream and for reads still in flight
+ * (bcs_get_particles_async), then frees everything it allocated. */
 bcs_status bcs_destroy(bcs_sim* sim);
 bcs_status bcs_get_info(bcs_sim* sim, bcs_info* out);
 bcs_status bcs_get_scene_info(bcs_sim* sim, int scene, bcs_scene_info* out);
@@ -417,6 +419,9 @@ typedef struct bcs_surrogate_stats {
 } bcs_surrogate_stats;
 
 bcs_status bcs_surrogate_create(bcs_sim* sim, const bcs_surrogate_desc* desc, bcs_surrogate** out);
+/* Either order of destruction is safe: bcs_destroy detaches the simulation's
+ * surrogates, after which every call on them but this one returns
+ * BCS_ERR_INVALID_ARGUMENT. */
 bcs_status bcs_surrogate_destroy(bcs_surrogate* sur);
 /* Run `macro_steps` plain macro steps of the surrogate's K and record every
  * cell of the model as a training sample (stops at the capacity). */

@@ -350,6 +350,7 @@ class Simulation:
         if getattr(self, "h", None):
             self.lib.bcs_destroy(self.h)
             self.h = None
+            self._async_keep.clear()   # bcs_destroy waited for the reads
 
     def __del__(self):
         try:

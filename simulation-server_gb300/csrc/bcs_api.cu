@@ -187,6 +187,7 @@ struct bcs_sim {
     std::map<long long, cudaGraphExec_t> graphs;   // by (sub-steps, cur, sorted slot)
     float4* fext = nullptr;      // macro steps: held external force per particle
     bcs_surrogate* surrogate = nullptr;   // enabled learned sub-step path, or null
+    std::vector<bcs_surrogate*> surrogates;   // every live surrogate of this simulation
     // host copies of the per-model tables (surrogate graphs and tolerances)
     std::vector<int> h_adj_off, h_adj_nbr;
     std::vector<float> h_adj_len, h_radius_model;
@@ -921,18 +922,22 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     return apply_tuning(s, t);
 }
 
+void detach_surrogates(bcs_sim* s);
+
 void destroy_impl(bcs_sim* s) {
+    detach_surrogates(s);
     drop_graphs(s);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    // reads still in flight copy out of device scratch: finish them first
+    if (s->copy_stream) {
+        cudaStreamSynchronize(s->copy_stream);
+        cudaStreamDestroy(s->copy_stream);
+    }
     for (void* p : s->allocations) cudaFree(p);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     for (auto& e : s->pev)
         if (e) cudaEventDestroy(e);
-    if (s->copy_stream) {
-        cudaStreamSynchronize(s->copy_stream);
-        cudaStreamDestroy(s->copy_stream);
-    }
     for (int k = 0; k < 2; ++k) {
         if (s->aready[k]) cudaEventDestroy(s->aready[k]);
         if (s->adone[k]) cudaEventDestroy(s->adone[k]);
@@ -1044,6 +1049,16 @@ struct bcs_surrogate {
 };
 
 namespace {
+// A surrogate outlives its simulation only as a handle to destroy: every
+// other call on it is refused.
+void detach_surrogates(bcs_sim* s) {
+    for (bcs_surrogate* z : s->surrogates) z->sim = nullptr;
+    s->surrogates.clear();
+    s->surrogate = nullptr;
+}
+
+bool live(const bcs_surrogate* z) { return z && z->sim; }
+
 void collect_after_first(bcs_sim* s) {
     bcs_surrogate* z = s->surrogate;
     launch_sur_features(s->args, z->dev(z->ds_raw + (size_t)z->stored * z->pic * 16), s->stream);
@@ -1891,23 +1906,27 @@ bcs_status bcs_surrogate_create(bcs_sim* s, const bcs_surrogate_desc* d, bcs_sur
     BCS_CUDA(cudaMemset(z->skip, 0, s->C));
     BCS_CUDA(cudaMemset(z->counts, 0, 2 * sizeof(unsigned long long)));
     BCS_CUDA(cudaMemset(z->ds_valid, 0, z->capacity));
+    s->surrogates.push_back(z.get());
     *out = z.release();
     return BCS_OK;
 }
 
 bcs_status bcs_surrogate_destroy(bcs_surrogate* z) {
     if (!z) return BCS_ERR_INVALID_ARGUMENT;
-    if (z->sim && z->sim->surrogate == z) {
-        z->sim->surrogate = nullptr;
-        drop_graphs(z->sim);
+    if (bcs_sim* s = z->sim) {
+        if (s->surrogate == z) {
+            s->surrogate = nullptr;
+            drop_graphs(s);
+        }
+        s->surrogates.erase(std::remove(s->surrogates.begin(), s->surrogates.end(), z), s->surrogates.end());
+        cudaStreamSynchronize(s->stream);
     }
-    cudaStreamSynchronize(z->sim->stream);
     delete z;
     return BCS_OK;
 }
 
 bcs_status bcs_surrogate_collect(bcs_surrogate* z, int macro_steps) {
-    if (!z || macro_steps < 0) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z) || macro_steps < 0) return BCS_ERR_INVALID_ARGUMENT;
     bcs_sim* s = z->sim;
     if (s->mid_frame || (s->surrogate && s->surrogate != z)) return BCS_ERR_INVALID_ARGUMENT;
     bcs_surrogate* prev = s->surrogate;
@@ -1935,7 +1954,7 @@ bcs_status bcs_surrogate_collect(bcs_surrogate* z, int macro_steps) {
 }
 
 bcs_status bcs_surrogate_train(bcs_surrogate* z, int iterations, int batch_cells, float lr, float* loss) {
-    if (!z || iterations < 0 || batch_cells < 1 || batch_cells > z->net.max_cells() || !(lr > 0.f))
+    if (!live(z) || iterations < 0 || batch_cells < 1 || batch_cells > z->net.max_cells() || !(lr > 0.f))
         return BCS_ERR_INVALID_ARGUMENT;
     if (z->nvalid == 0) return BCS_ERR_INVALID_ARGUMENT;
     bcs_status st;
@@ -1959,7 +1978,7 @@ bcs_status bcs_surrogate_train(bcs_surrogate* z, int iterations, int batch_cells
 }
 
 bcs_status bcs_surrogate_enable(bcs_surrogate* z, int on) {
-    if (!z) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z)) return BCS_ERR_INVALID_ARGUMENT;
     bcs_sim* s = z->sim;
     if (s->mid_frame || (s->surrogate && s->surrogate != z)) return BCS_ERR_INVALID_ARGUMENT;
     if (on && !z->scales_set) return BCS_ERR_INVALID_ARGUMENT;   // train (or set the scales) first
@@ -1974,7 +1993,7 @@ bcs_status bcs_surrogate_enable(bcs_surrogate* z, int on) {
 }
 
 bcs_status bcs_surrogate_get_stats(bcs_surrogate* z, bcs_surrogate_stats* o) {
-    if (!z || !o) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z) || !o) return BCS_ERR_INVALID_ARGUMENT;
     unsigned long long c[2] = {0, 0};
     BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
     BCS_CUDA(cudaMemcpy(c, z->counts, sizeof(c), cudaMemcpyDeviceToHost));
@@ -1997,7 +2016,7 @@ bcs_status bcs_surrogate_get_stats(bcs_surrogate* z, bcs_surrogate_stats* o) {
 }
 
 bcs_status bcs_surrogate_reset_stats(bcs_surrogate* z) {
-    if (!z) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z)) return BCS_ERR_INVALID_ARGUMENT;
     BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
     BCS_CUDA(cudaMemset(z->counts, 0, 2 * sizeof(unsigned long long)));
     return BCS_OK;
@@ -2006,14 +2025,14 @@ bcs_status bcs_surrogate_reset_stats(bcs_surrogate* z) {
 int64_t bcs_surrogate_param_count(bcs_surrogate* z) { return z ? z->net.param_count() : 0; }
 
 bcs_status bcs_surrogate_get_params(bcs_surrogate* z, float* out, int64_t count) {
-    if (!z || !out || count != z->net.param_count()) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z) || !out || count != z->net.param_count()) return BCS_ERR_INVALID_ARGUMENT;
     BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
     BCS_CUDA(cudaMemcpy(out, z->net.params(), sizeof(float) * count, cudaMemcpyDeviceToHost));
     return BCS_OK;
 }
 
 bcs_status bcs_surrogate_set_params(bcs_surrogate* z, const float* in, int64_t count) {
-    if (!z || !in || count != z->net.param_count()) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z) || !in || count != z->net.param_count()) return BCS_ERR_INVALID_ARGUMENT;
     BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
     BCS_CUDA(cudaMemcpy(z->net.params(), in, sizeof(float) * count, cudaMemcpyHostToDevice));
     z->net.refresh_bf16();
@@ -2023,7 +2042,7 @@ bcs_status bcs_surrogate_set_params(bcs_surrogate* z, const float* in, int64_t c
 
 bcs_status bcs_surrogate_loss_grad(bcs_surrogate* z, int cells, const float* features, const float* edge_features,
                                    const float* targets, float* loss, float* grads) {
-    if (!z || cells < 1 || cells > z->net.max_cells() || !features || !edge_features || !targets)
+    if (!live(z) || cells < 1 || cells > z->net.max_cells() || !features || !edge_features || !targets)
         return BCS_ERR_INVALID_ARGUMENT;
     cudaStream_t st = z->sim->stream;
     const size_t n = (size_t)cells * z->pic;
@@ -2042,7 +2061,7 @@ bcs_status bcs_surrogate_loss_grad(bcs_surrogate* z, int cells, const float* fea
 
 bcs_status bcs_surrogate_forward(bcs_surrogate* z, int cells, const float* features, const float* edge_features,
                                  float* outputs) {
-    if (!z || cells < 1 || cells > z->net.max_cells() || !features || !edge_features || !outputs)
+    if (!live(z) || cells < 1 || cells > z->net.max_cells() || !features || !edge_features || !outputs)
         return BCS_ERR_INVALID_ARGUMENT;
     cudaStream_t st = z->sim->stream;
     const size_t n = (size_t)cells * z->pic;
@@ -2056,7 +2075,7 @@ bcs_status bcs_surrogate_forward(bcs_surrogate* z, int cells, const float* featu
 }
 
 bcs_status bcs_surrogate_evaluate(bcs_surrogate* z, int first, int count, double* net_error, double* base_error) {
-    if (!z || first < 0 || count < 1 || first + count > z->stored || !z->scales_set) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z) || first < 0 || count < 1 || first + count > z->stored || !z->scales_set) return BCS_ERR_INVALID_ARGUMENT;
     cudaStream_t st = z->sim->stream;
     double* sums = nullptr;
     BCS_CUDA(cudaMalloc(&sums, 3 * sizeof(double)));
@@ -2093,7 +2112,7 @@ unsigned bcs_tensor_wait_expiries(void) {
 }
 
 bcs_status bcs_surrogate_set_scales(bcs_surrogate* z, const float* in) {
-    if (!z || !in) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z) || !in) return BCS_ERR_INVALID_ARGUMENT;
     BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
     std::memcpy(&z->scales, in, sizeof(SurScales));
     z->scales_set = true;
@@ -2102,7 +2121,7 @@ bcs_status bcs_surrogate_set_scales(bcs_surrogate* z, const float* in) {
 }
 
 bcs_status bcs_surrogate_get_scales(bcs_surrogate* z, float* out) {
-    if (!z || !out) return BCS_ERR_INVALID_ARGUMENT;
+    if (!live(z) || !out) return BCS_ERR_INVALID_ARGUMENT;
     std::memcpy(out, &z->scales, sizeof(SurScales));
     return z->scales_set ? BCS_OK : BCS_ERR_INVALID_ARGUMENT;
 }

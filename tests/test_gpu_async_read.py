@@ -46,3 +46,16 @@ def test_async_read_of_positions_only_and_midframe(lib):
     np.testing.assert_array_equal(pos.T, ref.get_particles()[0])
     with pytest.raises(ValueError):
         sim.get_particles_async(np.empty((sim.n, 3), np.float32))
+
+
+def test_close_with_reads_in_flight(lib):
+    """Destroying the handle waits for the reads it started."""
+    sc = S.straight_scene(cells=32, seed=6)
+    sim, ref = make(sc), make(sc)
+    bufs = [np.empty((3, sim.n), np.float32) for _ in range(3)]
+    sim.step(2)
+    sim.get_particles_async(*bufs)
+    sim.close()
+    ref.step(2)
+    for got, want in zip(bufs, ref.get_particles()):
+        np.testing.assert_array_equal(got.T, want)

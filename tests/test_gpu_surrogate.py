@@ -192,6 +192,23 @@ def test_surrogate_arguments(lib):
         sur.train(1)          # no samples yet
 
 
+def test_surrogate_outlives_its_simulation(lib):
+    """Destroying the simulation first detaches its surrogates: later calls
+    on them are refused, destroying them still works."""
+    sim = make(sphere_scene(cells=4))
+    sur = bcs.Surrogate(sim, max_samples=16)
+    sur.collect(1)
+    other = bcs.Surrogate(sim, max_samples=16)
+    other.close()                       # one destroyed while the simulation lives
+    sim.close()
+    with pytest.raises(bcs.BcsError) as e:
+        sur.collect(1)
+    assert e.value.status == 1
+    with pytest.raises(bcs.BcsError):
+        sur.stats()
+    sur.close()
+
+
 def test_fused_inference_matches_layer_kernels(lib, trained):
     sc, sim, sur, train_n, loss0, loss = trained
     out = []

@@ -233,8 +233,10 @@ bcs_status bcs_create(const bcs_scene_desc* desc, void* stream, bcs_sim** out);
  * scene computes exactly what it computes alone under bcs_create.  The
  * scenes must share every physics constant of bcs_params except the grid
  * cell sizes and margins, cylinder_radius, min_spawn_y and seed, and share
- * the grid kinds.  The reference runs one compile-time scene per process;
- * this is the batched form of src/main.cu:122-138. */
+ * the grid kinds.  The whole batch holds fewer than 2^30 particles, and its
+ * particle and triangle grids at most 2^31 - 1 cells each (keys are int32).
+ * The reference runs one compile-time scene per process; this is the
+ * batched form of src/main.cu:122-138. */
 bcs_status bcs_create_batch(const bcs_scene_desc* descs, int scene_count, void* stream,
                             bcs_sim** out);
 /* Waits for the handle's stream and for reads still in flight

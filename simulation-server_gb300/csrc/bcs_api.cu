@@ -242,7 +242,9 @@ template <class T>
 bcs_status upload(bcs_sim* s, T** ptr, const std::vector<T>& host) {
     bcs_status st = dalloc(s, ptr, host.size());
     if (st != BCS_OK) return st;
-    if (!host.empty()) BCS_CUDA(cudaMemcpy(*ptr, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice));
+    // stream-ordered: the handle's stream does not wait for the legacy one
+    if (!host.empty())
+        BCS_CUDA(cudaMemcpyAsync(*ptr, host.data(), sizeof(T) * host.size(), cudaMemcpyHostToDevice, s->stream));
     return BCS_OK;
 }
 
@@ -274,18 +276,18 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
     while (idb < 31 && (1LL << idb) < count) ++idb;
     dg.id_bits = idb;
     if ((st = dalloc(s, &dg.epoch, 1))) return st;
-    BCS_CUDA(cudaMemset(dg.epoch, 0, sizeof(int)));
+    BCS_CUDA(cudaMemsetAsync(dg.epoch, 0, sizeof(int), s->stream));
     dg.g.epoch = dg.epoch;
     if (dg.g.uniform) {
         if ((st = dalloc(s, &dg.table, (size_t)dg.g.cells))) return st;
         // every field -1: no entry matches an epoch before the grid's first build
-        BCS_CUDA(cudaMemset(dg.table, 0xFF, sizeof(int4) * (size_t)dg.g.cells));
+        BCS_CUDA(cudaMemsetAsync(dg.table, 0xFF, sizeof(int4) * (size_t)dg.g.cells, s->stream));
         if (incremental) {
             const size_t words = (size_t)((dg.g.cells + 31) / 32);
             if ((st = dalloc(s, &dg.occ, words)) || (st = dalloc(s, &dg.spos, count)) ||
                 (st = dalloc(s, &dg.svel, count)))
                 return st;
-            BCS_CUDA(cudaMemset(dg.occ, 0, sizeof(unsigned) * words));
+            BCS_CUDA(cudaMemsetAsync(dg.occ, 0, sizeof(unsigned) * words, s->stream));
         }
     }
     dg.bits = bits_for(dg.g.cells);
@@ -834,11 +836,11 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
             (st = dalloc(s, &s->frc[b], s->N)))
             return st;
     if ((st = dalloc(s, &s->fext, s->N))) return st;
-    BCS_CUDA(cudaMemset(s->fext, 0, sizeof(float4) * s->N));
+    BCS_CUDA(cudaMemsetAsync(s->fext, 0, sizeof(float4) * s->N, s->stream));
     for (int b = 0; b < 2; ++b) {
-        BCS_CUDA(cudaMemset(s->pos[b], 0, sizeof(float4) * s->N));
-        BCS_CUDA(cudaMemset(s->vel[b], 0, sizeof(float4) * s->N));
-        BCS_CUDA(cudaMemset(s->frc[b], 0, sizeof(float4) * s->N));
+        BCS_CUDA(cudaMemsetAsync(s->pos[b], 0, sizeof(float4) * s->N, s->stream));
+        BCS_CUDA(cudaMemsetAsync(s->vel[b], 0, sizeof(float4) * s->N, s->stream));
+        BCS_CUDA(cudaMemsetAsync(s->frc[b], 0, sizeof(float4) * s->N, s->stream));
     }
     for (int k = 0; k < kStepShapes; ++k)
         s->work_capacity = std::max(s->work_capacity, (int)work_items(s->types, kShapes[k].chunk).size());
@@ -847,8 +849,8 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
         (st = dalloc(s, &s->crowded, s->N)) || (st = dalloc(s, &s->crowded_cells, s->N)) ||
         (st = dalloc(s, &s->crowded_counter, 6)) || (st = dalloc(s, &s->cent, s->C)))
         return st;
-    BCS_CUDA(cudaMemset(s->work_counter, 0, 2 * sizeof(int)));
-    BCS_CUDA(cudaMemset(s->crowded_counter, 0, 6 * sizeof(int)));
+    BCS_CUDA(cudaMemsetAsync(s->work_counter, 0, 2 * sizeof(int), s->stream));
+    BCS_CUDA(cudaMemsetAsync(s->crowded_counter, 0, 6 * sizeof(int), s->stream));
     s->args.crowded = s->crowded;
     s->args.crowded_cells = s->crowded_cells;
     s->args.crowded_counter = s->crowded_counter;
@@ -864,8 +866,8 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
         (st = upload(s, &s->nb_ids, nb_ids)) || (st = upload(s, &s->nb_len, nb_len)) || (st = upload(s, &s->tri, tri)) ||
         (st = dalloc(s, &s->tcache, 3 * (size_t)s->T)))
         return st;
-    BCS_CUDA(cudaMemset(s->vvel, 0, sizeof(float4) * s->V));
-    BCS_CUDA(cudaMemset(s->vfrc, 0, sizeof(float4) * s->V));
+    BCS_CUDA(cudaMemsetAsync(s->vvel, 0, sizeof(float4) * s->V, s->stream));
+    BCS_CUDA(cudaMemsetAsync(s->vfrc, 0, sizeof(float4) * s->V, s->stream));
     if ((st = alloc_grid(s, s->pg, s->N, true)) || (st = alloc_grid(s, s->tg, std::max(1, s->T), false))) return st;
     s->tg.count = s->T;
     s->tg.g.count = s->T;
@@ -874,17 +876,17 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
         if (s->p.vein_dynamic && s->T > 0) {
             if ((st = dalloc(s, &s->wall_disp2, 1)) || (st = dalloc(s, &s->wall_ref, s->V))) return st;
             const float huge = 3.0e38f;
-            BCS_CUDA(cudaMemcpy(s->wall_disp2, &huge, sizeof(float), cudaMemcpyHostToDevice));
+            BCS_CUDA(cudaMemcpyAsync(s->wall_disp2, &huge, sizeof(float), cudaMemcpyHostToDevice, s->stream));
         }
         if (s->T > 0 && mask_total <= (1LL << 31)) {
             if ((st = dalloc(s, &s->wall_mask, (size_t)mask_total)) || (st = dalloc(s, &s->wall_epoch, 1))) return st;
-            BCS_CUDA(cudaMemset(s->wall_mask, 0, (size_t)mask_total));
-            BCS_CUDA(cudaMemset(s->wall_epoch, 0, sizeof(int)));
+            BCS_CUDA(cudaMemsetAsync(s->wall_mask, 0, (size_t)mask_total, s->stream));
+            BCS_CUDA(cudaMemsetAsync(s->wall_epoch, 0, sizeof(int), s->stream));
         }
     }
     if ((st = dalloc(s, &s->steps, 1)) || (st = dalloc(s, &s->err, 1))) return st;
-    BCS_CUDA(cudaMemset(s->steps, 0, sizeof(long long)));
-    BCS_CUDA(cudaMemset(s->err, 0, sizeof(unsigned)));
+    BCS_CUDA(cudaMemsetAsync(s->steps, 0, sizeof(long long), s->stream));
+    BCS_CUDA(cudaMemsetAsync(s->err, 0, sizeof(unsigned), s->stream));
 
     // ---- kernel arguments that never change
     StepArgs& a = s->args;
@@ -1246,10 +1248,14 @@ bcs_status bcs_create_batch(const bcs_scene_desc* descs, int scene_count, void* 
     *out = nullptr;
     if (!descs || scene_count <= 0) return BCS_ERR_INVALID_ARGUMENT;
     bcs_status st;
+    long long particles = 0;   // batch-wide particle ids are int32
     for (int k = 0; k < scene_count; ++k) {
         if ((st = validate(descs + k)) != BCS_OK) return st;
         if (!same_physics(descs[0].params, descs[k].params)) return BCS_ERR_INVALID_ARGUMENT;
+        for (int t = 0; t < descs[k].type_count; ++t)
+            particles += (long long)descs[k].types[t].count * descs[k].types[t].particles_in_cell;
     }
+    if (particles > INT32_MAX / 2) return BCS_ERR_INVALID_ARGUMENT;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return BCS_ERR_NO_DEVICE;
     bcs_sim* s = new (std::nothrow) bcs_sim();
@@ -1901,11 +1907,14 @@ bcs_status bcs_surrogate_create(bcs_sim* s, const bcs_surrogate_desc* d, bcs_sur
         !z->alloc(&z->ds_raw, (size_t)z->capacity * z->pic * 16) || !z->alloc(&z->ds_t, (size_t)z->capacity * z->pic * 9) ||
         !z->alloc(&z->ds_valid, z->capacity) || !z->alloc(&z->valid_list, z->capacity))
         return BCS_ERR_OUT_OF_MEMORY;
-    BCS_CUDA(cudaMemcpy(z->d_cell_type, z->cell_type.data(), sizeof(int) * z->cells, cudaMemcpyHostToDevice));
-    BCS_CUDA(cudaMemcpy(z->d_cell_index, z->cell_index.data(), sizeof(int) * z->cells, cudaMemcpyHostToDevice));
-    BCS_CUDA(cudaMemset(z->skip, 0, s->C));
-    BCS_CUDA(cudaMemset(z->counts, 0, 2 * sizeof(unsigned long long)));
-    BCS_CUDA(cudaMemset(z->ds_valid, 0, z->capacity));
+    BCS_CUDA(cudaMemcpyAsync(z->d_cell_type, z->cell_type.data(), sizeof(int) * z->cells, cudaMemcpyHostToDevice,
+                             s->stream));
+    BCS_CUDA(cudaMemcpyAsync(z->d_cell_index, z->cell_index.data(), sizeof(int) * z->cells, cudaMemcpyHostToDevice,
+                             s->stream));
+    BCS_CUDA(cudaMemsetAsync(z->skip, 0, s->C, s->stream));
+    BCS_CUDA(cudaMemsetAsync(z->counts, 0, 2 * sizeof(unsigned long long), s->stream));
+    BCS_CUDA(cudaMemsetAsync(z->ds_valid, 0, z->capacity, s->stream));
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
     s->surrogates.push_back(z.get());
     *out = z.release();
     return BCS_OK;
@@ -1949,7 +1958,9 @@ bcs_status bcs_surrogate_collect(bcs_surrogate* z, int macro_steps) {
     for (int i = 0; i < z->stored; ++i)
         if (ok[i]) list.push_back(i);
     z->nvalid = (int)list.size();
-    if (z->nvalid) BCS_CUDA(cudaMemcpy(z->valid_list, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
+    if (z->nvalid)
+        BCS_CUDA(cudaMemcpyAsync(z->valid_list, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice,
+                                 s->stream));
     return check_last();
 }
 
@@ -1987,7 +1998,7 @@ bcs_status bcs_surrogate_enable(bcs_surrogate* z, int on) {
     z->enabled = on != 0;
     if (on) z->mode = on;
     s->surrogate = z->enabled ? z : nullptr;
-    BCS_CUDA(cudaMemset(z->skip, 0, s->C));
+    BCS_CUDA(cudaMemsetAsync(z->skip, 0, s->C, s->stream));
     drop_graphs(s);
     return BCS_OK;
 }
@@ -2017,8 +2028,7 @@ bcs_status bcs_surrogate_get_stats(bcs_surrogate* z, bcs_surrogate_stats* o) {
 
 bcs_status bcs_surrogate_reset_stats(bcs_surrogate* z) {
     if (!live(z)) return BCS_ERR_INVALID_ARGUMENT;
-    BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
-    BCS_CUDA(cudaMemset(z->counts, 0, 2 * sizeof(unsigned long long)));
+    BCS_CUDA(cudaMemsetAsync(z->counts, 0, 2 * sizeof(unsigned long long), z->sim->stream));
     return BCS_OK;
 }
 
@@ -2033,8 +2043,7 @@ bcs_status bcs_surrogate_get_params(bcs_surrogate* z, float* out, int64_t count)
 
 bcs_status bcs_surrogate_set_params(bcs_surrogate* z, const float* in, int64_t count) {
     if (!live(z) || !in || count != z->net.param_count()) return BCS_ERR_INVALID_ARGUMENT;
-    BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
-    BCS_CUDA(cudaMemcpy(z->net.params(), in, sizeof(float) * count, cudaMemcpyHostToDevice));
+    BCS_CUDA(cudaMemcpyAsync(z->net.params(), in, sizeof(float) * count, cudaMemcpyHostToDevice, z->sim->stream));
     z->net.refresh_bf16();
     BCS_CUDA(cudaStreamSynchronize(z->sim->stream));
     return check_last();
@@ -2107,7 +2116,10 @@ int bcs_set_tensor_path(int path) {
 
 unsigned bcs_tensor_wait_expiries(void) {
     unsigned h = 0;
-    if (cudaMemcpy(&h, mpnn_gemm_error_word(), sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 0xFFFFFFFFu;
+    // the word is written by kernels on the simulations' own streams
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(&h, mpnn_gemm_error_word(), sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return 0xFFFFFFFFu;
     return h;
 }
 

@@ -732,6 +732,7 @@ unsigned* mpnn_gemm_error_word() {
     if (!g_gemm_err) {
         cudaMalloc(&g_gemm_err, sizeof(unsigned));
         cudaMemset(g_gemm_err, 0, sizeof(unsigned));
+        cudaDeviceSynchronize();   // cleared before any stream's kernel can write it
     }
     return g_gemm_err;
 }
@@ -816,7 +817,7 @@ int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, c
     for (int c = 0; c < max_cells; ++c) base[c] = c * edges_;
     auto up = [&](auto** dst, const auto* src, size_t n) {
         *dst = reinterpret_cast<std::remove_pointer_t<decltype(dst)>>(alloc((n * sizeof(**dst) + 3) / 4));
-        return *dst && cudaMemcpy(*dst, src, n * sizeof(**dst), cudaMemcpyHostToDevice) == cudaSuccess;
+        return *dst && cudaMemcpyAsync(*dst, src, n * sizeof(**dst), cudaMemcpyHostToDevice, st_) == cudaSuccess;
     };
     if (!up(&adj_off_, adj_off, pic + 1) || !up(&adj_nbr_, adj_nbr, edges_) || !up(&adj_len_, adj_len, edges_) ||
         !up(&edge_base_, base.data(), max_cells))
@@ -832,7 +833,7 @@ int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, c
     nsq_ = (int)sq.size();
     sq_ = reinterpret_cast<long long*>(alloc(2 * sq.size()));
     if (!p_ || !g_ || !m_ || !v_ || !pb_ || !pbt_ || !sq_) return (int)cudaErrorMemoryAllocation;
-    cudaMemcpy(sq_, sq.data(), sizeof(long long) * sq.size(), cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(sq_, sq.data(), sizeof(long long) * sq.size(), cudaMemcpyHostToDevice, st_);
     // weights uniform in +-1/sqrt(fan_in), biases 0
     std::vector<float> h(P, 0.f);
     unsigned long long x = seed;
@@ -851,9 +852,11 @@ int MpnnNet::init(int layers, int pic, const int* adj_off, const int* adj_nbr, c
         fill(L_.wv[l], kHidden, (long long)kHidden * kHidden);
     }
     fill(L_.w_out, kHidden, (long long)kHidden * kOut);
-    cudaMemcpy(p_, h.data(), sizeof(float) * P, cudaMemcpyHostToDevice);
-    cudaMemset(m_, 0, sizeof(float) * P);
-    cudaMemset(v_, 0, sizeof(float) * P);
+    // stream-ordered uploads: the kernels below run on st_, which does not
+    // wait for the legacy stream
+    cudaMemcpyAsync(p_, h.data(), sizeof(float) * P, cudaMemcpyHostToDevice, st_);
+    cudaMemsetAsync(m_, 0, sizeof(float) * P, st_);
+    cudaMemsetAsync(v_, 0, sizeof(float) * P, st_);
     // activations
     const size_t n = (size_t)max_cells * pic, H = kHidden;
     f_ = alloc(n * kFeatIn); e_ = alloc((size_t)max_cells * edges_ * kEdgeIn); t_ = alloc(n * kOut);

@@ -269,6 +269,25 @@ def _ptr(a) -> int | None:
     return int(a.data_ptr())     # torch tensor
 
 
+def _rows(a, n: int, what: str) -> np.ndarray:
+    """A host array of n xyz rows as float32 (the library reads exactly n)."""
+    a = np.asarray(a, dtype=np.float32)
+    if a.shape != (n, 3):
+        raise ValueError(f"{what}: expected shape ({n}, 3), got {a.shape}")
+    return a
+
+
+def _dev(t, n: int, what: str) -> int | None:
+    """Device pointer of a contiguous float32 CUDA tensor of n elements."""
+    if t is None:
+        return None
+    if isinstance(t, np.ndarray) or not getattr(t, "is_cuda", False):
+        raise ValueError(f"{what}: expected a CUDA tensor")
+    if str(t.dtype) != "torch.float32" or not t.is_contiguous() or t.numel() != n:
+        raise ValueError(f"{what}: expected a contiguous float32 tensor of {n} elements")
+    return int(t.data_ptr())
+
+
 def _check(status: int, what: str) -> None:
     if status != BCS_OK:
         raise BcsError(status, what)
@@ -367,8 +386,8 @@ class Simulation:
     # ---- state ------------------------------------------------------------
     def set_particles(self, pos, vel, force=None) -> None:
         """pos/vel/force: [N, 3] float32 numpy arrays (host)."""
-        soa = [np.ascontiguousarray(np.asarray(a, dtype=np.float32).T) for a in (pos, vel)]
-        f = None if force is None else np.ascontiguousarray(np.asarray(force, dtype=np.float32).T)
+        soa = [np.ascontiguousarray(_rows(a, self.n, k).T) for a, k in ((pos, "pos"), (vel, "vel"))]
+        f = None if force is None else np.ascontiguousarray(_rows(force, self.n, "force").T)
         vecs = [Vec3(a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data) for a in soa]
         fv = Vec3() if f is None else Vec3(f[0].ctypes.data, f[1].ctypes.data, f[2].ctypes.data)
         _check(self.lib.bcs_set_particles(self.h, vecs[0], vecs[1], fv, MEM_HOST), "bcs_set_particles")
@@ -412,12 +431,15 @@ class Simulation:
 
     def set_particles_device(self, x, y, z, vx, vy, vz) -> None:
         """Device pointers (torch CUDA tensors) in cudaVec3 SoA layout."""
-        _check(self.lib.bcs_set_particles(self.h, Vec3(_ptr(x), _ptr(y), _ptr(z)), Vec3(_ptr(vx), _ptr(vy), _ptr(vz)),
-                                          Vec3(), MEM_DEVICE), "bcs_set_particles")
+        p = [_dev(a, self.n, "set_particles_device") for a in (x, y, z, vx, vy, vz)]
+        if None in p:
+            raise ValueError("set_particles_device: all six component tensors are required")
+        _check(self.lib.bcs_set_particles(self.h, Vec3(*p[:3]), Vec3(*p[3:]), Vec3(), MEM_DEVICE), "bcs_set_particles")
 
     def get_particles_device(self, x, y, z, vx=None, vy=None, vz=None) -> None:
-        _check(self.lib.bcs_get_particles(self.h, Vec3(_ptr(x), _ptr(y), _ptr(z)), Vec3(_ptr(vx), _ptr(vy), _ptr(vz)),
-                                          Vec3(), MEM_DEVICE), "bcs_get_particles")
+        p = [_dev(a, self.n, "get_particles_device") for a in (x, y, z, vx, vy, vz)]
+        _check(self.lib.bcs_get_particles(self.h, Vec3(*p[:3]), Vec3(*p[3:]), Vec3(), MEM_DEVICE),
+               "bcs_get_particles")
 
     def set_vein(self, pos=None, vel=None) -> None:
         keep = []
@@ -425,7 +447,7 @@ class Simulation:
         def v3(a):
             if a is None:
                 return Vec3()
-            s = np.ascontiguousarray(np.asarray(a, dtype=np.float32).T)
+            s = np.ascontiguousarray(_rows(a, self.nv, "set_vein").T)
             keep.append(s)
             return Vec3(s[0].ctypes.data, s[1].ctypes.data, s[2].ctypes.data)
         _check(self.lib.bcs_set_vein(self.h, v3(pos), v3(vel), MEM_HOST), "bcs_set_vein")

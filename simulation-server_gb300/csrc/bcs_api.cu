@@ -217,13 +217,30 @@ namespace {
 constexpr float kWallMargin = 0.5f;
 constexpr int kDefaultShape = 3;
 
+// A failed runtime call is reported once, by its own status: the runtime's
+// last-error slot is cleared so that the next call's check does not report it
+// again (a sticky error keeps failing every later call anyway).
 #define BCS_CUDA(call)                                          \
     do {                                                        \
         cudaError_t e_ = (call);                                \
         if (e_ != cudaSuccess) {                                \
+            (void)cudaGetLastError();                           \
             return e_ == cudaErrorMemoryAllocation ? BCS_ERR_OUT_OF_MEMORY : BCS_ERR_CUDA; \
         }                                                       \
     } while (0)
+
+// Device scratch of one call, freed on every return path.
+struct ScopedDevice {
+    void* p = nullptr;
+    ScopedDevice() = default;
+    ScopedDevice(const ScopedDevice&) = delete;
+    ScopedDevice& operator=(const ScopedDevice&) = delete;
+    ~ScopedDevice() {
+        if (p) cudaFree(p);
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
 
 template <class T>
 bcs_status dalloc(bcs_sim* s, T** ptr, size_t count) {
@@ -231,7 +248,10 @@ bcs_status dalloc(bcs_sim* s, T** ptr, size_t count) {
     if (count == 0) count = 1;
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, sizeof(T) * count);
-    if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? BCS_ERR_OUT_OF_MEMORY : BCS_ERR_CUDA;
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? BCS_ERR_OUT_OF_MEMORY : BCS_ERR_CUDA;
+    }
     s->allocations.push_back(p);
     s->bytes += sizeof(T) * count;
     *ptr = static_cast<T*>(p);
@@ -1027,7 +1047,10 @@ struct bcs_surrogate {
     template <class T>
     bool alloc(T** p, size_t n) {
         void* q = nullptr;
-        if (cudaMalloc(&q, sizeof(T) * std::max<size_t>(1, n)) != cudaSuccess) return false;
+        if (cudaMalloc(&q, sizeof(T) * std::max<size_t>(1, n)) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return false;
+        }
         allocs.push_back(q);
         bytes += sizeof(T) * n;
         *p = static_cast<T*>(q);
@@ -1578,6 +1601,7 @@ bcs_status bcs_init_particles(bcs_sim* s, const bcs_init_desc* d) {
             if (cudaMalloc(&keys, sizeof(int) * n) || cudaMalloc(&ids, sizeof(int) * n) ||
                 cudaMalloc(&k2, sizeof(int) * n) || cudaMalloc(&i2, sizeof(int) * n) || cudaMalloc(&cnt, sizeof(int)) ||
                 cudaMalloc(&temp, sizeof(unsigned) * radix_temp_words(n))) {
+                (void)cudaGetLastError();
                 st = BCS_ERR_OUT_OF_MEMORY;
             } else {
                 cudaMemsetAsync(cnt, 0, sizeof(int), s->stream);
@@ -1750,20 +1774,21 @@ bcs_status bcs_get_grid(bcs_sim* s, int which, int* cell_ids, int* object_ids, i
     if (cell_starts || cell_ends) {
         int* ds = nullptr;
         int* de = nullptr;
+        ScopedDevice hs, he;   // host destinations go through device scratch
         if (where == BCS_MEM_DEVICE) {
             ds = cell_starts;
             de = cell_ends;
         } else {
-            if (cell_starts) BCS_CUDA(cudaMalloc(&ds, sizeof(int) * (size_t)dg.g.cells));
-            if (cell_ends) BCS_CUDA(cudaMalloc(&de, sizeof(int) * (size_t)dg.g.cells));
+            if (cell_starts) BCS_CUDA(cudaMalloc(&hs.p, sizeof(int) * (size_t)dg.g.cells));
+            if (cell_ends) BCS_CUDA(cudaMalloc(&he.p, sizeof(int) * (size_t)dg.g.cells));
+            ds = hs.as<int>();
+            de = he.as<int>();
         }
         launch_dense_ranges(dg.table, dg.epoch, dg.g.cells, ds, de, s->stream);
         if (where == BCS_MEM_HOST) {
             if (ds) BCS_CUDA(cudaMemcpyAsync(cell_starts, ds, sizeof(int) * (size_t)dg.g.cells, kind, s->stream));
             if (de) BCS_CUDA(cudaMemcpyAsync(cell_ends, de, sizeof(int) * (size_t)dg.g.cells, kind, s->stream));
             BCS_CUDA(cudaStreamSynchronize(s->stream));
-            if (ds) cudaFree(ds);
-            if (de) cudaFree(de);
         }
     }
     BCS_CUDA(cudaStreamSynchronize(s->stream));
@@ -1778,18 +1803,16 @@ bcs_status bcs_export_render(bcs_sim* s, float* particle_vbo, float* particle_of
         launch_export(s->pos[b], s->N, s->vpos, s->V, particle_vbo, particle_offsets, vein_vbo, s->stream);
         return check_last();
     }
-    float *dp = nullptr, *doff = nullptr, *dv = nullptr;
-    if (particle_vbo) BCS_CUDA(cudaMalloc(&dp, sizeof(float) * 6 * (size_t)s->N));
-    if (particle_offsets) BCS_CUDA(cudaMalloc(&doff, sizeof(float) * 3 * (size_t)s->N));
-    if (vein_vbo) BCS_CUDA(cudaMalloc(&dv, sizeof(float) * 6 * (size_t)s->V));
+    ScopedDevice sp, soff, sv;
+    if (particle_vbo) BCS_CUDA(cudaMalloc(&sp.p, sizeof(float) * 6 * (size_t)s->N));
+    if (particle_offsets) BCS_CUDA(cudaMalloc(&soff.p, sizeof(float) * 3 * (size_t)s->N));
+    if (vein_vbo) BCS_CUDA(cudaMalloc(&sv.p, sizeof(float) * 6 * (size_t)s->V));
+    float *dp = sp.as<float>(), *doff = soff.as<float>(), *dv = sv.as<float>();
     launch_export(s->pos[b], s->N, s->vpos, s->V, dp, doff, dv, s->stream);
     if (dp) BCS_CUDA(cudaMemcpyAsync(particle_vbo, dp, sizeof(float) * 6 * (size_t)s->N, cudaMemcpyDeviceToHost, s->stream));
     if (doff) BCS_CUDA(cudaMemcpyAsync(particle_offsets, doff, sizeof(float) * 3 * (size_t)s->N, cudaMemcpyDeviceToHost, s->stream));
     if (dv) BCS_CUDA(cudaMemcpyAsync(vein_vbo, dv, sizeof(float) * 6 * (size_t)s->V, cudaMemcpyDeviceToHost, s->stream));
     BCS_CUDA(cudaStreamSynchronize(s->stream));
-    if (dp) cudaFree(dp);
-    if (doff) cudaFree(doff);
-    if (dv) cudaFree(dv);
     return check_last();
 }
 
@@ -2086,8 +2109,9 @@ bcs_status bcs_surrogate_forward(bcs_surrogate* z, int cells, const float* featu
 bcs_status bcs_surrogate_evaluate(bcs_surrogate* z, int first, int count, double* net_error, double* base_error) {
     if (!live(z) || first < 0 || count < 1 || first + count > z->stored || !z->scales_set) return BCS_ERR_INVALID_ARGUMENT;
     cudaStream_t st = z->sim->stream;
-    double* sums = nullptr;
-    BCS_CUDA(cudaMalloc(&sums, 3 * sizeof(double)));
+    ScopedDevice scratch;
+    BCS_CUDA(cudaMalloc(&scratch.p, 3 * sizeof(double)));
+    double* sums = scratch.as<double>();
     BCS_CUDA(cudaMemsetAsync(sums, 0, 3 * sizeof(double), st));
     for (int b = first; b < first + count; b += z->net.max_cells()) {
         const int n = std::min(z->net.max_cells(), first + count - b);
@@ -2099,7 +2123,6 @@ bcs_status bcs_surrogate_evaluate(bcs_surrogate* z, int first, int count, double
     double h[3] = {0, 0, 0};
     cudaError_t e = cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(sums);
     if (e != cudaSuccess) return BCS_ERR_CUDA;
     if (h[2] <= 0) return BCS_ERR_INVALID_ARGUMENT;
     if (net_error) *net_error = h[0] / h[2];

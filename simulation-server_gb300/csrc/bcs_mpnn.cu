@@ -792,7 +792,10 @@ MpnnNet::~MpnnNet() {
 
 float* MpnnNet::alloc(size_t n) {
     void* p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(float)) != cudaSuccess) return nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(float)) != cudaSuccess) {
+        (void)cudaGetLastError();   // reported by the caller's status
+        return nullptr;
+    }
     allocs_.push_back(p);
     bytes_ += n * sizeof(float);
     return static_cast<float*>(p);

@@ -61,6 +61,38 @@ def test_batch_arguments_rejected_before_device_work(lib, tmp_path):
     assert lib.bcs_get_scene_info(None, 0, None) == 1
 
 
+def test_batch_particle_total_bounded(lib):
+    """Each scene under the limit, the batch over it (particle ids are int32):
+    rejected before any device work."""
+    import bcs_scenes
+    bufs = [bcs.SceneBuffers(bcs_scenes.tiny_scene(cells=2, seed=s)) for s in (1, 2)]
+    descs = (bcs.SceneDesc * 2)(*[b.desc for b in bufs])
+    for d in descs:
+        t = d.types[0]
+        t.count = (1 << 29) // t.particles_in_cell + 1
+    h = C.c_void_p()
+    assert lib.bcs_create_batch(descs, 2, None, C.byref(h)) == 1
+    assert not h.value
+
+
+def test_python_harness_checks_shapes():
+    rows = bcs._rows(np.zeros((4, 3)), 4, "pos")
+    assert rows.dtype == np.float32
+    for bad in (np.zeros((5, 3)), np.zeros((3, 4)), np.zeros(12)):
+        try:
+            bcs._rows(bad, 4, "pos")
+        except ValueError:
+            continue
+        raise AssertionError(f"shape {bad.shape} accepted")
+    assert bcs._dev(None, 4, "x") is None
+    try:
+        bcs._dev(np.zeros(4, np.float32), 4, "x")
+    except ValueError:
+        pass
+    else:
+        raise AssertionError("a host array accepted as a device pointer")
+
+
 STRUCTS = {
     "bcs_vec3": bcs.Vec3, "bcs_cell_type": bcs.CellType, "bcs_vein": bcs.Vein,
     "bcs_flow_segment": bcs.FlowSegment, "bcs_params": bcs.Params, "bcs_scene_desc": bcs.SceneDesc,

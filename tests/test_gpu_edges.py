@@ -76,3 +76,19 @@ def test_largest_cell_model(lib):
     sc.velocities = np.random.default_rng(7).normal(0, 3.0, sc.positions.shape).astype(np.float32)
     sim = check(sc)
     assert bcs.STEP_SHAPES[sim.get_tuning().step_shape][1] >= 642
+
+
+def test_wrong_shapes_rejected_on_the_host(lib):
+    """Arrays of the wrong row count never reach the library (it reads
+    exactly n rows); the state stays what it was."""
+    sc = S.straight_scene(cells=4, seed=2)
+    sim = bcs.Simulation(sc)
+    sim.set_particles(sc.positions, sc.velocities)
+    before = sim.get_particles()
+    for bad in (sc.positions[:-1], sc.positions.T, np.concatenate([sc.positions, sc.positions[:1]])):
+        with pytest.raises(ValueError):
+            sim.set_particles(bad, sc.velocities)
+    with pytest.raises(ValueError):
+        sim.set_vein(pos=sc.vein_positions[:-2])
+    for a, b in zip(sim.get_particles(), before):
+        np.testing.assert_array_equal(a, b)

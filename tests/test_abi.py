@@ -156,3 +156,67 @@ def test_cell_model_too_large_rejected(lib):
     h = C.c_void_p()
     assert lib.bcs_create(C.byref(buf.desc), None, C.byref(h)) == 5   # BCS_ERR_UNSUPPORTED
     assert not h.value
+
+
+def _mutations():
+    """(name, mutate(bufs)) pairs, each making one field of a valid scene
+    malformed."""
+    def types(b):
+        return b.desc.types
+
+    def first_array(b, dtype, ndim):
+        return next(a for a in b.keep if isinstance(a, np.ndarray) and a.dtype == dtype and a.ndim == ndim)
+
+    def no_particles(b):
+        for t in range(b.desc.type_count):
+            types(b)[t].count = 0
+
+    def spring_out_of_range(b):
+        s = next(a for a in b.keep if isinstance(a, np.ndarray) and a.dtype == np.int32 and a.ndim == 2 and a.size)
+        s[0, 0] = types(b)[0].particles_in_cell
+
+    def triangle_out_of_range(b):
+        first_array(b, np.uint32, 2)[0, 0] = b.desc.vein.vertex_count
+
+    return [
+        ("no particles", no_particles),
+        ("negative count", lambda b: setattr(types(b)[0], "count", -1)),
+        ("empty cell model", lambda b: setattr(types(b)[0], "particles_in_cell", 0)),
+        ("no vertices", lambda b: setattr(types(b)[0], "vertices", None)),
+        ("negative spring count", lambda b: setattr(types(b)[0], "spring_count", -1)),
+        ("springs without arrays", lambda b: setattr(types(b)[0], "springs", None)),
+        ("spring index out of range", spring_out_of_range),
+        ("no vein vertices", lambda b: setattr(b.desc.vein, "vertex_count", 0)),
+        ("no vein positions", lambda b: setattr(b.desc.vein, "positions", None)),
+        ("negative triangle count", lambda b: setattr(b.desc.vein, "triangle_count", -1)),
+        ("triangle index out of range", triangle_out_of_range),
+        ("too many endings", lambda b: setattr(b.desc.vein, "ending_count", 9)),
+        ("negative endings", lambda b: setattr(b.desc.vein, "ending_count", -1)),
+        ("flows without an array", lambda b: (setattr(b.desc, "flow_segment_count", 1),
+                                              setattr(b.desc, "flow_segments", None))),
+        ("zero grid cell", lambda b: setattr(b.desc.params, "cell_width", 0.0)),
+        ("NaN grid cell", lambda b: setattr(b.desc.params, "cell_height", float("nan"))),
+        ("negative triangle cell", lambda b: setattr(b.desc.params, "cell_depth_triangles", -1.0)),
+        ("zero bounding-sphere coefficient", lambda b: setattr(b.desc.params, "bounding_spheres_coeff", 0.0)),
+    ]
+
+
+def test_every_malformed_field_rejected_before_device_work(lib):
+    """Each field validate() checks, made malformed on its own, returns
+    BCS_ERR_INVALID_ARGUMENT before any device work (on a machine without a
+    GPU the unmodified scene gets as far as BCS_ERR_NO_DEVICE)."""
+    import bcs_scenes
+    sc = bcs_scenes.straight_scene(cells=4, seed=3)
+    h = C.c_void_p()
+    base = bcs.SceneBuffers(sc)
+    st = lib.bcs_create(C.byref(base.desc), None, C.byref(h))
+    assert st in (0, 4), st
+    if st == 0:
+        lib.bcs_destroy(h)
+    import copy
+    for name, mutate in _mutations():
+        b = bcs.SceneBuffers(copy.deepcopy(sc))   # in-place edits must not reach the next case
+        mutate(b)
+        h = C.c_void_p()
+        assert lib.bcs_create(C.byref(b.desc), None, C.byref(h)) == 1, name
+        assert not h.value, name

@@ -1,4 +1,4 @@
-"""Scene generators: the BASELINE shapes (CPU only)."""
+"""Scene generators: the shapes of the benchmark workloads (CPU only)."""
 import numpy as np
 
 import bcs_scenes as S

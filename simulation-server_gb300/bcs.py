@@ -288,6 +288,18 @@ def _dev(t, n: int, what: str) -> int | None:
     return int(t.data_ptr())
 
 
+def _edges_per_cell(cell_type) -> int:
+    """Directed spring edges of one cell as the library builds its graph:
+    the dense spring matrix (a later spring overwrites an earlier one on the
+    same pair, rest length 0 is no spring), self pairs left out."""
+    dense = {}
+    springs = np.asarray(cell_type.springs, np.int64).reshape(-1, 2)
+    for (a, b), length in zip(springs, np.asarray(cell_type.spring_lengths, np.float32).reshape(-1)):
+        dense[(int(a), int(b))] = length
+        dense[(int(b), int(a))] = length
+    return sum(1 for (a, b), length in dense.items() if a != b and length != 0.0)
+
+
 def _check(status: int, what: str) -> None:
     if status != BCS_OK:
         raise BcsError(status, what)
@@ -562,7 +574,9 @@ class Surrogate:
         _check(self.lib.bcs_surrogate_create(sim.h, C.byref(d), C.byref(h)), "bcs_surrogate_create")
         self.h = h
         self.substeps = int(substeps)
-        self.pic = len(sim.scene.types[cell_type].vertices) if hasattr(sim.scene, "types") else None
+        t = sim.scene.types[cell_type]
+        self.pic = len(t.vertices)
+        self.edges = _edges_per_cell(t)
 
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -605,13 +619,27 @@ class Surrogate:
         return out
 
     def set_params(self, p) -> None:
-        p = np.ascontiguousarray(p, np.float32)
+        p = np.ascontiguousarray(p, np.float32).reshape(-1)
         _check(self.lib.bcs_surrogate_set_params(self.h, p.ctypes.data, p.size), "bcs_surrogate_set_params")
 
+    def _inputs(self, cells, features, edge_features, targets=None):
+        """The host arrays of `cells` cells, checked against the sizes the
+        library reads: (cells x pic, 16) node features, (cells x edges, 8)
+        edge features, (cells x pic, 9) targets."""
+        n, m = int(cells) * self.pic, int(cells) * self.edges
+        want = [("features", features, (n, 16)), ("edge_features", edge_features, (m, 8))]
+        if targets is not None:
+            want.append(("targets", targets, (n, 9)))
+        out = []
+        for name, a, shape in want:
+            a = np.ascontiguousarray(a, np.float32)
+            if a.shape != shape:
+                raise ValueError(f"{name}: expected shape {shape} for {cells} cells, got {a.shape}")
+            out.append(a)
+        return out
+
     def loss_grad(self, cells, features, edge_features, targets):
-        f = np.ascontiguousarray(features, np.float32)
-        e = np.ascontiguousarray(edge_features, np.float32)
-        t = np.ascontiguousarray(targets, np.float32)
+        f, e, t = self._inputs(cells, features, edge_features, targets)
         loss = np.zeros(1, np.float32)
         g = np.empty(self.param_count(), np.float32)
         _check(self.lib.bcs_surrogate_loss_grad(self.h, int(cells), f.ctypes.data, e.ctypes.data, t.ctypes.data,
@@ -619,8 +647,7 @@ class Surrogate:
         return float(loss[0]), g
 
     def forward(self, cells, features, edge_features):
-        f = np.ascontiguousarray(features, np.float32)
-        e = np.ascontiguousarray(edge_features, np.float32)
+        f, e = self._inputs(cells, features, edge_features)
         y = np.empty((f.shape[0], 9), np.float32)
         _check(self.lib.bcs_surrogate_forward(self.h, int(cells), f.ctypes.data, e.ctypes.data, y.ctypes.data),
                "bcs_surrogate_forward")
@@ -639,6 +666,7 @@ class Surrogate:
         return out
 
     def set_scales(self, sc) -> None:
-        sc = np.ascontiguousarray(sc, np.float32)
-        assert sc.size == 53
+        sc = np.ascontiguousarray(sc, np.float32).reshape(-1)
+        if sc.size != 53:
+            raise ValueError(f"scales: expected 53 values, got {sc.size}")
         _check(self.lib.bcs_surrogate_set_scales(self.h, sc.ctypes.data), "bcs_surrogate_set_scales")

@@ -220,3 +220,21 @@ def test_every_malformed_field_rejected_before_device_work(lib):
         h = C.c_void_p()
         assert lib.bcs_create(C.byref(b.desc), None, C.byref(h)) == 1, name
         assert not h.value, name
+
+
+def test_surrogate_inputs_checked_on_the_host():
+    """The sizes the library reads for `cells` cells: node features, edge
+    features and targets of the wrong shape never reach it."""
+    import bcs_scenes
+    sc = bcs_scenes.straight_scene(cells=4, seed=3)
+    assert bcs._edges_per_cell(sc.types[0]) == 240        # 42-vertex icosphere: 120 springs, both ways
+    sur = object.__new__(bcs.Surrogate)                     # no device: only the host-side checks
+    sur.pic, sur.edges = 42, 240
+    f, e, t = np.zeros((84, 16)), np.zeros((480, 8)), np.zeros((84, 9))
+    assert [a.shape for a in sur._inputs(2, f, e, t)] == [(84, 16), (480, 8), (84, 9)]
+    for bad in ((f[:-1], e, t), (f, e[:-8], t), (f, e, t[:, :8]), (f.T, e, t)):
+        try:
+            sur._inputs(2, *bad)
+        except ValueError:
+            continue
+        raise AssertionError("a wrongly shaped input accepted")

@@ -465,7 +465,8 @@ bcs_status bcs_surrogate_evaluate(bcs_surrogate* sur, int first, int count, doub
  * with mma.sync), 1 = mma.sync.  Returns the previous setting,
  * or -1 for an invalid value.  bcs_tensor_wait_expiries counts tcgen05
  * completions that were not seen within the kernel's bounded wait (the
- * product is then skipped, not stalled). */
+ * product is then skipped, not stalled); it synchronises the device first,
+ * or returns 0xFFFFFFFF when that fails. */
 int bcs_set_tensor_path(int path);
 unsigned bcs_tensor_wait_expiries(void);
 /* The normalisation derived from the training set: 53 floats (feature means

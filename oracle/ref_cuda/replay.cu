@@ -1,0 +1,459 @@
+// replay.cu — runs the reference's own CUDA kernels from a cubin and a launch
+// tape (test infrastructure: the reference's CUDA build as a baseline on a
+// GPU machine that cannot compile the reference; see build_ref_cuda.py).
+//
+// Usage: ref_cuda_replay <dir> <reference|pinned> <state.bin|-> <frames> [<out.bin>]
+//   dir        oracle/_ref/refcuda_<scene>: kernels.cubin, kernels.txt, <mode>.tape
+//   state.bin  [N][3] positions then [N][3] velocities (float32), written into
+//              the buffers the tape marks (forces start at zero); "-" keeps
+//              the zeroed state
+//   frames     frames replayed after the construction, each the tape's first
+//              recorded frame (the recorder checks that its frames are equal)
+//   out.bin    positions, velocities, forces ([N][3] float32 each) afterwards
+// Prints one JSON line: frames run, ms per frame (CUDA events on the legacy
+// stream around each chunk of frames, which also covers the tape's device
+// synchronisations; the checks between chunks are not timed), launches per
+// frame.
+//
+// Every launch is checked before it is issued: the cubin entry exists, its
+// parameter count and sizes (cuFuncGetParamInfo) equal the recorded ones,
+// every relocated pointer lies inside its allocation, and the block shape is
+// legal.  A mismatch stops the replay before any kernel of it runs.
+//
+// The reference's grid key clamps with the box extent instead of the cell
+// count (uniform_grid.cu:31-34), so a particle outside the grid box would
+// make its kernels write past the cell tables.  The replay therefore runs in
+// chunks: before each chunk a check of our own (limits.txt: the box and dt)
+// confirms that every particle is inside the box shrunk by a guard band and
+// sizes the chunk (at most 50 frames) so that the fastest particle cannot
+// cross a quarter of that band within it; when that cannot be confirmed the
+// replay stops early and reports the frames it ran.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <thrust/execution_policy.h>
+#include <thrust/sort.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+namespace {
+
+[[noreturn]] void die(const std::string& what) {
+    std::fprintf(stderr, "ref_cuda_replay: %s\n", what.c_str());
+    std::exit(2);
+}
+
+void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) die(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void check(CUresult r, const char* what) {
+    if (r != CUDA_SUCCESS) {
+        const char* s = nullptr;
+        cuGetErrorString(r, &s);
+        die(std::string(what) + ": " + (s ? s : "driver error"));
+    }
+}
+
+struct Addr {
+    uint32_t id = 0;
+    uint64_t off = 0;
+};
+
+struct Reloc {
+    uint32_t offset, id;
+    uint64_t off;
+};
+
+struct Param {
+    std::vector<unsigned char> bytes;
+    std::vector<Reloc> relocs;
+};
+
+struct Op {
+    uint32_t code = 0;
+    // alloc / free / stream / sync_stream
+    uint32_t id = 0;
+    uint64_t bytes = 0;
+    // copies, memset, sort, fix_last_cell, buffer
+    Addr a, b, c;
+    int32_t value = 0;
+    uint32_t n = 0;
+    std::vector<unsigned char> data;
+    std::string text;
+    // launch
+    uint64_t kernel = 0;
+    uint32_t grid[3] = {}, block[3] = {}, shmem = 0, stream = 0;
+    std::vector<Param> params;
+};
+
+struct Cursor {
+    const unsigned char* p;
+    const unsigned char* end;
+    template <class T>
+    T take() {
+        if (p + sizeof(T) > end) die("truncated tape");
+        T v;
+        std::memcpy(&v, p, sizeof(T));
+        p += sizeof(T);
+        return v;
+    }
+    Addr addr() {
+        Addr a;
+        a.id = take<uint32_t>();
+        a.off = take<uint64_t>();
+        return a;
+    }
+    std::vector<unsigned char> raw(size_t n) {
+        if (p + n > end) die("truncated tape");
+        std::vector<unsigned char> v(p, p + n);
+        p += n;
+        return v;
+    }
+};
+
+std::vector<Op> read_tape(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) die("cannot open " + path);
+    std::vector<unsigned char> d((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    if (d.size() < 8 || std::memcmp(d.data(), "BCSTAPE1", 8) != 0) die(path + " is not a launch tape");
+    std::vector<Op> ops;
+    size_t o = 8;
+    while (o < d.size()) {
+        if (o + 12 > d.size()) die("truncated tape");
+        Op op;
+        std::memcpy(&op.code, &d[o], 4);
+        uint64_t size;
+        std::memcpy(&size, &d[o + 4], 8);
+        o += 12;
+        if (o + size > d.size()) die("truncated tape");
+        Cursor c{&d[o], &d[o] + size};
+        o += size;
+        switch (op.code) {
+            case 1: op.id = c.take<uint32_t>(); op.bytes = c.take<uint64_t>(); break;
+            case 2: op.id = c.take<uint32_t>(); break;
+            case 3: op.a = c.addr(); op.bytes = c.take<uint64_t>(); op.data = c.raw(op.bytes); break;
+            case 4: op.a = c.addr(); op.b = c.addr(); op.bytes = c.take<uint64_t>(); break;
+            case 5: op.a = c.addr(); op.value = c.take<int32_t>(); op.bytes = c.take<uint64_t>(); break;
+            case 6: case 10: op.stream = c.take<uint32_t>(); break;
+            case 7: {
+                op.kernel = c.take<uint64_t>();
+                for (auto& g : op.grid) g = c.take<uint32_t>();
+                for (auto& b : op.block) b = c.take<uint32_t>();
+                op.shmem = c.take<uint32_t>();
+                op.stream = c.take<uint32_t>();
+                const uint32_t np = c.take<uint32_t>();
+                for (uint32_t i = 0; i < np; ++i) {
+                    Param prm;
+                    const uint32_t sz = c.take<uint32_t>(), nr = c.take<uint32_t>();
+                    prm.bytes = c.raw(sz);
+                    for (uint32_t r = 0; r < nr; ++r) {
+                        Reloc rl;
+                        rl.offset = c.take<uint32_t>();
+                        rl.id = c.take<uint32_t>();
+                        rl.off = c.take<uint64_t>();
+                        prm.relocs.push_back(rl);
+                    }
+                    op.params.push_back(std::move(prm));
+                }
+                break;
+            }
+            case 8: op.a = c.addr(); op.b = c.addr(); op.n = c.take<uint32_t>(); break;
+            case 9: break;
+            case 11: { auto v = c.raw(size); op.text.assign(v.begin(), v.end()); break; }
+            case 12: {
+                op.a = c.addr();
+                op.bytes = c.take<uint64_t>();
+                auto v = c.raw(c.end - c.p);
+                op.text.assign(v.begin(), v.end());
+                break;
+            }
+            case 13: op.a = c.addr(); op.b = c.addr(); op.c = c.addr(); op.n = c.take<uint32_t>(); break;
+            default: die("unknown op in tape");
+        }
+        if (c.p != c.end) die("malformed op in tape");
+        ops.push_back(std::move(op));
+    }
+    return ops;
+}
+
+// The last occupied cell's range (the reference never writes its end,
+// uniform_grid.cu:78); the CPU pin sets it on the host after each build.
+__global__ void k_fix_last_cell(const int* keys, int n, int* starts, int* ends, long long cells) {
+    if (blockIdx.x != 0 || threadIdx.x != 0 || n <= 0) return;
+    const int last = keys[n - 1];
+    if (last < 0 || last >= cells) return;
+    int first = n - 1;
+    while (first > 0 && keys[first - 1] == last) --first;
+    starts[last] = first;
+    ends[last] = n - 1;
+}
+
+// Particles outside the guarded box, and the largest speed (as float bits;
+// speeds are non-negative, so their bit patterns order like the values).
+__global__ void k_guard(const float* x, const float* y, const float* z, const float* vx, const float* vy,
+                        const float* vz, int n, float3 lo, float3 hi, unsigned* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const bool inside = x[i] >= lo.x && x[i] <= hi.x && y[i] >= lo.y && y[i] <= hi.y && z[i] >= lo.z &&
+                            z[i] <= hi.z;
+        if (!inside) atomicAdd(&out[0], 1u);
+        const float s = sqrtf(vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+        atomicMax(&out[1], s == s ? __float_as_uint(s) : 0x7F800000u);
+    }
+}
+
+struct Replay {
+    CUmodule module = nullptr;
+    std::map<uint64_t, std::string> entry_of;
+    std::map<uint64_t, CUfunction> fn;
+    std::vector<void*> base;
+    std::vector<uint64_t> size;
+    std::vector<cudaStream_t> streams{nullptr};
+    std::map<std::string, std::pair<void*, uint64_t>> buffers;
+    long launches = 0;
+
+    char* at(const Addr& a, uint64_t bytes) {
+        if (a.id >= base.size() || !base[a.id]) die("tape names an allocation that does not exist");
+        if (a.off + bytes > size[a.id]) die("tape op reaches past its allocation");
+        return static_cast<char*>(base[a.id]) + a.off;
+    }
+
+    CUfunction function(uint64_t kernel) {
+        auto it = fn.find(kernel);
+        if (it != fn.end()) return it->second;
+        auto e = entry_of.find(kernel);
+        if (e == entry_of.end()) die("kernel without a cubin entry");
+        CUfunction f;
+        check(cuModuleGetFunction(&f, module, e->second.c_str()), e->second.c_str());
+        fn[kernel] = f;
+        return f;
+    }
+
+    // Every check a launch must pass, before the frame that holds it runs.
+    void validate(const Op& op) {
+        CUfunction f = function(op.kernel);
+        for (size_t i = 0; i < op.params.size(); ++i) {
+            size_t off = 0, sz = 0;
+            check(cuFuncGetParamInfo(f, i, &off, &sz), "cuFuncGetParamInfo");
+            if (sz != op.params[i].bytes.size()) die("recorded argument size differs from the kernel's parameter");
+            for (const Reloc& r : op.params[i].relocs) {
+                if (r.offset + 8 > op.params[i].bytes.size()) die("relocation outside its argument");
+                if (r.id >= size.size() || r.off > size[r.id]) die("relocated pointer outside its allocation");
+            }
+        }
+        size_t off = 0, sz = 0;
+        if (cuFuncGetParamInfo(f, op.params.size(), &off, &sz) == CUDA_SUCCESS) die("kernel takes more parameters");
+        const uint64_t threads = (uint64_t)op.block[0] * op.block[1] * op.block[2];
+        if (threads == 0 || threads > 1024 || !op.grid[0] || !op.grid[1] || !op.grid[2]) die("illegal launch shape");
+        if (op.stream >= streams.size()) die("launch on a stream that was not created");
+    }
+
+    void launch(const Op& op) {
+        std::vector<std::vector<unsigned char>> bufs(op.params.size());
+        std::vector<void*> args(op.params.size());
+        for (size_t i = 0; i < op.params.size(); ++i) {
+            bufs[i] = op.params[i].bytes;
+            for (const Reloc& r : op.params[i].relocs) {
+                const uint64_t v = reinterpret_cast<uint64_t>(base[r.id]) + r.off;
+                std::memcpy(&bufs[i][r.offset], &v, 8);
+            }
+            args[i] = bufs[i].data();
+        }
+        check(cuLaunchKernel(function(op.kernel), op.grid[0], op.grid[1], op.grid[2], op.block[0], op.block[1],
+                             op.block[2], op.shmem, reinterpret_cast<CUstream>(streams[op.stream]), args.data(),
+                             nullptr),
+              "cuLaunchKernel");
+        ++launches;
+    }
+
+    void run(const Op& op) {
+        switch (op.code) {
+            case 1: {
+                if (op.id != base.size()) die("allocations out of order");
+                void* p = nullptr;
+                check(cudaMalloc(&p, op.bytes), "cudaMalloc");
+                check(cudaMemset(p, 0, op.bytes), "cudaMemset");   // fresh pages read as zero
+                base.push_back(p);
+                size.push_back(op.bytes);
+                break;
+            }
+            case 2: break;   // freed at exit
+            case 3: check(cudaMemcpy(at(op.a, op.bytes), op.data.data(), op.bytes, cudaMemcpyHostToDevice), "h2d"); break;
+            case 4: check(cudaMemcpy(at(op.a, op.bytes), at(op.b, op.bytes), op.bytes, cudaMemcpyDeviceToDevice), "d2d"); break;
+            case 5: check(cudaMemset(at(op.a, op.bytes), op.value, op.bytes), "memset"); break;
+            case 6: {
+                if (op.stream != streams.size()) die("streams out of order");
+                cudaStream_t s;
+                check(cudaStreamCreate(&s), "cudaStreamCreate");   // as the reference creates them
+                streams.push_back(s);
+                break;
+            }
+            case 7: launch(op); break;
+            case 8: {
+                int* k = reinterpret_cast<int*>(at(op.a, sizeof(int) * (uint64_t)op.n));
+                int* v = reinterpret_cast<int*>(at(op.b, sizeof(int) * (uint64_t)op.n));
+                thrust::stable_sort_by_key(thrust::device, k, k + op.n, v);   // uniform_grid.cu:144-147
+                break;
+            }
+            case 9: check(cudaDeviceSynchronize(), "cudaDeviceSynchronize"); break;
+            case 10: check(cudaStreamSynchronize(streams.at(op.stream)), "cudaStreamSynchronize"); break;
+            case 11: break;
+            case 12: buffers[op.text] = {at(op.a, op.bytes), op.bytes}; break;
+            case 13: {
+                const int* k = reinterpret_cast<const int*>(at(op.a, sizeof(int) * (uint64_t)op.n));
+                int* s = reinterpret_cast<int*>(at(op.b, 0));
+                int* e = reinterpret_cast<int*>(at(op.c, 0));
+                const long long cells = (long long)std::min(size[op.b.id] - op.b.off, size[op.c.id] - op.c.off) / 4;
+                k_fix_last_cell<<<1, 1>>>(k, (int)op.n, s, e, cells);
+                check(cudaGetLastError(), "k_fix_last_cell");
+                break;
+            }
+        }
+    }
+
+    std::pair<float*, uint64_t> buffer(const std::string& name) {
+        auto it = buffers.find(name);
+        if (it == buffers.end()) die("tape marks no buffer " + name);
+        return {static_cast<float*>(it->second.first), it->second.second};
+    }
+};
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 5) {
+        std::fprintf(stderr, "usage: ref_cuda_replay <dir> <reference|pinned> <state.bin|-> <frames> [<out.bin>]\n");
+        return 1;
+    }
+    const std::string dir = argv[1], mode = argv[2], state = argv[3];
+    const int frames = std::atoi(argv[4]);
+    if (mode != "reference" && mode != "pinned") die("mode is reference or pinned");
+    Replay R;
+    {
+        std::ifstream k(dir + "/kernels.txt");
+        if (!k) die("cannot open kernels.txt");
+        std::string line;
+        while (std::getline(k, line)) {
+            std::istringstream ss(line);
+            std::string addr, entry;
+            if (ss >> addr >> entry) R.entry_of[std::stoull(addr, nullptr, 16)] = entry;
+        }
+    }
+    const std::vector<Op> ops = read_tape(dir + "/" + mode + ".tape");
+    // segments
+    std::vector<const Op*> setup, frame;
+    int phase = 0;   // 0 setup, 1 between, 2 first frame, 3 after it
+    for (const Op& op : ops) {
+        if (op.code == 11) {
+            if (op.text == "setup_end") phase = 1;
+            else if (op.text == "frame" && phase == 1) phase = 2;
+            else if (op.text == "frame_end" && phase == 2) phase = 3;
+            continue;
+        }
+        if (phase == 0) setup.push_back(&op);
+        else if (phase == 2) frame.push_back(&op);
+    }
+    if (phase != 3 || frame.empty()) die("tape holds no complete frame");
+
+    check(cudaSetDevice(0), "cudaSetDevice");
+    check(cudaFree(nullptr), "context");
+    check(cuModuleLoad(&R.module, (dir + "/kernels.cubin").c_str()), "cuModuleLoad");
+
+    for (const Op* op : setup) R.run(*op);
+    check(cudaDeviceSynchronize(), "construction");
+    for (const Op* op : frame)
+        if (op->code == 7) R.validate(*op);
+
+    auto [px, n4] = R.buffer("positions.x");
+    const size_t n = n4 / sizeof(float);
+    if (state != "-") {
+        std::ifstream f(state, std::ios::binary);
+        std::vector<float> s(6 * n);
+        if (!f.read(reinterpret_cast<char*>(s.data()), sizeof(float) * s.size())) die("state file too short");
+        const char* names[2] = {"positions", "velocities"};
+        for (int q = 0; q < 2; ++q)
+            for (int c = 0; c < 3; ++c) {
+                std::vector<float> comp(n);
+                for (size_t i = 0; i < n; ++i) comp[i] = s[3 * n * q + 3 * i + c];
+                auto b = R.buffer(std::string(names[q]) + "." + "xyz"[c]);
+                if (b.second != sizeof(float) * n) die("buffer sizes differ");
+                check(cudaMemcpy(b.first, comp.data(), b.second, cudaMemcpyHostToDevice), "state");
+            }
+    }
+    check(cudaDeviceSynchronize(), "state");
+
+    // the box and time step, and the guard band
+    float box[6], dt = 0.f;
+    {
+        std::ifstream l(dir + "/limits.txt");
+        if (!(l >> box[0] >> box[1] >> box[2] >> box[3] >> box[4] >> box[5] >> dt) || !(dt > 0.f))
+            die("cannot read limits.txt");
+    }
+    const float guard = 0.1f * std::min({box[1] - box[0], box[3] - box[2], box[5] - box[4]});
+    const float3 glo = make_float3(box[0] + guard, box[2] + guard, box[4] + guard);
+    const float3 ghi = make_float3(box[1] - guard, box[3] - guard, box[5] - guard);
+    unsigned* gword = nullptr;
+    check(cudaMalloc(&gword, 2 * sizeof(unsigned)), "cudaMalloc");
+    auto chunk_allowed = [&](int want) {
+        check(cudaMemset(gword, 0, 2 * sizeof(unsigned)), "cudaMemset");
+        auto b = [&](const char* nm) { return R.buffer(nm).first; };
+        k_guard<<<std::max<size_t>(1, std::min<size_t>(4096, (n + 255) / 256)), 256>>>(
+            b("positions.x"), b("positions.y"), b("positions.z"), b("velocities.x"), b("velocities.y"),
+            b("velocities.z"), (int)n, glo, ghi, gword);
+        unsigned h[2];
+        check(cudaMemcpy(h, gword, sizeof(h), cudaMemcpyDeviceToHost), "guard");
+        float vmax;
+        std::memcpy(&vmax, &h[1], 4);
+        if (h[0] != 0 || !(vmax < 3.0e38f)) return 0;
+        // a quarter of the band per chunk leaves room for the speed to grow
+        const double reach = vmax * (double)dt;
+        return reach <= 0.0 ? want : (int)std::min<double>(want, std::floor(0.25 * guard / reach));
+    };
+
+    const long before = R.launches;
+    cudaEvent_t e0, e1;
+    check(cudaEventCreate(&e0), "event");
+    check(cudaEventCreate(&e1), "event");
+    double total_ms = 0.0;
+    int done = 0;
+    while (done < frames) {
+        const int c = chunk_allowed(std::min(frames - done, 50));
+        if (c <= 0) break;
+        check(cudaEventRecord(e0, nullptr), "event");
+        for (int f = 0; f < c; ++f)
+            for (const Op* op : frame) R.run(*op);
+        check(cudaEventRecord(e1, nullptr), "event");
+        check(cudaEventSynchronize(e1), "frames");
+        float ms = 0.f;
+        check(cudaEventElapsedTime(&ms, e0, e1), "event");
+        check(cudaGetLastError(), "frames");
+        total_ms += ms;
+        done += c;
+    }
+
+    if (argc > 5) {
+        std::vector<float> out(9 * n);
+        const char* names[3] = {"positions", "velocities", "forces"};
+        for (int q = 0; q < 3; ++q)
+            for (int c = 0; c < 3; ++c) {
+                std::vector<float> comp(n);
+                auto b = R.buffer(std::string(names[q]) + "." + "xyz"[c]);
+                check(cudaMemcpy(comp.data(), b.first, b.second, cudaMemcpyDeviceToHost), "read back");
+                for (size_t i = 0; i < n; ++i) out[3 * n * q + 3 * i + c] = comp[i];
+            }
+        std::ofstream o(argv[5], std::ios::binary);
+        o.write(reinterpret_cast<const char*>(out.data()), sizeof(float) * out.size());
+    }
+    std::printf("{\"frames\": %d, \"frames_requested\": %d, \"ms_per_frame\": %.6f, \"particles\": %zu, "
+                "\"launches_per_frame\": %ld}\n",
+                done, frames, done ? total_ms / done : 0.0, n, done ? (R.launches - before) / done : 0L);
+    return 0;
+}

@@ -1,8 +1,13 @@
-"""Rewrite CUDA kernel launches `kernel<<<cfg>>>(args);` into
-`bcs_launch(bcs_cfg(cfg), [&]() { kernel(args); });` so that a scratch copy
-of the reference's sources compiles with g++ and its kernels run on the CPU
-through the serial launch shim (refcpu_shim.h).  Pin-recipe tooling: it only
-ever writes into the scratch directory it is given."""
+"""Rewrite CUDA kernel launches `kernel<<<cfg>>>(args);` of a scratch copy of
+the reference's sources so that it compiles with g++:
+
+  form "cpu":  `bcs_launch(bcs_cfg(cfg), [&]() { kernel(args); });` runs the
+               kernel on the CPU through the serial launch shim (refcpu_shim.h);
+  form "tape": `bcs_tape_launch(bcs_cfg(cfg), kernel, args);` records the
+               launch (oracle/ref_cuda/tape_shim.h).
+
+Pin-recipe tooling: it only ever writes into the scratch directory it is
+given."""
 from __future__ import annotations
 
 import re
@@ -27,7 +32,7 @@ def _statement_start(text: str, pos: int) -> int:
     return 0
 
 
-def rewrite(text: str) -> tuple[str, int]:
+def rewrite(text: str, form: str = "cpu") -> tuple[str, int]:
     out = []
     last = 0
     count = 0
@@ -56,7 +61,11 @@ def rewrite(text: str) -> tuple[str, int]:
         args = text[p + 1:q]
         semi = text.index(";", q)
         out.append(text[last:start])
-        out.append(f"bcs_launch(bcs_cfg({cfg}), [&]() {{ {kernel}({args}); }});")
+        if form == "tape":
+            rest = f", {args}" if args.strip() else ""
+            out.append(f"bcs_tape_launch(bcs_cfg({cfg}), {kernel}{rest});")
+        else:
+            out.append(f"bcs_launch(bcs_cfg({cfg}), [&]() {{ {kernel}({args}); }});")
         last = semi + 1
         count += 1
     out.append(text[last:])

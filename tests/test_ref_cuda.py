@@ -1,0 +1,158 @@
+"""The reference's own CUDA build as a replayable cubin and launch tape
+(oracle/ref_cuda), checked on the CPU: the recipe compiles the reference's
+simulation translation units unmodified for sm_103a, records its host code's
+launches, and every recorded launch is complete and safe to replay.
+
+Runs where the reference's sources are present (the recipe reads them).
+"""
+import os
+import struct
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(REPO, "oracle", "ref_cuda"))
+
+import build_ref_cuda as B  # noqa: E402
+import tape as T  # noqa: E402
+
+pytestmark = pytest.mark.skipif(not B.available(), reason="reference sources not present")
+
+SCENE = "icosphere_cfg1"
+
+
+@pytest.fixture(scope="module")
+def built():
+    B.build_all([SCENE])
+    return os.path.join(B.OUT, "refcuda_" + SCENE)
+
+
+def kernel_names(d):
+    out = {}
+    for line in open(os.path.join(d, "kernels.txt")):
+        addr, entry = line.split()
+        out[int(addr, 16)] = entry
+    return out
+
+
+def _shape(op):
+    """An op without the bytes of class arguments: their padding holds
+    whatever the recorder's copies left there, which differs between runs
+    and no kernel reads.  Scalar arguments (4 and 8 bytes) stay."""
+    o = dict(op)
+    if "params" in o:
+        o["params"] = [(len(p["bytes"]), p["bytes"] if len(p["bytes"]) <= 8 else b"",
+                        tuple((r["offset"], r["id"], r["off"]) for r in p["relocs"])) for p in o["params"]]
+    return repr(sorted(o.items()))
+
+
+def test_artifacts(built):
+    for f in ("kernels.cubin", "entries.txt", "kernels.txt", "reference.tape", "pinned.tape", "limits.txt"):
+        assert os.path.getsize(os.path.join(built, f)) > 0, f
+    with open(os.path.join(built, "kernels.cubin"), "rb") as f:
+        assert f.read(4) == b"\x7fELF"
+
+
+@pytest.mark.parametrize("mode", ["reference", "pinned"])
+def test_frames_repeat_exactly(built, mode):
+    """The frame is a fixed launch sequence: both recorded frames are equal
+    op for op (kernels, shapes, streams, scalar arguments, every pointer),
+    so replaying one frame K times is the reference's K frames."""
+    seg = T.segments(T.read(os.path.join(built, mode + ".tape")))
+    assert len(seg["frames"]) == 2
+    assert [_shape(o) for o in seg["frames"][0]] == [_shape(o) for o in seg["frames"][1]]
+
+
+def test_frame_follows_the_reference_call_order(built):
+    """main.cu:175-208: two grid builds (cell ids, stable sort, ranges), the
+    vein springs, centroids and springs per type, particle collisions per
+    type, vein collisions per type, the two integrations."""
+    names = kernel_names(built)
+    seg = T.segments(T.read(os.path.join(built, "reference.tape")))
+    seq = []
+    for op in seg["frames"][0]:
+        if op["op"] == "launch":
+            n = names[op["kernel"]]
+            for tag in ("calculateCellIdKernel", "calculateStartAndEndOfCellKernel", "calculateBloodCellsCenters",
+                        "gatherForcesKernelILi", "gatherForcesKerneliii13VeinTriangles",
+                        "calculateParticleCollisions", "detectVeinCollisions", "propagateParticleForcesKernel",
+                        "propagateForcesIntoPositionsKernel"):
+                if tag in n:
+                    seq.append(tag)
+                    break
+            else:
+                seq.append(n)
+        elif op["op"] == "sort":
+            seq.append("sort")
+    assert seq == ["calculateCellIdKernel", "sort", "calculateStartAndEndOfCellKernel",
+                   "calculateCellIdKernel", "sort", "calculateStartAndEndOfCellKernel",
+                   "gatherForcesKerneliii13VeinTriangles", "calculateBloodCellsCenters", "gatherForcesKernelILi",
+                   "calculateParticleCollisions", "detectVeinCollisions", "propagateParticleForcesKernel",
+                   "propagateForcesIntoPositionsKernel"]
+
+
+def test_pinned_tape_adds_only_the_q5_ops(built):
+    ref = [o for o in T.read(os.path.join(built, "reference.tape")) if o["op"] not in ("memset", "fix_last_cell")]
+    pin = [o for o in T.read(os.path.join(built, "pinned.tape")) if o["op"] not in ("memset", "fix_last_cell")]
+    assert [_shape(o) for o in ref] == [_shape(o) for o in pin]
+    seg = T.segments(T.read(os.path.join(built, "pinned.tape")))
+    assert sum(o["op"] == "fix_last_cell" for o in seg["frames"][0]) == 2
+
+
+def test_every_launch_is_safe_to_replay(built):
+    """Each kernel has one cubin entry; every device pointer inside an
+    argument lies in an allocation made before the launch; no argument word
+    looks like a host address; launch shapes are legal."""
+    names = kernel_names(built)
+    entries = set(open(os.path.join(built, "entries.txt")).read().split())
+    for mode in ("reference", "pinned"):
+        allocs = {}
+        for op in T.read(os.path.join(built, mode + ".tape")):
+            if op["op"] == "alloc":
+                allocs[op["id"]] = op["bytes"]
+            if op["op"] != "launch":
+                continue
+            assert names[op["kernel"]] in entries
+            threads = op["block"][0] * op["block"][1] * op["block"][2]
+            assert 0 < threads <= 1024 and min(op["grid"]) > 0 and op["shmem"] == 0
+            for p in op["params"]:
+                rel = {r["offset"] for r in p["relocs"]}
+                for r in p["relocs"]:
+                    assert r["id"] in allocs and r["off"] <= allocs[r["id"]]
+                    assert r["offset"] % 8 == 0 and r["offset"] + 8 <= len(p["bytes"])
+                for off in range(0, len(p["bytes"]) - 7, 8):
+                    if off in rel:
+                        continue
+                    w = struct.unpack_from("<Q", p["bytes"], off)[0]
+                    assert not (0x550000000000 <= w < 0x800000000000), "host address in a kernel argument"
+
+
+def test_cell_id_arguments(built):
+    """calculateCellIdKernel(x, y, z, cellIds, particleIds, count, cellWidth,
+    cellHeight, cellDepth) of the particle grid: five device pointers, then
+    the particle count and the integer cell sizes (uniform_grid.cu:38-39)."""
+    names = kernel_names(built)
+    seg = T.segments(T.read(os.path.join(built, "reference.tape")))
+    op = next(o for o in seg["frames"][0] if o["op"] == "launch")
+    assert "calculateCellIdKernel" in names[op["kernel"]]
+    assert [len(p["relocs"]) for p in op["params"]] == [1, 1, 1, 1, 1, 0, 0, 0, 0]
+    ints = [struct.unpack("<i", p["bytes"])[0] for p in op["params"][5:]]
+    assert ints == [16 * 42, 1, 1, 1]
+
+
+def test_state_buffers_are_marked(built):
+    ops = T.read(os.path.join(built, "reference.tape"))
+    bufs = {o["name"]: o["bytes"] for o in ops if o["op"] == "buffer"}
+    for q in ("positions", "velocities", "forces"):
+        for c in "xyz":
+            assert bufs[f"{q}.{c}"] == 4 * 16 * 42
+
+
+def test_replay_source_compiles_for_sm_103a(tmp_path):
+    out = tmp_path / "ref_cuda_replay"
+    r = subprocess.run(["nvcc", "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-o", str(out),
+                        os.path.join(REPO, "oracle", "ref_cuda", "replay.cu"), "-L/usr/local/cuda/lib64/stubs",
+                        "-lcuda"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]

@@ -15,6 +15,10 @@ oracle/_ref/refcuda_<scene>/:
                   applies (parity against the pin)
   kernels.txt     recorder address -> cubin entry, one line per kernel on a tape
   layout.json     counts of the folded scene
+  limits.txt      the reference's grid box and dt (the replay's guard)
+  tape_recorder   the recorder (host code of this machine); it also replays
+                  its tapes on the CPU (--replay-cpu), which the tests compare
+                  with the CPU pin
 
 The tape is recorded by the reference's own host code (constructors,
 calculateGrid, gatherForcesFromNeighbors, propagateForcesIntoPositions),
@@ -57,7 +61,8 @@ DEVICE_TUS = ["grids/uniform_grid.cu", "objects/blood_cells.cu", "objects/vein_n
               "simulation/vein_end.cu", "utilities/cuda_vec3.cu"]
 HOST_TUS = ["grids/uniform_grid.cu", "objects/blood_cells.cu", "objects/vein_triangles.cu",
             "objects/vein_neighbors.cu", "utilities/cuda_vec3.cu", "simulation/vein_collisions.cu"]
-RECIPE = [os.path.join(HERE, f) for f in ("build_ref_cuda.py", "tape_shim.h", "tape_runtime.cpp", "tape_driver.cpp")] + \
+RECIPE = [os.path.join(HERE, f) for f in ("build_ref_cuda.py", "tape_shim.h", "tape_format.h", "tape_runtime.cpp",
+                                          "tape_driver.cpp")] + \
          [os.path.join(PIN, "launch_rewrite.py")]
 _SORT = re.compile(r"thrust::stable_sort_by_key\(\s*(\w+)\s*,\s*\1\s*\+\s*(\w+)\s*,\s*(\w+)\s*\)\s*;")
 _ENTRY = re.compile(r"Compiling entry function '([^']+)'")
@@ -152,7 +157,7 @@ def build_recorder(src: str, out: str) -> str:
     jobs = [(os.path.join(src, tu), os.path.join(obj, os.path.basename(tu) + ".o"), flags) for tu in HOST_TUS]
     jobs.append((os.path.join(HERE, "tape_driver.cpp"), os.path.join(obj, "tape_driver.o"), flags))
     jobs.append((os.path.join(HERE, "tape_runtime.cpp"), os.path.join(obj, "tape_runtime.o"),
-                 ["-std=c++17", "-O1", "-fno-pie", "-I/usr/local/cuda/include"]))
+                 ["-std=c++17", "-O1", "-fno-pie", "-I" + HERE, "-I/usr/local/cuda/include"]))
 
     def one(job):
         s, o, fl = job
@@ -237,7 +242,6 @@ def build(tag: str, scene, frames: int = 2, force: bool = False) -> str:
         lines.append(f"{addr:x} {entry}")
     with open(os.path.join(out, "kernels.txt"), "w") as f:
         f.write("\n".join(lines) + "\n")
-    os.remove(exe)   # host code of this machine: only its symbol table was needed
     with open(os.path.join(out, "layout.json"), "w") as f:
         json.dump({"scene": tag, "particles": int(sum(t.count * len(t.vertices) for t in scene.types)),
                    "cells": int(sum(t.count for t in scene.types)), "vein_vertices": int(len(scene.vein_positions)),

@@ -33,6 +33,8 @@
 #include <thrust/execution_policy.h>
 #include <thrust/sort.h>
 
+#include "tape_format.h"
+
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -63,127 +65,7 @@ void check(CUresult r, const char* what) {
     }
 }
 
-struct Addr {
-    uint32_t id = 0;
-    uint64_t off = 0;
-};
-
-struct Reloc {
-    uint32_t offset, id;
-    uint64_t off;
-};
-
-struct Param {
-    std::vector<unsigned char> bytes;
-    std::vector<Reloc> relocs;
-};
-
-struct Op {
-    uint32_t code = 0;
-    // alloc / free / stream / sync_stream
-    uint32_t id = 0;
-    uint64_t bytes = 0;
-    // copies, memset, sort, fix_last_cell, buffer
-    Addr a, b, c;
-    int32_t value = 0;
-    uint32_t n = 0;
-    std::vector<unsigned char> data;
-    std::string text;
-    // launch
-    uint64_t kernel = 0;
-    uint32_t grid[3] = {}, block[3] = {}, shmem = 0, stream = 0;
-    std::vector<Param> params;
-};
-
-struct Cursor {
-    const unsigned char* p;
-    const unsigned char* end;
-    template <class T>
-    T take() {
-        if (p + sizeof(T) > end) die("truncated tape");
-        T v;
-        std::memcpy(&v, p, sizeof(T));
-        p += sizeof(T);
-        return v;
-    }
-    Addr addr() {
-        Addr a;
-        a.id = take<uint32_t>();
-        a.off = take<uint64_t>();
-        return a;
-    }
-    std::vector<unsigned char> raw(size_t n) {
-        if (p + n > end) die("truncated tape");
-        std::vector<unsigned char> v(p, p + n);
-        p += n;
-        return v;
-    }
-};
-
-std::vector<Op> read_tape(const std::string& path) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) die("cannot open " + path);
-    std::vector<unsigned char> d((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
-    if (d.size() < 8 || std::memcmp(d.data(), "BCSTAPE1", 8) != 0) die(path + " is not a launch tape");
-    std::vector<Op> ops;
-    size_t o = 8;
-    while (o < d.size()) {
-        if (o + 12 > d.size()) die("truncated tape");
-        Op op;
-        std::memcpy(&op.code, &d[o], 4);
-        uint64_t size;
-        std::memcpy(&size, &d[o + 4], 8);
-        o += 12;
-        if (o + size > d.size()) die("truncated tape");
-        Cursor c{&d[o], &d[o] + size};
-        o += size;
-        switch (op.code) {
-            case 1: op.id = c.take<uint32_t>(); op.bytes = c.take<uint64_t>(); break;
-            case 2: op.id = c.take<uint32_t>(); break;
-            case 3: op.a = c.addr(); op.bytes = c.take<uint64_t>(); op.data = c.raw(op.bytes); break;
-            case 4: op.a = c.addr(); op.b = c.addr(); op.bytes = c.take<uint64_t>(); break;
-            case 5: op.a = c.addr(); op.value = c.take<int32_t>(); op.bytes = c.take<uint64_t>(); break;
-            case 6: case 10: op.stream = c.take<uint32_t>(); break;
-            case 7: {
-                op.kernel = c.take<uint64_t>();
-                for (auto& g : op.grid) g = c.take<uint32_t>();
-                for (auto& b : op.block) b = c.take<uint32_t>();
-                op.shmem = c.take<uint32_t>();
-                op.stream = c.take<uint32_t>();
-                const uint32_t np = c.take<uint32_t>();
-                for (uint32_t i = 0; i < np; ++i) {
-                    Param prm;
-                    const uint32_t sz = c.take<uint32_t>(), nr = c.take<uint32_t>();
-                    prm.bytes = c.raw(sz);
-                    for (uint32_t r = 0; r < nr; ++r) {
-                        Reloc rl;
-                        rl.offset = c.take<uint32_t>();
-                        rl.id = c.take<uint32_t>();
-                        rl.off = c.take<uint64_t>();
-                        prm.relocs.push_back(rl);
-                    }
-                    op.params.push_back(std::move(prm));
-                }
-                break;
-            }
-            case 8: op.a = c.addr(); op.b = c.addr(); op.n = c.take<uint32_t>(); break;
-            case 9: break;
-            case 11: { auto v = c.raw(size); op.text.assign(v.begin(), v.end()); break; }
-            case 12: {
-                op.a = c.addr();
-                op.bytes = c.take<uint64_t>();
-                auto v = c.raw(c.end - c.p);
-                op.text.assign(v.begin(), v.end());
-                break;
-            }
-            case 13: op.a = c.addr(); op.b = c.addr(); op.c = c.addr(); op.n = c.take<uint32_t>(); break;
-            default: die("unknown op in tape");
-        }
-        if (c.p != c.end) die("malformed op in tape");
-        ops.push_back(std::move(op));
-    }
-    return ops;
-}
+using namespace bcs_tape;
 
 // The last occupied cell's range (the reference never writes its end,
 // uniform_grid.cu:78); the CPU pin sets it on the host after each build.
@@ -307,6 +189,7 @@ struct Replay {
             case 10: check(cudaStreamSynchronize(streams.at(op.stream)), "cudaStreamSynchronize"); break;
             case 11: break;
             case 12: buffers[op.text] = {at(op.a, op.bytes), op.bytes}; break;
+            case 14: break;   // host-side call thunks of the recorder's own CPU replay
             case 13: {
                 const int* k = reinterpret_cast<const int*>(at(op.a, sizeof(int) * (uint64_t)op.n));
                 int* s = reinterpret_cast<int*>(at(op.b, 0));
@@ -347,21 +230,14 @@ int main(int argc, char** argv) {
             if (ss >> addr >> entry) R.entry_of[std::stoull(addr, nullptr, 16)] = entry;
         }
     }
-    const std::vector<Op> ops = read_tape(dir + "/" + mode + ".tape");
-    // segments
+    std::vector<Op> ops;
     std::vector<const Op*> setup, frame;
-    int phase = 0;   // 0 setup, 1 between, 2 first frame, 3 after it
-    for (const Op& op : ops) {
-        if (op.code == 11) {
-            if (op.text == "setup_end") phase = 1;
-            else if (op.text == "frame" && phase == 1) phase = 2;
-            else if (op.text == "frame_end" && phase == 2) phase = 3;
-            continue;
-        }
-        if (phase == 0) setup.push_back(&op);
-        else if (phase == 2) frame.push_back(&op);
+    try {
+        ops = read(dir + "/" + mode + ".tape");
+        segments(ops, setup, frame);
+    } catch (const std::exception& e) {
+        die(e.what());
     }
-    if (phase != 3 || frame.empty()) die("tape holds no complete frame");
 
     check(cudaSetDevice(0), "cudaSetDevice");
     check(cudaFree(nullptr), "context");

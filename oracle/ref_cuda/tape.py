@@ -2,14 +2,14 @@
 
 read(path) returns the ops in order as dicts; an address is always an
 (allocation id, offset) pair.  The opcodes and payloads are listed in
-tape_runtime.cpp.
+tape_format.h.
 """
 from __future__ import annotations
 
 import struct
 
 OPS = {1: "alloc", 2: "free", 3: "h2d", 4: "d2d", 5: "memset", 6: "stream", 7: "launch", 8: "sort",
-       9: "sync_device", 10: "sync_stream", 11: "mark", 12: "buffer", 13: "fix_last_cell"}
+       9: "sync_device", 10: "sync_stream", 11: "mark", 12: "buffer", 13: "fix_last_cell", 14: "thunk"}
 
 
 class _Reader:
@@ -81,6 +81,8 @@ def read(path: str) -> list:
             op["at"] = r.addr()
             op["bytes"] = r.take("Q")
             op["name"] = r.raw(len(r.b) - r.o).decode()
+        elif name == "thunk":
+            op["kernel"], op["thunk"] = r.take("QQ")
         elif name == "fix_last_cell":
             op["keys"], op["starts"], op["ends"] = r.addr(), r.addr(), r.addr()
             op["n"] = r.take("I")
@@ -92,9 +94,11 @@ def read(path: str) -> list:
 
 def segments(ops: list) -> dict:
     """The ops before "setup_end" and between each "frame" / "frame_end"
-    pair: {"setup": [...], "frames": [[...], ...]}."""
+    pair, without thunk records: {"setup": [...], "frames": [[...], ...]}."""
     setup, frames, cur, in_setup = [], [], None, True
     for op in ops:
+        if op["op"] == "thunk":   # emitted where a kernel first appears; part of no segment
+            continue
         if op["op"] == "mark":
             if op["label"] == "setup_end":
                 in_setup = False

@@ -20,6 +20,8 @@
 //   reference: the reference's calls exactly (timing);
 //   pinned: also the Q5 clears before each grid build and the last occupied
 //           cell's range after it, as the CPU pin does (parity).
+//        tape_driver --replay-cpu <tape> <state.bin|-> <frames> <out.bin>
+//   runs a tape this executable recorded on the CPU (tape_runtime.cpp).
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -57,7 +59,11 @@ static void mark_vec3(const char* name, const cudaVec3& v, int n) {
     bcs_tape_mark_buffer((s + ".z").c_str(), v.z, sizeof(float) * (size_t)n);
 }
 
+int bcs_tape_replay_cpu(const char* tape, const char* state, int frames, const char* out);
+
 int main(int argc, char** argv) {
+    if (argc == 6 && std::strcmp(argv[1], "--replay-cpu") == 0)
+        return bcs_tape_replay_cpu(argv[2], argv[3], std::atoi(argv[4]), argv[5]);
     if (argc < 4) {
         std::fprintf(stderr, "usage: tape_driver <out.tape> <reference|pinned> <frames>\n");
         return 1;

@@ -9,9 +9,11 @@
 //
 // Tape format (little-endian): "BCSTAPE1", then ops, each
 //   u32 opcode, u64 payload bytes, payload
-// with the payloads listed at the Op enum.  An address inside an argument or
-// an op is always written as (u32 allocation id, u64 offset).
+// with the opcodes and payloads listed in tape_format.h.  An address inside
+// an argument or an op is always written as (u32 allocation id, u64 offset).
 #include <cuda_runtime.h>
+
+#include "tape_format.h"
 
 #include <algorithm>
 #include <cstdint>
@@ -21,28 +23,13 @@
 #include <string>
 #include <vector>
 
+using namespace bcs_tape;
+
 namespace {
 
 constexpr uint64_t kBase = 0x5EC0000000000000ull;
 constexpr uint64_t kAlign = 256;
 
-enum Op : uint32_t {
-    kAlloc = 1,        // u32 id, u64 bytes
-    kFree = 2,         // u32 id
-    kH2D = 3,          // u32 id, u64 off, u64 bytes, data
-    kD2D = 4,          // u32 dst id, u64 dst off, u32 src id, u64 src off, u64 bytes
-    kMemset = 5,       // u32 id, u64 off, i32 value, u64 bytes
-    kStream = 6,       // u32 stream id (1, 2, ...; 0 is the legacy default stream)
-    kLaunch = 7,       // u64 kernel address, u32 grid[3], u32 block[3], u32 shmem, u32 stream,
-                       // u32 params, per param: u32 size, u32 relocations, bytes,
-                       // per relocation: u32 offset in the param, u32 id, u64 off
-    kSort = 8,         // u32 keys id, u64 off, u32 values id, u64 off, u32 n
-    kSyncDevice = 9,   // -
-    kSyncStream = 10,  // u32 stream id
-    kMark = 11,        // label bytes
-    kBuffer = 12,      // u32 id, u64 off, u64 bytes, name bytes
-    kFixLastCell = 13, // u32 keys id, u64 off, u32 starts id, u64 off, u32 ends id, u64 off, u32 n
-};
 
 struct Alloc {
     uint32_t id;
@@ -205,6 +192,16 @@ cudaError_t cudaPeekAtLastError(void) { return cudaSuccess; }
 const char* cudaGetErrorString(cudaError_t) { return "tape recorder"; }
 }
 
+void bcs_tape_thunk(const void* fn, void (*thunk)(const void*, unsigned char* const*)) {
+    static std::vector<const void*> seen;
+    if (std::find(seen.begin(), seen.end(), fn) != seen.end()) return;
+    seen.push_back(fn);
+    std::vector<unsigned char> b;
+    put(b, reinterpret_cast<uint64_t>(fn));
+    put(b, reinterpret_cast<uint64_t>(thunk));
+    emit(kThunk, b);
+}
+
 void bcs_tape_begin_launch(const void* fn, dim3 grid, dim3 block, size_t shmem, cudaStream_t stream, int params) {
     Tape& t = tape();
     if (t.params_left) fail("nested launch");
@@ -285,4 +282,124 @@ int bcs_tape_write(const char* path) {
     std::fwrite("BCSTAPE1", 1, 8, f);
     std::fwrite(t.bytes.data(), 1, t.bytes.size(), f);
     return std::fclose(f) == 0 ? 0 : 1;
+}
+
+// ---------------------------------------------------------------------------
+// CPU replay of a tape by the executable that recorded it (the kernel and
+// thunk addresses on the tape are this executable's): allocations are host
+// memory, every launch runs its grid serially through the kernel's thunk,
+// the key sort is std::stable_sort.  This checks, without a GPU, that a tape
+// holds everything the reference's kernels need, and that its arguments and
+// relocations reproduce the reference's own host-driven run.
+#include <map>
+#include <numeric>
+
+int bcs_tape_replay_cpu(const char* tape_path, const char* state_path, int frames, const char* out_path) {
+    try {
+        const std::vector<Op> ops = read(tape_path);
+        std::vector<const Op*> setup, frame;
+        segments(ops, setup, frame);
+        std::vector<std::vector<unsigned char>> mem;
+        std::map<uint64_t, uint64_t> thunk;
+        std::map<std::string, std::pair<float*, uint64_t>> buffers;
+        auto at = [&](const Addr& a, uint64_t bytes) -> unsigned char* {
+            if (a.id >= mem.size() || a.off + bytes > mem[a.id].size()) throw std::runtime_error("op outside memory");
+            return mem[a.id].data() + a.off;
+        };
+        auto run = [&](const Op& op) {
+            switch (op.code) {
+                case kAlloc: mem.emplace_back(op.bytes, 0); break;
+                case kH2D: std::memcpy(at(op.a, op.bytes), op.data.data(), op.bytes); break;
+                case kD2D: std::memmove(at(op.a, op.bytes), at(op.b, op.bytes), op.bytes); break;
+                case kMemset: std::memset(at(op.a, op.bytes), op.value, op.bytes); break;
+                case kThunk: thunk[op.kernel] = op.thunk; break;
+                case kBuffer:
+                    buffers[op.text] = {reinterpret_cast<float*>(at(op.a, op.bytes)), op.bytes};
+                    break;
+                case kSort: {
+                    int* k = reinterpret_cast<int*>(at(op.a, 4ull * op.n));
+                    int* v = reinterpret_cast<int*>(at(op.b, 4ull * op.n));
+                    std::vector<uint32_t> idx(op.n);
+                    std::iota(idx.begin(), idx.end(), 0u);
+                    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) { return k[x] < k[y]; });
+                    std::vector<int> ks(op.n), vs(op.n);
+                    for (uint32_t i = 0; i < op.n; ++i) { ks[i] = k[idx[i]]; vs[i] = v[idx[i]]; }
+                    std::memcpy(k, ks.data(), 4ull * op.n);
+                    std::memcpy(v, vs.data(), 4ull * op.n);
+                    break;
+                }
+                case kFixLastCell: {
+                    const int* k = reinterpret_cast<const int*>(at(op.a, 4ull * op.n));
+                    if (op.n == 0) break;
+                    const int last = k[op.n - 1];
+                    int first = (int)op.n - 1;
+                    while (first > 0 && k[first - 1] == last) --first;
+                    *reinterpret_cast<int*>(at(Addr{op.b.id, op.b.off + 4ull * last}, 4)) = first;
+                    *reinterpret_cast<int*>(at(Addr{op.c.id, op.c.off + 4ull * last}, 4)) = (int)op.n - 1;
+                    break;
+                }
+                case kLaunch: {
+                    auto t = thunk.find(op.kernel);
+                    if (t == thunk.end()) throw std::runtime_error("launch without a thunk");
+                    std::vector<std::vector<unsigned char>> args(op.params.size());
+                    std::vector<unsigned char*> ptrs(op.params.size());
+                    for (size_t i = 0; i < op.params.size(); ++i) {
+                        args[i] = op.params[i].bytes;
+                        for (const Reloc& r : op.params[i].relocs) {
+                            const uint64_t v = reinterpret_cast<uint64_t>(at(Addr{r.id, 0}, r.off) + r.off);
+                            std::memcpy(&args[i][r.offset], &v, 8);
+                        }
+                        ptrs[i] = args[i].data();
+                    }
+                    auto call = reinterpret_cast<void (*)(const void*, unsigned char* const*)>(t->second);
+                    gridDim = dim3(op.grid[0], op.grid[1], op.grid[2]);
+                    blockDim = dim3(op.block[0], op.block[1], op.block[2]);
+                    for (unsigned bz = 0; bz < op.grid[2]; ++bz)
+                        for (unsigned by = 0; by < op.grid[1]; ++by)
+                            for (unsigned bx = 0; bx < op.grid[0]; ++bx)
+                                for (unsigned tz = 0; tz < op.block[2]; ++tz)
+                                    for (unsigned ty = 0; ty < op.block[1]; ++ty)
+                                        for (unsigned tx = 0; tx < op.block[0]; ++tx) {
+                                            blockIdx = uint3{bx, by, bz};
+                                            threadIdx = uint3{tx, ty, tz};
+                                            call(reinterpret_cast<const void*>(op.kernel), ptrs.data());
+                                        }
+                    break;
+                }
+                default: break;   // frees, streams, synchronisation, marks
+            }
+        };
+        for (const Op& op : ops)
+            if (op.code == kThunk) run(op);
+        for (const Op* op : setup) run(*op);
+        const auto& px = buffers.at("positions.x");
+        const size_t n = px.second / 4;
+        const char* names[3] = {"positions", "velocities", "forces"};
+        if (std::strcmp(state_path, "-") != 0) {
+            std::vector<float> s(6 * n);
+            FILE* f = std::fopen(state_path, "rb");
+            if (!f || std::fread(s.data(), 4, s.size(), f) != s.size()) throw std::runtime_error("bad state file");
+            std::fclose(f);
+            for (int q = 0; q < 2; ++q)
+                for (int c = 0; c < 3; ++c) {
+                    float* b = buffers.at(std::string(names[q]) + "." + "xyz"[c]).first;
+                    for (size_t i = 0; i < n; ++i) b[i] = s[3 * n * q + 3 * i + c];
+                }
+        }
+        for (int f = 0; f < frames; ++f)
+            for (const Op* op : frame) run(*op);
+        std::vector<float> out(9 * n);
+        for (int q = 0; q < 3; ++q)
+            for (int c = 0; c < 3; ++c) {
+                const float* b = buffers.at(std::string(names[q]) + "." + "xyz"[c]).first;
+                for (size_t i = 0; i < n; ++i) out[3 * n * q + 3 * i + c] = b[i];
+            }
+        FILE* o = std::fopen(out_path, "wb");
+        if (!o || std::fwrite(out.data(), 4, out.size(), o) != out.size()) throw std::runtime_error("cannot write");
+        std::fclose(o);
+        return 0;
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "tape CPU replay: %s\n", e.what());
+        return 2;
+    }
 }

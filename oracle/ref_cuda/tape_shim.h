@@ -51,6 +51,7 @@ extern dim3 gridDim;
 }
 
 // tape_runtime.cpp
+void bcs_tape_thunk(const void* fn, void (*thunk)(const void*, unsigned char* const*));
 void bcs_tape_begin_launch(const void* fn, dim3 grid, dim3 block, size_t shmem, cudaStream_t stream, int params);
 void bcs_tape_add_param(const void* bytes, size_t size);
 void bcs_tape_end_launch();
@@ -72,9 +73,21 @@ inline void bcs_tape_param(A&& a) {
     value->~P();
 }
 
+// The recorder's own CPU replay calls a kernel (a plain host function in
+// this build) with the bytes of its arguments through this thunk.
+template <class... P, size_t... I>
+inline void bcs_tape_invoke(void (*f)(P...), unsigned char* const* a, std::index_sequence<I...>) {
+    f(*reinterpret_cast<P*>(a[I])...);
+}
+template <class... P>
+void bcs_tape_call(const void* fn, unsigned char* const* a) {
+    bcs_tape_invoke(reinterpret_cast<void (*)(P...)>(const_cast<void*>(fn)), a, std::index_sequence_for<P...>{});
+}
+
 template <class... P, class... A>
 inline void bcs_tape_launch(bcs_dims d, void (*kernel)(P...), A&&... a) {
     static_assert(sizeof...(P) == sizeof...(A), "kernel argument count");
+    bcs_tape_thunk(reinterpret_cast<const void*>(kernel), &bcs_tape_call<P...>);
     bcs_tape_begin_launch(reinterpret_cast<const void*>(kernel), d.grid, d.block, d.shmem, d.stream,
                           (int)sizeof...(P));
     (bcs_tape_param<P>(std::forward<A>(a)), ...);

@@ -156,3 +156,38 @@ def test_replay_source_compiles_for_sm_103a(tmp_path):
                         os.path.join(REPO, "oracle", "ref_cuda", "replay.cu"), "-L/usr/local/cuda/lib64/stubs",
                         "-lcuda"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_cpu_replay_of_the_pinned_tape_is_the_pin(built, tmp_path):
+    """The recorder runs its own tape on the CPU (every launch through its
+    recorded argument bytes and relocations, the sort op, the Q5 ops, the
+    injected state): one frame and five frames equal the CPU pin of the same
+    scene bit for bit (tests/golden/ref_pin_icosphere_cfg1.npz).  The GPU
+    replay issues the same bytes with cuLaunchKernel."""
+    import numpy as np
+    g = np.load(os.path.join(REPO, "tests", "golden", "ref_pin_icosphere_cfg1.npz"))
+    state = tmp_path / "state.bin"
+    np.concatenate([g["init_positions"].ravel(), g["init_velocities"].ravel()]).astype(np.float32).tofile(state)
+    for frames, tag in ((1, "frame1"), (int(g["steps"]), "frameN")):
+        out = tmp_path / f"out{frames}.bin"
+        r = subprocess.run([os.path.join(built, "tape_recorder"), "--replay-cpu", os.path.join(built, "pinned.tape"),
+                            str(state), str(frames), str(out)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-2000:]
+        o = np.fromfile(out, np.float32).reshape(3, -1, 3)
+        for q, name in enumerate(("positions", "velocities", "forces")):
+            np.testing.assert_array_equal(o[q], g[f"{tag}_{name}"], err_msg=f"{tag} {name}")
+
+
+def test_cpu_replay_of_the_reference_tape_runs(built, tmp_path):
+    """The timing tape (the reference's calls without the pin's Q5 ops) runs
+    to the end with finite state."""
+    import numpy as np
+    g = np.load(os.path.join(REPO, "tests", "golden", "ref_pin_icosphere_cfg1.npz"))
+    state = tmp_path / "state.bin"
+    np.concatenate([g["init_positions"].ravel(), g["init_velocities"].ravel()]).astype(np.float32).tofile(state)
+    out = tmp_path / "out.bin"
+    r = subprocess.run([os.path.join(built, "tape_recorder"), "--replay-cpu", os.path.join(built, "reference.tape"),
+                        str(state), "3", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    o = np.fromfile(out, np.float32)
+    assert o.size == 9 * 16 * 42 and np.isfinite(o).all()

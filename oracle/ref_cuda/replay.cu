@@ -119,23 +119,26 @@ struct Replay {
         return f;
     }
 
-    // Every check a launch must pass, before the frame that holds it runs.
-    void validate(const Op& op) {
+    // Every check a launch must pass, made for all launches of the tape
+    // before any op runs.  `planned` holds each allocation's size and
+    // `streams_made` the streams created before this launch.
+    void validate(const Op& op, const std::vector<uint64_t>& planned, uint32_t streams_made) {
         CUfunction f = function(op.kernel);
         for (size_t i = 0; i < op.params.size(); ++i) {
             size_t off = 0, sz = 0;
             check(cuFuncGetParamInfo(f, i, &off, &sz), "cuFuncGetParamInfo");
             if (sz != op.params[i].bytes.size()) die("recorded argument size differs from the kernel's parameter");
             for (const Reloc& r : op.params[i].relocs) {
-                if (r.offset + 8 > op.params[i].bytes.size()) die("relocation outside its argument");
-                if (r.id >= size.size() || r.off > size[r.id]) die("relocated pointer outside its allocation");
+                if ((uint64_t)r.offset + 8 > op.params[i].bytes.size()) die("relocation outside its argument");
+                if (r.id >= planned.size() || r.off > planned[r.id]) die("relocated pointer outside its allocation");
             }
         }
         size_t off = 0, sz = 0;
         if (cuFuncGetParamInfo(f, op.params.size(), &off, &sz) == CUDA_SUCCESS) die("kernel takes more parameters");
         const uint64_t threads = (uint64_t)op.block[0] * op.block[1] * op.block[2];
         if (threads == 0 || threads > 1024 || !op.grid[0] || !op.grid[1] || !op.grid[2]) die("illegal launch shape");
-        if (op.stream >= streams.size()) die("launch on a stream that was not created");
+        if (op.shmem != 0) die("dynamic shared memory on a recorded launch");
+        if (op.stream > streams_made) die("launch on a stream that was not created");
     }
 
     void launch(const Op& op) {
@@ -158,7 +161,7 @@ struct Replay {
 
     void run(const Op& op) {
         switch (op.code) {
-            case 1: {
+            case kAlloc: {
                 if (op.id != base.size()) die("allocations out of order");
                 void* p = nullptr;
                 check(cudaMalloc(&p, op.bytes), "cudaMalloc");
@@ -167,30 +170,30 @@ struct Replay {
                 size.push_back(op.bytes);
                 break;
             }
-            case 2: break;   // freed at exit
-            case 3: check(cudaMemcpy(at(op.a, op.bytes), op.data.data(), op.bytes, cudaMemcpyHostToDevice), "h2d"); break;
-            case 4: check(cudaMemcpy(at(op.a, op.bytes), at(op.b, op.bytes), op.bytes, cudaMemcpyDeviceToDevice), "d2d"); break;
-            case 5: check(cudaMemset(at(op.a, op.bytes), op.value, op.bytes), "memset"); break;
-            case 6: {
+            case kFree: break;   // freed at exit
+            case kH2D: check(cudaMemcpy(at(op.a, op.bytes), op.data.data(), op.bytes, cudaMemcpyHostToDevice), "h2d"); break;
+            case kD2D: check(cudaMemcpy(at(op.a, op.bytes), at(op.b, op.bytes), op.bytes, cudaMemcpyDeviceToDevice), "d2d"); break;
+            case kMemset: check(cudaMemset(at(op.a, op.bytes), op.value, op.bytes), "memset"); break;
+            case kStream: {
                 if (op.stream != streams.size()) die("streams out of order");
                 cudaStream_t s;
                 check(cudaStreamCreate(&s), "cudaStreamCreate");   // as the reference creates them
                 streams.push_back(s);
                 break;
             }
-            case 7: launch(op); break;
-            case 8: {
+            case kLaunch: launch(op); break;
+            case kSort: {
                 int* k = reinterpret_cast<int*>(at(op.a, sizeof(int) * (uint64_t)op.n));
                 int* v = reinterpret_cast<int*>(at(op.b, sizeof(int) * (uint64_t)op.n));
                 thrust::stable_sort_by_key(thrust::device, k, k + op.n, v);   // uniform_grid.cu:144-147
                 break;
             }
-            case 9: check(cudaDeviceSynchronize(), "cudaDeviceSynchronize"); break;
-            case 10: check(cudaStreamSynchronize(streams.at(op.stream)), "cudaStreamSynchronize"); break;
-            case 11: break;
-            case 12: buffers[op.text] = {at(op.a, op.bytes), op.bytes}; break;
-            case 14: break;   // host-side call thunks of the recorder's own CPU replay
-            case 13: {
+            case kSyncDevice: check(cudaDeviceSynchronize(), "cudaDeviceSynchronize"); break;
+            case kSyncStream: check(cudaStreamSynchronize(streams.at(op.stream)), "cudaStreamSynchronize"); break;
+            case kMark: break;
+            case kBuffer: buffers[op.text] = {at(op.a, op.bytes), op.bytes}; break;
+            case kThunk: break;   // host-side call thunks of the recorder's own CPU replay
+            case kFixLastCell: {
                 const int* k = reinterpret_cast<const int*>(at(op.a, sizeof(int) * (uint64_t)op.n));
                 int* s = reinterpret_cast<int*>(at(op.b, 0));
                 int* e = reinterpret_cast<int*>(at(op.c, 0));
@@ -243,10 +246,25 @@ int main(int argc, char** argv) {
     check(cudaFree(nullptr), "context");
     check(cuModuleLoad(&R.module, (dir + "/kernels.cubin").c_str()), "cuModuleLoad");
 
+    {
+        // every launch of the construction and of the frame, checked against
+        // the allocations and streams made before it, before anything runs
+        std::vector<uint64_t> planned;
+        uint32_t streams_made = 0;
+        for (const std::vector<const Op*>* seg : {&setup, &frame})
+            for (const Op* op : *seg) {
+                if (op->code == kAlloc) {
+                    if (op->id != planned.size()) die("allocations out of order");
+                    planned.push_back(op->bytes);
+                } else if (op->code == kStream) {
+                    streams_made = std::max(streams_made, op->stream);
+                } else if (op->code == kLaunch) {
+                    R.validate(*op, planned, streams_made);
+                }
+            }
+    }
     for (const Op* op : setup) R.run(*op);
     check(cudaDeviceSynchronize(), "construction");
-    for (const Op* op : frame)
-        if (op->code == 7) R.validate(*op);
 
     auto [px, n4] = R.buffer("positions.x");
     const size_t n = n4 / sizeof(float);

@@ -1,0 +1,62 @@
+"""The reference's own kernels replayed on the GPU from their cubin and launch
+tape (oracle/ref_cuda/replay.cu), against the CPU pin of the same sources.
+
+The replay is built on the GPU machine from oracle/ref_cuda/replay.cu into
+oracle/_ref/ref_cuda_replay; these tests skip while it or the recorded
+artifacts are absent.  Tolerances as the oracle's pin tests: nvcc contracts
+multiply-adds that the pin (g++ -ffp-contract=off) does not, so positions,
+velocities and forces agree to 1e-5 relative after one frame and 1e-4 after
+five.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REPLAY = os.path.join(REPO, "oracle", "_ref", "ref_cuda_replay")
+SMALL = os.path.join(REPO, "oracle", "_ref", "refcuda_icosphere_cfg1")
+
+
+@pytest.fixture(scope="module")
+def replay():
+    if not (os.path.exists(REPLAY) and os.path.exists(os.path.join(SMALL, "kernels.cubin"))):
+        pytest.skip("the reference's replay is not built here")
+    return REPLAY
+
+
+def rel_err(g, o):
+    o = np.asarray(o, np.float64)
+    scale = np.abs(o) + np.sqrt(np.mean(o * o)) + 1e-30
+    return float(np.max(np.abs(np.asarray(g, np.float64) - o) / scale))
+
+
+def run(replay, tmp_path, mode, frames, g):
+    state = tmp_path / "state.bin"
+    np.concatenate([g["init_positions"].ravel(), g["init_velocities"].ravel()]).astype(np.float32).tofile(state)
+    out = tmp_path / f"{mode}{frames}.bin"
+    r = subprocess.run([replay, SMALL, mode, str(state), str(frames), str(out)], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return np.fromfile(out, np.float32).reshape(3, -1, 3), r.stdout
+
+
+def test_pinned_replay_matches_the_pin(replay, tmp_path):
+    g = np.load(os.path.join(REPO, "tests", "golden", "ref_pin_icosphere_cfg1.npz"))
+    for frames, tag, tol in ((1, "frame1", 1e-5), (int(g["steps"]), "frameN", 1e-4)):
+        o, _ = run(replay, tmp_path, "pinned", frames, g)
+        for q, name in enumerate(("positions", "velocities", "forces")):
+            e = rel_err(o[q], g[f"{tag}_{name}"])
+            assert e <= tol, f"{tag} {name}: relative error {e:.3e}"
+
+
+def test_reference_replay_runs_every_frame(replay, tmp_path):
+    import json
+    g = np.load(os.path.join(REPO, "tests", "golden", "ref_pin_icosphere_cfg1.npz"))
+    o, out = run(replay, tmp_path, "reference", 20, g)
+    line = json.loads(out.strip().splitlines()[-1])
+    assert line["frames"] == 20 and line["ms_per_frame"] > 0 and line["launches_per_frame"] == 11
+    assert np.isfinite(o).all()

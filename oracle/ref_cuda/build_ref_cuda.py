@@ -26,6 +26,7 @@ compiled with g++ against tape_shim.h: every <<<>>> launch and the one
 thrust::stable_sort_by_key become records instead of work.
 
   python oracle/ref_cuda/build_ref_cuda.py [scene ...]
+  python oracle/ref_cuda/build_ref_cuda.py --replay    # the GPU replay, on the GPU machine
 """
 from __future__ import annotations
 
@@ -260,6 +261,18 @@ def build(tag: str, scene, frames: int = 2, force: bool = False) -> str:
     return out
 
 
+def build_replay(out: str | None = None) -> str:
+    """The GPU replay (replay.cu, our own source) with this machine's nvcc;
+    built where it runs, since host code does not travel."""
+    exe = out or os.path.join(OUT, "ref_cuda_replay")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    stubs = "/usr/local/cuda/lib64/stubs"
+    _run(["nvcc", "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe,
+          os.path.join(HERE, "replay.cu")] + (["-L" + stubs] if os.path.isdir(stubs) else []) + ["-lcuda"],
+         "nvcc replay.cu")
+    return exe
+
+
 def build_all(tags=None) -> list:
     """Every scene (or the named ones); nothing when the reference sources
     are absent."""
@@ -271,5 +284,8 @@ def build_all(tags=None) -> list:
 
 
 if __name__ == "__main__":
-    for d in build_all(sys.argv[1:] or None):
-        print("built", d)
+    if sys.argv[1:] == ["--replay"]:
+        print("built", build_replay())
+    else:
+        for d in build_all(sys.argv[1:] or None):
+            print("built", d)

@@ -150,12 +150,9 @@ def test_state_buffers_are_marked(built):
             assert bufs[f"{q}.{c}"] == 4 * 16 * 42
 
 
-def test_replay_source_compiles_for_sm_103a(tmp_path):
-    out = tmp_path / "ref_cuda_replay"
-    r = subprocess.run(["nvcc", "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-o", str(out),
-                        os.path.join(REPO, "oracle", "ref_cuda", "replay.cu"), "-L/usr/local/cuda/lib64/stubs",
-                        "-lcuda"], capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-2000:]
+def test_replay_builds_for_sm_103a(tmp_path):
+    exe = B.build_replay(str(tmp_path / "ref_cuda_replay"))
+    assert os.path.getsize(exe) > 0
 
 
 def test_cpu_replay_of_the_pinned_tape_is_the_pin(built, tmp_path):

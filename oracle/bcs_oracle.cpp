@@ -30,7 +30,8 @@
 //   refresh_triangle_centers; Q10 normalize(0) = 0; Q11 respawn offsets from
 //   Philox4x32-10 keyed by (seed, cell, step), one draw per cell; Q12 the
 //   block-sync vein-end rule (ending spheres + thresholds) for every type;
-//   Q13 grid "none" is a brute-force scan with the same rules as "uniform".
+//   Q13 grid "none" is a brute-force scan with the same rules as "uniform";
+//   Q15 (reference order only) a radius index before the table reads 0.
 #include "../include/bcs.h"
 
 #include <algorithm>
@@ -407,8 +408,11 @@ void particle_collisions(Sim& s) {
         const TypeLayout& launch = s.types[s.type_of_particle[slot]];
         auto radius_of = [&](int particle) -> real {
             if (!s.reference_order) return particle_radius(s, particle);
+            // Q15: a particle of an earlier type gives a negative remainder,
+            // an index before the radius table (read as 0 here, as in the
+            // zero-padded table the reference's replay gets)
             int m = launch.model_start + (particle - launch.particle_start) % launch.pic;
-            return s.model_radius[m];
+            return m < 0 ? 0.0 : s.model_radius[m];
         };
         const real r1 = radius_of(pid);
         V3 acc{0, 0, 0};

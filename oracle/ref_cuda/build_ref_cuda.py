@@ -14,7 +14,9 @@ oracle/_ref/refcuda_<scene>/:
   pinned.tape     the same plus the Q5 clears and last-cell ranges the CPU pin
                   applies (parity against the pin)
   kernels.txt     recorder address -> cubin entry, one line per kernel on a tape
-  layout.json     counts of the folded scene
+  layout.json     counts of the scene and the folded type order (the
+                  reference merges and sorts the user's types, so a state
+                  handed to the replay follows reference_order())
   limits.txt      the reference's grid box and dt (the replay's guard)
   tape_recorder   the recorder (host code of this machine); it also replays
                   its tapes on the CPU (--replay-cpu), which the tests compare
@@ -74,9 +76,10 @@ def available() -> bool:
 
 
 def scenes():
-    """(tag, scene) pairs: the pinned small scene and the 4.2M-particle
-    bifurcation of the benchmark with the reference's physics (the axial flow
-    segments are this project's own and are dropped; useBloodFlow = 0)."""
+    """(tag, scene) pairs: the pinned small scene, a small scene with both
+    of the benchmark's cell models, and the 4.2M-particle bifurcation of the
+    benchmark with the reference's physics (the axial flow segments are this
+    project's own and are dropped; useBloodFlow = 0)."""
     q = bcs.default_params()
     q.use_blood_flow = 0
     q.dt = 1e-3
@@ -91,11 +94,49 @@ def scenes():
                     np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32))
     yield "icosphere_cfg1", small
 
+    def two_types():
+        # both cell models of the benchmark, a few cells each, with the
+        # bounding-sphere radii the reference computes (its config has no
+        # per-particle collision radius)
+        sc = S.bifurcation_scene(cells_per_type=12, seed=7)
+        sc.params.use_blood_flow = 0
+        sc.flow_segments = []
+        for t in sc.types:
+            t.collision_radius = None
+        return sc
+    yield "two_types", two_types
+
     def bifurcation():
         sc = S.bifurcation_scene(cells_per_type=20588, seed=2024)
         sc.params.use_blood_flow = 0
         return sc
     yield "bifurcation_4.2M", bifurcation
+
+
+def tape_layout(tape_path: str) -> list:
+    """(particles in cell, count, first particle) of every type in the
+    reference's folded order, as the recorder marked it."""
+    import tape as T
+    for op in T.read(tape_path):
+        if op["op"] == "mark" and op["label"].startswith("layout:"):
+            return [tuple(int(v) for v in t.split(",")) for t in op["label"][7:].split(";") if t]
+    raise ValueError(f"{tape_path} marks no layout")
+
+
+def reference_order(scene, layout) -> np.ndarray:
+    """Scene particle index of each particle in the reference's order: its
+    folded types take the scene's types of the same model size and count,
+    first unused first."""
+    starts = np.cumsum([0] + [t.count * len(t.vertices) for t in scene.types])
+    used, parts = set(), []
+    for pic, count, _ in layout:
+        k = next((i for i, t in enumerate(scene.types)
+                  if i not in used and len(t.vertices) == pic and t.count == count), None)
+        if k is None:
+            raise ValueError(f"no scene type of {count} cells x {pic} particles")
+        used.add(k)
+        parts.append(np.arange(starts[k], starts[k + 1]))
+    return np.concatenate(parts)
 
 
 def _scratch(scene, tape: bool) -> str:
@@ -246,7 +287,8 @@ def build(tag: str, scene, frames: int = 2, force: bool = False) -> str:
     with open(os.path.join(out, "layout.json"), "w") as f:
         json.dump({"scene": tag, "particles": int(sum(t.count * len(t.vertices) for t in scene.types)),
                    "cells": int(sum(t.count for t in scene.types)), "vein_vertices": int(len(scene.vein_positions)),
-                   "triangles": int(len(scene.vein_indices)), "frames_recorded": frames}, f)
+                   "triangles": int(len(scene.vein_indices)), "frames_recorded": frames,
+                   "types": tape_layout(os.path.join(out, "reference.tape"))}, f)
     # the reference's grid box (vein_factory.hpp:21-86) and dt, for the
     # replay's guard against particles leaving it
     p = scene.params

@@ -9,8 +9,9 @@
 // What the driver restates, as the CPU pin's driver does: the construction
 // of src/main.cu:122-138 and SimulationController's constructor
 // (simulation_controller.cu:27-54: one stream per cell type, the bounding
-// spheres of generateBoundingSpheres, :93-153) without the curand start (the
-// replay injects a seeded state into the buffers marked here), and the frame
+// spheres of generateBoundingSpheres, :93-153, in a zero-padded table) without
+// the curand start (the replay injects a seeded state into the buffers marked
+// here), and the frame
 // of src/main.cu:175-208: calculateGrid for both grids, calculateNextFrame
 // (simulation_controller.cu:246-294) and propagateAll (:315-323), with the
 // reference's device synchronisations, without HandleVeinEnd (the recorded
@@ -80,8 +81,15 @@ int main(int argc, char** argv) {
     // ---- SimulationController's constructor without the curand start
     std::array<cudaStream_t, bloodCellTypeCount> streams{};
     for (auto& s : streams) cudaStreamCreate(&s);
-    float* spheres_dev = nullptr;
-    cudaMalloc(reinterpret_cast<void**>(&spheres_dev), sizeof(float) * particleDistinctCellsCount);
+    // The bounding-sphere table, with particleDistinctCellsCount zeros in
+    // front: the collision kernel indexes it with the launching type's model
+    // start and size for the particle of any sorted slot in the type's range
+    // (particle_collisions.cuh:124), which for a particle of an earlier type
+    // is a negative remainder, up to one model size before the table (Q15).
+    // The padding keeps those reads inside the allocation.
+    float* spheres_mem = nullptr;
+    cudaMalloc(reinterpret_cast<void**>(&spheres_mem), sizeof(float) * 2 * particleDistinctCellsCount);
+    float* spheres_dev = spheres_mem + particleDistinctCellsCount;
     {
         // generateBoundingSpheres (simulation_controller.cu:93-153), restated
         // on the compile-time models
@@ -131,6 +139,18 @@ int main(int argc, char** argv) {
     mark_vec3("vein_velocities", triangles.velocities[0], VeinTriangles::vertexCount);
     bcs_tape_mark_buffer("particle_keys", particleGrid.gridCellIds[0], sizeof(int) * (size_t)particleCount);
     bcs_tape_mark_buffer("particle_ids", particleGrid.particleIds[0], sizeof(int) * (size_t)particleCount);
+    // the folded type order (blood_cell_factory.hpp:117-162 merges and sorts
+    // the user's types), which the injected state must follow:
+    // "layout:pic,count,first particle;..."
+    {
+        std::string layout = "layout:";
+        mp_for_each<mp_iota_c<bloodCellTypeCount>>([&](auto i) {
+            using Def = mp_at_c<BloodCellList, i>;
+            layout += std::to_string(Def::particlesInCell) + "," + std::to_string(Def::count) + "," +
+                      std::to_string(particleStarts[i]) + ";";
+        });
+        bcs_tape_mark(layout.c_str());
+    }
     bcs_tape_mark("setup_end");
 
     CudaThreads veinTrianglesThreads(triangleCount);

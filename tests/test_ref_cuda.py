@@ -188,3 +188,51 @@ def test_cpu_replay_of_the_reference_tape_runs(built, tmp_path):
     assert r.returncode == 0, r.stderr[-2000:]
     o = np.fromfile(out, np.float32)
     assert o.size == 9 * 16 * 42 and np.isfinite(o).all()
+
+
+def _replay_cpu(d, mode, scene, frames, tmp_path):
+    """CPU replay of a scene's tape from its own state, returned in the
+    scene's particle order."""
+    import numpy as np
+    order = B.reference_order(scene, B.tape_layout(os.path.join(d, mode + ".tape")))
+    state = tmp_path / "state.bin"
+    np.concatenate([scene.positions[order].ravel(), scene.velocities[order].ravel()]).astype(np.float32).tofile(state)
+    out = tmp_path / "out.bin"
+    r = subprocess.run([os.path.join(d, "tape_recorder"), "--replay-cpu", os.path.join(d, mode + ".tape"), str(state),
+                        str(frames), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = np.fromfile(out, np.float32).reshape(3, -1, 3)
+    back = np.empty_like(got)
+    back[:, order] = got
+    return back
+
+
+def test_two_models_against_the_oracle(tmp_path):
+    """Both cell models of the benchmark (42 and 162 particles).  The
+    reference folds them into its own type order (162 first), so the state
+    goes in through reference_order().  Its kernels, replayed on the CPU from
+    the pinned tape, agree with the FP64 oracle in reference order (the Q1
+    radius of the launching type, the Q3 serial force reads): 1e-5 relative
+    after one frame; after five, positions to 1e-6 and velocities and forces
+    to 5e-4 (FP32 against FP64 through the contact force, which amplifies
+    relative velocity, Q14; measured 1.2e-4)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    tag, make = next((t, s) for t, s in B.scenes() if t == "two_types")
+    d = B.build(tag, make)
+    scene = make()
+    layout = B.tape_layout(os.path.join(d, "pinned.tape"))
+    assert [(p, c) for p, c, _ in layout] == [(162, 12), (42, 12)]
+
+    def rel(a, b):
+        b = np.asarray(b, np.float64)
+        return float(np.max(np.abs(np.asarray(a, np.float64) - b) / (np.abs(b) + np.sqrt(np.mean(b * b)) + 1e-30)))
+    for frames, tols in ((1, (1e-5, 1e-5, 1e-5)), (5, (1e-6, 5e-4, 5e-4))):
+        got = _replay_cpu(d, "pinned", scene, frames, tmp_path)
+        o = O.OracleSim(scene)
+        o.set_reference_order()
+        o.step(frames)
+        for q, (name, want, tol) in enumerate(zip(("positions", "velocities", "forces"), o.get_particles(), tols)):
+            e = rel(got[q], want)
+            assert e <= tol, f"{frames} frames, {name}: relative error {e:.3e}"

@@ -60,3 +60,35 @@ def test_reference_replay_runs_every_frame(replay, tmp_path):
     line = json.loads(out.strip().splitlines()[-1])
     assert line["frames"] == 20 and line["ms_per_frame"] > 0 and line["launches_per_frame"] == 11
     assert np.isfinite(o).all()
+
+
+def test_two_models_against_the_oracle(replay, tmp_path):
+    """Both of the benchmark's cell models on the GPU, the state in the
+    reference's folded type order, against the FP64 oracle in reference order
+    after one frame (1e-5 relative, as on the CPU)."""
+    import sys
+    sys.path.insert(0, os.path.join(REPO, "oracle", "ref_cuda"))
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import build_ref_cuda as B
+    import oracle as O
+    d = os.path.join(REPO, "oracle", "_ref", "refcuda_two_types")
+    if not os.path.exists(os.path.join(d, "kernels.cubin")):
+        pytest.skip("the two-model tape is not built here")
+    scene = next(s for t, s in B.scenes() if t == "two_types")()
+    with open(os.path.join(d, "layout.json")) as f:
+        import json
+        order = B.reference_order(scene, [tuple(t) for t in json.load(f)["types"]])
+    state = tmp_path / "state.bin"
+    np.concatenate([scene.positions[order].ravel(), scene.velocities[order].ravel()]).astype(np.float32).tofile(state)
+    out = tmp_path / "out.bin"
+    r = subprocess.run([replay, d, "pinned", str(state), "1", str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = np.fromfile(out, np.float32).reshape(3, -1, 3)
+    back = np.empty_like(got)
+    back[:, order] = got
+    o = O.OracleSim(scene)
+    o.set_reference_order()
+    o.step(1)
+    for q, (name, want) in enumerate(zip(("positions", "velocities", "forces"), o.get_particles())):
+        e = rel_err(back[q], want)
+        assert e <= 1e-5, f"{name}: relative error {e:.3e}"

@@ -1,7 +1,7 @@
 """Recipe: the reference's own CUDA kernels for sm_103a plus the launch tape of
-its host code, so that a GPU machine which cannot build the reference (its
-sources do not reach it, and host code built here does not run there) can
-still run the reference's kernels.  Test infrastructure: it reads the
+its host code, so that the reference's kernels can run on a machine that
+cannot build the reference itself (without its sources, or of another
+architecture than the one that recorded the tape).  Test infrastructure: it reads the
 reference's sources (default /root/reference, override with BCS_REFERENCE),
 works on scratch copies under /tmp and writes only into
 oracle/_ref/refcuda_<scene>/:
@@ -28,7 +28,7 @@ compiled with g++ against tape_shim.h: every <<<>>> launch and the one
 thrust::stable_sort_by_key become records instead of work.
 
   python oracle/ref_cuda/build_ref_cuda.py [scene ...]
-  python oracle/ref_cuda/build_ref_cuda.py --replay    # the GPU replay, on the GPU machine
+  python oracle/ref_cuda/build_ref_cuda.py --replay    # the GPU replay, where it runs
 """
 from __future__ import annotations
 

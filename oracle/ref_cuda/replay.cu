@@ -1,6 +1,6 @@
 // replay.cu — runs the reference's own CUDA kernels from a cubin and a launch
-// tape (test infrastructure: the reference's CUDA build as a baseline on a
-// GPU machine that cannot compile the reference; see build_ref_cuda.py).
+// tape (test infrastructure: the reference's CUDA build as a baseline where
+// the reference itself cannot be compiled; see build_ref_cuda.py).
 //
 // Usage: ref_cuda_replay <dir> <reference|pinned> <state.bin|-> <frames> [<out.bin>]
 //   dir        oracle/_ref/refcuda_<scene>: kernels.cubin, kernels.txt, <mode>.tape

@@ -1,7 +1,7 @@
 """The reference's own kernels replayed on the GPU from their cubin and launch
 tape (oracle/ref_cuda/replay.cu), against the CPU pin of the same sources.
 
-The replay is built on the GPU machine from oracle/ref_cuda/replay.cu into
+The replay is built where it runs, from oracle/ref_cuda/replay.cu into
 oracle/_ref/ref_cuda_replay; these tests skip while it or the recorded
 artifacts are absent.  Tolerances as the oracle's pin tests: nvcc contracts
 multiply-adds that the pin (g++ -ffp-contract=off) does not, so positions,

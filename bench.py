@@ -27,9 +27,16 @@ simulation from the same state after the warm-up frames, with the tuning the
 autotuner picked in the first, so all three follow the same trajectory.
   cpu_baseline  the FP64 oracle (a C++ restatement of the reference step) on
             the host cores, on a bounded sample of the same workload
+  parity    before any timing: the workload's first frame from its initial
+            state against the FP64 oracle (grid bit-exact, largest relative
+            error of x, v, F and of the wall's x, v)
+  reference_cuda  the reference's own CUDA kernels (its sources compiled
+            unmodified, its host code replayed from a launch tape) on the same
+            GPU, the workload's geometry and population, per-frame CUDA events
 
 --impl reference times that CPU implementation alone (the reference has no
-CPU path of its own and its CUDA build cannot be carried to this machine).
+CPU path of its own; its CUDA kernels are timed beside the product through
+the replay of oracle/ref_cuda, reported as reference_cuda).
 Under torchrun each rank advances its own replica (the scene does not shard
 without a halo exchange): value = all ranks' particle-steps / max time.
 """
@@ -222,6 +229,97 @@ def time_oracle(scene, steps_budget_s, warmup=1, max_steps=None, threads=None):
     n = sample.particle_count
     info = {"steps": steps, "particles": n, "seconds": round(dt, 3)}
     return n * steps / dt, info, threads
+
+
+def rel_err(g, o):
+    """max |g - o| / (|o| + rms(o)) elementwise: the parity tests' rule."""
+    o = np.asarray(o, np.float64)
+    scale = np.abs(o) + np.sqrt(np.mean(o * o)) + 1e-30
+    return float(np.max(np.abs(np.asarray(g, np.float64) - o) / scale))
+
+
+def oracle_parity(bcs, scene, threads=None):
+    """The timed workload's first frame on the GPU against the FP64 oracle
+    from the same initial state: particle grid (keys and sorted ids)
+    bit-exact, then the largest elementwise relative error of the particles'
+    x, v, F and the wall's x, v after one frame (the parity tests' bound is
+    1e-5).  The oracle is the checker here, outside every timed region."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    t0 = time.perf_counter()
+    threads = threads or os.cpu_count() or 1
+    o = O.OracleSim(scene, threads=threads)
+    o.calculate_grids()
+    ok, oi, _, _ = o.get_grid(0, dense=False)
+    sim = bcs.Simulation(scene)
+    sim.set_particles(scene.positions, scene.velocities)
+    sim.calculate_grids()
+    k, i, _, _ = sim.get_grid(0, dense=False)
+    sim.close()
+    grid_exact = bool(np.array_equal(k, ok) and np.array_equal(i, oi))
+    del k, i, ok, oi
+    o.close()
+    o = O.OracleSim(scene, threads=threads)
+    o.step(1)
+    sim = bcs.Simulation(scene)
+    sim.set_particles(scene.positions, scene.velocities)
+    sim.step(1)
+    errs = {name: rel_err(a, b) for name, a, b in zip(("position", "velocity", "force"), sim.get_particles(),
+                                                       o.get_particles())}
+    gv, ov = sim.get_vein(), o.get_vein()
+    errs["wall_position"] = rel_err(gv[0], ov[0])
+    # a wall velocity after one frame is dt x (spring forces at rest length,
+    # FP32 rounding noise, + particle impacts): the deformable-wall tests'
+    # rule, relative error <= 1e-4 x max(1, largest |v|)
+    wv = rel_err(gv[1], ov[1])
+    wv_tol = 1e-4 * max(1.0, float(np.abs(ov[1]).max()))
+    sim.close()
+    o.close()
+    return {"frames": 1, "from": "the workload's initial state", "grid_bit_exact": grid_exact,
+            "max_rel_err": errs, "tolerance": 1e-5, "wall_velocity_rel_err": wv, "wall_velocity_tolerance": wv_tol,
+            "within_tolerance": grid_exact and max(errs.values()) <= 1e-5 and wv <= wv_tol,
+            "oracle_threads": threads, "seconds": round(time.perf_counter() - t0, 2)}
+
+
+def reference_cuda(scene, steps, warmup):
+    """The reference's own CUDA kernels on this GPU: its simulation sources
+    compiled unmodified into a cubin and its host code recorded as a launch
+    tape (oracle/ref_cuda), replayed for warm-up + steps frames from the
+    workload's initial state.  The recorded scene has the workload's
+    geometry and population with the reference's own physics (its config
+    has neither per-particle collision radii nor axial flow segments: the
+    bounding-sphere radii and the constant force apply, no vein-end rule).
+    Every frame is timed with its own CUDA events; the replay's box check
+    runs between frames, untimed.  Returns ms per frame over the frames after
+    the warm-up."""
+    d = os.path.join(REPO, "oracle", "_ref", "refcuda_bifurcation_4.2M")
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_cuda_replay")
+    for need in (exe, os.path.join(d, "kernels.cubin"), os.path.join(d, "reference.tape")):
+        if not os.path.exists(need):
+            return {"unavailable": f"{os.path.relpath(need, REPO)} is not built"}
+    sys.path.insert(0, os.path.join(REPO, "oracle", "ref_cuda"))
+    import build_ref_cuda as B
+    order = B.reference_order(scene, B.tape_layout(os.path.join(d, "reference.tape")))
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        state = os.path.join(tmp, "state.bin")
+        np.concatenate([scene.positions[order].ravel(), scene.velocities[order].ravel()]).astype(
+            np.float32).tofile(state)
+        r = subprocess.run([exe, d, "reference", state, str(warmup + steps)], capture_output=True, text=True,
+                           timeout=900)
+    if r.returncode != 0:
+        return {"unavailable": "replay failed: " + r.stderr.strip()[-300:]}
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    timed = line["ms_frames"][warmup:]
+    if not timed:
+        return {"unavailable": f"the replay stopped after {line['frames']} frames (a particle left the guarded box)"}
+    ms = float(np.mean(timed))
+    return {"kind": "reference cubin + launch tape", "ms_per_step": ms,
+            "value": scene.particle_count * 1e3 / ms, "unit": UNIT, "frames": len(timed), "warmup": warmup,
+            "frames_run": line["frames"], "frames_requested": line["frames_requested"],
+            "launches_per_frame": line["launches_per_frame"],
+            "physics": "the workload's geometry and population with the reference's own constants "
+                       "(bounding-sphere radii, constant G, no vein-end rule)"}
 
 
 def run_reference(args):
@@ -576,6 +674,11 @@ def run_ours(args):
                               "config": workload_config(scene, ws)}), flush=True)
         return 0
 
+    # ---- parity of the timed workload's first frame against the FP64 oracle
+    parity = None
+    if rank == 0 and not batched and not args.no_parity:
+        parity = oracle_parity(bcs, scene)
+
     # ---- pass 1: the timed run (graph replay, state resident in HBM)
     sim = fresh()
     n = sim.n
@@ -657,6 +760,13 @@ def run_ours(args):
         except Exception as exc:   # the plain line is still printed
             learned = {"error": f"{type(exc).__name__}: {exc}"}
 
+    ref_cuda = None
+    if rank == 0 and not batched and not args.no_reference_cuda:
+        try:
+            ref_cuda = reference_cuda(scene, args.steps, args.warmup)
+        except Exception as exc:
+            ref_cuda = {"unavailable": f"{type(exc).__name__}: {exc}"}
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline and not batched:
         v, cinfo, threads = time_oracle(scene, args.cpu_budget, warmup=1, max_steps=3)
@@ -689,6 +799,8 @@ def run_ours(args):
             "learned_substep": learned,
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "reference_cuda": ref_cuda,
+            "parity": parity,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -708,6 +820,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=0, help="0 = as many as --steps")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the one-frame oracle check of the workload")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip the replay of the reference's own kernels")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--autotune-frames", type=int, default=3)
     ap.add_argument("--tuning", default="", help="comma-separated bcs_tuning fields instead of the autotuner")

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BCS_ABI_VERSION 2
+#define BCS_ABI_VERSION 3
 
 typedef struct bcs_sim bcs_sim;
 
@@ -38,7 +38,9 @@ typedef enum bcs_status {
     BCS_ERR_CUDA = 2,             /* a CUDA runtime call failed             */
     BCS_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed               */
     BCS_ERR_NO_DEVICE = 4,        /* no CUDA device / extension unusable    */
-    BCS_ERR_UNSUPPORTED = 5       /* valid request this build cannot serve  */
+    BCS_ERR_UNSUPPORTED = 5,      /* valid request this build cannot serve  */
+    BCS_ERR_TIMEOUT = 6           /* a bounded device wait gave up; the work
+                                     it guarded was skipped                 */
 } bcs_status;
 
 /* Grid choice, replaces `using Grid = std::variant<UniformGrid*, NoGrid*>`
@@ -277,6 +279,12 @@ typedef struct bcs_tuning {
     int full_sort;
     int occupancy_filter;
     int sorted_positions;
+    int grid_collisions;   /* particle collisions in grid order (a kernel of their own over
+                              the sorted slots, before the step kernel), which implies the
+                              sorted copies of positions and velocities: 0 = off (the step
+                              kernel searches each stencil), 1 = each row's window found by
+                              a linear scan from the row's first slot, 2 = by a binary
+                              search of the row's keys */
 } bcs_tuning;
 #define BCS_STEP_SHAPES 6
 
@@ -463,12 +471,21 @@ bcs_status bcs_surrogate_evaluate(bcs_surrogate* sur, int first, int count, doub
  * and layer-by-layer inference): 0 = tcgen05 with tensor-memory
  * accumulators (the default; BCS_TENSOR_PATH=1 in the environment starts
  * with mma.sync), 1 = mma.sync.  Returns the previous setting,
- * or -1 for an invalid value.  bcs_tensor_wait_expiries counts tcgen05
- * completions that were not seen within the kernel's bounded wait (the
- * product is then skipped, not stalled); it synchronises the device first,
- * or returns 0xFFFFFFFF when that fails. */
+ * or -1 for an invalid value.  bcs_tensor_wait_expiries counts the CTAs
+ * whose tcgen05 completion was not seen within the kernel's bounded wait
+ * (the product is then skipped, not stalled; the CTA still waits, bounded,
+ * for the products it issued before it frees its tensor memory); it
+ * synchronises the device first, or returns 0xFFFFFFFF when that fails.
+ * bcs_surrogate_forward and bcs_surrogate_loss_grad return BCS_ERR_TIMEOUT
+ * when the count grew during the call. */
 int bcs_set_tensor_path(int path);
 unsigned bcs_tensor_wait_expiries(void);
+/* Testing aid with no counterpart in the reference: with polls > 0 the first
+ * product wait of every CTA of the tcgen05 kernels polls, that many times,
+ * an mbarrier that nothing arrives at, so it gives up as a lost completion
+ * would and the give-up path runs; 0 restores the normal waits.
+ * Synchronises the device. */
+bcs_status bcs_set_tensor_wait_probe(int polls);
 /* The normalisation derived from the training set: 53 floats (feature means
  * [16], feature 1/std [16], target medians [9], target robust spreads [9]
  * (1.4826 x the median absolute deviation), edge scales of position,
@@ -528,9 +545,20 @@ bcs_status bcs_time_macro_steps(bcs_sim* sim, int substeps, int n, float* ms_out
  * BCS_GRID_SORT_STATIC_MAX returns BCS_ERR_INVALID_ARGUMENT.  The first call
  * on a device looks up that array's device address (cudaGetSymbolAddress)
  * with the device current; make that first call before any stream capture.
- * All calls share the array, so calls that overlap on the GPU race. */
+ * All calls share the array, so calls that overlap on the GPU race.
+ * A position outside the grid box gets the key of the nearest edge cell,
+ * exactly as on the allocating path; the call records that in the array's
+ * error word (BCS_ERRW_OUT_OF_GRID), which bcs_grid_sort_static_error_word
+ * reads back. */
 bcs_status bcs_grid_sort_static(const float* x, const float* y, const float* z, int n, const float* bounds6,
                                 const float* cell3, int* cell_ids, int* object_ids, void* stream);
+
+/* Error word of the most recent bcs_grid_sort_static call on the current
+ * device (0, or BCS_ERRW_OUT_OF_GRID when some position lay outside the grid
+ * box), into *out.  Enqueued on `stream` after that call and synchronises
+ * the stream; allocates nothing.  This entry point has no counterpart in
+ * the reference (which only printf()s such positions, uniform_grid.cu:31-34). */
+bcs_status bcs_grid_sort_static_error_word(void* stream, uint32_t* out);
 
 /* Phases of one frame timed by bcs_profile_steps. */
 enum {

@@ -2,8 +2,8 @@
 its host code, so that the reference's kernels can run on a machine that
 cannot build the reference itself (without its sources, or of another
 architecture than the one that recorded the tape).  Test infrastructure: it reads the
-reference's sources (default /root/reference, override with BCS_REFERENCE),
-works on scratch copies under /tmp and writes only into
+reference's sources from the checkout named by BCS_REFERENCE (default: a
+directory "reference" beside this repository), works on scratch copies under /tmp and writes only into
 oracle/_ref/refcuda_<scene>/:
 
   kernels.cubin   the reference's simulation translation units, unmodified,
@@ -18,7 +18,7 @@ oracle/_ref/refcuda_<scene>/:
                   reference merges and sorts the user's types, so a state
                   handed to the replay follows reference_order())
   limits.txt      the reference's grid box and dt (the replay's guard)
-  tape_recorder   the recorder (host code of this machine); it also replays
+  tape_recorder   the recorder (host code of the build host); it also replays
                   its tapes on the CPU (--replay-cpu), which the tests compare
                   with the CPU pin
 
@@ -57,7 +57,7 @@ import bcs_refconfig as RC  # noqa: E402
 import bcs_scenes as S  # noqa: E402
 from launch_rewrite import rewrite  # noqa: E402
 
-REF = os.environ.get("BCS_REFERENCE", "/root/reference")
+REF = os.environ.get("BCS_REFERENCE", os.path.join(os.path.dirname(REPO), "reference"))
 OUT = os.path.join(ORACLE, "_ref")
 DEVICE_TUS = ["grids/uniform_grid.cu", "objects/blood_cells.cu", "objects/vein_neighbors.cu",
               "objects/vein_triangles.cu", "simulation/simulation_controller.cu", "simulation/vein_collisions.cu",
@@ -172,7 +172,10 @@ def build_cubin(src: str, out: str) -> list:
 
     def one(tu):
         o = os.path.join(obj, os.path.basename(tu) + ".o")
-        r = _run(["nvcc", "-std=c++17", "--expt-relaxed-constexpr", "-rdc=true", "-gencode",
+        # the reference's own device flags (CMakeLists.txt:32,145): -O3,
+        # --expt-relaxed-constexpr, --maxrregcount=40; its 1024-thread
+        # launches need the register cap
+        r = _run(["nvcc", "-std=c++17", "--expt-relaxed-constexpr", "--maxrregcount=40", "-rdc=true", "-gencode",
                   "arch=compute_103a,code=sm_103a", "-O3", "-I" + src,
                   "-I" + os.path.join(REF, "Libraries", "include"), "-Xptxas", "-v", "-c",
                   os.path.join(src, tu), "-o", o], "nvcc " + tu)
@@ -304,8 +307,9 @@ def build(tag: str, scene, frames: int = 2, force: bool = False) -> str:
 
 
 def build_replay(out: str | None = None) -> str:
-    """The GPU replay (replay.cu, our own source) with this machine's nvcc;
-    built where it runs, since host code does not travel."""
+    """The GPU replay (replay.cu, our own source) with the local nvcc; built
+    on the machine that runs it, since host code does not travel between
+    architectures."""
     exe = out or os.path.join(OUT, "ref_cuda_replay")
     os.makedirs(os.path.dirname(exe), exist_ok=True)
     stubs = "/usr/local/cuda/lib64/stubs"

@@ -1,7 +1,7 @@
 """Pin recipe: run the reference's own step on the CPU and record golden vectors.
 
-Test infrastructure.  Reads the reference's sources (default /root/reference,
-override with BCS_REFERENCE), works on a scratch copy under /tmp (launches
+Test infrastructure.  Reads the reference's sources from the checkout named by
+BCS_REFERENCE (default: a directory "reference" beside this repository), works on a scratch copy under /tmp (launches
 rewritten for the serial CPU shim, src/config replaced by a generated set),
 compiles the hot-path translation units with g++ into oracle/_ref/, runs the
 headless driver on a seeded state and writes tests/golden/ref_pin_<scene>.npz.
@@ -41,7 +41,7 @@ import bcs_refconfig as RC  # noqa: E402
 import bcs_scenes as S  # noqa: E402
 from launch_rewrite import rewrite  # noqa: E402
 
-REF = os.environ.get("BCS_REFERENCE", "/root/reference")
+REF = os.environ.get("BCS_REFERENCE", os.path.join(os.path.dirname(REPO), "reference"))
 OUT = os.path.join(ORACLE, "_ref")
 GOLDEN = os.path.join(REPO, "tests", "golden")
 TUS = ["grids/uniform_grid.cu", "objects/blood_cells.cu", "objects/vein_triangles.cu", "objects/vein_neighbors.cu",

@@ -28,7 +28,7 @@ EXPORTED = [
     "bcs_get_info", "bcs_set_particles", "bcs_get_particles", "bcs_set_vein", "bcs_get_vein",
     "bcs_calculate_grids", "bcs_calculate_next_frame", "bcs_propagate_all", "bcs_step",
     "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
-    "bcs_profile_steps", "bcs_grid_sort_static", "bcs_create_batch", "bcs_get_scene_info",
+    "bcs_profile_steps", "bcs_grid_sort_static", "bcs_grid_sort_static_error_word", "bcs_create_batch", "bcs_get_scene_info",
     "bcs_get_tuning", "bcs_set_tuning", "bcs_autotune", "bcs_macro_step",
     "bcs_surrogate_create", "bcs_surrogate_destroy", "bcs_surrogate_collect", "bcs_surrogate_train",
     "bcs_surrogate_enable", "bcs_surrogate_get_stats", "bcs_surrogate_reset_stats", "bcs_surrogate_param_count",
@@ -133,7 +133,8 @@ class InitDesc(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("step_shape", C.c_int), ("persistent", C.c_int), ("spatial_order", C.c_int),
-                ("full_sort", C.c_int), ("occupancy_filter", C.c_int), ("sorted_positions", C.c_int)]
+                ("full_sort", C.c_int), ("occupancy_filter", C.c_int), ("sorted_positions", C.c_int),
+                ("grid_collisions", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -217,6 +218,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_time_steps": ([P, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "bcs_profile_steps": ([P, C.c_int, C.POINTER(C.c_float)], C.c_int),
         "bcs_grid_sort_static": ([P, P, P, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), P, P, P], C.c_int),
+        "bcs_grid_sort_static_error_word": ([P, C.POINTER(C.c_uint32)], C.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
@@ -538,9 +540,9 @@ class Simulation:
         return t
 
     def set_tuning(self, step_shape=0, persistent=0, spatial_order=0, full_sort=0, occupancy_filter=0,
-                   sorted_positions=0) -> None:
+                   sorted_positions=0, grid_collisions=1) -> None:
         t = Tuning(int(step_shape), int(persistent), int(spatial_order), int(full_sort), int(occupancy_filter),
-                   int(sorted_positions))
+                   int(sorted_positions), int(grid_collisions))
         _check(self.lib.bcs_set_tuning(self.h, C.byref(t)), "bcs_set_tuning")
 
     def autotune(self, frames: int = 5):

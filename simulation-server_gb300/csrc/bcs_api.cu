@@ -34,6 +34,8 @@ void launch_tri_keys(const float4* vpos, const uint32_t* tri, int T, const Scene
 void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigned* occ, const int* ids,
                         const float4* pos, float4* spos, const float4* vel, float4* svel, cudaStream_t s);
 void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s);
+void launch_row_starts(const int* keys, int n, const SceneDev* scenes, int scene_count, long long rows, int* row_start,
+                       cudaStream_t s);
 void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
                          cudaStream_t s);
 void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s);
@@ -111,6 +113,11 @@ struct DeviceGrid {
     float4* spos = nullptr;    // positions in sorted order, kept while spos_on
     float4* svel = nullptr;    // velocities in sorted order, with spos
     bool spos_on = false;
+    int* row_start = nullptr;  // first sorted slot of every grid row (+1 entry), kept while rows_on
+    long long rows = 0;        // grid rows of all scenes
+    bool rows_on = false;
+    const SceneDev* scenes = nullptr;   // the batch's scenes (row geometry)
+    int scene_count = 0;
     unsigned* temp = nullptr;
     int bits = 0;
     int id_bits = 0;
@@ -129,7 +136,8 @@ struct bcs_sim {
     std::vector<TypeDev> types;
     std::vector<WorkItem> work_host;
     std::vector<SceneDev> scenes_host;
-    bcs_tuning tune{0, 0, 0, 0, 0, 0};
+    bcs_tuning tune{0, 0, 0, 0, 0, 0, 0};
+    float4* coll = nullptr;      // grid-order collision sums (float4 x N)
     int max_pic = 0;
     int work_capacity = 0;       // work items of the smallest shape
     int persistent_grid[2] = {0, 0};   // by mode, 0 until first needed
@@ -344,6 +352,8 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, con
     float4* svel_out = dg.spos_on && pos && vel ? dg.svel : nullptr;
     launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, dg.occ_on ? dg.occ : nullptr, dg.g.ids, pos,
                        dg.spos_on && pos ? dg.spos : nullptr, vel, svel_out, st);
+    if (dg.rows_on) launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, st);
+    dg.g.row_start = dg.rows_on ? dg.row_start : nullptr;
 }
 
 void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
@@ -357,6 +367,8 @@ void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
     a.keys_out = write_keys ? s->pg.in_k : nullptr;
     a.ids_out = write_keys ? s->pg.in_v : nullptr;
     a.pg = s->pg.g;
+    // grid-order collisions once the grid carries its row starts and sorted copies
+    a.coll = s->pg.rows_on && a.pg.row_start && a.pg.spos && a.pg.svel ? s->coll : nullptr;
     a.tg = s->tg.g;
     a.tcache = s->tcache;
     a.tbox = s->tbox;
@@ -616,7 +628,7 @@ bool tuning_valid(const bcs_sim* s, const bcs_tuning& t) {
     return t.step_shape >= 0 && t.step_shape < kStepShapes && kShapes[t.step_shape].chunk >= s->max_pic &&
            (t.persistent == 0 || t.persistent == 1) && (t.spatial_order == 0 || t.spatial_order == 1) &&
            (t.full_sort == 0 || t.full_sort == 1) && (t.occupancy_filter == 0 || t.occupancy_filter == 1) &&
-           (t.sorted_positions == 0 || t.sorted_positions == 1);
+           (t.sorted_positions == 0 || t.sorted_positions == 1) && t.grid_collisions >= 0 && t.grid_collisions <= 2;
 }
 
 bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
@@ -637,15 +649,24 @@ bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
     }
     s->pg.occ_on = occ;
     s->pg.g.occ = occ ? s->pg.occ : nullptr;
-    const bool sp = t.sorted_positions && s->pg.spos;
+    // grid-order collisions read the sorted copies and the row-start table
+    const bool gc = t.grid_collisions && s->pg.g.uniform && s->pg.row_start && s->coll;
+    const bool sp = (t.sorted_positions || gc) && s->pg.spos;
     if (sp && !s->pg.spos_on && s->pg.sorted_once) {
         launch_gather_rows(s->pos[s->cur], s->pg.s_v[s->pg.slot], s->pg.count, s->pg.spos, s->stream);
         launch_gather_rows(s->vel[s->cur], s->pg.s_v[s->pg.slot], s->pg.count, s->pg.svel, s->stream);
     }
+    if (gc && !s->pg.rows_on && s->pg.sorted_once)
+        launch_row_starts(s->pg.g.keys, s->pg.count, s->pg.scenes, s->pg.scene_count, s->pg.rows, s->pg.row_start,
+                          s->stream);
     s->pg.spos_on = sp;
     s->pg.g.spos = sp && s->pg.sorted_once ? s->pg.spos : nullptr;
     s->pg.g.svel = sp && s->pg.sorted_once ? s->pg.svel : nullptr;
+    s->pg.rows_on = gc;
+    s->pg.g.row_start = gc && s->pg.sorted_once ? s->pg.row_start : nullptr;
     s->args.pg = s->pg.g;
+    s->args.coll = gc && s->pg.g.row_start && s->pg.g.spos && s->pg.g.svel ? s->coll : nullptr;
+    s->args.collide_search = t.grid_collisions == 2 ? 1 : 0;
     s->persistent_grid[0] = t.persistent ? step_persistent_grid(0, t.step_shape) : 0;
     s->persistent_grid[1] = t.persistent ? step_persistent_grid(1, t.step_shape) : 0;
     drop_graphs(s);
@@ -679,7 +700,7 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     std::vector<bcs_flow_segment> flows;
     std::vector<int> nb_scene_ids[9];
     std::vector<float> nb_scene_len[9];
-    long long key_total = 0, tkey_total = 0, mask_total = 0;
+    long long key_total = 0, tkey_total = 0, mask_total = 0, row_total = 0;
     int pstart = 0, mstart = 0, cglobal = 0;
     for (int si = 0; si < scene_count; ++si) {
         const bcs_scene_desc* d = descs + si;
@@ -772,6 +793,8 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
             return st;
         sd.pg.key_offset = key_total;
         sd.tg.key_offset = tkey_total;
+        sd.pg.row_offset = row_total;
+        row_total += (long long)sd.pg.cy * sd.pg.cz;
         key_total += sd.pg.cells;
         tkey_total += sd.tg.cells;
         // Wall-proximity mask, cells of half the impact distance (1..8).
@@ -889,6 +912,13 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     BCS_CUDA(cudaMemsetAsync(s->vvel, 0, sizeof(float4) * s->V, s->stream));
     BCS_CUDA(cudaMemsetAsync(s->vfrc, 0, sizeof(float4) * s->V, s->stream));
     if ((st = alloc_grid(s, s->pg, s->N, true)) || (st = alloc_grid(s, s->tg, std::max(1, s->T), false))) return st;
+    if (s->pg.g.uniform) {
+        // grid-order collisions: the row-start table and the collision sums
+        s->pg.rows = row_total;
+        s->pg.scenes = s->scenes;
+        s->pg.scene_count = s->S;
+        if ((st = dalloc(s, &s->pg.row_start, (size_t)row_total + 1)) || (st = dalloc(s, &s->coll, s->N))) return st;
+    }
     s->tg.count = s->T;
     s->tg.g.count = s->T;
     if (tuniform) {
@@ -936,7 +966,7 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     // ---- default launch: 256 threads / 512 particles / 4 CTAs per SM (the
     // fastest shape at the 4.2M-particle bifurcation), else the first shape
     // that holds the largest cell
-    bcs_tuning t{kDefaultShape, 0, 0, 0, 0, 0};
+    bcs_tuning t{kDefaultShape, 0, 0, 0, 0, 0, 1};
     if (kShapes[t.step_shape].chunk < s->max_pic) {
         t.step_shape = 0;
         while (kShapes[t.step_shape].chunk < s->max_pic) ++t.step_shape;
@@ -1252,6 +1282,7 @@ const char* bcs_status_string(bcs_status s) {
         case BCS_ERR_OUT_OF_MEMORY: return "out of device memory";
         case BCS_ERR_NO_DEVICE: return "no CUDA device";
         case BCS_ERR_UNSUPPORTED: return "unsupported";
+        case BCS_ERR_TIMEOUT: return "a bounded device wait expired";
     }
     return "unknown status";
 }
@@ -1733,11 +1764,12 @@ bcs_status bcs_autotune(bcs_sim* s, int frames, bcs_tuning* chosen, float* ms_pe
     if (st == BCS_OK) st = trial(best, best_ms);
     int bcs_tuning::*fields[] = {&bcs_tuning::step_shape, &bcs_tuning::persistent, &bcs_tuning::spatial_order,
                                  &bcs_tuning::full_sort, &bcs_tuning::occupancy_filter,
-                                 &bcs_tuning::sorted_positions};
-    const int limits[] = {kStepShapes, 2, 2, 2, 2, 2};
+                                 &bcs_tuning::sorted_positions, &bcs_tuning::grid_collisions};
+    const int limits[] = {kStepShapes, 2, 2, 2, 2, 2, 3};
+    constexpr int kFields = sizeof(limits) / sizeof(limits[0]);
     for (int sweep = 0; sweep < 2 && st == BCS_OK; ++sweep) {
         bool improved = false;
-        for (int f = 0; f < 6 && st == BCS_OK; ++f)
+        for (int f = 0; f < kFields && st == BCS_OK; ++f)
             for (int v = 0; v < limits[f] && st == BCS_OK; ++v) {
                 bcs_tuning t = best;
                 if (t.*fields[f] == v) continue;
@@ -2082,13 +2114,16 @@ bcs_status bcs_surrogate_loss_grad(bcs_surrogate* z, int cells, const float* fea
     BCS_CUDA(cudaMemcpyAsync(z->net.edge_buf(), edge_features, sizeof(float) * (size_t)cells * z->net.edges() * kEdgeIn,
                              cudaMemcpyHostToDevice, st));
     BCS_CUDA(cudaMemcpyAsync(z->net.target_buf(), targets, sizeof(float) * n * kOut, cudaMemcpyHostToDevice, st));
+    const unsigned expired = bcs_tensor_wait_expiries();
     z->net.forward(z->net.input_buf(), z->net.edge_buf(), cells, true);
     z->net.backward(z->net.target_buf(), cells);
     if (loss) BCS_CUDA(cudaMemcpyAsync(loss, z->net.loss_dev(), sizeof(float), cudaMemcpyDeviceToHost, st));
     if (grads)
         BCS_CUDA(cudaMemcpyAsync(grads, z->net.grad(), sizeof(float) * z->net.param_count(), cudaMemcpyDeviceToHost, st));
     BCS_CUDA(cudaStreamSynchronize(st));
-    return check_last();
+    bcs_status r = check_last();
+    if (r == BCS_OK && bcs_tensor_wait_expiries() != expired) r = BCS_ERR_TIMEOUT;
+    return r;
 }
 
 bcs_status bcs_surrogate_forward(bcs_surrogate* z, int cells, const float* features, const float* edge_features,
@@ -2100,10 +2135,13 @@ bcs_status bcs_surrogate_forward(bcs_surrogate* z, int cells, const float* featu
     BCS_CUDA(cudaMemcpyAsync(z->net.input_buf(), features, sizeof(float) * n * kFeatIn, cudaMemcpyHostToDevice, st));
     BCS_CUDA(cudaMemcpyAsync(z->net.edge_buf(), edge_features, sizeof(float) * (size_t)cells * z->net.edges() * kEdgeIn,
                              cudaMemcpyHostToDevice, st));
+    const unsigned expired = bcs_tensor_wait_expiries();
     z->net.forward(z->net.input_buf(), z->net.edge_buf(), cells, false);
     BCS_CUDA(cudaMemcpyAsync(outputs, z->net.output(), sizeof(float) * n * kOut, cudaMemcpyDeviceToHost, st));
     BCS_CUDA(cudaStreamSynchronize(st));
-    return check_last();
+    bcs_status r = check_last();
+    if (r == BCS_OK && bcs_tensor_wait_expiries() != expired) r = BCS_ERR_TIMEOUT;
+    return r;
 }
 
 bcs_status bcs_surrogate_evaluate(bcs_surrogate* z, int first, int count, double* net_error, double* base_error) {
@@ -2135,6 +2173,11 @@ int bcs_set_tensor_path(int path) {
     const int prev = mpnn_gemm_path();
     mpnn_set_gemm_path(path);
     return prev;
+}
+
+bcs_status bcs_set_tensor_wait_probe(int polls) {
+    if (polls < 0) return BCS_ERR_INVALID_ARGUMENT;
+    return mpnn_set_wait_probe(polls) ? BCS_OK : BCS_ERR_CUDA;
 }
 
 unsigned bcs_tensor_wait_expiries(void) {

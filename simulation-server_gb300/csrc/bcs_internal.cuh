@@ -22,6 +22,12 @@
 //   vpos, vvel, vfrc         float4 x V (all scenes' veins, scene-major)
 //   vnb_ids[9], vnb_len[9]   int32 / float x V, the reference's nine
 //                            neighbour-slot arrays (VeinNeighbors)
+//   row_start                int32 per grid row (cy x cz rows of cx cells, all
+//                            scenes) + 1: the first sorted slot whose key is in
+//                            the row or after it; with the sorted keys it
+//                            bounds a stencil row's slots without the table
+//   coll                     float4 x N: each particle's collision force from
+//                            the grid-order collision kernel
 //   tkeys, tids, ttable      triangle grid, same representation as particles
 //   tcache                   3 float4 per sorted triangle slot: (v0, id),
 //                            (v1 - v0), (v2 - v0) — the Moller-Trumbore
@@ -81,6 +87,7 @@ struct GridGeom {         // one scene's uniform grid (uniform_grid.cu:83-104)
     int cx, cy, cz;       // cell counts (int(extent / cell))
     long long cells;
     long long key_offset; // first key of the scene in the batch key space
+    long long row_offset; // first grid row (cy * cz rows of cx cells) of the scene in the batch row space
 };
 
 struct MaskGeom {         // one scene's wall-proximity mask
@@ -113,6 +120,8 @@ struct GridDev {          // batch-wide sorted grid
     const unsigned* occ;  // occupancy bitmap, 1 bit per cell, or null
     const float4* spos;   // positions in sorted order (particle grid), or null
     const float4* svel;   // velocities in sorted order (set with spos), or null
+    const int* row_start; // particle grid, grid-order collisions: first sorted slot of each grid row
+                          // (batch row space, one entry past the last row), or null
     int count;            // objects
 };
 
@@ -138,6 +147,10 @@ struct StepArgs {
     int* crowded_counter; // [0] crowded entries, [1] CTAs of k_crowded finished, [2] crowded_cells entries,
                           // [3] particles of the listed cells taken, [4..5] 64-bit running total
     float4* cent;         // this step's cell centroids (batch-wide cell index), for k_crowded
+    float4* coll;         // grid-order collisions: each particle's collision force, written by
+                          // k_collide before the step kernel reads it; null: the step kernel
+                          // searches the stencil itself
+    int collide_search;   // grid-order collisions: 1 = binary search of each row window, 0 = linear scan
     const TypeDev* types;
     int type_count;
     const SceneDev* scenes;

@@ -139,6 +139,7 @@ __device__ inline unsigned to_u32_sat(float t) { return t <= 0.f ? 0u : (t >= 42
 // from the unclamped quotients (Q7).
 struct Stencil {
     int cell;                  // scene-local key of the centre cell
+    int ix, iy, iz;            // its cell coordinates
     int x0, x1, y0, y1, z0, z1;
     bool regular;              // the unclamped cell indices are the key's: every
                                // such particle of the cell has this stencil
@@ -152,6 +153,9 @@ __device__ inline Stencil particle_stencil(const GridGeom& geo, float3 x) {
     const int ix = axis_clamp(tx, geo.ext[0], geo.cx), iy = axis_clamp(ty, geo.ext[1], geo.cy),
               iz = axis_clamp(tz, geo.ext[2], geo.cz);
     st.cell = iz * geo.cx * geo.cy + iy * geo.cx + ix;   // key_of_quotients
+    st.ix = ix;
+    st.iy = iy;
+    st.iz = iz;
     st.regular = (int)tx == ix && (int)ty == iy && (int)tz == iz;
     stencil_range((int)tx, geo.cx, st.x0, st.x1);
     stencil_range((int)ty, geo.cy, st.y0, st.y1);
@@ -507,10 +511,34 @@ __device__ inline void vein_collision(const StepArgs& a, const SceneDev& sc, flo
         float3 ds = p.vein_collision_force_intensity * vel;
         uint32_t i0 = a.tri[3 * obj], i1 = a.tri[3 * obj + 1], i2 = a.tri[3 * obj + 2];
         float3 b = barycentric(x + t * dir, xyz(a.vpos[i0]), xyz(a.vpos[i1]), xyz(a.vpos[i2]));
-        float3 d0 = b.x * ds, d1 = b.y * ds, d2v = b.z * ds;
-        atomicAdd(&a.vfrc[i0].x, d0.x); atomicAdd(&a.vfrc[i0].y, d0.y); atomicAdd(&a.vfrc[i0].z, d0.z);
-        atomicAdd(&a.vfrc[i1].x, d1.x); atomicAdd(&a.vfrc[i1].y, d1.y); atomicAdd(&a.vfrc[i1].z, d1.z);
-        atomicAdd(&a.vfrc[i2].x, d2v.x); atomicAdd(&a.vfrc[i2].y, d2v.y); atomicAdd(&a.vfrc[i2].z, d2v.z);
+        float d[9];
+        const float3 d0 = b.x * ds, d1 = b.y * ds, d2v = b.z * ds;
+        d[0] = d0.x; d[1] = d0.y; d[2] = d0.z;
+        d[3] = d1.x; d[4] = d1.y; d[5] = d1.z;
+        d[6] = d2v.x; d[7] = d2v.y; d[8] = d2v.z;
+        // The reference's scatter (vein_collisions.cu:272-274) as
+        // warp-aggregated atomics: the lanes here that hit the same triangle
+        // add their shares in lane order and the lowest of them issues the
+        // nine atomics, once per distinct triangle per warp.
+        const unsigned act = __activemask();
+        const unsigned peers = __match_any_sync(act, obj);
+        const int lane = threadIdx.x & 31;
+        float sum[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) sum[k] = 0.f;
+        for (unsigned m = act; m; m &= m - 1u) {
+            const int l = __ffs(m) - 1;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const float v = __shfl_sync(act, d[k], l);
+                if ((peers >> l) & 1u) sum[k] += v;
+            }
+        }
+        if (lane == __ffs(peers) - 1) {
+            atomicAdd(&a.vfrc[i0].x, sum[0]); atomicAdd(&a.vfrc[i0].y, sum[1]); atomicAdd(&a.vfrc[i0].z, sum[2]);
+            atomicAdd(&a.vfrc[i1].x, sum[3]); atomicAdd(&a.vfrc[i1].y, sum[4]); atomicAdd(&a.vfrc[i1].z, sum[5]);
+            atomicAdd(&a.vfrc[i2].x, sum[6]); atomicAdd(&a.vfrc[i2].y, sum[7]); atomicAdd(&a.vfrc[i2].z, sum[8]);
+        }
     }
 }
 
@@ -646,7 +674,9 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
     for (int i = threadIdx.x; i < np; i += THREADS) {
         const float4 px = s_pos[i];
         float3 coll;
-        if (!particle_collisions(a, sc, p0 + i, xyz(px), xyz(s_vel[i]), px.w, coll, e)) {
+        if (a.coll) {
+            coll = xyz(__ldg(&a.coll[p0 + i]));   // k_collide's sum
+        } else if (!particle_collisions(a, sc, p0 + i, xyz(px), xyz(s_vel[i]), px.w, coll, e)) {
             // crowded: every particle of the cell that shares this stencil is
             // crowded too, and the first to claim the cell (the table entry's
             // spare word, zero after each build) lists it once for k_crowded
@@ -858,6 +888,119 @@ __global__ void __launch_bounds__(kCrowdedThreads, 3) k_crowded(const StepArgs a
             atomicExch(&a.crowded_counter[1], 0);
         }
     }
+}
+
+// ------------------------------------------------ grid-order collisions ----
+// First sorted slot of every grid row (the cx cells sharing y and z), batch
+// row space: the lower bound of the row's first key in the sorted keys of
+// its scene (a scene's keys fill exactly its particle range of slots).  One
+// entry past the last row holds n.
+__global__ void k_row_starts(const int* __restrict__ keys, int n, const SceneDev* __restrict__ scenes,
+                             int scene_count, long long rows, int* row_start) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > rows) return;
+    if (r == rows) {
+        row_start[r] = n;
+        return;
+    }
+    const int s = find_range(scene_count, r, [&](int k) { return scenes[k].pg.row_offset; });
+    const GridGeom& g = scenes[s].pg;
+    const long long target = g.key_offset + (r - g.row_offset) * (long long)g.cx;
+    int lo = scenes[s].particle_start, hi = scenes[s].particle_end;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((long long)__ldg(&keys[mid]) < target) lo = mid + 1;
+        else hi = mid;
+    }
+    row_start[r] = lo;
+}
+
+// calculateParticleCollisions<UniformGrid> (particle_collisions.cuh:26-38,
+// 53-83,104-269) in grid order: one thread per sorted slot, so a warp holds
+// particles of neighbouring cells that share most of their stencil (in a
+// crowded cell, all of it: every candidate load is a broadcast and the
+// loops are warp-uniform).  A stencil row (dz, dy) is the key window
+// [centre + dz cx cy + dy cx + x0, ... + x1] clipped to the scene's cells;
+// its slots are found from the row-start table and the sorted keys, and its
+// candidates are read from the sorted copies of positions and velocities.
+// Rows in stencil order and slots ascending within each: the same
+// candidates in the same order as particle_collisions, hence the same sum.
+// The particle's sum lands in a.coll at its id, for the step kernel.
+constexpr int kCollideThreads = 256;
+
+template <int SEARCH>
+__global__ void __launch_bounds__(kCollideThreads) k_collide(const StepArgs a) {
+    const int j = blockIdx.x * kCollideThreads + threadIdx.x;
+    if (j >= a.n) return;
+    const GridDev& g = a.pg;
+    const int s = find_range(a.scene_count, j, [&](int k) { return a.scenes[k].particle_start; });
+    const SceneDev& sc = a.scenes[s];
+    const GridGeom& geo = sc.pg;
+    const float4 px = __ldg(&g.spos[j]);
+    const float3 x = xyz(px), v = xyz(__ldg(&g.svel[j]));
+    const float R = px.w;
+    const Stencil st = particle_stencil(geo, x);
+    const long long cxy = (long long)geo.cx * geo.cy;
+    const int send = sc.particle_end;
+    const int* __restrict__ keys = g.keys;
+    float3 acc = f3(0.f, 0.f, 0.f);
+    unsigned e = 0;
+    // When the whole stencil lies inside the grid (every particle inside the
+    // grid box, and nearly all outside it), each window lies inside its row,
+    // takes its row from the cell coordinates and spans x1 - x0 + 1 keys;
+    // otherwise the windows are clipped to the grid row by row.
+    const bool inside = st.ix + st.x0 >= 0 && st.ix + st.x1 <= geo.cx - 1 && st.iy + st.y0 >= 0 &&
+                        st.iy + st.y1 <= geo.cy - 1 && st.iz + st.z0 >= 0 && st.iz + st.z1 <= geo.cz - 1;
+    if (SEARCH != 0 && inside) {
+        // The nine rows' key windows, then one binary search per row for the
+        // window's first slot, the nine searches advancing together (their
+        // loads are independent), then each window's slots in stencil order.
+        int lo[9], hi[9], end[9], wlo[9];
+        const int kbase = (int)geo.key_offset, rbase = (int)geo.row_offset;
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const int dz = r / 3 - 1, dy = r % 3 - 1;
+            lo[r] = hi[r] = end[r] = 0;
+            wlo[r] = 0;
+            if (dz < st.z0 || dz > st.z1 || dy < st.y0 || dy > st.y1) continue;
+            const int rr = (st.iz + dz) * geo.cy + st.iy + dy;   // the window's row
+            wlo[r] = kbase + rr * geo.cx + st.ix + st.x0;
+            lo[r] = __ldg(&g.row_start[rbase + rr]);
+            hi[r] = end[r] = __ldg(&g.row_start[rbase + rr + 1]);
+        }
+        for (bool more = true; more;) {
+            more = false;
+#pragma unroll
+            for (int r = 0; r < 9; ++r) {
+                if (lo[r] < hi[r]) {
+                    const int m = (lo[r] + hi[r]) >> 1;
+                    if (__ldg(&keys[m]) < wlo[r]) lo[r] = m + 1;
+                    else hi[r] = m;
+                    more |= lo[r] < hi[r];
+                }
+            }
+        }
+        const int wx = st.x1 - st.x0;
+#pragma unroll
+        for (int r = 0; r < 9; ++r)
+            for (int t = lo[r]; t < end[r] && __ldg(&keys[t]) - wlo[r] <= wx; ++t)
+                collide(a, x, v, R, __ldg(&g.spos[t]), [&g, t] { return __ldg(&g.svel[t]); }, acc, e);
+    } else {
+        // each row's window from a linear scan of the row's first slots
+        for (int dz = st.z0; dz <= st.z1; ++dz)
+            for (int dy = st.y0; dy <= st.y1; ++dy) {
+                const long long row = (long long)st.cell + dz * cxy + (long long)dy * geo.cx;
+                const long long klo = max(row + st.x0, 0LL), khi = min(row + st.x1, geo.cells - 1);
+                if (klo > khi) continue;
+                const int glo = (int)(geo.key_offset + klo), ghi = (int)(geo.key_offset + khi);
+                int t = __ldg(&g.row_start[geo.row_offset + klo / geo.cx]);
+                while (t < send && __ldg(&keys[t]) < glo) ++t;
+                for (; t < send && __ldg(&keys[t]) <= ghi; ++t)
+                    collide(a, x, v, R, __ldg(&g.spos[t]), [&g, t] { return __ldg(&g.svel[t]); }, acc, e);
+            }
+    }
+    a.coll[__ldg(&g.ids[j])] = make_float4(acc.x, acc.y, acc.z, 0.f);
+    if (e) atomicOr(a.err, e);
 }
 
 // handleVeinEndsBlockSync (src/simulation/vein_end.cu:57-108) after the
@@ -2079,8 +2222,13 @@ void launch_step(const StepArgs& a, int items, int mode, int shape, int persiste
     if (items <= 0) return;
     const bool persistent = persistent_grid > 0;
     const int blocks = persistent ? std::min(items, persistent_grid) : items;
+    if (a.coll && a.pg.uniform && a.pg.row_start && a.pg.spos && a.pg.svel && a.n > 0) {
+        const int blocks = (a.n + kCollideThreads - 1) / kCollideThreads;
+        if (a.collide_search) k_collide<1><<<blocks, kCollideThreads, 0, s>>>(a);
+        else k_collide<0><<<blocks, kCollideThreads, 0, s>>>(a);
+    }
     step_kernel_for(mode, shape, persistent)<<<blocks, kShapes[shape].threads, 0, s>>>(a);
-    if (!a.pg.uniform) return;   // no stencil, no crowded particles
+    if (!a.pg.uniform || a.coll) return;   // no stencil, or no crowded particles set aside
     static int grid = 0;
     if (!grid) {
         int dev = 0, sms = 0;
@@ -2109,6 +2257,10 @@ void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigne
                         const float4* pos, float4* spos, const float4* vel, float4* svel, cudaStream_t s) {
     k_next_epoch<<<1, 1, 0, s>>>(epoch);
     if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table, epoch, occ, ids, pos, spos, vel, svel);
+}
+void launch_row_starts(const int* keys, int n, const SceneDev* scenes, int scene_count, long long rows, int* row_start,
+                       cudaStream_t s) {
+    k_row_starts<<<(unsigned)((rows + 1 + 255) / 256), 256, 0, s>>>(keys, n, scenes, scene_count, rows, row_start);
 }
 void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s) {
     if (n > 0) k_occ_update<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, occ, set ? 1 : 0);

@@ -471,8 +471,15 @@ __device__ inline uint64_t tc_desc(uint32_t saddr, uint32_t sbo = 2048) {
 // kind::f16 instruction descriptor: FP32 D, bf16 A and B, both K-major, N 128, M 128.
 constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 
-__device__ inline bool tc_wait(uint32_t mbar, uint32_t phase) {
-    for (long long i = 0; i < kTcWaitBound; ++i) {
+// Testing aid (bcs_set_tensor_wait_probe): when positive, the first product
+// wait of every CTA polls, that many times, an mbarrier nothing arrives at
+// instead of the product's own, so it expires exactly as a lost completion
+// would; the give-up path then waits for the product's own completion with
+// the full bound before tensor memory is freed.
+__device__ int g_tc_probe_polls = 0;
+
+__device__ inline bool tc_wait(uint32_t mbar, uint32_t phase, long long bound = kTcWaitBound) {
+    for (long long i = 0; i < bound; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
@@ -491,11 +498,13 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const float* __restrict__ X1, c
     extern __shared__ __align__(1024) unsigned char smem_tc[];
     unsigned char* As = smem_tc;
     unsigned char* Bs = smem_tc + kTcTile;
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar, probe;
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int r0 = blockIdx.x * 128;
     const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    const uint32_t probe_a = (uint32_t)__cvta_generic_to_shared(&probe);
+    const int probe_polls = g_tc_probe_polls;
     if (warp == 0) {
         const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(slot) : "memory");
@@ -503,6 +512,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const float* __restrict__ X1, c
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(probe_a) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -557,13 +567,15 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const float* __restrict__ X1, c
         }
         // the same verdict on every thread: a CTA stops issuing (and
         // restaging the operands) as a whole
-        ok = __syncthreads_and(tc_wait(mbar_a, phase) ? 1 : 0) != 0;
+        const bool seen = in == 0 && probe_polls > 0 ? tc_wait(probe_a, 0, probe_polls) : tc_wait(mbar_a, phase);
+        ok = __syncthreads_and(seen ? 1 : 0) != 0;
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (!ok) break;
     }
     if (!ok) {
-        if (tid == 0) atomicOr(err, 1u);
+        if (tid == 0) atomicAdd(err, 1u);
+        // the products already issued complete before tensor memory is freed
         tc_wait(mbar_a, phase ^ 1u);
     } else {
         const int row = r0 + warp * 32 + lane;
@@ -622,12 +634,14 @@ __device__ inline uint32_t tc_offset64(int m, int k) {
 __global__ void __launch_bounds__(128) k_wgrad_tc(const float* __restrict__ X, const float* __restrict__ dY, float* dW,
                                                   int rows, int chunk, unsigned* err) {
     __shared__ __align__(1024) unsigned char smem_wg[2 * kTcWgTile];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar, probe;
     __shared__ uint32_t tmem_slot;
     unsigned char* As = smem_wg;
     unsigned char* Bs = smem_wg + kTcWgTile;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    const uint32_t probe_a = (uint32_t)__cvta_generic_to_shared(&probe);
+    const int probe_polls = g_tc_probe_polls;
     if (warp == 0) {
         const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(slot) : "memory");
@@ -635,6 +649,7 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const float* __restrict__ X, c
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar_a) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(probe_a) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -681,14 +696,16 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const float* __restrict__ X, c
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_a)
                          : "memory");
         }
+        const bool seen = !any && probe_polls > 0 ? tc_wait(probe_a, 0, probe_polls) : tc_wait(mbar_a, phase);
         any = true;
-        ok = __syncthreads_and(tc_wait(mbar_a, phase) ? 1 : 0) != 0;
+        ok = __syncthreads_and(seen ? 1 : 0) != 0;
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (!ok) break;
     }
     if (!ok) {
-        if (tid == 0) atomicOr(err, 1u);
+        if (tid == 0) atomicAdd(err, 1u);
+        // the products already issued complete before tensor memory is freed
         tc_wait(mbar_a, phase ^ 1u);
     } else if (any) {
         const int row = warp * 32 + lane;   // feature k of X
@@ -727,6 +744,11 @@ unsigned* g_gemm_err = nullptr;      // tcgen05 wait expiries (device word)
 }  // namespace
 
 void mpnn_set_gemm_path(int path) { g_gemm_path = path; }
+bool mpnn_set_wait_probe(int polls) {
+    return cudaDeviceSynchronize() == cudaSuccess &&
+           cudaMemcpyToSymbol(g_tc_probe_polls, &polls, sizeof(int)) == cudaSuccess &&
+           cudaDeviceSynchronize() == cudaSuccess;
+}
 int mpnn_gemm_path() { return g_gemm_path; }
 unsigned* mpnn_gemm_error_word() {
     if (!g_gemm_err) {

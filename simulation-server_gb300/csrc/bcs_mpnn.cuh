@@ -74,6 +74,7 @@ void mpnn_gemm(const float* X1, const __nv_bfloat16* W1t, const float* X2, const
 // accumulators, the default), 1 = mma.sync.  The error word counts tcgen05
 // waits that expired.
 void mpnn_set_gemm_path(int path);
+bool mpnn_set_wait_probe(int polls);
 int mpnn_gemm_path();
 unsigned* mpnn_gemm_error_word();
 // dX (+)= dY W^T for hidden x hidden W.

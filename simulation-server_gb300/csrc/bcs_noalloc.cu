@@ -14,7 +14,10 @@
 // calls share it, and it keeps the last call's contents, so calls that
 // overlap on the GPU (different streams or threads without ordering) race.
 // Every scratch word a call reads is written earlier in the same call, so
-// nothing has to be cleared between calls.
+// nothing has to be cleared between calls.  A call's error word (positions
+// outside the grid box, whose keys are clamped to the edge cells as in
+// bcs_get_grid) stays in the array until the next call clears it;
+// bcs_grid_sort_static_error_word reads it back.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -74,10 +77,13 @@ extern "C" bcs_status bcs_grid_sort_static(const float* x, const float* y, const
         return BCS_ERR_INVALID_ARGUMENT;
     if (n > kStaticMax) return BCS_ERR_INVALID_ARGUMENT;
     if (!(cell3[0] > 0 && cell3[1] > 0 && cell3[2] > 0)) return BCS_ERR_INVALID_ARGUMENT;
-    if (n == 0) return BCS_OK;
     unsigned* scratch = nullptr;
     bcs_status st = scratch_for_current_device(&scratch);
     if (st != BCS_OK) return st;
+    unsigned* err = scratch + 2 * (size_t)kStaticMax + 256 * (size_t)kStaticTiles + 256;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(err, 0, sizeof(unsigned), s) != cudaSuccess) return BCS_ERR_CUDA;
+    if (n == 0) return BCS_OK;
 
     // Grid geometry exactly as bcs_create derives it (FP32, uniform_grid.cu:83-104).
     bcs::GridGeom g{};
@@ -96,12 +102,9 @@ extern "C" bcs_status bcs_grid_sort_static(const float* x, const float* y, const
     int bits = 0;
     while (bits < 31 && (1LL << bits) < g.cells) ++bits;
 
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     int* sk = reinterpret_cast<int*>(scratch);
     int* sv = sk + kStaticMax;
     unsigned* temp = scratch + 2 * (size_t)kStaticMax;
-    unsigned* err = temp + 256 * (size_t)kStaticTiles + 256;
-    if (cudaMemsetAsync(err, 0, sizeof(unsigned), s) != cudaSuccess) return BCS_ERR_CUDA;
     // Keys land in the caller's outputs, which then serve as one ping-pong
     // buffer of the sort; the scratch pair is the other.
     k_keys_soa<<<(n + 255) / 256, 256, 0, s>>>(x, y, z, n, g, cell_ids, object_ids, err);
@@ -114,4 +117,19 @@ extern "C" bcs_status bcs_grid_sort_static(const float* x, const float* y, const
         }
     }
     return cudaGetLastError() == cudaSuccess ? BCS_OK : BCS_ERR_CUDA;
+}
+
+extern "C" bcs_status bcs_grid_sort_static_error_word(void* stream, uint32_t* out) {
+    if (!out) return BCS_ERR_INVALID_ARGUMENT;
+    unsigned* scratch = nullptr;
+    bcs_status st = scratch_for_current_device(&scratch);
+    if (st != BCS_OK) return st;
+    const unsigned* err = scratch + 2 * (size_t)kStaticMax + 256 * (size_t)kStaticTiles + 256;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned w = 0;
+    if (cudaMemcpyAsync(&w, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return BCS_ERR_CUDA;
+    *out = w;
+    return BCS_OK;
 }

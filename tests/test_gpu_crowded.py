@@ -1,12 +1,19 @@
-"""Crowded particles.  A particle whose collision stencil holds more than 128
-sorted slots is left by the step kernel to k_crowded: inside the grid box a
-warp takes its whole grid cell (the stencil's slots staged in shared memory,
-the lanes of each particle splitting them), outside it a warp takes the
-particle alone (lanes split the slots); fixed butterflies add the partial
-sums.  Scenes with cells piled onto a few points put many
-particles on both paths: the result must match the FP64 oracle like any
-other step, and stay bit-identical across every launch shape and grid
-option.
+"""Crowded particles.  Two collision paths take them:
+
+  * grid order (the default, tuning grid_collisions = 1): k_collide gives
+    every sorted slot a thread; the particles of a crowded cell sit in
+    neighbouring lanes and share their whole stencil, so each lane sums its
+    candidates in stencil order with warp-uniform loops;
+  * cell order (grid_collisions = 0): a particle whose collision stencil
+    holds more than 128 sorted slots is left by the step kernel to
+    k_crowded: inside the grid box a warp takes its whole grid cell (the
+    stencil's slots staged in shared memory, the lanes of each particle
+    splitting them), outside it a warp takes the particle alone (lanes split
+    the slots); fixed butterflies add the partial sums.
+
+Scenes with cells piled onto a few points put many particles on both paths:
+the result must match the FP64 oracle like any other step on either path,
+and stay bit-identical across every launch shape and grid option of a path.
 
 Tolerances as the plain parity tests: one step 1e-5 relative (FP32 against
 FP64, elementwise against |oracle| + rms(oracle)); after a few steps 1e-3 of
@@ -82,9 +89,13 @@ def test_scene_is_crowded():
 
 
 def test_crowded_count(lib):
-    """bcs_get_crowded counts the particles set aside, once per step."""
+    """bcs_get_crowded counts the particles the cell-order path sets aside,
+    once per step; the grid-order path sets none aside."""
     sc = crowded_scene()
-    sim = make(sc)
+    g = make(sc)
+    g.step(2)
+    assert g.crowded_particles() == 0
+    sim = make(sc, grid_collisions=0)
     assert sim.crowded_particles() == 0
     sim.step(1)
     host = int((stencil_slots(sc, sc.positions) > CROWDED).sum())
@@ -94,9 +105,10 @@ def test_crowded_count(lib):
     assert sim.crowded_particles() > 2 * got
 
 
-def test_one_step_matches_oracle(lib):
+@pytest.mark.parametrize("gc", [1, 0])
+def test_one_step_matches_oracle(lib, gc):
     sc = crowded_scene()
-    sim = make(sc)
+    sim = make(sc, grid_collisions=gc)
     sim.step(1)
     o = O.OracleSim(sc)
     o.step(1)
@@ -105,9 +117,10 @@ def test_one_step_matches_oracle(lib):
         assert e <= 1e-5, f"{name}: relative error {e:.3e}"
 
 
-def test_few_steps_within_1e3_radius(lib):
+@pytest.mark.parametrize("gc", [1, 0])
+def test_few_steps_within_1e3_radius(lib, gc):
     sc = crowded_scene(vel=0.5)
-    sim = make(sc)
+    sim = make(sc, grid_collisions=gc)
     sim.step(4)
     o = O.OracleSim(sc)
     o.step(4)
@@ -119,22 +132,24 @@ def test_few_steps_within_1e3_radius(lib):
 FLAGS = ("persistent", "spatial_order", "full_sort", "occupancy_filter", "sorted_positions")
 
 
+@pytest.mark.parametrize("gc", [1, 0])
 @pytest.mark.parametrize("shape", range(len(bcs.STEP_SHAPES)))
 @pytest.mark.parametrize("flags", [0, 1])
-def test_every_shape_same_state(lib, shape, flags):
+def test_every_shape_same_state(lib, shape, flags, gc):
     sc = crowded_scene()
-    want = make(sc)
+    want = make(sc, grid_collisions=gc)
     want.step(5)
     want = want.get_particles()
-    sim = make(sc, step_shape=shape, **{f: flags for f in FLAGS})
+    sim = make(sc, step_shape=shape, grid_collisions=gc, **{f: flags for f in FLAGS})
     sim.step(5)
     for a, b in zip(sim.get_particles(), want):
         np.testing.assert_array_equal(a, b)
 
 
-def test_split_phases_match_fused(lib):
+@pytest.mark.parametrize("gc", [1, 0])
+def test_split_phases_match_fused(lib, gc):
     sc = crowded_scene()
-    a, b = make(sc), make(sc, occupancy_filter=1, sorted_positions=1)
+    a, b = make(sc, grid_collisions=gc), make(sc, occupancy_filter=1, sorted_positions=1, grid_collisions=gc)
     for _ in range(3):
         a.calculate_grids()
         a.calculate_next_frame()
@@ -144,9 +159,10 @@ def test_split_phases_match_fused(lib):
         np.testing.assert_array_equal(x, y)
 
 
-def test_macro_steps_match_oracle(lib):
+@pytest.mark.parametrize("gc", [1, 0])
+def test_macro_steps_match_oracle(lib, gc):
     sc = crowded_scene(vel=0.5)
-    sim = make(sc)
+    sim = make(sc, grid_collisions=gc)
     o = O.OracleSim(sc)
     sim.macro_step(4, 1)
     o.macro_step(4, 1)
@@ -155,16 +171,17 @@ def test_macro_steps_match_oracle(lib):
     assert rel_err(g[1], r[1]) <= 4e-4
 
 
-def test_crowded_outside_the_grid_box(lib):
+@pytest.mark.parametrize("gc", [1, 0])
+def test_crowded_outside_the_grid_box(lib, gc):
     """A pile beyond the grid box's top face: clamped keys, so those
-    particles' stencils are not their cell's regular one (the per-particle
-    warp path); the other two piles are inside."""
+    particles' stencils are not their cell's regular one (on the cell-order
+    path the per-particle warp path); the other two piles are inside."""
     sc = crowded_scene(anchors=[[0.0, 47.0, 0.0], [3.0, -45.0, -2.0]], cells=120, length=150.0, use_blood_flow=False)
     inside = sc.positions[:, 1] < 0
     assert (stencil_slots(sc, sc.positions)[inside] > CROWDED).sum() > 1000
     top = sc.positions[:, 1].max()
     assert top > sc.vein_positions[:, 1].max() + sc.params.grid_y_margin
-    sim = make(sc)
+    sim = make(sc, grid_collisions=gc)
     sim.step(1)
     o = O.OracleSim(sc)
     o.step(1)
@@ -173,26 +190,28 @@ def test_crowded_outside_the_grid_box(lib):
         assert e <= 1e-5, f"{name}: relative error {e:.3e}"
     want = sim.get_particles()
     for shape in range(len(bcs.STEP_SHAPES)):
-        other = make(sc, step_shape=shape, **{f: shape % 2 for f in FLAGS})
+        other = make(sc, step_shape=shape, grid_collisions=gc, **{f: shape % 2 for f in FLAGS})
         other.step(1)
         for a, b in zip(other.get_particles(), want):
             np.testing.assert_array_equal(a, b)
 
 
 
-def test_batched_crowded_scenes_match_standalone(lib):
-    """Crowded cells of several scenes in one batch (batch-wide keys): every
-    scene's state equals its standalone run bit for bit."""
+@pytest.mark.parametrize("gc", [1, 0])
+def test_batched_crowded_scenes_match_standalone(lib, gc):
+    """Crowded cells of several scenes in one batch (batch-wide keys and
+    rows): every scene's state equals its standalone run bit for bit."""
     scenes = [crowded_scene(seed=s, anchors=[[0.0, -40.0 - 5.0 * (s - 7), 0.0]]) for s in (7, 8)]
     sim = bcs.Simulation(scenes)
+    sim.set_tuning(step_shape=3, grid_collisions=gc)
     sim.set_particles(np.concatenate([s.positions for s in scenes]), np.concatenate([s.velocities for s in scenes]))
     sim.step(3)
     got = sim.get_particles()
-    assert sim.crowded_particles() > 0
+    assert (sim.crowded_particles() > 0) == (gc == 0)
     for k, sc in enumerate(scenes):
         z = sim.scene_info(k)
         rows = slice(z.particle_start, z.particle_start + z.particle_count)
-        alone = make(sc)
+        alone = make(sc, grid_collisions=gc)
         alone.step(3)
         for a, b in zip(got, alone.get_particles()):
             np.testing.assert_array_equal(a[rows], b)

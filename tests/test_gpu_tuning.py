@@ -41,7 +41,7 @@ def run(sc, frames, tuning=None, phases=False, autotune_first=0):
     return sim
 
 
-FLAGS = ("persistent", "spatial_order", "full_sort", "occupancy_filter", "sorted_positions")
+FLAGS = ("persistent", "spatial_order", "full_sort", "occupancy_filter", "sorted_positions", "grid_collisions")
 # every shape with every flag off and every flag on, and every flag
 # combination on the default shape
 ALL = ([dict(step_shape=a, **{f: b for f in FLAGS}) for a in range(len(bcs.STEP_SHAPES)) for b in (0, 1)] +
@@ -52,12 +52,15 @@ ALL = ([dict(step_shape=a, **{f: b for f in FLAGS}) for a in range(len(bcs.STEP_
 def test_default_tuning(lib):
     t = bcs.Simulation(scene()).get_tuning().as_dict()
     assert t == dict(step_shape=3, persistent=0, spatial_order=0, full_sort=0, occupancy_filter=0,
-                     sorted_positions=0)
+                     sorted_positions=0, grid_collisions=1)
 
 
 @pytest.mark.parametrize("tuning", ALL, ids=lambda t: "s{step_shape}p{persistent}o{spatial_order}f{full_sort}b{occupancy_filter}"
-                         "x{sorted_positions}".format(**t))
+                         "x{sorted_positions}g{grid_collisions}".format(**t))
 def test_every_tuning_same_state(lib, tuning):
+    """No particle of this scene is crowded, so the grid-order collision
+    kernel and the step kernel's own stencil search sum the same candidates
+    in the same order."""
     sc = scene()
     frames = 12
     want = run(sc, frames).get_particles()
@@ -117,11 +120,11 @@ def test_invalid_tuning_rejected(lib):
     sim = bcs.Simulation(scene())
     for bad in (dict(step_shape=len(bcs.STEP_SHAPES)), dict(step_shape=-1), dict(persistent=2),
                 dict(spatial_order=-1), dict(full_sort=3), dict(occupancy_filter=2),
-                dict(sorted_positions=-1)):
+                dict(sorted_positions=-1), dict(grid_collisions=3)):
         with pytest.raises(bcs.BcsError):
             sim.set_tuning(**bad)
     assert sim.get_tuning().as_dict() == dict(step_shape=3, persistent=0, spatial_order=0, full_sort=0,
-                                              occupancy_filter=0, sorted_positions=0)
+                                              occupancy_filter=0, sorted_positions=0, grid_collisions=1)
 
 
 def test_tuning_survives_set_particles_between_phases(lib):
@@ -132,7 +135,8 @@ def test_tuning_survives_set_particles_between_phases(lib):
     rng = np.random.default_rng(9)
     pos2 = sc.positions + rng.normal(0, 0.05, sc.positions.shape).astype(np.float32)
     out = []
-    for t in (dict(), dict(sorted_positions=1, occupancy_filter=1)):
+    for t in (dict(), dict(sorted_positions=1, occupancy_filter=1, grid_collisions=0),
+              dict(grid_collisions=0)):
         sim = bcs.Simulation(sc)
         sim.set_particles(sc.positions, sc.velocities)
         sim.set_tuning(**t)
@@ -141,5 +145,6 @@ def test_tuning_survives_set_particles_between_phases(lib):
         sim.calculate_next_frame()
         sim.propagate_all()
         out.append(sim.get_particles())
-    for a, b in zip(*out):
-        np.testing.assert_array_equal(a, b)
+    for other in out[1:]:
+        for a, b in zip(other, out[0]):
+            np.testing.assert_array_equal(a, b)

@@ -67,6 +67,37 @@ def test_static_sort_matches_allocating_path_twice(lib):
     np.testing.assert_array_equal(si1, i1)
 
 
+def static_error_word(lib):
+    w = C.c_uint32(0xFFFFFFFF)
+    st = lib.bcs_grid_sort_static_error_word(None, C.byref(w))
+    assert st == 0, bcs.STATUS.get(st, st)
+    return w.value
+
+
+def test_static_sort_reports_out_of_box_positions(lib):
+    """A position outside the grid box is clamped to the edge cell, as on the
+    allocating path, and the call's error word says so; the next in-box call
+    clears it."""
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    bcs.set_device(0)
+    scene = S.straight_scene(cells=64, seed=23)
+    pos = scene.positions.copy()
+    k_in, i_in, b, c = allocating_grid(scene, pos)
+    out = pos.copy()
+    out[7] = (b[1] + 5.0, b[3] + 3.0, b[5] + 9.0)    # beyond every max face
+    out[11] = (b[0] - 2.0, 0.5 * (b[2] + b[3]), b[4] - 1.0)
+    k_out, i_out, _, _ = allocating_grid(scene, out)
+    sk, si = static_grid(lib, out, b, c)
+    np.testing.assert_array_equal(sk, k_out)
+    np.testing.assert_array_equal(si, i_out)
+    assert static_error_word(lib) == bcs.ERRW_OUT_OF_GRID
+    sk, si = static_grid(lib, pos, b, c)
+    np.testing.assert_array_equal(sk, k_in)
+    np.testing.assert_array_equal(si, i_in)
+    assert static_error_word(lib) == 0
+
+
 def test_static_sort_rejects_oversize(lib):
     fp = C.POINTER(C.c_float)
     b = np.zeros(6, np.float32)

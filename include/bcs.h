@@ -284,7 +284,8 @@ typedef struct bcs_tuning {
                               sorted copies of positions and velocities: 0 = off (the step
                               kernel searches each stencil), 1 = each row's window found by
                               a linear scan from the row's first slot, 2 = by a binary
-                              search of the row's keys */
+                              search of the row's keys, 3 = the same on the candidates
+                              staged in shared memory per block of sorted slots */
 } bcs_tuning;
 #define BCS_STEP_SHAPES 6
 

@@ -18,7 +18,8 @@ LIB_PATH = os.path.join(HERE, "libbcs.so")
 
 BCS_OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "out of device memory",
-          4: "no CUDA device", 5: "unsupported"}
+          4: "no CUDA device", 5: "unsupported", 6: "a bounded device wait expired"}
+ERR_TIMEOUT = 6
 GRID_UNIFORM, GRID_NONE = 0, 1
 MEM_HOST, MEM_DEVICE = 0, 1
 ERRW_OUT_OF_GRID, ERRW_NAN_NORMALIZE, ERRW_NONFINITE = 1, 2, 4
@@ -35,7 +36,7 @@ EXPORTED = [
     "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
     "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales", "bcs_time_macro_steps",
     "bcs_init_particles", "bcs_set_tensor_path", "bcs_tensor_wait_expiries", "bcs_get_particles_async",
-    "bcs_wait_particles", "bcs_get_crowded",
+    "bcs_wait_particles", "bcs_get_crowded", "bcs_set_tensor_wait_probe",
 ]
 INIT_REFERENCE, INIT_LATTICE = 0, 1
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
@@ -183,6 +184,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_init_particles": ([P, C.POINTER(InitDesc)], C.c_int),
         "bcs_set_tensor_path": ([C.c_int], C.c_int),
         "bcs_tensor_wait_expiries": ([], C.c_uint),
+        "bcs_set_tensor_wait_probe": ([C.c_int], C.c_int),
         "bcs_surrogate_create": ([P, C.POINTER(SurrogateDesc), C.POINTER(P)], C.c_int),
         "bcs_surrogate_destroy": ([P], C.c_int),
         "bcs_surrogate_collect": ([P, C.c_int], C.c_int),
@@ -314,6 +316,13 @@ def set_tensor_path(path: int) -> int:
 
 def tensor_wait_expiries() -> int:
     return int(load_library().bcs_tensor_wait_expiries())
+
+
+def set_tensor_wait_probe(polls: int) -> None:
+    """Testing aid: with polls > 0 the first product wait of every CTA of the
+    tcgen05 kernels gives up after that many polls of a barrier nothing
+    arrives at; 0 restores the normal waits."""
+    _check(load_library().bcs_set_tensor_wait_probe(int(polls)), "bcs_set_tensor_wait_probe")
 
 
 def set_device(device: int) -> None:
@@ -540,7 +549,7 @@ class Simulation:
         return t
 
     def set_tuning(self, step_shape=0, persistent=0, spatial_order=0, full_sort=0, occupancy_filter=0,
-                   sorted_positions=0, grid_collisions=1) -> None:
+                   sorted_positions=0, grid_collisions=3) -> None:
         t = Tuning(int(step_shape), int(persistent), int(spatial_order), int(full_sort), int(occupancy_filter),
                    int(sorted_positions), int(grid_collisions))
         _check(self.lib.bcs_set_tuning(self.h, C.byref(t)), "bcs_set_tuning")

@@ -36,6 +36,8 @@ void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigne
 void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s);
 void launch_row_starts(const int* keys, int n, const SceneDev* scenes, int scene_count, long long rows, int* row_start,
                        cudaStream_t s);
+void launch_tri_occupancy(const int4* table, const int* epoch, const SceneDev* scenes, int scene_count, long long cells,
+                          unsigned* occ, cudaStream_t s);
 void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
                          cudaStream_t s);
 void launch_vein_end(const StepArgs& a, int cells, cudaStream_t s);
@@ -181,6 +183,7 @@ struct bcs_sim {
     uint32_t* tri = nullptr;
     float4* tcache = nullptr;
     float4* tbox = nullptr;         // 2 per triangle-grid cell
+    unsigned* tocc = nullptr;       // per triangle-grid cell: occupied stencil neighbours
     unsigned char* wall_mask = nullptr;
     int* wall_epoch = nullptr;
     float* wall_disp2 = nullptr;     // dynamic wall: max squared vertex move since the last bounds build
@@ -372,6 +375,7 @@ void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
     a.tg = s->tg.g;
     a.tcache = s->tcache;
     a.tbox = s->tbox;
+    a.tocc = s->tocc;
     a.wall_mask = s->wall_mask;
     a.wall_epoch = s->wall_epoch;
 }
@@ -384,6 +388,8 @@ void build_triangle_grid(bcs_sim* s, bool regrid) {
         if (regrid) {
             launch_tri_keys(s->vpos, s->tri, s->T, s->scenes, s->S, s->tg.in_k, s->tg.in_v, s->stream);
             sort_grid(s->tg, s->stream);
+            if (s->tocc)
+                launch_tri_occupancy(s->tg.table, s->tg.epoch, s->scenes, s->S, s->tg.g.cells, s->tocc, s->stream);
         }
         launch_tri_cache(s->tg.g.ids, s->tri, s->vpos, s->T, s->tcache, s->stream);
         launch_tri_boxes(s->tg.g.keys, s->tg.g.ids, s->T, s->tri, s->vpos, s->tbox, s->scenes, s->S, s->wall_mask,
@@ -628,7 +634,7 @@ bool tuning_valid(const bcs_sim* s, const bcs_tuning& t) {
     return t.step_shape >= 0 && t.step_shape < kStepShapes && kShapes[t.step_shape].chunk >= s->max_pic &&
            (t.persistent == 0 || t.persistent == 1) && (t.spatial_order == 0 || t.spatial_order == 1) &&
            (t.full_sort == 0 || t.full_sort == 1) && (t.occupancy_filter == 0 || t.occupancy_filter == 1) &&
-           (t.sorted_positions == 0 || t.sorted_positions == 1) && t.grid_collisions >= 0 && t.grid_collisions <= 2;
+           (t.sorted_positions == 0 || t.sorted_positions == 1) && t.grid_collisions >= 0 && t.grid_collisions <= 3;
 }
 
 bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
@@ -666,7 +672,7 @@ bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
     s->pg.g.row_start = gc && s->pg.sorted_once ? s->pg.row_start : nullptr;
     s->args.pg = s->pg.g;
     s->args.coll = gc && s->pg.g.row_start && s->pg.g.spos && s->pg.g.svel ? s->coll : nullptr;
-    s->args.collide_search = t.grid_collisions == 2 ? 1 : 0;
+    s->args.collide_search = t.grid_collisions >= 2 ? t.grid_collisions - 1 : 0;
     s->persistent_grid[0] = t.persistent ? step_persistent_grid(0, t.step_shape) : 0;
     s->persistent_grid[1] = t.persistent ? step_persistent_grid(1, t.step_shape) : 0;
     drop_graphs(s);
@@ -922,7 +928,9 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     s->tg.count = s->T;
     s->tg.g.count = s->T;
     if (tuniform) {
-        if ((st = dalloc(s, &s->tbox, 2 * (size_t)std::max(1LL, tkey_total)))) return st;
+        if ((st = dalloc(s, &s->tbox, 2 * (size_t)std::max(1LL, tkey_total))) ||
+            (st = dalloc(s, &s->tocc, (size_t)std::max(1LL, tkey_total))))
+            return st;
         if (s->p.vein_dynamic && s->T > 0) {
             if ((st = dalloc(s, &s->wall_disp2, 1)) || (st = dalloc(s, &s->wall_ref, s->V))) return st;
             const float huge = 3.0e38f;
@@ -966,7 +974,7 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     // ---- default launch: 256 threads / 512 particles / 4 CTAs per SM (the
     // fastest shape at the 4.2M-particle bifurcation), else the first shape
     // that holds the largest cell
-    bcs_tuning t{kDefaultShape, 0, 0, 0, 0, 0, 1};
+    bcs_tuning t{kDefaultShape, 0, 0, 0, 0, 0, 3};
     if (kShapes[t.step_shape].chunk < s->max_pic) {
         t.step_shape = 0;
         while (kShapes[t.step_shape].chunk < s->max_pic) ++t.step_shape;
@@ -1765,7 +1773,7 @@ bcs_status bcs_autotune(bcs_sim* s, int frames, bcs_tuning* chosen, float* ms_pe
     int bcs_tuning::*fields[] = {&bcs_tuning::step_shape, &bcs_tuning::persistent, &bcs_tuning::spatial_order,
                                  &bcs_tuning::full_sort, &bcs_tuning::occupancy_filter,
                                  &bcs_tuning::sorted_positions, &bcs_tuning::grid_collisions};
-    const int limits[] = {kStepShapes, 2, 2, 2, 2, 2, 3};
+    const int limits[] = {kStepShapes, 2, 2, 2, 2, 2, 4};
     constexpr int kFields = sizeof(limits) / sizeof(limits[0]);
     for (int sweep = 0; sweep < 2 && st == BCS_OK; ++sweep) {
         bool improved = false;

@@ -35,8 +35,14 @@
 //   tbox                     2 float4 per triangle-grid cell: bounds of the
 //                            cell's triangles widened by the rebuild margin,
 //                            for ray culling
+//   tocc                     uint32 per triangle-grid cell: bit 9 (dx + 1) +
+//                            3 (dy + 1) + (dz + 1) set when that stencil
+//                            neighbour exists and holds triangles (rebuilt
+//                            with the triangle grid)
 //   wall_mask                uint8 per wall-mask cell: the mask epoch where a
-//                            triangle lies within vein_impact_distance of the cell
+//                            triangle lies within vein_impact_distance (plus
+//                            the rebuild margin) of the cell's centre, widened
+//                            by the cell's half-diagonal
 //   scenes, types, work      per-scene geometry, per (scene, cell type) ranges,
 //                            per-CTA work items (device arrays)
 #pragma once
@@ -150,7 +156,8 @@ struct StepArgs {
     float4* coll;         // grid-order collisions: each particle's collision force, written by
                           // k_collide before the step kernel reads it; null: the step kernel
                           // searches the stencil itself
-    int collide_search;   // grid-order collisions: 1 = binary search of each row window, 0 = linear scan
+    int collide_search;   // grid-order collisions: 0 = linear scan of each row window, 1 = binary
+                          // search, 2 = binary search on candidates staged in shared memory
     const TypeDev* types;
     int type_count;
     const SceneDev* scenes;
@@ -168,6 +175,7 @@ struct StepArgs {
     const uint32_t* tri;  // 3 * T vertex indices (batch-wide)
     const float4* tcache; // 3 per sorted triangle slot
     const float4* tbox;   // 2 per triangle-grid cell
+    const unsigned* tocc; // per triangle-grid cell: which of its 27 stencil cells hold triangles, or null
     const unsigned char* wall_mask;
     const int* wall_epoch;
     int T;

@@ -447,20 +447,33 @@ __device__ inline void vein_collision(const StepArgs& a, const SceneDev& sc, flo
         const long long cxy = (long long)geo.cx * geo.cy;
         // Stencil cell k = 9 (dx + 1) + 3 (dy + 1) + (dz + 1): stencil order
         // (x, then y, then z).  Pass 0: which cells are in the stencil and
-        // hold triangles; the 27 table reads are independent, so they are
-        // in flight together.
+        // hold triangles: the cell's precomputed neighbour word masked by
+        // the particle's stencil edges, or the 27 table reads (independent,
+        // in flight together).
         unsigned occ = 0u;
+        if (a.tocc) {
+            // neighbour-word bits of the dx, dy and dz values
+            constexpr unsigned kDx[3] = {0x000001FFu, 0x0003FE00u, 0x07FC0000u};
+            constexpr unsigned kDy[3] = {0x001C0E07u, 0x00E07038u, 0x070381C0u};
+            constexpr unsigned kDz[3] = {0x01249249u, 0x02492492u, 0x04924924u};
+            const unsigned mx = (x0 < 0 ? kDx[0] : 0u) | kDx[1] | (x1 > 0 ? kDx[2] : 0u);
+            const unsigned my = (y0 < 0 ? kDy[0] : 0u) | kDy[1] | (y1 > 0 ? kDy[2] : 0u);
+            const unsigned mz = (z0 < 0 ? kDz[0] : 0u) | kDz[1] | (z1 > 0 ? kDz[2] : 0u);
+            occ = __ldg(&a.tocc[geo.key_offset + cellId]) & mx & my & mz;
+        } else {
 #pragma unroll
-        for (int dx = -1; dx <= 1; ++dx)
+            for (int dx = -1; dx <= 1; ++dx)
 #pragma unroll
-            for (int dy = -1; dy <= 1; ++dy)
+                for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
-                for (int dz = -1; dz <= 1; ++dz) {
-                    if (dx < x0 || dx > x1 || dy < y0 || dy > y1 || dz < z0 || dz > z1) continue;
-                    const long long c = (long long)cellId + dz * cxy + (long long)dy * geo.cx + dx;
-                    if (c < 0 || c >= geo.cells) continue;
-                    if (__ldg(&g.table[geo.key_offset + c]).z == ep) occ |= 1u << (9 * (dx + 1) + 3 * (dy + 1) + dz + 1);
-                }
+                    for (int dz = -1; dz <= 1; ++dz) {
+                        if (dx < x0 || dx > x1 || dy < y0 || dy > y1 || dz < z0 || dz > z1) continue;
+                        const long long c = (long long)cellId + dz * cxy + (long long)dy * geo.cx + dx;
+                        if (c < 0 || c >= geo.cells) continue;
+                        if (__ldg(&g.table[geo.key_offset + c]).z == ep)
+                            occ |= 1u << (9 * (dx + 1) + 3 * (dy + 1) + dz + 1);
+                    }
+        }
         // Pass 1: which of them the ray enters, and the last one it enters
         // within reach.
         const float3 inv = f3(__frcp_rn(dir.x), __frcp_rn(dir.y), __frcp_rn(dir.z));
@@ -929,9 +942,7 @@ __global__ void k_row_starts(const int* __restrict__ keys, int n, const SceneDev
 constexpr int kCollideThreads = 256;
 
 template <int SEARCH>
-__global__ void __launch_bounds__(kCollideThreads) k_collide(const StepArgs a) {
-    const int j = blockIdx.x * kCollideThreads + threadIdx.x;
-    if (j >= a.n) return;
+__device__ inline void collide_slot(const StepArgs& a, int j) {
     const GridDev& g = a.pg;
     const int s = find_range(a.scene_count, j, [&](int k) { return a.scenes[k].particle_start; });
     const SceneDev& sc = a.scenes[s];
@@ -999,6 +1010,144 @@ __global__ void __launch_bounds__(kCollideThreads) k_collide(const StepArgs a) {
                     collide(a, x, v, R, __ldg(&g.spos[t]), [&g, t] { return __ldg(&g.svel[t]); }, acc, e);
             }
     }
+    a.coll[__ldg(&g.ids[j])] = make_float4(acc.x, acc.y, acc.z, 0.f);
+    if (e) atomicOr(a.err, e);
+}
+
+template <int SEARCH>
+__global__ void __launch_bounds__(kCollideThreads) k_collide(const StepArgs a) {
+    const int j = blockIdx.x * kCollideThreads + threadIdx.x;
+    if (j < a.n) collide_slot<SEARCH>(a, j);
+}
+
+// The same sum with the candidates staged in shared memory.  A CTA takes
+// kTileSlots consecutive sorted slots of one plane of one scene (grid rows
+// yf..yl of plane z).  Every stencil row of its particles lies in planes
+// z - 1 .. z + 1, rows yf - 1 .. yl + 1, and those rows of a plane are one
+// contiguous slot range: the CTA stages the three ranges' keys, positions
+// and velocities and the rows' first slots, then every thread runs the
+// nine binary searches and its windows' candidates on shared memory.  Same
+// candidates, same order, same sum as collide_slot.  A tile that spans two
+// planes or scenes, or whose ranges exceed kTileStage slots (crowded rows),
+// takes the global-memory search instead; so does a particle whose stencil
+// does not follow its sorted key.
+constexpr int kTileSlots = 256;
+constexpr int kTileStage = 1408;     // staged slots: 1408 x 36 B
+constexpr int kTileRows = 40;        // grid rows staged per plane
+constexpr size_t kTileSmem = (size_t)kTileStage * (2 * sizeof(float4) + sizeof(int)) + 3 * (kTileRows + 1) * sizeof(int);
+
+__global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a) {
+    extern __shared__ __align__(16) unsigned char tile_smem[];
+    float4* s_pos = reinterpret_cast<float4*>(tile_smem);
+    float4* s_vel = s_pos + kTileStage;
+    int* s_key = reinterpret_cast<int*>(s_vel + kTileStage);
+    int* s_row = s_key + kTileStage;   // [3][kTileRows + 1]: staged offset of each row's first slot
+    __shared__ int s_ok, s_scene, s_z, s_ylo, s_nrows, s_total;
+    __shared__ int s_A[3], s_base[4];
+    const GridDev& g = a.pg;
+    const int s0 = blockIdx.x * kTileSlots, j = s0 + threadIdx.x;
+    const int last = min(s0 + kTileSlots, a.n) - 1;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const int sc_i = find_range(a.scene_count, s0, [&](int k) { return a.scenes[k].particle_start; });
+        const SceneDev& sc = a.scenes[sc_i];
+        const GridGeom& geo = sc.pg;
+        const int cxy = geo.cx * geo.cy;
+        const int kf = __ldg(&g.keys[s0]) - (int)geo.key_offset, kl = __ldg(&g.keys[last]) - (int)geo.key_offset;
+        const int zf = kf / cxy, zl = kl / cxy;
+        const int yf = (kf - zf * cxy) / geo.cx, yl = (kl - zl * cxy) / geo.cx;
+        const int ylo = max(yf - 1, 0), yhi = min(yl + 1, geo.cy - 1);
+        if (last >= sc.particle_end || zf != zl || yhi - ylo + 1 > kTileRows) ok = 0;
+        int total = 0;
+        for (int p = 0; p < 3 && ok; ++p) {
+            const int z = zf + p - 1;
+            s_base[p] = total;
+            s_A[p] = 0;
+            if (z < 0 || z >= geo.cz) continue;
+            const int r0 = (int)geo.row_offset + z * geo.cy;
+            const int A = __ldg(&g.row_start[r0 + ylo]), B = __ldg(&g.row_start[r0 + yhi + 1]);
+            s_A[p] = A;
+            total += B - A;
+        }
+        s_base[3] = total;
+        if (total > kTileStage) ok = 0;
+        s_ok = ok;
+        s_scene = sc_i;
+        s_z = zf;
+        s_ylo = ylo;
+        s_nrows = yhi - ylo + 1;
+        s_total = total;
+    }
+    __syncthreads();
+    if (!s_ok) {
+        if (j <= last) collide_slot<1>(a, j);
+        return;
+    }
+    const SceneDev& sc = a.scenes[s_scene];
+    const GridGeom& geo = sc.pg;
+    const int nrows = s_nrows, ylo = s_ylo, zc = s_z;
+    // the rows' first slots as staged offsets, then the three ranges
+    for (int q = threadIdx.x; q < 3 * (nrows + 1); q += kTileSlots) {
+        const int p = q / (nrows + 1), i = q - p * (nrows + 1);
+        const int z = zc + p - 1;
+        int off = s_base[p];
+        if (z >= 0 && z < geo.cz) off += __ldg(&g.row_start[(int)geo.row_offset + z * geo.cy + ylo + i]) - s_A[p];
+        s_row[p * (kTileRows + 1) + i] = off;
+    }
+    for (int q = threadIdx.x; q < s_total; q += kTileSlots) {
+        const int p = q < s_base[1] ? 0 : (q < s_base[2] ? 1 : 2);
+        const int slot = s_A[p] + (q - s_base[p]);
+        s_key[q] = __ldg(&g.keys[slot]);
+        s_pos[q] = __ldg(&g.spos[slot]);
+        s_vel[q] = __ldg(&g.svel[slot]);
+    }
+    __syncthreads();
+    if (j > last) return;
+    const int me = s_base[1] + (j - s_A[1]);
+    const float4 px = s_pos[me];
+    const float3 x = xyz(px), v = xyz(s_vel[me]);
+    const float R = px.w;
+    const Stencil st = particle_stencil(geo, x);
+    const bool inside = st.ix + st.x0 >= 0 && st.ix + st.x1 <= geo.cx - 1 && st.iy + st.y0 >= 0 &&
+                        st.iy + st.y1 <= geo.cy - 1 && st.iz + st.z0 >= 0 && st.iz + st.z1 <= geo.cz - 1;
+    // the stencil's rows among the staged ones (a particle whose stencil
+    // does not follow its sorted key, after bcs_set_particles, searches globally)
+    if (!inside || st.iz != zc || st.iy + st.y0 < ylo || st.iy + st.y1 > ylo + nrows - 1) {
+        collide_slot<1>(a, j);
+        return;
+    }
+    int lo[9], hi[9], end[9], wlo[9];
+    const int kbase = (int)geo.key_offset;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const int dz = r / 3 - 1, dy = r % 3 - 1;
+        lo[r] = hi[r] = end[r] = 0;
+        wlo[r] = 0;
+        if (dz < st.z0 || dz > st.z1 || dy < st.y0 || dy > st.y1) continue;
+        const int i = st.iy + dy - ylo;   // the window's row among the staged ones
+        wlo[r] = kbase + ((st.iz + dz) * geo.cy + st.iy + dy) * geo.cx + st.ix + st.x0;
+        lo[r] = s_row[(dz + 1) * (kTileRows + 1) + i];
+        hi[r] = end[r] = s_row[(dz + 1) * (kTileRows + 1) + i + 1];
+    }
+    for (bool more = true; more;) {
+        more = false;
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            if (lo[r] < hi[r]) {
+                const int m = (lo[r] + hi[r]) >> 1;
+                if (s_key[m] < wlo[r]) lo[r] = m + 1;
+                else hi[r] = m;
+                more |= lo[r] < hi[r];
+            }
+        }
+    }
+    float3 acc = f3(0.f, 0.f, 0.f);
+    unsigned e = 0;
+    const int wx = st.x1 - st.x0;
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+        for (int t = lo[r]; t < end[r] && s_key[t] - wlo[r] <= wx; ++t)
+            collide(a, x, v, R, s_pos[t], [s_vel, t] { return s_vel[t]; }, acc, e);
     a.coll[__ldg(&g.ids[j])] = make_float4(acc.x, acc.y, acc.z, 0.f);
     if (e) atomicOr(a.err, e);
 }
@@ -2109,6 +2258,100 @@ __global__ void k_tri_boxes(const int* __restrict__ keys, const int* __restrict_
             for (int xx = x0; xx <= x1; ++xx) mask[m.offset + ((long long)z * m.ny + y) * m.nx + xx] = mark;
 }
 
+// Per triangle-grid cell, the 27-bit word of its stencil neighbours that
+// exist (key inside the scene's grid, the reference's key arithmetic) and
+// hold triangles in the current build: bit 9 (dx + 1) + 3 (dy + 1) + dz + 1.
+__global__ void k_tri_occupancy(const int4* __restrict__ table, const int* __restrict__ epoch,
+                                const SceneDev* __restrict__ scenes, int scene_count, long long cells, unsigned* occ) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cells) return;
+    const int sidx = find_range(scene_count, k, [&](int q) { return scenes[q].tg.key_offset; });
+    const GridGeom& geo = scenes[sidx].tg;
+    const long long c = k - geo.key_offset, cxy = (long long)geo.cx * geo.cy;
+    const int ep = *epoch;
+    unsigned w = 0u;
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dz = -1; dz <= 1; ++dz) {
+                const long long n = c + dz * cxy + (long long)dy * geo.cx + dx;
+                if (n >= 0 && n < geo.cells && table[geo.key_offset + n].z == ep)
+                    w |= 1u << (9 * (dx + 1) + 3 * (dy + 1) + dz + 1);
+            }
+    occ[k] = w;
+}
+
+// Squared distance from p to the triangle (a, b, c): the closest point by
+// its Voronoi region (vertex, edge or face), the method of Ericson, Real-Time
+// Collision Detection (2005), section 5.1.5.
+__device__ inline float point_triangle_d2(float3 p, float3 a, float3 b, float3 c) {
+    const float3 ab = b - a, ac = c - a, ap = p - a;
+    const float d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+    float3 q;
+    if (d1 <= 0.f && d2 <= 0.f) {
+        q = a;
+    } else {
+        const float3 bp = p - b;
+        const float d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+        const float3 cp = p - c;
+        const float d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+        const float vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+        if (d3 >= 0.f && d4 <= d3) q = b;
+        else if (d6 >= 0.f && d5 <= d6) q = c;
+        else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) q = a + (d1 / (d1 - d3)) * ab;
+        else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) q = a + (d2 / (d2 - d6)) * ac;
+        else if (va <= 0.f && d4 - d3 >= 0.f && d5 - d6 >= 0.f) q = b + ((d4 - d3) / ((d4 - d3) + (d5 - d6))) * (c - b);
+        else {
+            const float den = 1.f / (va + vb + vc);
+            q = a + (vb * den) * ab + (vc * den) * ac;
+        }
+    }
+    const float3 d = p - q;
+    return dot3(d, d);
+}
+
+// Wall mask from the triangles themselves: a mask cell is marked when its
+// centre lies within reach (the impact distance, with the rebuild margin)
+// plus the cell's half-diagonal of some triangle, so every point of an
+// unmarked cell is farther than reach from every triangle: a particle there
+// cannot be hit within the impact distance.  One thread per triangle over
+// the cells of its widened bounds; a distance that does not come out finite
+// (a degenerate triangle) marks the cell.
+__global__ void k_wall_mask_tris(const uint32_t* __restrict__ tri, const float4* __restrict__ vpos, int T,
+                                 const SceneDev* __restrict__ scenes, int scene_count, unsigned char* mask,
+                                 const int* __restrict__ mask_epoch, float reach, float margin,
+                                 const float* __restrict__ disp2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T) return;
+    if (disp2 && *disp2 <= margin * margin) return;   // the last build still covers the wall
+    const int sidx = find_range(scene_count, t, [&](int q) { return scenes[q].tri_start; });
+    const MaskGeom& m = scenes[sidx].wall;
+    const float3 a = xyz(vpos[tri[3 * t]]), b = xyz(vpos[tri[3 * t + 1]]), c = xyz(vpos[tri[3 * t + 2]]);
+    const float cell = 1.0f / m.inv_cell;
+    const float big = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(b.x))),
+                            fmaxf(fmaxf(fabsf(b.y), fabsf(b.z)), fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z))));
+    const float r = reach + 0.8661f * cell + 1e-3f + 1e-5f * big;
+    const float r2 = r * r;
+    const float3 lo = f3(fminf(a.x, fminf(b.x, c.x)) - r, fminf(a.y, fminf(b.y, c.y)) - r, fminf(a.z, fminf(b.z, c.z)) - r);
+    const float3 hi = f3(fmaxf(a.x, fmaxf(b.x, c.x)) + r, fmaxf(a.y, fmaxf(b.y, c.y)) + r, fmaxf(a.z, fmaxf(b.z, c.z)) + r);
+    const int x0 = max(0, (int)floorf((lo.x - m.lo[0]) * m.inv_cell)), x1 = min(m.nx - 1, (int)floorf((hi.x - m.lo[0]) * m.inv_cell));
+    const int y0 = max(0, (int)floorf((lo.y - m.lo[1]) * m.inv_cell)), y1 = min(m.ny - 1, (int)floorf((hi.y - m.lo[1]) * m.inv_cell));
+    const int z0 = max(0, (int)floorf((lo.z - m.lo[2]) * m.inv_cell)), z1 = min(m.nz - 1, (int)floorf((hi.z - m.lo[2]) * m.inv_cell));
+    const unsigned char mark = (unsigned char)*mask_epoch;
+    // a (nearly) degenerate triangle marks its whole widened bounds
+    const float3 n = cross3(b - a, c - a);
+    const bool flat = !(dot3(n, n) > 1e-10f * dot3(b - a, b - a) * dot3(c - a, c - a));
+    for (int z = z0; z <= z1; ++z)
+        for (int y = y0; y <= y1; ++y)
+            for (int xx = x0; xx <= x1; ++xx) {
+                const float3 p = f3(m.lo[0] + (xx + 0.5f) * cell, m.lo[1] + (y + 0.5f) * cell, m.lo[2] + (z + 0.5f) * cell);
+                if (flat || !(point_triangle_d2(p, a, b, c) > r2))
+                    mask[m.offset + ((long long)z * m.ny + y) * m.nx + xx] = mark;
+            }
+}
+
 // Largest squared displacement of any vein vertex since the last bounds
 // build (as the int bits of a non-negative float, so atomicMax orders it).
 __global__ void k_vein_disp(const float4* __restrict__ vpos, const float4* __restrict__ ref, int V, float* disp2) {
@@ -2224,8 +2467,18 @@ void launch_step(const StepArgs& a, int items, int mode, int shape, int persiste
     const int blocks = persistent ? std::min(items, persistent_grid) : items;
     if (a.coll && a.pg.uniform && a.pg.row_start && a.pg.spos && a.pg.svel && a.n > 0) {
         const int blocks = (a.n + kCollideThreads - 1) / kCollideThreads;
-        if (a.collide_search) k_collide<1><<<blocks, kCollideThreads, 0, s>>>(a);
-        else k_collide<0><<<blocks, kCollideThreads, 0, s>>>(a);
+        if (a.collide_search == 2) {
+            static bool attr = false;
+            if (!attr) {
+                cudaFuncSetAttribute(k_collide_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTileSmem);
+                attr = true;
+            }
+            k_collide_tile<<<(a.n + kTileSlots - 1) / kTileSlots, kTileSlots, kTileSmem, s>>>(a);
+        } else if (a.collide_search) {
+            k_collide<1><<<blocks, kCollideThreads, 0, s>>>(a);
+        } else {
+            k_collide<0><<<blocks, kCollideThreads, 0, s>>>(a);
+        }
     }
     step_kernel_for(mode, shape, persistent)<<<blocks, kShapes[shape].threads, 0, s>>>(a);
     if (!a.pg.uniform || a.coll) return;   // no stencil, or no crowded particles set aside
@@ -2280,13 +2533,22 @@ void launch_tri_boxes(const int* keys, const int* ids, int T, const uint32_t* tr
                       float margin, float* disp2, float4* vref, int V, cudaStream_t s) {
     if (disp2) k_vein_disp<<<BCS_GRID1(V, 256), 0, s>>>(vpos, vref, V, disp2);
     if (mask) k_next_epoch_if<<<1, 1, 0, s>>>(mask_epoch, disp2, margin);
-    if (T > 0)
-        k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box, scenes, scene_count, mask, mask_epoch,
+    if (T > 0) {
+        // boxes per cell; the mask from the triangles themselves
+        k_tri_boxes<<<BCS_GRID1(T, 256), 0, s>>>(keys, ids, T, tri, vpos, box, scenes, scene_count, nullptr, mask_epoch,
                                                  reach + margin, margin, disp2);
+        if (mask)
+            k_wall_mask_tris<<<BCS_GRID1(T, 128), 0, s>>>(tri, vpos, T, scenes, scene_count, mask, mask_epoch,
+                                                           reach + margin, margin, disp2);
+    }
     if (disp2) {
         k_vein_snapshot<<<BCS_GRID1(V, 256), 0, s>>>(vpos, vref, V, disp2, margin);
         k_disp_reset<<<1, 1, 0, s>>>(disp2, margin);
     }
+}
+void launch_tri_occupancy(const int4* table, const int* epoch, const SceneDev* scenes, int scene_count, long long cells,
+                          unsigned* occ, cudaStream_t s) {
+    if (cells > 0) k_tri_occupancy<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(table, epoch, scenes, scene_count, cells, occ);
 }
 void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, const int* nb_ids, const float* nb_len,
                          int V, float k, float d, unsigned* err, cudaStream_t s) {

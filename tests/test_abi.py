@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_status_strings_and_version(lib):
-    assert lib.bcs_abi_version() == 2
+    assert lib.bcs_abi_version() == 3
     assert lib.bcs_status_string(0) == b"ok"
     assert lib.bcs_status_string(3) == b"out of device memory"
 

@@ -1,9 +1,11 @@
 """Crowded particles.  Two collision paths take them:
 
-  * grid order (the default, tuning grid_collisions = 1): k_collide gives
-    every sorted slot a thread; the particles of a crowded cell sit in
-    neighbouring lanes and share their whole stencil, so each lane sums its
-    candidates in stencil order with warp-uniform loops;
+  * grid order (tuning grid_collisions = 1, 2, 3): every sorted slot gets a
+    thread; the particles of a crowded cell sit in neighbouring lanes and
+    share their whole stencil, so each lane sums its candidates in stencil
+    order with warp-uniform loops (3 stages a block's candidates in shared
+    memory and falls back to the global search when a crowded block's rows
+    exceed its capacity);
   * cell order (grid_collisions = 0): a particle whose collision stencil
     holds more than 128 sorted slots is left by the step kernel to
     k_crowded: inside the grid box a warp takes its whole grid cell (the
@@ -105,7 +107,7 @@ def test_crowded_count(lib):
     assert sim.crowded_particles() > 2 * got
 
 
-@pytest.mark.parametrize("gc", [1, 0])
+@pytest.mark.parametrize("gc", [3, 2, 1, 0])
 def test_one_step_matches_oracle(lib, gc):
     sc = crowded_scene()
     sim = make(sc, grid_collisions=gc)
@@ -117,7 +119,7 @@ def test_one_step_matches_oracle(lib, gc):
         assert e <= 1e-5, f"{name}: relative error {e:.3e}"
 
 
-@pytest.mark.parametrize("gc", [1, 0])
+@pytest.mark.parametrize("gc", [3, 2, 1, 0])
 def test_few_steps_within_1e3_radius(lib, gc):
     sc = crowded_scene(vel=0.5)
     sim = make(sc, grid_collisions=gc)
@@ -132,7 +134,7 @@ def test_few_steps_within_1e3_radius(lib, gc):
 FLAGS = ("persistent", "spatial_order", "full_sort", "occupancy_filter", "sorted_positions")
 
 
-@pytest.mark.parametrize("gc", [1, 0])
+@pytest.mark.parametrize("gc", [3, 2, 1, 0])
 @pytest.mark.parametrize("shape", range(len(bcs.STEP_SHAPES)))
 @pytest.mark.parametrize("flags", [0, 1])
 def test_every_shape_same_state(lib, shape, flags, gc):
@@ -146,7 +148,7 @@ def test_every_shape_same_state(lib, shape, flags, gc):
         np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("gc", [1, 0])
+@pytest.mark.parametrize("gc", [3, 2, 1, 0])
 def test_split_phases_match_fused(lib, gc):
     sc = crowded_scene()
     a, b = make(sc, grid_collisions=gc), make(sc, occupancy_filter=1, sorted_positions=1, grid_collisions=gc)
@@ -159,7 +161,7 @@ def test_split_phases_match_fused(lib, gc):
         np.testing.assert_array_equal(x, y)
 
 
-@pytest.mark.parametrize("gc", [1, 0])
+@pytest.mark.parametrize("gc", [3, 2, 1, 0])
 def test_macro_steps_match_oracle(lib, gc):
     sc = crowded_scene(vel=0.5)
     sim = make(sc, grid_collisions=gc)
@@ -171,7 +173,7 @@ def test_macro_steps_match_oracle(lib, gc):
     assert rel_err(g[1], r[1]) <= 4e-4
 
 
-@pytest.mark.parametrize("gc", [1, 0])
+@pytest.mark.parametrize("gc", [3, 2, 1, 0])
 def test_crowded_outside_the_grid_box(lib, gc):
     """A pile beyond the grid box's top face: clamped keys, so those
     particles' stencils are not their cell's regular one (on the cell-order
@@ -197,7 +199,7 @@ def test_crowded_outside_the_grid_box(lib, gc):
 
 
 
-@pytest.mark.parametrize("gc", [1, 0])
+@pytest.mark.parametrize("gc", [3, 2, 1, 0])
 def test_batched_crowded_scenes_match_standalone(lib, gc):
     """Crowded cells of several scenes in one batch (batch-wide keys and
     rows): every scene's state equals its standalone run bit for bit."""

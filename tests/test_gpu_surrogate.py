@@ -228,6 +228,7 @@ def test_fused_inference_matches_layer_kernels(lib, trained):
 
 @pytest.mark.parametrize("path", [0, 1])
 def test_gradients_both_tensor_paths(lib, path):
+    expired = bcs.tensor_wait_expiries()
     prev = bcs.set_tensor_path(path)
     try:
         sc = sphere_scene()
@@ -244,7 +245,7 @@ def test_gradients_both_tensor_paths(lib, path):
         assert np.abs(y - M.forward(P, f, e, src, dst, 3, bf=True)).max() <= 2e-3 * (np.abs(y).max() + 1e-6)
     finally:
         bcs.set_tensor_path(prev)
-    assert bcs.tensor_wait_expiries() == 0
+    assert bcs.tensor_wait_expiries() == expired
 
 
 def test_tensor_paths_agree(lib):
@@ -283,3 +284,40 @@ def test_fused_inference_matches_layer_kernels_disc_cells(lib):
     assert sa["predicted_cells"] == sb["predicted_cells"] == 10
     for x, y in zip(a, b):
         assert np.abs(x - y).max() <= 1e-4 * (np.abs(y).max() + 1.0)
+
+
+def test_bounded_wait_gives_up_and_recovers(lib):
+    """The tcgen05 products' bounded completion wait, made to run out: with
+    the wait probe on, every CTA's first wait polls a barrier nothing arrives
+    at, gives up, counts the expiry and skips its product (it still waits,
+    bounded, for the products it issued before freeing tensor memory), and
+    the call reports BCS_ERR_TIMEOUT.  With the probe off the next call
+    matches the oracle again and counts nothing."""
+    prev = bcs.set_tensor_path(0)
+    try:
+        sc = sphere_scene()
+        sim = make(sc)
+        sur = bcs.Surrogate(sim, max_samples=64)
+        f, e, t, src, dst, P = random_case(sur, sc, 2, 21)
+        before = bcs.tensor_wait_expiries()
+        bcs.set_tensor_wait_probe(16)
+        try:
+            with pytest.raises(bcs.BcsError) as err:
+                sur.loss_grad(2, f, e, t)
+            assert err.value.status == bcs.ERR_TIMEOUT
+            with pytest.raises(bcs.BcsError) as err:
+                sur.forward(2, f, e)
+            assert err.value.status == bcs.ERR_TIMEOUT
+        finally:
+            bcs.set_tensor_wait_probe(0)
+        after = bcs.tensor_wait_expiries()
+        assert after > before
+        loss, g = sur.loss_grad(2, f, e, t)
+        lo, go = M.loss_and_grads(P, f, e, src, dst, t, 3, bf=True)
+        assert abs(loss - lo) <= 2e-3 * abs(lo)
+        gg = unflatten(g, 3)
+        for k in M.param_names(3):
+            assert np.linalg.norm(gg[k] - go[k]) <= 1e-2 * np.linalg.norm(go[k]) + 1e-7, k
+        assert bcs.tensor_wait_expiries() == after
+    finally:
+        bcs.set_tensor_path(prev)

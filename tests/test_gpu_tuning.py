@@ -46,13 +46,15 @@ FLAGS = ("persistent", "spatial_order", "full_sort", "occupancy_filter", "sorted
 # combination on the default shape
 ALL = ([dict(step_shape=a, **{f: b for f in FLAGS}) for a in range(len(bcs.STEP_SHAPES)) for b in (0, 1)] +
        [dict(step_shape=0, **dict(zip(FLAGS, bits))) for bits in itertools.product((0, 1), repeat=len(FLAGS))
-        if 0 < sum(bits) < len(FLAGS)])
+        if 0 < sum(bits) < len(FLAGS)] +
+       [dict(step_shape=a, persistent=a % 2, spatial_order=1 - a % 2, full_sort=0, occupancy_filter=0,
+             sorted_positions=a % 2, grid_collisions=g) for a in range(len(bcs.STEP_SHAPES)) for g in (2, 3)])
 
 
 def test_default_tuning(lib):
     t = bcs.Simulation(scene()).get_tuning().as_dict()
     assert t == dict(step_shape=3, persistent=0, spatial_order=0, full_sort=0, occupancy_filter=0,
-                     sorted_positions=0, grid_collisions=1)
+                     sorted_positions=0, grid_collisions=3)
 
 
 @pytest.mark.parametrize("tuning", ALL, ids=lambda t: "s{step_shape}p{persistent}o{spatial_order}f{full_sort}b{occupancy_filter}"
@@ -120,11 +122,11 @@ def test_invalid_tuning_rejected(lib):
     sim = bcs.Simulation(scene())
     for bad in (dict(step_shape=len(bcs.STEP_SHAPES)), dict(step_shape=-1), dict(persistent=2),
                 dict(spatial_order=-1), dict(full_sort=3), dict(occupancy_filter=2),
-                dict(sorted_positions=-1), dict(grid_collisions=3)):
+                dict(sorted_positions=-1), dict(grid_collisions=4)):
         with pytest.raises(bcs.BcsError):
             sim.set_tuning(**bad)
     assert sim.get_tuning().as_dict() == dict(step_shape=3, persistent=0, spatial_order=0, full_sort=0,
-                                              occupancy_filter=0, sorted_positions=0, grid_collisions=1)
+                                              occupancy_filter=0, sorted_positions=0, grid_collisions=3)
 
 
 def test_tuning_survives_set_particles_between_phases(lib):
@@ -136,7 +138,7 @@ def test_tuning_survives_set_particles_between_phases(lib):
     pos2 = sc.positions + rng.normal(0, 0.05, sc.positions.shape).astype(np.float32)
     out = []
     for t in (dict(), dict(sorted_positions=1, occupancy_filter=1, grid_collisions=0),
-              dict(grid_collisions=0)):
+              dict(grid_collisions=0), dict(grid_collisions=2), dict(grid_collisions=3)):
         sim = bcs.Simulation(sc)
         sim.set_particles(sc.positions, sc.velocities)
         sim.set_tuning(**t)

@@ -18,10 +18,11 @@ particle kernel, vein integration) replayed from a CUDA graph.
             overlaps the next frame; the upload of the state from pinned
             memory opens the timed region and the last read's arrival on the
             host closes it
-  roofline  the particle phase (the fused step kernel, its crowded-particle
+  roofline  the particle phase (the grid-order collision kernel, the step
             kernel, the vein-end kernel): algorithmic bytes (80 B/particle:
             x, v, F read + written as 3 x 12 B, + 8 B key/id) / its mean
-            CUDA-event duration, against the measured HBM copy bandwidth
+            CUDA-event duration, against the measured HBM copy bandwidth;
+            per_kernel gives each kernel's own figure
 Each of the three passes (timed run, per-phase events, e2e) starts a fresh
 simulation from the same state after the warm-up frames, with the tuning the
 autotuner picked in the first, so all three follow the same trajectory.
@@ -58,6 +59,11 @@ METRIC = "particle-steps/s @4.2M particles: plain vs learned-substep at fixed er
 UNIT = "particle-steps/s"
 CELLS_PER_TYPE = 20588
 ALGO_BYTES_STEP_KERNEL = 80      # per particle, see docstring
+# grid-order collisions: sorted position and velocity read (24 B), key and
+# id (8 B), the sum written (12 B); the step kernel reads that sum (12 B)
+COLLIDE_BYTES = 44
+STEP_COLL_BYTES = 12
+COLLIDE_KERNELS = {1: "bcs::k_collide<0>", 2: "bcs::k_collide<1>", 3: "bcs::k_collide_tile"}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -268,16 +274,26 @@ def oracle_parity(bcs, scene, threads=None):
                                                        o.get_particles())}
     gv, ov = sim.get_vein(), o.get_vein()
     errs["wall_position"] = rel_err(gv[0], ov[0])
-    # a wall velocity after one frame is dt x (spring forces at rest length,
-    # FP32 rounding noise, + particle impacts): the deformable-wall tests'
-    # rule, relative error <= 1e-4 x max(1, largest |v|)
-    wv = rel_err(gv[1], ov[1])
-    wv_tol = 1e-4 * max(1.0, float(np.abs(ov[1]).max()))
+    # A wall velocity after one frame is dt x (spring forces at rest length +
+    # particle impacts); at rest length a spring force is FP32 rounding of
+    # |p - q| - L, at most k_vein L 2^-23 for each of a vertex's nine springs:
+    # the elementwise rule plus that floor, 9 dt k_vein L_max 2^-23 (the
+    # benchmark-configuration parity tests' rule).
+    tri = np.asarray(scene.vein_indices).reshape(-1, 3)
+    vp = np.asarray(scene.vein_positions)
+    edge = max(np.linalg.norm(vp[tri[:, i]] - vp[tri[:, k]], axis=1).max() for i, k in ((0, 1), (1, 2), (2, 0)))
+    p = scene.params
+    floor = 9 * p.dt * p.vein_k_sniff * edge * 2.0 ** -23
+    o1 = np.asarray(ov[1], np.float64)
+    excess = float((np.abs(np.asarray(gv[1], np.float64) - o1) -
+                    (1e-5 * (np.abs(o1) + np.sqrt(np.mean(o1 * o1))) + floor)).max())
     sim.close()
     o.close()
     return {"frames": 1, "from": "the workload's initial state", "grid_bit_exact": grid_exact,
-            "max_rel_err": errs, "tolerance": 1e-5, "wall_velocity_rel_err": wv, "wall_velocity_tolerance": wv_tol,
-            "within_tolerance": grid_exact and max(errs.values()) <= 1e-5 and wv <= wv_tol,
+            "max_rel_err": errs, "tolerance": 1e-5,
+            "wall_velocity": {"excess_over_bound": excess, "floor": floor,
+                              "rule": "|dv| <= 1e-5 (|v| + rms v) + 9 dt k_vein L_max 2^-23"},
+            "within_tolerance": grid_exact and max(errs.values()) <= 1e-5 and excess <= 0,
             "oracle_threads": threads, "seconds": round(time.perf_counter() - t0, 2)}
 
 
@@ -709,21 +725,34 @@ def run_ours(args):
     sim.close()
 
     # ---- pass 2: the same frames eagerly, CUDA events between the phases;
-    # the particle phase is the fused step kernel, its crowded-particle
-    # kernel and the vein-end kernel
+    # the particle phase is the grid-order collision kernel, the step
+    # kernel (with its crowded-particle kernel when the step kernel searches
+    # the stencils itself) and the vein-end kernel
     prof_steps = args.profile_steps if args.profile_steps > 0 else args.steps
     sim = fresh(tuning)
     phases = sim.profile_steps(prof_steps)
     sim.close()
-    k_ms = phases["particles"] / prof_steps
+    coll_ms = phases["collisions"] / prof_steps
+    step_ms = phases["particles"] / prof_steps
+    k_ms = coll_ms + step_ms
     peak, peak_kind = measured_peak()
     achieved = ALGO_BYTES_STEP_KERNEL * n / (k_ms / 1e3) / 1e9
-    traffic = None
-    tf = os.path.join(REPO, "profiles", "k_step_traffic.json")
+    traffic, traffic_note = None, None
+    tf = os.path.join(REPO, "profiles", "particle_phase_traffic.json")
     if os.path.exists(tf):
         with open(tf) as f:
             tr = json.load(f)
-        traffic = tr["dram_bytes_per_launch"] * n / tr["particles"]
+        traffic = sum(tr["dram_bytes_per_launch"].values()) * n / tr["particles"]
+        traffic_note = tr["note"]
+    per_kernel = {}
+    if coll_ms > 0:
+        per_kernel["collisions"] = {"ms": coll_ms, "algorithmic_bytes_per_particle": COLLIDE_BYTES,
+                                    "achieved_gbs": COLLIDE_BYTES * n / (coll_ms / 1e3) / 1e9}
+        per_kernel["collisions"]["frac"] = per_kernel["collisions"]["achieved_gbs"] / peak
+    step_bytes = ALGO_BYTES_STEP_KERNEL + (STEP_COLL_BYTES if coll_ms > 0 else 0)
+    per_kernel["step"] = {"ms": step_ms, "algorithmic_bytes_per_particle": step_bytes,
+                          "achieved_gbs": step_bytes * n / (step_ms / 1e3) / 1e9}
+    per_kernel["step"]["frac"] = per_kernel["step"]["achieved_gbs"] / peak
 
     # ---- pass 3: end to end through the C ABI with pinned host buffers:
     # the state after the warm-up is uploaded, then every frame is
@@ -788,12 +817,16 @@ def run_ours(args):
                     "h2d_bytes_per_step": int(36 * n / e2e_steps), "d2h_bytes_per_step": int(12 * n)},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm",
-                         "kernel": "bcs::k_step<0, {}, {}, {}, {}> + k_crowded<0> + k_vein_end".format(
-                             *shape, "true" if tuning["persistent"] else "false"),
+                         "kernel": ("{} + ".format(COLLIDE_KERNELS[tuning["grid_collisions"]])
+                                    if tuning["grid_collisions"] else "") +
+                                   "bcs::k_step<0, {}, {}, {}, {}>".format(
+                                       *shape, "true" if tuning["persistent"] else "false") +
+                                   (" + k_crowded<0>" if not tuning["grid_collisions"] else "") + " + k_vein_end",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_note,
                          "algorithmic_bytes_per_launch": ALGO_BYTES_STEP_KERNEL * n, "kernel_ms": k_ms,
-                         "kernel_ms_over": f"{prof_steps} eager frames of the same trajectory"},
+                         "kernel_ms_over": f"{prof_steps} eager frames of the same trajectory",
+                         "per_kernel": per_kernel},
             "phase_ms": {k: v / prof_steps for k, v in phases.items()},
             "diagnostics_after_timed_run": diag,
             "learned_substep": learned,

@@ -565,9 +565,12 @@ bcs_status bcs_grid_sort_static_error_word(void* stream, uint32_t* out);
 enum {
     BCS_PHASE_GRID = 0,         /* key sort + cell ranges                   */
     BCS_PHASE_VEIN_FORCES = 1,  /* vein spring gather                       */
-    BCS_PHASE_PARTICLES = 2,    /* the fused particle step kernel            */
-    BCS_PHASE_VEIN_UPDATE = 3,  /* vein integration + triangle cache         */
-    BCS_PHASE_COUNT = 4
+    BCS_PHASE_COLLISIONS = 2,   /* grid-order particle collisions (empty when
+                                   the step kernel searches the stencils)   */
+    BCS_PHASE_PARTICLES = 3,    /* the particle step kernel (springs, vein
+                                   ray, integration) and the vein-end rule  */
+    BCS_PHASE_VEIN_UPDATE = 4,  /* vein integration + triangle cache         */
+    BCS_PHASE_COUNT = 5
 };
 
 /* Run `nsteps` frames eagerly (no graph) with CUDA events between phases on

@@ -42,7 +42,7 @@ INIT_REFERENCE, INIT_LATTICE = 0, 1
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
 GRID_SORT_STATIC_MAX = 262144
 MAX_SUBSTEPS = 64
-PHASES = ("grid", "vein_forces", "particles", "vein_update")
+PHASES = ("grid", "vein_forces", "collisions", "particles", "vein_update")
 
 
 class BcsError(RuntimeError):

@@ -23,7 +23,8 @@
 
 namespace bcs {
 // bcs_kernels.cu
-void launch_step(const StepArgs& a, int items, int mode, int shape, int persistent_grid, cudaStream_t s);
+void launch_step(const StepArgs& a, int items, int mode, int shape, int persistent_grid, cudaStream_t s,
+                 cudaEvent_t after_collisions = nullptr);
 int step_persistent_grid(int mode, int shape);
 void launch_gather_rows(const float4* src, const int* idx, int n, float4* out, cudaStream_t s);
 void launch_propagate(const StepArgs& a, int blocks, cudaStream_t s);
@@ -435,11 +436,12 @@ void enqueue_frame(bcs_sim* s, cudaEvent_t* ev = nullptr) {
     if (ev) cudaEventRecord(ev[2], s->stream);
     const int in = s->cur, out = s->cur ^ 1;
     refresh_args(s, in, out, true);
-    launch_step(s->args, (int)s->work_host.size(), 0, s->tune.step_shape, s->persistent_grid[0], s->stream);
+    launch_step(s->args, (int)s->work_host.size(), 0, s->tune.step_shape, s->persistent_grid[0], s->stream,
+                ev ? ev[3] : nullptr);
     if (s->p.use_blood_flow) launch_vein_end(s->args, s->C, s->stream);
-    if (ev) cudaEventRecord(ev[3], s->stream);
-    enqueue_vein_propagate(s);
     if (ev) cudaEventRecord(ev[4], s->stream);
+    enqueue_vein_propagate(s);
+    if (ev) cudaEventRecord(ev[5], s->stream);
     s->cur = out;
     s->keys_valid = true;    // k_step wrote keys of the new positions
     ++s->host_steps;

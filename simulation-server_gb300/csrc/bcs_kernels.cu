@@ -2461,7 +2461,8 @@ int step_persistent_grid(int mode, int shape) {
     return std::max(1, per) * std::max(1, sms);
 }
 
-void launch_step(const StepArgs& a, int items, int mode, int shape, int persistent_grid, cudaStream_t s) {
+void launch_step(const StepArgs& a, int items, int mode, int shape, int persistent_grid, cudaStream_t s,
+                 cudaEvent_t after_collisions) {
     if (items <= 0) return;
     const bool persistent = persistent_grid > 0;
     const int blocks = persistent ? std::min(items, persistent_grid) : items;
@@ -2480,6 +2481,7 @@ void launch_step(const StepArgs& a, int items, int mode, int shape, int persiste
             k_collide<0><<<blocks, kCollideThreads, 0, s>>>(a);
         }
     }
+    if (after_collisions) cudaEventRecord(after_collisions, s);
     step_kernel_for(mode, shape, persistent)<<<blocks, kShapes[shape].threads, 0, s>>>(a);
     if (!a.pg.uniform || a.coll) return;   // no stencil, or no crowded particles set aside
     static int grid = 0;

@@ -283,7 +283,7 @@ def oracle_parity(bcs, scene, threads=None):
     vp = np.asarray(scene.vein_positions)
     edge = max(np.linalg.norm(vp[tri[:, i]] - vp[tri[:, k]], axis=1).max() for i, k in ((0, 1), (1, 2), (2, 0)))
     p = scene.params
-    floor = 9 * p.dt * p.vein_k_sniff * edge * 2.0 ** -23
+    floor = float(9 * p.dt * p.vein_k_sniff * edge * 2.0 ** -23)
     o1 = np.asarray(ov[1], np.float64)
     excess = float((np.abs(np.asarray(gv[1], np.float64) - o1) -
                     (1e-5 * (np.abs(o1) + np.sqrt(np.mean(o1 * o1))) + floor)).max())

@@ -116,6 +116,8 @@ struct DeviceGrid {
     float4* spos = nullptr;    // positions in sorted order, kept while spos_on
     float4* svel = nullptr;    // velocities in sorted order, with spos
     bool spos_on = false;
+    bool table_on = true;      // every build writes the range table (off under grid-order collisions,
+    bool table_current = false;// which need only the row starts; the getters then build it on demand)
     int* row_start = nullptr;  // first sorted slot of every grid row (+1 entry), kept while rows_on
     long long rows = 0;        // grid rows of all scenes
     bool rows_on = false;
@@ -354,10 +356,21 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, con
     dg.g.spos = dg.spos_on && pos ? dg.spos : nullptr;
     dg.g.svel = dg.spos_on && pos && vel ? dg.svel : nullptr;
     float4* svel_out = dg.spos_on && pos && vel ? dg.svel : nullptr;
-    launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, dg.occ_on ? dg.occ : nullptr, dg.g.ids, pos,
-                       dg.spos_on && pos ? dg.spos : nullptr, vel, svel_out, st);
+    launch_cell_ranges(dg.g.keys, dg.count, dg.table_on ? dg.table : nullptr, dg.epoch,
+                       dg.occ_on && dg.table_on ? dg.occ : nullptr, dg.g.ids, pos, dg.spos_on && pos ? dg.spos : nullptr,
+                       vel, svel_out, st);
+    dg.table_current = dg.table_on;
     if (dg.rows_on) launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, st);
     dg.g.row_start = dg.rows_on ? dg.row_start : nullptr;
+}
+
+// The range table of the current sorted keys, when the last build left it
+// out (grid-order collisions need only the row starts).
+void ensure_table(DeviceGrid& dg, cudaStream_t st) {
+    if (dg.table_current || !dg.sorted_once || !dg.table) return;
+    launch_cell_ranges(dg.g.keys, dg.count, dg.table, dg.epoch, dg.occ_on ? dg.occ : nullptr, dg.g.ids, nullptr,
+                       nullptr, nullptr, nullptr, st);
+    dg.table_current = true;
 }
 
 void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
@@ -671,6 +684,8 @@ bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
     s->pg.g.spos = sp && s->pg.sorted_once ? s->pg.spos : nullptr;
     s->pg.g.svel = sp && s->pg.sorted_once ? s->pg.svel : nullptr;
     s->pg.rows_on = gc;
+    s->pg.table_on = !gc;
+    if (!gc) ensure_table(s->pg, s->stream);
     s->pg.g.row_start = gc && s->pg.sorted_once ? s->pg.row_start : nullptr;
     s->args.pg = s->pg.g;
     s->args.coll = gc && s->pg.g.row_start && s->pg.g.spos && s->pg.g.svel ? s->coll : nullptr;
@@ -1826,6 +1841,7 @@ bcs_status bcs_get_grid(bcs_sim* s, int which, int* cell_ids, int* object_ids, i
             ds = hs.as<int>();
             de = he.as<int>();
         }
+        ensure_table(dg, s->stream);
         launch_dense_ranges(dg.table, dg.epoch, dg.g.cells, ds, de, s->stream);
         if (where == BCS_MEM_HOST) {
             if (ds) BCS_CUDA(cudaMemcpyAsync(cell_starts, ds, sizeof(int) * (size_t)dg.g.cells, kind, s->stream));

@@ -2134,6 +2134,7 @@ __global__ void k_cell_ranges(const int* __restrict__ keys, int n, int4* table, 
         spos[i] = pos[id];
         if (svel) svel[i] = vel[id];
     }
+    if (!table) return;   // grid-order collisions: the range table is built on demand only
     const int k = keys[i];
     if (i > 0 && keys[i - 1] == k) return;
     int j = i;

@@ -561,6 +561,81 @@ bcs_status bcs_grid_sort_static(const float* x, const float* y, const float* z, 
  * the reference (which only printf()s such positions, uniform_grid.cu:31-34). */
 bcs_status bcs_grid_sort_static_error_word(void* stream, uint32_t* out);
 
+/* ---- Control messages of the streaming server, without the network and
+ * the renderer.  The reference's client sends one byte per message over
+ * ENet (src/communication/server_endpoint.hpp:19-63, server_endpoint.cpp:
+ * 6-8,140-185): the low seven bits name the event, the high bit is set for
+ * "start" (a key pressed) and clear for "stop" (released).  Its
+ * MsgController (msg_controller.cpp:27-148) handles at most one message per
+ * frame.  Here a transport of the application's choosing posts the bytes it
+ * receives and takes the bytes to send; a renderer reads the held events and
+ * the render toggles. */
+typedef enum bcs_event_type {
+    BCS_EVENT_NO_MESSAGE = 0,
+    BCS_EVENT_CAMERA_LEFT, BCS_EVENT_CAMERA_RIGHT, BCS_EVENT_CAMERA_FORWARD, BCS_EVENT_CAMERA_BACK,
+    BCS_EVENT_CAMERA_ASCEND, BCS_EVENT_CAMERA_DESCEND,
+    BCS_EVENT_CAMERA_ROTATE_LEFT, BCS_EVENT_CAMERA_ROTATE_RIGHT, BCS_EVENT_CAMERA_ROTATE_UP,
+    BCS_EVENT_CAMERA_ROTATE_DOWN,
+    BCS_EVENT_TOGGLE_POLYGON_MODE, BCS_EVENT_TOGGLE_SPRINGS_RENDERING, BCS_EVENT_TOGGLE_SPHERES_RENDERING,
+    BCS_EVENT_STREAM_SUCCESSFULLY_ENDED, BCS_EVENT_STOP_RENDERING,
+    BCS_EVENT_NEW_CONNECTION, BCS_EVENT_PEER_DISCONNECTED,
+    BCS_EVENT_INVALID_MESSAGE
+} bcs_event_type;   /* EventType, same values */
+typedef enum bcs_event_state {
+    BCS_EVENT_START = 0, BCS_EVENT_STOP = 1, BCS_EVENT_NOT_RELEVANT = 2
+} bcs_event_state;  /* EventState */
+typedef struct bcs_event {
+    int32_t type;   /* bcs_event_type */
+    int32_t state;  /* bcs_event_state */
+} bcs_event;
+
+/* parseEvent (server_endpoint.cpp:168-185): one message's bytes; a length
+ * other than 1 or an unknown event gives BCS_EVENT_INVALID_MESSAGE. */
+bcs_event bcs_event_decode(const uint8_t* data, size_t length);
+/* SendEvent's byte (server_endpoint.cpp:140-163) into *byte; returns the
+ * channel + 1 (2 for the important events streamSuccessfullyEnded and
+ * stopRendering, 1 otherwise), or 0 for an invalid event. */
+int bcs_event_encode(bcs_event event, uint8_t* byte);
+
+/* The controller's state after a message. */
+typedef struct bcs_control_state {
+    uint32_t held;               /* bit t set while event t is held (started, not stopped) */
+    int32_t polygon_mode_line;   /* togglePolygonMode: vein drawn as lines (starts as fill) */
+    int32_t springs_rendering;   /* toggleSpringsRendering (starts on) */
+    int32_t spheres_rendering;   /* toggleSpheresRendering (starts on) */
+    int32_t stop_requested;      /* a stopRendering message was handled */
+    int32_t connected;           /* newConnection seen, no peerDisconnected since */
+    int64_t handled;             /* messages handled */
+} bcs_control_state;
+
+typedef struct bcs_control bcs_control;
+bcs_status bcs_control_create(bcs_control** out);
+void bcs_control_destroy(bcs_control* control);
+/* Queue one received message (the bytes of one packet); thread-safe. */
+bcs_status bcs_control_post(bcs_control* control, const uint8_t* data, size_t length);
+/* Queue a transport event (BCS_EVENT_NEW_CONNECTION / PEER_DISCONNECTED with
+ * BCS_EVENT_NOT_RELEVANT, as pollEvents reports them); thread-safe. */
+bcs_status bcs_control_post_event(bcs_control* control, bcs_event event);
+/* handleMsgs: handle the oldest queued message, if any, and write the
+ * state.  A start adds the event to the held set; a stop removes it and then,
+ * as in the reference (msg_controller.cpp:40-45), also takes the
+ * single-message path: render toggles flip, stopRendering requests the end
+ * of the run, peerDisconnected clears the held set. */
+bcs_status bcs_control_handle(bcs_control* control, bcs_control_state* state_out);
+/* Queue a message for the transport (SendEvent); bcs_control_take_outgoing
+ * hands the queued bytes out in order, returning 0 when none is left. */
+bcs_status bcs_control_send(bcs_control* control, bcs_event event);
+int bcs_control_take_outgoing(bcs_control* control, uint8_t* byte);
+
+/* The server loop of main.cu:158-245 without rendering and streaming: every
+ * frame is bcs_step(sim, 1) (the grids, calculateNextFrame, propagateAll),
+ * then one control message is handled (control may be NULL).  The loop ends
+ * once a handled message requested the stop, or after the frame that takes
+ * its frame count past max_frames (the count starts at 0, so max_frames + 1
+ * frames, as in the reference); then streamSuccessfullyEnded is queued for
+ * the transport (msg_controller.cpp:55-59).  Writes the frames run. */
+bcs_status bcs_run(bcs_sim* sim, bcs_control* control, int max_frames, int* frames_run);
+
 /* Phases of one frame timed by bcs_profile_steps. */
 enum {
     BCS_PHASE_GRID = 0,         /* key sort + cell ranges                   */

@@ -36,7 +36,9 @@ EXPORTED = [
     "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
     "bcs_surrogate_get_scales", "bcs_surrogate_evaluate", "bcs_surrogate_set_scales", "bcs_time_macro_steps",
     "bcs_init_particles", "bcs_set_tensor_path", "bcs_tensor_wait_expiries", "bcs_get_particles_async",
-    "bcs_wait_particles", "bcs_get_crowded", "bcs_set_tensor_wait_probe",
+    "bcs_wait_particles", "bcs_get_crowded", "bcs_set_tensor_wait_probe", "bcs_event_decode", "bcs_event_encode",
+    "bcs_control_create", "bcs_control_destroy", "bcs_control_post", "bcs_control_post_event", "bcs_control_handle",
+    "bcs_control_send", "bcs_control_take_outgoing", "bcs_run",
 ]
 INIT_REFERENCE, INIT_LATTICE = 0, 1
 STEP_SHAPES = ((256, 512, 3), (128, 256, 6), (384, 768, 2), (256, 512, 4), (256, 512, 2), (128, 256, 8))
@@ -146,6 +148,29 @@ class SurrogateDesc(C.Structure):
                 ("seed", C.c_uint64), ("tolerance", C.c_float), ("huber_delta", C.c_float)]
 
 
+# control messages of the streaming server (bcs_event_type, bcs_event_state)
+EVENT_NAMES = ("no_message", "camera_left", "camera_right", "camera_forward", "camera_back", "camera_ascend",
+               "camera_descend", "camera_rotate_left", "camera_rotate_right", "camera_rotate_up",
+               "camera_rotate_down", "toggle_polygon_mode", "toggle_springs_rendering", "toggle_spheres_rendering",
+               "stream_successfully_ended", "stop_rendering", "new_connection", "peer_disconnected",
+               "invalid_message")
+EVENT = {n: i for i, n in enumerate(EVENT_NAMES)}
+EVENT_START, EVENT_STOP, EVENT_NOT_RELEVANT = 0, 1, 2
+
+
+class Event(C.Structure):
+    _fields_ = [("type", C.c_int32), ("state", C.c_int32)]
+
+
+class ControlState(C.Structure):
+    _fields_ = [("held", C.c_uint32), ("polygon_mode_line", C.c_int32), ("springs_rendering", C.c_int32),
+                ("spheres_rendering", C.c_int32), ("stop_requested", C.c_int32), ("connected", C.c_int32),
+                ("handled", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class SurrogateStats(C.Structure):
     _fields_ = [("cells", C.c_int64), ("samples", C.c_int64), ("valid_samples", C.c_int64),
                 ("predicted_cells", C.c_int64), ("fallback_cells", C.c_int64), ("iterations", C.c_int64),
@@ -207,6 +232,16 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_get_particles_async": ([P, Vec3, Vec3, Vec3], C.c_int),
         "bcs_wait_particles": ([P], C.c_int),
         "bcs_get_crowded": ([P, C.POINTER(C.c_longlong)], C.c_int),
+        "bcs_event_decode": ([C.POINTER(C.c_uint8), C.c_size_t], Event),
+        "bcs_event_encode": ([Event, C.POINTER(C.c_uint8)], C.c_int),
+        "bcs_control_create": ([C.POINTER(P)], C.c_int),
+        "bcs_control_destroy": ([P], None),
+        "bcs_control_post": ([P, C.POINTER(C.c_uint8), C.c_size_t], C.c_int),
+        "bcs_control_post_event": ([P, Event], C.c_int),
+        "bcs_control_handle": ([P, C.POINTER(ControlState)], C.c_int),
+        "bcs_control_send": ([P, Event], C.c_int),
+        "bcs_control_take_outgoing": ([P, C.POINTER(C.c_uint8)], C.c_int),
+        "bcs_run": ([P, P, C.c_int, C.POINTER(C.c_int)], C.c_int),
         "bcs_set_vein": ([P, Vec3, Vec3, C.c_int], C.c_int),
         "bcs_get_vein": ([P, Vec3, Vec3, Vec3, C.c_int], C.c_int),
         "bcs_calculate_grids": ([P], C.c_int),
@@ -323,6 +358,60 @@ def set_tensor_wait_probe(polls: int) -> None:
     tcgen05 kernels gives up after that many polls of a barrier nothing
     arrives at; 0 restores the normal waits."""
     _check(load_library().bcs_set_tensor_wait_probe(int(polls)), "bcs_set_tensor_wait_probe")
+
+
+class Control:
+    """The streaming server's control messages (bcs_control): post received
+    bytes, handle one message per frame, take the bytes to send."""
+
+    def __init__(self):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        _check(self.lib.bcs_control_create(C.byref(self.h)), "bcs_control_create")
+
+    def post(self, data: bytes) -> None:
+        buf = (C.c_uint8 * max(1, len(data))).from_buffer_copy(bytes(data) or b"\0")
+        _check(self.lib.bcs_control_post(self.h, buf, len(data)), "bcs_control_post")
+
+    def post_event(self, name: str, state: int = EVENT_NOT_RELEVANT) -> None:
+        _check(self.lib.bcs_control_post_event(self.h, Event(EVENT[name], state)), "bcs_control_post_event")
+
+    def handle(self) -> dict:
+        st = ControlState()
+        _check(self.lib.bcs_control_handle(self.h, C.byref(st)), "bcs_control_handle")
+        return st.as_dict()
+
+    def send(self, name: str, state: int = EVENT_NOT_RELEVANT) -> None:
+        _check(self.lib.bcs_control_send(self.h, Event(EVENT[name], state)), "bcs_control_send")
+
+    def take_outgoing(self) -> list:
+        out, b = [], C.c_uint8()
+        while self.lib.bcs_control_take_outgoing(self.h, C.byref(b)):
+            out.append(int(b.value))
+        return out
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.bcs_control_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def decode_event(data: bytes):
+    buf = (C.c_uint8 * max(1, len(data))).from_buffer_copy(bytes(data) or b"\0")
+    e = load_library().bcs_event_decode(buf, len(data))
+    return EVENT_NAMES[e.type], e.state
+
+
+def encode_event(name: str, state: int):
+    b = C.c_uint8()
+    ch = load_library().bcs_event_encode(Event(EVENT[name], state), C.byref(b))
+    return (int(b.value), ch) if ch else (None, 0)
 
 
 def set_device(device: int) -> None:
@@ -493,6 +582,14 @@ class Simulation:
 
     def step(self, nsteps: int = 1) -> None:
         _check(self.lib.bcs_step(self.h, int(nsteps)), "bcs_step")
+
+    def run(self, max_frames: int, control=None) -> int:
+        """The server loop (bcs_run): frames until a handled stopRendering
+        message or max_frames + 1 frames; returns the frames run."""
+        n = C.c_int()
+        _check(self.lib.bcs_run(self.h, control.h if control is not None else None, int(max_frames), C.byref(n)),
+               "bcs_run")
+        return int(n.value)
 
     def macro_step(self, substeps: int, n: int = 1) -> None:
         """n multi-rate macro steps of `substeps` time steps each."""

@@ -17,7 +17,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbcs.so")
-SOURCES = ["bcs_kernels.cu", "bcs_sort.cu", "bcs_api.cu", "bcs_noalloc.cu", "bcs_mpnn.cu"]
+SOURCES = ["bcs_kernels.cu", "bcs_sort.cu", "bcs_api.cu", "bcs_noalloc.cu", "bcs_mpnn.cu", "bcs_events.cu"]
 HEADERS = ["bcs_internal.cuh", "bcs_mpnn.cuh", "bcs_mma.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1913,6 +1913,30 @@ bcs_status bcs_time_macro_steps(bcs_sim* s, int substeps, int n, float* ms_out) 
     return check_last();
 }
 
+bcs_status bcs_run(bcs_sim* s, bcs_control* control, int max_frames, int* frames_run) {
+    if (!s || max_frames < 0) return BCS_ERR_INVALID_ARGUMENT;
+    int count = 0, frames = 0;
+    bcs_status st = BCS_OK;
+    for (bool running = true; running;) {
+        if ((st = bcs_step(s, 1)) != BCS_OK) break;
+        ++frames;
+        if (control) {
+            bcs_control_state cs{};
+            if ((st = bcs_control_handle(control, &cs)) != BCS_OK) break;
+            if (cs.stop_requested) running = false;
+        }
+        if (++count > max_frames) running = false;
+    }
+    if (frames_run) *frames_run = frames;
+    if (st != BCS_OK) return st;
+    if (control) {
+        bcs_event done{BCS_EVENT_STREAM_SUCCESSFULLY_ENDED, BCS_EVENT_NOT_RELEVANT};
+        if ((st = bcs_control_send(control, done)) != BCS_OK) return st;
+    }
+    BCS_CUDA(cudaStreamSynchronize(s->stream));
+    return check_last();
+}
+
 bcs_status bcs_profile_steps(bcs_sim* s, int nsteps, float* phase_ms) {
     if (!s || !phase_ms || nsteps < 0 || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < nsteps; ++i) {

@@ -1047,8 +1047,10 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
     const GridDev& g = a.pg;
     const int s0 = blockIdx.x * kTileSlots, j = s0 + threadIdx.x;
     const int last = min(s0 + kTileSlots, a.n) - 1;
-    if (threadIdx.x == 0) {
-        int ok = 1;
+    if (threadIdx.x < 32) {
+        // the tile's plane and rows, and the three planes' slot ranges: lane
+        // p (0..2) looks up plane zf + p - 1, all loads in flight together
+        const int lane = threadIdx.x;
         const int sc_i = find_range(a.scene_count, s0, [&](int k) { return a.scenes[k].particle_start; });
         const SceneDev& sc = a.scenes[sc_i];
         const GridGeom& geo = sc.pg;
@@ -1057,26 +1059,30 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
         const int zf = kf / cxy, zl = kl / cxy;
         const int yf = (kf - zf * cxy) / geo.cx, yl = (kl - zl * cxy) / geo.cx;
         const int ylo = max(yf - 1, 0), yhi = min(yl + 1, geo.cy - 1);
-        if (last >= sc.particle_end || zf != zl || yhi - ylo + 1 > kTileRows) ok = 0;
-        int total = 0;
-        for (int p = 0; p < 3 && ok; ++p) {
-            const int z = zf + p - 1;
-            s_base[p] = total;
-            s_A[p] = 0;
-            if (z < 0 || z >= geo.cz) continue;
+        const bool ok = last < sc.particle_end && zf == zl && yhi - ylo + 1 <= kTileRows;
+        int A = 0, cnt = 0;
+        const int z = zf + lane - 1;
+        if (ok && lane < 3 && z >= 0 && z < geo.cz) {
             const int r0 = (int)geo.row_offset + z * geo.cy;
-            const int A = __ldg(&g.row_start[r0 + ylo]), B = __ldg(&g.row_start[r0 + yhi + 1]);
-            s_A[p] = A;
-            total += B - A;
+            A = __ldg(&g.row_start[r0 + ylo]);
+            cnt = __ldg(&g.row_start[r0 + yhi + 1]) - A;
         }
-        s_base[3] = total;
-        if (total > kTileStage) ok = 0;
-        s_ok = ok;
-        s_scene = sc_i;
-        s_z = zf;
-        s_ylo = ylo;
-        s_nrows = yhi - ylo + 1;
-        s_total = total;
+        const int c0 = __shfl_sync(0xffffffffu, cnt, 0), c1 = __shfl_sync(0xffffffffu, cnt, 1),
+                  c2 = __shfl_sync(0xffffffffu, cnt, 2);
+        if (lane < 3) s_A[lane] = A;
+        if (lane == 0) {
+            const int total = c0 + c1 + c2;
+            s_base[0] = 0;
+            s_base[1] = c0;
+            s_base[2] = c0 + c1;
+            s_base[3] = total;
+            s_ok = ok && total <= kTileStage;
+            s_scene = sc_i;
+            s_z = zf;
+            s_ylo = ylo;
+            s_nrows = yhi - ylo + 1;
+            s_total = total;
+        }
     }
     __syncthreads();
     if (!s_ok) {

@@ -992,10 +992,34 @@ __device__ inline void collide_slot(const StepArgs& a, int j) {
             }
         }
         const int wx = st.x1 - st.x0;
+        // four candidates per step, their keys, positions and velocities
+        // loaded together (a crowded window holds hundreds); the sum keeps
+        // the slots' order
+#pragma unroll 1
+        for (int r = 0; r < 9; ++r) {
+            int t = lo[r];
+            for (bool more = t < end[r]; more;) {
+                int k[4];
+                float4 pq[4], vq[4];
 #pragma unroll
-        for (int r = 0; r < 9; ++r)
-            for (int t = lo[r]; t < end[r] && __ldg(&keys[t]) - wlo[r] <= wx; ++t)
-                collide(a, x, v, R, __ldg(&g.spos[t]), [&g, t] { return __ldg(&g.svel[t]); }, acc, e);
+                for (int u = 0; u < 4; ++u) {
+                    const bool in = t + u < end[r];
+                    k[u] = in ? __ldg(&keys[t + u]) : 0x7fffffff;
+                    pq[u] = in ? __ldg(&g.spos[t + u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    vq[u] = in ? __ldg(&g.svel[t + u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (k[u] - wlo[r] > wx) {
+                        more = false;
+                        break;
+                    }
+                    collide(a, x, v, R, pq[u], [&vq, u] { return vq[u]; }, acc, e);
+                }
+                t += 4;
+                more = more && t < end[r];
+            }
+        }
     } else {
         // each row's window from a linear scan of the row's first slots
         for (int dz = st.z0; dz <= st.z1; ++dz)

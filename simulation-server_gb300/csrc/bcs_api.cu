@@ -86,8 +86,11 @@ struct IncrementalBuffers {
     int* kept_k; int* kept_v;
     int* mov_k; int* mov_v;
     int* t1_k; int* t1_v;
-    int* t2_k; int* t2_v;
-    unsigned* tile_kept;
+    unsigned* warp_kept;
+    unsigned* tile_base;
+    unsigned* id_movers;
+    unsigned* id_base;
+    unsigned char* moved;
     unsigned* temp;
     int* movers;
 };
@@ -300,12 +303,18 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
         (st = dalloc(s, &dg.temp, radix_temp_words(count))))
         return st;
     dg.inc.temp = dg.temp;
-    if (incremental &&
-        ((st = dalloc(s, &dg.inc.kept_k, count)) || (st = dalloc(s, &dg.inc.kept_v, count)) ||
-         (st = dalloc(s, &dg.inc.mov_k, count)) || (st = dalloc(s, &dg.inc.mov_v, count)) ||
-         (st = dalloc(s, &dg.inc.t2_k, count)) || (st = dalloc(s, &dg.inc.t2_v, count)) ||
-         (st = dalloc(s, &dg.inc.tile_kept, radix_tiles(count))) || (st = dalloc(s, &dg.inc.movers, 1))))
-        return st;
+    if (incremental) {
+        const int tiles = radix_tiles(count);
+        if ((st = dalloc(s, &dg.inc.kept_k, count)) || (st = dalloc(s, &dg.inc.kept_v, count)) ||
+            (st = dalloc(s, &dg.inc.mov_k, count)) || (st = dalloc(s, &dg.inc.mov_v, count)) ||
+            (st = dalloc(s, &dg.inc.warp_kept, 8 * (size_t)tiles)) || (st = dalloc(s, &dg.inc.tile_base, tiles)) ||
+            (st = dalloc(s, &dg.inc.id_movers, tiles)) || (st = dalloc(s, &dg.inc.id_base, tiles)) ||
+            (st = dalloc(s, &dg.inc.moved, 4096 * (size_t)tiles)) || (st = dalloc(s, &dg.inc.movers, 1)))
+            return st;
+        // mover flags and counts are zero between builds
+        BCS_CUDA(cudaMemsetAsync(dg.inc.id_movers, 0, sizeof(unsigned) * tiles, s->stream));
+        BCS_CUDA(cudaMemsetAsync(dg.inc.moved, 0, 4096 * (size_t)tiles, s->stream));
+    }
     int idb = 0;
     while (idb < 31 && (1LL << idb) < count) ++idb;
     dg.id_bits = idb;

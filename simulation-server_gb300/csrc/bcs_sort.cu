@@ -232,139 +232,225 @@ __device__ inline unsigned long long pack_pair(int key, int id) {
     return ((unsigned long long)(unsigned)key << 32) | (unsigned)id;
 }
 
-// Count, per tile of 4096 sorted slots, the pairs whose particle kept its key.
+// Slot i of a tile belongs to warp (i % 4096) / 512, round (i % 512) / 32,
+// lane i % 32: each warp compacts its own 512 consecutive slots.
+constexpr int kWarpSlots = kSortTile / kSortWarps;   // 512
+
+// Per warp of every 4096-slot tile, the pairs whose particle kept its key;
+// the movers' particle ids are flagged and counted per 4096-id tile.
 __global__ void __launch_bounds__(kSortThreads) k_inc_count(const int* __restrict__ old_k, const int* __restrict__ old_v,
                                                             const int* __restrict__ new_key_of, int n,
-                                                            unsigned* __restrict__ tile_kept) {
-    __shared__ unsigned s_warp[kSortWarps];
-    const int base = blockIdx.x * kSortTile;
-    unsigned c = 0;
+                                                            unsigned* __restrict__ warp_kept, unsigned char* moved,
+                                                            unsigned* id_movers) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wbase = blockIdx.x * kSortTile + warp * kWarpSlots;
+    unsigned kept = 0;
 #pragma unroll 4
-    for (int k = 0; k < kSortItems; ++k) {
-        const int i = base + k * kSortThreads + threadIdx.x;
-        if (i < n) c += __ldg(&new_key_of[old_v[i]]) == old_k[i];
+    for (int r = 0; r < kSortItems; ++r) {
+        const int i = wbase + r * 32 + lane;
+        bool keep = true;
+        int id = 0;
+        if (i < n) {
+            id = old_v[i];
+            keep = __ldg(&new_key_of[id]) == old_k[i];
+        }
+        kept += __popc(__ballot_sync(0xffffffffu, i < n && keep));
+        if (!keep) {
+            moved[id] = 1;
+            // one atomic per id tile among the warp's movers
+            const unsigned mask = __activemask();
+            const unsigned peers = __match_any_sync(mask, id >> 12);
+            if ((peers & ((1u << lane) - 1u)) == 0) atomicAdd(&id_movers[id >> 12], (unsigned)__popc(peers));
+        }
     }
-    unsigned tot;
-    block_scan_256(c, s_warp, &tot);
-    if (threadIdx.x == 0) tile_kept[blockIdx.x] = tot;
+    if (lane == 0) warp_kept[blockIdx.x * kSortWarps + warp] = kept;
 }
 
-// Exclusive scan of the per-tile kept counts (one CTA); writes the number of
-// movers to *movers.
-__global__ void __launch_bounds__(kSortThreads) k_inc_scan(unsigned* tile_kept, int ntiles, int n, int* movers) {
+// One CTA: exclusive scans of the per-tile kept counts (slot tiles) and of
+// the per-id-tile mover counts (which it clears for the next build); the
+// number of movers into *movers.
+__global__ void __launch_bounds__(kSortThreads) k_inc_scan(const unsigned* __restrict__ warp_kept, int ntiles, int n,
+                                                           unsigned* tile_base, unsigned* id_movers, unsigned* id_base,
+                                                           int* movers) {
     __shared__ unsigned s_warp[kSortWarps];
     unsigned carry = 0;
     for (int base = 0; base < ntiles; base += kSortThreads) {
         const int i = base + threadIdx.x;
-        const unsigned v = i < ntiles ? tile_kept[i] : 0u;
+        unsigned v = 0;
+        if (i < ntiles) {
+#pragma unroll
+            for (int w = 0; w < kSortWarps; ++w) v += warp_kept[i * kSortWarps + w];
+        }
         unsigned tot;
         const unsigned ex = block_scan_256(v, s_warp, &tot);
-        if (i < ntiles) tile_kept[i] = carry + ex;
+        if (i < ntiles) tile_base[i] = carry + ex;
         carry += tot;
+    }
+    unsigned mcarry = 0;
+    for (int base = 0; base < ntiles; base += kSortThreads) {
+        const int i = base + threadIdx.x;
+        const unsigned v = i < ntiles ? id_movers[i] : 0u;
+        unsigned tot;
+        const unsigned ex = block_scan_256(v, s_warp, &tot);
+        if (i < ntiles) {
+            id_base[i] = mcarry + ex;
+            id_movers[i] = 0u;
+        }
+        mcarry += tot;
     }
     if (threadIdx.x == 0) *movers = n - (int)carry;
 }
 
-// Order-preserving split of the old sorted slots into kept pairs and movers.
+// The kept pairs in their old order (each warp from its offset).
 __global__ void __launch_bounds__(kSortThreads) k_inc_split(const int* __restrict__ old_k, const int* __restrict__ old_v,
                                                             const int* __restrict__ new_key_of, int n,
-                                                            const unsigned* __restrict__ tile_kept_base,
-                                                            int* kept_k, int* kept_v, int* mov_k, int* mov_v) {
-    __shared__ unsigned s_warp[kSortWarps];
-    const int base = blockIdx.x * kSortTile;
-    unsigned kept_run = tile_kept_base[blockIdx.x];
-    unsigned mov_run = (unsigned)base - kept_run;
-    for (int k = 0; k < kSortItems; ++k) {
-        const int chunk = base + k * kSortThreads;
-        const int i = chunk + threadIdx.x;
+                                                            const unsigned* __restrict__ warp_kept,
+                                                            const unsigned* __restrict__ tile_base, int* kept_k,
+                                                            int* kept_v) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wbase = blockIdx.x * kSortTile + warp * kWarpSlots;
+    if (wbase >= n) return;
+    unsigned off = tile_base[blockIdx.x];
+    for (int w = 0; w < warp; ++w) off += warp_kept[blockIdx.x * kSortWarps + w];
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll 4
+    for (int r = 0; r < kSortItems; ++r) {
+        const int i = wbase + r * 32 + lane;
         int key = 0, id = 0;
-        unsigned keep = 0;
+        bool keep = false;
         if (i < n) {
             id = old_v[i];
             key = __ldg(&new_key_of[id]);
             keep = key == old_k[i];
         }
-        unsigned tot;
-        const unsigned ex = block_scan_256(keep, s_warp, &tot);
-        if (i < n) {
-            if (keep) {
-                kept_k[kept_run + ex] = key;
-                kept_v[kept_run + ex] = id;
-            } else {
-                const unsigned m = mov_run + (threadIdx.x - ex);
-                mov_k[m] = key;
-                mov_v[m] = id;
-            }
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            kept_k[off + __popc(bal & lt)] = key;
+            kept_v[off + __popc(bal & lt)] = id;
         }
-        const int valid = min(kSortThreads, max(0, n - chunk));
-        kept_run += tot;
-        mov_run += (unsigned)valid - tot;
+        off += __popc(bal);
     }
 }
 
-// Merge the kept pairs (n - m) and the sorted movers (m) by (key, id): each
-// thread finds its 8-output diagonal on the merge path, then merges.
-__global__ void __launch_bounds__(256) k_inc_merge(const int* __restrict__ a_k, const int* __restrict__ a_v,
-                                                   const int* __restrict__ b_k, const int* __restrict__ b_v, int n,
-                                                   const int* __restrict__ movers, int* out_k, int* out_v) {
-    constexpr int kItems = 8;
-    const int m = *movers;
-    const int na = n - m, nb = m;
-    const long long diag = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kItems;
-    if (diag >= n) return;
-    // largest i with A[i-1] before B[diag-i]: the number of kept pairs among
-    // the first `diag` outputs
-    int lo = (int)max(0LL, diag - nb), hi = (int)min((long long)na, diag);
+// The movers in id order (keys: their new keys), from the flags, which it
+// clears: one CTA per 4096 ids, 16 per thread.
+__global__ void __launch_bounds__(kSortThreads) k_inc_movers(const int* __restrict__ new_key_of, int n,
+                                                             uint4* moved, const unsigned* __restrict__ id_base,
+                                                             int* mov_k, int* mov_v) {
+    __shared__ unsigned s_warp[kSortWarps];
+    const int id0 = blockIdx.x * kSortTile + threadIdx.x * 16;
+    uint4 f = make_uint4(0u, 0u, 0u, 0u);
+    if (id0 < n) f = moved[id0 / 16];   // the flags are padded to whole tiles
+    const unsigned w[4] = {f.x, f.y, f.z, f.w};
+    unsigned cnt = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        cnt += __popc(w[q] & 0x01010101u);
+    unsigned tot;
+    unsigned off = id_base[blockIdx.x] + block_scan_256(cnt, s_warp, &tot);
+    if (cnt == 0) return;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+            if ((w[q] >> (8 * b)) & 1u) {
+                const int id = id0 + 4 * q + b;
+                mov_k[off] = __ldg(&new_key_of[id]);
+                mov_v[off] = id;
+                ++off;
+            }
+    moved[id0 / 16] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// First index in [lo, hi) whose pair is not below x (the pairs are distinct).
+__device__ inline int pairs_below(const int* __restrict__ k, const int* __restrict__ v, int lo, int hi,
+                                  unsigned long long x) {
     while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        const int j = (int)(diag - mid);
-        if (pack_pair(a_k[mid - 1], a_v[mid - 1]) < pack_pair(b_k[j], b_v[j])) lo = mid;
-        else hi = mid - 1;
+        const int mid = (lo + hi) >> 1;
+        if (pack_pair(__ldg(&k[mid]), __ldg(&v[mid])) < x) lo = mid + 1;
+        else hi = mid;
     }
-    int i = lo, j = (int)(diag - lo);
-    const int end = (int)min((long long)n, diag + kItems);
-    for (int o = (int)diag; o < end; ++o) {
-        bool take_a;
-        if (i >= na) take_a = false;
-        else if (j >= nb) take_a = true;
-        else take_a = pack_pair(a_k[i], a_v[i]) < pack_pair(b_k[j], b_v[j]);
-        if (take_a) { out_k[o] = a_k[i]; out_v[o] = a_v[i]; ++i; }
-        else { out_k[o] = b_k[j]; out_v[o] = b_v[j]; ++j; }
+    return lo;
+}
+
+// Merge the kept pairs A (n - m, sorted) and the sorted movers B (m) by
+// (key, id).  Every pair's output index is its own index plus the number of
+// pairs of the other list below it.  CTAs [0, a_ctas) place A, 2048 pairs
+// each (thread t: pairs t, t + 256, ..., its count of B found once and then
+// advanced), so the writes stay coalesced; the others place B, each mover
+// by a binary search of A.
+constexpr int kMergeItems = 8;
+constexpr int kMergeTile = kSortThreads * kMergeItems;
+__global__ void __launch_bounds__(kSortThreads) k_inc_merge(const int* __restrict__ a_k, const int* __restrict__ a_v,
+                                                            const int* __restrict__ b_k, const int* __restrict__ b_v,
+                                                            int n, const int* __restrict__ movers, int a_ctas,
+                                                            int* out_k, int* out_v) {
+    const int m = *movers, na = n - m;
+    if ((int)blockIdx.x < a_ctas) {
+        const int base = blockIdx.x * kMergeTile + threadIdx.x;
+        int c = -1;
+#pragma unroll 1
+        for (int k = 0; k < kMergeItems; ++k) {
+            const int i = base + k * kSortThreads;
+            if (i >= na) break;
+            const int key = a_k[i], id = a_v[i];
+            const unsigned long long x = pack_pair(key, id);
+            if (c < 0) {
+                c = pairs_below(b_k, b_v, 0, m, x);
+            } else {
+                int step = 0;
+                while (c < m && step < 4 && pack_pair(__ldg(&b_k[c]), __ldg(&b_v[c])) < x) ++c, ++step;
+                if (step == 4) c = pairs_below(b_k, b_v, c, m, x);
+            }
+            out_k[i + c] = key;
+            out_v[i + c] = id;
+        }
+    } else {
+        const int stride = (gridDim.x - a_ctas) * kSortThreads;
+        for (int j = (blockIdx.x - a_ctas) * kSortThreads + threadIdx.x; j < m; j += stride) {
+            const int key = b_k[j], id = b_v[j];
+            const int r = pairs_below(a_k, a_v, 0, na, pack_pair(key, id));
+            out_k[j + r] = key;
+            out_v[j + r] = id;
+        }
     }
 }
 
 struct IncrementalBuffers {
     int* kept_k; int* kept_v;      // n each
-    int* mov_k; int* mov_v;        // n each (movers, unsorted)
-    int* t1_k; int* t1_v;          // n each (mover sort ping-pong)
-    int* t2_k; int* t2_v;          // n each
-    unsigned* tile_kept;           // radix_tiles(n)
+    int* mov_k; int* mov_v;        // n each (movers; sorted in place through t1)
+    int* t1_k; int* t1_v;          // n each
+    unsigned* warp_kept;           // 8 per tile
+    unsigned* tile_base;           // per tile
+    unsigned* id_movers;           // per id tile, zero between builds
+    unsigned* id_base;             // per id tile
+    unsigned char* moved;          // 4096 per id tile, zero between builds
     unsigned* temp;                // radix_temp_words(n)
     int* movers;                   // 1
 };
 
 // New sorted (out_k, out_v) from the previous frame's sorted (old_k, old_v)
-// and the new keys by particle id.
+// and the new keys by particle id.  Movers are gathered in id order, so one
+// stable sort by key puts them in (key, id) order.
 void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_key_of, int* out_k, int* out_v, int n,
                            int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s) {
+    (void)id_bits;
     if (n <= 0) return;
     const int ntiles = radix_tiles(n);
-    k_inc_count<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.tile_kept);
-    k_inc_scan<<<1, kSortThreads, 0, s>>>(b.tile_kept, ntiles, n, b.movers);
-    k_inc_split<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.tile_kept, b.kept_k, b.kept_v, b.mov_k,
-                                                b.mov_v);
-    // movers by id (values: keys), then stably by key (values: ids)
-    const int w1 = radix_sort_pairs_n(b.mov_v, b.mov_k, b.t1_k, b.t1_v, b.t2_k, b.t2_v, n, b.movers, id_bits, b.temp, s);
-    const int* by_id_k = w1 ? b.t2_k : b.t1_k;   // ids
-    const int* by_id_v = w1 ? b.t2_v : b.t1_v;   // keys
-    int* free_k = w1 ? b.t1_k : b.t2_k;
-    int* free_v = w1 ? b.t1_v : b.t2_v;
-    const int w2 =
-        radix_sort_pairs_n(by_id_v, by_id_k, b.mov_k, b.mov_v, free_k, free_v, n, b.movers, key_bits, b.temp, s);
-    const int* ms_k = w2 ? free_k : b.mov_k;
-    const int* ms_v = w2 ? free_v : b.mov_v;
-    const int threads = (n + 7) / 8;
-    k_inc_merge<<<(threads + 255) / 256, 256, 0, s>>>(b.kept_k, b.kept_v, ms_k, ms_v, n, b.movers, out_k, out_v);
+    k_inc_count<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.moved, b.id_movers);
+    k_inc_scan<<<1, kSortThreads, 0, s>>>(b.warp_kept, ntiles, n, b.tile_base, b.id_movers, b.id_base, b.movers);
+    k_inc_split<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_base, b.kept_k,
+                                                b.kept_v);
+    k_inc_movers<<<ntiles, kSortThreads, 0, s>>>(new_key_of, n, reinterpret_cast<uint4*>(b.moved), b.id_base,
+                                                 b.mov_k, b.mov_v);
+    const int w = radix_sort_pairs_n(b.mov_k, b.mov_v, b.t1_k, b.t1_v, b.mov_k, b.mov_v, n, b.movers, key_bits,
+                                     b.temp, s);
+    const int* ms_k = w ? b.mov_k : b.t1_k;
+    const int* ms_v = w ? b.mov_v : b.t1_v;
+    const int a_ctas = (n + kMergeTile - 1) / kMergeTile;
+    const int b_ctas = ntiles < 4 * 152 ? ntiles : 4 * 152;
+    k_inc_merge<<<a_ctas + b_ctas, kSortThreads, 0, s>>>(b.kept_k, b.kept_v, ms_k, ms_v, n, b.movers, a_ctas, out_k,
+                                                          out_v);
 }
 
 }  // namespace bcs

@@ -447,6 +447,12 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
         return {"median": float(np.median(d)), "p99": float(np.percentile(d, 99)), "max": float(d.max()),
                 "frac_above_1e-3_radius": float(np.mean(d > 1e-3 * 0.5))}
 
+    # a seeded subset of the same state against the FP64 oracle
+    subset = None
+    if args.learned_oracle_cells > 0:
+        subset = oracle_subset(args, scene, tuning, bcs, params, scales, warm, args.learned_oracle_macro_steps,
+                               args.learned_oracle_cells, args.seed + 1)
+
     rate = lambda ms: n * K * M / (ms / 1e3)
     return {
         "substeps": K, "macro_steps": M, "simulated_time": K * M * float(scene.params.dt),
@@ -461,6 +467,7 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
         "speedup_vs_plain": {"macro_plain": ms_plain / ms_macro, "surrogate": ms_plain / ms_sur},
         "network": dict(training, parameters=st["parameters"], flops_per_cell=st["flops_per_cell"]),
         "error_reference": "positions after the same simulated time, against plain frames from the same state",
+        "oracle_subset": subset,
     }
 
 
@@ -503,6 +510,58 @@ def position_error(p, ref, radius=0.5):
     d = np.linalg.norm(np.asarray(p, np.float64) - np.asarray(ref, np.float64), axis=1)
     return {"median": float(np.median(d)), "p99": float(np.percentile(d, 99)), "max": float(d.max()),
             "frac_above_1e-3_radius": float(np.mean(d > 1e-3 * radius))}
+
+
+def oracle_subset(args, scene, tuning, bcs, params, scales, warm, macro_steps, cells, seed):
+    """A seeded subset of `cells` cells of `scene` (same vessel, constants and
+    state) advanced by `warm` frames and `macro_steps` x K sub-steps on the
+    FP64 oracle (the host cores) and on the GPU as plain frames, plain macro
+    steps and macro steps with the network; each GPU path's positions against
+    the oracle's."""
+    import bcs_scenes as S
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    K = args.learned_substeps
+    sub = S.subset_scene(scene, cells, seed=seed)
+    t1 = time.perf_counter()
+    o = O.OracleSim(sub, threads=os.cpu_count())
+    o.step(warm + K * macro_steps)
+    po = o.get_particles()[0]
+    o.close()
+    oracle_s = time.perf_counter() - t1
+
+    def fresh_sub():
+        sim = bcs.Simulation(sub)
+        sim.set_particles(sub.positions, sub.velocities)
+        sim.set_tuning(**tuning)
+        sim.step(warm)
+        return sim
+    s1 = fresh_sub()
+    s1.step(K * macro_steps)
+    g_plain = s1.get_particles()[0]
+    s1.close()
+    s1 = fresh_sub()
+    s1.macro_step(K, macro_steps)
+    g_macro = s1.get_particles()[0]
+    s1.close()
+    s1 = fresh_sub()
+    z = bcs.Surrogate(s1, cell_type=1, substeps=K, max_samples=1, seed=11)
+    z.set_params(params)
+    z.set_scales(scales)
+    z.enable(True)
+    s1.macro_step(K, macro_steps)
+    g_sur = s1.get_particles()[0]
+    zst = z.stats()
+    z.close()
+    s1.close()
+    return {"cells": int(sum(t.count for t in sub.types)), "particles": sub.particle_count, "seed": seed,
+            "frames": warm + K * macro_steps, "oracle_seconds": round(oracle_s, 2),
+            "oracle_threads": os.cpu_count(),
+            "plain_vs_oracle": position_error(g_plain, po),
+            "macro_plain_vs_oracle": position_error(g_macro, po),
+            "surrogate_vs_oracle": position_error(g_sur, po),
+            "surrogate_cells_predicted": zst["predicted_cells"],
+            "surrogate_cells_fallen_back": zst["fallback_cells"]}
 
 
 def percentiles(per):
@@ -579,31 +638,8 @@ def run_scale(args):
     rate = lambda ms: n * K * M / (ms / 1e3)
 
     # the seeded 1k-cell subset against the FP64 oracle
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O
-    sub = S.subset_scene(scene, args.scale_subset_cells, seed=args.seed + 1)
-    ms_sub = args.scale_subset_macro_steps
-    t1 = time.perf_counter()
-    o = O.OracleSim(sub, threads=os.cpu_count())
-    o.step(args.warmup + K * ms_sub)
-    po = o.get_particles()[0]
-    o.close()
-    oracle_s = time.perf_counter() - t1
-    s1 = fresh(sub, tuning)
-    s1.step(K * ms_sub)
-    g_plain = s1.get_particles()[0]
-    s1.close()
-    s1 = fresh(sub, tuning)
-    s1.macro_step(K, ms_sub)
-    g_macro = s1.get_particles()[0]
-    s1.close()
-    s1 = fresh(sub, tuning)
-    z = with_network(s1)
-    s1.macro_step(K, ms_sub)
-    g_sur = s1.get_particles()[0]
-    zst = z.stats()
-    z.close()
-    s1.close()
+    subset = oracle_subset(args, scene, tuning, bcs, params, scales, args.warmup, args.scale_subset_macro_steps,
+                           args.scale_subset_cells, args.seed + 1)
 
     if rank == 0:
         out = {
@@ -622,15 +658,7 @@ def run_scale(args):
                               "cells_predicted": st["predicted_cells"], "cells_fallen_back": st["fallback_cells"],
                               "tolerance": st["tolerance"]},
                 "speedup_vs_plain": {"macro_plain": ms_plain / ms_macro, "surrogate": ms_plain / ms_sur},
-                "oracle_subset": {
-                    "cells": int(sum(t.count for t in sub.types)), "particles": sub.particle_count,
-                    "seed": args.seed + 1, "frames": args.warmup + K * ms_sub,
-                    "oracle_seconds": round(oracle_s, 2), "oracle_threads": os.cpu_count(),
-                    "plain_vs_oracle": position_error(g_plain, po),
-                    "macro_plain_vs_oracle": position_error(g_macro, po),
-                    "surrogate_vs_oracle": position_error(g_sur, po),
-                    "surrogate_cells_predicted": zst["predicted_cells"],
-                    "surrogate_cells_fallen_back": zst["fallback_cells"]},
+                "oracle_subset": subset,
                 "network": dict(training, parameters=st["parameters"], flops_per_cell=st["flops_per_cell"]),
                 "tuning": tuning, "autotune_ms": tune_ms,
             },
@@ -874,6 +902,9 @@ def main():
     ap.add_argument("--learned-collect", type=int, default=97,
                     help="training macro steps collected (97 x 20 588 disc cells = 2.0M cell-steps)")
     ap.add_argument("--learned-iters", type=int, default=4000)
+    ap.add_argument("--learned-oracle-cells", type=int, default=1000,
+                    help="cells of the seeded subset checked against the FP64 oracle (0: none)")
+    ap.add_argument("--learned-oracle-macro-steps", type=int, default=4)
     ap.add_argument("--learned-batch", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -362,7 +362,20 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_movers(const int* __restri
     moved[id0 / 16] = make_uint4(0u, 0u, 0u, 0u);
 }
 
-// First index in [lo, hi) whose pair is not below x (the pairs are distinct).
+// Merge path: how many of the first `diag` outputs of merging sorted A (na)
+// and B (nb) come from A (the pairs are distinct, so the split is unique).
+template <class GetA, class GetB>
+__device__ inline int merge_split(int diag, int na, int nb, GetA A, GetB B) {
+    int lo = max(0, diag - nb), hi = min(diag, na);
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A(mid - 1) < B(diag - mid)) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// First index in [lo, hi) whose pair is not below x.
 __device__ inline int pairs_below(const int* __restrict__ k, const int* __restrict__ v, int lo, int hi,
                                   unsigned long long x) {
     while (lo < hi) {
@@ -374,45 +387,94 @@ __device__ inline int pairs_below(const int* __restrict__ k, const int* __restri
 }
 
 // Merge the kept pairs A (n - m, sorted) and the sorted movers B (m) by
-// (key, id).  Every pair's output index is its own index plus the number of
-// pairs of the other list below it.  CTAs [0, a_ctas) place A, 2048 pairs
-// each (thread t: pairs t, t + 256, ..., its count of B found once and then
-// advanced), so the writes stay coalesced; the others place B, each mover
-// by a binary search of A.
+// (key, id), into the same result by one of two methods chosen on the device:
+//  * few movers (m <= n / 16): every pair's output index is its own index
+//    plus the number of pairs of the other list below it.  CTAs [0, a_ctas)
+//    place A, 2048 pairs each (thread t: pairs t, t + 256, ..., its count of
+//    B found once and then advanced), so the writes stay coalesced; the other
+//    CTAs place B, each mover by a binary search of A;
+//  * otherwise a CTA of the first a_ctas makes 2048 consecutive outputs: its
+//    two merge-path splits on global memory, its runs of A and B staged in
+//    shared memory, each thread's 8 outputs merged there and the tile written
+//    out coalesced.
 constexpr int kMergeItems = 8;
 constexpr int kMergeTile = kSortThreads * kMergeItems;
 __global__ void __launch_bounds__(kSortThreads) k_inc_merge(const int* __restrict__ a_k, const int* __restrict__ a_v,
                                                             const int* __restrict__ b_k, const int* __restrict__ b_v,
                                                             int n, const int* __restrict__ movers, int a_ctas,
                                                             int* out_k, int* out_v) {
-    const int m = *movers, na = n - m;
-    if ((int)blockIdx.x < a_ctas) {
-        const int base = blockIdx.x * kMergeTile + threadIdx.x;
-        int c = -1;
+    __shared__ unsigned long long s_in[kMergeTile];
+    __shared__ int s_split[2];
+    const int m = *movers, na = n - m, nb = m;
+    if (m <= n / 16) {
+        if ((int)blockIdx.x < a_ctas) {
+            const int base = blockIdx.x * kMergeTile + threadIdx.x;
+            int c = -1;
 #pragma unroll 1
-        for (int k = 0; k < kMergeItems; ++k) {
-            const int i = base + k * kSortThreads;
-            if (i >= na) break;
-            const int key = a_k[i], id = a_v[i];
-            const unsigned long long x = pack_pair(key, id);
-            if (c < 0) {
-                c = pairs_below(b_k, b_v, 0, m, x);
-            } else {
-                int step = 0;
-                while (c < m && step < 4 && pack_pair(__ldg(&b_k[c]), __ldg(&b_v[c])) < x) ++c, ++step;
-                if (step == 4) c = pairs_below(b_k, b_v, c, m, x);
+            for (int k = 0; k < kMergeItems; ++k) {
+                const int i = base + k * kSortThreads;
+                if (i >= na) break;
+                const int key = a_k[i], id = a_v[i];
+                const unsigned long long x = pack_pair(key, id);
+                if (c < 0) {
+                    c = pairs_below(b_k, b_v, 0, nb, x);
+                } else {
+                    int step = 0;
+                    while (c < nb && step < 4 && pack_pair(__ldg(&b_k[c]), __ldg(&b_v[c])) < x) ++c, ++step;
+                    if (step == 4) c = pairs_below(b_k, b_v, c, nb, x);
+                }
+                out_k[i + c] = key;
+                out_v[i + c] = id;
             }
-            out_k[i + c] = key;
-            out_v[i + c] = id;
+        } else {
+            const int stride = (gridDim.x - a_ctas) * kSortThreads;
+            for (int j = (blockIdx.x - a_ctas) * kSortThreads + threadIdx.x; j < nb; j += stride) {
+                const int key = b_k[j], id = b_v[j];
+                const int r = pairs_below(a_k, a_v, 0, na, pack_pair(key, id));
+                out_k[j + r] = key;
+                out_v[j + r] = id;
+            }
         }
-    } else {
-        const int stride = (gridDim.x - a_ctas) * kSortThreads;
-        for (int j = (blockIdx.x - a_ctas) * kSortThreads + threadIdx.x; j < m; j += stride) {
-            const int key = b_k[j], id = b_v[j];
-            const int r = pairs_below(a_k, a_v, 0, na, pack_pair(key, id));
-            out_k[j + r] = key;
-            out_v[j + r] = id;
+        return;
+    }
+    const int o0 = blockIdx.x * kMergeTile;
+    if ((int)blockIdx.x >= a_ctas || o0 >= n) return;
+    const int o1 = min(n, o0 + kMergeTile);
+    if (threadIdx.x < 2) {
+        auto A = [&](int i) { return pack_pair(__ldg(&a_k[i]), __ldg(&a_v[i])); };
+        auto B = [&](int j) { return pack_pair(__ldg(&b_k[j]), __ldg(&b_v[j])); };
+        s_split[threadIdx.x] = merge_split(threadIdx.x ? o1 : o0, na, nb, A, B);
+    }
+    __syncthreads();
+    const int i0 = s_split[0], i1 = s_split[1];
+    const int j0 = o0 - i0, la = i1 - i0, lb = (o1 - i1) - j0, len = la + lb;
+    for (int q = threadIdx.x; q < len; q += kSortThreads)
+        s_in[q] = q < la ? pack_pair(a_k[i0 + q], a_v[i0 + q]) : pack_pair(b_k[j0 + q - la], b_v[j0 + q - la]);
+    __syncthreads();
+    const int d = threadIdx.x * kMergeItems;
+    unsigned long long out[kMergeItems];
+    if (d < len) {
+        auto A = [&](int i) { return s_in[i]; };
+        auto B = [&](int j) { return s_in[la + j]; };
+        int i = merge_split(d, la, lb, A, B), j = d - i;
+#pragma unroll
+        for (int k = 0; k < kMergeItems; ++k) {
+            if (d + k >= len) break;
+            const bool take_a = j >= lb || (i < la && s_in[i] < s_in[la + j]);
+            out[k] = take_a ? s_in[i++] : s_in[la + j++];
         }
+    }
+    __syncthreads();
+    if (d < len) {
+#pragma unroll
+        for (int k = 0; k < kMergeItems; ++k)
+            if (d + k < len) s_in[d + k] = out[k];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < len; q += kSortThreads) {
+        const unsigned long long x = s_in[q];
+        out_k[o0 + q] = (int)(unsigned)(x >> 32);
+        out_v[o0 + q] = (int)(unsigned)x;
     }
 }
 

@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __r
     __shared__ int2 s_stage[kSortTile];
     const int n = dyn_n(n_max, d_n);
     const int live = (n + kSortTile - 1) / kSortTile;
+    if ((int)blockIdx.x >= live) return;   // no tile for this CTA (a device-side count far below n_max)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned digit_base_total;
     {
@@ -240,7 +241,8 @@ constexpr int kWarpSlots = kSortTile / kSortWarps;   // 512
 // the movers' particle ids are flagged and counted per 4096-id tile.
 __global__ void __launch_bounds__(kSortThreads) k_inc_count(const int* __restrict__ old_k, const int* __restrict__ old_v,
                                                             const int* __restrict__ new_key_of, int n,
-                                                            unsigned* __restrict__ warp_kept, unsigned char* moved,
+                                                            unsigned* __restrict__ warp_kept,
+                                                            unsigned* __restrict__ tile_kept, unsigned char* moved,
                                                             unsigned* id_movers) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wbase = blockIdx.x * kSortTile + warp * kWarpSlots;
@@ -263,40 +265,41 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_count(const int* __restric
             if ((peers & ((1u << lane) - 1u)) == 0) atomicAdd(&id_movers[id >> 12], (unsigned)__popc(peers));
         }
     }
-    if (lane == 0) warp_kept[blockIdx.x * kSortWarps + warp] = kept;
+    __shared__ unsigned s_kept[kSortWarps];
+    if (lane == 0) {
+        warp_kept[blockIdx.x * kSortWarps + warp] = kept;
+        s_kept[warp] = kept;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) t += s_kept[w];
+        tile_kept[blockIdx.x] = t;
+    }
 }
 
 // One CTA: exclusive scans of the per-tile kept counts (slot tiles) and of
-// the per-id-tile mover counts (which it clears for the next build); the
-// number of movers into *movers.
-__global__ void __launch_bounds__(kSortThreads) k_inc_scan(const unsigned* __restrict__ warp_kept, int ntiles, int n,
+// the per-id-tile mover counts (which it clears for the next build), side by
+// side; the number of movers into *movers.
+__global__ void __launch_bounds__(kSortThreads) k_inc_scan(const unsigned* __restrict__ tile_kept, int ntiles, int n,
                                                            unsigned* tile_base, unsigned* id_movers, unsigned* id_base,
                                                            int* movers) {
-    __shared__ unsigned s_warp[kSortWarps];
-    unsigned carry = 0;
+    __shared__ unsigned s_warp[2][kSortWarps];
+    unsigned carry = 0, mcarry = 0;
     for (int base = 0; base < ntiles; base += kSortThreads) {
         const int i = base + threadIdx.x;
-        unsigned v = 0;
+        const unsigned v = i < ntiles ? tile_kept[i] : 0u, w = i < ntiles ? id_movers[i] : 0u;
+        unsigned tot, mtot;
+        const unsigned ex = block_scan_256(v, s_warp[0], &tot);
+        const unsigned mex = block_scan_256(w, s_warp[1], &mtot);
         if (i < ntiles) {
-#pragma unroll
-            for (int w = 0; w < kSortWarps; ++w) v += warp_kept[i * kSortWarps + w];
-        }
-        unsigned tot;
-        const unsigned ex = block_scan_256(v, s_warp, &tot);
-        if (i < ntiles) tile_base[i] = carry + ex;
-        carry += tot;
-    }
-    unsigned mcarry = 0;
-    for (int base = 0; base < ntiles; base += kSortThreads) {
-        const int i = base + threadIdx.x;
-        const unsigned v = i < ntiles ? id_movers[i] : 0u;
-        unsigned tot;
-        const unsigned ex = block_scan_256(v, s_warp, &tot);
-        if (i < ntiles) {
-            id_base[i] = mcarry + ex;
+            tile_base[i] = carry + ex;
+            id_base[i] = mcarry + mex;
             id_movers[i] = 0u;
         }
-        mcarry += tot;
+        carry += tot;
+        mcarry += mtot;
     }
     if (threadIdx.x == 0) *movers = n - (int)carry;
 }
@@ -483,6 +486,7 @@ struct IncrementalBuffers {
     int* mov_k; int* mov_v;        // n each (movers; sorted in place through t1)
     int* t1_k; int* t1_v;          // n each
     unsigned* warp_kept;           // 8 per tile
+    unsigned* tile_kept;           // per tile
     unsigned* tile_base;           // per tile
     unsigned* id_movers;           // per id tile, zero between builds
     unsigned* id_base;             // per id tile
@@ -499,8 +503,9 @@ void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_ke
     (void)id_bits;
     if (n <= 0) return;
     const int ntiles = radix_tiles(n);
-    k_inc_count<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.moved, b.id_movers);
-    k_inc_scan<<<1, kSortThreads, 0, s>>>(b.warp_kept, ntiles, n, b.tile_base, b.id_movers, b.id_base, b.movers);
+    k_inc_count<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_kept, b.moved,
+                                                b.id_movers);
+    k_inc_scan<<<1, kSortThreads, 0, s>>>(b.tile_kept, ntiles, n, b.tile_base, b.id_movers, b.id_base, b.movers);
     k_inc_split<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_base, b.kept_k,
                                                 b.kept_v);
     k_inc_movers<<<ntiles, kSortThreads, 0, s>>>(new_key_of, n, reinterpret_cast<uint4*>(b.moved), b.id_base,

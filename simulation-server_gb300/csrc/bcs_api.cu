@@ -1571,9 +1571,17 @@ static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
         else enqueue_frame(s);
     };
     for (int i = 0; i < n; ++i) {
-        if (!s->keys_valid || s->p.refresh_triangle_centers) {
+        // the first frame of a grid, or with triangle centres refreshed, runs
+        // eagerly (its sort is a full one)
+        if (s->p.refresh_triangle_centers || (!s->keys_valid && !s->pg.sorted_once)) {
             enqueue();
             continue;
+        }
+        if (!s->keys_valid) {
+            // keys of positions set from outside, then the frame's usual graph
+            launch_keys(s->pos[s->cur], s->N, s->pg.g.uniform, s->scenes, s->S, s->pg.in_k, s->pg.in_v, s->err,
+                        s->stream);
+            s->keys_valid = true;
         }
         cudaGraphExec_t& g = s->graphs[(long long)substeps * 4 + s->cur * 2 + s->pg.slot];
         if (!g) {

@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const int* __res
                                                                 unsigned* __restrict__ hist) {
     __shared__ unsigned s_hist[kRadix];
     const int n = dyn_n(n_max, d_n);
+    if (d_n && n <= kSortTile) return;   // k_radix_small sorted them
     const int live = (n + kSortTile - 1) / kSortTile;
     for (int tile = blockIdx.x; tile < live; tile += gridDim.x) {
         s_hist[threadIdx.x] = 0;
@@ -91,6 +92,7 @@ __device__ inline unsigned block_scan_256(unsigned v, unsigned* s_warp, unsigned
 __global__ void __launch_bounds__(kSortThreads) k_scan_rows(unsigned* rows, int stride, const int* __restrict__ d_n,
                                                             unsigned* totals) {
     __shared__ unsigned s_warp[kSortWarps];
+    if (d_n && *d_n <= kSortTile) return;   // k_radix_small sorted them
     unsigned* row = rows + (size_t)blockIdx.x * stride;
     const int len = d_n ? (*d_n + kSortTile - 1) / kSortTile : stride;
     unsigned carry = 0;
@@ -117,6 +119,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __r
     __shared__ unsigned s_warp[kSortWarps];
     __shared__ int2 s_stage[kSortTile];
     const int n = dyn_n(n_max, d_n);
+    if (d_n && n <= kSortTile) return;   // k_radix_small sorted them
     const int live = (n + kSortTile - 1) / kSortTile;
     if ((int)blockIdx.x >= live) return;   // no tile for this CTA (a device-side count far below n_max)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -188,6 +191,86 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __r
     }
 }
 
+// A device-side count of at most one tile (4 096 pairs), sorted by one CTA
+// through every pass in shared memory, with the downsweep's stable ranking
+// (pair j: warp j / 512, round j % 512 / 32, lane j % 32); larger counts are
+// left to the pass kernels, which return at once for small ones.  in and
+// out may be the same arrays.
+__global__ void __launch_bounds__(kSortThreads) k_radix_small(const int* in_k, const int* in_v, int* out_k, int* out_v,
+                                                              const int* __restrict__ d_n, int bits) {
+    __shared__ unsigned s_cnt[kSortWarps][kRadix];
+    __shared__ unsigned s_tile[kRadix];
+    __shared__ unsigned s_warp[kSortWarps];
+    __shared__ int2 s_stage[kSortTile];
+    const int n = *d_n;
+    if (n > kSortTile) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wbase = warp * (kSortTile / kSortWarps);
+    const unsigned lt = (1u << lane) - 1u;
+    int key[kSortItems], val[kSortItems];
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int i = wbase + r * 32 + lane;
+        key[r] = i < n ? in_k[i] : 0;
+        val[r] = i < n ? in_v[i] : 0;
+    }
+    for (int shift = 0; shift < bits; shift += 8) {
+        for (int d = lane; d < kRadix; d += 32) s_cnt[warp][d] = 0;
+        __syncwarp();
+        unsigned rank[kSortItems];
+#pragma unroll
+        for (int r = 0; r < kSortItems; ++r) {
+            const bool ok = wbase + r * 32 + lane < n;
+            const unsigned d = ok ? (((unsigned)key[r] >> shift) & 0xFFu) : 0x100u;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const unsigned before = __popc(peers & lt);
+            const unsigned cnt = ok ? s_cnt[warp][d] : 0u;
+            rank[r] = cnt + before;
+            __syncwarp();
+            if (ok && before == 0) s_cnt[warp][d] = cnt + __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        unsigned run = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) {
+            const unsigned c = s_cnt[w][threadIdx.x];
+            s_cnt[w][threadIdx.x] = run;
+            run += c;
+        }
+        {
+            unsigned tot;
+            s_tile[threadIdx.x] = block_scan_256(run, s_warp, &tot);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kSortItems; ++r) {
+            if (wbase + r * 32 + lane >= n) continue;
+            const unsigned d = ((unsigned)key[r] >> shift) & 0xFFu;
+            s_stage[s_tile[d] + s_cnt[warp][d] + rank[r]] = make_int2(key[r], val[r]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kSortItems; ++r) {
+            const int i = wbase + r * 32 + lane;
+            if (i < n) {
+                const int2 kv = s_stage[i];
+                key[r] = kv.x;
+                val[r] = kv.y;
+            }
+        }
+        __syncthreads();   // s_cnt and s_stage are rewritten by the next pass
+    }
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int i = wbase + r * 32 + lane;
+        if (i < n) {
+            out_k[i] = key[r];
+            out_v[i] = val[r];
+        }
+    }
+}
+
 int radix_tiles(int n) { return (n + kSortTile - 1) / kSortTile; }
 size_t radix_temp_words(int n) { return (size_t)kRadix * radix_tiles(n) + kRadix; }
 
@@ -204,6 +287,12 @@ int radix_sort_pairs_n(const int* in_k, const int* in_v, int* a_k, int* a_v, int
     // a device-side count is usually far below n: a bounded grid strides
     // over the tiles that hold data
     const int grid = d_n ? (ntiles < 4 * 152 ? ntiles : 4 * 152) : ntiles;
+    if (d_n) {
+        // where the passes would leave the result: (a) after an odd number
+        const int passes = (bits + 7) / 8;
+        k_radix_small<<<1, kSortThreads, 0, s>>>(in_k, in_v, (passes & 1) ? a_k : b_k, (passes & 1) ? a_v : b_v, d_n,
+                                                 bits);
+    }
     int pass = 0;
     for (int shift = 0; shift < bits; shift += 8, ++pass) {
         const int* ki = pass == 0 ? in_k : ((pass & 1) ? a_k : b_k);

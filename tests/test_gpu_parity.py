@@ -286,6 +286,26 @@ def test_incremental_grid_after_reshuffle(lib, small):
     np.testing.assert_array_equal(en, oen)
 
 
+@pytest.mark.parametrize("moved", [4000, 4096, 4200])
+def test_incremental_grid_mover_counts(lib, small, moved):
+    # Around one sort tile of movers (4 096): up to it the movers are sorted
+    # by one CTA, above it by the tiled passes; both must give the oracle's
+    # grid.
+    sim = make(small)
+    sim.step(2)
+    pos0, _, _ = sim.get_particles()
+    rng = np.random.default_rng(moved)
+    pick = rng.choice(len(pos0), size=moved, replace=False)
+    pos = pos0.copy()
+    pos[pick] = pos0[np.roll(pick, 1)]   # a cycle: each picked particle takes another's place
+    sim.set_particles(pos, np.zeros_like(pos))
+    sim.calculate_grids()
+    k, i, _, _ = sim.get_grid(0, dense=False)
+    ok, oi, _, _, _ = O.OracleSim(small).grid_of_points(pos)
+    np.testing.assert_array_equal(k, ok)
+    np.testing.assert_array_equal(i, oi)
+
+
 def test_moving_wall_rebuilds_bounds(lib):
     # Vein vertices start with a velocity that carries them past the 0.5
     # rebuild margin of the triangle bounds / wall mask within the run; the

@@ -393,7 +393,6 @@ void refresh_args(bcs_sim* s, int in, int out, bool write_keys) {
     a.vel_out = s->vel[out];
     a.frc_out = s->frc[out];
     a.keys_out = write_keys ? s->pg.in_k : nullptr;
-    a.ids_out = write_keys ? s->pg.in_v : nullptr;
     a.pg = s->pg.g;
     // grid-order collisions once the grid carries its row starts and sorted copies
     a.coll = s->pg.rows_on && a.pg.row_start && a.pg.spos && a.pg.svel ? s->coll : nullptr;

@@ -139,8 +139,8 @@ struct StepArgs {
     float4* pos_out;
     float4* vel_out;
     float4* frc_out;
-    int* keys_out;        // next-step grid keys (canonical order) or null
-    int* ids_out;
+    int* keys_out;        // next-step grid keys by particle id, or null (the ids beside them
+                          // stay the identity the key kernel wrote once)
     float4* fext;         // macro steps: external force of sub-step 1 (held), or null
     const unsigned char* skip_cell;   // macro steps: cells the network advanced (k_substeps skips them), or null
     int n;

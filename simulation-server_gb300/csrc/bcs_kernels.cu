@@ -632,10 +632,7 @@ __device__ inline void advance_particle(const StepArgs& a, const SceneDev& sc, c
     a.pos_out[pid] = make_float4(nx.x, nx.y, nx.z, px.w);
     a.vel_out[pid] = make_float4(nv.x, nv.y, nv.z, 0.f);
     a.frc_out[pid] = make_float4(F.x, F.y, F.z, 0.f);
-    if (MODE == kFull && a.keys_out) {
-        a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, nx, e) : 0;
-        a.ids_out[pid] = pid;
-    }
+    if (MODE == kFull && a.keys_out) a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, nx, e) : 0;
     if (MODE == kFull && a.fext) {
         // macro step: the external part of this force, held by sub-steps 2..K
         const float3 fx = F - favg;
@@ -1401,10 +1398,7 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
         a.pos_out[pid] = x;
         a.vel_out[pid] = v;
         a.frc_out[pid] = s_frc[i];
-        if (a.keys_out) {
-            a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, xyz(x), e) : 0;
-            a.ids_out[pid] = pid;
-        }
+        if (a.keys_out) a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, xyz(x), e) : 0;
     }
     if (e) atomicOr(a.err, e);
 }
@@ -1610,10 +1604,7 @@ __global__ void k_sur_apply(const StepArgs a, const SurDev d, const float* __res
         a.pos_out[p] = make_float4(x.x, x.y, x.z, w);
         a.vel_out[p] = make_float4(v.x, v.y, v.z, 0.f);
         a.frc_out[p] = make_float4(pF[nk].x, pF[nk].y, pF[nk].z, 0.f);
-        if (a.keys_out) {
-            a.keys_out[p] = a.pg.uniform ? grid_key(scn.pg, x, e) : 0;
-            a.ids_out[p] = p;
-        }
+        if (a.keys_out) a.keys_out[p] = a.pg.uniform ? grid_key(scn.pg, x, e) : 0;
     }
     if (e) atomicOr(a.err, e);
 }
@@ -2146,10 +2137,7 @@ __global__ void __launch_bounds__(MT * 64, 1)
         a.pos_out[p] = make_float4(x.x, x.y, x.z, w);
         a.vel_out[p] = make_float4(v.x, v.y, v.z, 0.f);
         a.frc_out[p] = make_float4(Ysm[k * kOut + 6], Ysm[k * kOut + 7], Ysm[k * kOut + 8], 0.f);
-        if (a.keys_out) {
-            a.keys_out[p] = a.pg.uniform ? grid_key(scn.pg, x, e) : 0;
-            a.ids_out[p] = p;
-        }
+        if (a.keys_out) a.keys_out[p] = a.pg.uniform ? grid_key(scn.pg, x, e) : 0;
     }
     if (e) atomicOr(a.err, e);
 }

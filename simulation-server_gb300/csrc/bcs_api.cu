@@ -216,6 +216,11 @@ struct bcs_sim {
     std::vector<float> h_type_bound, h_vein_box;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t pev[BCS_PHASE_COUNT + 1] = {};
+    // a second stream for independent work within a frame (the vein springs
+    // beside the grid build, the vein update beside the vein-end rule, the
+    // row starts beside the sorted copies), forked and joined with events
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev[3] = {}, join_ev[3] = {};
     float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
     int kernels_per_step = 0;
     // asynchronous reads of the particle state (bcs_get_particles_async):
@@ -342,7 +347,10 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
 // Sort the grid's unsorted keys into the other result slot and rebuild the
 // range table.  After the first build, a grid flagged incremental starts
 // from the previous order (any permutation works; few movers make it cheap).
-void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, const float4* vel = nullptr) {
+// With `side` (and its fork / join events) the row starts are built there,
+// beside the sorted copies on `st`.
+void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, const float4* vel = nullptr,
+               cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr) {
     const int out = dg.slot ^ 1;
     if (dg.incremental && dg.sorted_once) {
         sort_grid_incremental(dg.s_k[dg.slot], dg.s_v[dg.slot], dg.in_k, dg.s_k[out], dg.s_v[out], dg.count, dg.bits,
@@ -367,11 +375,19 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, con
     dg.g.spos = dg.spos_on && pos ? dg.spos : nullptr;
     dg.g.svel = dg.spos_on && pos && vel ? dg.svel : nullptr;
     float4* svel_out = dg.spos_on && pos && vel ? dg.svel : nullptr;
+    const bool beside = dg.rows_on && side;
+    if (beside) {
+        cudaEventRecord(fork, st);
+        cudaStreamWaitEvent(side, fork, 0);
+        launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, side);
+        cudaEventRecord(join, side);
+    }
     launch_cell_ranges(dg.g.keys, dg.count, dg.table_on ? dg.table : nullptr, dg.epoch,
                        dg.occ_on && dg.table_on ? dg.occ : nullptr, dg.g.ids, pos, dg.spos_on && pos ? dg.spos : nullptr,
                        vel, svel_out, st);
     dg.table_current = dg.table_on;
-    if (dg.rows_on) launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, st);
+    if (beside) cudaStreamWaitEvent(st, join, 0);
+    else if (dg.rows_on) launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, st);
     dg.g.row_start = dg.rows_on ? dg.row_start : nullptr;
 }
 
@@ -430,7 +446,8 @@ void enqueue_grids(bcs_sim* s) {
         launch_keys(s->pos[s->cur], s->N, s->pg.g.uniform, s->scenes, s->S, s->pg.in_k, s->pg.in_v, s->err, s->stream);
         s->keys_valid = true;
     }
-    if (s->pg.g.uniform) sort_grid(s->pg, s->stream, s->pos[s->cur], s->vel[s->cur]);
+    if (s->pg.g.uniform)
+        sort_grid(s->pg, s->stream, s->pos[s->cur], s->vel[s->cur], s->side, s->fork_ev[0], s->join_ev[0]);
     if (s->p.refresh_triangle_centers) build_triangle_grid(s, true);
     s->grid_ready = true;
 }
@@ -441,29 +458,63 @@ void enqueue_vein_forces(bcs_sim* s) {
                             s->err, s->stream);
 }
 
-void enqueue_vein_propagate(bcs_sim* s) {
+void enqueue_vein_propagate(bcs_sim* s, bool bump = true) {
     if (s->p.vein_dynamic && s->V > 0) {
         launch_vein_integrate(s->vpos, s->vvel, s->vfrc, s->V, s->p.dt, s->stream);
         build_triangle_grid(s, false);
     }
-    launch_bump_step(s->steps, 1, s->stream);
+    if (bump) launch_bump_step(s->steps, 1, s->stream);
 }
+
+// Work enqueued while it lives goes to the side stream, after everything
+// enqueued on the main stream so far (fork event k); join() makes the main
+// stream wait for it (join event k).
+struct OnSide {
+    bcs_sim* s;
+    cudaStream_t main;
+    int k;
+    OnSide(bcs_sim* sim, int slot) : s(sim), main(sim->stream), k(slot) {
+        cudaEventRecord(s->fork_ev[k], main);
+        cudaStreamWaitEvent(s->side, s->fork_ev[k], 0);
+        s->stream = s->side;
+    }
+    ~OnSide() {
+        cudaEventRecord(s->join_ev[k], s->side);
+        s->stream = main;
+    }
+    static void join(bcs_sim* sim, int slot) { cudaStreamWaitEvent(sim->stream, sim->join_ev[slot], 0); }
+};
 
 // One fused frame on the stream (no host synchronisation).  With `ev`, an
 // event is recorded before each phase and after the last one.
 void enqueue_frame(bcs_sim* s, cudaEvent_t* ev = nullptr) {
     if (ev) cudaEventRecord(ev[0], s->stream);
+    // The vein springs read only the vein and add into its forces: they run
+    // beside the grid build and end before the step kernel adds its impacts.
+    const bool vein = s->p.vein_dynamic && s->V > 0;
+    if (vein) {
+        OnSide side(s, 1);
+        enqueue_vein_forces(s);
+    }
     enqueue_grids(s);
     if (ev) cudaEventRecord(ev[1], s->stream);
-    enqueue_vein_forces(s);
+    if (vein) OnSide::join(s, 1);
+    else enqueue_vein_forces(s);
     if (ev) cudaEventRecord(ev[2], s->stream);
     const int in = s->cur, out = s->cur ^ 1;
     refresh_args(s, in, out, true);
     launch_step(s->args, (int)s->work_host.size(), 0, s->tune.step_shape, s->persistent_grid[0], s->stream,
                 ev ? ev[3] : nullptr);
+    // The vein update (integration, triangle operands for the next frame)
+    // runs beside the vein-end rule, which touches only particles.
+    if (vein) {
+        OnSide side(s, 2);
+        enqueue_vein_propagate(s, false);
+    }
     if (s->p.use_blood_flow) launch_vein_end(s->args, s->C, s->stream);
     if (ev) cudaEventRecord(ev[4], s->stream);
-    enqueue_vein_propagate(s);
+    if (vein) OnSide::join(s, 2);
+    launch_bump_step(s->steps, 1, s->stream);   // after the vein-end rule, which reads the counter
     if (ev) cudaEventRecord(ev[5], s->stream);
     s->cur = out;
     s->keys_valid = true;    // k_step wrote keys of the new positions
@@ -720,6 +771,11 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     BCS_CUDA(cudaEventCreate(&s->ev0));
     BCS_CUDA(cudaEventCreate(&s->ev1));
     for (auto& e : s->pev) BCS_CUDA(cudaEventCreate(&e));
+    BCS_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    for (int k = 0; k < 3; ++k) {
+        BCS_CUDA(cudaEventCreateWithFlags(&s->fork_ev[k], cudaEventDisableTiming));
+        BCS_CUDA(cudaEventCreateWithFlags(&s->join_ev[k], cudaEventDisableTiming));
+    }
     const bool puniform = s->p.particle_grid == BCS_GRID_UNIFORM;
     const bool tuniform = s->p.triangle_grid == BCS_GRID_UNIFORM;
 
@@ -1025,6 +1081,14 @@ void destroy_impl(bcs_sim* s) {
     if (s->ev1) cudaEventDestroy(s->ev1);
     for (auto& e : s->pev)
         if (e) cudaEventDestroy(e);
+    if (s->side) {
+        cudaStreamSynchronize(s->side);
+        cudaStreamDestroy(s->side);
+    }
+    for (int k = 0; k < 3; ++k) {
+        if (s->fork_ev[k]) cudaEventDestroy(s->fork_ev[k]);
+        if (s->join_ev[k]) cudaEventDestroy(s->join_ev[k]);
+    }
     for (int k = 0; k < 2; ++k) {
         if (s->aready[k]) cudaEventDestroy(s->aready[k]);
         if (s->adone[k]) cudaEventDestroy(s->adone[k]);

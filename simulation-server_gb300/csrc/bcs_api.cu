@@ -96,7 +96,8 @@ struct IncrementalBuffers {
     int* movers;
 };
 void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_key_of, int* out_k, int* out_v, int n,
-                           int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s);
+                           int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s,
+                           cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 }  // namespace bcs
 
 using namespace bcs;
@@ -220,7 +221,7 @@ struct bcs_sim {
     // beside the grid build, the vein update beside the vein-end rule, the
     // row starts beside the sorted copies), forked and joined with events
     cudaStream_t side = nullptr;
-    cudaEvent_t fork_ev[3] = {}, join_ev[3] = {};
+    cudaEvent_t fork_ev[4] = {}, join_ev[4] = {};
     float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
     int kernels_per_step = 0;
     // asynchronous reads of the particle state (bcs_get_particles_async):
@@ -348,13 +349,15 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
 // range table.  After the first build, a grid flagged incremental starts
 // from the previous order (any permutation works; few movers make it cheap).
 // With `side` (and its fork / join events) the row starts are built there,
-// beside the sorted copies on `st`.
+// beside the sorted copies on `st`, and (fork2 / join2) an incremental
+// build's movers are sorted there beside the compaction of the kept pairs.
 void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, const float4* vel = nullptr,
-               cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr) {
+               cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr,
+               cudaEvent_t fork2 = nullptr, cudaEvent_t join2 = nullptr) {
     const int out = dg.slot ^ 1;
     if (dg.incremental && dg.sorted_once) {
         sort_grid_incremental(dg.s_k[dg.slot], dg.s_v[dg.slot], dg.in_k, dg.s_k[out], dg.s_v[out], dg.count, dg.bits,
-                              dg.id_bits, dg.inc, st);
+                              dg.id_bits, dg.inc, st, side, side ? fork2 : nullptr, side ? join2 : nullptr);
     } else {
         // the full sort's result lands in its first ping-pong buffer after an
         // odd number of passes (or none), in the second after an even number
@@ -447,7 +450,8 @@ void enqueue_grids(bcs_sim* s) {
         s->keys_valid = true;
     }
     if (s->pg.g.uniform)
-        sort_grid(s->pg, s->stream, s->pos[s->cur], s->vel[s->cur], s->side, s->fork_ev[0], s->join_ev[0]);
+        sort_grid(s->pg, s->stream, s->pos[s->cur], s->vel[s->cur], s->side, s->fork_ev[0], s->join_ev[0],
+                  s->fork_ev[3], s->join_ev[3]);
     if (s->p.refresh_triangle_centers) build_triangle_grid(s, true);
     s->grid_ready = true;
 }
@@ -772,7 +776,7 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     BCS_CUDA(cudaEventCreate(&s->ev1));
     for (auto& e : s->pev) BCS_CUDA(cudaEventCreate(&e));
     BCS_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
         BCS_CUDA(cudaEventCreateWithFlags(&s->fork_ev[k], cudaEventDisableTiming));
         BCS_CUDA(cudaEventCreateWithFlags(&s->join_ev[k], cudaEventDisableTiming));
     }
@@ -1085,7 +1089,7 @@ void destroy_impl(bcs_sim* s) {
         cudaStreamSynchronize(s->side);
         cudaStreamDestroy(s->side);
     }
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
         if (s->fork_ev[k]) cudaEventDestroy(s->fork_ev[k]);
         if (s->join_ev[k]) cudaEventDestroy(s->join_ev[k]);
     }

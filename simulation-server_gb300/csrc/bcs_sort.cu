@@ -586,21 +586,32 @@ struct IncrementalBuffers {
 
 // New sorted (out_k, out_v) from the previous frame's sorted (old_k, old_v)
 // and the new keys by particle id.  Movers are gathered in id order, so one
-// stable sort by key puts them in (key, id) order.
+// stable sort by key puts them in (key, id) order.  With `side` (and its
+// fork / join events) the movers are gathered and sorted there, beside the
+// compaction of the kept pairs on `s`.
 void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_key_of, int* out_k, int* out_v, int n,
-                           int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s) {
+                           int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s,
+                           cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
     (void)id_bits;
     if (n <= 0) return;
     const int ntiles = radix_tiles(n);
     k_inc_count<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_kept, b.moved,
                                                 b.id_movers);
     k_inc_scan<<<1, kSortThreads, 0, s>>>(b.tile_kept, ntiles, n, b.tile_base, b.id_movers, b.id_base, b.movers);
+    cudaStream_t ms = s;
+    if (side) {
+        cudaEventRecord(fork, s);
+        cudaStreamWaitEvent(side, fork, 0);
+        ms = side;
+    }
+    k_inc_movers<<<ntiles, kSortThreads, 0, ms>>>(new_key_of, n, reinterpret_cast<uint4*>(b.moved), b.id_base,
+                                                  b.mov_k, b.mov_v);
+    const int w = radix_sort_pairs_n(b.mov_k, b.mov_v, b.t1_k, b.t1_v, b.mov_k, b.mov_v, n, b.movers, key_bits,
+                                     b.temp, ms);
+    if (side) cudaEventRecord(join, side);
     k_inc_split<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_base, b.kept_k,
                                                 b.kept_v);
-    k_inc_movers<<<ntiles, kSortThreads, 0, s>>>(new_key_of, n, reinterpret_cast<uint4*>(b.moved), b.id_base,
-                                                 b.mov_k, b.mov_v);
-    const int w = radix_sort_pairs_n(b.mov_k, b.mov_v, b.t1_k, b.t1_v, b.mov_k, b.mov_v, n, b.movers, key_bits,
-                                     b.temp, s);
+    if (side) cudaStreamWaitEvent(s, join, 0);
     const int* ms_k = w ? b.mov_k : b.t1_k;
     const int* ms_v = w ? b.mov_v : b.t1_v;
     const int a_ctas = (n + kMergeTile - 1) / kMergeTile;

@@ -36,9 +36,31 @@ constexpr int kSortWarps = kSortThreads / 32;
 
 __device__ inline int dyn_n(int n, const int* d_n) { return d_n ? *d_n : n; }
 
+// Programmatic dependent launch: a kernel launched with launch_after may be
+// scheduled while the kernel before it in the stream finishes; it calls
+// after_previous() before it touches memory (the wait returns once that
+// kernel has completed and its writes are visible; without the launch
+// attribute it returns at once).
+__device__ __forceinline__ void after_previous() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... Params, typename... Args>
+void launch_after(void (*kernel)(Params...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 __global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const int* __restrict__ keys, int n_max,
                                                                 const int* __restrict__ d_n, int shift, int ntiles,
                                                                 unsigned* __restrict__ hist) {
+    after_previous();
     __shared__ unsigned s_hist[kRadix];
     const int n = dyn_n(n_max, d_n);
     if (d_n && n <= kSortTile) return;   // k_radix_small sorted them
@@ -91,6 +113,7 @@ __device__ inline unsigned block_scan_256(unsigned v, unsigned* s_warp, unsigned
 // into totals[row].
 __global__ void __launch_bounds__(kSortThreads) k_scan_rows(unsigned* rows, int stride, const int* __restrict__ d_n,
                                                             unsigned* totals) {
+    after_previous();
     __shared__ unsigned s_warp[kSortWarps];
     if (d_n && *d_n <= kSortTile) return;   // k_radix_small sorted them
     unsigned* row = rows + (size_t)blockIdx.x * stride;
@@ -113,6 +136,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __r
                                                                   int shift, int ntiles,
                                                                   const unsigned* __restrict__ offsets,
                                                                   const unsigned* __restrict__ totals) {
+    after_previous();
     __shared__ unsigned s_cnt[kSortWarps][kRadix];
     __shared__ unsigned s_base[kRadix];      // global start of the tile's run of each digit
     __shared__ unsigned s_tile[kRadix];      // tile-local start of each digit
@@ -198,6 +222,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __r
 // out may be the same arrays.
 __global__ void __launch_bounds__(kSortThreads) k_radix_small(const int* in_k, const int* in_v, int* out_k, int* out_v,
                                                               const int* __restrict__ d_n, int bits) {
+    after_previous();
     __shared__ unsigned s_cnt[kSortWarps][kRadix];
     __shared__ unsigned s_tile[kRadix];
     __shared__ unsigned s_warp[kSortWarps];
@@ -290,8 +315,8 @@ int radix_sort_pairs_n(const int* in_k, const int* in_v, int* a_k, int* a_v, int
     if (d_n) {
         // where the passes would leave the result: (a) after an odd number
         const int passes = (bits + 7) / 8;
-        k_radix_small<<<1, kSortThreads, 0, s>>>(in_k, in_v, (passes & 1) ? a_k : b_k, (passes & 1) ? a_v : b_v, d_n,
-                                                 bits);
+        launch_after(k_radix_small, 1, kSortThreads, s, in_k, in_v, (passes & 1) ? a_k : b_k,
+                     (passes & 1) ? a_v : b_v, d_n, bits);
     }
     int pass = 0;
     for (int shift = 0; shift < bits; shift += 8, ++pass) {
@@ -299,9 +324,12 @@ int radix_sort_pairs_n(const int* in_k, const int* in_v, int* a_k, int* a_v, int
         const int* vi = pass == 0 ? in_v : ((pass & 1) ? a_v : b_v);
         int* ko = (pass & 1) ? b_k : a_k;
         int* vo = (pass & 1) ? b_v : a_v;
-        k_radix_upsweep<<<grid, kSortThreads, 0, s>>>(ki, n, d_n, shift, ntiles, temp);
-        k_scan_rows<<<kRadix, kSortThreads, 0, s>>>(temp, ntiles, d_n, totals);
-        k_radix_downsweep<<<grid, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, d_n, shift, ntiles, temp, totals);
+        // after the small sort (device-side count) or the previous pass
+        if (d_n || pass > 0) launch_after(k_radix_upsweep, grid, kSortThreads, s, ki, n, d_n, shift, ntiles, temp);
+        else k_radix_upsweep<<<grid, kSortThreads, 0, s>>>(ki, n, d_n, shift, ntiles, temp);
+        launch_after(k_scan_rows, kRadix, kSortThreads, s, temp, ntiles, d_n, totals);
+        launch_after(k_radix_downsweep, grid, kSortThreads, s, ki, vi, ko, vo, n, d_n, shift, ntiles,
+                     (const unsigned*)temp, (const unsigned*)totals);
     }
     return (pass & 1) ? 0 : 1;
 }
@@ -333,6 +361,7 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_count(const int* __restric
                                                             unsigned* __restrict__ warp_kept,
                                                             unsigned* __restrict__ tile_kept, unsigned char* moved,
                                                             unsigned* id_movers) {
+    after_previous();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wbase = blockIdx.x * kSortTile + warp * kWarpSlots;
     unsigned kept = 0;
@@ -374,6 +403,7 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_count(const int* __restric
 __global__ void __launch_bounds__(kSortThreads) k_inc_scan(const unsigned* __restrict__ tile_kept, int ntiles, int n,
                                                            unsigned* tile_base, unsigned* id_movers, unsigned* id_base,
                                                            int* movers) {
+    after_previous();
     __shared__ unsigned s_warp[2][kSortWarps];
     unsigned carry = 0, mcarry = 0;
     for (int base = 0; base < ntiles; base += kSortThreads) {
@@ -399,6 +429,7 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_split(const int* __restric
                                                             const unsigned* __restrict__ warp_kept,
                                                             const unsigned* __restrict__ tile_base, int* kept_k,
                                                             int* kept_v) {
+    after_previous();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wbase = blockIdx.x * kSortTile + warp * kWarpSlots;
     if (wbase >= n) return;
@@ -429,6 +460,7 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_split(const int* __restric
 __global__ void __launch_bounds__(kSortThreads) k_inc_movers(const int* __restrict__ new_key_of, int n,
                                                              uint4* moved, const unsigned* __restrict__ id_base,
                                                              int* mov_k, int* mov_v) {
+    after_previous();
     __shared__ unsigned s_warp[kSortWarps];
     const int id0 = blockIdx.x * kSortTile + threadIdx.x * 16;
     uint4 f = make_uint4(0u, 0u, 0u, 0u);
@@ -495,6 +527,7 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_merge(const int* __restric
                                                             const int* __restrict__ b_k, const int* __restrict__ b_v,
                                                             int n, const int* __restrict__ movers, int a_ctas,
                                                             int* out_k, int* out_v) {
+    after_previous();
     __shared__ unsigned long long s_in[kMergeTile];
     __shared__ int s_split[2];
     const int m = *movers, na = n - m, nb = m;
@@ -597,7 +630,8 @@ void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_ke
     const int ntiles = radix_tiles(n);
     k_inc_count<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_kept, b.moved,
                                                 b.id_movers);
-    k_inc_scan<<<1, kSortThreads, 0, s>>>(b.tile_kept, ntiles, n, b.tile_base, b.id_movers, b.id_base, b.movers);
+    launch_after(k_inc_scan, 1, kSortThreads, s, (const unsigned*)b.tile_kept, ntiles, n, b.tile_base, b.id_movers,
+                 b.id_base, b.movers);
     cudaStream_t ms = s;
     if (side) {
         cudaEventRecord(fork, s);
@@ -609,8 +643,8 @@ void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_ke
     const int w = radix_sort_pairs_n(b.mov_k, b.mov_v, b.t1_k, b.t1_v, b.mov_k, b.mov_v, n, b.movers, key_bits,
                                      b.temp, ms);
     if (side) cudaEventRecord(join, side);
-    k_inc_split<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_base, b.kept_k,
-                                                b.kept_v);
+    launch_after(k_inc_split, ntiles, kSortThreads, s, old_k, old_v, new_key_of, n, (const unsigned*)b.warp_kept,
+                 (const unsigned*)b.tile_base, b.kept_k, b.kept_v);
     if (side) cudaStreamWaitEvent(s, join, 0);
     const int* ms_k = w ? b.mov_k : b.t1_k;
     const int* ms_v = w ? b.mov_v : b.t1_v;

@@ -314,4 +314,25 @@ __device__ inline int find_range(int n, T x, F start_of) {
     return lo;
 }
 
+// Programmatic dependent launch: a kernel launched with launch_after may be
+// scheduled while the kernel before it in the stream finishes; it calls
+// after_previous() before it touches memory that kernel (or anything before
+// it) writes.  The wait returns once that kernel has completed and its writes
+// are visible; in a kernel launched without the attribute it returns at once.
+__device__ __forceinline__ void after_previous() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... Params, typename... Args>
+inline void launch_after(void (*kernel)(Params...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 }  // namespace bcs

@@ -26,6 +26,8 @@
 
 #include <cstdint>
 
+#include "bcs_internal.cuh"
+
 namespace bcs {
 
 constexpr int kSortThreads = 256;
@@ -36,26 +38,7 @@ constexpr int kSortWarps = kSortThreads / 32;
 
 __device__ inline int dyn_n(int n, const int* d_n) { return d_n ? *d_n : n; }
 
-// Programmatic dependent launch: a kernel launched with launch_after may be
-// scheduled while the kernel before it in the stream finishes; it calls
-// after_previous() before it touches memory (the wait returns once that
-// kernel has completed and its writes are visible; without the launch
-// attribute it returns at once).
-__device__ __forceinline__ void after_previous() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-template <typename... Params, typename... Args>
-void launch_after(void (*kernel)(Params...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kernel, args...);
-}
 
 __global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const int* __restrict__ keys, int n_max,
                                                                 const int* __restrict__ d_n, int shift, int ntiles,

@@ -12,7 +12,10 @@
  *  - Every call returns bcs_status; nothing exits the process or prints.
  *  - The library owns its device buffers.  A handle is used by one host
  *    thread at a time; different handles are independent.
- *  - All device work is enqueued on the handle's stream.  Getters that write
+ *  - All device work is enqueued on the handle's stream.  Inside a frame the
+ *    library forks independent work onto an internal stream of the handle
+ *    and joins it back before the frame's last operation, so the handle's
+ *    stream orders every call as if it ran all the work.  Getters that write
  *    host memory synchronise that stream.
  *  - Vectors cross the boundary as three SoA float arrays, the layout of the
  *    reference's cudaVec3 (src/utilities/cuda_vec3.cuh:11-72).

@@ -306,6 +306,25 @@ def test_incremental_grid_mover_counts(lib, small, moved):
     np.testing.assert_array_equal(i, oi)
 
 
+@pytest.mark.parametrize("moved", [3000, 6000])
+def test_captured_frame_mover_counts(lib, small, moved):
+    # The same inside a replayed frame graph, on both sides of one tile of
+    # movers (the one-CTA sort, the tiled passes).
+    sim = make(small)
+    sim.step(4)   # both buffer parities captured
+    pos0, _, _ = sim.get_particles()
+    rng = np.random.default_rng(moved + 1)
+    pick = rng.choice(len(pos0), size=moved, replace=False)
+    pos = pos0.copy()
+    pos[pick] = pos0[np.roll(pick, 1)]
+    sim.set_particles(pos, np.zeros_like(pos))
+    sim.step(1)   # keys of the uploaded state, then the captured frame
+    k, i, _, _ = sim.get_grid(0, dense=False)
+    ok, oi, _, _, _ = O.OracleSim(small).grid_of_points(pos)
+    np.testing.assert_array_equal(k, ok)
+    np.testing.assert_array_equal(i, oi)
+
+
 def test_moving_wall_rebuilds_bounds(lib):
     # Vein vertices start with a velocity that carries them past the 0.5
     # rebuild margin of the triangle bounds / wall mask within the run; the

@@ -41,7 +41,7 @@ typedef enum bcs_status {
     BCS_ERR_CUDA = 2,             /* a CUDA runtime call failed             */
     BCS_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed               */
     BCS_ERR_NO_DEVICE = 4,        /* no CUDA device / extension unusable    */
-    BCS_ERR_UNSUPPORTED = 5,      /* valid request this build cannot serve  */
+    BCS_ERR_UNSUPPORTED = 5,      /* valid request the library cannot serve */
     BCS_ERR_TIMEOUT = 6           /* a bounded device wait gave up; the work
                                      it guarded was skipped                 */
 } bcs_status;

@@ -74,7 +74,7 @@ inline void bcs_tape_param(A&& a) {
 }
 
 // The recorder's own CPU replay calls a kernel (a plain host function in
-// this build) with the bytes of its arguments through this thunk.
+// the recorder's compile) with the bytes of its arguments through this thunk.
 template <class... P, size_t... I>
 inline void bcs_tape_invoke(void (*f)(P...), unsigned char* const* a, std::index_sequence<I...>) {
     f(*reinterpret_cast<P*>(a[I])...);

@@ -314,7 +314,7 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
         const int tiles = radix_tiles(count);
         if ((st = dalloc(s, &dg.inc.kept_k, count)) || (st = dalloc(s, &dg.inc.kept_v, count)) ||
             (st = dalloc(s, &dg.inc.mov_k, count)) || (st = dalloc(s, &dg.inc.mov_v, count)) ||
-            (st = dalloc(s, &dg.inc.warp_kept, 8 * (size_t)tiles)) || (st = dalloc(s, &dg.inc.tile_kept, tiles)) ||
+            (st = dalloc(s, &dg.inc.warp_kept, 32 * (size_t)tiles)) || (st = dalloc(s, &dg.inc.tile_kept, tiles)) ||
             (st = dalloc(s, &dg.inc.tile_base, tiles)) ||
             (st = dalloc(s, &dg.inc.id_movers, tiles)) || (st = dalloc(s, &dg.inc.id_base, tiles)) ||
             (st = dalloc(s, &dg.inc.moved, 4096 * (size_t)tiles)) || (st = dalloc(s, &dg.inc.movers, 1)))

@@ -333,13 +333,18 @@ __device__ inline unsigned long long pack_pair(int key, int id) {
     return ((unsigned long long)(unsigned)key << 32) | (unsigned)id;
 }
 
-// Slot i of a tile belongs to warp (i % 4096) / 512, round (i % 512) / 32,
-// lane i % 32: each warp compacts its own 512 consecutive slots.
-constexpr int kWarpSlots = kSortTile / kSortWarps;   // 512
+// The compaction kernels run 1 024 threads per 4 096-slot tile (two CTAs
+// fill an SM): slot i of a tile belongs to warp (i % 4096) / 128, round
+// (i % 128) / 32, lane i % 32, so each warp compacts its own 128 consecutive
+// slots.
+constexpr int kIncThreads = 1024;
+constexpr int kIncWarps = kIncThreads / 32;            // 32
+constexpr int kWarpSlots = kSortTile / kIncWarps;      // 128
+constexpr int kWarpRounds = kWarpSlots / 32;           // 4
 
 // Per warp of every 4096-slot tile, the pairs whose particle kept its key;
 // the movers' particle ids are flagged and counted per 4096-id tile.
-__global__ void __launch_bounds__(kSortThreads) k_inc_count(const int* __restrict__ old_k, const int* __restrict__ old_v,
+__global__ void __launch_bounds__(kIncThreads) k_inc_count(const int* __restrict__ old_k, const int* __restrict__ old_v,
                                                             const int* __restrict__ new_key_of, int n,
                                                             unsigned* __restrict__ warp_kept,
                                                             unsigned* __restrict__ tile_kept, unsigned char* moved,
@@ -348,8 +353,8 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_count(const int* __restric
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wbase = blockIdx.x * kSortTile + warp * kWarpSlots;
     unsigned kept = 0;
-#pragma unroll 4
-    for (int r = 0; r < kSortItems; ++r) {
+#pragma unroll
+    for (int r = 0; r < kWarpRounds; ++r) {
         const int i = wbase + r * 32 + lane;
         bool keep = true;
         int id = 0;
@@ -366,17 +371,17 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_count(const int* __restric
             if ((peers & ((1u << lane) - 1u)) == 0) atomicAdd(&id_movers[id >> 12], (unsigned)__popc(peers));
         }
     }
-    __shared__ unsigned s_kept[kSortWarps];
+    __shared__ unsigned s_kept[kIncWarps];
     if (lane == 0) {
-        warp_kept[blockIdx.x * kSortWarps + warp] = kept;
+        warp_kept[blockIdx.x * kIncWarps + warp] = kept;
         s_kept[warp] = kept;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned t = 0;
+    if (warp == 0) {
+        unsigned t = s_kept[lane];
 #pragma unroll
-        for (int w = 0; w < kSortWarps; ++w) t += s_kept[w];
-        tile_kept[blockIdx.x] = t;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) tile_kept[blockIdx.x] = t;
     }
 }
 
@@ -407,7 +412,7 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_scan(const unsigned* __res
 }
 
 // The kept pairs in their old order (each warp from its offset).
-__global__ void __launch_bounds__(kSortThreads) k_inc_split(const int* __restrict__ old_k, const int* __restrict__ old_v,
+__global__ void __launch_bounds__(kIncThreads) k_inc_split(const int* __restrict__ old_k, const int* __restrict__ old_v,
                                                             const int* __restrict__ new_key_of, int n,
                                                             const unsigned* __restrict__ warp_kept,
                                                             const unsigned* __restrict__ tile_base, int* kept_k,
@@ -416,11 +421,14 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_split(const int* __restric
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wbase = blockIdx.x * kSortTile + warp * kWarpSlots;
     if (wbase >= n) return;
-    unsigned off = tile_base[blockIdx.x];
-    for (int w = 0; w < warp; ++w) off += warp_kept[blockIdx.x * kSortWarps + w];
+    // this warp's offset: the tile's, plus the kept counts of the warps before it
     const unsigned lt = (1u << lane) - 1u;
-#pragma unroll 4
-    for (int r = 0; r < kSortItems; ++r) {
+    unsigned before = lane < warp ? warp_kept[blockIdx.x * kIncWarps + lane] : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    unsigned off = tile_base[blockIdx.x] + before;
+#pragma unroll
+    for (int r = 0; r < kWarpRounds; ++r) {
         const int i = wbase + r * 32 + lane;
         int key = 0, id = 0;
         bool keep = false;
@@ -590,7 +598,7 @@ struct IncrementalBuffers {
     int* kept_k; int* kept_v;      // n each
     int* mov_k; int* mov_v;        // n each (movers; sorted in place through t1)
     int* t1_k; int* t1_v;          // n each
-    unsigned* warp_kept;           // 8 per tile
+    unsigned* warp_kept;           // 32 per tile
     unsigned* tile_kept;           // per tile
     unsigned* tile_base;           // per tile
     unsigned* id_movers;           // per id tile, zero between builds
@@ -611,8 +619,8 @@ void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_ke
     (void)id_bits;
     if (n <= 0) return;
     const int ntiles = radix_tiles(n);
-    k_inc_count<<<ntiles, kSortThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_kept, b.moved,
-                                                b.id_movers);
+    k_inc_count<<<ntiles, kIncThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_kept, b.moved,
+                                               b.id_movers);
     launch_after(k_inc_scan, 1, kSortThreads, s, (const unsigned*)b.tile_kept, ntiles, n, b.tile_base, b.id_movers,
                  b.id_base, b.movers);
     cudaStream_t ms = s;
@@ -626,7 +634,7 @@ void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_ke
     const int w = radix_sort_pairs_n(b.mov_k, b.mov_v, b.t1_k, b.t1_v, b.mov_k, b.mov_v, n, b.movers, key_bits,
                                      b.temp, ms);
     if (side) cudaEventRecord(join, side);
-    launch_after(k_inc_split, ntiles, kSortThreads, s, old_k, old_v, new_key_of, n, (const unsigned*)b.warp_kept,
+    launch_after(k_inc_split, ntiles, kIncThreads, s, old_k, old_v, new_key_of, n, (const unsigned*)b.warp_kept,
                  (const unsigned*)b.tile_base, b.kept_k, b.kept_v);
     if (side) cudaStreamWaitEvent(s, join, 0);
     const int* ms_k = w ? b.mov_k : b.t1_k;

@@ -830,6 +830,11 @@ def run_ours(args):
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{cinfo['particles']} particles (inflow end of the same vessel) x {cinfo['steps']} "
                          f"steps in {cinfo['seconds']} s, FP64 oracle, {threads} OpenMP threads"}
+        if threads > 1:
+            # the same oracle on one core, a smaller sample of the same scene
+            v1, c1, _ = time_oracle(scene, args.cpu_budget / 4, warmup=1, max_steps=2, threads=1)
+            cpu["one_core"] = {"value": v1, "unit": UNIT, "cores": 1,
+                               "sample": f"{c1['particles']} particles x {c1['steps']} steps in {c1['seconds']} s"}
 
     if rank == 0:
         shape = bcs.STEP_SHAPES[tuning["step_shape"]]

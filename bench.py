@@ -146,8 +146,14 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_scene(cells_per_type, seed):
+def build_scene(cells_per_type, seed, widen=1.0):
+    """The Y bifurcation (radii 40 and 28) with `cells_per_type` cells of each
+    type; widen > 1 scales the radii and the wall's resolution around them
+    (a shorter vessel for the same cells, so that the grid at cell 1.0 stays
+    inside the 31-bit key space: 100k cells need widen 1.5)."""
     import bcs_scenes as S
+    if widen != 1.0:
+        return S.scale_scene(2 * cells_per_type, seed=seed, widen=widen)
     return S.bifurcation_scene(cells_per_type=cells_per_type, seed=seed)
 
 
@@ -185,7 +191,8 @@ def workload_config(scene, n_gpus):
         "dt": round(float(p.dt), 8),
         "grid_cell": float(p.cell_width),
         "triangle_cell": float(p.cell_width_triangles),
-        "l2": "state (6 x float4 x N = 403 MB) exceeds the 129 MB L2; no flush",
+        "trunk_radius": float(p.cylinder_radius),
+        "l2": f"state (6 x float4 x N = {96 * scene.particle_count / 1e6:.0f} MB) exceeds the 129 MB L2; no flush",
         "parallelism": f"replicas x{n_gpus}",
     }
 
@@ -687,7 +694,7 @@ def run_ours(args):
     bcs_build.build()
     bcs.set_device(local)
     batched = args.workload == "batched"
-    scene = build_batch(args) if batched else build_scene(args.cells_per_type, args.seed + rank)
+    scene = build_batch(args) if batched else build_scene(args.cells_per_type, args.seed + rank, args.widen)
     all_pos = np.concatenate([sc.positions for sc in scene]) if batched else scene.positions
     all_vel = np.concatenate([sc.velocities for sc in scene]) if batched else scene.velocities
 
@@ -881,6 +888,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells-per-type", type=int, default=CELLS_PER_TYPE)
+    ap.add_argument("--widen", type=float, default=1.0,
+                    help="scale the vessel's radii (1.5 keeps 50k cells per type inside the key space)")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--profile-steps", type=int, default=0, help="0 = as many as --steps")
     ap.add_argument("--e2e-steps", type=int, default=0, help="0 = as many as --steps")

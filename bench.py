@@ -34,6 +34,10 @@ autotuner picked in the first, so all three follow the same trajectory.
   reference_cuda  the reference's own CUDA kernels (its sources compiled
             unmodified, its host code replayed from a launch tape) on the same
             GPU, the workload's geometry and population, per-frame CUDA events
+  batched_workload  the 64-vessel batched workload (71.8M particles) at full
+            size, 20 graph-replayed frames after the warm-up
+  scale_workload    the 1M-cell (102M-particle) surrogate workload, shortened
+            to two macro steps of each path, with its oracle subset
 
 --impl reference times that CPU implementation alone (the reference has no
 CPU path of its own; its CUDA kernels are timed beside the product through
@@ -462,6 +466,7 @@ def learned_substep(args, scene, tuning, bcs, fresh, warm):
 
     rate = lambda ms: n * K * M / (ms / 1e3)
     return {
+        "_params": params, "_scales": scales,
         "substeps": K, "macro_steps": M, "simulated_time": K * M * float(scene.params.dt),
         "plain": {"ms": ms_plain, "particle_steps_per_s": rate(ms_plain)},
         "macro_plain": {"ms": ms_macro, "particle_steps_per_s": rate(ms_macro), "position_error": err(pb),
@@ -573,6 +578,101 @@ def oracle_subset(args, scene, tuning, bcs, params, scales, warm, macro_steps, c
 
 def percentiles(per):
     return {f"p{q}": float(np.percentile(per, q)) for q in (50, 95, 99)}
+
+
+def batched_summary(args, tuning, bcs, frames, warm):
+    """The batched workload at its full size inside the default run: the 64
+    seeded straight vessels (71.8M particles) in one simulation, `warm`
+    frames, then `frames` graph-replayed frames timed with CUDA events.  The
+    tuning is the one the autotuner picked for the bifurcation workload (the
+    batched workload's own autotuning picks the same launch shape and
+    collision kernel); `--workload batched` runs the full measurement."""
+    t0 = time.perf_counter()
+    scenes = build_batch(args)
+    build_s = time.perf_counter() - t0
+    sim = bcs.Simulation(scenes)
+    sim.set_particles(np.concatenate([sc.positions for sc in scenes]),
+                      np.concatenate([sc.velocities for sc in scenes]))
+    sim.set_tuning(**tuning)
+    sim.step(warm)
+    ms = sim.time_steps(frames)
+    n = sim.n
+    errw = sim.error_word()
+    sim.close()
+    names = [nm for bit, nm in ((1, "a position outside the grid box"),
+                                (2, "a zero vector normalised (a particle at rest meets the vein ray, "
+                                    "as in the reference, whose normalize gives NaN there)"),
+                                (4, "a non-finite position or velocity")) if errw & bit]
+    return {"frames": frames, "warmup": warm, "ms_per_step": ms / frames,
+            "particle_steps_per_s": n * frames / (ms / 1e3), "unit": UNIT, "error_word": errw,
+            "error_word_bits": names,
+            "tuning": tuning, "tuning_source": "the bifurcation workload's autotuned setting",
+            "scene_build_seconds": round(build_s, 1), "config": batch_config(scenes, 1)}
+
+
+def scale_summary(args, tuning, bcs, params, scales, macro_steps, warm):
+    """The surrogate-at-scale workload inside the default run, shortened: 1M
+    cells (102M particles) in the 6x widened bifurcation; plain frames, plain
+    macro steps and macro steps with the network (the one trained for the
+    bifurcation workload) advance `macro_steps` x K sub-steps from the same
+    state, each frame or macro step timed alone; the seeded 1k-cell subset
+    is checked against the FP64 oracle.  `--workload scale` runs the full
+    measurement (125 macro steps)."""
+    import bcs_scenes as S
+    K = args.learned_substeps
+    t0 = time.perf_counter()
+    scene = S.scale_scene(args.scale_cells, seed=args.seed)
+    build_s = time.perf_counter() - t0
+
+    def fresh():
+        sim = bcs.Simulation(scene)
+        sim.set_particles(scene.positions, scene.velocities)
+        sim.set_tuning(**tuning)
+        sim.step(warm)
+        return sim
+
+    sim = fresh()
+    n = sim.n
+    per_frame = [sim.time_steps(1) for _ in range(K * macro_steps)]
+    pa = sim.get_particles()[0]
+    sim.close()
+    sim = fresh()
+    per_macro = [sim.time_macro_steps(K, 1) for _ in range(macro_steps)]
+    pb = sim.get_particles()[0]
+    sim.close()
+    sim = fresh()
+    sur = bcs.Surrogate(sim, cell_type=1, substeps=K, max_samples=1, seed=11)
+    sur.set_params(params)
+    sur.set_scales(scales)
+    sur.enable(True)
+    per_sur = [sim.time_macro_steps(K, 1) for _ in range(macro_steps)]
+    pc = sim.get_particles()[0]
+    st = sur.stats()
+    sur.close()
+    sim.close()
+    ms_plain, ms_macro, ms_sur = float(sum(per_frame)), float(sum(per_macro)), float(sum(per_sur))
+    rate = lambda ms: n * K * macro_steps / (ms / 1e3)
+    subset = oracle_subset(args, scene, tuning, bcs, params, scales, warm, args.scale_subset_macro_steps,
+                           args.scale_subset_cells, args.seed + 1)
+    return {
+        "substeps": K, "macro_steps": macro_steps, "plain_equivalent_steps": K * macro_steps, "warmup": warm,
+        "plain": {"ms": ms_plain, "particle_steps_per_s": rate(ms_plain),
+                  "frame_latency_ms": percentiles(per_frame)},
+        "macro_plain": {"ms": ms_macro, "particle_steps_per_s": rate(ms_macro),
+                        "macro_step_latency_ms": percentiles(per_macro),
+                        "position_error_vs_plain_frames": position_error(pb, pa)},
+        "surrogate": {"ms": ms_sur, "particle_steps_per_s": rate(ms_sur),
+                      "macro_step_latency_ms": percentiles(per_sur),
+                      "position_error_vs_plain_frames": position_error(pc, pa),
+                      "cells_predicted": st["predicted_cells"], "cells_fallen_back": st["fallback_cells"]},
+        "speedup_vs_plain": {"macro_plain": ms_plain / ms_macro, "surrogate": ms_plain / ms_sur},
+        "oracle_subset": subset,
+        "tuning_source": "the bifurcation workload's autotuned setting",
+        "config": dict(workload_config(scene, 1), scene_build_seconds=round(build_s, 1),
+                       workload=f"surrogate at scale, widened Y bifurcation, {scene.particle_count} particles "
+                                f"({scene.types[0].count} icosphere-42 + {scene.types[1].count} "
+                                f"biconcave-162 cells)"),
+    }
 
 
 def run_scale(args):
@@ -720,6 +820,8 @@ def run_ours(args):
         tuning = sim.get_tuning().as_dict()
         sim.close()
         learned = learned_substep(args, scene, tuning, bcs, fresh, args.warmup)
+        learned.pop("_params")
+        learned.pop("_scales")
         if rank == 0:
             print(json.dumps({"metric": METRIC, "unit": UNIT, "learned_substep": learned,
                               "config": workload_config(scene, ws)}), flush=True)
@@ -817,12 +919,29 @@ def run_ours(args):
     sim.close()
     e2e_value = whole_job_rate(n, e2e_steps, 1e3 * e2e_s, ws)
 
-    learned = None
+    learned, params, scales = None, None, None
     if rank == 0 and not args.no_learned and not batched:
         try:
             learned = learned_substep(args, scene, tuning, bcs, fresh, args.warmup)
+            params, scales = learned.pop("_params"), learned.pop("_scales")
         except Exception as exc:   # the plain line is still printed
             learned = {"error": f"{type(exc).__name__}: {exc}"}
+
+    # ---- the batched and the at-scale workloads, shortened, on the same GPU
+    # (each simulation of the passes above is closed by now)
+    batched_line = None
+    if rank == 0 and ws == 1 and not batched and not args.no_batched:
+        try:
+            batched_line = batched_summary(args, tuning, bcs, args.batched_frames, args.warmup)
+        except Exception as exc:
+            batched_line = {"error": f"{type(exc).__name__}: {exc}"}
+    scale_line = None
+    if rank == 0 and ws == 1 and not batched and not args.no_scale and params is not None:
+        try:
+            scale_line = scale_summary(args, tuning, bcs, params, scales, args.scale_summary_macro_steps,
+                                       args.warmup)
+        except Exception as exc:
+            scale_line = {"error": f"{type(exc).__name__}: {exc}"}
 
     ref_cuda = None
     if rank == 0 and not batched and not args.no_reference_cuda:
@@ -870,6 +989,8 @@ def run_ours(args):
             "phase_ms": {k: v / prof_steps for k, v in phases.items()},
             "diagnostics_after_timed_run": diag,
             "learned_substep": learned,
+            "batched_workload": batched_line,
+            "scale_workload": scale_line,
             "clocks": clocks,
             "cpu_baseline": cpu,
             "reference_cuda": ref_cuda,
@@ -911,6 +1032,12 @@ def main():
     ap.add_argument("--scale-subset-cells", type=int, default=1000)
     ap.add_argument("--scale-subset-macro-steps", type=int, default=4)
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the shortened batched-workload run of the default line")
+    ap.add_argument("--batched-frames", type=int, default=20)
+    ap.add_argument("--no-scale", action="store_true",
+                    help="skip the shortened at-scale surrogate run of the default line")
+    ap.add_argument("--scale-summary-macro-steps", type=int, default=2)
     ap.add_argument("--learned-substeps", type=int, default=8)
     ap.add_argument("--learned-macro-steps", type=int, default=40)
     ap.add_argument("--learned-collect", type=int, default=97,

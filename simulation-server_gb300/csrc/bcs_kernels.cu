@@ -581,11 +581,32 @@ __device__ inline void respawn(const StepArgs& a, const SceneDev& sc, int cell_i
     v = f3(a.p.init_velocity[0], a.p.init_velocity[1], a.p.init_velocity[2]);
 }
 
-// The scene of a CTA, staged in shared memory.
+// Asynchronous global -> shared copies (cp.async): a thread issues all of
+// its copies, then waits once (cp_async_wait_all) for every copy it issued;
+// a barrier after that publishes them to the CTA.  Staging through them
+// keeps every copy of a CTA in flight at once, where a load-then-store loop
+// waits for each of its loads in turn, and the threads can compute while
+// the copies land.
+__device__ inline void cp_async4(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ inline void cp_async16(void* smem, const void* gmem) {   // both 16-byte aligned
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ inline void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// The scene of a CTA, staged in shared memory (copies left in flight).
 __device__ inline void stage_scene(const SceneDev* src, SceneDev* dst) {
     const int* s = reinterpret_cast<const int*>(src);
     int* d = reinterpret_cast<int*>(dst);
-    for (int i = threadIdx.x; i < (int)(sizeof(SceneDev) / sizeof(int)); i += blockDim.x) d[i] = s[i];
+    for (int i = threadIdx.x; i < (int)(sizeof(SceneDev) / sizeof(int)); i += blockDim.x) cp_async4(d + i, s + i);
 }
 
 // ------------------------------------------------------------- k_step ----
@@ -654,10 +675,11 @@ __device__ inline void step_item(const StepArgs& a, int item, float4* s_pos, flo
     const int np = w.ncells * pic;
     stage_scene(a.scenes + ty.scene, &sc);
     for (int i = threadIdx.x; i < np; i += THREADS) {
-        s_pos[i] = a.pos_in[p0 + i];
-        s_vel[i] = a.vel_in[p0 + i];
-        s_frc[i] = a.frc_in[p0 + i];
+        cp_async16(s_pos + i, a.pos_in + p0 + i);
+        cp_async16(s_vel + i, a.vel_in + p0 + i);
+        cp_async16(s_frc + i, a.frc_in + p0 + i);
     }
+    cp_async_wait_all();
     __syncthreads();
 
     // Cell centroids (blood_cells.cu:44-61), one warp per cell, fixed-order
@@ -1048,10 +1070,12 @@ __global__ void __launch_bounds__(kCollideThreads) k_collide(const StepArgs a) {
 // contiguous slot range: the CTA stages the three ranges' keys, positions
 // and velocities and the rows' first slots, then every thread runs the
 // nine binary searches and its windows' candidates on shared memory.  Same
-// candidates, same order, same sum as collide_slot.  A tile that spans two
-// planes or scenes, or whose ranges exceed kTileStage slots (crowded rows),
-// takes the global-memory search instead; so does a particle whose stencil
-// does not follow its sorted key.
+// candidates, same order, same sum as collide_slot.  The staging is one
+// round of asynchronous copies, and each thread computes its particle's
+// stencil while they land.  A tile that spans two planes or scenes, or whose
+// ranges exceed kTileStage slots (crowded rows), takes the global-memory
+// search instead; so does a particle whose stencil does not follow its
+// sorted key.
 constexpr int kTileSlots = 256;
 constexpr int kTileStage = 1408;     // staged slots: 1408 x 36 B
 constexpr int kTileRows = 40;        // grid rows staged per plane
@@ -1062,12 +1086,17 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
     float4* s_pos = reinterpret_cast<float4*>(tile_smem);
     float4* s_vel = s_pos + kTileStage;
     int* s_key = reinterpret_cast<int*>(s_vel + kTileStage);
-    int* s_row = s_key + kTileStage;   // [3][kTileRows + 1]: staged offset of each row's first slot
+    int* s_row = s_key + kTileStage;   // [3][kTileRows + 1]: sorted slot of each row's first particle
     __shared__ int s_ok, s_scene, s_z, s_ylo, s_nrows, s_total;
     __shared__ int s_A[3], s_base[4];
     const GridDev& g = a.pg;
     const int s0 = blockIdx.x * kTileSlots, j = s0 + threadIdx.x;
     const int last = min(s0 + kTileSlots, a.n) - 1;
+    // the particle's own state and id, in flight during the tile's set-up
+    const int jj = min(j, last);
+    const float4 px = __ldg(&g.spos[jj]);
+    const float4 pv = __ldg(&g.svel[jj]);
+    const int pid = __ldg(&g.ids[jj]);
     if (threadIdx.x < 32) {
         // the tile's plane and rows, and the three planes' slot ranges: lane
         // p (0..2) looks up plane zf + p - 1, all loads in flight together
@@ -1113,33 +1142,36 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
     const SceneDev& sc = a.scenes[s_scene];
     const GridGeom& geo = sc.pg;
     const int nrows = s_nrows, ylo = s_ylo, zc = s_z;
-    // the rows' first slots as staged offsets, then the three ranges
+    // the rows' first slots and the three ranges as asynchronous copies (a
+    // plane outside the grid has no slots: its rows start at its range's
+    // start, A = 0)
     for (int q = threadIdx.x; q < 3 * (nrows + 1); q += kTileSlots) {
         const int p = q / (nrows + 1), i = q - p * (nrows + 1);
         const int z = zc + p - 1;
-        int off = s_base[p];
-        if (z >= 0 && z < geo.cz) off += __ldg(&g.row_start[(int)geo.row_offset + z * geo.cy + ylo + i]) - s_A[p];
-        s_row[p * (kTileRows + 1) + i] = off;
+        int* dst = &s_row[p * (kTileRows + 1) + i];
+        if (z >= 0 && z < geo.cz) cp_async4(dst, &g.row_start[(int)geo.row_offset + z * geo.cy + ylo + i]);
+        else *dst = s_A[p];
     }
     for (int q = threadIdx.x; q < s_total; q += kTileSlots) {
         const int p = q < s_base[1] ? 0 : (q < s_base[2] ? 1 : 2);
         const int slot = s_A[p] + (q - s_base[p]);
-        s_key[q] = __ldg(&g.keys[slot]);
-        s_pos[q] = __ldg(&g.spos[slot]);
-        s_vel[q] = __ldg(&g.svel[slot]);
+        cp_async4(&s_key[q], &g.keys[slot]);
+        cp_async16(&s_pos[q], &g.spos[slot]);
+        cp_async16(&s_vel[q], &g.svel[slot]);
     }
-    __syncthreads();
-    if (j > last) return;
-    const int me = s_base[1] + (j - s_A[1]);
-    const float4 px = s_pos[me];
-    const float3 x = xyz(px), v = xyz(s_vel[me]);
+    // the particle's stencil while the copies land
+    const float3 x = xyz(px), v = xyz(pv);
     const float R = px.w;
     const Stencil st = particle_stencil(geo, x);
     const bool inside = st.ix + st.x0 >= 0 && st.ix + st.x1 <= geo.cx - 1 && st.iy + st.y0 >= 0 &&
                         st.iy + st.y1 <= geo.cy - 1 && st.iz + st.z0 >= 0 && st.iz + st.z1 <= geo.cz - 1;
     // the stencil's rows among the staged ones (a particle whose stencil
     // does not follow its sorted key, after bcs_set_particles, searches globally)
-    if (!inside || st.iz != zc || st.iy + st.y0 < ylo || st.iy + st.y1 > ylo + nrows - 1) {
+    const bool staged = inside && st.iz == zc && st.iy + st.y0 >= ylo && st.iy + st.y1 <= ylo + nrows - 1;
+    cp_async_wait_all();
+    __syncthreads();
+    if (j > last) return;
+    if (!staged) {
         collide_slot<1>(a, j);
         return;
     }
@@ -1151,10 +1183,11 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
         lo[r] = hi[r] = end[r] = 0;
         wlo[r] = 0;
         if (dz < st.z0 || dz > st.z1 || dy < st.y0 || dy > st.y1) continue;
-        const int i = st.iy + dy - ylo;   // the window's row among the staged ones
+        const int i = st.iy + dy - ylo;                      // the window's row among the staged ones
+        const int shift = s_base[dz + 1] - s_A[dz + 1];      // sorted slot -> staged offset
         wlo[r] = kbase + ((st.iz + dz) * geo.cy + st.iy + dy) * geo.cx + st.ix + st.x0;
-        lo[r] = s_row[(dz + 1) * (kTileRows + 1) + i];
-        hi[r] = end[r] = s_row[(dz + 1) * (kTileRows + 1) + i + 1];
+        lo[r] = s_row[(dz + 1) * (kTileRows + 1) + i] + shift;
+        hi[r] = end[r] = s_row[(dz + 1) * (kTileRows + 1) + i + 1] + shift;
     }
     for (bool more = true; more;) {
         more = false;
@@ -1175,7 +1208,7 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
     for (int r = 0; r < 9; ++r)
         for (int t = lo[r]; t < end[r] && s_key[t] - wlo[r] <= wx; ++t)
             collide(a, x, v, R, s_pos[t], [s_vel, t] { return s_vel[t]; }, acc, e);
-    a.coll[__ldg(&g.ids[j])] = make_float4(acc.x, acc.y, acc.z, 0.f);
+    a.coll[pid] = make_float4(acc.x, acc.y, acc.z, 0.f);
     if (e) atomicOr(a.err, e);
 }
 
@@ -1308,12 +1341,13 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
     for (int r = 0; r < kSubstepPer; ++r) {
         const int i = threadIdx.x + r * kSubstepThreads;
         if (i < np) {
-            s_pos[i] = a.pos_out[p0 + i];
-            s_vel[i] = a.vel_out[p0 + i];
-            s_frc[i] = a.frc_out[p0 + i];
+            cp_async16(s_pos + i, a.pos_out + p0 + i);
+            cp_async16(s_vel + i, a.vel_out + p0 + i);
+            cp_async16(s_frc + i, a.frc_out + p0 + i);
             fe[r] = xyz(a.fext[p0 + i]);
         }
     }
+    cp_async_wait_all();
     __syncthreads();
     const long long step0 = *a.steps;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

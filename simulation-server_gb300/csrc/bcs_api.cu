@@ -36,7 +36,8 @@ void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigne
                         const float4* pos, float4* spos, const float4* vel, float4* svel, cudaStream_t s);
 void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s);
 void launch_row_starts(const int* keys, int n, const SceneDev* scenes, int scene_count, long long rows, int* row_start,
-                       cudaStream_t s);
+                       int4* tiles, cudaStream_t s);
+int tile_records(int n);
 void launch_tri_occupancy(const int4* table, const int* epoch, const SceneDev* scenes, int scene_count, long long cells,
                           unsigned* occ, cudaStream_t s);
 void launch_dense_ranges(const int4* table, const int* epoch, long long cells, int* starts, int* ends,
@@ -124,6 +125,7 @@ struct DeviceGrid {
     bool table_on = true;      // every build writes the range table (off under grid-order collisions,
     bool table_current = false;// which need only the row starts; the getters then build it on demand)
     int* row_start = nullptr;  // first sorted slot of every grid row (+1 entry), kept while rows_on
+    int4* tiles = nullptr;     // the collision kernel's tile records, built with row_start
     long long rows = 0;        // grid rows of all scenes
     bool rows_on = false;
     const SceneDev* scenes = nullptr;   // the batch's scenes (row geometry)
@@ -382,7 +384,7 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, con
     if (beside) {
         cudaEventRecord(fork, st);
         cudaStreamWaitEvent(side, fork, 0);
-        launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, side);
+        launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, dg.tiles, side);
         cudaEventRecord(join, side);
     }
     launch_cell_ranges(dg.g.keys, dg.count, dg.table_on ? dg.table : nullptr, dg.epoch,
@@ -390,8 +392,10 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, con
                        vel, svel_out, st);
     dg.table_current = dg.table_on;
     if (beside) cudaStreamWaitEvent(st, join, 0);
-    else if (dg.rows_on) launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, st);
+    else if (dg.rows_on)
+        launch_row_starts(dg.g.keys, dg.count, dg.scenes, dg.scene_count, dg.rows, dg.row_start, dg.tiles, st);
     dg.g.row_start = dg.rows_on ? dg.row_start : nullptr;
+    dg.g.tiles = dg.rows_on ? dg.tiles : nullptr;
 }
 
 // The range table of the current sorted keys, when the last build left it
@@ -744,7 +748,7 @@ bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
     }
     if (gc && !s->pg.rows_on && s->pg.sorted_once)
         launch_row_starts(s->pg.g.keys, s->pg.count, s->pg.scenes, s->pg.scene_count, s->pg.rows, s->pg.row_start,
-                          s->stream);
+                          s->pg.tiles, s->stream);
     s->pg.spos_on = sp;
     s->pg.g.spos = sp && s->pg.sorted_once ? s->pg.spos : nullptr;
     s->pg.g.svel = sp && s->pg.sorted_once ? s->pg.svel : nullptr;
@@ -752,6 +756,7 @@ bcs_status apply_tuning(bcs_sim* s, const bcs_tuning& t) {
     s->pg.table_on = !gc;
     if (!gc) ensure_table(s->pg, s->stream);
     s->pg.g.row_start = gc && s->pg.sorted_once ? s->pg.row_start : nullptr;
+    s->pg.g.tiles = gc && s->pg.sorted_once ? s->pg.tiles : nullptr;
     s->args.pg = s->pg.g;
     s->args.coll = gc && s->pg.g.row_start && s->pg.g.spos && s->pg.g.svel ? s->coll : nullptr;
     s->args.collide_search = t.grid_collisions >= 2 ? t.grid_collisions - 1 : 0;
@@ -1010,7 +1015,9 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
         s->pg.rows = row_total;
         s->pg.scenes = s->scenes;
         s->pg.scene_count = s->S;
-        if ((st = dalloc(s, &s->pg.row_start, (size_t)row_total + 1)) || (st = dalloc(s, &s->coll, s->N))) return st;
+        if ((st = dalloc(s, &s->pg.row_start, (size_t)row_total + 1)) || (st = dalloc(s, &s->coll, s->N)) ||
+            (st = dalloc(s, &s->pg.tiles, 3 * (size_t)tile_records(s->N))))
+            return st;
     }
     s->tg.count = s->T;
     s->tg.g.count = s->T;

@@ -128,6 +128,8 @@ struct GridDev {          // batch-wide sorted grid
     const float4* svel;   // velocities in sorted order (set with spos), or null
     const int* row_start; // particle grid, grid-order collisions: first sorted slot of each grid row
                           // (batch row space, one entry past the last row), or null
+    const int4* tiles;    // with row_start: 3 int4 per block of 256 sorted slots, the collision
+                          // kernel's tile record (k_tile_setup)
     int count;            // objects
 };
 

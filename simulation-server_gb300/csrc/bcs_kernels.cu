@@ -1081,67 +1081,70 @@ constexpr int kTileStage = 1408;     // staged slots: 1408 x 36 B
 constexpr int kTileRows = 40;        // grid rows staged per plane
 constexpr size_t kTileSmem = (size_t)kTileStage * (2 * sizeof(float4) + sizeof(int)) + 3 * (kTileRows + 1) * sizeof(int);
 
+// The tile record of every block of kTileSlots sorted slots, built with the
+// row starts: the tile's plane and staged rows and the three planes' slot
+// ranges, so that the collision kernel reads them in one round trip instead
+// of looking up the tile's keys and then its rows.  One thread per tile:
+//   [0] (staged?, scene, plane zf, first staged row ylo)
+//   [1] (staged rows, staged slots, A0, A1)      Ap: first slot of plane zf + p - 1
+//   [2] (A2, c0, c0 + c1, 0)                     cp: its slots (0 outside the grid)
+// A tile is staged when it lies in one scene and one plane, its rows with
+// their neighbours number at most kTileRows and the three ranges hold at most
+// kTileStage slots.
+__global__ void k_tile_setup(const int* __restrict__ keys, int n, const SceneDev* __restrict__ scenes,
+                             int scene_count, const int* __restrict__ row_start, int4* tiles) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= (n + kTileSlots - 1) / kTileSlots) return;
+    const int s0 = b * kTileSlots, last = min(s0 + kTileSlots, n) - 1;
+    const int sc_i = find_range(scene_count, s0, [&](int k) { return scenes[k].particle_start; });
+    const SceneDev& sc = scenes[sc_i];
+    const GridGeom& geo = sc.pg;
+    const int cxy = geo.cx * geo.cy;
+    const int kf = keys[s0] - (int)geo.key_offset, kl = keys[last] - (int)geo.key_offset;
+    const int zf = kf / cxy, zl = kl / cxy;
+    const int yf = (kf - zf * cxy) / geo.cx, yl = (kl - zl * cxy) / geo.cx;
+    const int ylo = max(yf - 1, 0), yhi = min(yl + 1, geo.cy - 1);
+    const bool ok = last < sc.particle_end && zf == zl && yhi - ylo + 1 <= kTileRows;
+    int A[3] = {0, 0, 0}, c[3] = {0, 0, 0};
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        const int z = zf + p - 1;
+        if (ok && z >= 0 && z < geo.cz) {
+            const int r0 = (int)geo.row_offset + z * geo.cy;
+            A[p] = row_start[r0 + ylo];
+            c[p] = row_start[r0 + yhi + 1] - A[p];
+        }
+    }
+    const int total = c[0] + c[1] + c[2];
+    tiles[3 * b] = make_int4(ok && total <= kTileStage ? 1 : 0, sc_i, zf, ylo);
+    tiles[3 * b + 1] = make_int4(yhi - ylo + 1, total, A[0], A[1]);
+    tiles[3 * b + 2] = make_int4(A[2], c[0], c[0] + c[1], 0);
+}
+
 __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a) {
     extern __shared__ __align__(16) unsigned char tile_smem[];
     float4* s_pos = reinterpret_cast<float4*>(tile_smem);
     float4* s_vel = s_pos + kTileStage;
     int* s_key = reinterpret_cast<int*>(s_vel + kTileStage);
     int* s_row = s_key + kTileStage;   // [3][kTileRows + 1]: sorted slot of each row's first particle
-    __shared__ int s_ok, s_scene, s_z, s_ylo, s_nrows, s_total;
-    __shared__ int s_A[3], s_base[4];
     const GridDev& g = a.pg;
     const int s0 = blockIdx.x * kTileSlots, j = s0 + threadIdx.x;
     const int last = min(s0 + kTileSlots, a.n) - 1;
-    // the particle's own state and id, in flight during the tile's set-up
+    // the tile's record and the particle's own state and id, all in flight together
+    const int4 t0 = __ldg(&g.tiles[3 * blockIdx.x]), t1 = __ldg(&g.tiles[3 * blockIdx.x + 1]),
+               t2 = __ldg(&g.tiles[3 * blockIdx.x + 2]);
     const int jj = min(j, last);
     const float4 px = __ldg(&g.spos[jj]);
     const float4 pv = __ldg(&g.svel[jj]);
     const int pid = __ldg(&g.ids[jj]);
-    if (threadIdx.x < 32) {
-        // the tile's plane and rows, and the three planes' slot ranges: lane
-        // p (0..2) looks up plane zf + p - 1, all loads in flight together
-        const int lane = threadIdx.x;
-        const int sc_i = find_range(a.scene_count, s0, [&](int k) { return a.scenes[k].particle_start; });
-        const SceneDev& sc = a.scenes[sc_i];
-        const GridGeom& geo = sc.pg;
-        const int cxy = geo.cx * geo.cy;
-        const int kf = __ldg(&g.keys[s0]) - (int)geo.key_offset, kl = __ldg(&g.keys[last]) - (int)geo.key_offset;
-        const int zf = kf / cxy, zl = kl / cxy;
-        const int yf = (kf - zf * cxy) / geo.cx, yl = (kl - zl * cxy) / geo.cx;
-        const int ylo = max(yf - 1, 0), yhi = min(yl + 1, geo.cy - 1);
-        const bool ok = last < sc.particle_end && zf == zl && yhi - ylo + 1 <= kTileRows;
-        int A = 0, cnt = 0;
-        const int z = zf + lane - 1;
-        if (ok && lane < 3 && z >= 0 && z < geo.cz) {
-            const int r0 = (int)geo.row_offset + z * geo.cy;
-            A = __ldg(&g.row_start[r0 + ylo]);
-            cnt = __ldg(&g.row_start[r0 + yhi + 1]) - A;
-        }
-        const int c0 = __shfl_sync(0xffffffffu, cnt, 0), c1 = __shfl_sync(0xffffffffu, cnt, 1),
-                  c2 = __shfl_sync(0xffffffffu, cnt, 2);
-        if (lane < 3) s_A[lane] = A;
-        if (lane == 0) {
-            const int total = c0 + c1 + c2;
-            s_base[0] = 0;
-            s_base[1] = c0;
-            s_base[2] = c0 + c1;
-            s_base[3] = total;
-            s_ok = ok && total <= kTileStage;
-            s_scene = sc_i;
-            s_z = zf;
-            s_ylo = ylo;
-            s_nrows = yhi - ylo + 1;
-            s_total = total;
-        }
-    }
-    __syncthreads();
-    if (!s_ok) {
+    if (!t0.x) {
         if (j <= last) collide_slot<1>(a, j);
         return;
     }
-    const SceneDev& sc = a.scenes[s_scene];
+    const SceneDev& sc = a.scenes[t0.y];
     const GridGeom& geo = sc.pg;
-    const int nrows = s_nrows, ylo = s_ylo, zc = s_z;
+    const int zc = t0.z, ylo = t0.w, nrows = t1.x, total = t1.y;
+    const int A0 = t1.z, A1 = t1.w, A2 = t2.x, B1 = t2.y, B2 = t2.z;
     // the rows' first slots and the three ranges as asynchronous copies (a
     // plane outside the grid has no slots: its rows start at its range's
     // start, A = 0)
@@ -1150,11 +1153,10 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
         const int z = zc + p - 1;
         int* dst = &s_row[p * (kTileRows + 1) + i];
         if (z >= 0 && z < geo.cz) cp_async4(dst, &g.row_start[(int)geo.row_offset + z * geo.cy + ylo + i]);
-        else *dst = s_A[p];
+        else *dst = p == 0 ? A0 : (p == 1 ? A1 : A2);
     }
-    for (int q = threadIdx.x; q < s_total; q += kTileSlots) {
-        const int p = q < s_base[1] ? 0 : (q < s_base[2] ? 1 : 2);
-        const int slot = s_A[p] + (q - s_base[p]);
+    for (int q = threadIdx.x; q < total; q += kTileSlots) {
+        const int slot = q < B1 ? A0 + q : (q < B2 ? A1 + (q - B1) : A2 + (q - B2));
         cp_async4(&s_key[q], &g.keys[slot]);
         cp_async16(&s_pos[q], &g.spos[slot]);
         cp_async16(&s_vel[q], &g.svel[slot]);
@@ -1183,8 +1185,9 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
         lo[r] = hi[r] = end[r] = 0;
         wlo[r] = 0;
         if (dz < st.z0 || dz > st.z1 || dy < st.y0 || dy > st.y1) continue;
-        const int i = st.iy + dy - ylo;                      // the window's row among the staged ones
-        const int shift = s_base[dz + 1] - s_A[dz + 1];      // sorted slot -> staged offset
+        const int i = st.iy + dy - ylo;   // the window's row among the staged ones
+        // sorted slot -> staged offset
+        const int shift = dz < 0 ? -A0 : (dz == 0 ? B1 - A1 : B2 - A2);
         wlo[r] = kbase + ((st.iz + dz) * geo.cy + st.iy + dy) * geo.cx + st.ix + st.x0;
         lo[r] = s_row[(dz + 1) * (kTileRows + 1) + i] + shift;
         hi[r] = end[r] = s_row[(dz + 1) * (kTileRows + 1) + i + 1] + shift;
@@ -2567,9 +2570,12 @@ void launch_cell_ranges(const int* keys, int n, int4* table, int* epoch, unsigne
     if (n > 0) k_cell_ranges<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, table, epoch, occ, ids, pos, spos, vel, svel);
 }
 void launch_row_starts(const int* keys, int n, const SceneDev* scenes, int scene_count, long long rows, int* row_start,
-                       cudaStream_t s) {
+                       int4* tiles, cudaStream_t s) {
     k_row_starts<<<(unsigned)((rows + 1 + 255) / 256), 256, 0, s>>>(keys, n, scenes, scene_count, rows, row_start);
+    const int nt = (n + kTileSlots - 1) / kTileSlots;
+    if (tiles && nt > 0) k_tile_setup<<<(nt + 127) / 128, 128, 0, s>>>(keys, n, scenes, scene_count, row_start, tiles);
 }
+int tile_records(int n) { return (n + kTileSlots - 1) / kTileSlots; }
 void launch_occ_update(const int* keys, int n, unsigned* occ, bool set, cudaStream_t s) {
     if (n > 0) k_occ_update<<<BCS_GRID1(n, 256), 0, s>>>(keys, n, occ, set ? 1 : 0);
 }

@@ -1227,8 +1227,9 @@ __global__ void __launch_bounds__(256) k_vein_end(const StepArgs a, int cells) {
     const SceneDev& sc = a.scenes[ty.scene];
     const int cell = cell_g - ty.cell_global;
     const int p0 = ty.particle_start + cell * ty.pic;
+    // every lane's positions in flight together (no early exit per lane)
     bool leave = false;
-    for (int k = lane; k < ty.pic; k += 32) leave = leave || leaves_vein(sc, xyz(a.pos_out[p0 + k]));
+    for (int k = lane; k < ty.pic; k += 32) leave |= leaves_vein(sc, xyz(__ldg(&a.pos_out[p0 + k])));
     if (!__any_sync(0xffffffffu, leave)) return;
     const long long step = *a.steps;
     unsigned e = 0;

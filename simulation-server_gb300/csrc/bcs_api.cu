@@ -221,7 +221,8 @@ struct bcs_sim {
     cudaEvent_t pev[BCS_PHASE_COUNT + 1] = {};
     // a second stream for independent work within a frame (the vein springs
     // beside the grid build, the vein update beside the vein-end rule, the
-    // row starts beside the sorted copies), forked and joined with events
+    // row starts and tile records beside the sorted copies), forked and
+    // joined with events
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev[4] = {}, join_ev[4] = {};
     float* scratch = nullptr;      // 3 * max(N, V) floats for host transfers
@@ -350,8 +351,9 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
 // Sort the grid's unsorted keys into the other result slot and rebuild the
 // range table.  After the first build, a grid flagged incremental starts
 // from the previous order (any permutation works; few movers make it cheap).
-// With `side` (and its fork / join events) the row starts are built there,
-// beside the sorted copies on `st`, and (fork2 / join2) an incremental
+// With `side` (and its fork / join events) the row starts and the collision
+// tile records are built there, beside the sorted copies on `st`, and
+// (fork2 / join2) an incremental
 // build's movers are sorted there beside the compaction of the kept pairs.
 void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, const float4* vel = nullptr,
                cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr,

@@ -890,6 +890,21 @@ def run_ours(args):
     per_kernel["step"] = {"ms": step_ms, "algorithmic_bytes_per_particle": step_bytes,
                           "achieved_gbs": step_bytes * n / (step_ms / 1e3) / 1e9}
     per_kernel["step"]["frac"] = per_kernel["step"]["achieved_gbs"] / peak
+    # the whole frame against its compulsory traffic: 96 B per particle (x, v,
+    # F read and written, key and id written, one sort pass over the pairs),
+    # 8 B per occupied grid cell, 72 B per vertex and 24 B per triangle of a
+    # deformable wall, over the graph-replayed frame time
+    walls = scene if batched else [scene]
+    dyn = [sc for sc in walls if int(sc.params.vein_dynamic)]
+    wall_bytes = sum(72 * len(sc.vein_positions) + 24 * len(sc.vein_indices) for sc in dyn)
+    occupied = diag.get("occupied_cells", 0)
+    step_total = 96 * n + 8 * occupied + wall_bytes
+    frame_ms = ms_max / args.steps
+    whole_step = {"algorithmic_bytes_per_step": int(step_total), "ms": frame_ms,
+                  "achieved_gbs": step_total / (frame_ms / 1e3) / 1e9,
+                  "terms": {"particles_96B": 96 * n, "occupied_cells_8B": 8 * occupied,
+                            "wall_72B_per_vertex_24B_per_triangle": wall_bytes}}
+    whole_step["frac"] = whole_step["achieved_gbs"] / peak
 
     # ---- pass 3: end to end through the C ABI with pinned host buffers:
     # the state after the warm-up is uploaded, then every frame is
@@ -985,7 +1000,7 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_note,
                          "algorithmic_bytes_per_launch": ALGO_BYTES_STEP_KERNEL * n, "kernel_ms": k_ms,
                          "kernel_ms_over": f"{prof_steps} eager frames of the same trajectory",
-                         "per_kernel": per_kernel},
+                         "per_kernel": per_kernel, "whole_step": whole_step},
             "phase_ms": {k: v / prof_steps for k, v in phases.items()},
             "diagnostics_after_timed_run": diag,
             "learned_substep": learned,

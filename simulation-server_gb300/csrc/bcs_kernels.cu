@@ -960,6 +960,12 @@ __global__ void k_row_starts(const int* __restrict__ keys, int n, const SceneDev
 // The particle's sum lands in a.coll at its id, for the step kernel.
 constexpr int kCollideThreads = 256;
 
+// Halvings that take a binary search over `len` slots to an empty range,
+// the same for every active lane of the warp (the largest of theirs): the
+// nine searches then run a warp-uniform loop, with no per-step test of
+// whether any search is still open.
+__device__ inline int search_steps(int len) { return __reduce_max_sync(__activemask(), 32 - __clz(len)); }
+
 template <int SEARCH>
 __device__ inline void collide_slot(const StepArgs& a, int j) {
     const GridDev& g = a.pg;
@@ -998,15 +1004,17 @@ __device__ inline void collide_slot(const StepArgs& a, int j) {
             lo[r] = __ldg(&g.row_start[rbase + rr]);
             hi[r] = end[r] = __ldg(&g.row_start[rbase + rr + 1]);
         }
-        for (bool more = true; more;) {
-            more = false;
+        int len = 0;
+#pragma unroll
+        for (int r = 0; r < 9; ++r) len = max(len, hi[r] - lo[r]);
+        const int steps = search_steps(len);
+        for (int it = 0; it < steps; ++it) {
 #pragma unroll
             for (int r = 0; r < 9; ++r) {
                 if (lo[r] < hi[r]) {
                     const int m = (lo[r] + hi[r]) >> 1;
                     if (__ldg(&keys[m]) < wlo[r]) lo[r] = m + 1;
                     else hi[r] = m;
-                    more |= lo[r] < hi[r];
                 }
             }
         }
@@ -1192,15 +1200,17 @@ __global__ void __launch_bounds__(kTileSlots, 4) k_collide_tile(const StepArgs a
         lo[r] = s_row[(dz + 1) * (kTileRows + 1) + i] + shift;
         hi[r] = end[r] = s_row[(dz + 1) * (kTileRows + 1) + i + 1] + shift;
     }
-    for (bool more = true; more;) {
-        more = false;
+    int len = 0;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) len = max(len, hi[r] - lo[r]);
+    const int steps = search_steps(len);
+    for (int it = 0; it < steps; ++it) {
 #pragma unroll
         for (int r = 0; r < 9; ++r) {
             if (lo[r] < hi[r]) {
                 const int m = (lo[r] + hi[r]) >> 1;
                 if (s_key[m] < wlo[r]) lo[r] = m + 1;
                 else hi[r] = m;
-                more |= lo[r] < hi[r];
             }
         }
     }

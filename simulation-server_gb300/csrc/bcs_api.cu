@@ -51,7 +51,7 @@ void launch_vein_springs(const float4* vpos, const float4* vvel, float4* vfrc, c
 void launch_vein_integrate(float4* vpos, float4* vvel, float4* vfrc, int V, float dt, cudaStream_t s);
 void launch_tri_cache(const int* ids, const uint32_t* tri, const float4* vpos, int T, float4* cache, cudaStream_t s);
 void launch_bump_step(long long* steps, int by, cudaStream_t s);
-void launch_substeps(const StepArgs& a, int items, int K, cudaStream_t s);
+void launch_substeps(const StepArgs& a, int items, int K, int chunk, cudaStream_t s);
 void launch_sur_features(const StepArgs& a, const SurDev& d, cudaStream_t s);
 void launch_sur_targets(const StepArgs& a, const SurDev& d, float* raw_t, unsigned char* valid, cudaStream_t s);
 void launch_sur_inputs(const float* raw, const float* raw_t, const int* list, int nvalid, unsigned long long seed,
@@ -558,7 +558,7 @@ void enqueue_macro(bcs_sim* s, int K, const MacroHooks* hooks = nullptr) {
     if (s->p.use_blood_flow) launch_vein_end(s->args, s->C, s->stream);
     refresh_args(s, in, out, true);
     if (hooks && hooks->after_first) hooks->after_first(s);
-    launch_substeps(s->args, (int)s->work_host.size(), K, s->stream);
+    launch_substeps(s->args, (int)s->work_host.size(), K, kShapes[s->tune.step_shape].chunk, s->stream);
     if (hooks && hooks->after_substeps) hooks->after_substeps(s);
     s->args.fext = nullptr;
     s->args.skip_cell = nullptr;

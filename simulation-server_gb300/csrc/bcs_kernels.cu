@@ -1333,14 +1333,19 @@ __global__ void k_next_epoch(int* epoch) { *epoch += 1; }
 // re-evaluates centroids, cell springs and environment with the external
 // force of sub-step 1 held, integrates (Heun) and applies the vein-end rule
 // (a respawned cell drops its held force).  Ends with the grid keys of the
-// final positions.
+// final positions.  The cell state is double-buffered in shared memory:
+// sub-step k reads one buffer and writes the other, so a thread writes its
+// particles' new state as soon as it has it (no copy of every result held
+// in registers until all threads have read their neighbours), and a
+// sub-step takes one barrier fewer.  PER particles per thread (the launch
+// shape's particles per CTA / 256); the buffers are dynamic shared memory.
 constexpr int kSubstepThreads = 256;
-constexpr int kSubstepPer = kMaxChunk / kSubstepThreads;
 
+template <int PER>
 __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, int K) {
-    __shared__ float4 s_pos[kMaxChunk];
-    __shared__ float4 s_vel[kMaxChunk];
-    __shared__ float4 s_frc[kMaxChunk];
+    extern __shared__ __align__(16) unsigned char sub_smem[];
+    constexpr int CAP = PER * kSubstepThreads;
+    float4* b_pos[2] = {reinterpret_cast<float4*>(sub_smem), reinterpret_cast<float4*>(sub_smem) + 3 * CAP};
     __shared__ float3 s_cent[kMaxCellsPerChunk];
     __shared__ int s_leave[kMaxCellsPerChunk];
     __shared__ SceneDev sc;
@@ -1350,15 +1355,18 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
     const int p0 = ty.particle_start + w.first_cell * pic;
     const int np = w.ncells * pic;
     stage_scene(a.scenes + ty.scene, &sc);
-    float3 fe[kSubstepPer];
+    float3 fe[PER];
+    bool skip[PER];
 #pragma unroll
-    for (int r = 0; r < kSubstepPer; ++r) {
+    for (int r = 0; r < PER; ++r) {
         const int i = threadIdx.x + r * kSubstepThreads;
+        skip[r] = true;
         if (i < np) {
-            cp_async16(s_pos + i, a.pos_out + p0 + i);
-            cp_async16(s_vel + i, a.vel_out + p0 + i);
-            cp_async16(s_frc + i, a.frc_out + p0 + i);
+            cp_async16(b_pos[0] + i, a.pos_out + p0 + i);
+            cp_async16(b_pos[0] + CAP + i, a.vel_out + p0 + i);
+            cp_async16(b_pos[0] + 2 * CAP + i, a.frc_out + p0 + i);
             fe[r] = xyz(a.fext[p0 + i]);
+            skip[r] = a.skip_cell && a.skip_cell[ty.cell_global + w.first_cell + i / pic];
         }
     }
     cp_async_wait_all();
@@ -1366,10 +1374,17 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
     const long long step0 = *a.steps;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned e = 0;
+    int cur = 0;
     for (int k = 2; k <= K; ++k) {
+        const float4* c_pos = b_pos[cur];
+        const float4* c_vel = c_pos + CAP;
+        const float4* c_frc = c_pos + 2 * CAP;
+        float4* n_pos = b_pos[cur ^ 1];
+        float4* n_vel = n_pos + CAP;
+        float4* n_frc = n_pos + 2 * CAP;
         for (int c = warp; c < w.ncells; c += kSubstepThreads / 32) {
             float3 acc = f3(0.f, 0.f, 0.f);
-            for (int q = lane; q < pic; q += 32) acc = acc + xyz(s_pos[c * pic + q]);
+            for (int q = lane; q < pic; q += 32) acc = acc + xyz(c_pos[c * pic + q]);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
@@ -1382,44 +1397,40 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
             }
         }
         __syncthreads();
-        float3 nx[kSubstepPer], nv[kSubstepPer], nF[kSubstepPer];
 #pragma unroll
-        for (int r = 0; r < kSubstepPer; ++r) {
+        for (int r = 0; r < PER; ++r) {
             const int i = threadIdx.x + r * kSubstepThreads;
             if (i >= np) continue;
+            if (skip[r]) {   // a cell the network advanced keeps its state
+                n_pos[i] = c_pos[i];
+                n_vel[i] = c_vel[i];
+                n_frc[i] = c_frc[i];
+                continue;
+            }
             const int c = i / pic, li = i - c * pic, cb = c * pic;
-            if (a.skip_cell && a.skip_cell[ty.cell_global + w.first_cell + c]) continue;
-            const float3 x = xyz(s_pos[i]), v = xyz(s_vel[i]), fprev = xyz(s_frc[i]);
+            const float4 xw = c_pos[i];
+            const float3 x = xyz(xw), v = xyz(c_vel[i]), fprev = xyz(c_frc[i]);
             float3 F = f3(0.f, 0.f, 0.f);
             const int e0 = __ldg(&a.adj_off[ty.adj_start + li]), e1 = __ldg(&a.adj_off[ty.adj_start + li + 1]);
             for (int q = e0; q < e1; ++q) {
                 const int j = cb + __ldg(&a.adj_nbr[q]);
-                F = F + cell_spring(a.p, x - xyz(s_pos[j]), v - xyz(s_vel[j]), fprev, xyz(s_frc[j]),
+                F = F + cell_spring(a.p, x - xyz(c_pos[j]), v - xyz(c_vel[j]), fprev, xyz(c_frc[j]),
                                     __ldg(&a.adj_len[q]), e);
             }
             const float ratio = len3(x - s_cent[c]) / __ldg(&a.r0[ty.model_start + li]);
             F = F + environment(a, sc, x, v, ratio);
             F = (fprev + F) / 2.0f + fe[r];
             const float3 v1 = v + a.p.dt * F;
-            nx[r] = x + (0.5f * a.p.dt) * (v1 + v);
-            nv[r] = v1;
-            nF[r] = F;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < kSubstepPer; ++r) {
-            const int i = threadIdx.x + r * kSubstepThreads;
-            if (i >= np) continue;
-            if (a.skip_cell && a.skip_cell[ty.cell_global + w.first_cell + i / pic]) continue;
-            s_pos[i] = make_float4(nx[r].x, nx[r].y, nx[r].z, s_pos[i].w);
-            s_vel[i] = make_float4(nv[r].x, nv[r].y, nv[r].z, 0.f);
-            s_frc[i] = make_float4(nF[r].x, nF[r].y, nF[r].z, 0.f);
-            if (a.p.use_blood_flow && leaves_vein(sc, nx[r])) atomicOr(&s_leave[i / pic], 1);
+            const float3 nx = x + (0.5f * a.p.dt) * (v1 + v);
+            n_pos[i] = make_float4(nx.x, nx.y, nx.z, xw.w);
+            n_vel[i] = make_float4(v1.x, v1.y, v1.z, 0.f);
+            n_frc[i] = make_float4(F.x, F.y, F.z, 0.f);
+            if (a.p.use_blood_flow && leaves_vein(sc, nx)) atomicOr(&s_leave[c], 1);
         }
         __syncthreads();
         if (a.p.use_blood_flow) {
 #pragma unroll
-            for (int r = 0; r < kSubstepPer; ++r) {
+            for (int r = 0; r < PER; ++r) {
                 const int i = threadIdx.x + r * kSubstepThreads;
                 if (i >= np) continue;
                 const int c = i / pic;
@@ -1427,25 +1438,26 @@ __global__ void __launch_bounds__(kSubstepThreads) k_substeps(const StepArgs a, 
                 float3 x, v;
                 respawn(a, sc, ty.cell_start + w.first_cell + c, step0 + (k - 1), ty.model_start + (i - c * pic),
                         x, v);
-                s_pos[i] = make_float4(x.x, x.y, x.z, s_pos[i].w);
-                s_vel[i] = make_float4(v.x, v.y, v.z, 0.f);
+                n_pos[i] = make_float4(x.x, x.y, x.z, n_pos[i].w);
+                n_vel[i] = make_float4(v.x, v.y, v.z, 0.f);
                 fe[r] = f3(0.f, 0.f, 0.f);
             }
             __syncthreads();
         }
+        cur ^= 1;
     }
+    const float4* c_pos = b_pos[cur];
 #pragma unroll
-    for (int r = 0; r < kSubstepPer; ++r) {
+    for (int r = 0; r < PER; ++r) {
         const int i = threadIdx.x + r * kSubstepThreads;
-        if (i >= np) continue;
-        if (a.skip_cell && a.skip_cell[ty.cell_global + w.first_cell + i / pic]) continue;
+        if (i >= np || skip[r]) continue;
         const int pid = p0 + i;
-        const float4 x = s_pos[i], v = s_vel[i];
+        const float4 x = c_pos[i], v = c_pos[CAP + i];
         if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) && isfinite(v.z)))
             e |= BCS_ERRW_NONFINITE;
         a.pos_out[pid] = x;
         a.vel_out[pid] = v;
-        a.frc_out[pid] = s_frc[i];
+        a.frc_out[pid] = c_pos[2 * CAP + i];
         if (a.keys_out) a.keys_out[pid] = a.pg.uniform ? grid_key(sc.pg, xyz(x), e) : 0;
     }
     if (e) atomicOr(a.err, e);
@@ -2701,8 +2713,22 @@ bool launch_sur_fused(const StepArgs& a, const SurDev& d, const SurScales& sc, c
     if (mt <= 12) return launch_fused_mt<12>(a, d, sc, P, PB, PBT, L, goff, gnbr, glen, first, cells, s);
     return false;
 }
-void launch_substeps(const StepArgs& a, int items, int K, cudaStream_t s) {
-    if (items > 0 && K > 1) k_substeps<<<items, kSubstepThreads, 0, s>>>(a, K);
+void launch_substeps(const StepArgs& a, int items, int K, int chunk, cudaStream_t s) {
+    if (items <= 0 || K <= 1) return;
+    {
+        static bool attr = false;
+        const size_t b1 = 6 * (size_t)kSubstepThreads * sizeof(float4);
+        if (!attr) {
+            cudaFuncSetAttribute(k_substeps<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b1);
+            cudaFuncSetAttribute(k_substeps<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(2 * b1));
+            cudaFuncSetAttribute(k_substeps<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(3 * b1));
+            attr = true;
+        }
+        const int per = (chunk + kSubstepThreads - 1) / kSubstepThreads;
+        if (per <= 1) k_substeps<1><<<items, kSubstepThreads, b1, s>>>(a, K);
+        else if (per == 2) k_substeps<2><<<items, kSubstepThreads, 2 * b1, s>>>(a, K);
+        else k_substeps<3><<<items, kSubstepThreads, 3 * b1, s>>>(a, K);
+    }
 }
 void launch_export(const float4* pos, int n, const float4* vpos, int V, float* pvbo, float* poff, float* vvbo,
                    cudaStream_t s) {

@@ -295,6 +295,15 @@ typedef struct bcs_tuning {
 bcs_status bcs_get_tuning(bcs_sim* sim, bcs_tuning* out);
 bcs_status bcs_set_tuning(bcs_sim* sim, const bcs_tuning* tuning);
 
+/* How the incremental grid sort orders the particles that changed cell (the
+ * reference's thrust::stable_sort_by_key, src/grids/uniform_grid.cu:144-147,
+ * has no such choice; every mode gives the same order, bit for bit):
+ * 0 (default) = by the mover count of a recent frame: one CTA while it is
+ * small, the multi-CTA radix passes otherwise; 1 = always the passes;
+ * 2 = always one CTA (correct for any count, slow for many).  Returns
+ * BCS_ERR_INVALID_ARGUMENT for another value. */
+bcs_status bcs_set_mover_sort(bcs_sim* sim, int mode);
+
 /* Autotuner: coordinate descent over the tuning fields (each field takes
  * every valid value with the others held, two sweeps), each trial timed on
  * `frames` fused frames after two warm-up frames, all starting from the

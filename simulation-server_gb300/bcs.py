@@ -30,7 +30,7 @@ EXPORTED = [
     "bcs_calculate_grids", "bcs_calculate_next_frame", "bcs_propagate_all", "bcs_step",
     "bcs_get_grid", "bcs_export_render", "bcs_get_error_word", "bcs_synchronize", "bcs_time_steps",
     "bcs_profile_steps", "bcs_grid_sort_static", "bcs_grid_sort_static_error_word", "bcs_create_batch", "bcs_get_scene_info",
-    "bcs_get_tuning", "bcs_set_tuning", "bcs_autotune", "bcs_macro_step",
+    "bcs_get_tuning", "bcs_set_tuning", "bcs_set_mover_sort", "bcs_autotune", "bcs_macro_step",
     "bcs_surrogate_create", "bcs_surrogate_destroy", "bcs_surrogate_collect", "bcs_surrogate_train",
     "bcs_surrogate_enable", "bcs_surrogate_get_stats", "bcs_surrogate_reset_stats", "bcs_surrogate_param_count",
     "bcs_surrogate_get_params", "bcs_surrogate_set_params", "bcs_surrogate_loss_grad", "bcs_surrogate_forward",
@@ -203,6 +203,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "bcs_get_scene_info": ([P, C.c_int, C.POINTER(SceneInfo)], C.c_int),
         "bcs_get_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "bcs_set_tuning": ([P, C.POINTER(Tuning)], C.c_int),
+        "bcs_set_mover_sort": ([P, C.c_int], C.c_int),
         "bcs_autotune": ([P, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_float)], C.c_int),
         "bcs_macro_step": ([P, C.c_int, C.c_int], C.c_int),
         "bcs_time_macro_steps": ([P, C.c_int, C.c_int, C.POINTER(C.c_float)], C.c_int),
@@ -650,6 +651,10 @@ class Simulation:
         t = Tuning(int(step_shape), int(persistent), int(spatial_order), int(full_sort), int(occupancy_filter),
                    int(sorted_positions), int(grid_collisions))
         _check(self.lib.bcs_set_tuning(self.h, C.byref(t)), "bcs_set_tuning")
+
+    def set_mover_sort(self, mode: int) -> None:
+        """0: by a recent frame's mover count, 1: radix passes, 2: one CTA (same order in all)."""
+        _check(self.lib.bcs_set_mover_sort(self.h, int(mode)), "bcs_set_mover_sort")
 
     def autotune(self, frames: int = 5):
         """Coordinate-descent search over the tuning; keeps the fastest, state unchanged."""

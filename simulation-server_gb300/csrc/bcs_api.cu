@@ -83,19 +83,6 @@ int radix_sort_pairs(const int* in_k, const int* in_v, int* a_k, int* a_v, int* 
                      unsigned* temp, cudaStream_t s);
 size_t radix_temp_words(int n);
 int radix_tiles(int n);
-struct IncrementalBuffers {
-    int* kept_k; int* kept_v;
-    int* mov_k; int* mov_v;
-    int* t1_k; int* t1_v;
-    unsigned* warp_kept;
-    unsigned* tile_kept;
-    unsigned* tile_base;
-    unsigned* id_movers;
-    unsigned* id_base;
-    unsigned char* moved;
-    unsigned* temp;
-    int* movers;
-};
 void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_key_of, int* out_k, int* out_v, int n,
                            int key_bits, int id_bits, const IncrementalBuffers& b, cudaStream_t s,
                            cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
@@ -205,7 +192,12 @@ struct bcs_sim {
     long long host_steps = 0;
     unsigned* err = nullptr;
     StepArgs args{};
-    std::map<long long, cudaGraphExec_t> graphs;   // by (sub-steps, cur, sorted slot)
+    std::map<long long, cudaGraphExec_t> graphs;   // by (sub-steps, mover sort, cur, sorted slot)
+    // the incremental sort's mover count of a recent frame, written by its
+    // scan kernel into mapped host memory (-1 until one was seen), and how the
+    // movers are sorted: 0 = by that count, 1 = pass kernels, 2 = one CTA
+    int* movers_seen = nullptr;
+    int mover_sort = 0;
     float4* fext = nullptr;      // macro steps: held external force per particle
     bcs_surrogate* surrogate = nullptr;   // enabled learned sub-step path, or null
     std::vector<bcs_surrogate*> surrogates;   // every live surrogate of this simulation
@@ -1012,6 +1004,16 @@ bcs_status create_impl(const bcs_scene_desc* descs, int scene_count, void* strea
     BCS_CUDA(cudaMemsetAsync(s->vvel, 0, sizeof(float4) * s->V, s->stream));
     BCS_CUDA(cudaMemsetAsync(s->vfrc, 0, sizeof(float4) * s->V, s->stream));
     if ((st = alloc_grid(s, s->pg, s->N, true)) || (st = alloc_grid(s, s->tg, std::max(1, s->T), false))) return st;
+    {
+        int* dev = nullptr;
+        if (cudaHostAlloc((void**)&s->movers_seen, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer((void**)&dev, s->movers_seen, 0) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return BCS_ERR_CUDA;
+        }
+        *s->movers_seen = -1;
+        s->pg.inc.host_movers = dev;
+    }
     if (s->pg.g.uniform) {
         // grid-order collisions: the row-start table and the collision sums
         s->pg.rows = row_total;
@@ -1090,6 +1092,7 @@ void destroy_impl(bcs_sim* s) {
         cudaStreamDestroy(s->copy_stream);
     }
     for (void* p : s->allocations) cudaFree(p);
+    if (s->movers_seen) cudaFreeHost(s->movers_seen);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     for (auto& e : s->pev)
@@ -1641,12 +1644,28 @@ bcs_status bcs_propagate_all(bcs_sim* s) {
 
 // n fused frames (substeps = 1) or multi-rate macro steps, each replayed
 // from a CUDA graph captured per (sub-steps, buffer parity, sorted slot).
+// Movers of at most one tile in a recent frame: the next frames sort theirs
+// with one CTA and no pass kernels (a larger count is still sorted correctly
+// by it, only slower).  The count is that of a frame a few frames back (the
+// host runs ahead of the device); on the 4.2M-particle bifurcation one CTA
+// stays faster than the passes up to about 7 000 movers, while the count
+// grows by a few percent per frame.
+constexpr int kOneCtaMovers = 4096;
+
+bool movers_one_cta(const bcs_sim* s) {
+    if (s->mover_sort != 0) return s->mover_sort == 2;
+    if (!s->movers_seen) return false;
+    const int seen = *(volatile const int*)s->movers_seen;
+    return seen >= 0 && seen <= kOneCtaMovers;
+}
+
 static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
     auto enqueue = [&]() {
         if (substeps > 1) enqueue_macro(s, substeps);
         else enqueue_frame(s);
     };
     for (int i = 0; i < n; ++i) {
+        s->pg.inc.one_cta = movers_one_cta(s);
         // the first frame of a grid, or with triangle centres refreshed, runs
         // eagerly (its sort is a full one)
         if (s->p.refresh_triangle_centers || (!s->keys_valid && !s->pg.sorted_once)) {
@@ -1659,7 +1678,8 @@ static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
                         s->stream);
             s->keys_valid = true;
         }
-        cudaGraphExec_t& g = s->graphs[(long long)substeps * 4 + s->cur * 2 + s->pg.slot];
+        cudaGraphExec_t& g =
+            s->graphs[((long long)substeps * 2 + (s->pg.inc.one_cta ? 1 : 0)) * 4 + s->cur * 2 + s->pg.slot];
         if (!g) {
             const int cur0 = s->cur;
             const int slot0 = s->pg.slot;
@@ -1780,6 +1800,12 @@ bcs_status bcs_init_particles(bcs_sim* s, const bcs_init_desc* d) {
     if (s->tune.spatial_order && ((st = order_work_spatially(s)) || (st = upload_work(s)))) return st;
     BCS_CUDA(cudaStreamSynchronize(s->stream));
     return check_last();
+}
+
+bcs_status bcs_set_mover_sort(bcs_sim* s, int mode) {
+    if (!s || mode < 0 || mode > 2) return BCS_ERR_INVALID_ARGUMENT;
+    s->mover_sort = mode;
+    return BCS_OK;
 }
 
 bcs_status bcs_get_tuning(bcs_sim* s, bcs_tuning* out) {

@@ -316,6 +316,23 @@ __device__ inline int find_range(int n, T x, F start_of) {
     return lo;
 }
 
+// Scratch of the incremental grid sort (bcs_sort.cu), owned by the grid.
+struct IncrementalBuffers {
+    int* kept_k; int* kept_v;      // n each
+    int* mov_k; int* mov_v;        // n each (movers; sorted in place through t1)
+    int* t1_k; int* t1_v;          // n each
+    unsigned* warp_kept;           // 32 per tile
+    unsigned* tile_kept;           // per tile
+    unsigned* tile_base;           // per tile
+    unsigned* id_movers;           // per id tile, zero between builds
+    unsigned* id_base;             // per id tile
+    unsigned char* moved;          // 4096 per id tile, zero between builds
+    unsigned* temp;                // radix_temp_words(n)
+    int* movers;                   // 1
+    int* host_movers;              // mapped host int the scan copies the mover count into, or null
+    bool one_cta;                  // sort the movers with k_radix_onecta alone (no pass kernels)
+};
+
 // Programmatic dependent launch: a kernel launched with launch_after may be
 // scheduled while the kernel before it in the stream finishes; it calls
 // after_previous() before it touches memory that kernel (or anything before

@@ -198,20 +198,11 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(const int* __r
     }
 }
 
-// A device-side count of at most one tile (4 096 pairs), sorted by one CTA
-// through every pass in shared memory, with the downsweep's stable ranking
-// (pair j: warp j / 512, round j % 512 / 32, lane j % 32); larger counts are
-// left to the pass kernels, which return at once for small ones.  in and
-// out may be the same arrays.
-__global__ void __launch_bounds__(kSortThreads) k_radix_small(const int* in_k, const int* in_v, int* out_k, int* out_v,
-                                                              const int* __restrict__ d_n, int bits) {
-    after_previous();
-    __shared__ unsigned s_cnt[kSortWarps][kRadix];
-    __shared__ unsigned s_tile[kRadix];
-    __shared__ unsigned s_warp[kSortWarps];
-    __shared__ int2 s_stage[kSortTile];
-    const int n = *d_n;
-    if (n > kSortTile) return;
+// Up to one tile (4 096 pairs) sorted by one CTA through every pass in
+// shared memory, with the downsweep's stable ranking (pair j: warp j / 512,
+// round j % 512 / 32, lane j % 32).  in and out may be the same arrays.
+__device__ inline void sort_one_tile(const int* in_k, const int* in_v, int* out_k, int* out_v, int n, int bits,
+                                     unsigned (*s_cnt)[kRadix], unsigned* s_tile, unsigned* s_warp, int2* s_stage) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wbase = warp * (kSortTile / kSortWarps);
     const unsigned lt = (1u << lane) - 1u;
@@ -279,6 +270,116 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_small(const int* in_k, c
     }
 }
 
+// A device-side count of at most one tile, sorted by one CTA (sort_one_tile);
+// larger counts are left to the pass kernels, which return at once for
+// small ones.
+__global__ void __launch_bounds__(kSortThreads) k_radix_small(const int* in_k, const int* in_v, int* out_k, int* out_v,
+                                                              const int* __restrict__ d_n, int bits) {
+    after_previous();
+    __shared__ unsigned s_cnt[kSortWarps][kRadix];
+    __shared__ unsigned s_tile[kRadix];
+    __shared__ unsigned s_warp[kSortWarps];
+    __shared__ int2 s_stage[kSortTile];
+    const int n = *d_n;
+    if (n > kSortTile) return;
+    sort_one_tile(in_k, in_v, out_k, out_v, n, bits, s_cnt, s_tile, s_warp, s_stage);
+}
+
+// A device-side count of any size sorted by one CTA, with no pass kernels
+// after it: up to one tile as k_radix_small does; a larger count through the
+// passes of the full sort (in -> a -> b -> a ...) with every tile ranked in
+// turn by the same stable per-warp ranking and scattered from a running
+// offset per digit.  The result lands where the pass kernels would leave it:
+// (a_k, a_v) after an odd number of passes, (b_k, b_v) after an even one.
+// Meant for frames whose movers fit one tile; a larger count is sorted
+// correctly but slowly.
+__global__ void __launch_bounds__(kSortThreads) k_radix_onecta(const int* in_k, const int* in_v, int* a_k, int* a_v,
+                                                               int* b_k, int* b_v, const int* __restrict__ d_n,
+                                                               int bits) {
+    after_previous();
+    __shared__ unsigned s_cnt[kSortWarps][kRadix];
+    __shared__ unsigned s_tile[kRadix];
+    __shared__ unsigned s_warp[kSortWarps];
+    __shared__ unsigned s_base[kRadix];
+    __shared__ int2 s_stage[kSortTile];
+    const int n = *d_n;
+    const int passes = (bits + 7) / 8;
+    if (n <= kSortTile) {
+        sort_one_tile(in_k, in_v, (passes & 1) ? a_k : b_k, (passes & 1) ? a_v : b_v, n, bits, s_cnt, s_tile,
+                      s_warp, s_stage);
+        return;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wbase = warp * (kSortTile / kSortWarps);
+    const unsigned lt = (1u << lane) - 1u;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        const int* ik = p == 0 ? in_k : ((p & 1) ? a_k : b_k);
+        const int* iv = p == 0 ? in_v : ((p & 1) ? a_v : b_v);
+        int* ok_ = (p & 1) ? b_k : a_k;
+        int* ov_ = (p & 1) ? b_v : a_v;
+        // the digit counts of all n keys, then their exclusive scan: the
+        // first output slot of every digit
+        s_base[threadIdx.x] = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += kSortThreads) atomicAdd(&s_base[((unsigned)ik[i] >> shift) & 0xFFu], 1u);
+        __syncthreads();
+        {
+            unsigned tot;
+            const unsigned c = s_base[threadIdx.x];
+            const unsigned ex = block_scan_256(c, s_warp, &tot);
+            s_base[threadIdx.x] = ex;
+        }
+        __syncthreads();
+        // the tiles in order: each ranked stably, scattered after the
+        // digits' earlier tiles
+        for (int t0 = 0; t0 < n; t0 += kSortTile) {
+            int key[kSortItems], val[kSortItems];
+            unsigned rank[kSortItems];
+            for (int d = lane; d < kRadix; d += 32) s_cnt[warp][d] = 0;
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < kSortItems; ++r) {
+                const int i = t0 + wbase + r * 32 + lane;
+                const bool ok = i < n;
+                key[r] = ok ? ik[i] : 0;
+                val[r] = ok ? iv[i] : 0;
+                const unsigned d = ok ? (((unsigned)key[r] >> shift) & 0xFFu) : 0x100u;
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                const unsigned before = __popc(peers & lt);
+                const unsigned cnt = ok ? s_cnt[warp][d] : 0u;
+                rank[r] = cnt + before;
+                __syncwarp();
+                if (ok && before == 0) s_cnt[warp][d] = cnt + __popc(peers);
+                __syncwarp();
+            }
+            __syncthreads();
+            unsigned run = 0;
+#pragma unroll
+            for (int w = 0; w < kSortWarps; ++w) {
+                const unsigned c = s_cnt[w][threadIdx.x];
+                s_cnt[w][threadIdx.x] = run;
+                run += c;
+            }
+            s_tile[threadIdx.x] = run;   // this tile's count of digit threadIdx.x
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kSortItems; ++r) {
+                if (t0 + wbase + r * 32 + lane >= n) continue;
+                const unsigned d = ((unsigned)key[r] >> shift) & 0xFFu;
+                const unsigned pos = s_base[d] + s_cnt[warp][d] + rank[r];
+                ok_[pos] = key[r];
+                ov_[pos] = val[r];
+            }
+            __syncthreads();
+            s_base[threadIdx.x] += s_tile[threadIdx.x];
+            __syncthreads();
+        }
+        // this pass's output is the next one's input: the CTA's writes are
+        // visible to its own threads after the barrier above
+    }
+}
+
 int radix_tiles(int n) { return (n + kSortTile - 1) / kSortTile; }
 size_t radix_temp_words(int n) { return (size_t)kRadix * radix_tiles(n) + kRadix; }
 
@@ -287,9 +388,14 @@ size_t radix_temp_words(int n) { return (size_t)kRadix * radix_tiles(n) + kRadix
 // is n, or *d_n when d_n is given (n then bounds it).  Returns 0 when the
 // result is in (a_k, a_v), 1 when it is in (b_k, b_v).
 int radix_sort_pairs_n(const int* in_k, const int* in_v, int* a_k, int* a_v, int* b_k, int* b_v, int n,
-                       const int* d_n, int bits, unsigned* temp, cudaStream_t s) {
+                       const int* d_n, int bits, unsigned* temp, cudaStream_t s, bool one_cta) {
     if (n <= 0) return 0;
     if (bits <= 0) bits = 1;
+    if (d_n && one_cta) {
+        // one kernel whatever the count (no pass kernels in the stream)
+        launch_after(k_radix_onecta, 1, kSortThreads, s, in_k, in_v, a_k, a_v, b_k, b_v, d_n, bits);
+        return (((bits + 7) / 8) & 1) ? 0 : 1;
+    }
     const int ntiles = radix_tiles(n);
     unsigned* totals = temp + (size_t)kRadix * ntiles;
     // a device-side count is usually far below n: a bounded grid strides
@@ -325,7 +431,7 @@ int radix_sort_pairs(const int* in_k, const int* in_v, int* a_k, int* a_v, int* 
         cudaMemcpyAsync(a_v, in_v, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
         return 0;
     }
-    return radix_sort_pairs_n(in_k, in_v, a_k, a_v, b_k, b_v, n, nullptr, bits, temp, s);
+    return radix_sort_pairs_n(in_k, in_v, a_k, a_v, b_k, b_v, n, nullptr, bits, temp, s, false);
 }
 
 // ------------------------------------------------------------ incremental --
@@ -390,7 +496,7 @@ __global__ void __launch_bounds__(kIncThreads) k_inc_count(const int* __restrict
 // side; the number of movers into *movers.
 __global__ void __launch_bounds__(kSortThreads) k_inc_scan(const unsigned* __restrict__ tile_kept, int ntiles, int n,
                                                            unsigned* tile_base, unsigned* id_movers, unsigned* id_base,
-                                                           int* movers) {
+                                                           int* movers, int* host_movers) {
     after_previous();
     __shared__ unsigned s_warp[2][kSortWarps];
     unsigned carry = 0, mcarry = 0;
@@ -408,7 +514,10 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_scan(const unsigned* __res
         carry += tot;
         mcarry += mtot;
     }
-    if (threadIdx.x == 0) *movers = n - (int)carry;
+    if (threadIdx.x == 0) {
+        *movers = n - (int)carry;
+        if (host_movers) *host_movers = n - (int)carry;   // read by the host to pick the next frames' mover sort
+    }
 }
 
 // The kept pairs in their old order (each warp from its offset).
@@ -594,19 +703,6 @@ __global__ void __launch_bounds__(kSortThreads) k_inc_merge(const int* __restric
     }
 }
 
-struct IncrementalBuffers {
-    int* kept_k; int* kept_v;      // n each
-    int* mov_k; int* mov_v;        // n each (movers; sorted in place through t1)
-    int* t1_k; int* t1_v;          // n each
-    unsigned* warp_kept;           // 32 per tile
-    unsigned* tile_kept;           // per tile
-    unsigned* tile_base;           // per tile
-    unsigned* id_movers;           // per id tile, zero between builds
-    unsigned* id_base;             // per id tile
-    unsigned char* moved;          // 4096 per id tile, zero between builds
-    unsigned* temp;                // radix_temp_words(n)
-    int* movers;                   // 1
-};
 
 // New sorted (out_k, out_v) from the previous frame's sorted (old_k, old_v)
 // and the new keys by particle id.  Movers are gathered in id order, so one
@@ -622,7 +718,7 @@ void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_ke
     k_inc_count<<<ntiles, kIncThreads, 0, s>>>(old_k, old_v, new_key_of, n, b.warp_kept, b.tile_kept, b.moved,
                                                b.id_movers);
     launch_after(k_inc_scan, 1, kSortThreads, s, (const unsigned*)b.tile_kept, ntiles, n, b.tile_base, b.id_movers,
-                 b.id_base, b.movers);
+                 b.id_base, b.movers, b.host_movers);
     cudaStream_t ms = s;
     if (side) {
         cudaEventRecord(fork, s);
@@ -632,7 +728,7 @@ void sort_grid_incremental(const int* old_k, const int* old_v, const int* new_ke
     k_inc_movers<<<ntiles, kSortThreads, 0, ms>>>(new_key_of, n, reinterpret_cast<uint4*>(b.moved), b.id_base,
                                                   b.mov_k, b.mov_v);
     const int w = radix_sort_pairs_n(b.mov_k, b.mov_v, b.t1_k, b.t1_v, b.mov_k, b.mov_v, n, b.movers, key_bits,
-                                     b.temp, ms);
+                                     b.temp, ms, b.one_cta);
     if (side) cudaEventRecord(join, side);
     launch_after(k_inc_split, ntiles, kIncThreads, s, old_k, old_v, new_key_of, n, (const unsigned*)b.warp_kept,
                  (const unsigned*)b.tile_base, b.kept_k, b.kept_v);

@@ -325,6 +325,48 @@ def test_captured_frame_mover_counts(lib, small, moved):
     np.testing.assert_array_equal(i, oi)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("moved", [3000, 9000])
+def test_mover_sort_modes(lib, small, mode, moved):
+    # The movers of a replayed frame sorted by the tiled radix passes (mode
+    # 1) or by one CTA alone (mode 2, which also takes more than one tile of
+    # movers): the oracle's grid either way.
+    sim = make(small)
+    sim.set_mover_sort(mode)
+    sim.step(4)
+    pos0, _, _ = sim.get_particles()
+    rng = np.random.default_rng(moved + 7)
+    pick = rng.choice(len(pos0), size=moved, replace=False)
+    pos = pos0.copy()
+    pos[pick] = pos0[np.roll(pick, 1)]
+    sim.set_particles(pos, np.zeros_like(pos))
+    sim.step(1)
+    k, i, _, _ = sim.get_grid(0, dense=False)
+    ok, oi, _, _, _ = O.OracleSim(small).grid_of_points(pos)
+    np.testing.assert_array_equal(k, ok)
+    np.testing.assert_array_equal(i, oi)
+
+
+def test_mover_sort_modes_agree_over_frames(lib):
+    # A fast flow, thousands of movers per frame: the frames and grids are
+    # the same bit for bit whichever way the movers are sorted.
+    sc = S.straight_scene(cells=256, seed=11)
+    sc.velocities[:] = np.random.default_rng(5).normal(0, 400.0, sc.velocities.shape).astype(np.float32)
+    out = []
+    for mode in (0, 1, 2):
+        sim = make(sc)
+        sim.set_mover_sort(mode)
+        sim.step(6)
+        out.append(tuple(sim.get_particles()) + tuple(sim.get_grid(0, dense=False)[:2]))
+        sim.close()
+    for other in out[1:]:
+        for a, b in zip(out[0], other):
+            np.testing.assert_array_equal(a, b)
+    sim = make(sc)
+    with pytest.raises(bcs.BcsError):
+        sim.set_mover_sort(3)
+
+
 def test_moving_wall_rebuilds_bounds(lib):
     # Vein vertices start with a velocity that carries them past the 0.5
     # rebuild margin of the triangle bounds / wall mask within the run; the

@@ -198,6 +198,10 @@ struct bcs_sim {
     // movers are sorted: 0 = by that count, 1 = pass kernels, 2 = one CTA
     int* movers_seen = nullptr;
     int mover_sort = 0;
+    // the automatic choice reads a count that is as old as the host's lead:
+    // run_steps keeps it within kLeadFrames launched frames (event per frame)
+    cudaEvent_t lead_ev[8] = {};
+    long long frames_launched = 0;
     float4* fext = nullptr;      // macro steps: held external force per particle
     bcs_surrogate* surrogate = nullptr;   // enabled learned sub-step path, or null
     std::vector<bcs_surrogate*> surrogates;   // every live surrogate of this simulation
@@ -1093,6 +1097,8 @@ void destroy_impl(bcs_sim* s) {
     }
     for (void* p : s->allocations) cudaFree(p);
     if (s->movers_seen) cudaFreeHost(s->movers_seen);
+    for (auto& e : s->lead_ev)
+        if (e) cudaEventDestroy(e);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     for (auto& e : s->pev)
@@ -1615,12 +1621,14 @@ bcs_status bcs_calculate_grids(bcs_sim* s) {
     if (!s) return BCS_ERR_INVALID_ARGUMENT;
     if (s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
     s->keys_valid = false;
+    s->pg.inc.one_cta = s->mover_sort == 2;   // unpaced calls: the passes unless fixed otherwise
     enqueue_grids(s);
     return check_last();
 }
 
 bcs_status bcs_calculate_next_frame(bcs_sim* s) {
     if (!s || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
+    s->pg.inc.one_cta = s->mover_sort == 2;
     if (!s->grid_ready) enqueue_grids(s);
     enqueue_vein_forces(s);
     refresh_args(s, s->cur, s->cur ^ 1, false);
@@ -1652,6 +1660,10 @@ bcs_status bcs_propagate_all(bcs_sim* s) {
 // grows by a few percent per frame.
 constexpr int kOneCtaMovers = 4096;
 
+// Frames the host may launch ahead of the device under the automatic mover
+// sort (several frames of queued work, a mover count at most this stale).
+constexpr int kLeadFrames = 4;
+
 bool movers_one_cta(const bcs_sim* s) {
     if (s->mover_sort != 0) return s->mover_sort == 2;
     if (!s->movers_seen) return false;
@@ -1664,12 +1676,26 @@ static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
         if (substeps > 1) enqueue_macro(s, substeps);
         else enqueue_frame(s);
     };
+    // an event after every launched frame (the automatic mover sort waits
+    // for the one kLeadFrames launches back)
+    auto mark = [&]() -> bcs_status {
+        cudaEvent_t& ev = s->lead_ev[s->frames_launched % 8];
+        if (!ev) BCS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        BCS_CUDA(cudaEventRecord(ev, s->stream));
+        ++s->frames_launched;
+        return BCS_OK;
+    };
     for (int i = 0; i < n; ++i) {
+        if (s->mover_sort == 0 && s->frames_launched >= kLeadFrames) {
+            cudaEvent_t& back = s->lead_ev[(s->frames_launched - kLeadFrames) % 8];
+            if (back) BCS_CUDA(cudaEventSynchronize(back));
+        }
         s->pg.inc.one_cta = movers_one_cta(s);
         // the first frame of a grid, or with triangle centres refreshed, runs
         // eagerly (its sort is a full one)
         if (s->p.refresh_triangle_centers || (!s->keys_valid && !s->pg.sorted_once)) {
             enqueue();
+            if (bcs_status st = mark()) return st;
             continue;
         }
         if (!s->keys_valid) {
@@ -1709,6 +1735,7 @@ static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
             if (ce != cudaSuccess) { g = nullptr; return BCS_ERR_CUDA; }
         }
         BCS_CUDA(cudaGraphLaunch(g, s->stream));
+        if (bcs_status st = mark()) return st;
         // A replay is one whole enqueue_frame: mirror its host-side state.
         s->cur ^= 1;
         s->pg.slot ^= 1;
@@ -2061,6 +2088,7 @@ bcs_status bcs_run(bcs_sim* s, bcs_control* control, int max_frames, int* frames
 bcs_status bcs_profile_steps(bcs_sim* s, int nsteps, float* phase_ms) {
     if (!s || !phase_ms || nsteps < 0 || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < nsteps; ++i) {
+        s->pg.inc.one_cta = movers_one_cta(s);   // the previous frame's count: this loop waits for each frame
         enqueue_frame(s, s->pev);
         BCS_CUDA(cudaEventSynchronize(s->pev[BCS_PHASE_COUNT]));
         for (int k = 0; k < BCS_PHASE_COUNT; ++k) {
@@ -2169,6 +2197,7 @@ bcs_status bcs_surrogate_collect(bcs_surrogate* z, int macro_steps) {
     z->collecting = true;
     bcs_status st = BCS_OK;
     for (int i = 0; i < macro_steps && z->stored + z->cells <= z->capacity; ++i) {
+        s->pg.inc.one_cta = s->mover_sort == 2;
         enqueue_macro(s, z->K, &kCollectHooks);
         if ((st = check_last())) break;
         z->stored += z->cells;

@@ -1078,12 +1078,13 @@ __global__ void __launch_bounds__(kCollideThreads) k_collide(const StepArgs a) {
 // contiguous slot range: the CTA stages the three ranges' keys, positions
 // and velocities and the rows' first slots, then every thread runs the
 // nine binary searches and its windows' candidates on shared memory.  Same
-// candidates, same order, same sum as collide_slot.  The staging is one
-// round of asynchronous copies, and each thread computes its particle's
-// stencil while they land.  A tile that spans two planes or scenes, or whose
-// ranges exceed kTileStage slots (crowded rows), takes the global-memory
-// search instead; so does a particle whose stencil does not follow its
-// sorted key.
+// candidates, same order, same sum as collide_slot.  The tile's plane, rows
+// and ranges come from its record (k_tile_setup), the staging is one round
+// of asynchronous copies during which each thread computes its particle's
+// stencil, and the nine searches run a warp-uniform number of halvings.  A
+// tile that spans two planes or scenes, or whose ranges exceed kTileStage
+// slots (crowded rows), takes the global-memory search instead; so does a
+// particle whose stencil does not follow its sorted key.
 constexpr int kTileSlots = 256;
 constexpr int kTileStage = 1408;     // staged slots: 1408 x 36 B
 constexpr int kTileRows = 40;        // grid rows staged per plane
@@ -1094,8 +1095,11 @@ constexpr size_t kTileSmem = (size_t)kTileStage * (2 * sizeof(float4) + sizeof(i
 // ranges, so that the collision kernel reads them in one round trip instead
 // of looking up the tile's keys and then its rows.  One thread per tile:
 //   [0] (staged?, scene, plane zf, first staged row ylo)
-//   [1] (staged rows, staged slots, A0, A1)      Ap: first slot of plane zf + p - 1
-//   [2] (A2, c0, c0 + c1, 0)                     cp: its slots (0 outside the grid)
+//   [1] (staged rows, staged slots, A0, A1)
+//   [2] (A2, c0, c0 + c1, 0)
+// where Ap is the first sorted slot of the staged rows of plane zf + p - 1
+// and cp their number of slots (Ap = cp = 0 for a plane outside the grid),
+// so that plane p starts at staged offset c0 + ... + c(p-1).
 // A tile is staged when it lies in one scene and one plane, its rows with
 // their neighbours number at most kTileRows and the three ranges hold at most
 // kTileStage slots.

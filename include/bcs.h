@@ -295,13 +295,15 @@ typedef struct bcs_tuning {
 bcs_status bcs_get_tuning(bcs_sim* sim, bcs_tuning* out);
 bcs_status bcs_set_tuning(bcs_sim* sim, const bcs_tuning* tuning);
 
-/* How the incremental grid sort orders the particles that changed cell (the
- * reference's thrust::stable_sort_by_key, src/grids/uniform_grid.cu:144-147,
- * has no such choice; every mode gives the same order, bit for bit):
- * 0 (default) = by the mover count of a recent frame: one CTA while it is
- * small, the multi-CTA radix passes otherwise; 1 = always the passes;
- * 2 = always one CTA (correct for any count, slow for many).  Returns
- * BCS_ERR_INVALID_ARGUMENT for another value. */
+/* How a frame's grid sort runs (the reference's thrust::stable_sort_by_key,
+ * src/grids/uniform_grid.cu:144-147, has no such choice; every mode gives
+ * the same order, bit for bit).  0 (default) = by the number of particles
+ * that changed cell in a recent frame: the incremental sort with its movers
+ * sorted by one CTA while they fit one tile (4 096), by the multi-CTA radix
+ * passes above that, and every pair sorted from scratch while more than half
+ * the particles move; 1 = always incremental with the passes; 2 = always
+ * incremental with one CTA (correct for any count, slow for many); 3 =
+ * always from scratch.  Returns BCS_ERR_INVALID_ARGUMENT for another value. */
 bcs_status bcs_set_mover_sort(bcs_sim* sim, int mode);
 
 /* Autotuner: coordinate descent over the tuning fields (each field takes

@@ -653,7 +653,8 @@ class Simulation:
         _check(self.lib.bcs_set_tuning(self.h, C.byref(t)), "bcs_set_tuning")
 
     def set_mover_sort(self, mode: int) -> None:
-        """0: by a recent frame's mover count, 1: radix passes, 2: one CTA (same order in all)."""
+        """0: by a recent frame's mover count, 1: movers by radix passes, 2: by one CTA,
+        3: every pair from scratch (the same order in all)."""
         _check(self.lib.bcs_set_mover_sort(self.h, int(mode)), "bcs_set_mover_sort")
 
     def autotune(self, frames: int = 5):

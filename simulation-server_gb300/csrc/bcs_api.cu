@@ -102,6 +102,7 @@ struct DeviceGrid {
     bool sorted_once = false;
     bool incremental = false;           // rebuild from the previous order
     IncrementalBuffers inc{};
+    bool full_now = false;     // this build sorts all pairs from scratch even when incremental
     int4* table = nullptr;
     int* epoch = nullptr;
     unsigned* occ = nullptr;   // occupancy bitmap; while occ_on it holds the
@@ -192,10 +193,11 @@ struct bcs_sim {
     long long host_steps = 0;
     unsigned* err = nullptr;
     StepArgs args{};
-    std::map<long long, cudaGraphExec_t> graphs;   // by (sub-steps, mover sort, cur, sorted slot)
+    std::map<long long, cudaGraphExec_t> graphs;   // by (sub-steps, sort form, cur, sorted slot)
     // the incremental sort's mover count of a recent frame, written by its
     // scan kernel into mapped host memory (-1 until one was seen), and how the
-    // movers are sorted: 0 = by that count, 1 = pass kernels, 2 = one CTA
+    // grid is sorted: 0 = by that count, 1 = movers by the pass kernels,
+    // 2 = movers by one CTA, 3 = every pair from scratch
     int* movers_seen = nullptr;
     int mover_sort = 0;
     // the automatic choice reads a count that is as old as the host's lead:
@@ -355,7 +357,7 @@ void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, con
                cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr,
                cudaEvent_t fork2 = nullptr, cudaEvent_t join2 = nullptr) {
     const int out = dg.slot ^ 1;
-    if (dg.incremental && dg.sorted_once) {
+    if (dg.incremental && dg.sorted_once && !dg.full_now) {
         sort_grid_incremental(dg.s_k[dg.slot], dg.s_v[dg.slot], dg.in_k, dg.s_k[out], dg.s_v[out], dg.count, dg.bits,
                               dg.id_bits, dg.inc, st, side, side ? fork2 : nullptr, side ? join2 : nullptr);
     } else {
@@ -1617,18 +1619,53 @@ bcs_status bcs_get_vein(bcs_sim* s, bcs_vec3 positions, bcs_vec3 velocities, bcs
     return get_vec(s, s->vfrc, s->V, forces, where);
 }
 
+// Movers of at most one tile in a recent frame: the next frames sort theirs
+// with one CTA and no pass kernels (a larger count is still sorted correctly
+// by it, only slower).  The count is that of a frame a few frames back (the
+// host runs ahead of the device); on the 4.2M-particle bifurcation one CTA
+// stays faster than the passes up to about 7 000 movers, while the count
+// grows by a few percent per frame.
+constexpr int kOneCtaMovers = 4096;
+
+// Frames the host may launch ahead of the device under the automatic mover
+// sort (several frames of queued work, a mover count at most this stale).
+constexpr int kLeadFrames = 4;
+
+// How a frame's grid sort runs: 0 = incremental, movers by the radix passes;
+// 1 = incremental, movers by one CTA; 2 = every pair from scratch.  When
+// more than half the particles moved in a recent frame the sort from scratch
+// is the faster (late in the 4.2M trajectory: grid phase 0.36 against
+// 0.57 ms); every kProbeFrames-th frame stays incremental so that the count
+// keeps being measured.
+constexpr int kProbeFrames = 16;
+
+int mover_form(const bcs_sim* s) {
+    if (s->mover_sort != 0) return s->mover_sort - 1;
+    if (!s->movers_seen) return 0;
+    const int seen = *(volatile const int*)s->movers_seen;
+    if (seen < 0) return 0;
+    if (seen <= kOneCtaMovers) return 1;
+    if (seen > s->N / 2 && s->frames_launched % kProbeFrames != 0) return 2;
+    return 0;
+}
+
+void set_mover_form(bcs_sim* s, int form) {
+    s->pg.inc.one_cta = form == 1;
+    s->pg.full_now = form == 2;
+}
+
 bcs_status bcs_calculate_grids(bcs_sim* s) {
     if (!s) return BCS_ERR_INVALID_ARGUMENT;
     if (s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
     s->keys_valid = false;
-    s->pg.inc.one_cta = s->mover_sort == 2;   // unpaced calls: the passes unless fixed otherwise
+    set_mover_form(s, s->mover_sort > 1 ? s->mover_sort - 1 : 0);   // unpaced calls: the passes unless fixed
     enqueue_grids(s);
     return check_last();
 }
 
 bcs_status bcs_calculate_next_frame(bcs_sim* s) {
     if (!s || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
-    s->pg.inc.one_cta = s->mover_sort == 2;
+    set_mover_form(s, s->mover_sort > 1 ? s->mover_sort - 1 : 0);
     if (!s->grid_ready) enqueue_grids(s);
     enqueue_vein_forces(s);
     refresh_args(s, s->cur, s->cur ^ 1, false);
@@ -1652,24 +1689,6 @@ bcs_status bcs_propagate_all(bcs_sim* s) {
 
 // n fused frames (substeps = 1) or multi-rate macro steps, each replayed
 // from a CUDA graph captured per (sub-steps, buffer parity, sorted slot).
-// Movers of at most one tile in a recent frame: the next frames sort theirs
-// with one CTA and no pass kernels (a larger count is still sorted correctly
-// by it, only slower).  The count is that of a frame a few frames back (the
-// host runs ahead of the device); on the 4.2M-particle bifurcation one CTA
-// stays faster than the passes up to about 7 000 movers, while the count
-// grows by a few percent per frame.
-constexpr int kOneCtaMovers = 4096;
-
-// Frames the host may launch ahead of the device under the automatic mover
-// sort (several frames of queued work, a mover count at most this stale).
-constexpr int kLeadFrames = 4;
-
-bool movers_one_cta(const bcs_sim* s) {
-    if (s->mover_sort != 0) return s->mover_sort == 2;
-    if (!s->movers_seen) return false;
-    const int seen = *(volatile const int*)s->movers_seen;
-    return seen >= 0 && seen <= kOneCtaMovers;
-}
 
 static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
     auto enqueue = [&]() {
@@ -1690,7 +1709,8 @@ static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
             cudaEvent_t& back = s->lead_ev[(s->frames_launched - kLeadFrames) % 8];
             if (back) BCS_CUDA(cudaEventSynchronize(back));
         }
-        s->pg.inc.one_cta = movers_one_cta(s);
+        const int form = mover_form(s);
+        set_mover_form(s, form);
         // the first frame of a grid, or with triangle centres refreshed, runs
         // eagerly (its sort is a full one)
         if (s->p.refresh_triangle_centers || (!s->keys_valid && !s->pg.sorted_once)) {
@@ -1704,8 +1724,7 @@ static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
                         s->stream);
             s->keys_valid = true;
         }
-        cudaGraphExec_t& g =
-            s->graphs[((long long)substeps * 2 + (s->pg.inc.one_cta ? 1 : 0)) * 4 + s->cur * 2 + s->pg.slot];
+        cudaGraphExec_t& g = s->graphs[((long long)substeps * 3 + form) * 4 + s->cur * 2 + s->pg.slot];
         if (!g) {
             const int cur0 = s->cur;
             const int slot0 = s->pg.slot;
@@ -1830,7 +1849,7 @@ bcs_status bcs_init_particles(bcs_sim* s, const bcs_init_desc* d) {
 }
 
 bcs_status bcs_set_mover_sort(bcs_sim* s, int mode) {
-    if (!s || mode < 0 || mode > 2) return BCS_ERR_INVALID_ARGUMENT;
+    if (!s || mode < 0 || mode > 3) return BCS_ERR_INVALID_ARGUMENT;
     s->mover_sort = mode;
     return BCS_OK;
 }
@@ -2088,8 +2107,9 @@ bcs_status bcs_run(bcs_sim* s, bcs_control* control, int max_frames, int* frames
 bcs_status bcs_profile_steps(bcs_sim* s, int nsteps, float* phase_ms) {
     if (!s || !phase_ms || nsteps < 0 || s->mid_frame) return BCS_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < nsteps; ++i) {
-        s->pg.inc.one_cta = movers_one_cta(s);   // the previous frame's count: this loop waits for each frame
+        set_mover_form(s, mover_form(s));   // the previous frame's count: this loop waits for each frame
         enqueue_frame(s, s->pev);
+        ++s->frames_launched;   // paces the probe frames (its events are not needed: each frame is waited for)
         BCS_CUDA(cudaEventSynchronize(s->pev[BCS_PHASE_COUNT]));
         for (int k = 0; k < BCS_PHASE_COUNT; ++k) {
             float ms = 0.f;
@@ -2197,7 +2217,7 @@ bcs_status bcs_surrogate_collect(bcs_surrogate* z, int macro_steps) {
     z->collecting = true;
     bcs_status st = BCS_OK;
     for (int i = 0; i < macro_steps && z->stored + z->cells <= z->capacity; ++i) {
-        s->pg.inc.one_cta = s->mover_sort == 2;
+        set_mover_form(s, s->mover_sort > 1 ? s->mover_sort - 1 : 0);
         enqueue_macro(s, z->K, &kCollectHooks);
         if ((st = check_last())) break;
         z->stored += z->cells;

@@ -325,12 +325,13 @@ def test_captured_frame_mover_counts(lib, small, moved):
     np.testing.assert_array_equal(i, oi)
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 @pytest.mark.parametrize("moved", [3000, 9000])
 def test_mover_sort_modes(lib, small, mode, moved):
     # The movers of a replayed frame sorted by the tiled radix passes (mode
     # 1) or by one CTA alone (mode 2, which also takes more than one tile of
-    # movers): the oracle's grid either way.
+    # movers), or every pair sorted from scratch (mode 3): the oracle's grid
+    # each way.
     sim = make(small)
     sim.set_mover_sort(mode)
     sim.step(4)
@@ -353,7 +354,7 @@ def test_mover_sort_modes_agree_over_frames(lib):
     sc = S.straight_scene(cells=256, seed=11)
     sc.velocities[:] = np.random.default_rng(5).normal(0, 400.0, sc.velocities.shape).astype(np.float32)
     out = []
-    for mode in (0, 1, 2):
+    for mode in (0, 1, 2, 3):
         sim = make(sc)
         sim.set_mover_sort(mode)
         sim.step(6)
@@ -364,7 +365,7 @@ def test_mover_sort_modes_agree_over_frames(lib):
             np.testing.assert_array_equal(a, b)
     sim = make(sc)
     with pytest.raises(bcs.BcsError):
-        sim.set_mover_sort(3)
+        sim.set_mover_sort(4)
 
 
 def test_moving_wall_rebuilds_bounds(lib):

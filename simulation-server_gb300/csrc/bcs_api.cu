@@ -351,8 +351,9 @@ bcs_status alloc_grid(bcs_sim* s, DeviceGrid& dg, int count, bool incremental) {
 // from the previous order (any permutation works; few movers make it cheap).
 // With `side` (and its fork / join events) the row starts and the collision
 // tile records are built there, beside the sorted copies on `st`, and
-// (fork2 / join2) an incremental
-// build's movers are sorted there beside the compaction of the kept pairs.
+// (fork2 / join2) an incremental build's movers are sorted there beside the
+// compaction of the kept pairs.  dg.full_now sorts an incremental grid from
+// scratch for this build (late in a trajectory most particles move).
 void sort_grid(DeviceGrid& dg, cudaStream_t st, const float4* pos = nullptr, const float4* vel = nullptr,
                cudaStream_t side = nullptr, cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr,
                cudaEvent_t fork2 = nullptr, cudaEvent_t join2 = nullptr) {
@@ -1688,8 +1689,8 @@ bcs_status bcs_propagate_all(bcs_sim* s) {
 }
 
 // n fused frames (substeps = 1) or multi-rate macro steps, each replayed
-// from a CUDA graph captured per (sub-steps, buffer parity, sorted slot).
-
+// from a CUDA graph captured per (sub-steps, sort form, buffer parity,
+// sorted slot).
 static bcs_status run_steps(bcs_sim* s, int n, int substeps = 1) {
     auto enqueue = [&]() {
         if (substeps > 1) enqueue_macro(s, substeps);
